@@ -1,0 +1,397 @@
+#!/usr/bin/env python
+"""Benchmark: particle-steps/s of particle-spray stream generation on GB300.
+
+Workload (default, --workload c2): NFW (5.4e11, 15.62) + Miyamoto-Nagai
+(6.8e10, 3.0, 0.28) + Hernquist (5e9, 1.0) in kpc/Myr/Msun; progenitor at
+present day (12, 0, 4) kpc, (0, 0.18, 0.04) kpc/Myr, integrated back 4 Gyr
+and forward with fixed-step Dopri5 at dt = 0.5 Myr (FP64); 4000 release
+times (1 Myr apart) x 250 particles (125 Fardal draws x lead/trail) = 1e6
+particles; the progenitor's Plummer (2e4 Msun, 0.01 kpc) moves on its cubic
+track; float32 snapshots every 50 steps [160, 1e6, 6] (3.84 GB, larger than
+L2).  One step = one whole stream run (progenitor back/forward orbit,
+release, stream integration with snapshots).  Inputs are seeded synthetic
+Gaussian draws (numpy PCG64).
+
+`value` is the FP32-compensated path (state error vs FP64 reported in the
+same line); the FP64 plain path is reported beside it.  `--impl reference`
+times the CPU FP64 restatement of the reference algorithm (the oracle;
+OpenMP on all host cores) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s on 1 GB300: FP64 plain vs FP32/MLP-force at stated error"
+UNIT = "particle-steps/s"
+WF = np.array([12.0, 0.0, 4.0, 0.0, 0.18, 0.04])
+MSAT = 2e4
+WORKLOADS = {
+    "c2": dict(n_rel=4000, ppr=250, dt=0.5, spr=2, snap=50, moving=True,
+               name="spray stream, 4000 releases x 250 particles (1e6), 4 Gyr at dt=0.5 Myr, NFW+MN+Hernquist "
+                    "+ moving Plummer progenitor, float32 snapshots every 50 steps"),
+    "c1": dict(n_rel=3000, ppr=2, dt=1.0, spr=1, snap=0, moving=False,
+               name="spray stream, 3000 releases x 2 particles (6000), 3 Gyr at dt=1 Myr, NFW+MN+Hernquist, "
+                    "final state only"),
+}
+
+
+def particle_steps(n_rel, ppr, spr):
+    n_steps = n_rel * spr
+    return ppr * (n_rel * n_steps - spr * n_rel * (n_rel - 1) // 2)
+
+
+def normals_for(wl, seed):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return rng.standard_normal((wl["n_rel"] + 1, wl["ppr"] // 2, 4))
+
+
+def emit(obj):
+    print(json.dumps(obj), flush=True)
+
+
+# ------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str):
+        self.gpu_id = gpu_id
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", self.gpu_id], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def gpu_id_for(local_rank: int) -> str:
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis:
+        ids = [x.strip() for x in vis.split(",") if x.strip()]
+        if local_rank < len(ids):
+            return ids[local_rank]
+    return str(local_rank)
+
+
+# ------------------------------------------------------------ CPU legs
+def oracle_sample(wl, normals, n_sample_rel, threads):
+    """Time the CPU FP64 oracle on `n_sample_rel` evenly spaced releases of
+    the workload (all their particles, full length).  Returns
+    (particle_steps, seconds, cores)."""
+    from oracle import oracle as O
+    from streamsculptor_gb300 import _abi
+    n_rel, ppr, dt, spr = wl["n_rel"], wl["ppr"], wl["dt"], wl["spr"]
+    n_steps = n_rel * spr
+    base = O.HostModel(O.mw3())
+    back = O.orbit(base, WF, 0.0, -dt, n_steps, n_steps)[0, -1]
+    t0 = -n_steps * dt
+    ws = O.orbit(base, back, t0, dt, n_steps, spr)[0]
+    ts = t0 + np.arange(n_rel + 1) * spr * dt
+    comps = O.mw3() + ([(_abi.SS_PLUMMER, 1, (MSAT, 0.01))] if wl["moving"] else [])
+    integ = O.HostModel(comps, track=(ts[0], spr * dt, ws[:, :3]) if wl["moving"] else None)
+    rels = np.unique(np.linspace(0, n_rel - 1, n_sample_rel).astype(np.int64))
+    ics, _ = O.release(base, ws[rels], ts[rels], MSAT, normals[rels])
+    work = 0
+    t_start = time.perf_counter()
+    for j, r in enumerate(rels):
+        nst = n_steps - int(r) * spr
+        O.stream(integ, ts[r], dt, nst, ics[j].reshape(-1, 6), ppr, 0, n_threads=threads)
+        work += ppr * nst
+    return work, time.perf_counter() - t_start, threads
+
+
+def reference_arm(args, wl):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    normals = normals_for(wl, 1234)
+    n_sample = 24 if args.workload == "c2" else 300
+    for _ in range(args.warmup):
+        oracle_sample(wl, normals, n_sample, threads)
+    work, secs = 0, 0.0
+    for _ in range(args.steps):
+        w, s, _ = oracle_sample(wl, normals, n_sample, threads)
+        work += w
+        secs += s
+    v = work / secs
+    sample = (f"{n_sample} evenly spaced releases x {wl['ppr']} particles, full length, per step "
+              f"({work // args.steps} particle-steps)")
+    emit({"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+          "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+          "data": "synthetic (seeded PCG64 Gaussian draws)",
+          "config": {"workload": wl["name"]},
+          "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+          "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+          "note": "reference = CPU FP64 restatement of streamsculptor's path (the JAX reference cannot run: "
+                  "jax/diffrax/astropy/gala are not installed); OpenMP over particles on all host threads"})
+
+
+# ------------------------------------------------------------ GPU leg
+def gpu_arm(args, wl):
+    import torch
+    import torch.distributed as dist
+
+    import streamsculptor_gb300 as ss
+    from streamsculptor_gb300 import _abi, _core, potential as P, roofline
+    from streamsculptor_gb300.streamhelpers import gen_stream
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = _abi.load()
+    u = ss.usys
+    pot = P.Potential_Combine([P.NFWPotential(m=5.4e11, r_s=15.62, units=u),
+                               P.MiyamotoNagaiDisk(m=6.8e10, a=3.0, b=0.28, units=u),
+                               P.HernquistPotential(m=5e9, r_s=1.0, units=u)], units=u)
+    prog = P.PlummerPotential(m=MSAT, r_s=0.01, units=u) if wl["moving"] else None
+    n_rel, ppr, dt, spr, snap = wl["n_rel"], wl["ppr"], wl["dt"], wl["spr"], wl["snap"]
+    n_steps = n_rel * spr
+    T = n_steps * dt
+    ts = -T + np.arange(n_rel + 1) * spr * dt
+    work = particle_steps(n_rel, ppr, spr)
+    normals_h = normals_for(wl, 1234 + rank)  # weak scaling: every rank runs its own stream
+    normals_d = torch.as_tensor(normals_h, device=dev)
+    wf_d = torch.as_tensor(WF, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)  # > L2 (129 MB)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def step(precision, wf, normals):
+        back = pot.integrate_orbit(w0=wf, ts=np.array([0.0, -T]), t0=0.0, t1=-T, dt=dt).ys[-1]
+        return gen_stream(pot, ts, back, MSAT, normals=normals, dt=dt, prog_pot=prog, n_particles_per_release=ppr,
+                          precision=precision, snapshot_every=snap or None)
+
+    def timed(precision, K, W):
+        for _ in range(W):
+            step(precision, wf_d, normals_d)
+        torch.cuda.synchronize()
+        barrier()
+        evs, kev = [], []
+        _core.STREAM_EVENTS = kev
+        l0 = lib.ss_kernel_launches()
+        clocks = ClockSampler(gpu_id_for(local))
+        clocks.start()
+        for _ in range(K):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            step(precision, wf_d, normals_d)
+            e1.record()
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        barrier()
+        ck = clocks.stop()
+        launches = lib.ss_kernel_launches() - l0
+        _core.STREAM_EVENTS = None
+        ms = sum(a.elapsed_time(b) for a, b in evs)
+        kms = [a.elapsed_time(b) for a, b in kev]
+        if world > 1:
+            t = torch.tensor([ms], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return {"ms_total": ms, "ms_per_step": ms / K, "kernel_ms": statistics.mean(kms) if kms else None,
+                "launches": launches, "clocks": ck}
+
+    def peak(precision):
+        sink = torch.empty(1024, dtype=torch.float32, device=dev)
+        import ctypes as C
+        fl = C.c_double()
+        iters = 100000 if precision == 32 else 3000
+        _abi.call("ss_peak_fma", precision, iters, C.byref(fl), _core.ptr(sink), _core.stream_handle())
+        torch.cuda.synchronize()
+        best = 0.0
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _abi.call("ss_peak_fma", precision, iters, C.byref(fl), _core.ptr(sink), _core.stream_handle())
+            e1.record()
+            torch.cuda.synchronize()
+            best = max(best, fl.value / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+        return best
+
+    # --- headline: FP32-compensated, inputs resident
+    r32 = timed("f32k", args.steps, args.warmup)
+    value = world * work / (r32["ms_per_step"] * 1e-3)
+    # --- FP64 plain beside it
+    k64 = max(1, min(args.steps, args.f64_steps))
+    r64 = timed("f64", k64, max(1, min(args.warmup, args.f64_warmup)))
+    value64 = world * work / (r64["ms_per_step"] * 1e-3)
+
+    # --- error of FP32-compensated vs FP64 on this workload
+    l32, t32 = step("f32k", wf_d, normals_d)[:2]
+    l64, t64 = step("f64", wf_d, normals_d)[:2]
+    a = torch.stack([l32, t32]).reshape(-1, 6)
+    b = torch.stack([l64, t64]).reshape(-1, 6)
+    ex = torch.linalg.norm(a[:, :3] - b[:, :3], dim=1) / torch.linalg.norm(b[:, :3], dim=1)
+    ev = torch.linalg.norm(a[:, 3:] - b[:, 3:], dim=1) / torch.linalg.norm(b[:, 3:], dim=1)
+    e = torch.maximum(ex, ev)
+    err = {"max": float(e.max()), "p99": float(torch.quantile(e.float(), 0.99)), "median": float(e.median()),
+           "measure": "per particle max(|dx|/|x|, |dv|/|v|) of final states, FP32-compensated vs FP64 GPU path"}
+    del l32, t32, l64, t64, a, b
+
+    # --- e2e through the public API with host buffers
+    n_snap = n_steps // snap if snap else 0
+    pin_snaps = torch.empty((n_snap, n_rel, ppr // 2, 2, 6), dtype=torch.float32, pin_memory=True) if snap else None
+    pin_final = torch.empty((2, n_rel, ppr // 2, 6), dtype=torch.float64, pin_memory=True)
+
+    def e2e_step():
+        sol = pot.integrate_orbit(w0=WF, ts=np.array([0.0, -T]), t0=0.0, t1=-T, dt=dt)
+        out = gen_stream(pot, ts, sol.ys[-1], MSAT, normals=normals_h, dt=dt, prog_pot=prog,
+                         n_particles_per_release=ppr, precision="f32k", snapshot_every=snap or None)
+        lead, trail = out[0], out[1]
+        pin_final[0].copy_(lead.reshape(n_rel, ppr // 2, 6), non_blocking=True)
+        pin_final[1].copy_(trail.reshape(n_rel, ppr // 2, 6), non_blocking=True)
+        if snap:
+            pin_snaps.copy_(out[2], non_blocking=True)
+        torch.cuda.synchronize()
+
+    for _ in range(2):
+        e2e_step()
+    k_e2e = max(1, min(args.steps, 5))
+    tsum = 0.0
+    for _ in range(k_e2e):
+        flush.zero_()
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        e2e_step()
+        barrier()
+        tsum += time.perf_counter() - t0
+    e2e_s = tsum / k_e2e
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = normals_h.nbytes + ts.nbytes + WF.nbytes + 2 * 8
+    d2h = pin_final.numel() * 8 + (pin_snaps.numel() * 4 if snap else 0)
+
+    # --- roofline of the dominant kernel (stream_f32k_kernel)
+    flat = P.Potential_Combine([pot] + ([P.TimeDepTranslatingPotential(prog, _core.CenterTrack(0.0, 1.0, wf_d.reshape(2, 3)))]
+                                        if prog is not None else []), units=u)._flatten()
+    w32 = roofline.particle_step_work(flat, "f32k")
+    w64 = roofline.particle_step_work(flat, "f64")
+    p32, p64 = peak(32), peak(64)
+
+    def roof(r, w, pk, kernel):
+        ach = w["flops"] * work / (r["kernel_ms"] * 1e-3) / 1e12
+        return {"kernel": kernel, "bound": "fp32" if "f32" in kernel else "fp64", "achieved": ach, "peak": pk,
+                "unit": "TFLOP/s", "frac": ach / pk, "traffic": traffic_for(kernel),
+                "flops_per_particle_step": w["flops"], "specials_per_particle_step": w["specials"],
+                "kernel_ms": r["kernel_ms"],
+                "peak_source": "measured in this run by ss_peak_fma (FMA chains on every SM); "
+                               "MEASURED_PEAKS.json has no FP32/FP64 pipe figure",
+                "snapshot_write_GBps": (n_snap * n_rel * ppr * 24) / (r["kernel_ms"] * 1e-3) / 1e9 if snap else 0.0}
+
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.no_cpu_baseline:
+            cw, cs, cores = oracle_sample(wl, normals_h, 100 if args.workload == "c2" else 3000, os.cpu_count() or 1)
+            cpu = {"value": cw / cs, "unit": UNIT, "cores": cores, "kind": "port",
+                   "sample": f"CPU FP64 oracle (OpenMP) on 100 evenly spaced releases x {ppr} particles, "
+                             f"full length ({cw} particle-steps, {cs:.1f} s)"}
+        clk = r32["clocks"]
+        emit({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+              "warmup": args.warmup, "ms_per_step": r32["ms_per_step"], "higher_is_better": True,
+              "scaling": "weak", "vs_baseline": None,
+              "dtype": "f32 (compensated hi+lo state; FP64 progenitor, time, release)",
+              "data": "synthetic (seeded PCG64 Gaussian draws)",
+              "config": {"workload": wl["name"], "particles": n_rel * ppr, "n_steps": n_steps,
+                         "particle_steps_per_step": work, "dt_myr": dt, "snapshot_every": snap,
+                         "l2": "512 MB buffer zeroed between timed steps; snapshots (3.84 GB) exceed L2"},
+              "f64": {"value": value64, "unit": UNIT, "ms_per_step": r64["ms_per_step"], "steps": k64,
+                      "clocks": r64["clocks"], "roofline": roof(r64, w64, p64, "stream_f64_kernel")},
+              "speedup_f32k_vs_f64": value / value64,
+              "error_vs_f64": err,
+              "roofline": roof(r32, w32, p32, "stream_f32k_kernel"),
+              "cpu_baseline": cpu,
+              "e2e": {"value": world * work / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                      "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
+                      "path": "integrate_orbit + streamhelpers.gen_stream with host numpy inputs; results "
+                              "copied to pinned host memory"},
+              "clocks": clk, "gpu_launches": r32["launches"],
+              "gpu_launches_per_step": r32["launches"] / args.steps})
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def traffic_for(kernel):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
+    ap.add_argument("--f64-steps", type=int, default=2)
+    ap.add_argument("--f64-warmup", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        reference_arm(args, wl)
+    else:
+        gpu_arm(args, wl)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,270 @@
+/*
+ * streamsculptor_gb300 — C ABI of the GB300 (sm_103a) stream-generation library.
+ *
+ * Everything here is plain C: pointers, sizes and POD structs.  Device
+ * buffers are owned by the caller (any allocator: torch, cudaMalloc, a pool);
+ * the library never allocates after the first call on a device.  Every entry
+ * point is stream-ordered on the `stream` argument (a cudaStream_t passed as
+ * void*; NULL = legacy default stream) and returns SS_OK (0) or a negative
+ * ss_status code; ss_last_error() then gives a one-line reason (thread-local).
+ *
+ * Units are the reference's: kpc, Myr, Msun (G = 4.498502151469553e-12
+ * kpc^3 Msun^-1 Myr^-2 is passed in ss_potential.G, so dimensionless runs work
+ * too).  Each entry point names the reference interface it replaces
+ * (paths relative to the jnibauer/streamsculptor source tree).
+ */
+#ifndef STREAMSCULPTOR_GB300_H
+#define STREAMSCULPTOR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SS_ABI_VERSION 1
+#define SS_MAX_COMPONENTS 16
+
+/* ---------------------------------------------------------------- status */
+typedef enum ss_status {
+    SS_OK = 0,
+    SS_ERR_INVALID_ARGUMENT = -1, /* null pointer, bad size, unsupported kind */
+    SS_ERR_CUDA = -2,             /* a CUDA runtime call failed */
+    SS_ERR_NONFINITE = -3,        /* integration produced inf/nan (per-item status set) */
+    SS_ERR_WORKSPACE = -4,        /* caller workspace too small */
+    SS_ERR_UNSUPPORTED = -5       /* valid request outside what this build implements */
+} ss_status;
+
+/* ------------------------------------------------------ potential model */
+/* Component kinds and their raw parameters p[] (reference potential.py):
+ *   SS_NFW            p = {m, r_s, soft}           NFWPotential          potential.py:74-84
+ *                     (soft is added to r^2; 0 = the reference's current form)
+ *   SS_TRIAXIAL_NFW   p = {m, r_s, q1, q2, q3}     TriaxialNFWPotential  potential.py:86-97
+ *   SS_MIYAMOTO_NAGAI p = {m, a, b}                MiyamotoNagaiDisk     potential.py:66-72
+ *   SS_HERNQUIST      p = {m, r_s, soft}           HernquistPotential    potential.py:132-138
+ *   SS_PLUMMER        p = {m, r_s}                 PlummerPotential      potential.py:124-130
+ *   SS_ISOCHRONE      p = {m, a}                   Isochrone             potential.py:114-122
+ * A component with center = SS_CENTER_TRACK is evaluated at x - c(t), where
+ * c(t) is the potential's center track: TimeDepTranslatingPotential,
+ * potential.py:448-462.  Components are summed in list order
+ * (Potential_Combine, potential.py:1279-1296). */
+typedef enum ss_kind {
+    SS_NFW = 1,
+    SS_TRIAXIAL_NFW = 2,
+    SS_MIYAMOTO_NAGAI = 3,
+    SS_HERNQUIST = 4,
+    SS_PLUMMER = 5,
+    SS_ISOCHRONE = 6
+} ss_kind;
+
+enum { SS_CENTER_ORIGIN = 0, SS_CENTER_TRACK = 1 };
+
+typedef struct ss_component {
+    int32_t kind;   /* ss_kind */
+    int32_t center; /* SS_CENTER_ORIGIN or SS_CENTER_TRACK */
+    double p[6];
+} ss_component;
+
+/* Center track: C1 cubic Hermite spline through knots at t0 + k*dt, with knot
+ * slopes (dx/dt).  ss_track_slopes() fills the slopes the way the reference's
+ * interpax.Interpolator1D(method='cubic') does (streamhelpers.py:520):
+ * mean of the adjacent secants, one-sided at the two ends.  Outside
+ * [t0, t0+(n-1)dt] the end cubic is extrapolated.  Pointers are device
+ * pointers for device entry points. */
+typedef struct ss_track {
+    const double* knots;  /* [n_knots, 3] */
+    const double* slopes; /* [n_knots, 3] */
+    double t0;
+    double dt;            /* knot spacing, > 0 */
+    int64_t n_knots;      /* >= 2 when any component uses the track */
+} ss_track;
+
+/* Subhalos moving on straight lines x0 + v (t - t0), active while
+ * |t - t0| < t_window: SubhaloLinePotential, potential.py:802-850, and its
+ * d/d(r_s) companion SubhaloLinePotential_dRadius, potential.py:852-904. */
+typedef enum ss_subhalo_kind { SS_SH_PLUMMER = 1, SS_SH_HERNQUIST = 2 } ss_subhalo_kind;
+
+typedef struct ss_subhalos {
+    int32_t kind;       /* ss_subhalo_kind */
+    int32_t reserved;
+    int64_t n;          /* number of subhalos (0 = none) */
+    const double* m;    /* [n] */
+    const double* a;    /* [n] scale radius */
+    const double* x0;   /* [n, 3] position at t0 */
+    const double* v;    /* [n, 3] */
+    const double* t0;   /* [n] */
+    double t_window;    /* +inf = always active */
+} ss_subhalos;
+
+typedef struct ss_potential {
+    double G;
+    int32_t n_components;
+    int32_t reserved;
+    ss_component comp[SS_MAX_COMPONENTS];
+    ss_track track;
+    /* When subhalos.n > 0 their summed potential is part of this potential
+     * (Potential_Combine([pot_base, pot_pert]), streamhelpers.py:89-146). */
+    ss_subhalos subhalos;
+} ss_potential;
+
+/* ------------------------------------------------------------- configs */
+/* Particle p belongs to release r = p / particles_per_release and starts at
+ * global step r * steps_per_release, i.e. at t0 + r*steps_per_release*dt,
+ * then takes fixed Dormand-Prince 5(4) steps of size dt up to global step
+ * n_steps (gen_stream_vmapped, main.py:343-368: every particle is integrated
+ * from its release time ts[i] to ts[-1]). */
+typedef struct ss_stream_cfg {
+    double t0;
+    double dt;                 /* > 0 */
+    int64_t n_steps;
+    int64_t n_particles;
+    int32_t particles_per_release;
+    int32_t steps_per_release;
+    int32_t snap_stride;       /* 0 = final state only; else snapshot after every snap_stride global steps */
+    int32_t reserved;
+} ss_stream_cfg;
+
+typedef enum ss_release_model { SS_RELEASE_FARDAL = 0, SS_RELEASE_CHEN25 = 1 } ss_release_model;
+
+/* Release (particle spray).  The reference draws its Gaussian numbers with
+ * the JAX PRNG; here they are inputs (`normals`), so any generator can feed
+ * them.  Fardal: 4 normals per draw (kr, kvphi, kz, kvz), main.py:209-280.
+ * Chen25: 6 normals per draw, mapped to N(mean, cov) as mean + L z,
+ * streamhelpers.py:352-432. */
+typedef struct ss_release_cfg {
+    int64_t n_release;
+    int32_t n_draw;    /* draws per release; each draw gives a lead and a trail particle */
+    int32_t model;     /* ss_release_model */
+    double kvals[8];   /* Fardal k-values: kr_bar, kvphi_bar, kz_bar, kvz_bar, s_kr, s_kvphi, s_kz, s_kvz */
+    double chen_mean[6];
+    double chen_L[36]; /* row-major 6x6 factor with L L^T = cov */
+} ss_release_cfg;
+
+/* First-order response to subhalos (MassRadiusPerturbation_OTF,
+ * fields.py:159-206).  Per particle: base state (6) and, per subhalo, ncol
+ * columns: d(x,v)/d(eps) (6) and, when ncol == 12, d^2(x,v)/d(eps)d(r_s) (6). */
+typedef struct ss_pert_cfg {
+    double t0;
+    double dt;                 /* signed: < 0 integrates backwards in time */
+    int64_t n_steps;
+    int64_t n_particles;
+    int32_t particles_per_release;
+    int32_t steps_per_release;
+    int32_t ncol;              /* 6 or 12 */
+    int32_t save_stride;       /* 0 = final only; else save at steps 0, s, 2s, ... n_steps */
+} ss_pert_cfg;
+
+/* ------------------------------------------------------------ entry points */
+
+/* Library / ABI identity. */
+int ss_abi_version(void);
+const char* ss_last_error(void);
+/* sizeof of the ABI structs in this build: which = 0 ss_potential, 1 ss_stream_cfg,
+ * 2 ss_release_cfg, 3 ss_pert_cfg, 4 ss_component, 5 ss_track, 6 ss_subhalos. */
+int64_t ss_abi_sizeof(int which);
+/* Number of kernels this library has launched in the process so far. */
+int64_t ss_kernel_launches(void);
+
+/* Phi, grad Phi, Hessian at n points (device arrays; any output may be NULL).
+ * t: per-point times [n] or NULL to use t_scalar.
+ * Replaces Potential.potential / gradient / acceleration / jacobian_force
+ * batched with jax.vmap (main.py:37-65; potential.py:1285-1296). */
+int ss_potential_eval(const ss_potential* pot, const double* xyz, int64_t n,
+                      const double* t, double t_scalar,
+                      double* phi, double* grad, double* hess, void* stream);
+
+/* Fixed-step Dopri5 orbits in FP64, one thread per orbit.
+ * w0 [n_orbits, 6]; out [n_orbits, n_steps/save_every + 1, 6] holds the state
+ * at steps 0, save_every, ...  dt may be negative (backwards integration).
+ * Replaces Potential.integrate_orbit / integrate_orbit_batch_vmapped
+ * (main.py:125-202) with dtmin = dtmax = dt. */
+int ss_orbit_f64(const ss_potential* pot, const double* w0, int64_t n_orbits,
+                 double t0, double dt, int64_t n_steps, int64_t save_every,
+                 double* out, void* stream);
+
+/* Spline slopes for a center track: knots [n,3] -> slopes [n,3] (device). */
+int ss_track_slopes(const double* knots, int64_t n_knots, double dt, double* slopes, void* stream);
+
+/* Release model, FP64, one thread per (release, draw).
+ * prog_w [n_release, 6] progenitor states, t_rel [n_release], msat [n_release],
+ * normals [n_release, n_draw, 4 or 6]; ics [n_release, n_draw, 2, 6] with
+ * index 0 = lead, 1 = trail; jac (nullable) [n_release, n_draw, 2, 6, 6] =
+ * d(ics)/d(prog_w).  Replaces Potential.release_model + gen_stream_ics
+ * (main.py:209-306), release_model_Chen25 (streamhelpers.py:352-459) and
+ * BaseStreamModel.release_func_jacobian (perturbative.py:280-296). */
+int ss_release_f64(const ss_potential* pot, const ss_release_cfg* cfg,
+                   const double* prog_w, const double* t_rel, const double* msat,
+                   const double* normals, double* ics, double* jac, void* stream);
+
+/* Stream integration (the hot path).  ics [n_particles, 6] FP64.
+ * final_w [n_particles, 6] FP64 state at global step n_steps (nullable).
+ * snaps (nullable) [n_steps/snap_stride, n_particles, 6] float32: snapshot k
+ * is the state after global step (k+1)*snap_stride; particles not yet
+ * released then are NaN.  status (nullable) [n_particles]: 0 ok, 1 non-finite.
+ * Replaces gen_stream_vmapped / gen_stream_scan (main.py:312-368),
+ * gen_stream_vmapped_Chen25 (streamhelpers.py:491-543) and, with
+ * pot->subhalos, gen_stream_vmapped_with_pert (streamhelpers.py:89-146);
+ * snapshots replace the dense-output streams (main.py:376-430). */
+int ss_stream_f64(const ss_potential* pot, const ss_stream_cfg* cfg, const double* ics,
+                  double* final_w, float* snaps, int32_t* status, void* stream);
+
+/* Same, FP32 stage arithmetic with compensated (hi+lo) position/velocity
+ * accumulation; time and release bookkeeping stay FP64.  The progenitor
+ * track and the subhalo lines are tabulated in FP32 at the run's stage times
+ * into `workspace` (device, 256-byte aligned, >= ss_stream_workspace_bytes;
+ * may be NULL when that is 0). */
+int64_t ss_stream_workspace_bytes(const ss_potential* pot, const ss_stream_cfg* cfg);
+int ss_stream_f32k(const ss_potential* pot, const ss_stream_cfg* cfg, const double* ics,
+                   double* final_w, float* snaps, int32_t* status,
+                   void* workspace, int64_t workspace_bytes, void* stream);
+
+/* First-order subhalo response (fields.MassRadiusPerturbation_OTF.term,
+ * fields.py:174-206, integrated as in
+ * GenerateMassRadiusPerturbation.compute_perturbation_OTF, perturbative.py:100-135).
+ *   base   : smooth potential (its subhalos must be empty)
+ *   sh     : the subhalo table (device pointers)
+ *   base_ics [n_particles, 6] FP64
+ *   pert_ics [n_particles, sh->n, ncol] (nullable: zero initial response)
+ *   base_out [n_particles, 6] FP64 final base state (nullable)
+ *   pert_out [n_saves, n_particles, sh->n, ncol], n_saves = 1 when
+ *            save_stride == 0 else n_steps/save_stride + 1
+ *   workspace: device scratch of >= ss_pert_workspace_bytes(cfg, precision, 1) bytes.
+ * precision: 64 -> pert_ics/pert_out are double*; 32 -> float* (FP32 response,
+ * FP64 base track and time). */
+int64_t ss_pert_workspace_bytes(const ss_pert_cfg* cfg, int precision, int64_t particles_per_chunk);
+int ss_pert_response(const ss_potential* base, const ss_subhalos* sh, const ss_pert_cfg* cfg,
+                     int precision, const double* base_ics, const void* pert_ics,
+                     double* base_out, void* pert_out,
+                     void* workspace, int64_t workspace_bytes, void* stream);
+
+/* Per-subhalo potential, gradient, dPhi/da and its gradient at n points
+ * (device): phi [n, sh->n], grad [n, sh->n, 3], dphi_da [n, sh->n],
+ * grad_dphi_da [n, sh->n, 3] (any may be NULL); zero outside the window.
+ * Replaces potential_per_SH and jacfwd(potential_per_SH) of
+ * SubhaloLinePotential / SubhaloLinePotential_dRadius (potential.py:832-904;
+ * perturbative.py:40-41). */
+int ss_subhalo_eval(const ss_subhalos* sh, double G, const double* xyz, int64_t n, double t,
+                    double* phi, double* grad, double* dphi_da, double* grad_dphi_da, void* stream);
+
+/* Binned mean track (computed_binned_track, streamhelpers.py:201-228).
+ * values [n, ncomp] FP64, key [n] FP64, edges [n_edges] ascending.
+ * bin(i) = number of edges <= key[i] (numpy.digitize, right=False);
+ * sums [n_edges-1, ncomp] and counts [n_edges-1, ncomp] accumulate the items
+ * with bin == b for b in [0, n_edges-2], skipping NaN values per component
+ * (nanmean).  Outputs are zeroed by the call. */
+int ss_binned_sums(const double* values, const double* key, int64_t n, int32_t ncomp,
+                   const double* edges, int32_t n_edges,
+                   double* sums, double* counts, void* stream);
+
+/* Peak arithmetic throughput probe used for rooflines: eight independent
+ * FMA chains per thread on 8 blocks per SM.  precision 64 or 32;
+ * *out_flops = flops the launch executes; sink: device buffer of >= 512
+ * floats (never written in practice). */
+int ss_peak_fma(int precision, int64_t iters, double* out_flops, float* sink, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* STREAMSCULPTOR_GB300_H */

@@ -1,0 +1,155 @@
+"""ctypes mirror of include/streamsculptor_gb300.h and the library loader.
+
+The Python facade calls the CUDA library only through these C-ABI entry
+points (plain pointers and sizes).  There is no CPU fallback: if the library
+is missing the import of any compute entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+SS_ABI_VERSION = 1
+SS_MAX_COMPONENTS = 16
+
+SS_OK = 0
+SS_ERR_INVALID_ARGUMENT = -1
+SS_ERR_CUDA = -2
+SS_ERR_NONFINITE = -3
+SS_ERR_WORKSPACE = -4
+SS_ERR_UNSUPPORTED = -5
+
+SS_NFW = 1
+SS_TRIAXIAL_NFW = 2
+SS_MIYAMOTO_NAGAI = 3
+SS_HERNQUIST = 4
+SS_PLUMMER = 5
+SS_ISOCHRONE = 6
+
+SS_CENTER_ORIGIN = 0
+SS_CENTER_TRACK = 1
+
+SS_SH_PLUMMER = 1
+SS_SH_HERNQUIST = 2
+
+SS_RELEASE_FARDAL = 0
+SS_RELEASE_CHEN25 = 1
+
+VP = C.c_void_p
+DP = C.POINTER(C.c_double)
+
+
+class ss_component(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("center", C.c_int32), ("p", C.c_double * 6)]
+
+
+class ss_track(C.Structure):
+    _fields_ = [("knots", VP), ("slopes", VP), ("t0", C.c_double), ("dt", C.c_double),
+                ("n_knots", C.c_int64)]
+
+
+class ss_subhalos(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("reserved", C.c_int32), ("n", C.c_int64),
+                ("m", VP), ("a", VP), ("x0", VP), ("v", VP), ("t0", VP), ("t_window", C.c_double)]
+
+
+class ss_potential(C.Structure):
+    _fields_ = [("G", C.c_double), ("n_components", C.c_int32), ("reserved", C.c_int32),
+                ("comp", ss_component * SS_MAX_COMPONENTS), ("track", ss_track),
+                ("subhalos", ss_subhalos)]
+
+
+class ss_stream_cfg(C.Structure):
+    _fields_ = [("t0", C.c_double), ("dt", C.c_double), ("n_steps", C.c_int64),
+                ("n_particles", C.c_int64), ("particles_per_release", C.c_int32),
+                ("steps_per_release", C.c_int32), ("snap_stride", C.c_int32), ("reserved", C.c_int32)]
+
+
+class ss_release_cfg(C.Structure):
+    _fields_ = [("n_release", C.c_int64), ("n_draw", C.c_int32), ("model", C.c_int32),
+                ("kvals", C.c_double * 8), ("chen_mean", C.c_double * 6), ("chen_L", C.c_double * 36)]
+
+
+class ss_pert_cfg(C.Structure):
+    _fields_ = [("t0", C.c_double), ("dt", C.c_double), ("n_steps", C.c_int64),
+                ("n_particles", C.c_int64), ("particles_per_release", C.c_int32),
+                ("steps_per_release", C.c_int32), ("ncol", C.c_int32), ("save_stride", C.c_int32)]
+
+
+STRUCTS = [ss_potential, ss_stream_cfg, ss_release_cfg, ss_pert_cfg, ss_component, ss_track, ss_subhalos]
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "ss_abi_version": (C.c_int, []),
+    "ss_last_error": (C.c_char_p, []),
+    "ss_abi_sizeof": (C.c_int64, [C.c_int]),
+    "ss_kernel_launches": (C.c_int64, []),
+    "ss_potential_eval": (C.c_int, [C.POINTER(ss_potential), VP, C.c_int64, VP, C.c_double, VP, VP, VP, VP]),
+    "ss_orbit_f64": (C.c_int, [C.POINTER(ss_potential), VP, C.c_int64, C.c_double, C.c_double, C.c_int64,
+                               C.c_int64, VP, VP]),
+    "ss_track_slopes": (C.c_int, [VP, C.c_int64, C.c_double, VP, VP]),
+    "ss_release_f64": (C.c_int, [C.POINTER(ss_potential), C.POINTER(ss_release_cfg), VP, VP, VP, VP, VP, VP, VP]),
+    "ss_stream_f64": (C.c_int, [C.POINTER(ss_potential), C.POINTER(ss_stream_cfg), VP, VP, VP, VP, VP]),
+    "ss_stream_workspace_bytes": (C.c_int64, [C.POINTER(ss_potential), C.POINTER(ss_stream_cfg)]),
+    "ss_stream_f32k": (C.c_int, [C.POINTER(ss_potential), C.POINTER(ss_stream_cfg), VP, VP, VP, VP, VP,
+                                 C.c_int64, VP]),
+    "ss_subhalo_eval": (C.c_int, [C.POINTER(ss_subhalos), C.c_double, VP, C.c_int64, C.c_double, VP, VP, VP,
+                                  VP, VP]),
+    "ss_pert_workspace_bytes": (C.c_int64, [C.POINTER(ss_pert_cfg), C.c_int, C.c_int64]),
+    "ss_pert_response": (C.c_int, [C.POINTER(ss_potential), C.POINTER(ss_subhalos), C.POINTER(ss_pert_cfg),
+                                   C.c_int, VP, VP, VP, VP, VP, C.c_int64, VP]),
+    "ss_binned_sums": (C.c_int, [VP, VP, C.c_int64, C.c_int32, VP, C.c_int32, VP, VP, VP]),
+    "ss_peak_fma": (C.c_int, [C.c_int, C.c_int64, DP, VP, VP]),
+}
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libssgb300.so")
+
+_lib = None
+_lock = threading.Lock()
+
+
+class SSError(RuntimeError):
+    """A C-ABI call returned an error status."""
+
+    def __init__(self, name: str, code: int, msg: str):
+        super().__init__(f"{name} failed ({code}): {msg}")
+        self.code = code
+
+
+def load(path: str | None = None):
+    """Load libssgb300.so (raises if it is missing: there is no fallback)."""
+    global _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise RuntimeError(
+                f"streamsculptor_gb300 CUDA library not found at {p}; build it with "
+                "`python -c 'import __graft_entry__ as g; g.build()'` (nvcc, sm_103a)")
+        lib = C.CDLL(p)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        if lib.ss_abi_version() != SS_ABI_VERSION:
+            raise RuntimeError("libssgb300.so ABI version mismatch")
+        for i, st in enumerate(STRUCTS):
+            if lib.ss_abi_sizeof(i) != C.sizeof(st):
+                raise RuntimeError(f"ABI struct size mismatch for {st.__name__}: "
+                                   f"C {lib.ss_abi_sizeof(i)} vs ctypes {C.sizeof(st)}")
+        if path is None:
+            _lib = lib
+        return lib
+
+
+def call(name: str, *args) -> int:
+    """Call entry point `name`; raise SSError on a negative status."""
+    lib = load()
+    rc = getattr(lib, name)(*args)
+    if rc < 0:
+        msg = lib.ss_last_error().decode(errors="replace")
+        raise SSError(name, rc, msg)
+    return rc

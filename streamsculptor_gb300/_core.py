@@ -1,0 +1,361 @@
+"""Plumbing between the reference-style Python API and the C ABI.
+
+* tensors: every array handed to the library is a contiguous CUDA tensor;
+  torch is used for device memory and streams only.
+* potentials: a tree of Potential objects is flattened into one
+  ``ss_potential`` descriptor (components in list order, at most one center
+  track, at most one subhalo table), cached per device.
+* thin wrappers around each C entry point, issued on torch's current stream.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional, Tuple
+
+import numpy as np
+import torch
+
+from . import _abi
+
+G_KPC_MYR_MSUN = 4.498502151469553e-12  # kpc^3 / (Msun Myr^2), CODATA-2018 G, IAU Msun, Julian yr
+
+
+# ----------------------------------------------------------------- units
+class UnitSystem:
+    """Minimal stand-in for gala's UnitSystem: only the reference's usys
+    (kpc, Myr, Msun, radian) and dimensionless are supported."""
+
+    def __init__(self, *units):
+        if len(units) == 1 and isinstance(units[0], UnitSystem):
+            units = units[0].units
+        self.units = tuple(str(u) for u in units)
+
+    def __eq__(self, other):
+        return isinstance(other, UnitSystem) and self.units == other.units
+
+    def __hash__(self):
+        return hash(self.units)
+
+    def __repr__(self):
+        return f"UnitSystem{self.units}"
+
+
+usys = UnitSystem("kpc", "Myr", "Msun", "radian")
+dimensionless = UnitSystem()
+
+
+def G_for(units) -> float:
+    """Potential.__init__ (main.py:22-30): G = 1 when dimensionless."""
+    if units is None or units == dimensionless:
+        return 1.0
+    if UnitSystem(units) == usys:
+        return G_KPC_MYR_MSUN
+    raise NotImplementedError(f"unit system {units!r}: only usys (kpc, Myr, Msun, radian) or dimensionless")
+
+
+# --------------------------------------------------------------- tensors
+def device() -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("streamsculptor_gb300 needs a CUDA device (GB300, sm_103a); there is no CPU path")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def f64(x, dev=None) -> torch.Tensor:
+    """Contiguous float64 CUDA tensor view/copy of x."""
+    dev = dev or device()
+    if isinstance(x, torch.Tensor):
+        return x.to(device=dev, dtype=torch.float64).contiguous()
+    return torch.as_tensor(np.asarray(x, dtype=np.float64), device=dev).contiguous()
+
+
+def host64(x) -> np.ndarray:
+    if isinstance(x, torch.Tensor):
+        return x.detach().to("cpu", torch.float64).numpy()
+    return np.asarray(x, dtype=np.float64)
+
+
+def ptr(t: Optional[torch.Tensor]):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def stream_handle():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+# ------------------------------------------------------ flattened model
+@dataclass
+class CenterTrack:
+    """Uniform-knot progenitor track for TimeDepTranslatingPotential.
+
+    The reference uses interpax.Interpolator1D(x=ts, f=positions,
+    method='cubic') (streamhelpers.py:520).  Knot slopes are filled on the
+    device by ss_track_slopes (mean of adjacent secants, one-sided ends)."""
+
+    t0: float
+    dt: float
+    knots: torch.Tensor  # [n, 3] float64 (device)
+    slopes: Optional[torch.Tensor] = None
+
+    @staticmethod
+    def from_samples(ts, positions) -> "CenterTrack":
+        ts_h = host64(ts)
+        if ts_h.ndim != 1 or len(ts_h) < 2:
+            raise ValueError("track needs >= 2 knot times")
+        d = np.diff(ts_h)
+        if not np.allclose(d, d[0], rtol=1e-9, atol=1e-12) or d[0] <= 0:
+            raise NotImplementedError("track knots must be uniformly spaced and increasing")
+        knots = f64(positions)
+        if knots.ndim != 2 or knots.shape[1] < 3 or knots.shape[0] != len(ts_h):
+            raise ValueError("positions must be [len(ts), >=3]")
+        knots = knots[:, :3].contiguous()
+        return CenterTrack(float(ts_h[0]), float(d[0]), knots)
+
+    def ensure_slopes(self):
+        if self.slopes is None or self.slopes.device != self.knots.device:
+            self.slopes = torch.empty_like(self.knots)
+            _abi.call("ss_track_slopes", ptr(self.knots), self.knots.shape[0], self.dt, ptr(self.slopes),
+                      stream_handle())
+        return self.slopes
+
+
+@dataclass
+class SubhaloTable:
+    kind: int
+    m: torch.Tensor
+    a: torch.Tensor
+    x0: torch.Tensor
+    v: torch.Tensor
+    t0: torch.Tensor
+    t_window: float
+
+    def struct(self) -> _abi.ss_subhalos:
+        s = _abi.ss_subhalos()
+        s.kind = self.kind
+        s.n = int(self.m.shape[0])
+        s.m, s.a, s.x0, s.v, s.t0 = (self.m.data_ptr(), self.a.data_ptr(), self.x0.data_ptr(),
+                                     self.v.data_ptr(), self.t0.data_ptr())
+        s.t_window = float(self.t_window)
+        return s
+
+    def same_lines(self, other: "SubhaloTable") -> bool:
+        return (self.kind == other.kind and self.t_window == other.t_window and
+                all(torch.equal(getattr(self, k), getattr(other, k)) for k in ("m", "a", "x0", "v", "t0")))
+
+
+@dataclass
+class Flat:
+    comps: List[Tuple[int, int, Tuple[float, ...]]] = field(default_factory=list)
+    track: Optional[CenterTrack] = None
+    subhalos: Optional[SubhaloTable] = None
+
+    def extend(self, other: "Flat"):
+        self.comps.extend(other.comps)
+        if other.track is not None:
+            if self.track is not None and self.track is not other.track:
+                raise NotImplementedError("at most one center track per potential")
+            self.track = other.track
+        if other.subhalos is not None:
+            if self.subhalos is not None:
+                raise NotImplementedError("at most one subhalo table per potential")
+            self.subhalos = other.subhalos
+
+
+def make_struct(flat: Flat, G: float) -> _abi.ss_potential:
+    if len(flat.comps) > _abi.SS_MAX_COMPONENTS:
+        raise NotImplementedError(f"more than {_abi.SS_MAX_COMPONENTS} potential components")
+    P = _abi.ss_potential()
+    P.G = float(G)
+    P.n_components = len(flat.comps)
+    for i, (kind, center, params) in enumerate(flat.comps):
+        P.comp[i].kind = kind
+        P.comp[i].center = center
+        for j, v in enumerate(params):
+            P.comp[i].p[j] = float(v)
+    if flat.track is not None:
+        flat.track.ensure_slopes()
+        P.track.knots = flat.track.knots.data_ptr()
+        P.track.slopes = flat.track.slopes.data_ptr()
+        P.track.t0 = flat.track.t0
+        P.track.dt = flat.track.dt
+        P.track.n_knots = flat.track.knots.shape[0]
+    if flat.subhalos is not None:
+        P.subhalos = flat.subhalos.struct()
+    return P
+
+
+# ------------------------------------------------------------ fixed step
+def fixed_step(span: float, dt=None, grid=None, dtmin=None, dtmax=None) -> Tuple[float, int]:
+    """Step h (signed like span) and step count for a fixed-step solve.
+
+    The reference's adaptive PIDController (main.py:146) becomes a fixed step:
+    `dt` when given; else the spacing of the save grid (reduced to a divisor
+    no larger than dtmax); else dtmin.  The span must be a whole number of
+    steps."""
+    if span == 0:
+        return (1.0 if dt is None else float(abs(dt))), 0
+    sign = 1.0 if span > 0 else -1.0
+    if dt is not None:
+        h = abs(float(dt))
+    elif grid is not None and grid > 0:
+        h = float(grid)
+        if dtmax is not None and dtmax < h:
+            h = h / math.ceil(h / float(dtmax) - 1e-12)
+    elif dtmin is not None:
+        h = float(dtmin)
+    else:
+        raise ValueError("fixed-step integration needs dt")
+    n = round(abs(span) / h)
+    if n < 1 or abs(n * h - abs(span)) > 1e-9 * max(1.0, abs(span)):
+        raise ValueError(f"span {span} is not a whole number of steps of {h}; pass dt=")
+    return sign * h, int(n)
+
+
+def check_solver(solver):
+    """Only Dopri5 is implemented (fixed step); others raise."""
+    if solver is None:
+        return
+    name = solver if isinstance(solver, str) else type(solver).__name__
+    if "dopri5" not in str(name).lower():
+        raise NotImplementedError(f"solver {name!r}: only fixed-step Dopri5 is implemented on the GPU path")
+
+
+# ------------------------------------------------------- entry wrappers
+def potential_eval(P, xyz: torch.Tensor, t, phi=True, grad=True, hess=False):
+    n = xyz.shape[0]
+    dev = xyz.device
+    tt = None
+    ts = 0.0
+    if isinstance(t, torch.Tensor) and t.ndim > 0 or isinstance(t, np.ndarray) and np.ndim(t) > 0:
+        tt = f64(t, dev).reshape(-1)
+        if tt.shape[0] != n:
+            raise ValueError("t must be scalar or have one entry per point")
+    else:
+        ts = float(t)
+    o_phi = torch.empty(n, dtype=torch.float64, device=dev) if phi else None
+    o_g = torch.empty(n, 3, dtype=torch.float64, device=dev) if grad else None
+    o_h = torch.empty(n, 3, 3, dtype=torch.float64, device=dev) if hess else None
+    _abi.call("ss_potential_eval", C.byref(P), ptr(xyz), n, ptr(tt), ts, ptr(o_phi), ptr(o_g), ptr(o_h),
+              stream_handle())
+    return o_phi, o_g, o_h
+
+
+def orbit(P, w0: torch.Tensor, t0: float, dt: float, n_steps: int, save_every: int) -> torch.Tensor:
+    n = w0.shape[0]
+    out = torch.empty(n, n_steps // save_every + 1, 6, dtype=torch.float64, device=w0.device)
+    _abi.call("ss_orbit_f64", C.byref(P), ptr(w0), n, float(t0), float(dt), int(n_steps), int(save_every),
+              ptr(out), stream_handle())
+    return out
+
+
+def release(P, cfg, prog_w, t_rel, msat, normals, jac=False):
+    n_rel, n_draw = cfg.n_release, cfg.n_draw
+    ics = torch.empty(n_rel, n_draw, 2, 6, dtype=torch.float64, device=prog_w.device)
+    J = torch.empty(n_rel, n_draw, 2, 6, 6, dtype=torch.float64, device=prog_w.device) if jac else None
+    _abi.call("ss_release_f64", C.byref(P), C.byref(cfg), ptr(prog_w), ptr(t_rel), ptr(msat), ptr(normals),
+              ptr(ics), ptr(J), stream_handle())
+    return ics, J
+
+
+class Workspace:
+    """Grow-only device scratch shared by the calls of one process."""
+
+    _bufs = {}
+
+    @classmethod
+    def get(cls, nbytes: int, dev: torch.device) -> Optional[torch.Tensor]:
+        if nbytes <= 0:
+            return None
+        key = (dev.type, dev.index)
+        buf = cls._bufs.get(key)
+        if buf is None or buf.numel() < nbytes:
+            buf = torch.empty(int(nbytes) + 256, dtype=torch.uint8, device=dev)
+            cls._bufs[key] = buf
+        return buf
+
+
+def aligned_ptr(buf: Optional[torch.Tensor], align: int = 256):
+    if buf is None:
+        return None, 0
+    p = buf.data_ptr()
+    off = (-p) % align
+    return C.c_void_p(p + off), buf.numel() - off
+
+
+# When set to a list, stream() appends a (start, end) CUDA event pair recorded
+# around each stream-kernel call on the current stream (benchmark timing).
+STREAM_EVENTS = None
+
+
+def stream(P, cfg, ics: torch.Tensor, precision: str, want_final=True, snaps=None, status=True):
+    N = cfg.n_particles
+    dev = ics.device
+    final = torch.empty(N, 6, dtype=torch.float64, device=dev) if want_final else None
+    st = torch.empty(N, dtype=torch.int32, device=dev) if status else None
+    evs = STREAM_EVENTS
+    if evs is not None:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+    if precision == "f64":
+        _abi.call("ss_stream_f64", C.byref(P), C.byref(cfg), ptr(ics), ptr(final), ptr(snaps), ptr(st),
+                  stream_handle())
+    elif precision == "f32k":
+        need = _abi.load().ss_stream_workspace_bytes(C.byref(P), C.byref(cfg))
+        if need < 0:
+            raise _abi.SSError("ss_stream_workspace_bytes", need, _abi.load().ss_last_error().decode())
+        ws, nb = aligned_ptr(Workspace.get(need, dev))
+        _abi.call("ss_stream_f32k", C.byref(P), C.byref(cfg), ptr(ics), ptr(final), ptr(snaps), ptr(st),
+                  ws, nb, stream_handle())
+    else:
+        raise ValueError("precision must be 'f64' or 'f32k'")
+    if evs is not None:
+        e1.record()
+        evs.append((e0, e1))
+    return final, st
+
+
+def subhalo_eval(table: SubhaloTable, G: float, xyz: torch.Tensor, t: float):
+    n, ns = xyz.shape[0], int(table.m.shape[0])
+    dev = xyz.device
+    phi = torch.empty(n, ns, dtype=torch.float64, device=dev)
+    grad = torch.empty(n, ns, 3, dtype=torch.float64, device=dev)
+    dphi = torch.empty(n, ns, dtype=torch.float64, device=dev)
+    gdphi = torch.empty(n, ns, 3, dtype=torch.float64, device=dev)
+    S = table.struct()
+    _abi.call("ss_subhalo_eval", C.byref(S), float(G), ptr(xyz), n, float(t), ptr(phi), ptr(grad), ptr(dphi),
+              ptr(gdphi), stream_handle())
+    return phi, grad, dphi, gdphi
+
+
+def pert_response(P, table: SubhaloTable, cfg, precision: int, base_ics, pert_ics, chunk_particles=None):
+    dev = base_ics.device
+    dtype = torch.float64 if precision == 64 else torch.float32
+    N, ns, ncol = cfg.n_particles, int(table.m.shape[0]), cfg.ncol
+    n_saves = cfg.n_steps // cfg.save_stride + 1 if cfg.save_stride > 0 else 1
+    out = torch.empty(n_saves, N, ns, ncol, dtype=dtype, device=dev)
+    base_out = torch.empty(N, 6, dtype=torch.float64, device=dev)
+    if chunk_particles is None:
+        # about 2 GB of base-track records per chunk
+        per = max(1, cfg.n_steps) * 56 * (8 if precision == 64 else 4)
+        chunk_particles = max(1, min(N, (2 << 30) // per))
+    need = _abi.load().ss_pert_workspace_bytes(C.byref(cfg), precision, int(chunk_particles))
+    if need < 0:
+        raise _abi.SSError("ss_pert_workspace_bytes", need, _abi.load().ss_last_error().decode())
+    ws, nb = aligned_ptr(Workspace.get(need, dev))
+    S = table.struct()
+    if pert_ics is not None:
+        pert_ics = pert_ics.to(dtype).contiguous()
+    _abi.call("ss_pert_response", C.byref(P), C.byref(S), C.byref(cfg), int(precision), ptr(base_ics),
+              ptr(pert_ics), ptr(base_out), ptr(out), ws, nb, stream_handle())
+    return base_out, out
+
+
+def binned_sums(values: torch.Tensor, key: torch.Tensor, edges: torch.Tensor):
+    n, ncomp = values.shape
+    nb = edges.shape[0] - 1
+    sums = torch.empty(nb, ncomp, dtype=torch.float64, device=values.device)
+    counts = torch.empty(nb, ncomp, dtype=torch.float64, device=values.device)
+    _abi.call("ss_binned_sums", ptr(values), ptr(key), n, ncomp, ptr(edges), edges.shape[0], ptr(sums),
+              ptr(counts), stream_handle())
+    return sums, counts

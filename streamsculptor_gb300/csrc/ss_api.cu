@@ -1,0 +1,532 @@
+// ss_api.cu — C ABI entry points for potential evaluation, FP64 orbits,
+// the progenitor track, the release model, binned sums and the FMA peak probe.
+// The stream kernels live in ss_stream.cu, the response kernels in ss_pert.cu.
+
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <atomic>
+#include <cmath>
+
+#include "ss_common.cuh"
+
+namespace ssg {
+
+static thread_local char g_err[512] = "";
+static std::atomic<long long> g_launches{0};
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+int set_error(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+const char* last_error() { return g_err; }
+
+template <class R>
+int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalos) {
+    SS_CHECK_ARG(in != nullptr, "potential is NULL");
+    SS_CHECK_ARG(in->n_components >= 0 && in->n_components <= SS_MAX_COMPONENTS,
+                 "n_components=%d outside [0, %d]", in->n_components, SS_MAX_COMPONENTS);
+    SS_CHECK_ARG(std::isfinite(in->G) && in->G > 0.0, "G must be finite and > 0");
+    memset(out, 0, sizeof(*out));
+    out->n = in->n_components;
+    bool need_track = false;
+    const double G = in->G;
+    for (int k = 0; k < in->n_components; ++k) {
+        const ss_component& c = in->comp[k];
+        const double* p = c.p;
+        CompDev<R>& d = out->c[k];
+        d.kind = c.kind;
+        SS_CHECK_ARG(c.center == SS_CENTER_ORIGIN || c.center == SS_CENTER_TRACK,
+                     "component %d: center=%d invalid", k, c.center);
+        d.center = c.center;
+        need_track |= (c.center == SS_CENTER_TRACK);
+        for (int i = 0; i < 6; ++i) SS_CHECK_ARG(std::isfinite(p[i]), "component %d: non-finite parameter p[%d]", k, i);
+        switch (c.kind) {
+            case SS_NFW:
+                SS_CHECK_ARG(p[1] > 0.0 && p[2] >= 0.0, "component %d (NFW): need r_s > 0, soft >= 0", k);
+                d.q[0] = R(G * p[0]); d.q[1] = R(p[1]); d.q[2] = R(1.0 / p[1]); d.q[3] = R(p[2]);
+                break;
+            case SS_TRIAXIAL_NFW:
+                SS_CHECK_ARG(p[1] > 0.0 && p[2] > 0.0 && p[3] > 0.0 && p[4] > 0.0,
+                             "component %d (TriaxialNFW): need r_s, q1, q2, q3 > 0", k);
+                d.q[0] = R(G * p[0]); d.q[1] = R(p[1]); d.q[2] = R(1.0 / p[2]); d.q[3] = R(1.0 / p[3]);
+                d.q[4] = R(1.0 / p[4]); d.q[5] = R(1.0 / p[1]);
+                break;
+            case SS_MIYAMOTO_NAGAI:
+                SS_CHECK_ARG(p[1] >= 0.0 && p[2] > 0.0, "component %d (MiyamotoNagai): need a >= 0, b > 0", k);
+                d.q[0] = R(G * p[0]); d.q[1] = R(p[1]); d.q[2] = R(p[2] * p[2]);
+                break;
+            case SS_HERNQUIST:
+                SS_CHECK_ARG(p[1] >= 0.0 && p[2] >= 0.0, "component %d (Hernquist): need r_s >= 0, soft >= 0", k);
+                d.q[0] = R(G * p[0]); d.q[1] = R(p[1]); d.q[2] = R(p[2]);
+                break;
+            case SS_PLUMMER:
+                SS_CHECK_ARG(p[1] >= 0.0, "component %d (Plummer): need r_s >= 0", k);
+                d.q[0] = R(G * p[0]); d.q[1] = R(p[1] * p[1]);
+                break;
+            case SS_ISOCHRONE:
+                SS_CHECK_ARG(p[1] > 0.0, "component %d (Isochrone): need a > 0", k);
+                d.q[0] = R(G * p[0]); d.q[1] = R(p[1]); d.q[2] = R(p[1] * p[1]);
+                break;
+            default:
+                return set_error(SS_ERR_INVALID_ARGUMENT, "component %d: unknown kind %d", k, c.kind);
+        }
+    }
+    out->has_track = need_track ? 1 : 0;
+    if (need_track) {
+        const ss_track& tr = in->track;
+        SS_CHECK_ARG(tr.knots != nullptr && tr.slopes != nullptr, "center track: knots/slopes NULL");
+        SS_CHECK_ARG(tr.n_knots >= 2, "center track: need >= 2 knots");
+        SS_CHECK_ARG(std::isfinite(tr.dt) && tr.dt > 0.0 && std::isfinite(tr.t0), "center track: need dt > 0");
+        out->track.knots = tr.knots;
+        out->track.slopes = tr.slopes;
+        out->track.t0 = tr.t0;
+        out->track.dt = tr.dt;
+        out->track.n = tr.n_knots;
+    }
+    const ss_subhalos& sh = in->subhalos;
+    SS_CHECK_ARG(sh.n >= 0 && sh.n <= (int64_t)1 << 30, "subhalos: bad n");
+    if (sh.n > 0) {
+        SS_CHECK_ARG(allow_subhalos, "this entry point takes the subhalos separately; potential.subhalos must be empty");
+        SS_CHECK_ARG(sh.kind == SS_SH_PLUMMER || sh.kind == SS_SH_HERNQUIST, "subhalos: unknown kind %d", sh.kind);
+        SS_CHECK_ARG(sh.m && sh.a && sh.x0 && sh.v && sh.t0, "subhalos: NULL table pointer");
+        SS_CHECK_ARG(!(sh.t_window < 0.0), "subhalos: t_window < 0");
+        out->sh.kind = sh.kind;
+        out->sh.n = (int32_t)sh.n;
+        out->sh.m = sh.m;
+        out->sh.a = sh.a;
+        out->sh.x0 = sh.x0;
+        out->sh.v = sh.v;
+        out->sh.t0 = sh.t0;
+        out->sh.t_window = sh.t_window;
+        out->sh.G = G;
+    }
+    return SS_OK;
+}
+
+template int prepare_potential<double>(const ss_potential*, PotDev<double>*, bool);
+template int prepare_potential<float>(const ss_potential*, PotDev<float>*, bool);
+
+// ------------------------------------------------------------- Phi (FP64)
+__device__ double comp_phi(const CompDev<double>& c, const double x[3]) {
+    const double* q = c.q;
+    double r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+    switch (c.kind) {
+        case SS_NFW: {
+            double r = sqrt(r2 + q[3]);
+            return -q[0] * log1p(r * q[2]) / r;
+        }
+        case SS_TRIAXIAL_NFW: {
+            double a = x[0] * q[2], b = x[1] * q[3], d = x[2] * q[4];
+            double r = sqrt(a * a + b * b + d * d);
+            return -q[0] * log1p(r * q[5]) / r;
+        }
+        case SS_MIYAMOTO_NAGAI: {
+            double az = sqrt(x[2] * x[2] + q[2]) + q[1];
+            return -q[0] / sqrt(x[0] * x[0] + x[1] * x[1] + az * az);
+        }
+        case SS_HERNQUIST:
+            return -q[0] / (sqrt(r2 + q[2]) + q[1]);
+        case SS_PLUMMER:
+            return -q[0] / sqrt(r2 + q[1]);
+        case SS_ISOCHRONE:
+            return -q[0] / (q[1] + sqrt(r2 + q[2]));
+        default:
+            return nan("");
+    }
+}
+
+__global__ void potential_eval_kernel(PotDev<double> P, const double* __restrict__ xyz, int64_t n,
+                                      const double* __restrict__ tarr, double t_scalar, double* phi,
+                                      double* grad, double* hess) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double t = tarr ? tarr[i] : t_scalar;
+    double x[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+    double c[3] = {0.0, 0.0, 0.0};
+    if (P.has_track) track_eval(P.track, t, c);
+    if (phi) {
+        double f = 0.0;
+        for (int k = 0; k < P.n; ++k) {
+            if (P.c[k].center == SS_CENTER_TRACK) {
+                double xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
+                f += comp_phi(P.c[k], xs);
+            } else {
+                f += comp_phi(P.c[k], x);
+            }
+        }
+        for (int j = 0; j < P.sh.n; ++j) {
+            double tau = t - P.sh.t0[j];
+            if (!(fabs(tau) < P.sh.t_window)) continue;
+            double rel[3];
+            for (int k = 0; k < 3; ++k) rel[k] = x[k] - (P.sh.x0[3 * j + k] + P.sh.v[3 * j + k] * tau);
+            double r2 = rel[0] * rel[0] + rel[1] * rel[1] + rel[2] * rel[2];
+            double Gm = P.sh.G * P.sh.m[j], a = P.sh.a[j];
+            f += P.sh.kind == SS_SH_PLUMMER ? -Gm / sqrt(r2 + a * a) : -Gm / (sqrt(r2) + a);
+        }
+        phi[i] = f;
+    }
+    if (grad || hess) {
+        double g[3], H[6];
+        pot_grad<double, double, true>(P, x, c, g, H);
+        if (P.sh.n > 0) subhalo_sum_grad<double>(P.sh, x, t, g);
+        if (grad)
+            for (int k = 0; k < 3; ++k) grad[3 * i + k] = g[k];
+        if (hess) {
+            double* o = hess + 9 * i;
+            o[0] = H[0]; o[1] = H[3]; o[2] = H[4];
+            o[3] = H[3]; o[4] = H[1]; o[5] = H[5];
+            o[6] = H[4]; o[7] = H[5]; o[8] = H[2];
+        }
+    }
+}
+
+// ------------------------------------------------------------- orbits
+__global__ void __launch_bounds__(64) orbit_f64_kernel(PotDev<double> P, const double* __restrict__ w0,
+                                                       int64_t n_orbits, double t0, double dt, int64_t n_steps,
+                                                       int64_t save_every, double* __restrict__ out) {
+    int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= n_orbits) return;
+    const int64_t n_save = n_steps / save_every + 1;
+    double y[6];
+    for (int i = 0; i < 6; ++i) y[i] = w0[6 * o + i];
+    double* base = out + o * n_save * 6;
+    for (int i = 0; i < 6; ++i) base[i] = y[i];
+    for (int64_t n = 0; n < n_steps; ++n) {
+        dopri5_step_f64(P, t0 + (double)n * dt, dt, y);
+        if ((n + 1) % save_every == 0) {
+            double* b = base + 6 * ((n + 1) / save_every);
+            for (int i = 0; i < 6; ++i) b[i] = y[i];
+        }
+    }
+}
+
+// ------------------------------------------------------------- track
+// Knot slopes as interpax 'cubic' defines them: mean of the adjacent
+// secants, one-sided at the ends.
+__global__ void track_slopes_kernel(const double* __restrict__ knots, int64_t n, double dt, double* slopes) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * n) return;
+    int64_t k = i / 3;
+    int c = (int)(i % 3);
+    double s;
+    if (n < 2) {
+        s = 0.0;
+    } else if (k == 0) {
+        s = (knots[3 + c] - knots[c]) / dt;
+    } else if (k == n - 1) {
+        s = (knots[3 * k + c] - knots[3 * (k - 1) + c]) / dt;
+    } else {
+        double sl = (knots[3 * k + c] - knots[3 * (k - 1) + c]) / dt;
+        double sr = (knots[3 * (k + 1) + c] - knots[3 * k + c]) / dt;
+        s = 0.5 * (sl + sr);
+    }
+    slopes[i] = s;
+}
+
+// ------------------------------------------------------------- release
+// tidal radius pieces, templated on double / Dual<6>:
+// omega (main.py:88-96), d2phidr2 (main.py:76-85), tidalr (main.py:98-104).
+template <class T>
+__device__ T release_tidal_radius(const PotDev<double>& P, const T x[3], const T v[3], double GMsat, double t,
+                                  T rh[3], T zh[3], T ph[3], T& om) {
+    T r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+    T r = s_sqrt(r2);
+    T ir = s_rcp(r);
+    rh[0] = x[0] * ir; rh[1] = x[1] * ir; rh[2] = x[2] * ir;
+    T L[3] = {x[1] * v[2] - x[2] * v[1], x[2] * v[0] - x[0] * v[2], x[0] * v[1] - x[1] * v[0]};
+    T L2 = L[0] * L[0] + L[1] * L[1] + L[2] * L[2];
+    T Ln = s_sqrt(L2);
+    om = Ln * s_rcp(r2);
+    T iLn = s_rcp(Ln);
+    zh[0] = L[0] * iLn; zh[1] = L[1] * iLn; zh[2] = L[2] * iLn;
+    T vr = v[0] * rh[0] + v[1] * rh[1] + v[2] * rh[2];
+    T pv[3] = {v[0] - vr * rh[0], v[1] - vr * rh[1], v[2] - vr * rh[2]};
+    T ipn = s_rsqrt(pv[0] * pv[0] + pv[1] * pv[1] + pv[2] * pv[2]);
+    ph[0] = pv[0] * ipn; ph[1] = pv[1] * ipn; ph[2] = pv[2] * ipn;
+    double c[3] = {0.0, 0.0, 0.0};
+    if (P.has_track) track_eval(P.track, t, c);
+    T cc[3] = {T(c[0]), T(c[1]), T(c[2])};
+    T g[3], H[6];
+    pot_grad<T, double, true>(P, x, cc, g, H);
+    // r_hat^T H r_hat
+    T d2 = H[0] * rh[0] * rh[0] + H[1] * rh[1] * rh[1] + H[2] * rh[2] * rh[2] +
+           2.0 * (H[3] * rh[0] * rh[1] + H[4] * rh[0] * rh[2] + H[5] * rh[1] * rh[2]);
+    return s_cbrt(GMsat * s_rcp(om * om - d2));
+}
+
+template <class T>
+__device__ void release_one(const PotDev<double>& P, double G, const ss_release_cfg& cfg, const T x[3],
+                            const T v[3], double Msat, double t, const double* z, T out[2][6]) {
+    T rh[3], zh[3], ph[3], om;
+    T rt = release_tidal_radius<T>(P, x, v, G * Msat, t, rh, zh, ph, om);
+    if (cfg.model == SS_RELEASE_CHEN25) {
+        // release_model_Chen25, streamhelpers.py:352-432
+        double pvs[6];
+        for (int i = 0; i < 6; ++i) {
+            double s = cfg.chen_mean[i];
+            for (int j = 0; j < 6; ++j) s += cfg.chen_L[6 * i + j] * z[j];
+            pvs[i] = s;
+        }
+        T Dr = pvs[0] * rt;
+        T vesc = s_sqrt(2.0 * G * Msat * s_rcp(Dr));
+        T Dv = pvs[3] * vesc;
+        const double deg = 0.017453292519943295;
+        double phi = pvs[1] * deg, theta = pvs[2] * deg, alpha = pvs[4] * deg, beta = pvs[5] * deg;
+        double ct = cos(theta), st = sin(theta), cp = cos(phi), sp = sin(phi);
+        double ca = cos(alpha), sa = sin(alpha), cb = cos(beta), sb = sin(beta);
+        for (int i = 0; i < 3; ++i) {
+            T ax = (Dr * (ct * cp)) * rh[i], ay = (Dr * (ct * sp)) * ph[i], az = (Dr * st) * zh[i];
+            T bx = (Dv * (cb * ca)) * rh[i], by = (Dv * (cb * sa)) * ph[i], bz = (Dv * sb) * zh[i];
+            out[1][i] = x[i] + ax + ay + az;
+            out[1][3 + i] = v[i] + bx + by + bz;
+            out[0][i] = x[i] - ax - ay + az;
+            out[0][3 + i] = v[i] - bx - by + bz;
+        }
+    } else {
+        // Potential.release_model, main.py:209-280
+        const double* kv = cfg.kvals;
+        double kr = kv[0] + z[0] * kv[4];
+        double kvphi = kr * (kv[1] + z[1] * kv[5]);
+        double kz = kv[2] + z[2] * kv[6];
+        double kvz = kv[3] + z[3] * kv[7];
+        T vc = om * rt;
+        for (int i = 0; i < 3; ++i) {
+            T dpos = (kr * rt) * rh[i] + (kz * rt) * zh[i];
+            T dvel = (kvphi * vc) * ph[i] + (kvz * vc) * zh[i];
+            out[1][i] = x[i] + dpos;      // trailing: nudged out
+            out[1][3 + i] = v[i] + dvel;
+            out[0][i] = x[i] - dpos;      // leading: nudged in
+            out[0][3 + i] = v[i] - dvel;
+        }
+    }
+}
+
+template <bool JAC>
+__global__ void release_kernel(PotDev<double> P, double G, ss_release_cfg cfg, const double* __restrict__ prog_w,
+                               const double* __restrict__ t_rel, const double* __restrict__ msat,
+                               const double* __restrict__ normals, double* __restrict__ ics,
+                               double* __restrict__ jac) {
+    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t total = cfg.n_release * cfg.n_draw;
+    if (q >= total) return;
+    int64_t r = q / cfg.n_draw;
+    const int nz = cfg.model == SS_RELEASE_CHEN25 ? 6 : 4;
+    const double* z = normals + q * nz;
+    const double* w = prog_w + 6 * r;
+    if (!JAC) {
+        double x[3] = {w[0], w[1], w[2]}, v[3] = {w[3], w[4], w[5]};
+        double out[2][6];
+        release_one<double>(P, G, cfg, x, v, msat[r], t_rel[r], z, out);
+        for (int a = 0; a < 2; ++a)
+            for (int i = 0; i < 6; ++i) ics[q * 12 + 6 * a + i] = out[a][i];
+    } else {
+        typedef Dual<6> D6;
+        D6 x[3], v[3];
+        for (int i = 0; i < 3; ++i) {
+            x[i] = D6(w[i]);
+            x[i].d[i] = 1.0;
+            v[i] = D6(w[3 + i]);
+            v[i].d[3 + i] = 1.0;
+        }
+        D6 out[2][6];
+        release_one<D6>(P, G, cfg, x, v, msat[r], t_rel[r], z, out);
+        for (int a = 0; a < 2; ++a)
+            for (int i = 0; i < 6; ++i) {
+                ics[q * 12 + 6 * a + i] = out[a][i].v;
+                for (int j = 0; j < 6; ++j) jac[q * 72 + 36 * a + 6 * i + j] = out[a][i].d[j];
+            }
+    }
+}
+
+// ------------------------------------------------------------- binned sums
+__global__ void binned_sums_kernel(const double* __restrict__ values, const double* __restrict__ key, int64_t n,
+                                   int ncomp, const double* __restrict__ edges, int n_edges, double* sums,
+                                   double* counts) {
+    extern __shared__ double sm[];
+    const int nb = n_edges - 1;
+    const int nslots = nb * ncomp;
+    double* s_sum = sm;
+    double* s_cnt = sm + nslots;
+    for (int i = threadIdx.x; i < 2 * nslots; i += blockDim.x) sm[i] = 0.0;
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double k = key[i];
+        // number of edges <= k (upper bound); NaN keys compare false -> bin 0
+        int lo = 0, hi = n_edges;
+        while (lo < hi) {
+            int mid = (lo + hi) >> 1;
+            if (edges[mid] <= k) lo = mid + 1; else hi = mid;
+        }
+        int b = lo;
+        if (b >= nb) continue;
+        for (int c = 0; c < ncomp; ++c) {
+            double v = values[i * ncomp + c];
+            if (isnan(v)) continue;
+            atomicAdd(s_sum + b * ncomp + c, v);
+            atomicAdd(s_cnt + b * ncomp + c, 1.0);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nslots; i += blockDim.x) {
+        if (s_cnt[i] != 0.0) {
+            atomicAdd(sums + i, s_sum[i]);
+            atomicAdd(counts + i, s_cnt[i]);
+        }
+    }
+}
+
+// ------------------------------------------------------------- FMA peak
+template <class T>
+__global__ void __launch_bounds__(256) peak_fma_kernel(int64_t iters, T* sink) {
+    T a0 = T(threadIdx.x) * T(1e-3), a1 = a0 + T(1), a2 = a0 + T(2), a3 = a0 + T(3);
+    T a4 = a0 + T(4), a5 = a0 + T(5), a6 = a0 + T(6), a7 = a0 + T(7);
+    const T b = T(0.999999), c = T(1e-6);
+    for (int64_t i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+            a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+        }
+    }
+    T s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (s == T(-12345.678)) sink[threadIdx.x] = s;
+}
+
+}  // namespace ssg
+
+using namespace ssg;
+
+static inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+extern "C" {
+
+int ss_abi_version(void) { return SS_ABI_VERSION; }
+
+int64_t ss_kernel_launches(void) { return (int64_t)g_launches.load(std::memory_order_relaxed); }
+
+const char* ss_last_error(void) { return ssg::last_error(); }
+
+int64_t ss_abi_sizeof(int which) {
+    switch (which) {
+        case 0: return (int64_t)sizeof(ss_potential);
+        case 1: return (int64_t)sizeof(ss_stream_cfg);
+        case 2: return (int64_t)sizeof(ss_release_cfg);
+        case 3: return (int64_t)sizeof(ss_pert_cfg);
+        case 4: return (int64_t)sizeof(ss_component);
+        case 5: return (int64_t)sizeof(ss_track);
+        case 6: return (int64_t)sizeof(ss_subhalos);
+        default: return -1;
+    }
+}
+
+int ss_potential_eval(const ss_potential* pot, const double* xyz, int64_t n, const double* t, double t_scalar,
+                      double* phi, double* grad, double* hess, void* stream) {
+    PotDev<double> P;
+    int rc = prepare_potential<double>(pot, &P, true);
+    if (rc) return rc;
+    SS_CHECK_ARG(n >= 0, "n < 0");
+    if (n == 0) return SS_OK;
+    SS_CHECK_ARG(xyz != nullptr, "xyz is NULL");
+    potential_eval_kernel<<<grid_for(n, 128), 128, 0, (cudaStream_t)stream>>>(P, xyz, n, t, t_scalar, phi, grad,
+                                                                              hess);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
+int ss_orbit_f64(const ss_potential* pot, const double* w0, int64_t n_orbits, double t0, double dt,
+                 int64_t n_steps, int64_t save_every, double* out, void* stream) {
+    PotDev<double> P;
+    int rc = prepare_potential<double>(pot, &P, true);
+    if (rc) return rc;
+    SS_CHECK_ARG(n_orbits >= 0 && n_steps >= 0, "negative size");
+    SS_CHECK_ARG(save_every >= 1, "save_every must be >= 1");
+    SS_CHECK_ARG(std::isfinite(dt) && dt != 0.0 && std::isfinite(t0), "dt must be finite and non-zero");
+    if (n_orbits == 0) return SS_OK;
+    SS_CHECK_ARG(w0 && out, "NULL buffer");
+    orbit_f64_kernel<<<grid_for(n_orbits, 64), 64, 0, (cudaStream_t)stream>>>(P, w0, n_orbits, t0, dt, n_steps,
+                                                                            save_every, out);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
+int ss_track_slopes(const double* knots, int64_t n_knots, double dt, double* slopes, void* stream) {
+    SS_CHECK_ARG(knots && slopes, "NULL buffer");
+    SS_CHECK_ARG(n_knots >= 2, "need >= 2 knots");
+    SS_CHECK_ARG(std::isfinite(dt) && dt > 0.0, "dt must be > 0");
+    track_slopes_kernel<<<grid_for(3 * n_knots, 256), 256, 0, (cudaStream_t)stream>>>(knots, n_knots, dt, slopes);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
+int ss_release_f64(const ss_potential* pot, const ss_release_cfg* cfg, const double* prog_w, const double* t_rel,
+                   const double* msat, const double* normals, double* ics, double* jac, void* stream) {
+    PotDev<double> P;
+    int rc = prepare_potential<double>(pot, &P, true);
+    if (rc) return rc;
+    SS_CHECK_ARG(cfg != nullptr, "cfg is NULL");
+    SS_CHECK_ARG(cfg->n_release >= 0 && cfg->n_draw >= 1, "n_release >= 0 and n_draw >= 1 required");
+    SS_CHECK_ARG(cfg->model == SS_RELEASE_FARDAL || cfg->model == SS_RELEASE_CHEN25, "unknown release model %d",
+                 cfg->model);
+    int64_t total = cfg->n_release * cfg->n_draw;
+    if (total == 0) return SS_OK;
+    SS_CHECK_ARG(prog_w && t_rel && msat && normals && ics, "NULL buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (jac)
+        release_kernel<true><<<grid_for(total, 64), 64, 0, s>>>(P, pot->G, *cfg, prog_w, t_rel, msat, normals, ics, jac);
+    else
+        release_kernel<false><<<grid_for(total, 128), 128, 0, s>>>(P, pot->G, *cfg, prog_w, t_rel, msat, normals, ics,
+                                                                   nullptr);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
+int ss_binned_sums(const double* values, const double* key, int64_t n, int32_t ncomp, const double* edges,
+                   int32_t n_edges, double* sums, double* counts, void* stream) {
+    SS_CHECK_ARG(ncomp >= 1 && ncomp <= 64, "ncomp must be in [1, 64]");
+    SS_CHECK_ARG(n_edges >= 2, "need >= 2 edges");
+    SS_CHECK_ARG(n >= 0, "n < 0");
+    SS_CHECK_ARG(edges && sums && counts, "NULL buffer");
+    int64_t nslots = (int64_t)(n_edges - 1) * ncomp;
+    SS_CHECK_ARG(2 * nslots * (int64_t)sizeof(double) <= 96 * 1024, "too many bins x components for one block");
+    cudaStream_t s = (cudaStream_t)stream;
+    SS_CUDA_TRY(cudaMemsetAsync(sums, 0, nslots * sizeof(double), s));
+    SS_CUDA_TRY(cudaMemsetAsync(counts, 0, nslots * sizeof(double), s));
+    if (n == 0) return SS_OK;
+    SS_CHECK_ARG(values && key, "NULL buffer");
+    size_t smem = 2 * nslots * sizeof(double);
+    if (smem > 48 * 1024)
+        SS_CUDA_TRY(cudaFuncSetAttribute(binned_sums_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int64_t blocks = grid_for(n, 256);
+    if (blocks > 4 * 152) blocks = 4 * 152;
+    binned_sums_kernel<<<(unsigned)blocks, 256, smem, s>>>(values, key, n, ncomp, edges, n_edges, sums, counts);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
+int ss_peak_fma(int precision, int64_t iters, double* out_flops, float* sink, void* stream) {
+    SS_CHECK_ARG(precision == 32 || precision == 64, "precision must be 32 or 64");
+    SS_CHECK_ARG(iters >= 1 && sink != nullptr, "iters >= 1 and a sink buffer of >= 256 floats required");
+    int dev = 0, sms = 0;
+    SS_CUDA_TRY(cudaGetDevice(&dev));
+    SS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    unsigned blocks = (unsigned)sms * 8u;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (precision == 32)
+        peak_fma_kernel<float><<<blocks, 256, 0, s>>>(iters, sink);
+    else
+        peak_fma_kernel<double><<<blocks, 256, 0, s>>>(iters, reinterpret_cast<double*>(sink));  // sink >= 512 floats
+    SS_LAUNCH_CHECK();
+    if (out_flops) *out_flops = 2.0 * 32.0 * (double)iters * 256.0 * (double)blocks;
+    return SS_OK;
+}
+
+}  // extern "C"

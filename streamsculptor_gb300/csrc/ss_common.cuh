@@ -1,0 +1,124 @@
+// ss_common.cuh — host-side helpers shared by the translation units:
+// error reporting, potential preparation (raw reference parameters ->
+// pre-combined device parameters), the Dormand-Prince tableau and the FP64
+// step used by the orbit / stream / release / response kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+
+#include <cmath>
+
+#include "ss_device.cuh"
+
+namespace ssg {
+
+// ------------------------------------------------------------- errors
+int set_error(int code, const char* fmt, ...);
+const char* last_error();
+
+#define SS_CHECK_ARG(cond, ...)                                          \
+    do {                                                                 \
+        if (!(cond)) return ::ssg::set_error(SS_ERR_INVALID_ARGUMENT, __VA_ARGS__); \
+    } while (0)
+
+#define SS_CUDA_TRY(expr)                                                              \
+    do {                                                                               \
+        cudaError_t _e = (expr);                                                       \
+        if (_e != cudaSuccess)                                                         \
+            return ::ssg::set_error(SS_ERR_CUDA, "%s: %s", #expr, cudaGetErrorString(_e)); \
+    } while (0)
+
+// Every kernel launch is followed by SS_LAUNCH_CHECK, which also counts it
+// (ss_kernel_launches).
+void count_launch();
+
+#define SS_LAUNCH_CHECK()                                                                    \
+    do {                                                                                     \
+        ::ssg::count_launch();                                                               \
+        cudaError_t _e = cudaGetLastError();                                                 \
+        if (_e != cudaSuccess)                                                               \
+            return ::ssg::set_error(SS_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(_e)); \
+    } while (0)
+
+// Raw parameters (reference units) -> PotDev<R>.  Validates kinds, counts,
+// positivity and the center track.  `allow_subhalos` = false rejects a
+// potential that carries a subhalo table.
+template <class R>
+int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalos);
+
+// ------------------------------------------------------ Dopri5 tableau
+// Dormand & Prince (1980) RK5(4)7M; 5th-order weights b (b2 = b7 = 0).
+#define SS_C2 (1.0 / 5.0)
+#define SS_C3 (3.0 / 10.0)
+#define SS_C4 (4.0 / 5.0)
+#define SS_C5 (8.0 / 9.0)
+#define SS_A21 (1.0 / 5.0)
+#define SS_A31 (3.0 / 40.0)
+#define SS_A32 (9.0 / 40.0)
+#define SS_A41 (44.0 / 45.0)
+#define SS_A42 (-56.0 / 15.0)
+#define SS_A43 (32.0 / 9.0)
+#define SS_A51 (19372.0 / 6561.0)
+#define SS_A52 (-25360.0 / 2187.0)
+#define SS_A53 (64448.0 / 6561.0)
+#define SS_A54 (-212.0 / 729.0)
+#define SS_A61 (9017.0 / 3168.0)
+#define SS_A62 (-355.0 / 33.0)
+#define SS_A63 (46732.0 / 5247.0)
+#define SS_A64 (49.0 / 176.0)
+#define SS_A65 (-5103.0 / 18656.0)
+#define SS_B1 (35.0 / 384.0)
+#define SS_B3 (500.0 / 1113.0)
+#define SS_B4 (125.0 / 192.0)
+#define SS_B5 (-2187.0 / 6784.0)
+#define SS_B6 (11.0 / 84.0)
+
+// FP64 acceleration of the full potential (components + track + subhalos)
+// at time t: velocity_acceleration, main.py:116-120.
+__device__ __forceinline__ void accel_f64(const PotDev<double>& P, const double x[3], double t, double a[3]) {
+    double c[3] = {0.0, 0.0, 0.0};
+    if (P.has_track) track_eval(P.track, t, c);
+    double g[3];
+    pot_grad<double, double, false>(P, x, c, g, nullptr);
+    if (P.sh.n > 0) subhalo_sum_grad<double>(P.sh, x, t, g);
+    a[0] = -g[0];
+    a[1] = -g[1];
+    a[2] = -g[2];
+}
+
+// One fixed Dopri5 step of the Hamiltonian flow (x, v) in FP64.
+__device__ __forceinline__ void dopri5_step_f64(const PotDev<double>& P, double t, double h, double y[6]) {
+    double k1[6], k2[6], k3[6], k4[6], k5[6], k6[6], ys[6];
+    // stage 1
+    k1[0] = y[3]; k1[1] = y[4]; k1[2] = y[5];
+    accel_f64(P, y, t, k1 + 3);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) ys[i] = y[i] + h * (SS_A21 * k1[i]);
+    k2[0] = ys[3]; k2[1] = ys[4]; k2[2] = ys[5];
+    accel_f64(P, ys, t + SS_C2 * h, k2 + 3);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) ys[i] = y[i] + h * (SS_A31 * k1[i] + SS_A32 * k2[i]);
+    k3[0] = ys[3]; k3[1] = ys[4]; k3[2] = ys[5];
+    accel_f64(P, ys, t + SS_C3 * h, k3 + 3);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) ys[i] = y[i] + h * (SS_A41 * k1[i] + SS_A42 * k2[i] + SS_A43 * k3[i]);
+    k4[0] = ys[3]; k4[1] = ys[4]; k4[2] = ys[5];
+    accel_f64(P, ys, t + SS_C4 * h, k4 + 3);
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        ys[i] = y[i] + h * (SS_A51 * k1[i] + SS_A52 * k2[i] + SS_A53 * k3[i] + SS_A54 * k4[i]);
+    k5[0] = ys[3]; k5[1] = ys[4]; k5[2] = ys[5];
+    accel_f64(P, ys, t + SS_C5 * h, k5 + 3);
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        ys[i] = y[i] + h * (SS_A61 * k1[i] + SS_A62 * k2[i] + SS_A63 * k3[i] + SS_A64 * k4[i] + SS_A65 * k5[i]);
+    k6[0] = ys[3]; k6[1] = ys[4]; k6[2] = ys[5];
+    accel_f64(P, ys, t + h, k6 + 3);
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        y[i] = y[i] + h * (SS_B1 * k1[i] + SS_B3 * k3[i] + SS_B4 * k4[i] + SS_B5 * k5[i] + SS_B6 * k6[i]);
+}
+
+}  // namespace ssg

@@ -1,0 +1,368 @@
+// ss_pert.cu — first-order response of stream tracks to many subhalos.
+//
+// Reference: MassRadiusPerturbation_OTF.term (fields.py:174-206) integrated
+// per particle by GenerateMassRadiusPerturbation.compute_perturbation_OTF
+// (perturbative.py:100-135).  The reference's state per particle is the
+// pytree [x0v0 (6), (N_sh, 12)]; every stage evaluates the base force, the
+// tidal tensor T = -Hessian(Phi_base)(x0) and, per subhalo s,
+//   d/dt (x1, v1)   = (v1,  -grad Phi_s(x0)        + T x1)
+//   d/dt (x1r, v1r) = (v1r, -grad dPhi_s/da_s(x0)  + T x1r)
+//
+// The base track does not depend on the subhalos, so it is computed once per
+// particle instead of once per (particle, subhalo):
+//   phase 1  one thread per particle integrates x0v0 in FP64 with the same
+//            Dopri5 steps and writes, for every step, the six stage
+//            positions x0 and tidal tensors T (a 56-value record) to the
+//            caller's workspace;
+//   phase 2  one thread per (particle, subhalo) system integrates the linear
+//            response with the identical tableau, reading the particle's
+//            records (all threads of a block share a particle, so the reads
+//            are broadcasts).
+// Integrating the coupled system and integrating the base first give the
+// same stage values: the base stages never read the response.
+// Particles are processed in chunks whose records fit the workspace.
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "ss_common.cuh"
+
+namespace ssg {
+
+static constexpr int REC = 56;  // 6 stages x (x0[3], T[6]) + 2 pad
+
+struct PertArgs {
+    int64_t N;       // particles in the whole run
+    int64_t p0;      // first particle of the chunk
+    int64_t np;      // particles in the chunk
+    int32_t ppr;
+    int32_t spr;
+    int32_t n_steps;
+    int32_t ncol;
+    int32_t save_stride;
+    int32_t n_saves;
+    double t0;
+    double dt;
+    const double* base_ics;
+    double* base_out;
+    const void* pert_ics;
+    void* pert_out;
+    void* table;
+};
+
+__host__ __device__ inline int64_t pert_start(int64_t p, int32_t ppr, int32_t spr) { return (p / ppr) * (int64_t)spr; }
+
+// Number of records (steps) of particles [0, p): sum of (n_steps - start_q).
+__host__ __device__ inline int64_t pert_offset(int64_t p, int32_t ppr, int32_t spr, int32_t n_steps) {
+    int64_t R = p / ppr;
+    int64_t floors = (int64_t)ppr * (R * (R - 1) / 2) + (p - R * ppr) * R;
+    return p * (int64_t)n_steps - (int64_t)spr * floors;
+}
+
+// ------------------------------------------------------------- phase 1
+template <class R>
+__global__ void __launch_bounds__(64) pert_base_kernel(PotDev<double> P, PertArgs a) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.np) return;
+    const int64_t p = a.p0 + i;
+    const int start = (int)pert_start(p, a.ppr, a.spr);
+    R* rec = reinterpret_cast<R*>(a.table) +
+             (pert_offset(p, a.ppr, a.spr, a.n_steps) - pert_offset(a.p0, a.ppr, a.spr, a.n_steps)) * REC;
+    double y[6];
+    for (int k = 0; k < 6; ++k) y[k] = a.base_ics[6 * p + k];
+    const double h = a.dt;
+    const double cs[6] = {0.0, SS_C2, SS_C3, SS_C4, SS_C5, 1.0};
+    for (int n = start; n < a.n_steps; ++n, rec += REC) {
+        const double t = a.t0 + (double)n * h;
+        double k[6][6];
+        double ys[6];
+#pragma unroll
+        for (int s = 0; s < 6; ++s) {
+            // stage state
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                double acc = 0.0;
+                if (s == 1) acc = SS_A21 * k[0][c];
+                if (s == 2) acc = SS_A31 * k[0][c] + SS_A32 * k[1][c];
+                if (s == 3) acc = SS_A41 * k[0][c] + SS_A42 * k[1][c] + SS_A43 * k[2][c];
+                if (s == 4) acc = SS_A51 * k[0][c] + SS_A52 * k[1][c] + SS_A53 * k[2][c] + SS_A54 * k[3][c];
+                if (s == 5)
+                    acc = SS_A61 * k[0][c] + SS_A62 * k[1][c] + SS_A63 * k[2][c] + SS_A64 * k[3][c] + SS_A65 * k[4][c];
+                ys[c] = s == 0 ? y[c] : y[c] + h * acc;
+            }
+            const double ts = t + cs[s] * h;
+            double cc[3] = {0.0, 0.0, 0.0};
+            if (P.has_track) track_eval(P.track, ts, cc);
+            double g[3], H[6];
+            pot_grad<double, double, true>(P, ys, cc, g, H);
+            k[s][0] = ys[3];
+            k[s][1] = ys[4];
+            k[s][2] = ys[5];
+            k[s][3] = -g[0];
+            k[s][4] = -g[1];
+            k[s][5] = -g[2];
+            R* r = rec + 9 * s;
+            r[0] = (R)ys[0];
+            r[1] = (R)ys[1];
+            r[2] = (R)ys[2];
+            // tidal tensor T = -H  (xx, yy, zz, xy, xz, yz)
+#pragma unroll
+            for (int c = 0; c < 6; ++c) r[3 + c] = (R)(-H[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < 6; ++c)
+            y[c] = y[c] + h * (SS_B1 * k[0][c] + SS_B3 * k[2][c] + SS_B4 * k[3][c] + SS_B5 * k[4][c] + SS_B6 * k[5][c]);
+    }
+    if (a.base_out)
+        for (int c = 0; c < 6; ++c) a.base_out[6 * p + c] = y[c];
+}
+
+// ------------------------------------------------------------- phase 2
+// derivative of one ncol-state at a stage: K = (v1, a1 + T x1 [, v1r, a1r + T x1r])
+template <class R, int NCOL>
+__device__ __forceinline__ void pert_rhs(const R* rec, const R U[NCOL], int kind, R Gm, R a, const R P0[3], const R V[3],
+                                         R trel, R tau0, R window, R K[NCOL]) {
+    R rel[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) rel[i] = rec[i] - (P0[i] + V[i] * trel);
+    R gphi[3], gdphi[3];
+    subhalo_grad<R, NCOL == 12>(kind, Gm, a, rel, gphi, gdphi);
+    // window: |t - t0_s| < t_window
+    R on = fabs(trel - tau0) < window ? R(1) : R(0);
+    const R* T = rec + 3;
+    // T: xx yy zz xy xz yz
+#pragma unroll
+    for (int b = 0; b < NCOL / 6; ++b) {
+        const R* x1 = U + 6 * b;
+        K[6 * b + 0] = U[6 * b + 3];
+        K[6 * b + 1] = U[6 * b + 4];
+        K[6 * b + 2] = U[6 * b + 5];
+        const R* gs = b == 0 ? gphi : gdphi;
+        K[6 * b + 3] = -on * gs[0] + (T[0] * x1[0] + T[3] * x1[1] + T[4] * x1[2]);
+        K[6 * b + 4] = -on * gs[1] + (T[3] * x1[0] + T[1] * x1[1] + T[5] * x1[2]);
+        K[6 * b + 5] = -on * gs[2] + (T[4] * x1[0] + T[5] * x1[1] + T[2] * x1[2]);
+    }
+}
+
+template <class R, int NCOL>
+__global__ void __launch_bounds__(128) pert_response_kernel(ShDev sh, PertArgs a, int sblocks) {
+    const int64_t i = blockIdx.x / sblocks;          // particle within the chunk
+    const int sb = blockIdx.x - (int)(i * sblocks);
+    const int s = sb * blockDim.x + threadIdx.x;     // subhalo
+    if (i >= a.np || s >= sh.n) return;
+    const int64_t p = a.p0 + i;
+    const int start = (int)pert_start(p, a.ppr, a.spr);
+    const R* rec = reinterpret_cast<const R*>(a.table) +
+                   (pert_offset(p, a.ppr, a.spr, a.n_steps) - pert_offset(a.p0, a.ppr, a.spr, a.n_steps)) * REC;
+    // subhalo line relative to the run start t0: P0 + V (t - t0)
+    const double tau = a.t0 - sh.t0[s];
+    const R P0[3] = {(R)(sh.x0[3 * s] + sh.v[3 * s] * tau), (R)(sh.x0[3 * s + 1] + sh.v[3 * s + 1] * tau),
+                     (R)(sh.x0[3 * s + 2] + sh.v[3 * s + 2] * tau)};
+    const R V[3] = {(R)sh.v[3 * s], (R)sh.v[3 * s + 1], (R)sh.v[3 * s + 2]};
+    const R Gm = (R)(sh.G * sh.m[s]);
+    const R am = (R)sh.a[s];
+    const R tau0 = (R)(sh.t0[s] - a.t0);
+    const R window = (R)sh.t_window;
+    const int64_t nsh = sh.n;
+
+    R u[NCOL];
+    const R* ic = reinterpret_cast<const R*>(a.pert_ics);
+#pragma unroll
+    for (int c = 0; c < NCOL; ++c) u[c] = ic ? ic[(p * nsh + s) * NCOL + c] : R(0);
+    R* out = reinterpret_cast<R*>(a.pert_out);
+    auto save = [&](int slot) {
+        R* o = out + (((int64_t)slot * a.N + p) * nsh + s) * NCOL;
+#pragma unroll
+        for (int c = 0; c < NCOL; ++c) o[c] = u[c];
+    };
+    if (a.save_stride > 0) {
+        for (int k = 0; k < a.n_saves && (int64_t)k * a.save_stride <= start; ++k) save(k);
+    }
+    const R h = (R)a.dt;
+    const R cs[6] = {R(0), R(SS_C2), R(SS_C3), R(SS_C4), R(SS_C5), R(1)};
+    for (int n = start; n < a.n_steps; ++n, rec += REC) {
+        const R tn = (R)n * h;
+        R k[6][NCOL];
+        R U[NCOL];
+#pragma unroll
+        for (int st = 0; st < 6; ++st) {
+#pragma unroll
+            for (int c = 0; c < NCOL; ++c) {
+                R acc = R(0);
+                if (st == 1) acc = R(SS_A21) * k[0][c];
+                if (st == 2) acc = R(SS_A31) * k[0][c] + R(SS_A32) * k[1][c];
+                if (st == 3) acc = R(SS_A41) * k[0][c] + R(SS_A42) * k[1][c] + R(SS_A43) * k[2][c];
+                if (st == 4) acc = R(SS_A51) * k[0][c] + R(SS_A52) * k[1][c] + R(SS_A53) * k[2][c] + R(SS_A54) * k[3][c];
+                if (st == 5)
+                    acc = R(SS_A61) * k[0][c] + R(SS_A62) * k[1][c] + R(SS_A63) * k[2][c] + R(SS_A64) * k[3][c] +
+                          R(SS_A65) * k[4][c];
+                U[c] = st == 0 ? u[c] : u[c] + h * acc;
+            }
+            pert_rhs<R, NCOL>(rec + 9 * st, U, sh.kind, Gm, am, P0, V, tn + cs[st] * h, tau0, window, k[st]);
+        }
+#pragma unroll
+        for (int c = 0; c < NCOL; ++c)
+            u[c] = u[c] + h * (R(SS_B1) * k[0][c] + R(SS_B3) * k[2][c] + R(SS_B4) * k[3][c] + R(SS_B5) * k[4][c] +
+                               R(SS_B6) * k[5][c]);
+        if (a.save_stride > 0 && (n + 1) % a.save_stride == 0) save((n + 1) / a.save_stride);
+    }
+    if (a.save_stride == 0) save(0);
+}
+
+// Per-subhalo potentials and derivatives at points (the perturbation
+// generator's jacfwd(potential_per_SH), perturbative.py:40-41).
+__global__ void subhalo_eval_kernel(ShDev sh, const double* __restrict__ xyz, int64_t n, double t, double* phi,
+                                    double* grad, double* dphi_da, double* grad_dphi_da) {
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n * sh.n) return;
+    int64_t i = idx / sh.n;
+    int s = (int)(idx % sh.n);
+    double tau = t - sh.t0[s];
+    bool on = fabs(tau) < sh.t_window;
+    double rel[3];
+    for (int k = 0; k < 3; ++k) rel[k] = xyz[3 * i + k] - (sh.x0[3 * s + k] + sh.v[3 * s + k] * tau);
+    double Gm = sh.G * sh.m[s], a = sh.a[s];
+    double r2 = rel[0] * rel[0] + rel[1] * rel[1] + rel[2] * rel[2];
+    double gphi[3], gd[3];
+    subhalo_grad<double, true>(sh.kind, Gm, a, rel, gphi, gd);
+    if (phi) phi[idx] = on ? (sh.kind == SS_SH_PLUMMER ? -Gm / sqrt(r2 + a * a) : -Gm / (sqrt(r2) + a)) : 0.0;
+    if (dphi_da) {
+        double v = sh.kind == SS_SH_PLUMMER ? Gm * a / ((r2 + a * a) * sqrt(r2 + a * a))
+                                            : Gm / ((sqrt(r2) + a) * (sqrt(r2) + a));
+        dphi_da[idx] = on ? v : 0.0;
+    }
+    for (int k = 0; k < 3; ++k) {
+        if (grad) grad[3 * idx + k] = on ? gphi[k] : 0.0;
+        if (grad_dphi_da) grad_dphi_da[3 * idx + k] = on ? gd[k] : 0.0;
+    }
+}
+
+static int prepare_subhalos(const ss_subhalos* in, double G, ShDev* out) {
+    SS_CHECK_ARG(in != nullptr, "subhalos is NULL");
+    SS_CHECK_ARG(in->n >= 1 && in->n <= (1 << 30), "subhalos: n must be in [1, 2^30]");
+    SS_CHECK_ARG(in->kind == SS_SH_PLUMMER || in->kind == SS_SH_HERNQUIST, "subhalos: unknown kind %d", in->kind);
+    SS_CHECK_ARG(in->m && in->a && in->x0 && in->v && in->t0, "subhalos: NULL table pointer");
+    SS_CHECK_ARG(!(in->t_window < 0.0), "subhalos: t_window < 0");
+    out->kind = in->kind;
+    out->n = (int32_t)in->n;
+    out->m = in->m;
+    out->a = in->a;
+    out->x0 = in->x0;
+    out->v = in->v;
+    out->t0 = in->t0;
+    out->t_window = in->t_window;
+    out->G = G;
+    return SS_OK;
+}
+
+}  // namespace ssg
+
+using namespace ssg;
+
+extern "C" {
+
+int ss_subhalo_eval(const ss_subhalos* sh, double G, const double* xyz, int64_t n, double t, double* phi,
+                    double* grad, double* dphi_da, double* grad_dphi_da, void* stream) {
+    ShDev S;
+    int rc = prepare_subhalos(sh, G, &S);
+    if (rc) return rc;
+    SS_CHECK_ARG(n >= 0, "n < 0");
+    if (n == 0) return SS_OK;
+    SS_CHECK_ARG(xyz != nullptr, "xyz is NULL");
+    int64_t total = n * S.n;
+    subhalo_eval_kernel<<<(unsigned)((total + 127) / 128), 128, 0, (cudaStream_t)stream>>>(S, xyz, n, t, phi, grad,
+                                                                                          dphi_da, grad_dphi_da);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
+int64_t ss_pert_workspace_bytes(const ss_pert_cfg* cfg, int precision, int64_t particles_per_chunk) {
+    if (!cfg || (precision != 32 && precision != 64) || particles_per_chunk < 1 || cfg->n_steps < 0)
+        return set_error(SS_ERR_INVALID_ARGUMENT, "bad arguments");
+    // the first particles are the longest: n_steps records each
+    return particles_per_chunk * cfg->n_steps * REC * (precision == 64 ? 8 : 4);
+}
+
+int ss_pert_response(const ss_potential* base, const ss_subhalos* sh, const ss_pert_cfg* cfg, int precision,
+                     const double* base_ics, const void* pert_ics, double* base_out, void* pert_out, void* workspace,
+                     int64_t workspace_bytes, void* stream) {
+    PotDev<double> P;
+    int rc = prepare_potential<double>(base, &P, false);
+    if (rc) return rc;
+    ShDev S;
+    rc = prepare_subhalos(sh, base->G, &S);
+    if (rc) return rc;
+    SS_CHECK_ARG(cfg != nullptr, "cfg is NULL");
+    SS_CHECK_ARG(precision == 32 || precision == 64, "precision must be 32 or 64");
+    SS_CHECK_ARG(cfg->ncol == 6 || cfg->ncol == 12, "ncol must be 6 or 12");
+    SS_CHECK_ARG(cfg->n_particles >= 0 && cfg->n_steps >= 0 && cfg->n_steps < (1LL << 30), "bad sizes");
+    SS_CHECK_ARG(cfg->particles_per_release >= 1 && cfg->steps_per_release >= 0, "bad release layout");
+    SS_CHECK_ARG(std::isfinite(cfg->dt) && cfg->dt != 0.0 && std::isfinite(cfg->t0), "dt must be finite, non-zero");
+    SS_CHECK_ARG(cfg->save_stride >= 0, "save_stride < 0");
+    if (cfg->n_particles == 0) return SS_OK;
+    SS_CHECK_ARG(base_ics && pert_out, "NULL buffer");
+    int64_t n_rel = (cfg->n_particles + cfg->particles_per_release - 1) / cfg->particles_per_release;
+    SS_CHECK_ARG((n_rel - 1) * (int64_t)cfg->steps_per_release <= cfg->n_steps, "last release starts after n_steps");
+    const int64_t esz = precision == 64 ? 8 : 4;
+    const int64_t rec_bytes = REC * esz;
+    const int64_t cap_records = workspace ? workspace_bytes / rec_bytes : 0;
+    if (cfg->n_steps > 0 && cap_records < cfg->n_steps)
+        return set_error(SS_ERR_WORKSPACE, "workspace of >= %lld bytes needed (one particle), %lld given",
+                         (long long)(cfg->n_steps * rec_bytes), (long long)workspace_bytes);
+    SS_CHECK_ARG(workspace == nullptr || ((uintptr_t)workspace % 16) == 0, "workspace must be 16-byte aligned");
+
+    PertArgs a;
+    memset(&a, 0, sizeof(a));
+    a.N = cfg->n_particles;
+    a.ppr = cfg->particles_per_release;
+    a.spr = cfg->steps_per_release;
+    a.n_steps = (int32_t)cfg->n_steps;
+    a.ncol = cfg->ncol;
+    a.save_stride = cfg->save_stride;
+    a.n_saves = cfg->save_stride > 0 ? (int32_t)(cfg->n_steps / cfg->save_stride + 1) : 1;
+    a.t0 = cfg->t0;
+    a.dt = cfg->dt;
+    a.base_ics = base_ics;
+    a.base_out = base_out;
+    a.pert_ics = pert_ics;
+    a.pert_out = pert_out;
+    a.table = workspace;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int sblock = 128;
+    const int sblocks = (int)((S.n + sblock - 1) / sblock);
+    int64_t p0 = 0;
+    while (p0 < a.N) {
+        // largest chunk [p0, p1) whose records fit the workspace
+        int64_t lo = p0 + 1, hi = a.N;
+        const int64_t base_off = pert_offset(p0, a.ppr, a.spr, a.n_steps);
+        while (lo < hi) {
+            int64_t mid = (lo + hi + 1) / 2;
+            if (pert_offset(mid, a.ppr, a.spr, a.n_steps) - base_off <= cap_records) lo = mid; else hi = mid - 1;
+        }
+        int64_t p1 = lo;
+        // keep the grid within limits
+        const int64_t max_np = ((1LL << 31) - 1) / sblocks;
+        if (p1 - p0 > max_np) p1 = p0 + max_np;
+        a.p0 = p0;
+        a.np = p1 - p0;
+        unsigned g1 = (unsigned)((a.np + 63) / 64);
+        unsigned g2 = (unsigned)(a.np * sblocks);
+        if (precision == 64) {
+            pert_base_kernel<double><<<g1, 64, 0, st>>>(P, a);
+            SS_LAUNCH_CHECK();
+            if (a.ncol == 12) pert_response_kernel<double, 12><<<g2, sblock, 0, st>>>(S, a, sblocks);
+            else pert_response_kernel<double, 6><<<g2, sblock, 0, st>>>(S, a, sblocks);
+        } else {
+            pert_base_kernel<float><<<g1, 64, 0, st>>>(P, a);
+            SS_LAUNCH_CHECK();
+            if (a.ncol == 12) pert_response_kernel<float, 12><<<g2, sblock, 0, st>>>(S, a, sblocks);
+            else pert_response_kernel<float, 6><<<g2, sblock, 0, st>>>(S, a, sblocks);
+        }
+        SS_LAUNCH_CHECK();
+        p0 = p1;
+    }
+    return SS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,143 @@
+"""Perturbation generators — the reference's perturbative.py API.
+
+BaseStreamModel (perturbative.py:243-296) holds the zeroth-order stream:
+release ICs, the forward progenitor orbit and the release Jacobians
+d(release)/d(progenitor w) (computed by forward-mode dual numbers on the GPU,
+including the third derivatives of Phi that r_t needs).
+GenerateMassRadiusPerturbation (perturbative.py:24-135) integrates the
+progenitor's response backwards from the observation time, maps it through
+the release Jacobians to per-particle initial responses and integrates every
+(particle, subhalo) response forward with ss_pert_response.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _abi, _core
+from ._core import f64, host64
+from .main import Potential, _grid_spacing, release_normals
+
+
+class BaseStreamModel(Potential):
+    def __init__(self, potential_base, prog_w0, ts, Msat, seednum, solver=None, units=None, dense=False, cpu=True,
+                 *, dt=None, normals=None, **kwargs):
+        super().__init__(units, {"potential_base": potential_base, "prog_w0": prog_w0, "ts": ts, "Msat": Msat,
+                                 "seednum": seednum, "solver": solver, "dense": dense, "cpu": cpu})
+        if dense:
+            raise NotImplementedError("dense stream interpolants are replaced by snapshots")
+        _core.check_solver(solver)
+        self.potential_base = potential_base
+        ts_h = host64(ts).reshape(-1)
+        self._ts_h = ts_h
+        self._dt = dt
+        self.normals = normals if normals is not None else release_normals(seednum, len(ts_h), 1, 4)
+        ws, self._h, self._spr = potential_base._prog_orbit(ts_h, prog_w0, dt)
+        self.prog_loc_fwd = ws  # [len(ts), 6]
+        ics, J = potential_base._release(ws, ts_h, Msat, self.normals, jac=True)
+        ics = ics[:, 0]
+        self.streamICs = (ics[:, 0, :3], ics[:, 1, :3], ics[:, 0, 3:], ics[:, 1, 3:])
+        self.IDs = torch.arange(len(ts_h), device=ws.device)
+        self.dRel_dIC = J[:, 0]  # [len(ts), 2, 6, 6]
+        self.stream_interp = None
+
+    def release_func_jacobian(self):
+        """[len(ts), 2, 6, 6]: d(lead/trail ICs)/d(progenitor w) (perturbative.py:280-296)."""
+        return self.dRel_dIC
+
+
+class GenerateMassRadiusPerturbation(Potential):
+    """First-order response in subhalo mass and scale radius (perturbative.py:24-135)."""
+
+    _ncol = 12
+
+    def __init__(self, potential_base, potential_perturbation, potential_structural=None, BaseStreamModel=None,
+                 units=None, *, precision=64, **kwargs):
+        super().__init__(units, {"potential_base": potential_base, "potential_perturbation": potential_perturbation,
+                                 "potential_structural": potential_structural, "BaseStreamModel": BaseStreamModel})
+        self.potential_base = potential_base
+        self.gradientPotentialBase = potential_base.gradient
+        self.gradientPotentialPerturbation_per_SH = potential_perturbation.gradient_per_SH
+        self.sh_table = potential_perturbation.table()
+        if potential_structural is not None:
+            self.gradientPotentialStructural_per_SH = potential_structural.gradient_per_SH
+            if not self.sh_table.same_lines(potential_structural.table()):
+                raise NotImplementedError("perturbation and structural potentials must share one subhalo table")
+        self.precision = int(precision)
+        if BaseStreamModel is not None:
+            bsm = BaseStreamModel
+            self.base_stream = bsm
+            self.num_pert = int(self.sh_table.m.shape[0])
+            self.jump_ts = None
+            ts_h = bsm._ts_h
+            n = len(ts_h)
+            # backward progenitor response from the observation time, zero at t_obs
+            cfg = _abi.ss_pert_cfg()
+            cfg.t0, cfg.dt = float(ts_h[-1]), -float(bsm._h)
+            cfg.n_steps, cfg.n_particles = bsm._spr * (n - 1), 1
+            cfg.particles_per_release, cfg.steps_per_release = 1, 0
+            cfg.ncol, cfg.save_stride = self._ncol, bsm._spr
+            w_obs = bsm.prog_loc_fwd[-1:].contiguous()
+            _, out = _core.pert_response(potential_base._desc(), self.sh_table, cfg, 64, w_obs, None)
+            self.prog_fieldICs = torch.flip(out[:, 0], dims=[0])  # [len(ts), N_sh, ncol], time increasing
+            self.perturbation_ICs_lead, self.perturbation_ICs_trail = self.compute_perturbation_ICs()
+            self.base_realspace_ICs_lead = torch.cat([bsm.streamICs[0], bsm.streamICs[2]], dim=1)
+            self.base_realspace_ICs_trail = torch.cat([bsm.streamICs[1], bsm.streamICs[3]], dim=1)
+
+    def potential(self, xyz, t):
+        raise NotImplementedError
+
+    def compute_perturbation_ICs(self):
+        """einsum of release Jacobians with the progenitor response (perturbative.py:84-98)."""
+        J = self.base_stream.dRel_dIC
+        pf = self.prog_fieldICs
+        out = []
+        for arm in (0, 1):
+            parts = [torch.einsum("ijk,ilk->ilj", J[:, arm], pf[:, :, 6 * b:6 * b + 6])
+                     for b in range(self._ncol // 6)]
+            out.append(torch.cat(parts, dim=2))
+        return out[0], out[1]
+
+    def compute_base_stream(self, cpu=True):
+        """perturbative.py:67-81"""
+        b = self.base_stream
+        return self.potential_base.gen_stream_vmapped(ts=b._ts_h, prog_w0=b.prog_w0, Msat=b.Msat,
+                                                      seed_num=b.seednum, dt=b._dt, normals=b.normals)
+
+    def compute_perturbation_OTF(self, cpu=True, solver=None, rtol=1e-6, atol=1e-6, dtmin=0.05, dtmax=None,
+                                 max_steps=10_000, *, precision=None):
+        """Per-particle response from release to the observation time
+        (perturbative.py:100-135).  Returns (lead, trail), each
+        [x0v0 [len(ts)-1, 6], derivs [len(ts)-1, N_sh, ncol]]."""
+        _core.check_solver(solver)
+        prec = int(precision or self.precision)
+        b = self.base_stream
+        n = len(b._ts_h)
+        nrel = n - 1
+        base = torch.stack([self.base_realspace_ICs_lead[:nrel], self.base_realspace_ICs_trail[:nrel]], dim=1)
+        pert = torch.stack([self.perturbation_ICs_lead[:nrel], self.perturbation_ICs_trail[:nrel]], dim=1)
+        cfg = _abi.ss_pert_cfg()
+        cfg.t0, cfg.dt = float(b._ts_h[0]), float(b._h)
+        cfg.n_steps, cfg.n_particles = b._spr * nrel, 2 * nrel
+        cfg.particles_per_release, cfg.steps_per_release = 2, b._spr
+        cfg.ncol, cfg.save_stride = self._ncol, 0
+        base_out, out = _core.pert_response(self.potential_base._desc(), self.sh_table, cfg, prec,
+                                            base.reshape(2 * nrel, 6).contiguous(),
+                                            pert.reshape(2 * nrel, self.num_pert, self._ncol).contiguous())
+        base_out = base_out.reshape(nrel, 2, 6)
+        d = out[0].reshape(nrel, 2, self.num_pert, self._ncol)
+        return [base_out[:, 0], d[:, 0]], [base_out[:, 1], d[:, 1]]
+
+
+class GenerateMassPerturbation(GenerateMassRadiusPerturbation):
+    """Mass-only response (6 columns per subhalo) at fixed subhalo radius
+    (perturbative.py:224-241; the reference's constructor references an
+    undefined name and cannot be built, this one works)."""
+
+    _ncol = 6
+
+    def __init__(self, potential_base, potential_perturbation, BaseStreamModel=None, units=None, **kw):
+        super().__init__(potential_base, potential_perturbation, None, BaseStreamModel, units, **kw)
+
+
+__all__ = ["BaseStreamModel", "GenerateMassRadiusPerturbation", "GenerateMassPerturbation"]

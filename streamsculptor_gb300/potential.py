@@ -1,0 +1,245 @@
+"""Potential classes — the reference's potential.py names and keyword arguments.
+
+Each class flattens into components of the device descriptor
+(ss_potential).  Supported on the GPU path (jnibauer/streamsculptor
+potential.py): MiyamotoNagaiDisk (66-72), NFWPotential (74-84),
+TriaxialNFWPotential (86-97), Isochrone (114-122), PlummerPotential
+(124-130), HernquistPotential (132-138), ProgenitorPotential (140-153),
+GalaMilkyWayPotential (390-418), TimeDepTranslatingPotential (448-462),
+SubhaloLinePotential (802-850), SubhaloLinePotential_dRadius (852-904),
+SubhaloLinePotential_Custom (908-956) with a Plummer or Hernquist profile,
+Potential_Combine (1279-1296).  CustomPotential (787-797) holds an arbitrary
+Python callable and cannot run in a CUDA kernel: using it raises.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _abi, _core
+from ._core import CenterTrack, Flat, SubhaloTable, f64, host64, usys  # noqa: F401
+from .main import Potential
+
+
+def _f(x) -> float:
+    return float(host64(x))
+
+
+class MiyamotoNagaiDisk(Potential):
+    def __init__(self, m, a, b, units=None):
+        super().__init__(units, {"m": m, "a": a, "b": b})
+
+    def _flatten(self):
+        return Flat([(_abi.SS_MIYAMOTO_NAGAI, _abi.SS_CENTER_ORIGIN, (_f(self.m), _f(self.a), _f(self.b)))])
+
+
+class NFWPotential(Potential):
+    """Phi = -G m log(1 + r/r_s) / r (unsoftened, potential.py:80-84)."""
+
+    def __init__(self, m, r_s, units=None, _soft=0.0):
+        super().__init__(units, {"m": m, "r_s": r_s})
+        self._soft = float(_soft)
+
+    def _flatten(self):
+        return Flat([(_abi.SS_NFW, _abi.SS_CENTER_ORIGIN, (_f(self.m), _f(self.r_s), self._soft))])
+
+
+class TriaxialNFWPotential(Potential):
+    """Flattening in the potential: NFW of (x/q1, y/q2, z/q3)."""
+
+    def __init__(self, m, r_s, q1=1.0, q2=1.0, q3=1.0, units=None):
+        super().__init__(units, {"m": m, "r_s": r_s, "q1": q1, "q2": q2, "q3": q3})
+
+    def _flatten(self):
+        return Flat([(_abi.SS_TRIAXIAL_NFW, _abi.SS_CENTER_ORIGIN,
+                      (_f(self.m), _f(self.r_s), _f(self.q1), _f(self.q2), _f(self.q3)))])
+
+
+class Isochrone(Potential):
+    def __init__(self, m, a, units=None):
+        super().__init__(units, {"m": m, "a": a})
+
+    def _flatten(self):
+        return Flat([(_abi.SS_ISOCHRONE, _abi.SS_CENTER_ORIGIN, (_f(self.m), _f(self.a)))])
+
+
+class PlummerPotential(Potential):
+    def __init__(self, m, r_s, units=None):
+        super().__init__(units, {"m": m, "r_s": r_s})
+
+    def _flatten(self):
+        return Flat([(_abi.SS_PLUMMER, _abi.SS_CENTER_ORIGIN, (_f(self.m), _f(self.r_s)))])
+
+
+class HernquistPotential(Potential):
+    def __init__(self, m, r_s, soft=0.0, units=None):
+        super().__init__(units, {"m": m, "r_s": r_s, "soft": soft})
+
+    def _flatten(self):
+        return Flat([(_abi.SS_HERNQUIST, _abi.SS_CENTER_ORIGIN, (_f(self.m), _f(self.r_s), _f(self.soft)))])
+
+
+class Potential_Combine(Potential):
+    """Sum of potentials in list order (potential.py:1279-1296)."""
+
+    def __init__(self, potential_list, units=None):
+        super().__init__(units, {"potential_list": list(potential_list)})
+
+    def _flatten(self):
+        flat = Flat()
+        for p in self.potential_list:
+            flat.extend(p._flatten())
+        return flat
+
+
+class TimeDepTranslatingPotential(Potential):
+    """pot evaluated at x - center(t) (potential.py:448-462).
+
+    center_spl must be a CenterTrack (uniform knots; Hermite cubic with
+    interpax-'cubic' slopes), e.g. CenterTrack.from_samples(ts, orbit[:, :3])."""
+
+    def __init__(self, pot, center_spl, units=None):
+        super().__init__(units, {"pot": pot, "center_spl": center_spl})
+
+    def _flatten(self):
+        if not isinstance(self.center_spl, CenterTrack):
+            raise NotImplementedError("center_spl must be a CenterTrack (arbitrary callables cannot run on the GPU)")
+        inner = self.pot._flatten()
+        if inner.track is not None or inner.subhalos is not None:
+            raise NotImplementedError("nested translating potentials / subhalos inside a translating potential")
+        comps = [(k, _abi.SS_CENTER_TRACK, p) for (k, _, p) in inner.comps]
+        return Flat(comps, track=self.center_spl)
+
+
+class ProgenitorPotential(Potential):
+    """prog_pot(m, r_s) centred on the progenitor track (potential.py:140-153)."""
+
+    def __init__(self, m, r_s, interp_func, prog_pot, units=None):
+        super().__init__(units, {"m": m, "r_s": r_s, "interp_func": interp_func})
+        self.prog_pot = prog_pot(m=m, r_s=r_s, units=units)
+
+    def _flatten(self):
+        return TimeDepTranslatingPotential(self.prog_pot, self.interp_func, units=self.units)._flatten()
+
+
+class GalaMilkyWayPotential(Potential):
+    """Disk + bulge + nucleus + halo (potential.py:390-418), summed in that order."""
+
+    def __init__(self, units=None):
+        super().__init__(units, {"params": None})
+        self.m_disk, self.a_disk, self.b_disk = 6.80e10, 3.0, 0.28
+        self.m_bulge, self.c_bulge = 5e9, 1.0
+        self.m_nucleus, self.c_nucleus = 1.71e9, 0.07
+        self.m_halo, self.r_s_halo = 5.4e11, 15.62
+        self.pot = Potential_Combine([
+            MiyamotoNagaiDisk(m=self.m_disk, a=self.a_disk, b=self.b_disk, units=self.units),
+            HernquistPotential(m=self.m_bulge, r_s=self.c_bulge, units=self.units),
+            HernquistPotential(m=self.m_nucleus, r_s=self.c_nucleus, units=self.units),
+            NFWPotential(m=self.m_halo, r_s=self.r_s_halo, units=self.units),
+        ], units=self.units)
+
+    def _flatten(self):
+        return self.pot._flatten()
+
+
+class _SubhaloLines(Potential):
+    _kind = _abi.SS_SH_PLUMMER
+
+    def _table(self) -> SubhaloTable:
+        dev = _core.device()
+        x0 = f64(self.subhalo_x0, dev).reshape(-1, 3)
+        n = x0.shape[0]
+        m = f64(np.broadcast_to(host64(self.m), (n,)).copy(), dev)
+        a = f64(np.broadcast_to(host64(self.a), (n,)).copy(), dev)
+        v = f64(self.subhalo_v, dev).reshape(n, 3)
+        t0 = f64(np.broadcast_to(host64(self.subhalo_t0), (n,)).copy(), dev)
+        return SubhaloTable(self._kind, m, a, x0, v, t0, _f(self.t_window))
+
+    def table(self) -> SubhaloTable:
+        key = ("table", _core.device().index)
+        t = self._desc_cache.get(key)
+        if t is None:
+            t = self._table()
+            self._desc_cache[key] = t
+        return t
+
+    def _flatten(self):
+        return Flat([], subhalos=self.table())
+
+    def _per_sh(self, xyz, t):
+        pts = f64(xyz)
+        single = pts.ndim == 1
+        pts = pts.reshape(-1, 3).contiguous()
+        o = _core.subhalo_eval(self.table(), self._G, pts, float(host64(t)))
+        return o, single
+
+    def potential_per_SH(self, xyz, t):
+        """Phi_s(x, t) per subhalo, zero outside the window (potential.py:832-850)."""
+        (phi, _, _, _), single = self._per_sh(xyz, t)
+        return phi[0] if single else phi
+
+    def gradient_per_SH(self, xyz, t):
+        """jacfwd(potential_per_SH) (perturbative.py:40): [N_sh, 3]."""
+        (_, g, _, _), single = self._per_sh(xyz, t)
+        return g[0] if single else g
+
+
+class SubhaloLinePotential(_SubhaloLines):
+    """Plummer subhalos on lines x0 + v (t - t0), active while |t - t0| < t_window."""
+
+    def __init__(self, m, a, subhalo_x0, subhalo_v, subhalo_t0, t_window, units=None):
+        super().__init__(units, {"m": m, "a": a, "subhalo_x0": subhalo_x0, "subhalo_v": subhalo_v,
+                                 "subhalo_t0": subhalo_t0, "t_window": t_window})
+
+
+class SubhaloLinePotential_dRadius(_SubhaloLines):
+    """dPhi_s/da_s of the Plummer subhalos (potential.py:852-904).
+
+    It is the structural companion used by the perturbation generator; as a
+    force potential of its own it is not part of any stream integration."""
+
+    def __init__(self, m, a, subhalo_x0, subhalo_v, subhalo_t0, t_window, units=None):
+        super().__init__(units, {"m": m, "a": a, "subhalo_x0": subhalo_x0, "subhalo_v": subhalo_v,
+                                 "subhalo_t0": subhalo_t0, "t_window": t_window})
+
+    def _flatten(self):
+        raise NotImplementedError("SubhaloLinePotential_dRadius is a structural derivative, not a force potential")
+
+    def potential_per_SH(self, xyz, t):
+        (_, _, d, _), single = self._per_sh(xyz, t)
+        return d[0] if single else d
+
+    def gradient_per_SH(self, xyz, t):
+        (_, _, _, gd), single = self._per_sh(xyz, t)
+        return gd[0] if single else gd
+
+
+class SubhaloLinePotential_Custom(_SubhaloLines):
+    """One profile `pot` (PlummerPotential or HernquistPotential) for all
+    subhalos on lines (potential.py:908-956)."""
+
+    def __init__(self, pot, subhalo_x0, subhalo_v, subhalo_t0, t_window, units=None):
+        if isinstance(pot, PlummerPotential):
+            kind, m, a = _abi.SS_SH_PLUMMER, pot.m, pot.r_s
+        elif isinstance(pot, HernquistPotential):
+            if _f(pot.soft) != 0.0:
+                raise NotImplementedError("softened Hernquist subhalos")
+            kind, m, a = _abi.SS_SH_HERNQUIST, pot.m, pot.r_s
+        else:
+            raise NotImplementedError("SubhaloLinePotential_Custom supports Plummer and Hernquist profiles")
+        super().__init__(units, {"pot": pot, "m": m, "a": a, "subhalo_x0": subhalo_x0, "subhalo_v": subhalo_v,
+                                 "subhalo_t0": subhalo_t0, "t_window": t_window})
+        self._kind = kind
+
+
+class CustomPotential(Potential):
+    """Arbitrary Python potential_func(xyz, t): no GPU implementation."""
+
+    def __init__(self, potential_func=None, units=None):
+        super().__init__(units, {"potential_func": potential_func})
+
+
+__all__ = ["MiyamotoNagaiDisk", "NFWPotential", "TriaxialNFWPotential", "Isochrone", "PlummerPotential",
+           "HernquistPotential", "Potential_Combine", "TimeDepTranslatingPotential", "ProgenitorPotential",
+           "GalaMilkyWayPotential", "SubhaloLinePotential", "SubhaloLinePotential_dRadius",
+           "SubhaloLinePotential_Custom", "CustomPotential", "CenterTrack", "usys"]

@@ -1,0 +1,58 @@
+"""Algorithmic work per particle-step, counted from the kernel source.
+
+Convention: add / sub / mul = 1 flop, fma = 2 flops; sqrt, rsqrt,
+reciprocal / division and log1p are counted separately as "special" ops
+(they expand to several pipe instructions, so flop rates computed from the
+algorithmic count understate pipe utilisation; ncu gives the latter).
+
+Force evaluation (ss_device.cuh, comp_grad without Hessian), per component:
+  NFW          r^2 (5) + soft (1) + r*q (1) + (r+rs) (1) + 1/r^2 (1)
+               + g = q0/r^2 (L/r - 1/(r+rs)) (4) + grad += g x (6)  = 19; specials 4
+  TriaxialNFW  x/q (3) + NFW radial part (13) + grad (6) + 3 scale (3) = 25; specials 4
+  MiyamotoNagai zeta (2) + a+zeta (1) + S^2 (5) + 1/S^3 (3) + fz (1) + grad (7) = 19; specials 3
+  Hernquist    r^2 (5) + soft (1) + r+rs (1) + g (3) + grad (6)      = 16; specials 3
+  Plummer      r^2 (5) + b^2 (1) + g (3) + grad (6)                    = 15; specials 1
+  Isochrone    r^2 (5) + a^2 (1) + a+s (1) + g (3) + grad (6)          = 16; specials 3
+  translating  + 3 (x - c(t))
+  subhalo line + 9 (line position) + 15 (Plummer form) + 1 window test
+Dopri5 combinations per step (6 force evaluations, FSAL reuse):
+  FP64 plain          6 components x (stages 35 + update 11)            = 276
+  FP32 compensated    3 x (stages 84 + position update 27 + velocity 28) = 417
+"""
+from __future__ import annotations
+
+from . import _abi
+
+FORCE_FLOPS = {
+    _abi.SS_NFW: (19, 4),
+    _abi.SS_TRIAXIAL_NFW: (25, 4),
+    _abi.SS_MIYAMOTO_NAGAI: (19, 3),
+    _abi.SS_HERNQUIST: (16, 3),
+    _abi.SS_PLUMMER: (15, 1),
+    _abi.SS_ISOCHRONE: (16, 3),
+}
+TRANSLATE_FLOPS = 3
+SUBHALO_FLOPS = (25, 1)
+RK_FLOPS = {"f64": 276, "f32k": 417}
+STAGES = 6
+
+
+def force_work(flat) -> tuple:
+    """(flops, specials) of one force evaluation of a flattened potential."""
+    fl, sp = 0, 0
+    for kind, center, _ in flat.comps:
+        f, s = FORCE_FLOPS[kind]
+        fl += f + (TRANSLATE_FLOPS if center == _abi.SS_CENTER_TRACK else 0)
+        sp += s
+    if flat.subhalos is not None:
+        n = int(flat.subhalos.m.shape[0])
+        fl += n * SUBHALO_FLOPS[0]
+        sp += n * SUBHALO_FLOPS[1]
+    return fl, sp
+
+
+def particle_step_work(flat, precision: str) -> dict:
+    """Flops and special ops of one Dopri5 step of one particle."""
+    fl, sp = force_work(flat)
+    return {"flops": STAGES * fl + RK_FLOPS[precision], "specials": STAGES * sp,
+            "force_flops": fl, "force_specials": sp, "rk_flops": RK_FLOPS[precision]}

@@ -1,0 +1,214 @@
+"""Stream generators and helpers — the reference's streamhelpers.py API.
+
+`gen_stream` is the one engine behind every generator here and behind
+Potential.gen_stream_vmapped: FP64 progenitor orbit (ss_orbit_f64), release
+(ss_release_f64), optional moving-progenitor potential on a cubic track, then
+the stream kernel (ss_stream_f64 or ss_stream_f32k).
+"""
+from __future__ import annotations
+
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _abi, _core
+from ._core import CenterTrack, f64, host64
+from .main import Potential, _grid_spacing, _n_draw, _split_ics, release_normals
+from . import potential as _pot
+
+# release_model_Chen25 mean and covariance (streamhelpers.py:360-369)
+CHEN25_MEAN = np.array([1.6, -30.0, 0.0, 1.0, 20.0, 0.0])
+CHEN25_COV = np.array([
+    [0.1225, 0, 0, 0, -4.9, 0],
+    [0, 529, 0, 0, 0, 0],
+    [0, 0, 144, 0, 0, 0],
+    [0, 0, 0, 0, 0, 0],
+    [-4.9, 0, 0, 0, 400, 0],
+    [0, 0, 0, 0, 0, 484],
+], dtype=np.float64)
+
+
+def chen25_factor(cov=CHEN25_COV) -> np.ndarray:
+    """L with L L^T = cov, from the SVD (jax multivariate_normal method='svd')."""
+    u, s, _ = np.linalg.svd(cov)
+    return u * np.sqrt(s)[None, :]
+
+
+def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=None, *, solver=None,
+               kval_arr=1.0, dt=None, dtmax=None, n_particles_per_release=2, normals=None, precision="f64",
+               snapshot_every=None, throw=False, release="fardal", prog_pot: Optional[Potential] = None,
+               pot_pert: Optional[Potential] = None, prog_in_pert=False, return_ics=False):
+    """Generate a particle-spray stream on the GPU.
+
+    pot_base    smooth potential (release model and integration)
+    prog_pot    optional progenitor potential moving on the progenitor's
+                orbit (TimeDepTranslatingPotential on its cubic track,
+                streamhelpers.py:520-522)
+    pot_pert    optional perturbation (subhalos) added for integration
+                (streamhelpers.py:89-146); with prog_in_pert the progenitor
+                orbit is integrated in base + pert too (gen_stream_ics_pert)
+    release     'fardal' (main.py:209-280) or 'chen25' (streamhelpers.py:352-432)
+    Returns (lead, trail) [len(ts)-1, 6] (or [len(ts)-1, n_draw, 6]); with
+    snapshot_every also the float32 snapshots [n_snap, len(ts)-1, n_draw, 2, 6].
+    """
+    _core.check_solver(solver)
+    ts_h = host64(ts).reshape(-1)
+    if len(ts_h) < 2:
+        raise ValueError("need at least two release times")
+    total = pot_base if pot_pert is None else _pot.Potential_Combine([pot_base, pot_pert], units=pot_base.units)
+    prog_src = total if (pot_pert is not None and prog_in_pert) else pot_base
+    ws, h, spr = prog_src._prog_orbit(ts_h, prog_w0, dt, None, dtmax)
+    n_draw = _n_draw(n_particles_per_release)
+    model = _abi.SS_RELEASE_CHEN25 if release == "chen25" else _abi.SS_RELEASE_FARDAL
+    if release not in ("fardal", "chen25"):
+        raise ValueError("release must be 'fardal' or 'chen25'")
+    nz = 6 if model == _abi.SS_RELEASE_CHEN25 else 4
+    if normals is None:
+        normals = release_normals(seed_num, len(ts_h), n_draw, nz)
+    chen = (CHEN25_MEAN, chen25_factor()) if model == _abi.SS_RELEASE_CHEN25 else None
+    ics, _ = pot_base._release(ws, ts_h, Msat, normals, kval_arr, model=model, chen=chen)
+    integ = total
+    if prog_pot is not None:
+        track = CenterTrack.from_samples(ts_h, ws[:, :3])
+        moving = _pot.TimeDepTranslatingPotential(prog_pot, track, units=pot_base.units)
+        integ = _pot.Potential_Combine([total, moving], units=pot_base.units)
+    n_rel = len(ts_h) - 1
+    ppr = 2 * n_draw
+    N = n_rel * ppr
+    cfg = _abi.ss_stream_cfg()
+    cfg.t0 = float(ts_h[0])
+    cfg.dt = float(h)
+    cfg.n_steps = spr * n_rel
+    cfg.n_particles = N
+    cfg.particles_per_release = ppr
+    cfg.steps_per_release = spr
+    cfg.snap_stride = int(snapshot_every or 0)
+    snaps = None
+    if snapshot_every:
+        n_snap = cfg.n_steps // int(snapshot_every)
+        snaps = torch.empty(n_snap, N, 6, dtype=torch.float32, device=ws.device)
+    stream_ics = ics[:n_rel].reshape(N, 6).contiguous()
+    final, status = _core.stream(integ._desc(), cfg, stream_ics, precision, snaps=snaps)
+    if throw and bool((status != 0).any()):
+        raise RuntimeError("gen_stream: non-finite particle state")
+    final = final.reshape(n_rel, n_draw, 2, 6)
+    if n_draw == 1:
+        lead, trail = final[:, 0, 0], final[:, 0, 1]
+    else:
+        lead, trail = final[:, :, 0], final[:, :, 1]
+    out = (lead, trail)
+    if snapshot_every:
+        out = out + (snaps.reshape(-1, n_rel, n_draw, 2, 6),)
+    if return_ics:
+        out = out + (ics, ws)
+    return out
+
+
+# ----------------------------------------------------- reference names
+def eval_dense_stream(t_eval=None, dense_stream=None):
+    raise NotImplementedError("dense streams are replaced by snapshots (gen_stream_vmapped(..., snapshot_every=k))")
+
+
+def eval_dense_stream_id(time=None, interp_func=None, idx=None, lead=True):
+    raise NotImplementedError("dense streams are replaced by snapshots (gen_stream_vmapped(..., snapshot_every=k))")
+
+
+def gen_stream_ics_pert(pot_base=None, pot_pert=None, ts=None, prog_w0=None, Msat=None, seed_num=None, solver=None,
+                        kval_arr=1.0, max_steps=10_000, rtol=1e-7, atol=1e-7, dtmin=0.1, *, dt=None,
+                        n_particles_per_release=2, normals=None):
+    """Release in the smooth potential from a progenitor orbit integrated in
+    base + perturbation (streamhelpers.py:56-84)."""
+    ts_h = host64(ts).reshape(-1)
+    total = _pot.Potential_Combine([pot_base, pot_pert], units=pot_base.units)
+    ws, _, _ = total._prog_orbit(ts_h, prog_w0, dt)
+    n_draw = _n_draw(n_particles_per_release)
+    if normals is None:
+        normals = release_normals(seed_num, len(ts_h), n_draw, 4)
+    ics, _ = pot_base._release(ws, ts_h, Msat, normals, kval_arr)
+    return _split_ics(ics, n_draw)
+
+
+def gen_stream_vmapped_with_pert(pot_base=None, pot_pert=None, ts=None, prog_w0=None, Msat=None, seed_num=None,
+                                 solver=None, kval_arr=1.0, max_steps=10_000, rtol=1e-7, atol=1e-7, dtmin=0.1, *,
+                                 dt=None, precision="f64", **kw):
+    """Perturbed stream, progenitor in base + pert (streamhelpers.py:89-116)."""
+    return gen_stream(pot_base, ts, prog_w0, Msat, seed_num, solver=solver, kval_arr=kval_arr, dt=dt,
+                      pot_pert=pot_pert, prog_in_pert=True, precision=precision, **kw)
+
+
+def gen_stream_vmapped_with_pert_fixed_prog(pot_base=None, pot_pert=None, ts=None, prog_w0=None, Msat=None,
+                                            seed_num=None, solver=None, kval_arr=1.0, max_steps=10_000, rtol=1e-7,
+                                            atol=1e-7, dtmin=0.1, *, dt=None, precision="f64", **kw):
+    """Perturbed stream with the unperturbed progenitor (streamhelpers.py:119-146)."""
+    return gen_stream(pot_base, ts, prog_w0, Msat, seed_num, solver=solver, kval_arr=kval_arr, dt=dt,
+                      pot_pert=pot_pert, prog_in_pert=False, precision=precision, **kw)
+
+
+gen_stream_scan_with_pert = gen_stream_vmapped_with_pert
+
+
+def custom_release_model(pos_prog=None, vel_prog=None, pos_rel=None, vel_rel=None):
+    """streamhelpers.py:186-198"""
+    return f64(pos_prog) + f64(pos_rel), f64(vel_prog) + f64(vel_rel)
+
+
+def computed_binned_track(stream, phi1, bins=20):
+    """Mean 6-D state in phi1 bins (streamhelpers.py:201-228).
+
+    Same conventions as the reference: edges = linspace(min, max, bins),
+    bin = digitize(phi1, edges), output row b is the nan-mean of the items
+    with bin == b for b = 0..bins-2 (so row 0 and the last interval stay
+    empty, as in the reference), and empty or exactly-zero means are NaN."""
+    s = f64(stream).reshape(-1, 6)
+    key = f64(phi1).reshape(-1)
+    lo, hi = float(key.min()), float(key.max())
+    edges = f64(np.linspace(lo, hi, int(bins)))
+    sums, counts = _core.binned_sums(s, key, edges)
+    mean = sums / counts
+    return torch.where(mean == 0, torch.full_like(mean, float("nan")), mean)
+
+
+def release_model_Chen25(pot_base, key, x, v, Msat, t, normals=None):
+    """Chen+25 6-D Gaussian release at one time (streamhelpers.py:352-432).
+
+    `key` seeds numpy's PCG64 (JAX keys are not available)."""
+    if normals is None:
+        normals = release_normals(int(np.asarray(key).ravel()[-1]), 1, 1, 6)[0]
+    w = torch.cat([f64(x).reshape(1, 3), f64(v).reshape(1, 3)], dim=1)
+    ics, _ = pot_base._release(w, [float(host64(t))], Msat, np.asarray(host64(normals)).reshape(1, 1, 6),
+                               model=_abi.SS_RELEASE_CHEN25, chen=(CHEN25_MEAN, chen25_factor()))
+    o = ics[0, 0]
+    return o[0, :3], o[1, :3], o[0, 3:], o[1, 3:]
+
+
+def gen_stream_ics_Chen25(pot_base=None, ts=None, prog_w0=None, Msat=None, key=None, solver=None, rtol=1e-7,
+                          atol=1e-7, dtmin=0.3, dtmax=None, max_steps=10_000, *, dt=None, normals=None):
+    """streamhelpers.py:434-459: returns ([pos_close, pos_far, vel_close, vel_far], progenitor Solution)."""
+    from .main import Solution
+    ts_h = host64(ts).reshape(-1)
+    ws, _, _ = pot_base._prog_orbit(ts_h, prog_w0, dt, dtmin, dtmax)
+    if normals is None:
+        normals = release_normals(int(np.asarray(key).ravel()[-1]), len(ts_h), 1, 6)
+    ics, _ = pot_base._release(ws, ts_h, Msat, normals, model=_abi.SS_RELEASE_CHEN25,
+                               chen=(CHEN25_MEAN, chen25_factor()))
+    return list(_split_ics(ics, 1)), Solution(torch.as_tensor(ts_h, device=ws.device), ws)
+
+
+def gen_stream_vmapped_Chen25(pot_base, ts, prog_w0, Msat, key, solver=None, rtol=1e-7, atol=1e-7, dtmin=0.3,
+                              dtmax=None, max_steps=10_000, throw=False, prog_pot=None, *, dt=None,
+                              precision="f64", snapshot_every=None, normals=None, n_particles_per_release=2):
+    """Chen+25 stream with the progenitor's own potential moving on its
+    orbit (streamhelpers.py:491-543)."""
+    if prog_pot is None:
+        prog_pot = _pot.PlummerPotential(m=0.0, r_s=1.0, units=pot_base.units)
+    seed = int(np.asarray(key).ravel()[-1])
+    return gen_stream(pot_base, ts, prog_w0, Msat, seed, solver=solver, dt=dt, dtmax=dtmax, release="chen25",
+                      prog_pot=prog_pot, precision=precision, snapshot_every=snapshot_every, normals=normals,
+                      n_particles_per_release=n_particles_per_release, throw=throw)
+
+
+__all__ = ["gen_stream", "eval_dense_stream", "eval_dense_stream_id", "gen_stream_ics_pert",
+           "gen_stream_vmapped_with_pert", "gen_stream_vmapped_with_pert_fixed_prog", "gen_stream_scan_with_pert",
+           "custom_release_model", "computed_binned_track", "release_model_Chen25", "gen_stream_ics_Chen25",
+           "gen_stream_vmapped_Chen25", "chen25_factor", "CHEN25_MEAN", "CHEN25_COV"]

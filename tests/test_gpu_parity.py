@@ -1,0 +1,334 @@
+"""GPU parity: every kernel against the CPU FP64 oracle on the same seeded
+inputs, through the C ABI (via the package facade).
+
+Tolerances: FP64 paths <= 1e-10 relative in final phase-space coordinates
+(1e-12 for single evaluations); FP32-compensated streams <= 1e-5 relative;
+FP32 responses as stated per test."""
+import numpy as np
+import pytest
+import torch
+
+from streamsculptor_gb300 import _abi
+
+from .conftest import PROG_WF, mw3_gpu, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def np64(t):
+    return t.detach().cpu().double().numpy()
+
+
+def phase_err(a, b):
+    """max over particles of max(|dx|/|x|, |dv|/|v|)."""
+    a, b = np.asarray(a).reshape(-1, 6), np.asarray(b).reshape(-1, 6)
+    ex = np.linalg.norm(a[:, :3] - b[:, :3], axis=1) / np.linalg.norm(b[:, :3], axis=1)
+    ev = np.linalg.norm(a[:, 3:] - b[:, 3:], axis=1) / np.linalg.norm(b[:, 3:], axis=1)
+    return float(np.max(np.maximum(ex, ev)))
+
+
+KINDS = [
+    ("NFWPotential", dict(m=5.4e11, r_s=15.62), (_abi.SS_NFW, 0, (5.4e11, 15.62, 0.0))),
+    ("TriaxialNFWPotential", dict(m=3e11, r_s=12.0, q1=1.0, q2=0.9, q3=0.8),
+     (_abi.SS_TRIAXIAL_NFW, 0, (3e11, 12.0, 1.0, 0.9, 0.8))),
+    ("MiyamotoNagaiDisk", dict(m=6.8e10, a=3.0, b=0.28), (_abi.SS_MIYAMOTO_NAGAI, 0, (6.8e10, 3.0, 0.28))),
+    ("HernquistPotential", dict(m=5e9, r_s=1.0, soft=0.01), (_abi.SS_HERNQUIST, 0, (5e9, 1.0, 0.01))),
+    ("PlummerPotential", dict(m=2e9, r_s=0.5), (_abi.SS_PLUMMER, 0, (2e9, 0.5))),
+    ("Isochrone", dict(m=4e9, a=1.5), (_abi.SS_ISOCHRONE, 0, (4e9, 1.5))),
+]
+
+
+@pytest.mark.parametrize("name,kw,spec", KINDS)
+def test_potential_eval_every_kind(ss, oracle, name, kw, spec):
+    from streamsculptor_gb300 import potential as P
+    pot = getattr(P, name)(**kw, units=ss.usys)
+    x = np.random.default_rng(7).normal(0, 8, size=(300, 3))
+    x = x[np.linalg.norm(x, axis=1) > 0.3]
+    phi_o, g_o, H_o = oracle.potential_eval(oracle.HostModel([spec]), x)
+    assert rel_err(np64(pot.potential(x, 0.0)), phi_o) < 1e-12
+    assert rel_err(np64(pot.gradient(x, 0.0)), g_o) < 1e-12
+    assert rel_err(np64(pot.jacobian_force(x, 0.0)), H_o) < 1e-11
+
+
+def test_nfw_golden_through_gpu(ss):
+    # examples/tests.ipynb:1671: hamiltonian_field(NFW(1e12, 20)).term(0, [1,2,3,.2,.3,.4])
+    from streamsculptor_gb300 import fields, potential as P
+    f = fields.hamiltonian_field(P.NFWPotential(m=1e12, r_s=20.0, units=ss.usys))
+    out = np64(f.term(0.0, np.array([1.0, 2.0, 3.0, 0.2, 0.3, 0.4])))
+    printed = np.array([0.2, 0.3, 0.4, -0.0011937, -0.00238739, -0.00358109])
+    assert np.all(np.abs(out - printed) <= 5e-9)
+
+
+def _track_and_subhalos(ss, oracle):
+    from streamsculptor_gb300 import potential as P
+    rng = np.random.default_rng(11)
+    tk = np.arange(40) * 2.0 - 20.0
+    knots = np.stack([8 + np.cos(tk / 30), np.sin(tk / 25) * 3, 0.1 * tk], axis=1)
+    track = ss.CenterTrack.from_samples(tk, knots)
+    nsh = 5
+    sh = dict(m=10 ** rng.uniform(6, 8, nsh), a=rng.uniform(0.1, 1.0, nsh), x0=rng.normal(0, 5, (nsh, 3)),
+              v=rng.normal(0, 0.1, (nsh, 3)), t0=rng.uniform(-10, 10, nsh), t_window=15.0)
+    gpu = P.Potential_Combine([mw3_gpu(ss),
+                               P.TimeDepTranslatingPotential(P.PlummerPotential(m=3e8, r_s=0.3, units=ss.usys), track,
+                                                             units=ss.usys),
+                               P.SubhaloLinePotential(sh["m"], sh["a"], sh["x0"], sh["v"], sh["t0"], sh["t_window"],
+                                                      units=ss.usys)], units=ss.usys)
+    orc = oracle.HostModel(oracle.mw3() + [(_abi.SS_PLUMMER, 1, (3e8, 0.3))], track=(tk[0], 2.0, knots),
+                           subhalos=dict(sh, kind=1))
+    return gpu, orc
+
+
+def test_time_dependent_potential_eval(ss, oracle):
+    gpu, orc = _track_and_subhalos(ss, oracle)
+    x = np.random.default_rng(3).normal(0, 6, size=(200, 3))
+    for t in (-30.0, -5.5, 0.0, 13.3, 90.0):
+        phi_o, g_o, H_o = oracle.potential_eval(orc, x, t)
+        assert rel_err(np64(gpu.potential(x, t)), phi_o) < 1e-12
+        assert rel_err(np64(gpu.gradient(x, t)), g_o) < 1e-12
+
+
+def test_orbit_backwards_f64(ss, oracle):
+    pot = mw3_gpu(ss)
+    ts = np.array([0.0, -1000.0, -3000.0])
+    sol = pot.integrate_orbit(w0=PROG_WF, ts=ts, t0=0.0, t1=-3000.0, dt=1.0)
+    ref = oracle.orbit(oracle.HostModel(oracle.mw3()), PROG_WF, 0.0, -1.0, 3000, 1000)[0]
+    assert phase_err(np64(sol.ys), ref) < 1e-11
+
+
+def test_orbit_batch(ss, oracle):
+    pot = mw3_gpu(ss)
+    w0 = PROG_WF + np.random.default_rng(0).normal(0, 0.5, size=(64, 6)) * np.array([1, 1, 1, .01, .01, .01])
+    ts = np.arange(0, 501.0, 50.0)
+    ys = np64(pot.integrate_orbit_batch_vmapped(w0=w0, ts=ts, dt=0.5).ys)
+    ref = oracle.orbit(oracle.HostModel(oracle.mw3()), w0, 0.0, 0.5, 1000, 100)
+    assert ys.shape == (64, 11, 6)
+    assert phase_err(ys, ref) < 1e-11
+
+
+@pytest.mark.parametrize("model", ["fardal", "chen25"])
+def test_release_and_jacobian(ss, oracle, model):
+    from streamsculptor_gb300.streamhelpers import CHEN25_MEAN, chen25_factor
+    pot = mw3_gpu(ss)
+    orc = oracle.HostModel(oracle.mw3())
+    w = oracle.orbit(orc, PROG_WF, 0.0, 1.0, 300, 10)[0]
+    n = w.shape[0]
+    kind = 1 if model == "chen25" else 0
+    nz = 6 if kind else 4
+    z = np.random.default_rng(5).standard_normal((n, 3, nz))
+    chen = (CHEN25_MEAN, chen25_factor()) if kind else None
+    ics, J = pot._release(w, np.arange(n) * 10.0, 2e4, z, model=kind, chen=chen, jac=True)
+    ics_o, J_o = oracle.release(orc, w, np.arange(n) * 10.0, 2e4, z, model_kind=kind, chen=chen, jac=True)
+    assert phase_err(np64(ics), ics_o) < 1e-12
+    assert rel_err(np64(J), J_o) < 1e-9
+
+
+def _c1_setup(oracle, n_rel=3000, dt=1.0):
+    orc = oracle.HostModel(oracle.mw3())
+    T = n_rel * dt
+    back = oracle.orbit(orc, PROG_WF, 0.0, -dt, n_rel, n_rel)[0, -1]
+    ts = -T + np.arange(n_rel + 1) * dt
+    normals = np.random.default_rng(2024).standard_normal((n_rel + 1, 1, 4))
+    return orc, back, ts, normals
+
+
+def test_stream_f64_c1_full_parity(ss, oracle):
+    """3000 releases x 2 = 6000 particles, 3000 steps of 1 Myr, final snapshot."""
+    orc, back, ts, normals = _c1_setup(oracle)
+    pot = mw3_gpu(ss)
+    lead, trail = pot.gen_stream_vmapped(ts=ts, prog_w0=back, Msat=2e4, normals=normals)
+    ws = oracle.orbit(orc, back, ts[0], 1.0, 3000, 1)[0]
+    ics, _ = oracle.release(orc, ws, ts, 2e4, normals)
+    final, _, st = oracle.stream(orc, ts[0], 1.0, 3000, ics[:-1].reshape(-1, 6), 2, 1)
+    final = final.reshape(3000, 2, 6)
+    assert (st == 0).all()
+    assert phase_err(np64(lead), final[:, 0]) <= 1e-10
+    assert phase_err(np64(trail), final[:, 1]) <= 1e-10
+
+
+def test_stream_f32k_c1_error_bound(ss, oracle):
+    """FP32 stages + compensated accumulation vs the FP64 oracle: <= 1e-5."""
+    orc, back, ts, normals = _c1_setup(oracle)
+    pot = mw3_gpu(ss)
+    lead, trail = pot.gen_stream_vmapped(ts=ts, prog_w0=back, Msat=2e4, normals=normals, precision="f32k")
+    ws = oracle.orbit(orc, back, ts[0], 1.0, 3000, 1)[0]
+    ics, _ = oracle.release(orc, ws, ts, 2e4, normals)
+    final, _, _ = oracle.stream(orc, ts[0], 1.0, 3000, ics[:-1].reshape(-1, 6), 2, 1)
+    final = final.reshape(3000, 2, 6)
+    err = max(phase_err(np64(lead), final[:, 0]), phase_err(np64(trail), final[:, 1]))
+    print(f"f32k C1 max relative phase-space error: {err:.3e}")
+    assert err <= 1e-5
+
+
+def _moving_prog_case(ss, oracle, n_rel=150, ppr=8, dt=0.5, spr=2):
+    from streamsculptor_gb300 import potential as P
+    orc = oracle.HostModel(oracle.mw3())
+    T = n_rel * spr * dt
+    back = oracle.orbit(orc, PROG_WF, 0.0, -dt, n_rel * spr, n_rel * spr)[0, -1]
+    ts = -T + np.arange(n_rel + 1) * spr * dt
+    normals = np.random.default_rng(99).standard_normal((n_rel + 1, ppr // 2, 4))
+    ws = oracle.orbit(orc, back, ts[0], dt, n_rel * spr, spr)[0]
+    ics, _ = oracle.release(orc, ws, ts, 2e4, normals)
+    orc_mov = oracle.HostModel(oracle.mw3() + [(_abi.SS_PLUMMER, 1, (2e4, 0.01))], track=(ts[0], spr * dt, ws[:, :3]))
+    prog = P.PlummerPotential(m=2e4, r_s=0.01, units=ss.usys)
+    return orc_mov, back, ts, normals, ics, prog, dict(n_rel=n_rel, ppr=ppr, dt=dt, spr=spr)
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-10), ("f32k", 1e-5)])
+def test_moving_progenitor_stream_with_snapshots(ss, oracle, precision, tol):
+    from streamsculptor_gb300.streamhelpers import gen_stream
+    orc_mov, back, ts, normals, ics, prog, c = _moving_prog_case(ss, oracle)
+    n_rel, ppr, dt, spr = c["n_rel"], c["ppr"], c["dt"], c["spr"]
+    lead, trail, snaps = gen_stream(mw3_gpu(ss), ts, back, 2e4, normals=normals, dt=dt, prog_pot=prog,
+                                    n_particles_per_release=ppr, precision=precision, snapshot_every=25)
+    final, snaps_o, st = oracle.stream(orc_mov, ts[0], dt, n_rel * spr, ics[:-1].reshape(-1, 6), ppr, spr,
+                                       snap_stride=25)
+    final = final.reshape(n_rel, ppr // 2, 2, 6)
+    assert phase_err(np64(lead), final[:, :, 0]) <= tol
+    assert phase_err(np64(trail), final[:, :, 1]) <= tol
+    s = snaps.detach().cpu().numpy().reshape(snaps_o.shape)
+    assert np.array_equal(np.isnan(s), np.isnan(snaps_o))
+    ok = ~np.isnan(snaps_o)
+    assert np.max(np.abs(s[ok] - snaps_o[ok]) / np.maximum(np.abs(snaps_o[ok]), 1e-3)) < max(tol, 3e-7) * 10
+
+
+def test_nonlinear_subhalo_stream_parity(ss, oracle):
+    from streamsculptor_gb300 import potential as P
+    from streamsculptor_gb300.streamhelpers import gen_stream_vmapped_with_pert_fixed_prog
+    orc, back, ts, normals = _c1_setup(oracle, n_rel=400)
+    rng = np.random.default_rng(8)
+    sh = dict(m=np.array([3e7, 1e6, 5e7]), a=np.array([0.5, 0.2, 0.8]), x0=rng.normal(0, 8, (3, 3)),
+              v=rng.normal(0, 0.15, (3, 3)), t0=np.array([-300.0, -150.0, -50.0]), t_window=120.0)
+    pert = P.SubhaloLinePotential(sh["m"], sh["a"], sh["x0"], sh["v"], sh["t0"], sh["t_window"], units=ss.usys)
+    lead, trail = gen_stream_vmapped_with_pert_fixed_prog(mw3_gpu(ss), pert, ts=ts, prog_w0=back, Msat=2e4,
+                                                          normals=normals)
+    ws = oracle.orbit(orc, back, ts[0], 1.0, 400, 1)[0]
+    ics, _ = oracle.release(orc, ws, ts, 2e4, normals)
+    tot = oracle.HostModel(oracle.mw3(), subhalos=dict(sh, kind=1))
+    final, _, _ = oracle.stream(tot, ts[0], 1.0, 400, ics[:-1].reshape(-1, 6), 2, 1)
+    final = final.reshape(400, 2, 6)
+    assert phase_err(np64(lead), final[:, 0]) <= 1e-10
+    assert phase_err(np64(trail), final[:, 1]) <= 1e-10
+
+
+def _pert_case(oracle, N=24, nsh=7, n_steps=120, seed=4):
+    rng = np.random.default_rng(seed)
+    sh = dict(kind=1, m=10 ** rng.uniform(5, 8, nsh), a=rng.uniform(0.1, 1.0, nsh), x0=rng.normal(0, 10, (nsh, 3)),
+              v=rng.normal(0, 0.12, (nsh, 3)), t0=rng.uniform(0, 100, nsh), t_window=60.0)
+    orc = oracle.HostModel(oracle.mw3(), subhalos=sh)
+    base = PROG_WF + rng.normal(0, 0.3, (N, 6)) * np.array([1, 1, 1, 0.01, 0.01, 0.01])
+    pert = rng.normal(0, 1e-3, (N, nsh, 12))
+    return sh, orc, base, pert
+
+
+@pytest.mark.parametrize("ncol", [12, 6])
+def test_pert_response_f64_and_f32(ss, oracle, ncol):
+    from streamsculptor_gb300 import _core
+    sh, orc, base, pert = _pert_case(oracle)
+    pert = np.ascontiguousarray(pert[:, :, :ncol])
+    N, nsh = pert.shape[0], pert.shape[1]
+    ppr, spr, n_steps, dt = 4, 10, 120, 1.0
+    bo, po = oracle.pert_response(orc, 0.0, dt, n_steps, base, pert, ppr, spr, ncol=ncol, save_stride=30)
+    table = _core.SubhaloTable(1, *(_core.f64(sh[k]) for k in ("m", "a")), _core.f64(sh["x0"]), _core.f64(sh["v"]),
+                               _core.f64(sh["t0"]), sh["t_window"])
+    cfg = _abi.ss_pert_cfg()
+    cfg.t0, cfg.dt, cfg.n_steps, cfg.n_particles = 0.0, dt, n_steps, N
+    cfg.particles_per_release, cfg.steps_per_release, cfg.ncol, cfg.save_stride = ppr, spr, ncol, 30
+    P = mw3_gpu(ss)._desc()
+    for prec, tol in ((64, 1e-10), (32, 2e-4)):
+        # a small chunk forces several particle chunks through the workspace
+        b, p = _core.pert_response(P, table, cfg, prec, _core.f64(base), _core.f64(pert), chunk_particles=5)
+        assert phase_err(np64(b), bo) < 1e-12
+        assert rel_err(np64(p), po) < tol, prec
+
+
+def test_pert_field_term_matches_oracle(ss, oracle):
+    from streamsculptor_gb300 import fields, perturbative, potential as P
+    sh, orc, base, pert = _pert_case(oracle, N=1)
+    pot_sh = P.SubhaloLinePotential(sh["m"], sh["a"], sh["x0"], sh["v"], sh["t0"], sh["t_window"], units=ss.usys)
+    pot_st = P.SubhaloLinePotential_dRadius(sh["m"], sh["a"], sh["x0"], sh["v"], sh["t0"], sh["t_window"],
+                                            units=ss.usys)
+    gen = perturbative.GenerateMassRadiusPerturbation(mw3_gpu(ss), pot_sh, pot_st)
+    f = fields.MassRadiusPerturbation_OTF(gen)
+    for t in (10.0, 55.0):
+        d0, d1 = f.term(t, [base[0], pert[0]])
+        o0, o1 = oracle.pert_term(orc, t, base[0], pert[0])
+        assert rel_err(np64(d0), o0) < 1e-12
+        assert rel_err(np64(d1), o1) < 1e-11
+
+
+def test_linear_response_matches_nonlinear_difference(ss, oracle):
+    """d(stream)/d(eps) from the perturbation generator vs the nonlinear
+    stream with a small subhalo (the check of examples/tests.ipynb cells 120-130)."""
+    from streamsculptor_gb300 import perturbative, potential as P
+    from streamsculptor_gb300.streamhelpers import gen_stream_vmapped_with_pert
+    n_rel = 300
+    orc, back, ts, normals = _c1_setup(oracle, n_rel=n_rel)
+    base_pot = mw3_gpu(ss)
+    # a subhalo passing close to the stream mid-way
+    ws = oracle.orbit(orc, back, ts[0], 1.0, n_rel, 1)[0]
+    t_imp = ts[200]
+    x_imp = ws[200, :3] * 0.995
+    m_sh, a_sh = 1e5, 0.3
+    v_sh = np.array([0.05, -0.1, 0.08])
+    args = (np.array([m_sh]), np.array([a_sh]), x_imp[None], v_sh[None], np.array([t_imp]), 1e9)
+    pot_sh = P.SubhaloLinePotential(*args, units=ss.usys)
+    pot_st = P.SubhaloLinePotential_dRadius(*args, units=ss.usys)
+    bsm = perturbative.BaseStreamModel(base_pot, back, ts, 2e4, 0, normals=normals)
+    gen = perturbative.GenerateMassRadiusPerturbation(base_pot, pot_sh, pot_st, bsm)
+    (lb, ld), (tb, td) = gen.compute_perturbation_OTF()
+    lead0, trail0 = base_pot.gen_stream_vmapped(ts=ts, prog_w0=back, Msat=2e4, normals=normals)
+    assert phase_err(np64(lb), np64(lead0)) < 1e-12
+    lead1, trail1 = gen_stream_vmapped_with_pert(base_pot, pot_sh, ts=ts, prog_w0=back, Msat=2e4, normals=normals)
+    dn = np64(lead1) - np64(lead0)
+    dl = np64(ld)[:, 0, :6]
+    # second-order remainder: relative difference of the responses small
+    assert np.max(np.abs(dn - dl)) <= 0.02 * np.max(np.abs(dn))
+    dn_t = np64(trail1) - np64(trail0)
+    assert np.max(np.abs(dn_t - np64(td)[:, 0, :6])) <= 0.02 * np.max(np.abs(dn_t))
+
+
+def test_binned_track_matches_oracle(ss, oracle):
+    from streamsculptor_gb300 import computed_binned_track
+    rng = np.random.default_rng(12)
+    stream = rng.normal(size=(5000, 6))
+    stream[::31, 2] = np.nan
+    phi1 = rng.uniform(-1.0, 1.5, 5000)
+    out = np64(computed_binned_track(stream, phi1, bins=33))
+    edges = np.linspace(phi1.min(), phi1.max(), 33)
+    sums, counts = oracle.binned_sums(stream, phi1, edges)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        ref = sums / counts
+    ref[ref == 0] = np.nan
+    assert out.shape == (32, 6)
+    assert np.array_equal(np.isnan(out), np.isnan(ref))
+    ok = ~np.isnan(ref)
+    assert rel_err(out[ok], ref[ok]) < 1e-12
+
+
+def test_edge_cases(ss):
+    from streamsculptor_gb300 import _core
+    pot = mw3_gpu(ss)
+    # empty batch
+    assert pot.gradient(np.zeros((0, 3)), 0.0).shape == (0, 3)
+    # non-finite initial condition -> status 1, others 0
+    P = pot._desc()
+    cfg = _abi.ss_stream_cfg()
+    cfg.t0, cfg.dt, cfg.n_steps, cfg.n_particles = 0.0, 1.0, 10, 4
+    cfg.particles_per_release, cfg.steps_per_release = 2, 1
+    ics = torch.tensor(np.tile(PROG_WF, (4, 1)), dtype=torch.float64, device="cuda")
+    ics[3, 0] = float("nan")
+    for prec in ("f64", "f32k"):
+        final, st = _core.stream(P, cfg, ics, prec)
+        assert st.tolist() == [0, 0, 0, 1]
+    # a particle released at the last step keeps its initial state
+    cfg.n_particles, cfg.particles_per_release, cfg.steps_per_release = 2, 1, 10
+    final, st = _core.stream(P, cfg, ics[:2].contiguous(), "f64")
+    assert torch.equal(final[1], ics[1]) and st.tolist() == [0, 0]
+    # invalid arguments raise with the library's message
+    bad = _abi.ss_stream_cfg()
+    bad.dt = 0.0
+    bad.particles_per_release = 1
+    with pytest.raises(_abi.SSError, match="dt"):
+        _core.stream(P, bad, ics, "f64")
+    with pytest.raises(NotImplementedError):
+        pot.integrate_orbit(w0=PROG_WF, ts=[0.0, 10.0], solver="Dopri8")
