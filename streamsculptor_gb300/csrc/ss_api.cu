@@ -176,7 +176,8 @@ __global__ void potential_eval_kernel(PotDev<double> P, const double* __restrict
     }
     if (grad || hess) {
         double g[3], H[6];
-        pot_grad<double, double, true>(P, x, c, g, H);
+        const double xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
+        pot_grad<double, double, true>(P, x, xs, g, H);
         if (P.sh.n > 0) subhalo_sum_grad<double>(P.sh, x, t, g);
         if (grad)
             for (int k = 0; k < 3; ++k) grad[3 * i + k] = g[k];
@@ -254,9 +255,9 @@ __device__ T release_tidal_radius(const PotDev<double>& P, const T x[3], const T
     ph[0] = pv[0] * ipn; ph[1] = pv[1] * ipn; ph[2] = pv[2] * ipn;
     double c[3] = {0.0, 0.0, 0.0};
     if (P.has_track) track_eval(P.track, t, c);
-    T cc[3] = {T(c[0]), T(c[1]), T(c[2])};
+    T xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
     T g[3], H[6];
-    pot_grad<T, double, true>(P, x, cc, g, H);
+    pot_grad<T, double, true>(P, x, xs, g, H);
     // r_hat^T H r_hat
     T d2 = H[0] * rh[0] * rh[0] + H[1] * rh[1] * rh[1] + H[2] * rh[2] * rh[2] +
            2.0 * (H[3] * rh[0] * rh[1] + H[4] * rh[0] * rh[2] + H[5] * rh[1] * rh[2]);

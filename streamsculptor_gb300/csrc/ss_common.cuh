@@ -80,8 +80,9 @@ int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalo
 __device__ __forceinline__ void accel_f64(const PotDev<double>& P, const double x[3], double t, double a[3]) {
     double c[3] = {0.0, 0.0, 0.0};
     if (P.has_track) track_eval(P.track, t, c);
+    const double xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
     double g[3];
-    pot_grad<double, double, false>(P, x, c, g, nullptr);
+    pot_grad<double, double, false>(P, x, xs, g, nullptr);
     if (P.sh.n > 0) subhalo_sum_grad<double>(P.sh, x, t, g);
     a[0] = -g[0];
     a[1] = -g[1];

@@ -348,11 +348,13 @@ __device__ __forceinline__ void subhalo_grad(int kind, T Gm, T a, const T rel[3]
     }
 }
 
-// Composite gradient (and Hessian) at x, time t, components summed in list
-// order (Potential_Combine.gradient_func, potential.py:1291-1296).
-// `center` is the track position at t (used by SS_CENTER_TRACK components).
+// Composite gradient (and Hessian), components summed in list order
+// (Potential_Combine.gradient_func, potential.py:1291-1296).  `x` is the
+// position; `xs` the same position relative to the center track at this
+// time (used by SS_CENTER_TRACK components; callers that can form it more
+// accurately than x - c pass it directly).
 template <class T, class R, bool HESS>
-__device__ __forceinline__ void pot_grad(const PotDev<R>& P, const T x[3], const T center[3], T grad[3], T H[6]) {
+__device__ __forceinline__ void pot_grad(const PotDev<R>& P, const T x[3], const T xs[3], T grad[3], T H[6]) {
     grad[0] = grad[1] = grad[2] = T(0);
     if (HESS) {
 #pragma unroll
@@ -361,12 +363,7 @@ __device__ __forceinline__ void pot_grad(const PotDev<R>& P, const T x[3], const
 #pragma unroll 1
     for (int k = 0; k < P.n; ++k) {
         const CompDev<R>& c = P.c[k];
-        if (c.center == SS_CENTER_TRACK) {
-            T xs[3] = {x[0] - center[0], x[1] - center[1], x[2] - center[2]};
-            comp_grad<T, R, HESS>(c, xs, grad, H);
-        } else {
-            comp_grad<T, R, HESS>(c, x, grad, H);
-        }
+        comp_grad<T, R, HESS>(c, c.center == SS_CENTER_TRACK ? xs : x, grad, H);
     }
 }
 

@@ -95,7 +95,8 @@ __global__ void __launch_bounds__(64) pert_base_kernel(PotDev<double> P, PertArg
             double cc[3] = {0.0, 0.0, 0.0};
             if (P.has_track) track_eval(P.track, ts, cc);
             double g[3], H[6];
-            pot_grad<double, double, true>(P, ys, cc, g, H);
+            const double xs[3] = {ys[0] - cc[0], ys[1] - cc[1], ys[2] - cc[2]};
+            pot_grad<double, double, true>(P, ys, xs, g, H);
             k[s][0] = ys[3];
             k[s][1] = ys[4];
             k[s][2] = ys[5];

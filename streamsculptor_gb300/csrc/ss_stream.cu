@@ -49,7 +49,7 @@ struct StreamArgs {
     // f32k only
     float h_hi;
     float h_lo;
-    const float4* ctab;   // [(n_steps*5+1)] track positions at stage times
+    const float4* ctab;   // [(n_steps*5+1) x 2] track positions (hi, lo) at stage times
     const float4* shtab;  // [n_sh*3] subhalo lines
     int32_t n_sh;
     int32_t sh_kind;
@@ -120,17 +120,23 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     e = (a - (s - bb)) + (b - bb);
 }
 
-__device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamArgs& a, const float X[3], int slot,
-                                          float trel, float A[3]) {
-    float c[3] = {0.f, 0.f, 0.f};
+// Acceleration at the stage position xh + d (xh: the particle's hi part,
+// d: the small remainder of the stage offset).  Components on the center
+// track use (xh - c_hi) + (d - c_lo): xh and c_hi are close, so the
+// difference is exact and the separation keeps its relative precision.
+__device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamArgs& a, const float xh[3],
+                                          const float d[3], int slot, float trel, float A[3]) {
+    const float X[3] = {xh[0] + d[0], xh[1] + d[1], xh[2] + d[2]};
+    float xs[3] = {X[0], X[1], X[2]};
     if (P.has_track) {
-        float4 cc = __ldg(a.ctab + slot);
-        c[0] = cc.x;
-        c[1] = cc.y;
-        c[2] = cc.z;
+        const float4 ch = __ldg(a.ctab + 2 * slot);
+        const float4 cl = __ldg(a.ctab + 2 * slot + 1);
+        xs[0] = (xh[0] - ch.x) + (d[0] - cl.x);
+        xs[1] = (xh[1] - ch.y) + (d[1] - cl.y);
+        xs[2] = (xh[2] - ch.z) + (d[2] - cl.z);
     }
     float g[3];
-    pot_grad<float, float, false>(P, X, c, g, nullptr);
+    pot_grad<float, float, false>(P, X, xs, g, nullptr);
 #pragma unroll 1
     for (int j = 0; j < a.n_sh; ++j) {
         float4 s0 = __ldg(a.shtab + 3 * j);
@@ -160,53 +166,53 @@ __device__ __forceinline__ void step_f32k(const PotDev<float>& P, const StreamAr
     const int s0 = 5 * n;
     float A1[3], A2[3], A3[3], A4[3], A5[3], A6[3];
     float d1[3], d2[3], d3[3], d4[3], d5[3], d6[3];
-    float X[3];
+    float D[3];  // stage position offset from xh (small)
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        X[i] = xh[i] + xl[i];
+        D[i] = xl[i];
         d1[i] = vl[i];
     }
-    accel_f32(P, a, X, s0, tn, A1);
+    accel_f32(P, a, xh, D, s0, tn, A1);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d2[i] = vl[i] + h * (F_(SS_A21) * A1[i]);
-        X[i] = xh[i] + (xl[i] + h * (F_C2 * vh[i] + F_(SS_A21) * d1[i]));
+        D[i] = xl[i] + h * (F_C2 * vh[i] + F_(SS_A21) * d1[i]);
     }
-    accel_f32(P, a, X, s0 + 1, tn + F_C2 * h, A2);
+    accel_f32(P, a, xh, D, s0 + 1, tn + F_C2 * h, A2);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d3[i] = vl[i] + h * (F_(SS_A31) * A1[i] + F_(SS_A32) * A2[i]);
-        X[i] = xh[i] + (xl[i] + h * (F_C3 * vh[i] + F_(SS_A31) * d1[i] + F_(SS_A32) * d2[i]));
+        D[i] = xl[i] + h * (F_C3 * vh[i] + F_(SS_A31) * d1[i] + F_(SS_A32) * d2[i]);
     }
-    accel_f32(P, a, X, s0 + 2, tn + F_C3 * h, A3);
+    accel_f32(P, a, xh, D, s0 + 2, tn + F_C3 * h, A3);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d4[i] = vl[i] + h * (F_(SS_A41) * A1[i] + F_(SS_A42) * A2[i] + F_(SS_A43) * A3[i]);
-        X[i] = xh[i] + (xl[i] + h * (F_C4 * vh[i] + F_(SS_A41) * d1[i] + F_(SS_A42) * d2[i] + F_(SS_A43) * d3[i]));
+        D[i] = xl[i] + h * (F_C4 * vh[i] + F_(SS_A41) * d1[i] + F_(SS_A42) * d2[i] + F_(SS_A43) * d3[i]);
     }
-    accel_f32(P, a, X, s0 + 3, tn + F_C4 * h, A4);
+    accel_f32(P, a, xh, D, s0 + 3, tn + F_C4 * h, A4);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d5[i] = vl[i] + h * (F_(SS_A51) * A1[i] + F_(SS_A52) * A2[i] + F_(SS_A53) * A3[i] + F_(SS_A54) * A4[i]);
-        X[i] = xh[i] + (xl[i] + h * (F_C5 * vh[i] + F_(SS_A51) * d1[i] + F_(SS_A52) * d2[i] + F_(SS_A53) * d3[i] +
-                                     F_(SS_A54) * d4[i]));
+        D[i] = xl[i] + h * (F_C5 * vh[i] + F_(SS_A51) * d1[i] + F_(SS_A52) * d2[i] + F_(SS_A53) * d3[i] +
+                            F_(SS_A54) * d4[i]);
     }
-    accel_f32(P, a, X, s0 + 4, tn + F_C5 * h, A5);
+    accel_f32(P, a, xh, D, s0 + 4, tn + F_C5 * h, A5);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d6[i] = vl[i] + h * (F_(SS_A61) * A1[i] + F_(SS_A62) * A2[i] + F_(SS_A63) * A3[i] + F_(SS_A64) * A4[i] +
                              F_(SS_A65) * A5[i]);
-        X[i] = xh[i] + (xl[i] + h * (vh[i] + F_(SS_A61) * d1[i] + F_(SS_A62) * d2[i] + F_(SS_A63) * d3[i] +
-                                     F_(SS_A64) * d4[i] + F_(SS_A65) * d5[i]));
+        D[i] = xl[i] + h * (vh[i] + F_(SS_A61) * d1[i] + F_(SS_A62) * d2[i] + F_(SS_A63) * d3[i] +
+                            F_(SS_A64) * d4[i] + F_(SS_A65) * d5[i]);
     }
-    accel_f32(P, a, X, s0 + 5, tn + h, A6);
+    accel_f32(P, a, xh, D, s0 + 5, tn + h, A6);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        // position: h * (vh + D), D = sum b_i d_i
-        float D = F_(SS_B1) * d1[i] + F_(SS_B3) * d3[i] + F_(SS_B4) * d4[i] + F_(SS_B5) * d5[i] + F_(SS_B6) * d6[i];
+        // position: h * (vh + Db), Db = sum b_i d_i
+        float Db = F_(SS_B1) * d1[i] + F_(SS_B3) * d3[i] + F_(SS_B4) * d4[i] + F_(SS_B5) * d5[i] + F_(SS_B6) * d6[i];
         float pp = h * vh[i];
         float pe = fmaf(h, vh[i], -pp);
-        float lo = pe + (a.h_lo * vh[i] + h * D);
+        float lo = pe + (a.h_lo * vh[i] + h * Db);
         float s, e;
         two_sum(xh[i], pp, s, e);
         float l2 = xl[i] + (e + lo);
@@ -267,9 +273,9 @@ __global__ void __launch_bounds__(128) stream_f32k_kernel(PotDev<float> P, Strea
     }
 }
 
-// Track positions at every stage time of the run, FP64 Hermite -> float4.
-// slot 5n + s holds c(t0 + (n + c_s) dt) for c = {0, 1/5, 3/10, 4/5, 8/9};
-// slot 5 n_steps holds c(t0 + n_steps dt).
+// Track positions at every stage time of the run, FP64 Hermite -> a hi/lo
+// float pair (two float4).  Slot 5n + s holds c(t0 + (n + c_s) dt) for
+// c = {0, 1/5, 3/10, 4/5, 8/9}; slot 5 n_steps holds c(t0 + n_steps dt).
 __global__ void track_table_kernel(TrackDev tr, double t0, double dt, int32_t n_steps, float4* tab) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int64_t total = 5 * (int64_t)n_steps + 1;
@@ -280,7 +286,9 @@ __global__ void track_table_kernel(TrackDev tr, double t0, double dt, int32_t n_
     double t = t0 + ((double)n + cs[s]) * dt;
     double c[3];
     track_eval(tr, t, c);
-    tab[i] = make_float4((float)c[0], (float)c[1], (float)c[2], 0.f);
+    float hx = (float)c[0], hy = (float)c[1], hz = (float)c[2];
+    tab[2 * i] = make_float4(hx, hy, hz, 0.f);
+    tab[2 * i + 1] = make_float4((float)(c[0] - (double)hx), (float)(c[1] - (double)hy), (float)(c[2] - (double)hz), 0.f);
 }
 
 // Subhalo lines relative to the run start t0: position at t0, velocity,
@@ -333,7 +341,7 @@ static int64_t f32k_workspace(const ss_potential* pot, const ss_stream_cfg* cfg)
     int64_t bytes = 0;
     bool track = false;
     for (int k = 0; k < pot->n_components && k < SS_MAX_COMPONENTS; ++k) track |= pot->comp[k].center == SS_CENTER_TRACK;
-    if (track) bytes += (5 * cfg->n_steps + 1) * (int64_t)sizeof(float4);
+    if (track) bytes += (5 * cfg->n_steps + 1) * 2 * (int64_t)sizeof(float4);
     bytes = (bytes + 255) / 256 * 256;
     if (pot->subhalos.n > 0) bytes += 3 * pot->subhalos.n * (int64_t)sizeof(float4);
     return bytes;
@@ -391,7 +399,7 @@ int ss_stream_f32k(const ss_potential* pot, const ss_stream_cfg* cfg, const doub
                                                                             (int32_t)cfg->n_steps, tab);
         SS_LAUNCH_CHECK();
         a.ctab = tab;
-        ws += (total * (int64_t)sizeof(float4) + 255) / 256 * 256;
+        ws += (total * 2 * (int64_t)sizeof(float4) + 255) / 256 * 256;
     }
     if (pot->subhalos.n > 0) {
         PotDev<double> Pd;

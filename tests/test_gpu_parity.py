@@ -92,7 +92,8 @@ def test_orbit_backwards_f64(ss, oracle):
     ts = np.array([0.0, -1000.0, -3000.0])
     sol = pot.integrate_orbit(w0=PROG_WF, ts=ts, t0=0.0, t1=-3000.0, dt=1.0)
     ref = oracle.orbit(oracle.HostModel(oracle.mw3()), PROG_WF, 0.0, -1.0, 3000, 1000)[0]
-    assert phase_err(np64(sol.ys), ref) < 1e-11
+    assert sol.ys.shape == (3, 6)
+    assert phase_err(np64(sol.ys), ref[[0, 1, 3]]) < 1e-11
 
 
 def test_orbit_batch(ss, oracle):
@@ -187,8 +188,9 @@ def test_moving_progenitor_stream_with_snapshots(ss, oracle, precision, tol):
     assert phase_err(np64(trail), final[:, :, 1]) <= tol
     s = snaps.detach().cpu().numpy().reshape(snaps_o.shape)
     assert np.array_equal(np.isnan(s), np.isnan(snaps_o))
-    ok = ~np.isnan(snaps_o)
-    assert np.max(np.abs(s[ok] - snaps_o[ok]) / np.maximum(np.abs(snaps_o[ok]), 1e-3)) < max(tol, 3e-7) * 10
+    ok = ~np.isnan(snaps_o[..., 0])
+    # float32 snapshots: one float32 rounding on top of the path's own error
+    assert phase_err(s[ok], snaps_o[ok].astype(np.float64)) <= tol + 3e-7
 
 
 def test_nonlinear_subhalo_stream_parity(ss, oracle):
@@ -258,13 +260,16 @@ def test_pert_field_term_matches_oracle(ss, oracle):
 
 def test_linear_response_matches_nonlinear_difference(ss, oracle):
     """d(stream)/d(eps) from the perturbation generator vs the nonlinear
-    stream with a small subhalo (the check of examples/tests.ipynb cells 120-130)."""
+    stream with a small subhalo (the check of examples/tests.ipynb cells
+    120-130).  The linear theory holds the progenitor's present-day state
+    fixed (its response is integrated backwards from t_obs), so the
+    nonlinear stream starts from the progenitor integrated back from the
+    same present-day state in base + subhalo."""
     from streamsculptor_gb300 import perturbative, potential as P
     from streamsculptor_gb300.streamhelpers import gen_stream_vmapped_with_pert
     n_rel = 300
     orc, back, ts, normals = _c1_setup(oracle, n_rel=n_rel)
     base_pot = mw3_gpu(ss)
-    # a subhalo passing close to the stream mid-way
     ws = oracle.orbit(orc, back, ts[0], 1.0, n_rel, 1)[0]
     t_imp = ts[200]
     x_imp = ws[200, :3] * 0.995
@@ -278,13 +283,15 @@ def test_linear_response_matches_nonlinear_difference(ss, oracle):
     (lb, ld), (tb, td) = gen.compute_perturbation_OTF()
     lead0, trail0 = base_pot.gen_stream_vmapped(ts=ts, prog_w0=back, Msat=2e4, normals=normals)
     assert phase_err(np64(lb), np64(lead0)) < 1e-12
-    lead1, trail1 = gen_stream_vmapped_with_pert(base_pot, pot_sh, ts=ts, prog_w0=back, Msat=2e4, normals=normals)
-    dn = np64(lead1) - np64(lead0)
-    dl = np64(ld)[:, 0, :6]
-    # second-order remainder: relative difference of the responses small
-    assert np.max(np.abs(dn - dl)) <= 0.02 * np.max(np.abs(dn))
-    dn_t = np64(trail1) - np64(trail0)
-    assert np.max(np.abs(dn_t - np64(td)[:, 0, :6])) <= 0.02 * np.max(np.abs(dn_t))
+    total = P.Potential_Combine([base_pot, pot_sh], units=ss.usys)
+    w_obs = np64(bsm.prog_loc_fwd[-1])
+    back_p = total.integrate_orbit(w0=w_obs, ts=[ts[-1], ts[0]], t0=ts[-1], t1=ts[0], dt=1.0).ys[-1]
+    lead1, trail1 = gen_stream_vmapped_with_pert(base_pot, pot_sh, ts=ts, prog_w0=back_p, Msat=2e4, normals=normals)
+    for nl, base, lin in ((lead1, lead0, ld), (trail1, trail0, td)):
+        dn = np64(nl) - np64(base)
+        dl = np64(lin)[:, 0, :6]
+        # the remainder is second order in the subhalo mass
+        assert np.max(np.abs(dn - dl)) <= 0.02 * np.max(np.abs(dn))
 
 
 def test_binned_track_matches_oracle(ss, oracle):
