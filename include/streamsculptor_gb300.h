@@ -219,6 +219,24 @@ int ss_stream_f32k(const ss_potential* pot, const ss_stream_cfg* cfg, const doub
                    double* final_w, float* snaps, int32_t* status,
                    void* workspace, int64_t workspace_bytes, void* stream);
 
+/* ss_stream_f32k for callers that cannot allocate device memory.  It has no
+ * counterpart in the reference.  Some callers hold no device allocator or
+ * must not call cudaMalloc/cudaFree (which may synchronize the device): a
+ * bare C FFI binding, host code on a latency-critical path, an application
+ * whose device memory belongs to another allocator.  This entry point takes
+ * the same inputs and outputs as ss_stream_f32k (still caller-provided) and
+ * keeps its scratch in a fixed 4 MiB device array inside the library
+ * (SS_NOALLOC_SCRATCH_BYTES), held by every GPU that loads the library until
+ * the process exits.  Runs whose scratch would exceed it (about 26000 steps
+ * with a moving progenitor) return SS_ERR_WORKSPACE.  The first call on a
+ * device looks the array's device address up (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture.
+ * Every call overwrites the whole scratch it uses before reading it, and
+ * all calls share the one array: calls that overlap on the GPU (different
+ * streams, no ordering between them) race and must not be issued. */
+int ss_stream_f32k_noalloc(const ss_potential* pot, const ss_stream_cfg* cfg, const double* ics,
+                           double* final_w, float* snaps, int32_t* status, void* stream);
+
 /* First-order subhalo response (fields.MassRadiusPerturbation_OTF.term,
  * fields.py:174-206, integrated as in
  * GenerateMassRadiusPerturbation.compute_perturbation_OTF, perturbative.py:100-135).

@@ -420,3 +420,57 @@ int ss_stream_f32k(const ss_potential* pot, const ss_stream_cfg* cfg, const doub
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// No-allocation variant of ss_stream_f32k.
+//
+// Some callers cannot allocate device memory at all: language bindings that
+// reach this library through a bare C FFI and hold no device allocator, host
+// code that must not make a call that may synchronize the device (cudaMalloc
+// and cudaFree can), and applications whose device memory is owned entirely
+// by another allocator.  For them the FP32 stream's scratch (the progenitor
+// track and subhalo tables) lives in this fixed file-scope array instead of
+// a caller workspace.  Every GPU that loads the library holds the array until
+// the process exits.
+#define SS_NOALLOC_SCRATCH_BYTES (4LL << 20)
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[SS_NOALLOC_SCRATCH_BYTES];
+
+#include <mutex>
+
+namespace {
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64] = {nullptr};
+}  // namespace
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device (host code cannot use the symbol's host-side name as a device
+// pointer).
+static int noalloc_scratch(void** out) {
+    int dev = 0;
+    SS_CUDA_TRY(cudaGetDevice(&dev));
+    SS_CHECK_ARG(dev >= 0 && dev < 64, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (g_noalloc_ptr[dev] == nullptr) {
+        void* p = nullptr;
+        SS_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return SS_OK;
+}
+
+extern "C" int ss_stream_f32k_noalloc(const ss_potential* pot, const ss_stream_cfg* cfg, const double* ics,
+                                      double* final_w, float* snaps, int32_t* status, void* stream) {
+    if (!pot || !cfg) return set_error(SS_ERR_INVALID_ARGUMENT, "NULL argument");
+    const int64_t need = f32k_workspace(pot, cfg);
+    if (need > SS_NOALLOC_SCRATCH_BYTES)
+        return set_error(SS_ERR_WORKSPACE,
+                         "ss_stream_f32k_noalloc: this run needs %lld bytes of scratch but the fixed scratch holds "
+                         "%lld (about 26000 steps with a moving progenitor); use ss_stream_f32k with a workspace",
+                         (long long)need, (long long)SS_NOALLOC_SCRATCH_BYTES);
+    void* scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    return ss_stream_f32k(pot, cfg, ics, final_w, snaps, status, scratch, SS_NOALLOC_SCRATCH_BYTES, stream);
+}
