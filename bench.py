@@ -355,7 +355,7 @@ def gpu_arm(args, wl):
         emit({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
               "warmup": args.warmup, "ms_per_step": r32["ms_per_step"], "higher_is_better": True,
               "scaling": "weak", "vs_baseline": None,
-              "dtype": "f32 (compensated hi+lo state; FP64 progenitor, time, release)",
+              "dtype": "f32 (compensated hi+lo state; FP64 progenitor orbit, time and release)",
               "data": "synthetic (seeded PCG64 Gaussian draws)",
               "config": {"workload": wl["name"], "particles": n_rel * ppr, "n_steps": n_steps,
                          "particle_steps_per_step": work, "dt_myr": dt, "snapshot_every": snap,
@@ -376,6 +376,78 @@ def gpu_arm(args, wl):
         dist.destroy_process_group()
 
 
+# ------------------------------------------------------------ config 3
+C3 = dict(n_rel=2000, ppr=50, dt=1.0, n_sh=1000, ncol=6,
+          name="first-order response: 2000 releases x 50 particles (1e5) x 1000 Plummer subhalos "
+               "(log10 M ~ U(5,8), r_s = 1.62 kpc (M/1e8)^0.5, x0 uniform in 30 kpc, v ~ N(0, 0.12 kpc/Myr), "
+               "always active), 2 Gyr at dt = 1 Myr, FP32 response (6 mass columns), FP64 base track and time")
+
+
+def c3_subhalos(n, seed=3):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    m = 10 ** rng.uniform(5, 8, n)
+    a = 1.62 * np.sqrt(m / 1e8)
+    d = rng.normal(size=(n, 3))
+    x0 = d / np.linalg.norm(d, axis=1, keepdims=True) * (30.0 * rng.uniform(size=(n, 1)) ** (1 / 3))
+    v = rng.normal(0, 0.12, (n, 3))
+    return m, a, x0, v
+
+
+C3S = dict(C3, n_rel=200, name="profiling case shaped like config 3: 200 releases x 50 particles x 1000 subhalos, "
+                                 "200 steps")
+
+
+def c3_arm(args):
+    import torch
+
+    import streamsculptor_gb300 as ss
+    from streamsculptor_gb300 import _abi, _core, potential as P
+
+    torch.cuda.set_device(0)
+    c3 = C3S if args.workload == "c3s" else C3
+    u = ss.usys
+    pot = P.Potential_Combine([P.NFWPotential(m=5.4e11, r_s=15.62, units=u),
+                               P.MiyamotoNagaiDisk(m=6.8e10, a=3.0, b=0.28, units=u),
+                               P.HernquistPotential(m=5e9, r_s=1.0, units=u)], units=u)
+    n_rel, ppr, dt, nsh, ncol = c3["n_rel"], c3["ppr"], c3["dt"], c3["n_sh"], c3["ncol"]
+    T = n_rel * dt
+    ts = -T + np.arange(n_rel + 1) * dt
+    back = pot.integrate_orbit(w0=WF, ts=np.array([0.0, -T]), t0=0.0, t1=-T, dt=dt).ys[-1]
+    normals = np.random.Generator(np.random.PCG64(77)).standard_normal((n_rel + 1, ppr // 2, 4))
+    ws, _, _ = pot._prog_orbit(ts, back, dt)
+    ics, _ = pot._release(ws, ts, MSAT, normals)
+    base = ics[:n_rel].reshape(-1, 6).contiguous()
+    m, a, x0, v = c3_subhalos(nsh)
+    table = _core.SubhaloTable(_abi.SS_SH_PLUMMER, _core.f64(m), _core.f64(a), _core.f64(x0), _core.f64(v),
+                               _core.f64(np.full(nsh, ts[0])), float("inf"))
+    cfg = _abi.ss_pert_cfg()
+    cfg.t0, cfg.dt, cfg.n_steps, cfg.n_particles = float(ts[0]), dt, n_rel, base.shape[0]
+    cfg.particles_per_release, cfg.steps_per_release, cfg.ncol, cfg.save_stride = ppr, 1, ncol, 0
+    Pd = pot._desc()
+    work = ppr * (n_rel * n_rel - n_rel * (n_rel - 1) // 2) * nsh
+    for _ in range(args.warmup):
+        _core.pert_response(Pd, table, cfg, 32, base, None)
+    torch.cuda.synchronize()
+    l0 = _abi.load().ss_kernel_launches()
+    ms = 0.0
+    clocks = ClockSampler(gpu_id_for(0))
+    clocks.start()
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _core.pert_response(Pd, table, cfg, 32, base, None)
+        e1.record()
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
+    ck = clocks.stop()
+    launches = _abi.load().ss_kernel_launches() - l0
+    emit({"metric": "(particle x subhalo)-steps/s, first-order response", "value": work / (ms / args.steps * 1e-3),
+          "unit": "(particle x subhalo)-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+          "ms_per_step": ms / args.steps, "higher_is_better": True, "dtype": "f32 response, f64 base track",
+          "data": "synthetic (seeded)", "config": {"workload": c3["name"], "system_steps_per_step": work},
+          "clocks": ck, "gpu_launches": launches})
+
+
 def traffic_for(kernel):
     """DRAM bytes per launch from the committed ncu summary, if present."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
@@ -392,12 +464,15 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["c3", "c3s"], default="c2")
     ap.add_argument("--f64-steps", type=int, default=2)
     ap.add_argument("--f64-warmup", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precisions", default="f32k,f64", help="f32k,f64 (default) or f32k alone for profiling")
     args = ap.parse_args()
+    if args.workload in ("c3", "c3s"):
+        c3_arm(args)
+        return
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         reference_arm(args, wl)

@@ -183,6 +183,20 @@ int ss_orbit_f64(const ss_potential* pot, const double* w0, int64_t n_orbits,
                  double t0, double dt, int64_t n_steps, int64_t save_every,
                  double* out, void* stream);
 
+/* One orbit, parallel in time (multiple shooting with Newton's method): the
+ * n_steps fixed Dopri5 steps are split into slices that are integrated in
+ * parallel in FP64 together with their 6x6 Jacobians, and a serial Newton
+ * sweep joins them; converged when the joins move by less than tol
+ * (relative).  The result is the serial fixed-step FP64 orbit up to
+ * round-off at the joins, at a fraction of its latency on GB300.
+ * out [n_steps/save_every + 1, 6]; workspace >=
+ * ss_orbit_shoot_workspace_bytes(n_steps) bytes (8-byte aligned).  Static
+ * potentials only; others run the serial ss_orbit_f64 kernel. */
+int64_t ss_orbit_shoot_workspace_bytes(int64_t n_steps);
+int ss_orbit_shoot_f64(const ss_potential* pot, const double* w0, double t0, double dt,
+                       int64_t n_steps, int64_t save_every, double* out,
+                       void* workspace, int64_t workspace_bytes, double tol, void* stream);
+
 /* Spline slopes for a center track: knots [n,3] -> slopes [n,3] (device). */
 int ss_track_slopes(const double* knots, int64_t n_knots, double dt, double* slopes, void* stream);
 
@@ -264,6 +278,44 @@ int ss_pert_response(const ss_potential* base, const ss_subhalos* sh, const ss_p
  * perturbative.py:40-41). */
 int ss_subhalo_eval(const ss_subhalos* sh, double G, const double* xyz, int64_t n, double t,
                     double* phi, double* grad, double* dphi_da, double* grad_dphi_da, void* stream);
+
+/* ---- gradients of a loss on the final stream (no reference counterpart in
+ * code: the reference differentiates with jax.jacfwd through diffrax,
+ * main.py:160, examples/tests.ipynb:2959).  Parameter slot 6 c + j is raw
+ * parameter p[j] of component c; static potentials (no center track). */
+
+/* ss_stream_f32k storing the compensated state every ckpt_stride (= 64) local
+ * steps of each particle: ckpt [n_steps/64 + 1, n_particles, 12] floats. */
+int ss_stream_f32k_ckpt(const ss_potential* pot, const ss_stream_cfg* cfg, const double* ics,
+                        double* final_w, int32_t* status, float* ckpt, int32_t ckpt_stride,
+                        void* stream);
+
+/* Discrete adjoint of every particle's FP32 Dopri5 steps from the checkpoints:
+ * lam_final [n_particles, 6] = dL/d(final states) -> lam_ic [n_particles, 6]
+ * = dL/d(initial states); g_theta [6 n_comp] += dL/d(raw parameters). */
+int ss_stream_adjoint_f32(const ss_potential* pot, const ss_stream_cfg* cfg, const float* ckpt,
+                          int32_t ckpt_stride, const double* lam_final, double* lam_ic,
+                          double* g_theta, void* stream);
+
+/* Vector-Jacobian product of the release (ss_release_f64's map): lam_ics
+ * [n_release, n_draw, 2, 6] -> g_prog [n_release, 6] += dL/d(progenitor
+ * state) and g_theta [6 n_comp] += dL/d(raw parameters) through the tidal
+ * radius; raw_params [n_comp, 6]. */
+int ss_release_vjp(const ss_potential* pot, const ss_release_cfg* cfg, const double* prog_w,
+                   const double* t_rel, const double* msat, const double* normals,
+                   const double* lam_ics, const double* raw_params, double* g_prog,
+                   double* g_theta, void* stream);
+
+/* Progenitor orbit from the present-day state w0 back n_steps of dt and
+ * forward again (FP64, parallel in time as ss_orbit_shoot_f64), with
+ * forward-mode tangents along every raw parameter and every component of w0
+ * (n_dir = 6 n_comp + 6): states [n_steps/save_every + 1, 6] and tangents
+ * [n_steps/save_every + 1, n_dir, 6] on the forward leg.  workspace >=
+ * ss_prog_tangents_workspace_bytes(n_steps, n_comp). */
+int64_t ss_prog_tangents_workspace_bytes(int64_t n_steps, int32_t n_comp);
+int ss_prog_tangents_f64(const ss_potential* pot, const double* raw_params, const double* w0,
+                         double dt, int32_t n_steps, int32_t save_every, double* states,
+                         double* tangents, void* workspace, int64_t workspace_bytes, void* stream);
 
 /* Binned mean track (computed_binned_track, streamhelpers.py:201-228).
  * values [n, ncomp] FP64, key [n] FP64, edges [n_edges] ascending.

@@ -88,6 +88,9 @@ SIGNATURES = {
     "ss_potential_eval": (C.c_int, [C.POINTER(ss_potential), VP, C.c_int64, VP, C.c_double, VP, VP, VP, VP]),
     "ss_orbit_f64": (C.c_int, [C.POINTER(ss_potential), VP, C.c_int64, C.c_double, C.c_double, C.c_int64,
                                C.c_int64, VP, VP]),
+    "ss_orbit_shoot_workspace_bytes": (C.c_int64, [C.c_int64]),
+    "ss_orbit_shoot_f64": (C.c_int, [C.POINTER(ss_potential), VP, C.c_double, C.c_double, C.c_int64, C.c_int64, VP,
+                                     VP, C.c_int64, C.c_double, VP]),
     "ss_track_slopes": (C.c_int, [VP, C.c_int64, C.c_double, VP, VP]),
     "ss_release_f64": (C.c_int, [C.POINTER(ss_potential), C.POINTER(ss_release_cfg), VP, VP, VP, VP, VP, VP, VP]),
     "ss_stream_f64": (C.c_int, [C.POINTER(ss_potential), C.POINTER(ss_stream_cfg), VP, VP, VP, VP, VP]),
@@ -100,6 +103,15 @@ SIGNATURES = {
     "ss_pert_workspace_bytes": (C.c_int64, [C.POINTER(ss_pert_cfg), C.c_int, C.c_int64]),
     "ss_pert_response": (C.c_int, [C.POINTER(ss_potential), C.POINTER(ss_subhalos), C.POINTER(ss_pert_cfg),
                                    C.c_int, VP, VP, VP, VP, VP, C.c_int64, VP]),
+    "ss_stream_f32k_ckpt": (C.c_int, [C.POINTER(ss_potential), C.POINTER(ss_stream_cfg), VP, VP, VP, VP, C.c_int32,
+                                      VP]),
+    "ss_stream_adjoint_f32": (C.c_int, [C.POINTER(ss_potential), C.POINTER(ss_stream_cfg), VP, C.c_int32, VP, VP, VP,
+                                        VP]),
+    "ss_release_vjp": (C.c_int, [C.POINTER(ss_potential), C.POINTER(ss_release_cfg), VP, VP, VP, VP, VP, VP, VP, VP,
+                                 VP]),
+    "ss_prog_tangents_workspace_bytes": (C.c_int64, [C.c_int64, C.c_int32]),
+    "ss_prog_tangents_f64": (C.c_int, [C.POINTER(ss_potential), VP, VP, C.c_double, C.c_int32, C.c_int32, VP, VP,
+                                       VP, C.c_int64, VP]),
     "ss_binned_sums": (C.c_int, [VP, VP, C.c_int64, C.c_int32, VP, C.c_int32, VP, VP, VP]),
     "ss_peak_fma": (C.c_int, [C.c_int, C.c_int64, DP, VP, VP]),
 }

@@ -241,12 +241,37 @@ def potential_eval(P, xyz: torch.Tensor, t, phi=True, grad=True, hess=False):
     return o_phi, o_g, o_h
 
 
-def orbit(P, w0: torch.Tensor, t0: float, dt: float, n_steps: int, save_every: int) -> torch.Tensor:
+SHOOT_TOL = 1e-14
+
+
+def orbit(P, w0: torch.Tensor, t0: float, dt: float, n_steps: int, save_every: int,
+          method: str = "auto") -> torch.Tensor:
+    """Fixed-step FP64 Dopri5 orbits.  method: 'serial' (one thread per
+    orbit), 'shoot' (one orbit, parallel in time by multiple shooting; the
+    serial orbit up to round-off) or 'auto' (shoot for a single long orbit in
+    a static potential)."""
     n = w0.shape[0]
     out = torch.empty(n, n_steps // save_every + 1, 6, dtype=torch.float64, device=w0.device)
-    _abi.call("ss_orbit_f64", C.byref(P), ptr(w0), n, float(t0), float(dt), int(n_steps), int(save_every),
-              ptr(out), stream_handle())
+    if method == "auto":
+        method = "shoot" if (n == 1 and n_steps >= 64 and is_static(P)) else "serial"
+    if method == "shoot":
+        if n != 1:
+            raise ValueError("the parallel-in-time orbit integrates one orbit")
+        need = _abi.load().ss_orbit_shoot_workspace_bytes(int(n_steps))
+        ws, nb = aligned_ptr(Workspace.get(int(need), w0.device, slot="shoot"))
+        _abi.call("ss_orbit_shoot_f64", C.byref(P), ptr(w0), float(t0), float(dt), int(n_steps), int(save_every),
+                  ptr(out), ws, nb, SHOOT_TOL, stream_handle())
+    elif method == "serial":
+        _abi.call("ss_orbit_f64", C.byref(P), ptr(w0), n, float(t0), float(dt), int(n_steps), int(save_every),
+                  ptr(out), stream_handle())
+    else:
+        raise ValueError("method must be 'auto', 'serial' or 'shoot'")
     return out
+
+
+def is_static(P) -> bool:
+    """True when the descriptor has no center-track component and no subhalos."""
+    return P.subhalos.n == 0 and all(P.comp[i].center == _abi.SS_CENTER_ORIGIN for i in range(P.n_components))
 
 
 def release(P, cfg, prog_w, t_rel, msat, normals, jac=False):
@@ -264,10 +289,10 @@ class Workspace:
     _bufs = {}
 
     @classmethod
-    def get(cls, nbytes: int, dev: torch.device) -> Optional[torch.Tensor]:
+    def get(cls, nbytes: int, dev: torch.device, slot: str = "main") -> Optional[torch.Tensor]:
         if nbytes <= 0:
             return None
-        key = (dev.type, dev.index)
+        key = (dev.type, dev.index, slot)
         buf = cls._bufs.get(key)
         if buf is None or buf.numel() < nbytes:
             buf = torch.empty(int(nbytes) + 256, dtype=torch.uint8, device=dev)

@@ -10,7 +10,7 @@
 #include <atomic>
 #include <cmath>
 
-#include "ss_common.cuh"
+#include "ss_release.cuh"
 
 namespace ssg {
 
@@ -191,6 +191,7 @@ __global__ void potential_eval_kernel(PotDev<double> P, const double* __restrict
 }
 
 // ------------------------------------------------------------- orbits
+template <class C>
 __global__ void __launch_bounds__(64) orbit_f64_kernel(PotDev<double> P, const double* __restrict__ w0,
                                                        int64_t n_orbits, double t0, double dt, int64_t n_steps,
                                                        int64_t save_every, double* __restrict__ out) {
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(64) orbit_f64_kernel(PotDev<double> P, const d
     double* base = out + o * n_save * 6;
     for (int i = 0; i < 6; ++i) base[i] = y[i];
     for (int64_t n = 0; n < n_steps; ++n) {
-        dopri5_step_f64(P, t0 + (double)n * dt, dt, y);
+        dopri5_step_f64<C>(P, t0 + (double)n * dt, dt, y);
         if ((n + 1) % save_every == 0) {
             double* b = base + 6 * ((n + 1) / save_every);
             for (int i = 0; i < 6; ++i) b[i] = y[i];
@@ -231,84 +232,6 @@ __global__ void track_slopes_kernel(const double* __restrict__ knots, int64_t n,
         s = 0.5 * (sl + sr);
     }
     slopes[i] = s;
-}
-
-// ------------------------------------------------------------- release
-// tidal radius pieces, templated on double / Dual<6>:
-// omega (main.py:88-96), d2phidr2 (main.py:76-85), tidalr (main.py:98-104).
-template <class T>
-__device__ T release_tidal_radius(const PotDev<double>& P, const T x[3], const T v[3], double GMsat, double t,
-                                  T rh[3], T zh[3], T ph[3], T& om) {
-    T r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
-    T r = s_sqrt(r2);
-    T ir = s_rcp(r);
-    rh[0] = x[0] * ir; rh[1] = x[1] * ir; rh[2] = x[2] * ir;
-    T L[3] = {x[1] * v[2] - x[2] * v[1], x[2] * v[0] - x[0] * v[2], x[0] * v[1] - x[1] * v[0]};
-    T L2 = L[0] * L[0] + L[1] * L[1] + L[2] * L[2];
-    T Ln = s_sqrt(L2);
-    om = Ln * s_rcp(r2);
-    T iLn = s_rcp(Ln);
-    zh[0] = L[0] * iLn; zh[1] = L[1] * iLn; zh[2] = L[2] * iLn;
-    T vr = v[0] * rh[0] + v[1] * rh[1] + v[2] * rh[2];
-    T pv[3] = {v[0] - vr * rh[0], v[1] - vr * rh[1], v[2] - vr * rh[2]};
-    T ipn = s_rsqrt(pv[0] * pv[0] + pv[1] * pv[1] + pv[2] * pv[2]);
-    ph[0] = pv[0] * ipn; ph[1] = pv[1] * ipn; ph[2] = pv[2] * ipn;
-    double c[3] = {0.0, 0.0, 0.0};
-    if (P.has_track) track_eval(P.track, t, c);
-    T xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
-    T g[3], H[6];
-    pot_grad<T, double, true>(P, x, xs, g, H);
-    // r_hat^T H r_hat
-    T d2 = H[0] * rh[0] * rh[0] + H[1] * rh[1] * rh[1] + H[2] * rh[2] * rh[2] +
-           2.0 * (H[3] * rh[0] * rh[1] + H[4] * rh[0] * rh[2] + H[5] * rh[1] * rh[2]);
-    return s_cbrt(GMsat * s_rcp(om * om - d2));
-}
-
-template <class T>
-__device__ void release_one(const PotDev<double>& P, double G, const ss_release_cfg& cfg, const T x[3],
-                            const T v[3], double Msat, double t, const double* z, T out[2][6]) {
-    T rh[3], zh[3], ph[3], om;
-    T rt = release_tidal_radius<T>(P, x, v, G * Msat, t, rh, zh, ph, om);
-    if (cfg.model == SS_RELEASE_CHEN25) {
-        // release_model_Chen25, streamhelpers.py:352-432
-        double pvs[6];
-        for (int i = 0; i < 6; ++i) {
-            double s = cfg.chen_mean[i];
-            for (int j = 0; j < 6; ++j) s += cfg.chen_L[6 * i + j] * z[j];
-            pvs[i] = s;
-        }
-        T Dr = pvs[0] * rt;
-        T vesc = s_sqrt(2.0 * G * Msat * s_rcp(Dr));
-        T Dv = pvs[3] * vesc;
-        const double deg = 0.017453292519943295;
-        double phi = pvs[1] * deg, theta = pvs[2] * deg, alpha = pvs[4] * deg, beta = pvs[5] * deg;
-        double ct = cos(theta), st = sin(theta), cp = cos(phi), sp = sin(phi);
-        double ca = cos(alpha), sa = sin(alpha), cb = cos(beta), sb = sin(beta);
-        for (int i = 0; i < 3; ++i) {
-            T ax = (Dr * (ct * cp)) * rh[i], ay = (Dr * (ct * sp)) * ph[i], az = (Dr * st) * zh[i];
-            T bx = (Dv * (cb * ca)) * rh[i], by = (Dv * (cb * sa)) * ph[i], bz = (Dv * sb) * zh[i];
-            out[1][i] = x[i] + ax + ay + az;
-            out[1][3 + i] = v[i] + bx + by + bz;
-            out[0][i] = x[i] - ax - ay + az;
-            out[0][3 + i] = v[i] - bx - by + bz;
-        }
-    } else {
-        // Potential.release_model, main.py:209-280
-        const double* kv = cfg.kvals;
-        double kr = kv[0] + z[0] * kv[4];
-        double kvphi = kr * (kv[1] + z[1] * kv[5]);
-        double kz = kv[2] + z[2] * kv[6];
-        double kvz = kv[3] + z[3] * kv[7];
-        T vc = om * rt;
-        for (int i = 0; i < 3; ++i) {
-            T dpos = (kr * rt) * rh[i] + (kz * rt) * zh[i];
-            T dvel = (kvphi * vc) * ph[i] + (kvz * vc) * zh[i];
-            out[1][i] = x[i] + dpos;      // trailing: nudged out
-            out[1][3 + i] = v[i] + dvel;
-            out[0][i] = x[i] - dpos;      // leading: nudged in
-            out[0][3 + i] = v[i] - dvel;
-        }
-    }
 }
 
 template <bool JAC>
@@ -453,8 +376,11 @@ int ss_orbit_f64(const ss_potential* pot, const double* w0, int64_t n_orbits, do
     SS_CHECK_ARG(std::isfinite(dt) && dt != 0.0 && std::isfinite(t0), "dt must be finite and non-zero");
     if (n_orbits == 0) return SS_OK;
     SS_CHECK_ARG(w0 && out, "NULL buffer");
-    orbit_f64_kernel<<<grid_for(n_orbits, 64), 64, 0, (cudaStream_t)stream>>>(P, w0, n_orbits, t0, dt, n_steps,
-                                                                            save_every, out);
+    dispatch_comp(P, [&](auto comp) {
+        orbit_f64_kernel<decltype(comp)><<<grid_for(n_orbits, 64), 64, 0, (cudaStream_t)stream>>>(
+            P, w0, n_orbits, t0, dt, n_steps, save_every, out);
+        return 0;
+    });
     SS_LAUNCH_CHECK();
     return SS_OK;
 }

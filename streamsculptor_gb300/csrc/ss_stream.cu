@@ -30,248 +30,9 @@
 
 #include <cmath>
 
-#include "ss_common.cuh"
+#include "ss_stream.cuh"
 
 namespace ssg {
-
-struct StreamArgs {
-    const double* ics;
-    double* final_w;
-    float* snaps;
-    int32_t* status;
-    int64_t N;
-    int32_t ppr;
-    int32_t spr;
-    int32_t n_steps;
-    int32_t stride;
-    double t0;
-    double dt;
-    // f32k only
-    float h_hi;
-    float h_lo;
-    const float4* ctab;   // [(n_steps*5+1) x 2] track positions (hi, lo) at stage times
-    const float4* shtab;  // [n_sh*3] subhalo lines
-    int32_t n_sh;
-    int32_t sh_kind;
-};
-
-// Write the snapshot k for lane state y (or NaN when not yet released).
-template <class T>
-__device__ __forceinline__ void write_snap(float* snaps, int64_t N, int64_t k, int64_t p, bool exists, const T y[6]) {
-    float2* o = reinterpret_cast<float2*>(snaps + (k * N + p) * 6);
-    const float nanf_ = __int_as_float(0x7fc00000);
-    if (exists) {
-        o[0] = make_float2((float)y[0], (float)y[1]);
-        o[1] = make_float2((float)y[2], (float)y[3]);
-        o[2] = make_float2((float)y[4], (float)y[5]);
-    } else {
-        o[0] = make_float2(nanf_, nanf_);
-        o[1] = make_float2(nanf_, nanf_);
-        o[2] = make_float2(nanf_, nanf_);
-    }
-}
-
-// ------------------------------------------------------------------ FP64
-__global__ void __launch_bounds__(64) stream_f64_kernel(PotDev<double> P, StreamArgs a) {
-    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = p < a.N;
-    const int start = valid ? (int)((p / a.ppr) * (int64_t)a.spr) : a.n_steps;
-    const int wstart = (int)__reduce_min_sync(0xffffffffu, (unsigned)start);
-    double y[6];
-    if (valid) {
-#pragma unroll
-        for (int i = 0; i < 6; ++i) y[i] = a.ics[6 * p + i];
-    } else {
-#pragma unroll
-        for (int i = 0; i < 6; ++i) y[i] = 0.0;
-    }
-    if (a.snaps && valid) {
-        for (int64_t k = 0; (k + 1) * (int64_t)a.stride <= wstart; ++k) {
-            int64_t step = (k + 1) * (int64_t)a.stride;
-            write_snap<double>(a.snaps, a.N, k, p, step >= start, y);
-        }
-    }
-    for (int n = wstart; n < a.n_steps; ++n) {
-        if (valid && n >= start) dopri5_step_f64(P, a.t0 + (double)n * a.dt, a.dt, y);
-        if (a.snaps && (n + 1) % a.stride == 0 && valid)
-            write_snap<double>(a.snaps, a.N, (n + 1) / a.stride - 1, p, n + 1 >= start, y);
-    }
-    if (!valid) return;
-    bool ok = true;
-#pragma unroll
-    for (int i = 0; i < 6; ++i) ok = ok && isfinite(y[i]);
-    if (a.status) a.status[p] = ok ? 0 : 1;
-    if (a.final_w) {
-#pragma unroll
-        for (int i = 0; i < 6; ++i) a.final_w[6 * p + i] = y[i];
-    }
-}
-
-// ------------------------------------------------------------------ FP32-K
-#define F_C2 0.2f
-#define F_C3 0.3f
-#define F_C4 0.8f
-#define F_C5 ((float)(8.0 / 9.0))
-#define F_(x) ((float)(x))
-
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-    s = a + b;
-    float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
-
-// Acceleration at the stage position xh + d (xh: the particle's hi part,
-// d: the small remainder of the stage offset).  Components on the center
-// track use (xh - c_hi) + (d - c_lo): xh and c_hi are close, so the
-// difference is exact and the separation keeps its relative precision.
-__device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamArgs& a, const float xh[3],
-                                          const float d[3], int slot, float trel, float A[3]) {
-    const float X[3] = {xh[0] + d[0], xh[1] + d[1], xh[2] + d[2]};
-    float xs[3] = {X[0], X[1], X[2]};
-    if (P.has_track) {
-        const float4 ch = __ldg(a.ctab + 2 * slot);
-        const float4 cl = __ldg(a.ctab + 2 * slot + 1);
-        xs[0] = (xh[0] - ch.x) + (d[0] - cl.x);
-        xs[1] = (xh[1] - ch.y) + (d[1] - cl.y);
-        xs[2] = (xh[2] - ch.z) + (d[2] - cl.z);
-    }
-    float g[3];
-    pot_grad<float, float, false>(P, X, xs, g, nullptr);
-#pragma unroll 1
-    for (int j = 0; j < a.n_sh; ++j) {
-        float4 s0 = __ldg(a.shtab + 3 * j);
-        float4 s1 = __ldg(a.shtab + 3 * j + 1);
-        float4 s2 = __ldg(a.shtab + 3 * j + 2);
-        float tau = trel - s2.x;
-        if (!(fabsf(tau) < s2.y)) continue;
-        float rel[3] = {X[0] - (s0.x + s1.x * trel), X[1] - (s0.y + s1.y * trel), X[2] - (s0.z + s1.z * trel)};
-        float gp[3], dummy[3];
-        subhalo_grad<float, false>(a.sh_kind, s0.w, s1.w, rel, gp, dummy);
-        g[0] += gp[0];
-        g[1] += gp[1];
-        g[2] += gp[2];
-    }
-    A[0] = -g[0];
-    A[1] = -g[1];
-    A[2] = -g[2];
-}
-
-// One compensated step.  V_i = vh + d_i and sum_j a_ij = c_i, sum_i b_i = 1
-// are used exactly, so only the small parts d_i and A_i - A_1 see the
-// rounded tableau.
-__device__ __forceinline__ void step_f32k(const PotDev<float>& P, const StreamArgs& a, int n, float xh[3],
-                                          float xl[3], float vh[3], float vl[3]) {
-    const float h = a.h_hi;
-    const float tn = (float)n * h;  // time since global step 0 (subhalo lines)
-    const int s0 = 5 * n;
-    float A1[3], A2[3], A3[3], A4[3], A5[3], A6[3];
-    float d1[3], d2[3], d3[3], d4[3], d5[3], d6[3];
-    float D[3];  // stage position offset from xh (small)
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        D[i] = xl[i];
-        d1[i] = vl[i];
-    }
-    accel_f32(P, a, xh, D, s0, tn, A1);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        d2[i] = vl[i] + h * (F_(SS_A21) * A1[i]);
-        D[i] = xl[i] + h * (F_C2 * vh[i] + F_(SS_A21) * d1[i]);
-    }
-    accel_f32(P, a, xh, D, s0 + 1, tn + F_C2 * h, A2);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        d3[i] = vl[i] + h * (F_(SS_A31) * A1[i] + F_(SS_A32) * A2[i]);
-        D[i] = xl[i] + h * (F_C3 * vh[i] + F_(SS_A31) * d1[i] + F_(SS_A32) * d2[i]);
-    }
-    accel_f32(P, a, xh, D, s0 + 2, tn + F_C3 * h, A3);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        d4[i] = vl[i] + h * (F_(SS_A41) * A1[i] + F_(SS_A42) * A2[i] + F_(SS_A43) * A3[i]);
-        D[i] = xl[i] + h * (F_C4 * vh[i] + F_(SS_A41) * d1[i] + F_(SS_A42) * d2[i] + F_(SS_A43) * d3[i]);
-    }
-    accel_f32(P, a, xh, D, s0 + 3, tn + F_C4 * h, A4);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        d5[i] = vl[i] + h * (F_(SS_A51) * A1[i] + F_(SS_A52) * A2[i] + F_(SS_A53) * A3[i] + F_(SS_A54) * A4[i]);
-        D[i] = xl[i] + h * (F_C5 * vh[i] + F_(SS_A51) * d1[i] + F_(SS_A52) * d2[i] + F_(SS_A53) * d3[i] +
-                            F_(SS_A54) * d4[i]);
-    }
-    accel_f32(P, a, xh, D, s0 + 4, tn + F_C5 * h, A5);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        d6[i] = vl[i] + h * (F_(SS_A61) * A1[i] + F_(SS_A62) * A2[i] + F_(SS_A63) * A3[i] + F_(SS_A64) * A4[i] +
-                             F_(SS_A65) * A5[i]);
-        D[i] = xl[i] + h * (vh[i] + F_(SS_A61) * d1[i] + F_(SS_A62) * d2[i] + F_(SS_A63) * d3[i] +
-                            F_(SS_A64) * d4[i] + F_(SS_A65) * d5[i]);
-    }
-    accel_f32(P, a, xh, D, s0 + 5, tn + h, A6);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        // position: h * (vh + Db), Db = sum b_i d_i
-        float Db = F_(SS_B1) * d1[i] + F_(SS_B3) * d3[i] + F_(SS_B4) * d4[i] + F_(SS_B5) * d5[i] + F_(SS_B6) * d6[i];
-        float pp = h * vh[i];
-        float pe = fmaf(h, vh[i], -pp);
-        float lo = pe + (a.h_lo * vh[i] + h * Db);
-        float s, e;
-        two_sum(xh[i], pp, s, e);
-        float l2 = xl[i] + (e + lo);
-        xh[i] = s + l2;
-        xl[i] = l2 - (xh[i] - s);
-        // velocity: h * (A1 + sum_{i>=3} b_i (A_i - A1))
-        float Sv = A1[i] + (F_(SS_B3) * (A3[i] - A1[i]) + F_(SS_B4) * (A4[i] - A1[i]) + F_(SS_B5) * (A5[i] - A1[i]) +
-                            F_(SS_B6) * (A6[i] - A1[i]));
-        float qp = h * Sv;
-        float qe = fmaf(h, Sv, -qp) + a.h_lo * Sv;
-        two_sum(vh[i], qp, s, e);
-        l2 = vl[i] + (e + qe);
-        vh[i] = s + l2;
-        vl[i] = l2 - (vh[i] - s);
-    }
-}
-
-__global__ void __launch_bounds__(128) stream_f32k_kernel(PotDev<float> P, StreamArgs a) {
-    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = p < a.N;
-    const int start = valid ? (int)((p / a.ppr) * (int64_t)a.spr) : a.n_steps;
-    const int wstart = (int)__reduce_min_sync(0xffffffffu, (unsigned)start);
-    float xh[3], xl[3], vh[3], vl[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        double xd = valid ? a.ics[6 * p + i] : 0.0;
-        double vd = valid ? a.ics[6 * p + 3 + i] : 0.0;
-        xh[i] = (float)xd;
-        xl[i] = (float)(xd - (double)xh[i]);
-        vh[i] = (float)vd;
-        vl[i] = (float)(vd - (double)vh[i]);
-    }
-    if (a.snaps && valid) {
-        float y[6] = {xh[0], xh[1], xh[2], vh[0], vh[1], vh[2]};
-        for (int64_t k = 0; (k + 1) * (int64_t)a.stride <= wstart; ++k) {
-            int64_t step = (k + 1) * (int64_t)a.stride;
-            write_snap<float>(a.snaps, a.N, k, p, step >= start, y);
-        }
-    }
-    for (int n = wstart; n < a.n_steps; ++n) {
-        if (valid && n >= start) step_f32k(P, a, n, xh, xl, vh, vl);
-        if (a.snaps && (n + 1) % a.stride == 0 && valid) {
-            float y[6] = {xh[0], xh[1], xh[2], vh[0], vh[1], vh[2]};
-            write_snap<float>(a.snaps, a.N, (n + 1) / a.stride - 1, p, n + 1 >= start, y);
-        }
-    }
-    if (!valid) return;
-    bool ok = true;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) ok = ok && isfinite(xh[i]) && isfinite(vh[i]) && isfinite(xl[i]) && isfinite(vl[i]);
-    if (a.status) a.status[p] = ok ? 0 : 1;
-    if (a.final_w) {
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            a.final_w[6 * p + i] = (double)xh[i] + (double)xl[i];
-            a.final_w[6 * p + 3 + i] = (double)vh[i] + (double)vl[i];
-        }
-    }
-}
 
 // Track positions at every stage time of the run, FP64 Hermite -> a hi/lo
 // float pair (two float4).  Slot 5n + s holds c(t0 + (n + c_s) dt) for
@@ -365,7 +126,10 @@ int ss_stream_f64(const ss_potential* pot, const ss_stream_cfg* cfg, const doubl
     StreamArgs a = make_args(cfg, ics, final_w, snaps, status);
     const int block = 64;
     unsigned grid = (unsigned)((cfg->n_particles + block - 1) / block);
-    stream_f64_kernel<<<grid, block, 0, (cudaStream_t)stream>>>(P, a);
+    dispatch_comp(P, [&](auto comp) {
+        stream_f64_kernel<decltype(comp)><<<grid, block, 0, (cudaStream_t)stream>>>(P, a);
+        return 0;
+    });
     SS_LAUNCH_CHECK();
     return SS_OK;
 }
@@ -414,7 +178,10 @@ int ss_stream_f32k(const ss_potential* pot, const ss_stream_cfg* cfg, const doub
     }
     const int block = 128;
     unsigned grid = (unsigned)((cfg->n_particles + block - 1) / block);
-    stream_f32k_kernel<<<grid, block, 0, s>>>(P, a);
+    dispatch_comp(P, [&](auto comp) {
+        stream_f32k_kernel<decltype(comp)><<<grid, block, 0, s>>>(P, a);
+        return 0;
+    });
     SS_LAUNCH_CHECK();
     return SS_OK;
 }

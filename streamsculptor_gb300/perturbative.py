@@ -129,6 +129,83 @@ class GenerateMassRadiusPerturbation(Potential):
         return [base_out[:, 0], d[:, 0]], [base_out[:, 1], d[:, 1]]
 
 
+class BaseStreamModelChen25(Potential):
+    """Chen+25 base stream with the progenitor's own potential moving on its
+    orbit (perturbative.py:588-658).  Particles are ordered by release time,
+    lead before trail (the reference's sorted [ts, ts + 1e-12] stack)."""
+
+    def __init__(self, pot_base, ts, prog_w0, Msat, key, solver=None, rtol=1e-7, atol=1e-7, dtmin=0.3, dtmax=None,
+                 max_steps=10_000, throw=False, prog_pot=None, units=None, *, dt=None, normals=None):
+        from . import potential as P
+        from .streamhelpers import CHEN25_MEAN, chen25_factor
+        units = units if units is not None else pot_base.units
+        super().__init__(units, {"pot_base": pot_base, "ts": ts, "prog_w0": prog_w0, "Msat": Msat, "key": key,
+                                 "solver": solver, "prog_pot": prog_pot})
+        _core.check_solver(solver)
+        if prog_pot is None:
+            prog_pot = P.PlummerPotential(m=0.0, r_s=1.0, units=units)
+        self.prog_pot = prog_pot
+        ts_h = host64(ts).reshape(-1)
+        self._ts_h = ts_h
+        seed = int(np.asarray(key).ravel()[-1])
+        self.normals = normals if normals is not None else release_normals(seed, len(ts_h), 1, 6)
+        ws, self._h, self._spr = pot_base._prog_orbit(ts_h, prog_w0, dt)
+        self.prog_loc_fwd = ws
+        ics, _ = pot_base._release(ws, ts_h, Msat, self.normals, model=_abi.SS_RELEASE_CHEN25,
+                                   chen=(CHEN25_MEAN, chen25_factor()))
+        self.streamICs = ics[:, 0].reshape(-1, 6)  # [2 len(ts), 6]: lead_0, trail_0, lead_1, ...
+        track = _core.CenterTrack.from_samples(ts_h, ws[:, :3])
+        self.pot_tot = P.Potential_Combine(
+            [pot_base, P.TimeDepTranslatingPotential(prog_pot, track, units=units)], units=units)
+        self.BaseModel = self
+
+
+class GenerateMassRadiusPerturbation_Chen25(Potential):
+    """First-order response for the Chen+25 base stream (perturbative.py:661-773).
+
+    As in the reference, the perturbation initial conditions are zero
+    (perturbative.py:712) and the base potential includes the moving
+    progenitor.  compute_perturbation_OTF returns
+    [x0v0 [2 len(ts) - 1, 6], derivs [2 len(ts) - 1, N_sh, 12]] in release
+    order (lead, trail), the last trail star dropped as in the reference."""
+
+    def __init__(self, potential_base, potential_perturbation, BaseStreamModel, units=None, **kwargs):
+        super().__init__(units if units is not None else potential_base.units,
+                         {"potential_base": potential_base, "potential_perturbation": potential_perturbation,
+                          "BaseStreamModel": BaseStreamModel})
+        self.base_model = BaseStreamModel
+        self.potential_base = potential_base
+        self.sh_table = potential_perturbation.table()
+        self.num_pert = int(self.sh_table.m.shape[0])
+        self.gradientPotentialBase = BaseStreamModel.pot_tot.gradient
+        self.gradientPotentialPerturbation_per_SH = potential_perturbation.gradient_per_SH
+
+    def compute_perturbation_OTF(self, cpu=True, solver=None, rtol=1e-6, atol=1e-6, dtmin=0.05, max_steps=10_000,
+                                 dtmax=None, *, precision=64):
+        _core.check_solver(solver)
+        b = self.base_model
+        n = len(b._ts_h)
+        N = 2 * n
+        cfg = _abi.ss_pert_cfg()
+        cfg.t0, cfg.dt = float(b._ts_h[0]), float(b._h)
+        cfg.n_steps, cfg.n_particles = b._spr * (n - 1), N
+        cfg.particles_per_release, cfg.steps_per_release = 2, b._spr
+        cfg.ncol, cfg.save_stride = 12, 0
+        base_out, out = _core.pert_response(b.pot_tot._desc(), self.sh_table, cfg, int(precision),
+                                            b.streamICs.contiguous(), None)
+        return [base_out[:N - 1], out[0][:N - 1]]
+
+    def run_nonlinear_sim(self, pot_pert=None, solver=None, rtol=1e-6, atol=1e-6, dtmin=0.05, max_steps=10_000):
+        """Nonlinear Chen+25 stream in base + perturbation with the unperturbed
+        progenitor (perturbative.py:775-813): [2 (len(ts) - 1), 6], lead then trail."""
+        from .streamhelpers import gen_stream
+        b = self.base_model
+        pot_pert = pot_pert if pot_pert is not None else self.potential_perturbation
+        lead, trail = gen_stream(b.pot_base, b._ts_h, b.prog_w0, b.Msat, solver=solver, dt=b._h, release="chen25",
+                                 prog_pot=b.prog_pot, pot_pert=pot_pert, normals=b.normals)
+        return torch.cat([lead, trail], dim=0)
+
+
 class GenerateMassPerturbation(GenerateMassRadiusPerturbation):
     """Mass-only response (6 columns per subhalo) at fixed subhalo radius
     (perturbative.py:224-241; the reference's constructor references an
@@ -140,4 +217,5 @@ class GenerateMassPerturbation(GenerateMassRadiusPerturbation):
         super().__init__(potential_base, potential_perturbation, None, BaseStreamModel, units, **kw)
 
 
-__all__ = ["BaseStreamModel", "GenerateMassRadiusPerturbation", "GenerateMassPerturbation"]
+__all__ = ["BaseStreamModel", "GenerateMassRadiusPerturbation", "GenerateMassPerturbation", "BaseStreamModelChen25",
+           "GenerateMassRadiusPerturbation_Chen25"]

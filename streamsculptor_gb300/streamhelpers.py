@@ -1,9 +1,10 @@
 """Stream generators and helpers — the reference's streamhelpers.py API.
 
 `gen_stream` is the one engine behind every generator here and behind
-Potential.gen_stream_vmapped: FP64 progenitor orbit (ss_orbit_f64), release
-(ss_release_f64), optional moving-progenitor potential on a cubic track, then
-the stream kernel (ss_stream_f64 or ss_stream_f32k).
+Potential.gen_stream_vmapped: FP64 progenitor orbit (ss_orbit_shoot_f64,
+parallel in time, or ss_orbit_f64), release (ss_release_f64),
+optional moving-progenitor potential on a cubic track, then the stream kernel
+(ss_stream_f64 or ss_stream_f32k).
 """
 from __future__ import annotations
 
@@ -38,7 +39,7 @@ def chen25_factor(cov=CHEN25_COV) -> np.ndarray:
 def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=None, *, solver=None,
                kval_arr=1.0, dt=None, dtmax=None, n_particles_per_release=2, normals=None, precision="f64",
                snapshot_every=None, throw=False, release="fardal", prog_pot: Optional[Potential] = None,
-               pot_pert: Optional[Potential] = None, prog_in_pert=False, return_ics=False):
+               pot_pert: Optional[Potential] = None, prog_in_pert=False, return_ics=False, prog_method="auto"):
     """Generate a particle-spray stream on the GPU.
 
     pot_base    smooth potential (release model and integration)
@@ -49,6 +50,9 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
                 (streamhelpers.py:89-146); with prog_in_pert the progenitor
                 orbit is integrated in base + pert too (gen_stream_ics_pert)
     release     'fardal' (main.py:209-280) or 'chen25' (streamhelpers.py:352-432)
+    prog_method progenitor orbit solver (FP64 either way): 'serial', 'shoot'
+                (parallel in time, multiple shooting) or 'auto' (shoot when the
+                progenitor's potential is static)
     Returns (lead, trail) [len(ts)-1, 6] (or [len(ts)-1, n_draw, 6]); with
     snapshot_every also the float32 snapshots [n_snap, len(ts)-1, n_draw, 2, 6].
     """
@@ -58,7 +62,7 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
         raise ValueError("need at least two release times")
     total = pot_base if pot_pert is None else _pot.Potential_Combine([pot_base, pot_pert], units=pot_base.units)
     prog_src = total if (pot_pert is not None and prog_in_pert) else pot_base
-    ws, h, spr = prog_src._prog_orbit(ts_h, prog_w0, dt, None, dtmax)
+    ws, h, spr = prog_src._prog_orbit(ts_h, prog_w0, dt, None, dtmax, method=prog_method)
     n_draw = _n_draw(n_particles_per_release)
     model = _abi.SS_RELEASE_CHEN25 if release == "chen25" else _abi.SS_RELEASE_FARDAL
     if release not in ("fardal", "chen25"):

@@ -339,3 +339,51 @@ def test_edge_cases(ss):
         _core.stream(P, bad, ics, "f64")
     with pytest.raises(NotImplementedError):
         pot.integrate_orbit(w0=PROG_WF, ts=[0.0, 10.0], solver="Dopri8")
+
+
+def test_chen25_perturbation_matches_oracle(ss, oracle):
+    """GenerateMassRadiusPerturbation_Chen25: base stream in base + moving
+    progenitor, zero initial response (perturbative.py:661-773)."""
+    from streamsculptor_gb300 import perturbative, potential as P
+    from streamsculptor_gb300.streamhelpers import CHEN25_MEAN, chen25_factor
+    n_rel = 60
+    orc, back, ts, _ = _c1_setup(oracle, n_rel=n_rel)
+    rng = np.random.default_rng(21)
+    z = rng.standard_normal((n_rel + 1, 1, 6))
+    sh = dict(kind=1, m=np.array([3e6, 2e7]), a=np.array([0.3, 0.6]), x0=rng.normal(0, 8, (2, 3)),
+              v=rng.normal(0, 0.1, (2, 3)), t0=np.array([ts[20], ts[45]]), t_window=30.0)
+    prog = P.PlummerPotential(m=2e4, r_s=0.01, units=ss.usys)
+    bsm = perturbative.BaseStreamModelChen25(mw3_gpu(ss), ts, back, 2e4, 7, prog_pot=prog, normals=z)
+    pot_sh = P.SubhaloLinePotential(sh["m"], sh["a"], sh["x0"], sh["v"], sh["t0"], sh["t_window"], units=ss.usys)
+    gen = perturbative.GenerateMassRadiusPerturbation_Chen25(mw3_gpu(ss), pot_sh, bsm)
+    base, derivs = gen.compute_perturbation_OTF()
+    ws = oracle.orbit(orc, back, ts[0], 1.0, n_rel, 1)[0]
+    ics, _ = oracle.release(orc, ws, ts, 2e4, z, model_kind=1, chen=(CHEN25_MEAN, chen25_factor()))
+    model = oracle.HostModel(oracle.mw3() + [(_abi.SS_PLUMMER, 1, (2e4, 0.01))], track=(ts[0], 1.0, ws[:, :3]),
+                             subhalos=sh)
+    bo, po = oracle.pert_response(model, ts[0], 1.0, n_rel, ics.reshape(-1, 6), None, 2, 1, ncol=12)
+    N = 2 * (n_rel + 1) - 1
+    assert base.shape == (N, 6) and derivs.shape == (N, 2, 12)
+    assert phase_err(np64(base), bo[:N]) <= 1e-10
+    assert rel_err(np64(derivs), po[0][:N]) <= 1e-9
+
+
+def test_orbit_parallel_in_time_vs_oracle(ss, oracle):
+    """Multiple-shooting FP64 orbit (8000 steps back, 500 slices) against the
+    serial FP64 oracle, and the serial GPU kernel."""
+    pot = mw3_gpu(ss)
+    ts = [0.0, -1000.0, -2000.0, -3000.0, -4000.0]
+    shoot = pot.integrate_orbit(w0=PROG_WF, ts=ts, t0=0.0, t1=-4000.0, dt=0.5, method="shoot")
+    serial = pot.integrate_orbit(w0=PROG_WF, ts=ts, t0=0.0, t1=-4000.0, dt=0.5, method="serial")
+    ref = oracle.orbit(oracle.HostModel(oracle.mw3()), PROG_WF, 0.0, -0.5, 8000, 2000)[0]
+    assert phase_err(np64(shoot.ys), ref) < 1e-11
+    assert phase_err(np64(shoot.ys), np64(serial.ys)) < 1e-12
+    # a length that is not a multiple of the slice, saved every step
+    w = pot.integrate_orbit(w0=PROG_WF, ts=np.arange(0.0, 101.5, 0.5), dt=0.5, method="shoot").ys
+    ref2 = oracle.orbit(oracle.HostModel(oracle.mw3()), PROG_WF, 0.0, 0.5, 203, 1)[0]
+    assert phase_err(np64(w), ref2) < 1e-12
+    # time-dependent potentials fall back to the serial kernel
+    gpu, orc = _track_and_subhalos(ss, oracle)
+    w3, _, _ = gpu._prog_orbit(np.arange(0.0, 41.0, 2.0) - 20.0, PROG_WF, 0.5, method="shoot")
+    ref3 = oracle.orbit(orc, PROG_WF, -20.0, 0.5, 80, 4)[0]
+    assert phase_err(np64(w3), ref3) < 1e-11
