@@ -288,8 +288,27 @@ def gpu_arm(args, wl):
     ev = torch.linalg.norm(a[:, 3:] - b[:, 3:], dim=1) / torch.linalg.norm(b[:, 3:], dim=1)
     e = torch.maximum(ex, ev)
     err = {"max": float(e.max()), "p99": float(torch.quantile(e.float(), 0.99)), "median": float(e.median()),
+           "frac_above_1e-5": float((e > 1e-5).double().mean()),
            "measure": "per particle max(|dx|/|x|, |dv|/|v|) of final states, FP32-compensated vs FP64 GPU path"}
-    del l32, t32, l64, t64, a, b
+    # Sensitivity of each FP64 track to a 1e-12 relative change of the
+    # progenitor state (growth = final change / 1e-12): particles on chaotic
+    # tracks (close passages by the progenitor) amplify any rounding, FP64's
+    # included, so the FP32 error is also quoted on the regular tracks.
+    eps = 1e-12
+    wf_p = wf_d + eps * torch.cat([wf_d[:3].norm().expand(3), wf_d[3:].norm().expand(3)])
+    l64p, t64p = step("f64", wf_p, normals_d)[:2]
+    bp = torch.stack([l64p, t64p]).reshape(-1, 6)
+    gx = torch.linalg.norm(bp[:, :3] - b[:, :3], dim=1) / torch.linalg.norm(b[:, :3], dim=1)
+    gv = torch.linalg.norm(bp[:, 3:] - b[:, 3:], dim=1) / torch.linalg.norm(b[:, 3:], dim=1)
+    growth = torch.maximum(gx, gv) / eps
+    regular = growth <= 1e3
+    err["fp64_sensitivity"] = {
+        "perturbation": eps, "growth_median": float(growth.median()),
+        "growth_p99": float(torch.quantile(growth.float(), 0.99)), "growth_max": float(growth.max()),
+        "frac_growth_above_1e3": float((~regular).double().mean()),
+        "max_err_growth_le_1e3": float(e[regular].max()) if bool(regular.any()) else None,
+        "p99_err_growth_le_1e3": float(torch.quantile(e[regular].float(), 0.99)) if bool(regular.any()) else None}
+    del l32, t32, l64, t64, a, b, l64p, t64p, bp
 
     # --- e2e through the public API with host buffers
     n_snap = n_steps // snap if snap else 0
@@ -448,6 +467,63 @@ def c3_arm(args):
           "clocks": ck, "gpu_launches": launches})
 
 
+# ------------------------------------------------------------ config 5
+C5 = dict(n_rel=2000, spr=2, dt=1.0, ppr=50,
+          name="gradient of a 64-bin stream-track loss w.r.t. 14 parameters (TriaxialNFW M, r_s, q; MN M, a, b; "
+               "Hernquist M, c; progenitor w0): 2000 releases x 50 particles (1e5), 4000 steps of 1 Myr, FP32 "
+               "forward with checkpoints every 64 steps, hand-written adjoint")
+
+
+def c5_arm(args):
+    import torch
+
+    from streamsculptor_gb300 import adjoint as A
+
+    torch.cuda.set_device(0)
+    model = A.TriaxialHaloModel
+    theta = np.array([5.4e11, 15.62, 0.9, 6.8e10, 3.0, 0.28, 5e9, 1.0, 12.0, 0.0, 4.0, 0.0, 0.18, 0.04])
+    rng = np.random.Generator(np.random.PCG64(5))
+    setup = A.StreamSetup(n_rel=C5["n_rel"], spr=C5["spr"], dt=C5["dt"], ppr=C5["ppr"], msat=MSAT,
+                          normals=rng.standard_normal((C5["n_rel"] + 1, C5["ppr"] // 2, 4)))
+    theta_t = theta * (1 + 0.01 * rng.standard_normal(14)) + np.r_[np.zeros(8), 0.05 * rng.standard_normal(3),
+                                                                    1e-3 * rng.standard_normal(3)]
+    loss = A.TrackLoss(theta[-6:], A.forward_stream(model, theta_t, setup), n_bins=64)
+    work = setup.ppr * (setup.n_rel * setup.n_steps - setup.spr * setup.n_rel * (setup.n_rel - 1) // 2)
+
+    def fwd():
+        return A.forward_stream(model, theta, setup, keep=True)
+
+    def grad(final, saved):
+        th = torch.tensor(theta, dtype=torch.float64, device="cuda", requires_grad=True)
+        f = final.detach().requires_grad_(True)
+        L = loss(f)
+        L.backward()
+        return A.backward_stream(model, theta, setup, saved, f.grad)
+
+    for _ in range(args.warmup):
+        final, saved = fwd()
+        grad(final, saved)
+    torch.cuda.synchronize()
+    tf, tb = 0.0, 0.0
+    for _ in range(args.steps):
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record()
+        final, saved = fwd()
+        e1.record()
+        g = grad(final, saved)
+        e2.record()
+        torch.cuda.synchronize()
+        tf += e0.elapsed_time(e1)
+        tb += e1.elapsed_time(e2)
+    K = args.steps
+    emit({"metric": "adjoint gradient cost / forward stream cost", "value": tb / tf, "unit": "ratio",
+          "higher_is_better": False, "n_gpus": 1, "steps": K, "warmup": args.warmup,
+          "forward_ms": tf / K, "gradient_ms": tb / K,
+          "forward_particle_steps_per_s": work / (tf / K * 1e-3), "dtype": "f32 forward and adjoint, f64 progenitor",
+          "data": "synthetic (seeded)", "config": {"workload": C5["name"], "particle_steps": work},
+          "grad_norm": float(torch.linalg.norm(g))})
+
+
 def traffic_for(kernel):
     """DRAM bytes per launch from the committed ncu summary, if present."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
@@ -464,7 +540,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["c3", "c3s"], default="c2")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["c3", "c3s", "c5"], default="c2")
     ap.add_argument("--f64-steps", type=int, default=2)
     ap.add_argument("--f64-warmup", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -472,6 +548,9 @@ def main():
     args = ap.parse_args()
     if args.workload in ("c3", "c3s"):
         c3_arm(args)
+        return
+    if args.workload == "c5":
+        c5_arm(args)
         return
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":

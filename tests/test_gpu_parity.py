@@ -379,8 +379,8 @@ def test_orbit_parallel_in_time_vs_oracle(ss, oracle):
     assert phase_err(np64(shoot.ys), ref) < 1e-11
     assert phase_err(np64(shoot.ys), np64(serial.ys)) < 1e-12
     # a length that is not a multiple of the slice, saved every step
-    w = pot.integrate_orbit(w0=PROG_WF, ts=np.arange(0.0, 101.5, 0.5), dt=0.5, method="shoot").ys
-    ref2 = oracle.orbit(oracle.HostModel(oracle.mw3()), PROG_WF, 0.0, 0.5, 203, 1)[0]
+    w = pot.integrate_orbit(w0=PROG_WF, ts=np.arange(0.0, 101.5, 0.5), dt=0.5, method="shoot").ys  # 202 steps
+    ref2 = oracle.orbit(oracle.HostModel(oracle.mw3()), PROG_WF, 0.0, 0.5, 202, 1)[0]
     assert phase_err(np64(w), ref2) < 1e-12
     # time-dependent potentials fall back to the serial kernel
     gpu, orc = _track_and_subhalos(ss, oracle)
