@@ -43,6 +43,10 @@ WORKLOADS = {
     "c2s": dict(n_rel=4000, ppr=50, dt=0.5, spr=2, snap=50, moving=True,
                 name="profiling case shaped like c2: 4000 releases x 50 particles (2e5), 4 Gyr at dt=0.5 Myr, "
                      "NFW+MN+Hernquist + moving Plummer progenitor, float32 snapshots every 50 steps"),
+    "c4x": dict(n_rel=3000, ppr=334, dt=1.0, spr=1, snap=0, moving=False, potential="expansion",
+                name="spray stream, 3000 releases x 334 particles (1.0e6), 3 Gyr at dt=1 Myr, triaxial halo as a "
+                     "spherical-harmonic expansion (l_max=8, 64 log knots over 0.1-200 kpc, seeded 2^-l "
+                     "coefficients), exact expansion force, final state only"),
     "c1": dict(n_rel=3000, ppr=2, dt=1.0, spr=1, snap=0, moving=False,
                name="spray stream, 3000 releases x 2 particles (6000), 3 Gyr at dt=1 Myr, NFW+MN+Hernquist, "
                     "final state only"),
@@ -192,9 +196,12 @@ def gpu_arm(args, wl):
     dev = torch.device("cuda", local)
     lib = _abi.load()
     u = ss.usys
-    pot = P.Potential_Combine([P.NFWPotential(m=5.4e11, r_s=15.62, units=u),
-                               P.MiyamotoNagaiDisk(m=6.8e10, a=3.0, b=0.28, units=u),
-                               P.HernquistPotential(m=5e9, r_s=1.0, units=u)], units=u)
+    if wl.get("potential") == "expansion":
+        pot = P.seeded_triaxial_expansion(units=u)
+    else:
+        pot = P.Potential_Combine([P.NFWPotential(m=5.4e11, r_s=15.62, units=u),
+                                   P.MiyamotoNagaiDisk(m=6.8e10, a=3.0, b=0.28, units=u),
+                                   P.HernquistPotential(m=5e9, r_s=1.0, units=u)], units=u)
     prog = P.PlummerPotential(m=MSAT, r_s=0.01, units=u) if wl["moving"] else None
     n_rel, ppr, dt, spr, snap = wl["n_rel"], wl["ppr"], wl["dt"], wl["spr"], wl["snap"]
     n_steps = n_rel * spr

@@ -45,6 +45,9 @@ typedef enum ss_status {
  *   SS_HERNQUIST      p = {m, r_s, soft}           HernquistPotential    potential.py:132-138
  *   SS_PLUMMER        p = {m, r_s}                 PlummerPotential      potential.py:124-130
  *   SS_ISOCHRONE      p = {m, a}                   Isochrone             potential.py:114-122
+ *   SS_SH_EXPANSION   p = {scale}                  the potential's ss_expansion table times scale
+ *                     (a multipole expansion in place of the reference's optional bfeax
+ *                     package; at most one expansion per potential)
  * A component with center = SS_CENTER_TRACK is evaluated at x - c(t), where
  * c(t) is the potential's center track: TimeDepTranslatingPotential,
  * potential.py:448-462.  Components are summed in list order
@@ -55,8 +58,12 @@ typedef enum ss_kind {
     SS_MIYAMOTO_NAGAI = 3,
     SS_HERNQUIST = 4,
     SS_PLUMMER = 5,
-    SS_ISOCHRONE = 6
+    SS_ISOCHRONE = 6,
+    SS_SH_EXPANSION = 7
 } ss_kind;
+
+/* Largest degree of a spherical-harmonic expansion. */
+#define SS_SHEXP_LMAX 8
 
 enum { SS_CENTER_ORIGIN = 0, SS_CENTER_TRACK = 1 };
 
@@ -97,6 +104,25 @@ typedef struct ss_subhalos {
     double t_window;    /* +inf = always active */
 } ss_subhalos;
 
+/* Real spherical-harmonic expansion with spline radial functions:
+ *   Phi(x) = sum_{l<=l_max} sum_{m=-l..l} f_lm(r) Y_lm(theta, phi)
+ * with Schmidt semi-normalised real harmonics
+ *   Y_l0 = P_l(cos theta),
+ *   Y_lm = sqrt(2 (l-m)!/(l+m)!) P_l^m(cos theta) cos(m phi)     (m > 0),
+ *   Y_l,-m = sqrt(2 (l-m)!/(l+m)!) P_l^m(cos theta) sin(m phi)  (m > 0),
+ * P_l^m without the Condon-Shortley phase.  Term j = l*l + l + m.  Each
+ * f_lm is a cubic Hermite spline in u = ln r through n_knots knots at
+ * u_k = log_r0 + k*dlog_r, given by its value and du-derivative at each
+ * knot; outside the knots it continues linearly in u.  coef is a device
+ * pointer [n_knots][(l_max+1)^2][2] (value, d/du). */
+typedef struct ss_expansion {
+    int32_t l_max;        /* 0..SS_SHEXP_LMAX */
+    int32_t n_knots;      /* >= 2 */
+    double log_r0;
+    double dlog_r;        /* > 0 */
+    const double* coef;
+} ss_expansion;
+
 typedef struct ss_potential {
     double G;
     int32_t n_components;
@@ -106,6 +132,8 @@ typedef struct ss_potential {
     /* When subhalos.n > 0 their summed potential is part of this potential
      * (Potential_Combine([pot_base, pot_pert]), streamhelpers.py:89-146). */
     ss_subhalos subhalos;
+    /* Table of the SS_SH_EXPANSION component (unused otherwise). */
+    ss_expansion expansion;
 } ss_potential;
 
 /* ------------------------------------------------------------- configs */
@@ -332,6 +360,64 @@ int ss_binned_sums(const double* values, const double* key, int64_t n, int32_t n
  * *out_flops = flops the launch executes; sink: device buffer of >= 512
  * floats (never written in practice). */
 int ss_peak_fma(int precision, int64_t iters, double* out_flops, float* sink, void* stream);
+
+/* ---------------------------------------------------- MLP force surrogate
+ * A learned potential for expensive expansion potentials:
+ *   Phi(x) ~ out_scale * N(u) + out_shift,
+ *   u = ((x - in_shift[0]) in_scale[0], (y - in_shift[1]) in_scale[1],
+ *        (z - in_shift[2]) in_scale[2], (ln r - in_shift[3]) in_scale[3]),
+ *   N: 4 -> 128 -> 128 -> 128 -> 128 -> 1 with SiLU after each hidden layer;
+ * the force is the network's analytic input gradient (hand-written
+ * backward).  params: device FP32, packed as
+ *   W1 [128][4], b1 [128], W2 [128][128], b2 [128], W3, b3, W4, b4,
+ *   w5 [128], b5 [1]   (W[out][in], SS_MLP_NPARAM floats). */
+#define SS_MLP_WIDTH 128
+#define SS_MLP_NPARAM (128 * 4 + 128 + 3 * (128 * 128 + 128) + 128 + 1)
+
+typedef struct ss_mlp {
+    const float* params;
+    float in_scale[4];
+    float in_shift[4];
+    float out_scale;
+    float out_shift;
+} ss_mlp;
+
+/* FP32 evaluation (CUDA cores) of Phi and grad Phi at n points xyz [n,3]
+ * (either output may be NULL).  Workspace: ss_mlp_eval_workspace_bytes(n). */
+int64_t ss_mlp_eval_workspace_bytes(int64_t n);
+int ss_mlp_eval(const ss_mlp* mlp, const double* xyz, int64_t n, double* phi, double* grad,
+                void* workspace, int64_t workspace_bytes, void* stream);
+
+/* Training loss of one batch and its gradient with respect to params:
+ *   L = sum_b w_val[b] (Phi_b - phi_t[b])^2 + w_force[b] |grad Phi_b - g_t[b]|^2
+ * (Sobolev training: the force term is differentiated through the network's
+ * input gradient).  x [B,3], phi_t [B], g_t [B,3] (grad Phi targets),
+ * w_val, w_force [B] FP32 device arrays.  Writes loss[0] (value part),
+ * loss[1] (force part) and grad [SS_MLP_NPARAM] (overwritten).
+ * Workspace: ss_mlp_train_workspace_bytes(B). */
+int64_t ss_mlp_train_workspace_bytes(int64_t batch);
+int ss_mlp_loss_grad(const ss_mlp* mlp, const float* x, const float* phi_t, const float* g_t,
+                     const float* w_val, const float* w_force, int64_t batch, float* loss, float* grad,
+                     void* workspace, int64_t workspace_bytes, void* stream);
+
+/* One Adam step (bias-corrected; step counts from 1) on n parameters. */
+int ss_mlp_adam(float* params, const float* grad, float* m, float* v, int64_t n, int64_t step, float lr,
+                float beta1, float beta2, float eps, void* stream);
+
+/* grad Phi of the surrogate at xyz [n,3] through the tensor-core path of
+ * ss_stream_mlp_bf16 (BF16 weights and activations, FP32 accumulation).
+ * status [n] (optional): 0, or 2 if a tensor-core wait timed out. */
+int ss_mlp_grad_bf16(const ss_mlp* mlp, const double* xyz, int64_t n, double* grad, int32_t* status,
+                     void* stream);
+
+/* Particle-spray stream with the surrogate's force on the tensor cores
+ * (tcgen05, BF16 weights and activations, FP32 accumulation in TMEM), FP32
+ * compensated state, FP64 time: the ss_stream_f32k contract with the force
+ * of `mlp` in place of a potential.  Workspace:
+ * ss_stream_mlp_workspace_bytes(cfg). */
+int64_t ss_stream_mlp_workspace_bytes(const ss_stream_cfg* cfg);
+int ss_stream_mlp_bf16(const ss_mlp* mlp, const ss_stream_cfg* cfg, const double* ics, double* final_w,
+                       float* snaps, int32_t* status, void* workspace, int64_t workspace_bytes, void* stream);
 
 #ifdef __cplusplus
 }

@@ -78,6 +78,7 @@ class HostModel:
     G: float = G_KPC
     track: Optional[Tuple[float, float, np.ndarray]] = None  # (t0, dt, knots [n,3])
     subhalos: Optional[dict] = None  # kind, m, a, x0, v, t0, t_window
+    expansion: Optional[tuple] = None  # (l_max, log_r0, dlog_r, coef [n_knots, (l_max+1)^2, 2])
     _keep: list = field(default_factory=list)
 
     def struct(self) -> _abi.ss_potential:
@@ -101,6 +102,15 @@ class HostModel:
             P.track.n_knots = knots.shape[0]
         if self.subhalos is not None:
             P.subhalos = self.sh_struct()
+        if self.expansion is not None:
+            l_max, log_r0, dlog_r, coef = self.expansion
+            coef = f8(coef)
+            self._keep.append(coef)
+            P.expansion.l_max = int(l_max)
+            P.expansion.n_knots = coef.shape[0]
+            P.expansion.log_r0 = float(log_r0)
+            P.expansion.dlog_r = float(dlog_r)
+            P.expansion.coef = coef.ctypes.data
         return P
 
     def sh_struct(self) -> _abi.ss_subhalos:

@@ -239,6 +239,70 @@ S phi_subhalo(int kind, double G, double m, const S& a, const double x0[3], cons
     return -G * m / (sqrt_(r2) + a);
 }
 
+// Spherical-harmonic expansion (SS_SH_EXPANSION): restated from the
+// definition in the C header with spherical angles and the textbook
+// associated-Legendre recurrence in cos(theta) (no Condon-Shortley phase),
+//   P_m^m = (2m-1)!! sin^m(theta),  P_{m+1}^m = (2m+1) cos(theta) P_m^m,
+//   (l-m) P_l^m = (2l-1) cos(theta) P_{l-1}^m - (l+m-1) P_{l-2}^m,
+// cos(m phi), sin(m phi) by the angle-addition recurrence, Schmidt factors
+// sqrt(2 (l-m)!/(l+m)!), and the radial cubic Hermite spline in ln r with
+// linear continuation outside the knots.  (The product kernels use Cartesian
+// solid harmonics and analytic derivatives instead.)
+template <class S>
+S phi_expansion(const ss_expansion& E, double scale, const S x[3]) {
+    const int L = E.l_max, nt = (L + 1) * (L + 1);
+    S rho2 = x[0] * x[0] + x[1] * x[1];
+    S r = sqrt_(rho2 + x[2] * x[2]);
+    S rho = sqrt_(rho2);
+    S ct = x[2] / r, st = rho / r, cp = x[0] / rho, sp = x[1] / rho;
+    // radial spline
+    S u = log_(r);
+    double us = (value(u) - E.log_r0) / E.dlog_r;
+    int k = (int)std::floor(us);
+    if (k < 0) k = 0;
+    if (k > E.n_knots - 2) k = E.n_knots - 2;
+    S s = (u - (E.log_r0 + k * E.dlog_r)) / E.dlog_r;
+    S sc = s;
+    if (value(s) < 0.0) sc = S(0.0);
+    if (value(s) > 1.0) sc = S(1.0);
+    S ext = s - sc;
+    S h00 = (1.0 + 2.0 * sc) * (1.0 - sc) * (1.0 - sc), h10 = sc * (1.0 - sc) * (1.0 - sc);
+    S h01 = sc * sc * (3.0 - 2.0 * sc), h11 = sc * sc * (sc - 1.0);
+    S d00 = 6.0 * sc * (sc - 1.0), d10 = (1.0 - sc) * (1.0 - 3.0 * sc), d01 = 6.0 * sc * (1.0 - sc),
+      d11 = sc * (3.0 * sc - 2.0);
+    auto radial = [&](int j) {
+        const double* a = E.coef + ((size_t)k * nt + j) * 2;
+        const double* b = a + 2 * nt;
+        double f0 = a[0], g0 = a[1] * E.dlog_r, f1 = b[0], g1 = b[1] * E.dlog_r;
+        S fs = d00 * f0 + d10 * g0 + d01 * f1 + d11 * g1;
+        return h00 * f0 + h10 * g0 + h01 * f1 + h11 * g1 + ext * fs;
+    };
+    // associated Legendre functions P[l][m] and cos/sin(m phi)
+    S P[SS_SHEXP_LMAX + 1][SS_SHEXP_LMAX + 1];
+    S cm[SS_SHEXP_LMAX + 1], sm[SS_SHEXP_LMAX + 1];
+    cm[0] = S(1.0);
+    sm[0] = S(0.0);
+    for (int m = 1; m <= L; ++m) {
+        cm[m] = cm[m - 1] * cp - sm[m - 1] * sp;
+        sm[m] = sm[m - 1] * cp + cm[m - 1] * sp;
+    }
+    P[0][0] = S(1.0);
+    for (int m = 1; m <= L; ++m) P[m][m] = (2.0 * m - 1.0) * st * P[m - 1][m - 1];
+    for (int m = 0; m < L; ++m) P[m + 1][m] = (2.0 * m + 1.0) * ct * P[m][m];
+    for (int m = 0; m <= L; ++m)
+        for (int l = m + 2; l <= L; ++l)
+            P[l][m] = ((2.0 * l - 1.0) * ct * P[l - 1][m] - (l + m - 1.0) * P[l - 2][m]) / (double)(l - m);
+    S phi(0.0);
+    for (int l = 0; l <= L; ++l) {
+        phi = phi + radial(l * l + l) * P[l][0];
+        for (int m = 1; m <= l; ++m) {
+            double norm = std::sqrt(2.0 * std::tgamma(l - m + 1.0) / std::tgamma(l + m + 1.0));
+            phi = phi + norm * P[l][m] * (radial(l * l + l + m) * cm[m] + radial(l * l + l - m) * sm[m]);
+        }
+    }
+    return scale * phi;
+}
+
 template <class S>
 S phi_total(const ss_potential& P, const S x[3], double t) {
     S acc(0.0);
@@ -252,9 +316,11 @@ S phi_total(const ss_potential& P, const S x[3], double t) {
                 have_c = true;
             }
             S xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
-            acc = acc + phi_component(comp, P.G, xs);
+            acc = acc + (comp.kind == SS_SH_EXPANSION ? phi_expansion(P.expansion, comp.p[0], xs)
+                                                      : phi_component(comp, P.G, xs));
         } else {
-            acc = acc + phi_component(comp, P.G, x);
+            acc = acc + (comp.kind == SS_SH_EXPANSION ? phi_expansion(P.expansion, comp.p[0], x)
+                                                      : phi_component(comp, P.G, x));
         }
     }
     const ss_subhalos& sh = P.subhalos;
@@ -545,6 +611,8 @@ int64_t or_abi_sizeof(int which) {
         case 4: return (int64_t)sizeof(ss_component);
         case 5: return (int64_t)sizeof(ss_track);
         case 6: return (int64_t)sizeof(ss_subhalos);
+        case 7: return (int64_t)sizeof(ss_expansion);
+        case 8: return (int64_t)sizeof(ss_mlp);
         default: return -1;
     }
 }

@@ -26,6 +26,8 @@ SS_MIYAMOTO_NAGAI = 3
 SS_HERNQUIST = 4
 SS_PLUMMER = 5
 SS_ISOCHRONE = 6
+SS_SH_EXPANSION = 7
+SS_SHEXP_LMAX = 8
 
 SS_CENTER_ORIGIN = 0
 SS_CENTER_TRACK = 1
@@ -54,10 +56,15 @@ class ss_subhalos(C.Structure):
                 ("m", VP), ("a", VP), ("x0", VP), ("v", VP), ("t0", VP), ("t_window", C.c_double)]
 
 
+class ss_expansion(C.Structure):
+    _fields_ = [("l_max", C.c_int32), ("n_knots", C.c_int32), ("log_r0", C.c_double), ("dlog_r", C.c_double),
+                ("coef", VP)]
+
+
 class ss_potential(C.Structure):
     _fields_ = [("G", C.c_double), ("n_components", C.c_int32), ("reserved", C.c_int32),
                 ("comp", ss_component * SS_MAX_COMPONENTS), ("track", ss_track),
-                ("subhalos", ss_subhalos)]
+                ("subhalos", ss_subhalos), ("expansion", ss_expansion)]
 
 
 class ss_stream_cfg(C.Structure):
@@ -77,7 +84,17 @@ class ss_pert_cfg(C.Structure):
                 ("steps_per_release", C.c_int32), ("ncol", C.c_int32), ("save_stride", C.c_int32)]
 
 
-STRUCTS = [ss_potential, ss_stream_cfg, ss_release_cfg, ss_pert_cfg, ss_component, ss_track, ss_subhalos]
+SS_MLP_WIDTH = 128
+SS_MLP_NPARAM = 128 * 4 + 128 + 3 * (128 * 128 + 128) + 128 + 1
+
+
+class ss_mlp(C.Structure):
+    _fields_ = [("params", VP), ("in_scale", C.c_float * 4), ("in_shift", C.c_float * 4),
+                ("out_scale", C.c_float), ("out_shift", C.c_float)]
+
+
+STRUCTS = [ss_potential, ss_stream_cfg, ss_release_cfg, ss_pert_cfg, ss_component, ss_track, ss_subhalos,
+           ss_expansion, ss_mlp]
 
 # name -> (restype, argtypes)
 SIGNATURES = {
@@ -114,6 +131,16 @@ SIGNATURES = {
                                        VP, C.c_int64, VP]),
     "ss_binned_sums": (C.c_int, [VP, VP, C.c_int64, C.c_int32, VP, C.c_int32, VP, VP, VP]),
     "ss_peak_fma": (C.c_int, [C.c_int, C.c_int64, DP, VP, VP]),
+    "ss_mlp_eval_workspace_bytes": (C.c_int64, [C.c_int64]),
+    "ss_mlp_eval": (C.c_int, [C.POINTER(ss_mlp), VP, C.c_int64, VP, VP, VP, C.c_int64, VP]),
+    "ss_mlp_train_workspace_bytes": (C.c_int64, [C.c_int64]),
+    "ss_mlp_loss_grad": (C.c_int, [C.POINTER(ss_mlp), VP, VP, VP, VP, VP, C.c_int64, VP, VP, VP, C.c_int64, VP]),
+    "ss_mlp_adam": (C.c_int, [VP, VP, VP, VP, C.c_int64, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float,
+                              VP]),
+    "ss_mlp_grad_bf16": (C.c_int, [C.POINTER(ss_mlp), VP, C.c_int64, VP, VP, VP]),
+    "ss_stream_mlp_workspace_bytes": (C.c_int64, [C.POINTER(ss_stream_cfg)]),
+    "ss_stream_mlp_bf16": (C.c_int, [C.POINTER(ss_mlp), C.POINTER(ss_stream_cfg), VP, VP, VP, VP, VP, C.c_int64,
+                                     VP]),
 }
 
 HERE = os.path.dirname(os.path.abspath(__file__))

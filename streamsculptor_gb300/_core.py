@@ -145,10 +145,31 @@ class SubhaloTable:
 
 
 @dataclass
+class ExpansionTable:
+    """Spline table of a spherical-harmonic expansion (ss_expansion):
+    coef [n_knots, (l_max+1)^2, 2] float64 on the device holds the value and
+    d/dln r of every radial function f_lm at knots ln r = log_r0 + k dlog_r."""
+    l_max: int
+    log_r0: float
+    dlog_r: float
+    coef: torch.Tensor
+
+    def struct(self) -> _abi.ss_expansion:
+        e = _abi.ss_expansion()
+        e.l_max = int(self.l_max)
+        e.n_knots = int(self.coef.shape[0])
+        e.log_r0 = float(self.log_r0)
+        e.dlog_r = float(self.dlog_r)
+        e.coef = self.coef.data_ptr()
+        return e
+
+
+@dataclass
 class Flat:
     comps: List[Tuple[int, int, Tuple[float, ...]]] = field(default_factory=list)
     track: Optional[CenterTrack] = None
     subhalos: Optional[SubhaloTable] = None
+    expansion: Optional[ExpansionTable] = None
 
     def extend(self, other: "Flat"):
         self.comps.extend(other.comps)
@@ -160,6 +181,10 @@ class Flat:
             if self.subhalos is not None:
                 raise NotImplementedError("at most one subhalo table per potential")
             self.subhalos = other.subhalos
+        if other.expansion is not None:
+            if self.expansion is not None and self.expansion is not other.expansion:
+                raise NotImplementedError("at most one spherical-harmonic expansion per potential")
+            self.expansion = other.expansion
 
 
 def make_struct(flat: Flat, G: float) -> _abi.ss_potential:
@@ -182,6 +207,8 @@ def make_struct(flat: Flat, G: float) -> _abi.ss_potential:
         P.track.n_knots = flat.track.knots.shape[0]
     if flat.subhalos is not None:
         P.subhalos = flat.subhalos.struct()
+    if flat.expansion is not None:
+        P.expansion = flat.expansion.struct()
     return P
 
 
@@ -313,7 +340,7 @@ def aligned_ptr(buf: Optional[torch.Tensor], align: int = 256):
 STREAM_EVENTS = None
 
 
-def stream(P, cfg, ics: torch.Tensor, precision: str, want_final=True, snaps=None, status=True):
+def stream(P, cfg, ics: torch.Tensor, precision: str, want_final=True, snaps=None, status=True, mlp=None):
     N = cfg.n_particles
     dev = ics.device
     final = torch.empty(N, 6, dtype=torch.float64, device=dev) if want_final else None
@@ -332,8 +359,14 @@ def stream(P, cfg, ics: torch.Tensor, precision: str, want_final=True, snaps=Non
         ws, nb = aligned_ptr(Workspace.get(need, dev))
         _abi.call("ss_stream_f32k", C.byref(P), C.byref(cfg), ptr(ics), ptr(final), ptr(snaps), ptr(st),
                   ws, nb, stream_handle())
+    elif precision == "mlp":
+        if mlp is None:
+            raise ValueError("precision='mlp' needs a force surrogate")
+        m = mlp.struct()
+        _abi.call("ss_stream_mlp_bf16", C.byref(m), C.byref(cfg), ptr(ics), ptr(final), ptr(snaps), ptr(st), None, 0,
+                  stream_handle())
     else:
-        raise ValueError("precision must be 'f64' or 'f32k'")
+        raise ValueError("precision must be 'f64', 'f32k' or 'mlp'")
     if evs is not None:
         e1.record()
         evs.append((e0, e1))

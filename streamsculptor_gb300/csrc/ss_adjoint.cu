@@ -453,6 +453,8 @@ int ss_stream_adjoint_f32(const ss_potential* pot, const ss_stream_cfg* cfg, con
     PotDev<float> P;
     int rc = prepare_potential<float>(pot, &P, false);
     if (rc) return rc;
+    for (int k = 0; k < P.n; ++k)
+        SS_CHECK_ARG(P.c[k].kind != SS_SH_EXPANSION, "component %d: SS_SH_EXPANSION has no adjoint", k);
     SS_CHECK_ARG(!P.has_track, "the adjoint supports static potentials (no center track) only");
     SS_CHECK_ARG(cfg && cfg->n_particles >= 0 && cfg->n_steps >= 0 && cfg->n_steps < (1LL << 30), "bad cfg");
     SS_CHECK_ARG(cfg->particles_per_release >= 1 && cfg->steps_per_release >= 0, "bad release layout");
@@ -499,6 +501,8 @@ int ss_release_vjp(const ss_potential* pot, const ss_release_cfg* cfg, const dou
     PotDev<double> P;
     int rc = prepare_potential<double>(pot, &P, false);
     if (rc) return rc;
+    for (int k = 0; k < P.n; ++k)
+        SS_CHECK_ARG(P.c[k].kind != SS_SH_EXPANSION, "component %d: SS_SH_EXPANSION has no adjoint", k);
     SS_CHECK_ARG(cfg && cfg->n_release >= 0 && cfg->n_draw >= 1, "bad cfg");
     int64_t total = cfg->n_release * cfg->n_draw;
     if (total == 0) return SS_OK;

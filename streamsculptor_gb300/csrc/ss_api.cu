@@ -38,6 +38,7 @@ int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalo
     memset(out, 0, sizeof(*out));
     out->n = in->n_components;
     bool need_track = false;
+    bool need_expansion = false;
     const double G = in->G;
     for (int k = 0; k < in->n_components; ++k) {
         const ss_component& c = in->comp[k];
@@ -76,6 +77,26 @@ int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalo
                 SS_CHECK_ARG(p[1] > 0.0, "component %d (Isochrone): need a > 0", k);
                 d.q[0] = R(G * p[0]); d.q[1] = R(p[1]); d.q[2] = R(p[1] * p[1]);
                 break;
+            case SS_SH_EXPANSION: {
+                const ss_expansion& e = in->expansion;
+                SS_CHECK_ARG(!need_expansion, "component %d: only one SS_SH_EXPANSION component per potential", k);
+                SS_CHECK_ARG(e.coef != nullptr, "component %d (expansion): coefficient table is NULL", k);
+                SS_CHECK_ARG(e.l_max >= 0 && e.l_max <= SS_SHEXP_LMAX, "component %d (expansion): l_max=%d outside [0, %d]",
+                             k, e.l_max, SS_SHEXP_LMAX);
+                SS_CHECK_ARG(e.n_knots >= 2 && e.n_knots <= (1 << 20), "component %d (expansion): need >= 2 knots", k);
+                SS_CHECK_ARG(std::isfinite(e.log_r0) && std::isfinite(e.dlog_r) && e.dlog_r > 0.0,
+                             "component %d (expansion): need finite log_r0 and dlog_r > 0", k);
+                need_expansion = true;
+                d.q[0] = R(p[0]);
+                out->ex.tab64 = e.coef;
+                out->ex.tab32 = nullptr;
+                out->ex.u0 = e.log_r0;
+                out->ex.du = e.dlog_r;
+                out->ex.inv_du = 1.0 / e.dlog_r;
+                out->ex.nk = e.n_knots;
+                out->ex.lmax = e.l_max;
+                break;
+            }
             default:
                 return set_error(SS_ERR_INVALID_ARGUMENT, "component %d: unknown kind %d", k, c.kind);
         }
@@ -116,10 +137,12 @@ template int prepare_potential<double>(const ss_potential*, PotDev<double>*, boo
 template int prepare_potential<float>(const ss_potential*, PotDev<float>*, bool);
 
 // ------------------------------------------------------------- Phi (FP64)
-__device__ double comp_phi(const CompDev<double>& c, const double x[3]) {
+__device__ double comp_phi(const PotDev<double>& P, const CompDev<double>& c, const double x[3]) {
     const double* q = c.q;
     double r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
     switch (c.kind) {
+        case SS_SH_EXPANSION:
+            return shexp_phi(P.ex, q[0], x);
         case SS_NFW: {
             double r = sqrt(r2 + q[3]);
             return -q[0] * log1p(r * q[2]) / r;
@@ -158,9 +181,9 @@ __global__ void potential_eval_kernel(PotDev<double> P, const double* __restrict
         for (int k = 0; k < P.n; ++k) {
             if (P.c[k].center == SS_CENTER_TRACK) {
                 double xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
-                f += comp_phi(P.c[k], xs);
+                f += comp_phi(P, P.c[k], xs);
             } else {
-                f += comp_phi(P.c[k], x);
+                f += comp_phi(P, P.c[k], x);
             }
         }
         for (int j = 0; j < P.sh.n; ++j) {
@@ -348,6 +371,8 @@ int64_t ss_abi_sizeof(int which) {
         case 4: return (int64_t)sizeof(ss_component);
         case 5: return (int64_t)sizeof(ss_track);
         case 6: return (int64_t)sizeof(ss_subhalos);
+        case 7: return (int64_t)sizeof(ss_expansion);
+        case 8: return (int64_t)sizeof(ss_mlp);
         default: return -1;
     }
 }

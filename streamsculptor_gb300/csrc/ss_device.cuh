@@ -139,6 +139,13 @@ template <int N> __device__ inline Dual<N> s_rsqrt(const Dual<N>& x) { double s 
 template <int N> __device__ inline Dual<N> s_log1p(const Dual<N>& x) { return chain(x, log1p(x.v), 1.0 / (1.0 + x.v)); }
 template <int N> __device__ inline Dual<N> s_rcp(const Dual<N>& x) { double r = 1.0 / x.v; return chain(x, r, -r * r); }
 template <int N> __device__ inline Dual<N> s_cbrt(const Dual<N>& x) { double c = cbrt(x.v); return chain(x, c, c / (3.0 * x.v)); }
+__device__ __forceinline__ float  s_log(float x) { return logf(x); }
+__device__ __forceinline__ double s_log(double x) { return log(x); }
+template <int N> __device__ inline Dual<N> s_log(const Dual<N>& x) { return chain(x, log(x.v), 1.0 / x.v); }
+// value part of a scalar or dual number
+__device__ __forceinline__ double sval(float x) { return (double)x; }
+__device__ __forceinline__ double sval(double x) { return x; }
+template <int N> __device__ __forceinline__ double sval(const Dual<N>& x) { return x.v; }
 
 // ---------------------------------------------------- prepared potential
 // Parameters are pre-combined on the host (G*m, 1/r_s, b^2 ...).
@@ -147,6 +154,17 @@ struct CompDev {
     int32_t kind;
     int32_t center;
     R q[6];
+};
+
+// Spherical-harmonic expansion table (SS_SH_EXPANSION).  tab64 is the
+// caller's [nk][nt][2] (value, d/du) table; tab32, when set, is the FP32
+// per-interval copy {f_k, du f'_k, f_k+1, du f'_k+1} [nk-1][nt] that the
+// FP32 stream builds in its workspace.
+struct ExpDev {
+    const double* tab64;
+    const float4* tab32;
+    double u0, du, inv_du;
+    int32_t nk, lmax;
 };
 
 struct TrackDev {
@@ -176,6 +194,7 @@ struct PotDev {
     CompDev<R> c[SS_MAX_COMPONENTS];
     TrackDev track;
     ShDev sh;
+    ExpDev ex;
 };
 
 // --------------------------------------------------------------- track
@@ -378,6 +397,358 @@ __device__ __forceinline__ void comp_grad(const CompDev<R>& c, const T x[3], T g
     }
 }
 
+// ------------------------------------------- spherical-harmonic expansion
+// Phi = scale * sum_lm f_lm(r) Y_lm(n), n = x / r, real Schmidt harmonics
+// (the layout is documented with ss_expansion in the C header).  The
+// angular parts come from the regular solid harmonics at the unit vector,
+//   R_l^m = r^l P_l^m(cos theta) e^{i m phi} / (l+m)!,
+//   R_m^m = (x + i y)/(2m) R_{m-1}^{m-1},  R_{m+1}^m = z R_m^m,
+//   R_l^m = ((2l-1) z R_{l-1}^m - r^2 R_{l-2}^m) / ((l-m)(l+m)),
+// so Y_lm = N_lm {Re, Im} R_l^m(n) with N_l0 = l!, N_lm = sqrt(2 (l-m)!(l+m)!).
+// Their derivatives are lower-degree harmonics (R_l^{-m} = (-1)^m conj R_l^m):
+//   d/dx R_l^m = (R_{l-1}^{m-1} - R_{l-1}^{m+1}) / 2,
+//   d/dy R_l^m = i (R_{l-1}^{m+1} + R_{l-1}^{m-1}) / 2,   d/dz R_l^m = R_{l-1}^m,
+// which gives gradients and Hessians without differentiating the recurrence.
+// With K = Y_lm(n), a0 = f, a1 = f', a2 = f'' (in r), homogeneity gives
+//   grad = sum [G1 K n + (a0/r) (grad K)(n)],           G1 = a1 - l a0 / r,
+//   H    = sum [G2 K n n^T + (G1/r) K (I - n n^T) + (G1/r)(n gK^T + gK n^T)
+//               + (a0/r^2) (hess K)(n)],               G2 = a2 - 2 l a1/r + l(l+1) a0/r^2.
+static __constant__ double c_shnorm[SS_SHEXP_LMAX + 1][SS_SHEXP_LMAX + 1] = {
+    {1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {1.0, 2.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {2.0, 3.4641016151377544, 6.928203230275509, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {6.0, 9.797958971132712, 15.491933384829668, 37.94733192202055, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {24.0, 37.94733192202055, 53.665631459994955, 100.39920318408906, 283.9718295887816, 0.0, 0.0, 0.0, 0.0},
+    {120.0, 185.903200617956, 245.92681838303037, 401.59681273635624, 851.9154887663448, 2693.9933184772376, 0.0,
+     0.0, 0.0},
+    {720.0, 1099.8181667894016, 1391.172167634186, 2086.758251451279, 3809.8818879330106, 8934.965025113417,
+     30951.626774694734, 0.0, 0.0},
+    {5040.0, 7619.763775866021, 9332.266605707318, 13197.818001472819, 21886.105181141756, 43772.21036228351,
+     111597.67739518596, 417560.27397251286, 0.0},
+    {40320.0, 60480.0, 72287.42629254413, 97877.63789548662, 151631.38461413587, 273357.36609793414,
+     590519.4025601529, 1617203.9871333486, 6468815.948533394}};
+
+template <class T>
+struct SolidH {
+    T C[SS_SHEXP_LMAX + 1][SS_SHEXP_LMAX + 1];
+    T S[SS_SHEXP_LMAX + 1][SS_SHEXP_LMAX + 1];
+    // real and imaginary parts of R_l^m for any integer l, m (zero outside)
+    __device__ __forceinline__ T c(int l, int m) const {
+        if (l < 0 || m > l || -m > l) return T(0);
+        if (m >= 0) return C[l][m];
+        return (m & 1) ? T(0) - C[l][-m] : C[l][-m];
+    }
+    __device__ __forceinline__ T s(int l, int m) const {
+        if (l < 0 || m > l || -m > l) return T(0);
+        if (m >= 0) return S[l][m];
+        return (m & 1) ? S[l][-m] : T(0) - S[l][-m];
+    }
+};
+
+// Straight-line code for float/double; rolled loops for the dual-number
+// types (their unrolled form only adds spills and compile time).
+template <class T>
+struct ShUnroll {
+    static constexpr int n = std::is_floating_point<T>::value ? 32 : 1;
+};
+
+template <class T>
+__device__ __forceinline__ void solid_harmonics(const T n[3], SolidH<T>& R) {
+    constexpr int LM = SS_SHEXP_LMAX;
+    constexpr int UR = ShUnroll<T>::n;
+    R.C[0][0] = T(1);
+    R.S[0][0] = T(0);
+#pragma unroll UR
+    for (int m = 1; m <= LM; ++m) {
+        const T f = T(1.0 / (2.0 * m));
+        R.C[m][m] = (n[0] * R.C[m - 1][m - 1] - n[1] * R.S[m - 1][m - 1]) * f;
+        R.S[m][m] = (n[0] * R.S[m - 1][m - 1] + n[1] * R.C[m - 1][m - 1]) * f;
+    }
+#pragma unroll UR
+    for (int m = 0; m < LM; ++m) {
+        R.C[m + 1][m] = n[2] * R.C[m][m];
+        R.S[m + 1][m] = n[2] * R.S[m][m];
+    }
+#pragma unroll UR
+    for (int m = 0; m <= LM; ++m) {
+#pragma unroll UR
+        for (int l = m + 2; l <= LM; ++l) {
+            const T a = T((2.0 * l - 1.0) / ((double)(l - m) * (l + m)));
+            const T b = T(1.0 / ((double)(l - m) * (l + m)));
+            R.C[l][m] = a * n[2] * R.C[l - 1][m] - b * R.C[l - 2][m];
+            R.S[l][m] = a * n[2] * R.S[l - 1][m] - b * R.S[l - 2][m];
+        }
+    }
+}
+
+// Radial spline of every term at u = ln r: Hermite basis weights and the
+// knot interval.  e is the distance (in knot spacings) beyond the end knot
+// where the spline continues linearly.
+template <class T>
+struct RadialBasis {
+    int k;
+    T h[4], hs[4], hss[4], e;
+};
+
+template <class T>
+__device__ __forceinline__ void radial_basis(const ExpDev& E, const T& u, RadialBasis<T>& B) {
+    const double us = (sval(u) - E.u0) * E.inv_du;
+    int k = (int)floor(us);
+    k = k < 0 ? 0 : (k > E.nk - 2 ? E.nk - 2 : k);
+    B.k = k;
+    T s = (u - T(E.u0 + (double)k * E.du)) * T(E.inv_du);
+    T sc = s;
+    if (sval(s) < 0.0) sc = T(0);
+    if (sval(s) > 1.0) sc = T(1);
+    B.e = s - sc;
+    const T one(1), two(2), three(3), six(6);
+    T om = one - sc;
+    B.h[0] = (one + two * sc) * om * om;
+    B.h[1] = sc * om * om;
+    B.h[2] = sc * sc * (three - two * sc);
+    B.h[3] = sc * sc * (sc - one);
+    B.hs[0] = six * sc * (sc - one);
+    B.hs[1] = om * (one - three * sc);
+    B.hs[2] = six * sc * om;
+    B.hs[3] = sc * (three * sc - two);
+    const bool inside = sval(B.e) == 0.0;
+    B.hss[0] = inside ? T(12) * sc - six : T(0);
+    B.hss[1] = inside ? six * sc - T(4) : T(0);
+    B.hss[2] = inside ? six - T(12) * sc : T(0);
+    B.hss[3] = inside ? six * sc - two : T(0);
+}
+
+// f, df/ds, d2f/ds2 of term j (s in knot spacings).
+template <class T>
+__device__ __forceinline__ void radial_term(const ExpDev& E, const RadialBasis<T>& B, int nt, int j, T& f, T& fs,
+                                            T& fss) {
+    T c0, c1, c2, c3;
+    if constexpr (std::is_same<T, float>::value) {
+        if (E.tab32) {
+            const float4 t = __ldg(E.tab32 + (size_t)B.k * nt + j);
+            c0 = t.x; c1 = t.y; c2 = t.z; c3 = t.w;
+        } else {
+            const double* a = E.tab64 + ((size_t)B.k * nt + j) * 2;
+            const double* b = a + (size_t)nt * 2;
+            c0 = (float)__ldg(a); c1 = (float)(__ldg(a + 1) * E.du);
+            c2 = (float)__ldg(b); c3 = (float)(__ldg(b + 1) * E.du);
+        }
+    } else {
+        const double* a = E.tab64 + ((size_t)B.k * nt + j) * 2;
+        const double* b = a + (size_t)nt * 2;
+        c0 = T(__ldg(a)); c1 = T(__ldg(a + 1) * E.du);
+        c2 = T(__ldg(b)); c3 = T(__ldg(b + 1) * E.du);
+    }
+    fs = B.hs[0] * c0 + B.hs[1] * c1 + B.hs[2] * c2 + B.hs[3] * c3;
+    f = B.h[0] * c0 + B.h[1] * c1 + B.h[2] * c2 + B.h[3] * c3 + B.e * fs;
+    fss = B.hss[0] * c0 + B.hss[1] * c1 + B.hss[2] * c2 + B.hss[3] * c3;
+}
+
+// Rows of R_l^m (m = 0..l): the gradient of a degree-l term needs degree
+// l-1 and its Hessian degree l-2, so the recurrence runs degree by degree
+// keeping three rows (the live set stays small).
+template <class T>
+struct ShRow {
+    T c[SS_SHEXP_LMAX + 1], s[SS_SHEXP_LMAX + 1];
+};
+
+// {Re, Im} R_l^m of a row of degree l for any m (R_l^{-m} = (-1)^m conj R_l^m)
+template <class T>
+__device__ __forceinline__ T row_c(const ShRow<T>& R, int l, int m) {
+    if (l < 0 || m > l || -m > l) return T(0);
+    if (m >= 0) return R.c[m];
+    return (m & 1) ? T(0) - R.c[-m] : R.c[-m];
+}
+template <class T>
+__device__ __forceinline__ T row_s(const ShRow<T>& R, int l, int m) {
+    if (l < 0 || m > l || -m > l) return T(0);
+    if (m >= 0) return R.s[m];
+    return (m & 1) ? R.s[-m] : T(0) - R.s[-m];
+}
+
+template <class T, class R, bool HESS>
+__device__ __forceinline__ void shexp_grad_impl(const ExpDev& E, const R scale, const T x[3], T grad[3], T H[6]) {
+    constexpr int LM = SS_SHEXP_LMAX;
+    constexpr int UR = ShUnroll<T>::n;
+    const int L = E.lmax;
+    const int nt = (L + 1) * (L + 1);
+    T r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+    T ir = s_rsqrt(r2);
+    T r = r2 * ir;
+    T n[3] = {x[0] * ir, x[1] * ir, x[2] * ir};
+    RadialBasis<T> B;
+    radial_basis<T>(E, s_log(r), B);
+    const T idu = T(E.inv_du);
+    ShRow<T> R0, R1, R2;  // degrees l, l-1, l-2 (at the unit vector, r = 1)
+#pragma unroll UR
+    for (int m = 0; m <= LM; ++m) {
+        R0.c[m] = R0.s[m] = R1.c[m] = R1.s[m] = R2.c[m] = R2.s[m] = T(0);
+    }
+    R0.c[0] = T(1);
+    T S1(0), S2(0), V[3] = {T(0), T(0), T(0)}, W[3] = {T(0), T(0), T(0)};
+    T M[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+#pragma unroll UR
+    for (int l = 0; l <= LM; ++l) {
+        if (l > L) break;
+        if (l > 0) {
+#pragma unroll UR
+            for (int m = 0; m < l; ++m) {
+                R2.c[m] = R1.c[m];
+                R2.s[m] = R1.s[m];
+                R1.c[m] = R0.c[m];
+                R1.s[m] = R0.s[m];
+            }
+#pragma unroll UR
+            for (int m = 0; m + 2 <= l; ++m) {
+                const T a = T((2.0 * l - 1.0) / ((double)(l - m) * (l + m)));
+                const T b = T(1.0 / ((double)(l - m) * (l + m)));
+                R0.c[m] = a * n[2] * R1.c[m] - b * R2.c[m];
+                R0.s[m] = a * n[2] * R1.s[m] - b * R2.s[m];
+            }
+            R0.c[l - 1] = n[2] * R1.c[l - 1];
+            R0.s[l - 1] = n[2] * R1.s[l - 1];
+            const T f = T(1.0 / (2.0 * l));
+            R0.c[l] = (n[0] * R1.c[l - 1] - n[1] * R1.s[l - 1]) * f;
+            R0.s[l] = (n[0] * R1.s[l - 1] + n[1] * R1.c[l - 1]) * f;
+        }
+        const T fl = T((double)l);
+#pragma unroll UR
+        for (int mm = -l; mm <= l; ++mm) {
+            const int m = mm < 0 ? -mm : mm;
+            const bool cs = mm >= 0;  // cos part (Re) or sin part (Im)
+            const T N = T(c_shnorm[l][m]);
+            T f, fs, fss;
+            radial_term<T>(E, B, nt, l * l + l + mm, f, fs, fss);
+            // radial derivatives in r: a1 = f_u / r, a2 = (f_uu - f_u) / r^2
+            const T fu = fs * idu;
+            const T a0 = f * N;
+            const T a1 = fu * ir * N;
+            const T G1 = a1 - fl * a0 * ir;
+            const T K = cs ? R0.c[m] : R0.s[m];
+            S1 += G1 * K;
+            // grad of {Re, Im} R_l^m at n, from degree l-1
+            T gk[3];
+            if (cs) {
+                gk[0] = T(0.5) * (row_c(R1, l - 1, m - 1) - row_c(R1, l - 1, m + 1));
+                gk[1] = T(0) - T(0.5) * (row_s(R1, l - 1, m + 1) + row_s(R1, l - 1, m - 1));
+                gk[2] = row_c(R1, l - 1, m);
+            } else {
+                gk[0] = T(0.5) * (row_s(R1, l - 1, m - 1) - row_s(R1, l - 1, m + 1));
+                gk[1] = T(0.5) * (row_c(R1, l - 1, m + 1) + row_c(R1, l - 1, m - 1));
+                gk[2] = row_s(R1, l - 1, m);
+            }
+            V[0] += a0 * gk[0];
+            V[1] += a0 * gk[1];
+            V[2] += a0 * gk[2];
+            if constexpr (HESS) {
+                const T fuu = fss * idu * idu;
+                const T a2 = (fuu - fu) * ir * ir * N;
+                const T G2 = a2 - T(2.0) * fl * a1 * ir + fl * (fl + T(1)) * a0 * ir * ir;
+                S2 += G2 * K;
+                W[0] += G1 * gk[0];
+                W[1] += G1 * gk[1];
+                W[2] += G1 * gk[2];
+                // Hessian of R_l^m from degree l-2: xx (Q_{m-2} - 2Q_m + Q_{m+2})/4,
+                // yy -(Q_{m+2} + 2Q_m + Q_{m-2})/4, zz Q_m, xy i(Q_{m-2} - Q_{m+2})/4,
+                // xz (Q_{m-1} - Q_{m+1})/2, yz i(Q_{m+1} + Q_{m-1})/2
+                const int k2 = l - 2;
+                T hk[6];
+                if (cs) {
+                    hk[0] = T(0.25) * (row_c(R2, k2, m - 2) - T(2) * row_c(R2, k2, m) + row_c(R2, k2, m + 2));
+                    hk[1] = T(0) - T(0.25) * (row_c(R2, k2, m + 2) + T(2) * row_c(R2, k2, m) + row_c(R2, k2, m - 2));
+                    hk[2] = row_c(R2, k2, m);
+                    hk[3] = T(0) - T(0.25) * (row_s(R2, k2, m - 2) - row_s(R2, k2, m + 2));
+                    hk[4] = T(0.5) * (row_c(R2, k2, m - 1) - row_c(R2, k2, m + 1));
+                    hk[5] = T(0) - T(0.5) * (row_s(R2, k2, m + 1) + row_s(R2, k2, m - 1));
+                } else {
+                    hk[0] = T(0.25) * (row_s(R2, k2, m - 2) - T(2) * row_s(R2, k2, m) + row_s(R2, k2, m + 2));
+                    hk[1] = T(0) - T(0.25) * (row_s(R2, k2, m + 2) + T(2) * row_s(R2, k2, m) + row_s(R2, k2, m - 2));
+                    hk[2] = row_s(R2, k2, m);
+                    hk[3] = T(0.25) * (row_c(R2, k2, m - 2) - row_c(R2, k2, m + 2));
+                    hk[4] = T(0.5) * (row_s(R2, k2, m - 1) - row_s(R2, k2, m + 1));
+                    hk[5] = T(0.5) * (row_c(R2, k2, m + 1) + row_c(R2, k2, m - 1));
+                }
+#pragma unroll
+                for (int i = 0; i < 6; ++i) M[i] += a0 * hk[i];
+            }
+        }
+    }
+    const T sc = T(scale);
+    grad[0] += sc * (S1 * n[0] + V[0] * ir);
+    grad[1] += sc * (S1 * n[1] + V[1] * ir);
+    grad[2] += sc * (S1 * n[2] + V[2] * ir);
+    if constexpr (HESS) {
+        const int ia[6] = {0, 1, 2, 0, 0, 1}, ib[6] = {0, 1, 2, 1, 2, 2};
+        const T Sr = S1 * ir, ir2 = ir * ir;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const int a = ia[q], b = ib[q];
+            T v = S2 * n[a] * n[b] - Sr * n[a] * n[b] + (n[a] * W[b] + W[a] * n[b]) * ir + M[q] * ir2;
+            if (a == b) v += Sr;
+            H[q] += sc * v;
+        }
+    }
+}
+
+// Out-of-line entry points: the expansion is ~2000 instructions, so the
+// stage loops call it instead of inlining it six times.  The gradient-only
+// forms pass the position by value so that it stays in registers.
+template <class S>
+struct Vec3 {
+    S x, y, z;
+};
+
+template <class S>
+__device__ __noinline__ Vec3<S> shexp_grad_value(const ExpDev E, S scale, S x0, S x1, S x2) {
+    const S x[3] = {x0, x1, x2};
+    S g[3] = {S(0), S(0), S(0)};
+    shexp_grad_impl<S, S, false>(E, scale, x, g, nullptr);
+    return Vec3<S>{g[0], g[1], g[2]};
+}
+
+template <class T, class R, bool HESS>
+__device__ __noinline__ void shexp_grad_ref(const ExpDev& E, const R scale, const T x[3], T grad[3], T H[6]) {
+    shexp_grad_impl<T, R, HESS>(E, scale, x, grad, H);
+}
+
+template <class T, class R, bool HESS>
+__device__ __forceinline__ void shexp_grad(const ExpDev& E, const R scale, const T x[3], T grad[3], T H[6]) {
+    if constexpr (std::is_floating_point<T>::value && std::is_same<T, R>::value && !HESS) {
+        const Vec3<T> g = shexp_grad_value<T>(E, scale, x[0], x[1], x[2]);
+        grad[0] += g.x;
+        grad[1] += g.y;
+        grad[2] += g.z;
+    } else {
+        shexp_grad_ref<T, R, HESS>(E, scale, x, grad, H);
+    }
+}
+
+// Phi of the expansion (FP64; potential evaluation only).
+__device__ inline double shexp_phi(const ExpDev& E, double scale, const double x[3]) {
+    double r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+    double ir = rsqrt(r2);
+    double r = r2 * ir;
+    double n[3] = {x[0] * ir, x[1] * ir, x[2] * ir};
+    SolidH<double> Q;
+    solid_harmonics<double>(n, Q);
+    RadialBasis<double> B;
+    radial_basis<double>(E, log(r), B);
+    const int nt = (E.lmax + 1) * (E.lmax + 1);
+    double phi = 0.0;
+#pragma unroll
+    for (int l = 0; l <= SS_SHEXP_LMAX; ++l) {
+        if (l > E.lmax) break;
+#pragma unroll
+        for (int mm = -l; mm <= l; ++mm) {
+            const int m = mm < 0 ? -mm : mm;
+            double f, fs, fss;
+            radial_term<double>(E, B, nt, l * l + l + mm, f, fs, fss);
+            phi += f * c_shnorm[l][m] * (mm >= 0 ? Q.c(l, m) : Q.s(l, m));
+        }
+    }
+    return scale * phi;
+}
+
 // Subhalo line potential (potential.py:802-904): grad Phi_s and, for the
 // response kernel, grad of dPhi_s/da.  rel = x - (x0 + v (t - t0)).
 // Plummer: Phi = -Gm/sqrt(r^2+a^2);  dPhi/da = Gm a / D^3.
@@ -421,7 +792,10 @@ __device__ __forceinline__ void pot_grad(const PotDev<R>& P, const T x[3], const
 #pragma unroll 1
     for (int k = 0; k < P.n; ++k) {
         const CompDev<R>& c = P.c[k];
-        comp_grad<T, R, HESS>(c, c.center == SS_CENTER_TRACK ? xs : x, grad, H);
+        if (c.kind == SS_SH_EXPANSION)
+            shexp_grad<T, R, HESS>(P.ex, c.q[0], c.center == SS_CENTER_TRACK ? xs : x, grad, H);
+        else
+            comp_grad<T, R, HESS>(c, c.center == SS_CENTER_TRACK ? xs : x, grad, H);
     }
 }
 
@@ -439,7 +813,14 @@ struct Comp {
     template <class T, class R, bool HESS, int... I>
     static __device__ __forceinline__ void add(const PotDev<R>& P, const T x[3], const T xs[3], T grad[3], T H[6],
                                                std::integer_sequence<int, I...>) {
-        (kind_grad<(KCS & 15), T, R, HESS>(P.c[I].q, (KCS >> 4) ? xs : x, grad, H), ...);
+        (one<(KCS & 15), T, R, HESS>(P, I, (KCS >> 4) ? xs : x, grad, H), ...);
+    }
+    template <int KIND, class T, class R, bool HESS>
+    static __device__ __forceinline__ void one(const PotDev<R>& P, int i, const T x[3], T grad[3], T H[6]) {
+        if constexpr (KIND == SS_SH_EXPANSION)
+            shexp_grad<T, R, HESS>(P.ex, P.c[i].q[0], x, grad, H);
+        else
+            kind_grad<KIND, T, R, HESS>(P.c[i].q, x, grad, H);
     }
     template <class T, class R, bool HESS>
     static __device__ __forceinline__ void grad(const PotDev<R>& P, const T x[3], const T xs[3], T g[3], T H[6]) {
@@ -479,6 +860,7 @@ using CompTri3 = Comp<SS_TRIAXIAL_NFW, SS_MIYAMOTO_NAGAI, SS_HERNQUIST>;
 using CompTri3P = Comp<SS_TRIAXIAL_NFW, SS_MIYAMOTO_NAGAI, SS_HERNQUIST, SS_PLUMMER | SS_T_>;
 using CompNFW = Comp<SS_NFW>;
 using CompPlummer = Comp<SS_PLUMMER>;
+using CompSHExp = Comp<SS_SH_EXPANSION>;
 
 // Calls f(Comp{}) for the matching compiled composition, else f(GenericComp{}).
 template <class R, class F>
@@ -491,6 +873,7 @@ inline auto dispatch_comp(const PotDev<R>& P, F&& f) {
     if (CompTri3P::matches(P)) return f(CompTri3P{});
     if (CompNFW::matches(P)) return f(CompNFW{});
     if (CompPlummer::matches(P)) return f(CompPlummer{});
+    if (CompSHExp::matches(P)) return f(CompSHExp{});
     return f(GenericComp{});
 }
 

@@ -17,6 +17,7 @@ struct D1 {
     __host__ __device__ constexpr D1(const S& a, const S& b) : v(a), d(b) {}
     __host__ __device__ constexpr D1(int a) : v(a), d(0) {}  // NOLINT
     __host__ __device__ D1(float a) : v(a), d(0) {}          // NOLINT
+    __host__ __device__ D1(double a) : v(S(a)), d(0) {}      // NOLINT
 };
 
 template <class S> __device__ __forceinline__ D1<S> operator+(const D1<S>& a, const D1<S>& b) { return D1<S>(a.v + b.v, a.d + b.d); }
@@ -47,6 +48,10 @@ template <class S> __device__ __forceinline__ D1<S> s_rcp(const D1<S>& x) {
 template <class S> __device__ __forceinline__ D1<S> s_log1p(const D1<S>& x) {
     return D1<S>(s_log1p(x.v), x.d * s_rcp(S(1) + x.v));
 }
+template <class S> __device__ __forceinline__ D1<S> s_log(const D1<S>& x) {
+    return D1<S>(s_log(x.v), x.d * s_rcp(x.v));
+}
+template <class S> __device__ __forceinline__ double sval(const D1<S>& x) { return (double)x.v; }
 template <class S> __device__ __forceinline__ D1<S> s_sqrt(const D1<S>& x) {
     S r = s_sqrt(x.v);
     return D1<S>(r, (0.5f * s_rcp(r)) * x.d);
@@ -127,6 +132,9 @@ __host__ __device__ inline void prepared_param_tangent(int kind, const double* p
         case SS_ISOCHRONE:  // q = {G m, a, a^2}
             if (j == 0) dq[0] = G;
             if (j == 1) { dq[1] = 1.0; dq[2] = 2.0 * p[1]; }
+            break;
+        case SS_SH_EXPANSION:  // q = {scale}
+            if (j == 0) dq[0] = 1.0;
             break;
         default:
             break;

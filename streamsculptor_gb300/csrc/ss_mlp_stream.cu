@@ -1,0 +1,594 @@
+// ss_mlp_stream.cu — particle-spray stream whose force is the learned
+// surrogate, evaluated on the 5th-generation tensor cores.
+//
+// One CTA = one warpgroup (128 threads) = a tile of 128 particles, persistent
+// over tiles.  The CTA integrates its tile with the FP32-compensated Dopri5
+// step of the plain stream (step_f32k); every stage's force is one
+// CTA-collective network evaluation:
+//   layer 1 (4 -> 128) on CUDA cores in FP32 (keeps the input precision),
+//   layers 2-4 as tcgen05.mma 128 x 128 x 128 BF16 GEMMs with FP32
+//   accumulators in tensor memory (TMEM),
+//   the input gradient (the force) as three more tcgen05 GEMMs with the same
+//   weight tiles read transposed (MN-major B operand), the final 128 -> 4
+//   product on CUDA cores.
+// Shared memory holds W2..W4 as BF16 in the no-swizzle core-matrix layout
+// (8 rows x 16 bytes per core matrix; element (o, i) of W at byte
+// (o/8)*2048 + (i/8)*128 + (o%8)*16 + (i%8)*2), the activation/delta tile
+// A [128 particles x 128] in the same layout, and W1, biases and w5 in FP32.
+// TMEM (512 columns x 128 lanes, lane = particle): R1..R3 keep s'(z1..z3)
+// for the backward chain, R4 is the accumulator of layer 4 and of the three
+// backward GEMMs.  One thread issues the MMAs; completion is signalled by
+// tcgen05.commit on an mbarrier; each evaluation waits six times, so the
+// wait parities are 0,1,0,1,0,1 in every evaluation.  Every wait is bounded:
+// on a timeout the CTA records SS_STATUS_ABORTED for its particles, stops
+// issuing MMAs and releases its TMEM.
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+
+#include "ss_stream.cuh"
+
+namespace ssg {
+
+static constexpr int MLP_W = SS_MLP_WIDTH;
+static constexpr int64_t P_W1 = 0, P_B1 = 512, P_W2 = 640, P_B2 = P_W2 + 16384, P_W3 = P_B2 + 128,
+                         P_B3 = P_W3 + 16384, P_W4 = P_B3 + 128, P_B4 = P_W4 + 16384, P_W5 = P_B4 + 128,
+                         P_B5 = P_W5 + 128;
+static_assert(P_B5 + 1 == SS_MLP_NPARAM, "parameter packing");
+
+// shared-memory map (bytes from a 1024-aligned base)
+static constexpr uint32_t SM_W2 = 0, SM_W3 = 32768, SM_W4 = 65536, SM_A = 98304;
+static constexpr uint32_t SM_W1 = 131072;             // float [128][4]
+static constexpr uint32_t SM_B = SM_W1 + 2048;        // float b1..b4 [4][128]
+static constexpr uint32_t SM_W5 = SM_B + 2048;        // float [128]
+static constexpr uint32_t SM_BAR = SM_W5 + 512;       // mbarrier (8 B)
+static constexpr uint32_t SM_TMEM = SM_BAR + 8;       // TMEM base address
+static constexpr uint32_t SM_ABORT = SM_TMEM + 4;     // abort flag
+static constexpr uint32_t SM_START = SM_ABORT + 4;    // tile start step
+static constexpr uint32_t SM_BYTES = SM_START + 4;
+static constexpr uint32_t SM_ALLOC = SM_BYTES + 1024;  // slack for the 1024-byte alignment
+
+// TMEM columns
+static constexpr uint32_t T_R1 = 0, T_R2 = 128, T_R3 = 256, T_R4 = 384;
+
+// MN-major B operand, no swizzle: SBO = stride between core matrices along
+// N (the contiguous 16 bytes), LBO = stride along K.
+static constexpr uint32_t MN_LBO = 2048, MN_SBO = 128;
+
+static constexpr int64_t WAIT_LIMIT = 1ll << 26;
+enum { SS_STATUS_ABORTED = 2 };
+
+struct MlpDev {
+    const float* params;
+    float c[4], s[4];
+    float out_scale, out_shift;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint8_t* mlp_smem() {
+    extern __shared__ uint8_t ss_mlp_dyn[];
+    return (uint8_t*)(((uintptr_t)ss_mlp_dyn + 1023) & ~(uintptr_t)1023);
+}
+
+// shared-memory matrix descriptor, no swizzle (tcgen05 descriptor version 1)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+
+// kind::f16 instruction descriptor: D F32, A and B BF16, M = N = 128,
+// A K-major, B K-major (b_mn = 0) or MN-major (b_mn = 1)
+__device__ __forceinline__ uint32_t idesc_bf16(uint32_t b_mn) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (b_mn << 16) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (int64_t it = 0; it < WAIT_LIMIT; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+#define SS_TMEM_LD32(r, taddr)                                                                                     \
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"  \
+                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"                       \
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), \
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),        \
+                   "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),      \
+                   "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),      \
+                   "=r"(r[29]), "=r"(r[30]), "=r"(r[31])                                                            \
+                 : "r"(taddr)                                                                                       \
+                 : "memory")
+
+#define SS_TMEM_ST32(taddr, r)                                                                                      \
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"    \
+                 "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),           \
+                 "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), \
+                 "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]),     \
+                 "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]),    \
+                 "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])                 \
+                 : "memory")
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// sigmoid via the hardware tanh: s(z) = 0.5 + 0.5 tanh(z / 2)
+__device__ __forceinline__ float sigm(float z) {
+    float t;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * z));
+    return fmaf(0.5f, t, 0.5f);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&v);
+}
+
+// 32 consecutive features (8-aligned chunk c of row t) into the A tile.
+__device__ __forceinline__ void store_row32(uint8_t* sm, int t, int c, const float v[32]) {
+    uint8_t* row = sm + SM_A + (t >> 3) * 2048 + (t & 7) * 16;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        uint4 w;
+        w.x = pack_bf16(v[8 * q + 0], v[8 * q + 1]);
+        w.y = pack_bf16(v[8 * q + 2], v[8 * q + 3]);
+        w.z = pack_bf16(v[8 * q + 4], v[8 * q + 5]);
+        w.w = pack_bf16(v[8 * q + 6], v[8 * q + 7]);
+        *reinterpret_cast<uint4*>(row + (4 * c + q) * 128) = w;
+    }
+}
+
+struct MlpCta {
+    uint32_t tmem;      // TMEM base (lane 0, column 0)
+    uint32_t lane_off;  // this warp's lane offset << 16
+    uint32_t bar;       // mbarrier shared address
+    uint32_t base;      // shared address of the aligned base
+};
+
+// Issue one 128x128x128 GEMM into TMEM column `dcol` and wait for it.
+// wsm: weight tile offset; b_mn: 0 = z = A W^T (forward), 1 = u = A W
+// (backward).  Returns false on a wait timeout (abort).
+__device__ __forceinline__ bool gemm_layer(const MlpCta& cx, uint32_t wsm, uint32_t b_mn, uint32_t dcol,
+                                           uint32_t parity, volatile uint32_t* abort) {
+    tmem_wait_st();
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    if (*abort) return false;
+    if (threadIdx.x == 0) {
+        fence_after();
+        const uint32_t id = idesc_bf16(b_mn);
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk) {
+            const uint64_t ad = smem_desc(cx.base + SM_A + kk * 256, 128, 2048);
+            const uint64_t bd = b_mn ? smem_desc(cx.base + wsm + kk * 4096, MN_LBO, MN_SBO)
+                                     : smem_desc(cx.base + wsm + kk * 256, 128, 2048);
+            mma_bf16(cx.tmem + dcol, ad, bd, id, kk > 0 ? 1u : 0u);
+        }
+        mma_commit(cx.bar);
+    }
+    const bool ok = mbar_wait(cx.bar, parity);
+    fence_after();
+    // every thread takes the same path after a timeout in any of them
+    if (__syncthreads_or(!ok)) {
+        *abort = 1u;
+        return false;
+    }
+    return true;
+}
+
+// grad Phi at X (FP32) for every thread of the CTA (collective).
+__device__ __noinline__ void mlp_grad_cta(const MlpDev& M, const MlpCta& cx, float X0, float X1, float X2, float& g0,
+                                          float& g1, float& g2) {
+    uint8_t* sm = mlp_smem();
+    volatile uint32_t* abort = reinterpret_cast<volatile uint32_t*>(sm + SM_ABORT);
+    const float* W1 = reinterpret_cast<const float*>(sm + SM_W1);
+    const float* Bb = reinterpret_cast<const float*>(sm + SM_B);
+    const float* w5 = reinterpret_cast<const float*>(sm + SM_W5);
+    const int t = threadIdx.x;
+    const uint32_t tl = cx.tmem + cx.lane_off;
+    g0 = g1 = g2 = 0.0f;
+    if (*abort) return;
+    const float r2 = X0 * X0 + X1 * X1 + X2 * X2;
+    const float u0 = (X0 - M.s[0]) * M.c[0], u1 = (X1 - M.s[1]) * M.c[1], u2 = (X2 - M.s[2]) * M.c[2];
+    const float u3 = (0.5f * logf(r2) - M.s[3]) * M.c[3];
+    // layer 1 on CUDA cores: a1 -> A tile, s'(z1) -> TMEM R1
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+        float a[32];
+        uint32_t sp[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const int f = 32 * c + j;
+            const float4 w = *reinterpret_cast<const float4*>(W1 + 4 * f);
+            const float z = fmaf(w.x, u0, fmaf(w.y, u1, fmaf(w.z, u2, fmaf(w.w, u3, Bb[f]))));
+            const float s = sigm(z);
+            a[j] = z * s;
+            sp[j] = __float_as_uint(s * fmaf(z, 1.0f - s, 1.0f));
+        }
+        store_row32(sm, t, c, a);
+        SS_TMEM_ST32(tl + T_R1 + 32 * c, sp);
+    }
+    // layers 2 and 3: z = a W^T + b, a = SiLU(z) -> A tile, s'(z) -> TMEM
+#pragma unroll 1
+    for (int k = 2; k <= 3; ++k) {
+        const uint32_t col = k == 2 ? T_R2 : T_R3;
+        if (!gemm_layer(cx, k == 2 ? SM_W2 : SM_W3, 0, col, k == 2 ? 0u : 1u, abort)) return;
+        const float* bk = Bb + (k - 1) * MLP_W;
+#pragma unroll 1
+        for (int c = 0; c < 4; ++c) {
+            uint32_t r[32];
+            float a[32];
+            SS_TMEM_LD32(r, tl + col + 32 * c);
+            tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const float z = __uint_as_float(r[j]) + bk[32 * c + j];
+                const float s = sigm(z);
+                a[j] = z * s;
+                r[j] = __float_as_uint(s * fmaf(z, 1.0f - s, 1.0f));
+            }
+            store_row32(sm, t, c, a);
+            SS_TMEM_ST32(tl + col + 32 * c, r);
+        }
+    }
+    // layer 4: only s'(z4) is needed: d4 = w5 s'(z4) -> A tile
+    if (!gemm_layer(cx, SM_W4, 0, T_R4, 0u, abort)) return;
+    {
+        const float* b4 = Bb + 3 * MLP_W;
+#pragma unroll 1
+        for (int c = 0; c < 4; ++c) {
+            uint32_t r[32];
+            float d[32];
+            SS_TMEM_LD32(r, tl + T_R4 + 32 * c);
+            tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const float z = __uint_as_float(r[j]) + b4[32 * c + j];
+                const float s = sigm(z);
+                d[j] = w5[32 * c + j] * (s * fmaf(z, 1.0f - s, 1.0f));
+            }
+            store_row32(sm, t, c, d);
+        }
+    }
+    // backward: u = d W_k (MN-major B), d_{k-1} = u s'(z_{k-1})
+    const uint32_t wk[3] = {SM_W4, SM_W3, SM_W2};
+    const uint32_t sk[3] = {T_R3, T_R2, T_R1};
+    float gi[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll 1
+    for (int q = 0; q < 3; ++q) {
+        if (!gemm_layer(cx, wk[q], 1, T_R4, q == 1 ? 0u : 1u, abort)) return;
+#pragma unroll 1
+        for (int c = 0; c < 4; ++c) {
+            uint32_t r[32], s[32];
+            SS_TMEM_LD32(r, tl + T_R4 + 32 * c);
+            SS_TMEM_LD32(s, tl + sk[q] + 32 * c);
+            tmem_wait_ld();
+            float d[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) d[j] = __uint_as_float(r[j]) * __uint_as_float(s[j]);
+            if (q < 2) {
+                store_row32(sm, t, c, d);
+            } else {
+                // g = W1^T d1 (FP32)
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const float4 w = *reinterpret_cast<const float4*>(W1 + 4 * (32 * c + j));
+                    gi[0] = fmaf(w.x, d[j], gi[0]);
+                    gi[1] = fmaf(w.y, d[j], gi[1]);
+                    gi[2] = fmaf(w.z, d[j], gi[2]);
+                    gi[3] = fmaf(w.w, d[j], gi[3]);
+                }
+            }
+        }
+    }
+    const float k3 = gi[3] * M.c[3] / r2;
+    g0 = M.out_scale * (gi[0] * M.c[0] + k3 * X0);
+    g1 = M.out_scale * (gi[1] * M.c[1] + k3 * X1);
+    g2 = M.out_scale * (gi[2] * M.c[2] + k3 * X2);
+}
+
+// The "composition" handed to step_f32k: its gradient is the CTA-collective
+// network evaluation (the CTA context lives in shared memory).
+struct MlpComp {
+    static constexpr int n = 1;
+    template <class T, class R, bool HESS>
+    static __device__ __forceinline__ void grad(const PotDev<R>& P, const T x[3], const T xs[3], T g[3], T H[6]);
+};
+
+struct MlpKernelArgs {
+    MlpDev M;
+    StreamArgs a;
+    int64_t n_tiles;
+};
+
+__device__ __forceinline__ const MlpKernelArgs*& mlp_args_ptr() {
+    __shared__ const MlpKernelArgs* p;
+    return p;
+}
+
+template <class T, class R, bool HESS>
+__device__ __forceinline__ void MlpComp::grad(const PotDev<R>&, const T x[3], const T*, T g[3], T*) {
+    uint8_t* sm = mlp_smem();
+    MlpCta cx;
+    cx.tmem = *reinterpret_cast<volatile uint32_t*>(sm + SM_TMEM);
+    cx.lane_off = (uint32_t)(32 * (threadIdx.x >> 5)) << 16;
+    cx.bar = smem_u32(sm + SM_BAR);
+    cx.base = smem_u32(sm);
+    const MlpKernelArgs* ka = mlp_args_ptr();
+    mlp_grad_cta(ka->M, cx, x[0], x[1], x[2], g[0], g[1], g[2]);
+}
+
+// CTA prologue: weights -> shared memory (BF16 core-matrix tiles, FP32
+// small parts), mbarrier, 512 TMEM columns.
+__device__ __forceinline__ void mlp_cta_setup(const MlpKernelArgs& ka) {
+    uint8_t* sm = mlp_smem();
+    const int t = threadIdx.x;
+    const float* prm = ka.M.params;
+    for (int e = t; e < 3 * 16384; e += 128) {
+        const int k = e / 16384, idx = e % 16384, o = idx / 128, i = idx % 128;
+        const float w = prm[(k == 0 ? P_W2 : k == 1 ? P_W3 : P_W4) + idx];
+        __nv_bfloat16 b = __float2bfloat16_rn(w);
+        *reinterpret_cast<__nv_bfloat16*>(sm + 32768 * k + (o >> 3) * 2048 + (i >> 3) * 128 + (o & 7) * 16 +
+                                          (i & 7) * 2) = b;
+    }
+    float* W1 = reinterpret_cast<float*>(sm + SM_W1);
+    float* Bb = reinterpret_cast<float*>(sm + SM_B);
+    float* w5 = reinterpret_cast<float*>(sm + SM_W5);
+    for (int e = t; e < 512; e += 128) W1[e] = prm[P_W1 + e];
+    for (int e = t; e < 128; e += 128) {
+        Bb[e] = prm[P_B1 + e];
+        Bb[128 + e] = prm[P_B2 + e];
+        Bb[256 + e] = prm[P_B3 + e];
+        Bb[384 + e] = prm[P_B4 + e];
+        w5[e] = prm[P_W5 + e];
+    }
+    if (t == 0) {
+        mlp_args_ptr() = &ka;
+        *reinterpret_cast<uint32_t*>(sm + SM_ABORT) = 0u;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(sm + SM_BAR)), "r"(1));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if ((t >> 5) == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(sm + SM_TMEM)),
+                     "r"(512));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+}
+
+// CTA epilogue: release TMEM (after a timeout, first give the outstanding
+// commit a bounded wait).
+__device__ __forceinline__ void mlp_cta_teardown() {
+    uint8_t* sm = mlp_smem();
+    volatile uint32_t* abort = reinterpret_cast<volatile uint32_t*>(sm + SM_ABORT);
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (*abort && threadIdx.x == 0) {
+        mbar_wait(smem_u32(sm + SM_BAR), 0u);
+        mbar_wait(smem_u32(sm + SM_BAR), 1u);
+    }
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) {
+        const uint32_t tm = *reinterpret_cast<volatile uint32_t*>(sm + SM_TMEM);
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(512));
+    }
+}
+
+// grad Phi of the surrogate at points xyz [n,3] (tensor-core path; tests)
+__global__ void __launch_bounds__(128, 1) mlp_grad_kernel(const __grid_constant__ MlpKernelArgs ka, const double* xyz,
+                                                          int64_t n, double* grad, int32_t* status) {
+    mlp_cta_setup(ka);
+    uint8_t* sm = mlp_smem();
+    volatile uint32_t* abort = reinterpret_cast<volatile uint32_t*>(sm + SM_ABORT);
+    PotDev<float> P;
+    P.n = 0;
+    P.has_track = 0;
+    for (int64_t tile = blockIdx.x; tile < (n + 127) / 128; tile += gridDim.x) {
+        const int64_t p = tile * 128 + threadIdx.x;
+        const int64_t q = p < n ? p : 0;
+        const float x[3] = {(float)xyz[3 * q], (float)xyz[3 * q + 1], (float)xyz[3 * q + 2]};
+        float g[3];
+        MlpComp::grad<float, float, false>(P, x, x, g, nullptr);
+        if (p < n) {
+            for (int i = 0; i < 3; ++i) grad[3 * p + i] = (double)g[i];
+            if (status) status[p] = *abort ? SS_STATUS_ABORTED : 0;
+        }
+        if (*abort) break;
+    }
+    mlp_cta_teardown();
+}
+
+__global__ void __launch_bounds__(128, 1) stream_mlp_kernel(const __grid_constant__ MlpKernelArgs ka) {
+    mlp_cta_setup(ka);
+    uint8_t* sm = mlp_smem();
+    const int t = threadIdx.x;
+    const StreamArgs& a = ka.a;
+    volatile uint32_t* abort = reinterpret_cast<volatile uint32_t*>(sm + SM_ABORT);
+    PotDev<float> P;  // unused by MlpComp (no track, no subhalos)
+    P.n = 0;
+    P.has_track = 0;
+    for (int64_t tile = blockIdx.x; tile < ka.n_tiles; tile += gridDim.x) {
+        const int64_t p = tile * 128 + t;
+        const bool valid = p < a.N;
+        const int start = valid ? (int)((p / a.ppr) * (int64_t)a.spr) : a.n_steps;
+        // the tile steps from its earliest start; particles not yet released
+        // step a copy (their rows of the GEMMs are independent)
+        int* s_start = reinterpret_cast<int*>(sm + SM_START);
+        if (t == 0) *s_start = a.n_steps;
+        __syncthreads();
+        atomicMin(s_start, start);
+        __syncthreads();
+        const int tstart = *s_start;
+        float xh[3], xl[3], vh[3], vl[3];
+        const int64_t q = valid ? p : (a.N > 0 ? (int64_t)0 : 0);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const double xd = a.ics[6 * q + i], vd = a.ics[6 * q + 3 + i];
+            xh[i] = (float)xd;
+            xl[i] = (float)(xd - (double)xh[i]);
+            vh[i] = (float)vd;
+            vl[i] = (float)(vd - (double)vh[i]);
+        }
+        if (a.snaps && valid) {
+            const float y[6] = {xh[0], xh[1], xh[2], vh[0], vh[1], vh[2]};
+            for (int64_t k = 0; (k + 1) * (int64_t)a.stride <= tstart; ++k)
+                write_snap<float>(a.snaps, a.N, k, p, (k + 1) * (int64_t)a.stride >= start, y);
+        }
+        for (int n = tstart; n < a.n_steps; ++n) {
+            if (*abort) break;
+            float th[3], tlo[3], uh[3], ul[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                th[i] = xh[i];
+                tlo[i] = xl[i];
+                uh[i] = vh[i];
+                ul[i] = vl[i];
+            }
+            step_f32k<MlpComp>(P, a, n, th, tlo, uh, ul);
+            if (valid && n >= start) {
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    xh[i] = th[i];
+                    xl[i] = tlo[i];
+                    vh[i] = uh[i];
+                    vl[i] = ul[i];
+                }
+            }
+            if (a.snaps && (n + 1) % a.stride == 0 && valid) {
+                const float y[6] = {xh[0], xh[1], xh[2], vh[0], vh[1], vh[2]};
+                write_snap<float>(a.snaps, a.N, (n + 1) / a.stride - 1, p, n + 1 >= start, y);
+            }
+        }
+        if (valid) {
+            bool ok = true;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) ok = ok && isfinite(xh[i]) && isfinite(vh[i]) && isfinite(xl[i]) && isfinite(vl[i]);
+            if (a.status) a.status[p] = *abort ? SS_STATUS_ABORTED : (ok ? 0 : 1);
+            if (a.final_w) {
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    a.final_w[6 * p + i] = (double)xh[i] + (double)xl[i];
+                    a.final_w[6 * p + 3 + i] = (double)vh[i] + (double)vl[i];
+                }
+            }
+        }
+        if (*abort) break;
+    }
+    mlp_cta_teardown();
+}
+
+static void mlp_dev_of(const ss_mlp* mlp, MlpDev* M) {
+    M->params = mlp->params;
+    for (int i = 0; i < 4; ++i) {
+        M->c[i] = mlp->in_scale[i];
+        M->s[i] = mlp->in_shift[i];
+    }
+    M->out_scale = mlp->out_scale;
+    M->out_shift = mlp->out_shift;
+}
+
+}  // namespace ssg
+
+using namespace ssg;
+
+extern "C" {
+
+int ss_mlp_grad_bf16(const ss_mlp* mlp, const double* xyz, int64_t n, double* grad, int32_t* status, void* stream) {
+    SS_CHECK_ARG(mlp != nullptr && mlp->params != nullptr, "mlp or its params is NULL");
+    SS_CHECK_ARG(n >= 0, "n < 0");
+    if (n == 0) return SS_OK;
+    SS_CHECK_ARG(xyz != nullptr && grad != nullptr, "NULL buffer");
+    MlpKernelArgs ka;
+    memset(&ka, 0, sizeof(ka));
+    mlp_dev_of(mlp, &ka.M);
+    int dev = 0, sms = 0;
+    SS_CUDA_TRY(cudaGetDevice(&dev));
+    SS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    SS_CUDA_TRY(cudaFuncSetAttribute(mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM_ALLOC));
+    const int64_t tiles = (n + 127) / 128;
+    mlp_grad_kernel<<<(unsigned)(tiles < sms ? tiles : sms), 128, SM_ALLOC, (cudaStream_t)stream>>>(ka, xyz, n, grad,
+                                                                                                      status);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
+int64_t ss_stream_mlp_workspace_bytes(const ss_stream_cfg* cfg) {
+    if (cfg == nullptr) return set_error(SS_ERR_INVALID_ARGUMENT, "cfg is NULL");
+    return 0;
+}
+
+int ss_stream_mlp_bf16(const ss_mlp* mlp, const ss_stream_cfg* cfg, const double* ics, double* final_w, float* snaps,
+                       int32_t* status, void* workspace, int64_t workspace_bytes, void* stream) {
+    (void)workspace;
+    (void)workspace_bytes;
+    SS_CHECK_ARG(mlp != nullptr && mlp->params != nullptr, "mlp or its params is NULL");
+    SS_CHECK_ARG(cfg != nullptr, "cfg is NULL");
+    SS_CHECK_ARG(cfg->n_particles >= 0, "n_particles < 0");
+    SS_CHECK_ARG(cfg->n_steps >= 0 && cfg->n_steps < (1LL << 30), "n_steps outside [0, 2^30)");
+    SS_CHECK_ARG(cfg->particles_per_release >= 1 && cfg->steps_per_release >= 0, "bad release layout");
+    SS_CHECK_ARG(std::isfinite(cfg->dt) && cfg->dt > 0.0 && std::isfinite(cfg->t0), "dt must be finite and > 0");
+    SS_CHECK_ARG(cfg->snap_stride >= 0, "snap_stride < 0");
+    const int64_t n_rel = (cfg->n_particles + cfg->particles_per_release - 1) / cfg->particles_per_release;
+    SS_CHECK_ARG(n_rel == 0 || (n_rel - 1) * (int64_t)cfg->steps_per_release <= cfg->n_steps,
+                 "last release starts after n_steps");
+    if (cfg->n_particles == 0) return SS_OK;
+    SS_CHECK_ARG(ics != nullptr, "ics is NULL");
+    MlpKernelArgs ka;
+    memset(&ka, 0, sizeof(ka));
+    mlp_dev_of(mlp, &ka.M);
+    StreamArgs& a = ka.a;
+    a.ics = ics;
+    a.final_w = final_w;
+    a.snaps = cfg->snap_stride > 0 && cfg->n_steps >= cfg->snap_stride ? snaps : nullptr;
+    a.status = status;
+    a.N = cfg->n_particles;
+    a.ppr = cfg->particles_per_release;
+    a.spr = cfg->steps_per_release;
+    a.n_steps = (int32_t)cfg->n_steps;
+    a.stride = cfg->snap_stride > 0 ? cfg->snap_stride : 1;
+    a.t0 = cfg->t0;
+    a.dt = cfg->dt;
+    a.h_hi = (float)cfg->dt;
+    a.h_lo = (float)(cfg->dt - (double)a.h_hi);
+    ka.n_tiles = (cfg->n_particles + 127) / 128;
+    int dev = 0, sms = 0;
+    SS_CUDA_TRY(cudaGetDevice(&dev));
+    SS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    SS_CUDA_TRY(cudaFuncSetAttribute(stream_mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM_ALLOC));
+    const int64_t grid = ka.n_tiles < sms ? ka.n_tiles : sms;
+    stream_mlp_kernel<<<(unsigned)grid, 128, SM_ALLOC, (cudaStream_t)stream>>>(ka);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
+}  // extern "C"

@@ -28,7 +28,7 @@
 namespace ssg {
 
 static constexpr int SHOOT_M = 16;  // FP64 steps per slice
-static constexpr int SHOOT_C = 4;   // FP64 steps per coarse FP32 guess step
+static constexpr int SHOOT_C = 8;   // FP64 steps per coarse FP32 guess step
 static constexpr int SHOOT_ITERS = 8;
 
 struct ShootArgs {
@@ -114,6 +114,7 @@ __global__ void __launch_bounds__(96) shoot_slice_kernel(PotDev<double> P, Shoot
     PotDev<T> Q;
     Q.n = P.n;
     Q.has_track = 0;
+    Q.ex = P.ex;
 #pragma unroll
     for (int c = 0; c < C::n; ++c) {
         Q.c[c].kind = P.c[c].kind;
@@ -134,34 +135,64 @@ __global__ void __launch_bounds__(96) shoot_slice_kernel(PotDev<double> P, Shoot
         for (int j = 0; j < 6; ++j) a.F[6 * n + j] = y[j].v;
 }
 
-// Newton sweep over the slice joins.
-__global__ void shoot_sweep_kernel(ShootArgs a) {
-    if (threadIdx.x != 0 || blockIdx.x != 0 || a.flag[0]) return;
+// Newton sweep over the slice joins.  The recurrence is serial and its
+// FP64 FMA chain (6 deep per slice) is latency-bound, so the block stages
+// chunks of J, F and U in shared memory with coalesced loads and one thread
+// runs the chain from there; the convergence test compares squares (no
+// division or square root on the serial path).
+static constexpr int SWEEP_CHUNK = 64;
+static constexpr int SWEEP_THREADS = 128;
+
+__global__ void __launch_bounds__(SWEEP_THREADS) shoot_sweep_kernel(ShootArgs a) {
+    if (a.flag[0]) return;
+    __shared__ double sJ[SWEEP_CHUNK * 36];
+    __shared__ double sF[SWEEP_CHUNK * 6];
+    __shared__ double sU[SWEEP_CHUNK * 6];
     double d[6] = {0, 0, 0, 0, 0, 0};  // U_n^new - U_n^old (zero at n = 0)
-    double worst = 0.0;
-    for (int n = 0; n < a.S; ++n) {
-        double unew[6], uold[6];
-        for (int r = 0; r < 6; ++r) {
-            double s = a.F[6 * n + r];
-            for (int c = 0; c < 6; ++c) s += a.J[36 * n + 6 * r + c] * d[c];
-            unew[r] = s;
-            uold[r] = a.U[6 * (n + 1) + r];
+    const double tol2 = a.tol * a.tol;
+    bool ok = true;
+    for (int base = 0; base < a.S; base += SWEEP_CHUNK) {
+        const int cnt = min(SWEEP_CHUNK, a.S - base);
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt * 36; k += blockDim.x) sJ[k] = a.J[36 * base + k];
+        for (int k = threadIdx.x; k < cnt * 6; k += blockDim.x) {
+            sF[k] = a.F[6 * base + k];
+            sU[k] = a.U[6 * (base + 1) + k];
         }
-        double dx = 0.0, dv = 0.0, nx = 0.0, nv = 0.0;
-        for (int r = 0; r < 3; ++r) {
-            dx += (unew[r] - uold[r]) * (unew[r] - uold[r]);
-            dv += (unew[3 + r] - uold[3 + r]) * (unew[3 + r] - uold[3 + r]);
-            nx += unew[r] * unew[r];
-            nv += unew[3 + r] * unew[3 + r];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int n = 0; n < cnt; ++n) {
+                double unew[6];
+#pragma unroll
+                for (int r = 0; r < 6; ++r) {
+                    double s = sF[6 * n + r];
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) s = fma(sJ[36 * n + 6 * r + c], d[c], s);
+                    unew[r] = s;
+                }
+                double dx = 0.0, dv = 0.0, nx = 0.0, nv = 0.0;
+#pragma unroll
+                for (int r = 0; r < 6; ++r) {
+                    d[r] = unew[r] - sU[6 * n + r];
+                    sU[6 * n + r] = unew[r];
+                }
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    dx = fma(d[r], d[r], dx);
+                    dv = fma(d[3 + r], d[3 + r], dv);
+                    nx = fma(unew[r], unew[r], nx);
+                    nv = fma(unew[3 + r], unew[3 + r], nv);
+                }
+                ok = ok && dx <= tol2 * nx && dv <= tol2 * nv;
+            }
         }
-        worst = fmax(worst, fmax(sqrt(dx / fmax(nx, 1e-300)), sqrt(dv / fmax(nv, 1e-300))));
-        for (int r = 0; r < 6; ++r) {
-            d[r] = unew[r] - uold[r];
-            a.U[6 * (n + 1) + r] = unew[r];
-        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt * 6; k += blockDim.x) a.U[6 * (base + 1) + k] = sU[k];
     }
-    a.flag[1] += 1;
-    if (worst < a.tol) a.flag[0] = 1;
+    if (threadIdx.x == 0) {
+        a.flag[1] += 1;
+        if (ok) a.flag[0] = 1;
+    }
 }
 
 // Converged starts -> saved states (plain FP64 steps, the serial step map).
@@ -189,7 +220,7 @@ static int launch_shoot(const PotDev<double>& P, const PotDev<float>& P32, const
     shoot_guess_kernel<C><<<1, 32, 0, st>>>(P32, a);
     for (int it = 0; it < SHOOT_ITERS; ++it) {
         shoot_slice_kernel<C><<<(unsigned)((6 * a.S + 95) / 96), 96, 0, st>>>(P, a);
-        shoot_sweep_kernel<<<1, 32, 0, st>>>(a);
+        shoot_sweep_kernel<<<1, SWEEP_THREADS, 0, st>>>(a);
     }
     return 1 + 2 * SHOOT_ITERS;
 }
@@ -223,6 +254,7 @@ template <class S_>
 __device__ __forceinline__ void seed_params(const PotDev<double>& P, const TanArgs& a, int slot, PotDev<D1<S_>>& Q) {
     Q.n = P.n;
     Q.has_track = 0;
+    Q.ex = P.ex;
     for (int c = 0; c < P.n; ++c) {
         double dq[6] = {0, 0, 0, 0, 0, 0};
         if (slot >= 0 && slot / 6 == c) prepared_param_tangent(P.c[c].kind, a.raw + 6 * c, slot % 6, a.G, dq);

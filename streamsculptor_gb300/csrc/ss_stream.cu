@@ -98,6 +98,29 @@ static StreamArgs make_args(const ss_stream_cfg* cfg, const double* ics, double*
     return a;
 }
 
+static bool has_expansion(const ss_potential* pot) {
+    for (int k = 0; k < pot->n_components && k < SS_MAX_COMPONENTS; ++k)
+        if (pot->comp[k].kind == SS_SH_EXPANSION) return true;
+    return false;
+}
+
+static int64_t expansion_table_bytes(const ss_expansion& e) {
+    const int64_t nt = (int64_t)(e.l_max + 1) * (e.l_max + 1);
+    return (int64_t)(e.n_knots - 1) * nt * (int64_t)sizeof(float4);
+}
+
+// FP32 per-interval copy of the expansion's spline table:
+// {f_k, du f'_k, f_k+1, du f'_k+1} for interval k and term j.
+__global__ void expansion_table_kernel(ExpDev E, float4* out) {
+    const int nt = (E.lmax + 1) * (E.lmax + 1);
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)(E.nk - 1) * nt) return;
+    const int64_t k = i / nt, j = i - k * nt;
+    const double* a = E.tab64 + (k * nt + j) * 2;
+    const double* b = a + 2 * nt;
+    out[i] = make_float4((float)a[0], (float)(a[1] * E.du), (float)b[0], (float)(b[1] * E.du));
+}
+
 static int64_t f32k_workspace(const ss_potential* pot, const ss_stream_cfg* cfg) {
     int64_t bytes = 0;
     bool track = false;
@@ -105,6 +128,8 @@ static int64_t f32k_workspace(const ss_potential* pot, const ss_stream_cfg* cfg)
     if (track) bytes += (5 * cfg->n_steps + 1) * 2 * (int64_t)sizeof(float4);
     bytes = (bytes + 255) / 256 * 256;
     if (pot->subhalos.n > 0) bytes += 3 * pot->subhalos.n * (int64_t)sizeof(float4);
+    bytes = (bytes + 255) / 256 * 256;
+    if (has_expansion(pot)) bytes += expansion_table_bytes(pot->expansion);
     return bytes;
 }
 
@@ -175,6 +200,14 @@ int ss_stream_f32k(const ss_potential* pot, const ss_stream_cfg* cfg, const doub
         a.shtab = tab;
         a.n_sh = Pd.sh.n;
         a.sh_kind = Pd.sh.kind;
+        ws += (3 * Pd.sh.n * (int64_t)sizeof(float4) + 255) / 256 * 256;
+    }
+    if (P.ex.tab64) {
+        float4* tab = (float4*)ws;
+        const int64_t total = (int64_t)(P.ex.nk - 1) * (P.ex.lmax + 1) * (P.ex.lmax + 1);
+        expansion_table_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(P.ex, tab);
+        SS_LAUNCH_CHECK();
+        P.ex.tab32 = tab;
     }
     const int block = 128;
     unsigned grid = (unsigned)((cfg->n_particles + block - 1) / block);

@@ -79,6 +79,72 @@ class HernquistPotential(Potential):
         return Flat([(_abi.SS_HERNQUIST, _abi.SS_CENTER_ORIGIN, (_f(self.m), _f(self.r_s), _f(self.soft)))])
 
 
+class SphericalHarmonicExpansionPotential(Potential):
+    """Multipole expansion Phi = scale * sum_lm f_lm(r) Y_lm(theta, phi) with
+    real Schmidt semi-normalised harmonics up to l_max <= 8 and cubic Hermite
+    radial splines in ln r (the layout of ss_expansion in the C header).
+    The reference names an optional multipole package (bfeax) for such
+    potentials; this class is the table-driven form the kernels evaluate.
+
+    coef: [n_knots, (l_max+1)^2, 2] value and d f / d ln r of every f_lm at
+    the knots ln r_k = log_r0 + k dlog_r; term index l*l + l + m (m < 0 are
+    the sin(|m| phi) parts)."""
+
+    def __init__(self, coef, log_r0, dlog_r, scale=1.0, units=None):
+        c = torch.as_tensor(np.asarray(coef) if not torch.is_tensor(coef) else coef, dtype=torch.float64)
+        if c.ndim != 3 or c.shape[2] != 2 or c.shape[0] < 2:
+            raise ValueError("coef must be [n_knots >= 2, (l_max+1)^2, 2]")
+        l_max = int(round(np.sqrt(c.shape[1]))) - 1
+        if (l_max + 1) ** 2 != c.shape[1] or l_max > _abi.SS_SHEXP_LMAX:
+            raise ValueError(f"coef has {c.shape[1]} terms: need (l_max+1)^2 with l_max <= {_abi.SS_SHEXP_LMAX}")
+        super().__init__(units, {"coef": c, "log_r0": float(log_r0), "dlog_r": float(dlog_r), "scale": scale,
+                                 "l_max": l_max})
+        self._table = None
+
+    def _flatten(self):
+        if self._table is None:
+            self._table = _core.ExpansionTable(self.l_max, self.log_r0, self.dlog_r,
+                                               self.coef.to(_core.device()).contiguous())
+        return Flat([(_abi.SS_SH_EXPANSION, _abi.SS_CENTER_ORIGIN, (_f(self.scale),))], expansion=self._table)
+
+
+def _nfw_phi_and_rderiv(r, GM, rs):
+    """NFW potential and r dPhi/dr (= dPhi/d ln r)."""
+    L = np.log1p(r / rs)
+    phi = -GM * L / r
+    dphidr = GM * (L / r ** 2 - 1.0 / (r * (r + rs)))
+    return phi, r * dphidr
+
+
+def seeded_triaxial_expansion(m=5.4e11, r_s=15.62, eps=0.1, l_max=8, n_knots=64, r_min=0.1, r_max=200.0,
+                              seed=4, units=None) -> SphericalHarmonicExpansionPotential:
+    """A triaxial halo as a spherical-harmonic expansion: the monopole is the
+    NFW(m, r_s) potential and every even-l, even-m cosine term (triaxial
+    symmetry) with l >= 2 is
+        f_lm(r) = eps 2^-l z_lm Phi_NFW(r) r^2 / (r^2 + r_s^2),   z_lm ~ N(0, 1)
+    from numpy's PCG64(seed), on n_knots log-spaced knots over [r_min, r_max]
+    with exact knot derivatives."""
+    G = _core.G_for(units)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    log_r0 = np.log(r_min)
+    dlog_r = (np.log(r_max) - np.log(r_min)) / (n_knots - 1)
+    r = np.exp(log_r0 + dlog_r * np.arange(n_knots))
+    phi0, dphi0 = _nfw_phi_and_rderiv(r, G * m, r_s)
+    g = r ** 2 / (r ** 2 + r_s ** 2)
+    dg = 2.0 * r ** 2 * r_s ** 2 / (r ** 2 + r_s ** 2) ** 2  # r dg/dr
+    nt = (l_max + 1) ** 2
+    coef = np.zeros((n_knots, nt, 2))
+    coef[:, 0, 0], coef[:, 0, 1] = phi0, dphi0
+    for l in range(2, l_max + 1, 2):
+        for mm in range(0, l + 1, 2):
+            z = rng.standard_normal()
+            a = eps * 2.0 ** -l * z
+            j = l * l + l + mm
+            coef[:, j, 0] = a * phi0 * g
+            coef[:, j, 1] = a * (dphi0 * g + phi0 * dg)
+    return SphericalHarmonicExpansionPotential(coef, log_r0, dlog_r, units=units)
+
+
 class Potential_Combine(Potential):
     """Sum of potentials in list order (potential.py:1279-1296)."""
 

@@ -13,6 +13,12 @@ Force evaluation (ss_device.cuh, comp_grad without Hessian), per component:
   Hernquist    r^2 (5) + soft (1) + r+rs (1) + g (3) + grad (6)      = 16; specials 3
   Plummer      r^2 (5) + b^2 (1) + g (3) + grad (6)                    = 15; specials 1
   Isochrone    r^2 (5) + a^2 (1) + a+s (1) + g (3) + grad (6)          = 16; specials 3
+  SH expansion (l_max, nt = (l_max+1)^2 terms; gradient only):
+               r^2, n = x/r, ln r, spline basis (~45) + solid-harmonic
+               recurrences up to degree 8 (232) + per term: spline value and
+               slope (17), radial factors a0, a1, G1 (6), S1 += G1 K (2),
+               angular gradient (5), V += a0 grad K (6) = 36 / term;
+               total 270 + 36 nt (3186 at l_max = 8); specials 2 (rsqrt, log)
   translating  + 3 (x - c(t))
   subhalo line + 9 (line position) + 15 (Plummer form) + 1 window test
 Dopri5 combinations per step (6 force evaluations, FSAL reuse):
@@ -41,7 +47,11 @@ def force_work(flat) -> tuple:
     """(flops, specials) of one force evaluation of a flattened potential."""
     fl, sp = 0, 0
     for kind, center, _ in flat.comps:
-        f, s = FORCE_FLOPS[kind]
+        if kind == _abi.SS_SH_EXPANSION:
+            nt = (flat.expansion.l_max + 1) ** 2
+            f, s = 270 + 36 * nt, 2
+        else:
+            f, s = FORCE_FLOPS[kind]
         fl += f + (TRANSLATE_FLOPS if center == _abi.SS_CENTER_TRACK else 0)
         sp += s
     if flat.subhalos is not None:

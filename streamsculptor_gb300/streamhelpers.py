@@ -39,7 +39,8 @@ def chen25_factor(cov=CHEN25_COV) -> np.ndarray:
 def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=None, *, solver=None,
                kval_arr=1.0, dt=None, dtmax=None, n_particles_per_release=2, normals=None, precision="f64",
                snapshot_every=None, throw=False, release="fardal", prog_pot: Optional[Potential] = None,
-               pot_pert: Optional[Potential] = None, prog_in_pert=False, return_ics=False, prog_method="auto"):
+               pot_pert: Optional[Potential] = None, prog_in_pert=False, return_ics=False, prog_method="auto",
+               force_surrogate=None):
     """Generate a particle-spray stream on the GPU.
 
     pot_base    smooth potential (release model and integration)
@@ -53,6 +54,10 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
     prog_method progenitor orbit solver (FP64 either way): 'serial', 'shoot'
                 (parallel in time, multiple shooting) or 'auto' (shoot when the
                 progenitor's potential is static)
+    precision   'f64', 'f32k' (FP32 compensated) or 'mlp': the particles move
+                in the force of `force_surrogate` (surrogate.MLPSurrogate, BF16
+                tensor cores) while the progenitor orbit and the release use
+                the exact pot_base
     Returns (lead, trail) [len(ts)-1, 6] (or [len(ts)-1, n_draw, 6]); with
     snapshot_every also the float32 snapshots [n_snap, len(ts)-1, n_draw, 2, 6].
     """
@@ -93,7 +98,10 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
         n_snap = cfg.n_steps // int(snapshot_every)
         snaps = torch.empty(n_snap, N, 6, dtype=torch.float32, device=ws.device)
     stream_ics = ics[:n_rel].reshape(N, 6).contiguous()
-    final, status = _core.stream(integ._desc(), cfg, stream_ics, precision, snaps=snaps)
+    if precision == "mlp" and (integ is not pot_base or force_surrogate is None):
+        raise NotImplementedError("precision='mlp' integrates in the surrogate alone: give force_surrogate and no "
+                                  "prog_pot / pot_pert")
+    final, status = _core.stream(integ._desc(), cfg, stream_ics, precision, snaps=snaps, mlp=force_surrogate)
     if throw and bool((status != 0).any()):
         raise RuntimeError("gen_stream: non-finite particle state")
     final = final.reshape(n_rel, n_draw, 2, 6)

@@ -1,0 +1,200 @@
+"""Learned force surrogate for expensive potentials (the spherical-harmonic
+expansion): an MLP (x, y, z, ln r) -> Phi with 4 hidden SiLU layers of width
+128, trained on the GPU by the library's own kernels (ss_mlp_loss_grad:
+value + force loss differentiated through the network's input gradient;
+ss_mlp_adam), evaluated in FP32 on CUDA cores (ss_mlp_eval) or with BF16
+weights on the tensor cores inside the stream integrator
+(ss_stream_mlp_bf16).  The exact potential stays the reference: it makes
+the training set and judges the surrogate's error.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _abi, _core
+from ._core import ptr, stream_handle
+
+NPARAM = _abi.SS_MLP_NPARAM
+W = _abi.SS_MLP_WIDTH
+# packed offsets (W[out][in])
+OFF = {"W1": 0, "b1": 512, "W2": 640, "b2": 640 + 16384, "W3": 640 + 16384 + 128,
+       "b3": 640 + 2 * 16384 + 128, "W4": 640 + 2 * 16384 + 256, "b4": 640 + 3 * 16384 + 256,
+       "w5": 640 + 3 * 16384 + 384, "b5": 640 + 3 * 16384 + 512}
+
+
+def unpack(params: torch.Tensor) -> dict:
+    """Views of the packed parameter vector as matrices / vectors."""
+    p = params
+    return {"W1": p[0:512].view(W, 4), "b1": p[512:640],
+            "W2": p[OFF["W2"]:OFF["b2"]].view(W, W), "b2": p[OFF["b2"]:OFF["W3"]],
+            "W3": p[OFF["W3"]:OFF["b3"]].view(W, W), "b3": p[OFF["b3"]:OFF["W4"]],
+            "W4": p[OFF["W4"]:OFF["b4"]].view(W, W), "b4": p[OFF["b4"]:OFF["w5"]],
+            "w5": p[OFF["w5"]:OFF["b5"]], "b5": p[OFF["b5"]:OFF["b5"] + 1]}
+
+
+@dataclass
+class MLPSurrogate:
+    params: torch.Tensor                 # [NPARAM] float32 (device)
+    in_scale: tuple = (1.0, 1.0, 1.0, 1.0)
+    in_shift: tuple = (0.0, 0.0, 0.0, 0.0)
+    out_scale: float = 1.0
+    out_shift: float = 0.0
+    history: list = field(default_factory=list)
+
+    @staticmethod
+    def init(seed=0, in_scale=(1.0, 1.0, 1.0, 1.0), in_shift=(0.0, 0.0, 0.0, 0.0), out_scale=1.0, out_shift=0.0,
+             device=None) -> "MLPSurrogate":
+        """Random initialisation: W ~ N(0, 1/fan_in), zero biases."""
+        g = torch.Generator().manual_seed(seed)
+        p = torch.zeros(NPARAM, dtype=torch.float32)
+        v = unpack(p)
+        v["W1"].copy_(torch.randn(W, 4, generator=g) / math.sqrt(4.0))
+        for k in ("W2", "W3", "W4"):
+            v[k].copy_(torch.randn(W, W, generator=g) / math.sqrt(W))
+        v["w5"].copy_(torch.randn(W, generator=g) / math.sqrt(W))
+        return MLPSurrogate(p.to(device or _core.device()), tuple(in_scale), tuple(in_shift), float(out_scale),
+                            float(out_shift))
+
+    def struct(self) -> _abi.ss_mlp:
+        m = _abi.ss_mlp()
+        m.params = self.params.data_ptr()
+        for i in range(4):
+            m.in_scale[i] = float(self.in_scale[i])
+            m.in_shift[i] = float(self.in_shift[i])
+        m.out_scale = float(self.out_scale)
+        m.out_shift = float(self.out_shift)
+        return m
+
+    # ---------------------------------------------------------- evaluation
+    def potential_and_gradient(self, xyz):
+        """FP32 CUDA-core evaluation: (Phi [n], grad Phi [n,3]) float64."""
+        x = _core.f64(xyz).reshape(-1, 3).contiguous()
+        n = x.shape[0]
+        phi = torch.empty(n, dtype=torch.float64, device=x.device)
+        grad = torch.empty(n, 3, dtype=torch.float64, device=x.device)
+        m = self.struct()
+        need = _abi.load().ss_mlp_eval_workspace_bytes(n)
+        ws, nb = _core.aligned_ptr(_core.Workspace.get(need, x.device, "mlp"))
+        _abi.call("ss_mlp_eval", C.byref(m), ptr(x), n, ptr(phi), ptr(grad), ws, nb, stream_handle())
+        return phi, grad
+
+    def gradient_bf16(self, xyz):
+        """grad Phi through the tensor-core path of the stream integrator."""
+        x = _core.f64(xyz).reshape(-1, 3).contiguous()
+        n = x.shape[0]
+        grad = torch.empty(n, 3, dtype=torch.float64, device=x.device)
+        st = torch.empty(n, dtype=torch.int32, device=x.device)
+        m = self.struct()
+        _abi.call("ss_mlp_grad_bf16", C.byref(m), ptr(x), n, ptr(grad), ptr(st), stream_handle())
+        if bool((st != 0).any()):
+            raise RuntimeError("ss_mlp_grad_bf16: a tensor-core wait timed out")
+        return grad
+
+    def loss_grad(self, x, phi_t, g_t, w_val, w_force):
+        """(loss [2] = (value part, force part), grad [NPARAM]) of one batch."""
+        B = x.shape[0]
+        loss = torch.empty(2, dtype=torch.float32, device=x.device)
+        grad = torch.empty(NPARAM, dtype=torch.float32, device=x.device)
+        m = self.struct()
+        need = _abi.load().ss_mlp_train_workspace_bytes(B)
+        ws, nb = _core.aligned_ptr(_core.Workspace.get(need, x.device, "mlp_train"))
+        _abi.call("ss_mlp_loss_grad", C.byref(m), ptr(x), ptr(phi_t), ptr(g_t), ptr(w_val), ptr(w_force), B,
+                  ptr(loss), ptr(grad), ws, nb, stream_handle())
+        return loss, grad
+
+    # ------------------------------------------------------------ training
+    def fit(self, x, phi, grad, steps=4000, batch=8192, lr=2e-3, lr_min=2e-5, force_weight=1.0, seed=0,
+            log_every=0):
+        """Adam on the value + force loss with cosine learning-rate decay.
+        x [N,3], phi [N], grad [N,3] (exact targets, any float dtype)."""
+        dev = self.params.device
+        x = x.to(dev, torch.float32).contiguous()
+        phi = phi.to(dev, torch.float32).contiguous()
+        grad = grad.to(dev, torch.float32).contiguous()
+        N = x.shape[0]
+        batch = min(batch, N)
+        gnorm2 = (grad.double() ** 2).sum(1).clamp_min(1e-300)
+        w_val_all = torch.full((N,), 1.0 / (batch * self.out_scale ** 2), dtype=torch.float32, device=dev)
+        w_force_all = (force_weight / (batch * gnorm2)).float()
+        m = torch.zeros_like(self.params)
+        v = torch.zeros_like(self.params)
+        gen = torch.Generator(device=dev).manual_seed(seed)
+        perm = torch.randperm(N, generator=gen, device=dev)
+        pos = 0
+        for it in range(1, steps + 1):
+            if pos + batch > N:
+                perm = torch.randperm(N, generator=gen, device=dev)
+                pos = 0
+            idx = perm[pos:pos + batch]
+            pos += batch
+            loss, g = self.loss_grad(x[idx], phi[idx], grad[idx], w_val_all[idx], w_force_all[idx])
+            lr_t = lr_min + 0.5 * (lr - lr_min) * (1.0 + math.cos(math.pi * (it - 1) / max(steps - 1, 1)))
+            _abi.call("ss_mlp_adam", ptr(self.params), ptr(g), ptr(m), ptr(v), NPARAM, it, C.c_float(lr_t),
+                      C.c_float(0.9), C.c_float(0.999), C.c_float(1e-8), stream_handle())
+            if log_every and (it % log_every == 0 or it == steps):
+                self.history.append((it, float(loss[0]), float(loss[1])))
+        return self
+
+    @staticmethod
+    def normalisation(x, phi):
+        """Input / output affine maps from a training set."""
+        x = torch.as_tensor(x, dtype=torch.float64)
+        phi = torch.as_tensor(phi, dtype=torch.float64)
+        L = float(x.abs().mean()) * 1.5
+        lr = 0.5 * torch.log((x ** 2).sum(1))
+        return dict(in_scale=(1.0 / L, 1.0 / L, 1.0 / L, 1.0 / float(lr.std())),
+                    in_shift=(0.0, 0.0, 0.0, float(lr.mean())),
+                    out_scale=float(phi.std()), out_shift=float(phi.mean()))
+
+
+def orbit_samples(pot, prog_w0, n_orbits=4096, n_per_orbit=1024, dt=1.0, every=2, seed=0, broad_fraction=0.25):
+    """Training points along orbits in `pot` (FP64 orbit kernel): most
+    orbits start near the progenitor's orbit (position scatter 2 kpc,
+    velocity scatter 10 % + 0.02 kpc/Myr), the rest isotropically with
+    ln r uniform over [ln 1, ln 100] kpc and speeds of 0.3-1.2 times the
+    circular speed.  Returns positions [n_orbits * n_per_orbit, 3] (float64)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n_near = int(round(n_orbits * (1.0 - broad_fraction)))
+    n_broad = n_orbits - n_near
+    w0 = np.asarray(prog_w0, dtype=np.float64)
+    T = n_per_orbit * every * dt
+    prog = pot.integrate_orbit(w0=w0, ts=np.linspace(0.0, -T, 257), t0=0.0, t1=-T, dt=dt).ys
+    prog = prog.detach().cpu().numpy()
+    pick = prog[rng.integers(0, len(prog), n_near)]
+    near = pick.copy()
+    near[:, :3] += rng.normal(0.0, 2.0, (n_near, 3))
+    near[:, 3:] = near[:, 3:] * (1.0 + rng.normal(0.0, 0.1, (n_near, 1))) + rng.normal(0.0, 0.02, (n_near, 3))
+    r = np.exp(rng.uniform(np.log(1.0), np.log(100.0), n_broad))
+    u = rng.normal(size=(n_broad, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    pos = u * r[:, None]
+    g = pot.gradient(pos, 0.0).detach().cpu().numpy()
+    vc = np.sqrt(np.maximum((g * pos).sum(1), 1e-30))
+    d = rng.normal(size=(n_broad, 3))
+    d -= (d * u).sum(1, keepdims=True) * u
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    vel = d * (vc * rng.uniform(0.3, 1.2, n_broad))[:, None]
+    ics = np.concatenate([near, np.concatenate([pos, vel], 1)], 0)
+    w = _core.f64(ics).contiguous()
+    ys = _core.orbit(pot._desc(), w, 0.0, float(dt), n_per_orbit * every, every, method="serial")
+    return ys[:, 1:, :3].reshape(-1, 3).contiguous()
+
+
+def train_surrogate(pot, prog_w0, n_points=1 << 22, steps=6000, batch=8192, seed=0, **kw) -> MLPSurrogate:
+    """Sample `n_points` along orbits of the exact potential, evaluate Phi and
+    grad Phi there with the exact FP64 kernels, and fit the network."""
+    n_per = 1024
+    n_orb = max(1, n_points // n_per)
+    x = orbit_samples(pot, prog_w0, n_orbits=n_orb, n_per_orbit=n_per, seed=seed)
+    phi = pot.potential(x, 0.0)
+    grad = pot.gradient(x, 0.0)
+    nm = MLPSurrogate.normalisation(x.cpu(), phi.cpu())
+    s = MLPSurrogate.init(seed=seed, **nm)
+    s.fit(x, phi, grad, steps=steps, batch=batch, seed=seed, **kw)
+    return s

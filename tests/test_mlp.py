@@ -1,0 +1,160 @@
+"""Learned force surrogate: the FP32 network kernels against a float64
+PyTorch restatement of the same network on the CPU (values, input
+gradients, and the Sobolev-loss parameter gradient by double backward), the
+tensor-core (tcgen05, BF16) force against the FP32 one, training against
+the exact expansion (what the trained network gains over the spherical
+approximation), and the stream integrated in the surrogate's force."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+PROG = np.array([12.0, 0.0, 4.0, 0.0, 0.18, 0.04])
+
+
+def _net64(params, s, x):
+    """Phi(x) of the surrogate in float64 (CPU, autograd-able in x and params)."""
+    from streamsculptor_gb300.surrogate import unpack
+    v = unpack(params)
+    c = torch.tensor(s.in_scale, dtype=torch.float64)
+    sh = torch.tensor(s.in_shift, dtype=torch.float64)
+    r2 = (x ** 2).sum(1)
+    u = torch.stack([(x[:, 0] - sh[0]) * c[0], (x[:, 1] - sh[1]) * c[1], (x[:, 2] - sh[2]) * c[2],
+                     (0.5 * torch.log(r2) - sh[3]) * c[3]], 1)
+    a = u
+    for k in (1, 2, 3, 4):
+        z = a @ v[f"W{k}"].T + v[f"b{k}"]
+        a = z * torch.sigmoid(z)
+    return s.out_scale * (a @ v["w5"] + v["b5"][0]) + s.out_shift
+
+
+def _surrogate(ss, seed=3):
+    from streamsculptor_gb300.surrogate import MLPSurrogate
+    return MLPSurrogate.init(seed=seed, in_scale=(1 / 15, 1 / 15, 1 / 15, 1.2), in_shift=(0.5, -0.3, 0.2, 2.3),
+                             out_scale=0.2, out_shift=-0.5)
+
+
+def _points(n, seed=0):
+    rng = np.random.default_rng(seed)
+    u = rng.normal(size=(n, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    return u * np.exp(rng.uniform(np.log(2.0), np.log(60.0), n))[:, None]
+
+
+def test_mlp_eval_matches_float64_network(ss):
+    s = _surrogate(ss)
+    x = _points(3000)
+    phi, g = s.potential_and_gradient(x)
+    xt = torch.tensor(x, requires_grad=True)
+    ref = _net64(s.params.detach().cpu().double(), s, xt)
+    (gref,) = torch.autograd.grad(ref.sum(), xt)
+    phi, g = phi.cpu().numpy(), g.cpu().numpy()
+    ref, gref = ref.detach().numpy(), gref.numpy()
+    assert np.max(np.abs(phi - ref)) <= 1e-5 * np.max(np.abs(ref))
+    assert np.max(np.abs(g - gref)) <= 1e-4 * np.max(np.abs(gref))
+
+
+def test_mlp_loss_gradient_matches_double_backward(ss):
+    s = _surrogate(ss, seed=5)
+    B = 700
+    x = _points(B, seed=2)
+    rng = np.random.default_rng(4)
+    phi_t = rng.normal(-0.5, 0.2, B)
+    g_t = rng.normal(0, 0.01, (B, 3))
+    w_val = rng.uniform(0.5, 1.5, B) / B
+    w_force = rng.uniform(0.5, 1.5, B) / B * 1e4
+    dev = s.params.device
+    f32 = lambda a: torch.tensor(a, dtype=torch.float32, device=dev)  # noqa: E731
+    loss, grad = s.loss_grad(f32(x), f32(phi_t), f32(g_t), f32(w_val), f32(w_force))
+    # float64 reference: L = sum w_v (Phi - Phi_t)^2 + w_f |grad Phi - g_t|^2, by double backward
+    p = s.params.detach().cpu().double().requires_grad_(True)
+    xt = torch.tensor(x, requires_grad=True)
+    phi = _net64(p, s, xt)
+    (gx,) = torch.autograd.grad(phi.sum(), xt, create_graph=True)
+    lv = (torch.tensor(w_val) * (phi - torch.tensor(phi_t)) ** 2).sum()
+    lf = (torch.tensor(w_force) * ((gx - torch.tensor(g_t)) ** 2).sum(1)).sum()
+    (gp,) = torch.autograd.grad(lv + lf, p)
+    lo = loss.cpu().numpy()
+    assert abs(lo[0] - float(lv)) <= 1e-4 * abs(float(lv))
+    assert abs(lo[1] - float(lf)) <= 1e-4 * abs(float(lf))
+    gp = gp.numpy()
+    err = np.max(np.abs(grad.cpu().numpy() - gp)) / np.max(np.abs(gp))
+    print(f"Sobolev-loss gradient vs float64 double backward: {err:.2e}")
+    assert err <= 2e-3
+
+
+def test_mlp_tensor_core_force_matches_fp32(ss):
+    """The tcgen05 path (BF16 weights and activations, FP32 accumulation in
+    TMEM, transposed weight tiles for the backward chain) against the FP32
+    CUDA-core evaluation of the same network."""
+    s = _surrogate(ss, seed=7)
+    x = _points(5000, seed=9)  # 40 tiles of 128, the last one partial
+    _, g32 = s.potential_and_gradient(x)
+    g16 = s.gradient_bf16(x)
+    g32, g16 = g32.cpu().numpy(), g16.cpu().numpy()
+    rel = np.linalg.norm(g16 - g32) / np.linalg.norm(g32)
+    per = np.linalg.norm(g16 - g32, axis=1) / np.linalg.norm(g32, axis=1)
+    print(f"BF16 tensor-core force vs FP32: overall {rel:.2e}, median {np.median(per):.2e}")
+    assert rel < 3e-2
+    assert np.median(per) < 3e-2
+
+
+@pytest.fixture(scope="module")
+def trained(ss):
+    from streamsculptor_gb300 import potential as P
+    from streamsculptor_gb300.surrogate import MLPSurrogate, orbit_samples
+    pot = P.seeded_triaxial_expansion(units=ss.usys)
+    x = orbit_samples(pot, PROG, n_orbits=192, n_per_orbit=512, seed=1)
+    phi, g = pot.potential(x, 0.0), pot.gradient(x, 0.0)
+    s = MLPSurrogate.init(seed=1, **MLPSurrogate.normalisation(x.cpu(), phi.cpu()))
+    s.fit(x, phi, g, steps=2500, batch=4096, lr=3e-3, seed=1, log_every=500)
+    return pot, s
+
+
+def test_trained_surrogate_beats_spherical_approximation(ss, trained):
+    """On held-out orbit points the trained network's force is closer to the
+    exact expansion than the expansion's own monopole (the spherical model
+    one would use without the surrogate)."""
+    from streamsculptor_gb300 import potential as P
+    from streamsculptor_gb300.surrogate import orbit_samples
+    pot, s = trained
+    x = orbit_samples(pot, PROG, n_orbits=32, n_per_orbit=256, seed=11)
+    g = pot.gradient(x, 0.0).cpu().numpy()
+    mono = P.SphericalHarmonicExpansionPotential(pot.coef[:, :1, :], pot.log_r0, pot.dlog_r, units=ss.usys)
+    gm = mono.gradient(x, 0.0).cpu().numpy()
+    _, gs = s.potential_and_gradient(x)
+    gb = s.gradient_bf16(x).cpu().numpy()
+    gs = gs.cpu().numpy()
+    nrm = np.linalg.norm(g, axis=1)
+    e_mono = np.median(np.linalg.norm(gm - g, axis=1) / nrm)
+    e_s32 = np.median(np.linalg.norm(gs - g, axis=1) / nrm)
+    e_s16 = np.median(np.linalg.norm(gb - g, axis=1) / nrm)
+    print(f"median relative force error: monopole {e_mono:.2e}, surrogate FP32 {e_s32:.2e}, BF16 {e_s16:.2e}; "
+          f"loss history {s.history}")
+    assert s.history[-1][1] < 0.05 * s.history[0][1] or s.history[-1][1] < 1e-4
+    assert e_s32 < 0.5 * e_mono
+    assert e_s16 < e_mono
+
+
+def test_stream_in_surrogate_force(ss, trained):
+    """Stream with the surrogate's force (tensor cores) against the stream
+    in the exact expansion (FP32 compensated): 150 releases x 8 particles,
+    300 steps of 1 Myr."""
+    from streamsculptor_gb300.streamhelpers import gen_stream
+    pot, s = trained
+    n_rel, ppr = 150, 8
+    back = pot.integrate_orbit(w0=PROG, ts=np.array([0.0, -2.0 * n_rel]), t0=0.0, t1=-2.0 * n_rel, dt=1.0).ys[-1]
+    ts = -2.0 * n_rel + np.arange(n_rel + 1) * 2.0
+    normals = np.random.default_rng(3).standard_normal((n_rel + 1, ppr // 2, 4))
+    exact = gen_stream(pot, ts, back, 2e4, normals=normals, dt=1.0, n_particles_per_release=ppr, precision="f32k")
+    mlp = gen_stream(pot, ts, back, 2e4, normals=normals, dt=1.0, n_particles_per_release=ppr, precision="mlp",
+                     force_surrogate=s)
+    a = torch.stack([exact[0], exact[1]]).reshape(-1, 6).cpu().numpy()
+    b = torch.stack([mlp[0], mlp[1]]).reshape(-1, 6).cpu().numpy()
+    assert np.isfinite(b).all()
+    dx = np.linalg.norm(a[:, :3] - b[:, :3], axis=1) / np.linalg.norm(a[:, :3], axis=1)
+    print(f"surrogate stream vs exact: median position error {np.median(dx):.2e}, max {dx.max():.2e}")
+    assert np.median(dx) < 5e-2
