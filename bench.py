@@ -47,6 +47,9 @@ WORKLOADS = {
                 name="spray stream, 3000 releases x 334 particles (1.0e6), 3 Gyr at dt=1 Myr, triaxial halo as a "
                      "spherical-harmonic expansion (l_max=8, 64 log knots over 0.1-200 kpc, seeded 2^-l "
                      "coefficients), exact expansion force, final state only"),
+    "c4xs": dict(n_rel=600, ppr=334, dt=1.0, spr=1, snap=0, moving=False, potential="expansion",
+                 name="profiling case shaped like the expansion stream: 600 releases x 334 particles (2.0e5), "
+                      "600 steps of 1 Myr, spherical-harmonic expansion (l_max=8), final state only"),
     "c1": dict(n_rel=3000, ppr=2, dt=1.0, spr=1, snap=0, moving=False,
                name="spray stream, 3000 releases x 2 particles (6000), 3 Gyr at dt=1 Myr, NFW+MN+Hernquist, "
                     "final state only"),
@@ -531,6 +534,143 @@ def c5_arm(args):
           "grad_norm": float(torch.linalg.norm(g))})
 
 
+C4 = dict(n_rel=3000, ppr=334, dt=1.0, spr=1,
+          name="learned force surrogate: 3000 releases x 334 particles (1.0e6), 3 Gyr at dt=1 Myr in a triaxial halo "
+               "given as a spherical-harmonic expansion (l_max=8, 64 log knots over 0.1-200 kpc, seeded 2^-l "
+               "coefficients); MLP (x,y,z,ln r) -> Phi, 4 x 128 SiLU, trained on 2^22 orbit points, forces from its "
+               "hand-written backward on the tensor cores (BF16, FP32 accumulation)")
+# tensor-core work of one surrogate force: layers 2-4 forward + 3 backward
+# GEMMs of 128 x 128 per particle (2 flops per multiply-add)
+MLP_TENSOR_FLOPS = 6 * 2 * 128 * 128
+
+
+def c4_arm(args):
+    import torch
+
+    import streamsculptor_gb300 as ss
+    from streamsculptor_gb300 import _abi, _core, potential as P
+    from streamsculptor_gb300.streamhelpers import gen_stream
+    from streamsculptor_gb300.surrogate import MLPSurrogate, orbit_samples
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    lib = _abi.load()
+    u = ss.usys
+    pot = P.seeded_triaxial_expansion(units=u)
+    n_rel, ppr, dt = C4["n_rel"], C4["ppr"], C4["dt"]
+    T = n_rel * dt
+    ts = -T + np.arange(n_rel + 1) * dt
+    work = particle_steps(n_rel, ppr, 1)
+    normals_h = np.random.Generator(np.random.PCG64(1234)).standard_normal((n_rel + 1, ppr // 2, 4))
+    normals_d = torch.as_tensor(normals_h, device=dev)
+    # --- training set and training (timed separately)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    x = orbit_samples(pot, WF, n_orbits=args.c4_points // 1024, n_per_orbit=1024, seed=0)
+    phi, g = pot.potential(x, 0.0), pot.gradient(x, 0.0)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    sur = MLPSurrogate.init(seed=0, **MLPSurrogate.normalisation(x.cpu(), phi.cpu()))
+    sur.fit(x, phi, g, steps=args.c4_train_steps, batch=8192, lr=3e-3, seed=0, log_every=max(1, args.c4_train_steps // 5))
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    xv = orbit_samples(pot, WF, n_orbits=64, n_per_orbit=256, seed=7)
+    gv = pot.gradient(xv, 0.0)
+    _, g32 = sur.potential_and_gradient(xv)
+    g16 = sur.gradient_bf16(xv)
+    nrm = torch.linalg.norm(gv, dim=1)
+    e32 = torch.linalg.norm(g32 - gv, dim=1) / nrm
+    e16 = torch.linalg.norm(g16 - gv, dim=1) / nrm
+    del x, phi, g
+    back = pot.integrate_orbit(w0=WF, ts=np.array([0.0, -T]), t0=0.0, t1=-T, dt=dt).ys[-1]
+
+    def step(precision, normals):
+        return gen_stream(pot, ts, back, MSAT, normals=normals, dt=dt, n_particles_per_release=ppr,
+                          precision=precision, force_surrogate=sur if precision == "mlp" else None)
+
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+
+    def timed(precision, K, W):
+        for _ in range(W):
+            step(precision, normals_d)
+        torch.cuda.synchronize()
+        evs, kev = [], []
+        _core.STREAM_EVENTS = kev
+        l0 = lib.ss_kernel_launches()
+        clk = ClockSampler(gpu_id_for(0))
+        clk.start()
+        for _ in range(K):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            step(precision, normals_d)
+            e1.record()
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        ck = clk.stop()
+        _core.STREAM_EVENTS = None
+        return {"ms_per_step": sum(a.elapsed_time(b) for a, b in evs) / K,
+                "kernel_ms": statistics.mean(a.elapsed_time(b) for a, b in kev), "clocks": ck,
+                "launches": lib.ss_kernel_launches() - l0}
+
+    rm = timed("mlp", args.steps, args.warmup)
+    rx = timed("f32k", 1, 1)
+    lm = step("mlp", normals_d)
+    lx = step("f32k", normals_d)
+    a = torch.stack([lm[0], lm[1]]).reshape(-1, 6)
+    b = torch.stack([lx[0], lx[1]]).reshape(-1, 6)
+    ex = torch.linalg.norm(a[:, :3] - b[:, :3], dim=1) / torch.linalg.norm(b[:, :3], dim=1)
+    ev = torch.linalg.norm(a[:, 3:] - b[:, 3:], dim=1) / torch.linalg.norm(b[:, 3:], dim=1)
+    e = torch.maximum(ex, ev)
+    # e2e: host normals in, final states to pinned host memory
+    pin = torch.empty((2, n_rel, ppr // 2, 6), dtype=torch.float64, pin_memory=True)
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    for _ in range(args.steps):
+        out = step("mlp", normals_h)
+        pin[0].copy_(out[0], non_blocking=True)
+        pin[1].copy_(out[1], non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t3) / args.steps
+    peak = MEASURED_BF16_TFLOPS
+    ach = MLP_TENSOR_FLOPS * 6 * work / (rm["kernel_ms"] * 1e-3) / 1e12
+    emit({"metric": METRIC, "value": work / (rm["ms_per_step"] * 1e-3), "unit": UNIT, "n_gpus": 1,
+          "steps": args.steps, "warmup": args.warmup, "ms_per_step": rm["ms_per_step"], "higher_is_better": True,
+          "scaling": "weak", "vs_baseline": None, "dtype": "bf16 tensor-core force (FP32 accumulation), f32 "
+          "compensated state, f64 progenitor and release",
+          "data": "synthetic (seeded expansion, PCG64 draws; training points along orbits of the exact expansion)",
+          "config": {"workload": C4["name"], "particles": n_rel * ppr, "n_steps": n_rel, "particle_steps_per_step":
+                     work, "l2": "512 MB buffer zeroed between timed steps"},
+          "exact_expansion_f32k": {"value": work / (rx["ms_per_step"] * 1e-3), "ms_per_step": rx["ms_per_step"],
+                                   "kernel_ms": rx["kernel_ms"]},
+          "speedup_vs_exact_expansion": rx["ms_per_step"] / rm["ms_per_step"],
+          "surrogate": {"train_points": int(args.c4_points), "train_steps": args.c4_train_steps, "batch": 8192,
+                        "sample_s": t1 - t0, "train_s": t2 - t1, "loss_history": sur.history,
+                        "force_rel_err_fp32": {"median": float(e32.median()), "p99": float(torch.quantile(e32.float(), 0.99))},
+                        "force_rel_err_bf16": {"median": float(e16.median()), "p99": float(torch.quantile(e16.float(), 0.99))}},
+          "error_vs_exact_expansion": {"median": float(e.median()), "p99": float(torch.quantile(e.float(), 0.99)),
+                                       "max": float(e.max()), "measure": "per particle max(|dx|/|x|, |dv|/|v|) of "
+                                       "final states, surrogate stream vs exact-expansion FP32-compensated stream"},
+          "roofline": {"kernel": "stream_mlp_kernel", "bound": "tensor", "achieved": ach, "peak": peak,
+                       "unit": "TFLOP/s", "frac": ach / peak, "traffic": None,
+                       "flops_per_particle_step": MLP_TENSOR_FLOPS * 6, "kernel_ms": rm["kernel_ms"],
+                       "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst)"},
+          "e2e": {"value": work / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(normals_h.nbytes),
+                  "d2h_bytes_per_step": int(pin.numel() * 8), "ms_per_step": e2e_s * 1e3},
+          "clocks": rm["clocks"], "gpu_launches": rm["launches"]})
+
+
+def _measured_bf16():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"])
+    except (OSError, ValueError, KeyError):
+        return 1900.0  # fallback figure of the profiling recipe
+
+
+MEASURED_BF16_TFLOPS = _measured_bf16()
+
+
 def traffic_for(kernel):
     """DRAM bytes per launch from the committed ncu summary, if present."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
@@ -547,7 +687,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["c3", "c3s", "c5"], default="c2")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["c3", "c3s", "c4", "c5"], default="c2")
+    ap.add_argument("--c4-points", type=int, default=1 << 22, help="surrogate training points (c4)")
+    ap.add_argument("--c4-train-steps", type=int, default=6000, help="surrogate Adam steps (c4)")
     ap.add_argument("--f64-steps", type=int, default=2)
     ap.add_argument("--f64-warmup", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -558,6 +700,9 @@ def main():
         return
     if args.workload == "c5":
         c5_arm(args)
+        return
+    if args.workload == "c4":
+        c4_arm(args)
         return
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":

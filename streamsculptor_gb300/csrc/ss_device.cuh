@@ -427,6 +427,24 @@ static __constant__ double c_shnorm[SS_SHEXP_LMAX + 1][SS_SHEXP_LMAX + 1] = {
      111597.67739518596, 417560.27397251286, 0.0},
     {40320.0, 60480.0, 72287.42629254413, 97877.63789548662, 151631.38461413587, 273357.36609793414,
      590519.4025601529, 1617203.9871333486, 6468815.948533394}};
+// the same table as a compile-time function (immediates in unrolled code)
+__host__ __device__ constexpr double shnorm_ct(int l, int m) {
+    const double t[SS_SHEXP_LMAX + 1][SS_SHEXP_LMAX + 1] = {
+    {1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {1.0, 2.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {2.0, 3.4641016151377544, 6.928203230275509, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {6.0, 9.797958971132712, 15.491933384829668, 37.94733192202055, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {24.0, 37.94733192202055, 53.665631459994955, 100.39920318408906, 283.9718295887816, 0.0, 0.0, 0.0, 0.0},
+    {120.0, 185.903200617956, 245.92681838303037, 401.59681273635624, 851.9154887663448, 2693.9933184772376, 0.0,
+     0.0, 0.0},
+    {720.0, 1099.8181667894016, 1391.172167634186, 2086.758251451279, 3809.8818879330106, 8934.965025113417,
+     30951.626774694734, 0.0, 0.0},
+    {5040.0, 7619.763775866021, 9332.266605707318, 13197.818001472819, 21886.105181141756, 43772.21036228351,
+     111597.67739518596, 417560.27397251286, 0.0},
+    {40320.0, 60480.0, 72287.42629254413, 97877.63789548662, 151631.38461413587, 273357.36609793414,
+     590519.4025601529, 1617203.9871333486, 6468815.948533394}};
+    return t[l][m];
+}
 
 template <class T>
 struct SolidH {
@@ -706,6 +724,327 @@ __device__ __noinline__ Vec3<S> shexp_grad_value(const ExpDev E, S scale, S x0, 
     return Vec3<S>{g[0], g[1], g[2]};
 }
 
+// ------------------------------------ expansion gradient for FP32 streams
+// The stream integrator calls this form: each thread keeps its solid
+// harmonics R_l^m(n) in a column of shared memory (slot 2q, 2q+1 = Re, Im
+// of q = l(l+1)/2 + m; slot 90 = 0) and one rolled loop runs over the terms,
+// reading each term's slots and coefficients (normalisation and the
+// derivative rules folded in) from constant memory.  Small code, no
+// dynamically indexed registers.  Term j: K = cK R[sK],
+// grad K = (cx1 R[sx1] + cx2 R[sx2], cy1 R[sy1] + cy2 R[sy2], cz R[sz]).
+static __constant__ short4 c_shterm_i[81][2] = {
+    {{0, 90, 90, 90}, {90, 90, 0, 0}},
+    {{5, 1, 90, 90}, {0, 90, 1, 0}},
+    {{2, 90, 90, 90}, {90, 0, 1, 0}},
+    {{4, 0, 90, 90}, {1, 90, 1, 0}},
+    {{11, 5, 90, 90}, {4, 90, 2, 0}},
+    {{9, 3, 90, 90}, {2, 5, 2, 0}},
+    {{6, 4, 4, 5}, {5, 2, 2, 0}},
+    {{8, 2, 90, 90}, {3, 4, 2, 0}},
+    {{10, 4, 90, 90}, {5, 90, 2, 0}},
+    {{19, 11, 90, 90}, {10, 90, 3, 0}},
+    {{17, 9, 90, 90}, {8, 11, 3, 0}},
+    {{15, 7, 11, 10}, {6, 9, 3, 0}},
+    {{12, 8, 8, 9}, {9, 6, 3, 0}},
+    {{14, 6, 10, 11}, {7, 8, 3, 0}},
+    {{16, 8, 90, 90}, {9, 10, 3, 0}},
+    {{18, 10, 90, 90}, {11, 90, 3, 0}},
+    {{29, 19, 90, 90}, {18, 90, 4, 0}},
+    {{27, 17, 90, 90}, {16, 19, 4, 0}},
+    {{25, 15, 19, 18}, {14, 17, 4, 0}},
+    {{23, 13, 17, 16}, {12, 15, 4, 0}},
+    {{20, 14, 14, 15}, {15, 12, 4, 0}},
+    {{22, 12, 16, 17}, {13, 14, 4, 0}},
+    {{24, 14, 18, 19}, {15, 16, 4, 0}},
+    {{26, 16, 90, 90}, {17, 18, 4, 0}},
+    {{28, 18, 90, 90}, {19, 90, 4, 0}},
+    {{41, 29, 90, 90}, {28, 90, 5, 0}},
+    {{39, 27, 90, 90}, {26, 29, 5, 0}},
+    {{37, 25, 29, 28}, {24, 27, 5, 0}},
+    {{35, 23, 27, 26}, {22, 25, 5, 0}},
+    {{33, 21, 25, 24}, {20, 23, 5, 0}},
+    {{30, 22, 22, 23}, {23, 20, 5, 0}},
+    {{32, 20, 24, 25}, {21, 22, 5, 0}},
+    {{34, 22, 26, 27}, {23, 24, 5, 0}},
+    {{36, 24, 28, 29}, {25, 26, 5, 0}},
+    {{38, 26, 90, 90}, {27, 28, 5, 0}},
+    {{40, 28, 90, 90}, {29, 90, 5, 0}},
+    {{55, 41, 90, 90}, {40, 90, 6, 0}},
+    {{53, 39, 90, 90}, {38, 41, 6, 0}},
+    {{51, 37, 41, 40}, {36, 39, 6, 0}},
+    {{49, 35, 39, 38}, {34, 37, 6, 0}},
+    {{47, 33, 37, 36}, {32, 35, 6, 0}},
+    {{45, 31, 35, 34}, {30, 33, 6, 0}},
+    {{42, 32, 32, 33}, {33, 30, 6, 0}},
+    {{44, 30, 34, 35}, {31, 32, 6, 0}},
+    {{46, 32, 36, 37}, {33, 34, 6, 0}},
+    {{48, 34, 38, 39}, {35, 36, 6, 0}},
+    {{50, 36, 40, 41}, {37, 38, 6, 0}},
+    {{52, 38, 90, 90}, {39, 40, 6, 0}},
+    {{54, 40, 90, 90}, {41, 90, 6, 0}},
+    {{71, 55, 90, 90}, {54, 90, 7, 0}},
+    {{69, 53, 90, 90}, {52, 55, 7, 0}},
+    {{67, 51, 55, 54}, {50, 53, 7, 0}},
+    {{65, 49, 53, 52}, {48, 51, 7, 0}},
+    {{63, 47, 51, 50}, {46, 49, 7, 0}},
+    {{61, 45, 49, 48}, {44, 47, 7, 0}},
+    {{59, 43, 47, 46}, {42, 45, 7, 0}},
+    {{56, 44, 44, 45}, {45, 42, 7, 0}},
+    {{58, 42, 46, 47}, {43, 44, 7, 0}},
+    {{60, 44, 48, 49}, {45, 46, 7, 0}},
+    {{62, 46, 50, 51}, {47, 48, 7, 0}},
+    {{64, 48, 52, 53}, {49, 50, 7, 0}},
+    {{66, 50, 54, 55}, {51, 52, 7, 0}},
+    {{68, 52, 90, 90}, {53, 54, 7, 0}},
+    {{70, 54, 90, 90}, {55, 90, 7, 0}},
+    {{89, 71, 90, 90}, {70, 90, 8, 0}},
+    {{87, 69, 90, 90}, {68, 71, 8, 0}},
+    {{85, 67, 71, 70}, {66, 69, 8, 0}},
+    {{83, 65, 69, 68}, {64, 67, 8, 0}},
+    {{81, 63, 67, 66}, {62, 65, 8, 0}},
+    {{79, 61, 65, 64}, {60, 63, 8, 0}},
+    {{77, 59, 63, 62}, {58, 61, 8, 0}},
+    {{75, 57, 61, 60}, {56, 59, 8, 0}},
+    {{72, 58, 58, 59}, {59, 56, 8, 0}},
+    {{74, 56, 60, 61}, {57, 58, 8, 0}},
+    {{76, 58, 62, 63}, {59, 60, 8, 0}},
+    {{78, 60, 64, 65}, {61, 62, 8, 0}},
+    {{80, 62, 66, 67}, {63, 64, 8, 0}},
+    {{82, 64, 68, 69}, {65, 66, 8, 0}},
+    {{84, 66, 70, 71}, {67, 68, 8, 0}},
+    {{86, 68, 90, 90}, {69, 70, 8, 0}},
+    {{88, 70, 90, 90}, {71, 90, 8, 0}}};
+static __constant__ float c_shterm_f[81][6] = {
+    {1.000000000e+00f, 0.000000000e+00f, 0.000000000e+00f, 0.000000000e+00f, 0.000000000e+00f, 0.000000000e+00f},
+    {2.000000000e+00f, 1.000000000e+00f, 0.000000000e+00f, 0.000000000e+00f, 1.000000000e+00f, 0.000000000e+00f},
+    {1.000000000e+00f, 0.000000000e+00f, 0.000000000e+00f, 0.000000000e+00f, 0.000000000e+00f, 1.000000000e+00f},
+    {2.000000000e+00f, 1.000000000e+00f, 0.000000000e+00f, 0.000000000e+00f, -1.000000000e+00f, 0.000000000e+00f},
+    {6.928203230e+00f, 3.464101615e+00f, 0.000000000e+00f, 0.000000000e+00f, 3.464101615e+00f, 0.000000000e+00f},
+    {3.464101615e+00f, 1.732050808e+00f, 0.000000000e+00f, 0.000000000e+00f, 1.732050808e+00f, 3.464101615e+00f},
+    {2.000000000e+00f, -1.000000000e+00f, -1.000000000e+00f, -1.000000000e+00f, -1.000000000e+00f, 2.000000000e+00f},
+    {3.464101615e+00f, 1.732050808e+00f, 0.000000000e+00f, 0.000000000e+00f, -1.732050808e+00f, 3.464101615e+00f},
+    {6.928203230e+00f, 3.464101615e+00f, 0.000000000e+00f, 0.000000000e+00f, -3.464101615e+00f, 0.000000000e+00f},
+    {3.794733192e+01f, 1.897366596e+01f, 0.000000000e+00f, 0.000000000e+00f, 1.897366596e+01f, 0.000000000e+00f},
+    {1.549193338e+01f, 7.745966692e+00f, 0.000000000e+00f, 0.000000000e+00f, 7.745966692e+00f, 1.549193338e+01f},
+    {9.797958971e+00f, 4.898979486e+00f, -4.898979486e+00f, 4.898979486e+00f, 4.898979486e+00f, 9.797958971e+00f},
+    {6.000000000e+00f, -3.000000000e+00f, -3.000000000e+00f, -3.000000000e+00f, -3.000000000e+00f, 6.000000000e+00f},
+    {9.797958971e+00f, 4.898979486e+00f, -4.898979486e+00f, -4.898979486e+00f, -4.898979486e+00f, 9.797958971e+00f},
+    {1.549193338e+01f, 7.745966692e+00f, 0.000000000e+00f, 0.000000000e+00f, -7.745966692e+00f, 1.549193338e+01f},
+    {3.794733192e+01f, 1.897366596e+01f, 0.000000000e+00f, 0.000000000e+00f, -1.897366596e+01f, 0.000000000e+00f},
+    {2.839718296e+02f, 1.419859148e+02f, 0.000000000e+00f, 0.000000000e+00f, 1.419859148e+02f, 0.000000000e+00f},
+    {1.003992032e+02f, 5.019960159e+01f, 0.000000000e+00f, 0.000000000e+00f, 5.019960159e+01f, 1.003992032e+02f},
+    {5.366563146e+01f, 2.683281573e+01f, -2.683281573e+01f, 2.683281573e+01f, 2.683281573e+01f, 5.366563146e+01f},
+    {3.794733192e+01f, 1.897366596e+01f, -1.897366596e+01f, 1.897366596e+01f, 1.897366596e+01f, 3.794733192e+01f},
+    {2.400000000e+01f, -1.200000000e+01f, -1.200000000e+01f, -1.200000000e+01f, -1.200000000e+01f, 2.400000000e+01f},
+    {3.794733192e+01f, 1.897366596e+01f, -1.897366596e+01f, -1.897366596e+01f, -1.897366596e+01f, 3.794733192e+01f},
+    {5.366563146e+01f, 2.683281573e+01f, -2.683281573e+01f, -2.683281573e+01f, -2.683281573e+01f, 5.366563146e+01f},
+    {1.003992032e+02f, 5.019960159e+01f, 0.000000000e+00f, 0.000000000e+00f, -5.019960159e+01f, 1.003992032e+02f},
+    {2.839718296e+02f, 1.419859148e+02f, 0.000000000e+00f, 0.000000000e+00f, -1.419859148e+02f, 0.000000000e+00f},
+    {2.693993318e+03f, 1.346996659e+03f, 0.000000000e+00f, 0.000000000e+00f, 1.346996659e+03f, 0.000000000e+00f},
+    {8.519154888e+02f, 4.259577444e+02f, 0.000000000e+00f, 0.000000000e+00f, 4.259577444e+02f, 8.519154888e+02f},
+    {4.015968127e+02f, 2.007984064e+02f, -2.007984064e+02f, 2.007984064e+02f, 2.007984064e+02f, 4.015968127e+02f},
+    {2.459268184e+02f, 1.229634092e+02f, -1.229634092e+02f, 1.229634092e+02f, 1.229634092e+02f, 2.459268184e+02f},
+    {1.859032006e+02f, 9.295160031e+01f, -9.295160031e+01f, 9.295160031e+01f, 9.295160031e+01f, 1.859032006e+02f},
+    {1.200000000e+02f, -6.000000000e+01f, -6.000000000e+01f, -6.000000000e+01f, -6.000000000e+01f, 1.200000000e+02f},
+    {1.859032006e+02f, 9.295160031e+01f, -9.295160031e+01f, -9.295160031e+01f, -9.295160031e+01f, 1.859032006e+02f},
+    {2.459268184e+02f, 1.229634092e+02f, -1.229634092e+02f, -1.229634092e+02f, -1.229634092e+02f, 2.459268184e+02f},
+    {4.015968127e+02f, 2.007984064e+02f, -2.007984064e+02f, -2.007984064e+02f, -2.007984064e+02f, 4.015968127e+02f},
+    {8.519154888e+02f, 4.259577444e+02f, 0.000000000e+00f, 0.000000000e+00f, -4.259577444e+02f, 8.519154888e+02f},
+    {2.693993318e+03f, 1.346996659e+03f, 0.000000000e+00f, 0.000000000e+00f, -1.346996659e+03f, 0.000000000e+00f},
+    {3.095162677e+04f, 1.547581339e+04f, 0.000000000e+00f, 0.000000000e+00f, 1.547581339e+04f, 0.000000000e+00f},
+    {8.934965025e+03f, 4.467482513e+03f, 0.000000000e+00f, 0.000000000e+00f, 4.467482513e+03f, 8.934965025e+03f},
+    {3.809881888e+03f, 1.904940944e+03f, -1.904940944e+03f, 1.904940944e+03f, 1.904940944e+03f, 3.809881888e+03f},
+    {2.086758251e+03f, 1.043379126e+03f, -1.043379126e+03f, 1.043379126e+03f, 1.043379126e+03f, 2.086758251e+03f},
+    {1.391172168e+03f, 6.955860838e+02f, -6.955860838e+02f, 6.955860838e+02f, 6.955860838e+02f, 1.391172168e+03f},
+    {1.099818167e+03f, 5.499090834e+02f, -5.499090834e+02f, 5.499090834e+02f, 5.499090834e+02f, 1.099818167e+03f},
+    {7.200000000e+02f, -3.600000000e+02f, -3.600000000e+02f, -3.600000000e+02f, -3.600000000e+02f, 7.200000000e+02f},
+    {1.099818167e+03f, 5.499090834e+02f, -5.499090834e+02f, -5.499090834e+02f, -5.499090834e+02f, 1.099818167e+03f},
+    {1.391172168e+03f, 6.955860838e+02f, -6.955860838e+02f, -6.955860838e+02f, -6.955860838e+02f, 1.391172168e+03f},
+    {2.086758251e+03f, 1.043379126e+03f, -1.043379126e+03f, -1.043379126e+03f, -1.043379126e+03f, 2.086758251e+03f},
+    {3.809881888e+03f, 1.904940944e+03f, -1.904940944e+03f, -1.904940944e+03f, -1.904940944e+03f, 3.809881888e+03f},
+    {8.934965025e+03f, 4.467482513e+03f, 0.000000000e+00f, 0.000000000e+00f, -4.467482513e+03f, 8.934965025e+03f},
+    {3.095162677e+04f, 1.547581339e+04f, 0.000000000e+00f, 0.000000000e+00f, -1.547581339e+04f, 0.000000000e+00f},
+    {4.175602740e+05f, 2.087801370e+05f, 0.000000000e+00f, 0.000000000e+00f, 2.087801370e+05f, 0.000000000e+00f},
+    {1.115976774e+05f, 5.579883870e+04f, 0.000000000e+00f, 0.000000000e+00f, 5.579883870e+04f, 1.115976774e+05f},
+    {4.377221036e+04f, 2.188610518e+04f, -2.188610518e+04f, 2.188610518e+04f, 2.188610518e+04f, 4.377221036e+04f},
+    {2.188610518e+04f, 1.094305259e+04f, -1.094305259e+04f, 1.094305259e+04f, 1.094305259e+04f, 2.188610518e+04f},
+    {1.319781800e+04f, 6.598909001e+03f, -6.598909001e+03f, 6.598909001e+03f, 6.598909001e+03f, 1.319781800e+04f},
+    {9.332266606e+03f, 4.666133303e+03f, -4.666133303e+03f, 4.666133303e+03f, 4.666133303e+03f, 9.332266606e+03f},
+    {7.619763776e+03f, 3.809881888e+03f, -3.809881888e+03f, 3.809881888e+03f, 3.809881888e+03f, 7.619763776e+03f},
+    {5.040000000e+03f, -2.520000000e+03f, -2.520000000e+03f, -2.520000000e+03f, -2.520000000e+03f, 5.040000000e+03f},
+    {7.619763776e+03f, 3.809881888e+03f, -3.809881888e+03f, -3.809881888e+03f, -3.809881888e+03f, 7.619763776e+03f},
+    {9.332266606e+03f, 4.666133303e+03f, -4.666133303e+03f, -4.666133303e+03f, -4.666133303e+03f, 9.332266606e+03f},
+    {1.319781800e+04f, 6.598909001e+03f, -6.598909001e+03f, -6.598909001e+03f, -6.598909001e+03f, 1.319781800e+04f},
+    {2.188610518e+04f, 1.094305259e+04f, -1.094305259e+04f, -1.094305259e+04f, -1.094305259e+04f, 2.188610518e+04f},
+    {4.377221036e+04f, 2.188610518e+04f, -2.188610518e+04f, -2.188610518e+04f, -2.188610518e+04f, 4.377221036e+04f},
+    {1.115976774e+05f, 5.579883870e+04f, 0.000000000e+00f, 0.000000000e+00f, -5.579883870e+04f, 1.115976774e+05f},
+    {4.175602740e+05f, 2.087801370e+05f, 0.000000000e+00f, 0.000000000e+00f, -2.087801370e+05f, 0.000000000e+00f},
+    {6.468815949e+06f, 3.234407974e+06f, 0.000000000e+00f, 0.000000000e+00f, 3.234407974e+06f, 0.000000000e+00f},
+    {1.617203987e+06f, 8.086019936e+05f, 0.000000000e+00f, 0.000000000e+00f, 8.086019936e+05f, 1.617203987e+06f},
+    {5.905194026e+05f, 2.952597013e+05f, -2.952597013e+05f, 2.952597013e+05f, 2.952597013e+05f, 5.905194026e+05f},
+    {2.733573661e+05f, 1.366786830e+05f, -1.366786830e+05f, 1.366786830e+05f, 1.366786830e+05f, 2.733573661e+05f},
+    {1.516313846e+05f, 7.581569231e+04f, -7.581569231e+04f, 7.581569231e+04f, 7.581569231e+04f, 1.516313846e+05f},
+    {9.787763790e+04f, 4.893881895e+04f, -4.893881895e+04f, 4.893881895e+04f, 4.893881895e+04f, 9.787763790e+04f},
+    {7.228742629e+04f, 3.614371315e+04f, -3.614371315e+04f, 3.614371315e+04f, 3.614371315e+04f, 7.228742629e+04f},
+    {6.048000000e+04f, 3.024000000e+04f, -3.024000000e+04f, 3.024000000e+04f, 3.024000000e+04f, 6.048000000e+04f},
+    {4.032000000e+04f, -2.016000000e+04f, -2.016000000e+04f, -2.016000000e+04f, -2.016000000e+04f, 4.032000000e+04f},
+    {6.048000000e+04f, 3.024000000e+04f, -3.024000000e+04f, -3.024000000e+04f, -3.024000000e+04f, 6.048000000e+04f},
+    {7.228742629e+04f, 3.614371315e+04f, -3.614371315e+04f, -3.614371315e+04f, -3.614371315e+04f, 7.228742629e+04f},
+    {9.787763790e+04f, 4.893881895e+04f, -4.893881895e+04f, -4.893881895e+04f, -4.893881895e+04f, 9.787763790e+04f},
+    {1.516313846e+05f, 7.581569231e+04f, -7.581569231e+04f, -7.581569231e+04f, -7.581569231e+04f, 1.516313846e+05f},
+    {2.733573661e+05f, 1.366786830e+05f, -1.366786830e+05f, -1.366786830e+05f, -1.366786830e+05f, 2.733573661e+05f},
+    {5.905194026e+05f, 2.952597013e+05f, -2.952597013e+05f, -2.952597013e+05f, -2.952597013e+05f, 5.905194026e+05f},
+    {1.617203987e+06f, 8.086019936e+05f, 0.000000000e+00f, 0.000000000e+00f, -8.086019936e+05f, 1.617203987e+06f},
+    {6.468815949e+06f, 3.234407974e+06f, 0.000000000e+00f, 0.000000000e+00f, -3.234407974e+06f, 0.000000000e+00f}};
+static __constant__ float c_shrec[9][9][2] = {
+    {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}},
+    {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}},
+    {{7.500000000e-01f, 2.500000000e-01f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}},
+    {{5.555555556e-01f, 1.111111111e-01f}, {6.250000000e-01f, 1.250000000e-01f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}},
+    {{4.375000000e-01f, 6.250000000e-02f}, {4.666666667e-01f, 6.666666667e-02f}, {5.833333333e-01f, 8.333333333e-02f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}},
+    {{3.600000000e-01f, 4.000000000e-02f}, {3.750000000e-01f, 4.166666667e-02f}, {4.285714286e-01f, 4.761904762e-02f}, {5.625000000e-01f, 6.250000000e-02f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}},
+    {{3.055555556e-01f, 2.777777778e-02f}, {3.142857143e-01f, 2.857142857e-02f}, {3.437500000e-01f, 3.125000000e-02f}, {4.074074074e-01f, 3.703703704e-02f}, {5.500000000e-01f, 5.000000000e-02f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}},
+    {{2.653061224e-01f, 2.040816327e-02f}, {2.708333333e-01f, 2.083333333e-02f}, {2.888888889e-01f, 2.222222222e-02f}, {3.250000000e-01f, 2.500000000e-02f}, {3.939393939e-01f, 3.030303030e-02f}, {5.416666667e-01f, 4.166666667e-02f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}},
+    {{2.343750000e-01f, 1.562500000e-02f}, {2.380952381e-01f, 1.587301587e-02f}, {2.500000000e-01f, 1.666666667e-02f}, {2.727272727e-01f, 1.818181818e-02f}, {3.125000000e-01f, 2.083333333e-02f}, {3.846153846e-01f, 2.564102564e-02f}, {5.357142857e-01f, 3.571428571e-02f}, {0.0f, 0.0f}, {0.0f, 0.0f}}};
+static __constant__ float c_shinv2l[9] = {0.0f, 5.000000000e-01f, 2.500000000e-01f, 1.666666667e-01f, 1.250000000e-01f, 1.000000000e-01f, 8.333333333e-02f, 7.142857143e-02f, 6.250000000e-02f};
+static constexpr int SH_COLS = 128, SH_SLOTS = 91;
+
+static __device__ __noinline__ Vec3<float> shexp_grad_smem(const ExpDev E, float scale, float x0, float x1, float x2) {
+    __shared__ float shcol[SH_SLOTS * SH_COLS];
+    float* col = shcol + threadIdx.x;
+#define SH_(s) col[(s) * SH_COLS]
+    const int L = E.lmax;
+    const int nt = (L + 1) * (L + 1);
+    const float r2 = x0 * x0 + x1 * x1 + x2 * x2;
+    const float ir = s_rsqrt(r2);
+    const float r = r2 * ir;
+    const float n0 = x0 * ir, n1 = x1 * ir, n2 = x2 * ir;
+    SH_(90) = 0.0f;
+    SH_(0) = 1.0f;
+    SH_(1) = 0.0f;
+#pragma unroll 1
+    for (int l = 1; l <= L; ++l) {
+        const int qp = (l - 1) * l / 2, q0 = l * (l + 1) / 2;  // rows l-1 and l
+        const float cpp = SH_(2 * (qp + l - 1)), spp = SH_(2 * (qp + l - 1) + 1);
+        const float f = c_shinv2l[l];
+        SH_(2 * (q0 + l)) = (n0 * cpp - n1 * spp) * f;
+        SH_(2 * (q0 + l) + 1) = (n0 * spp + n1 * cpp) * f;
+        SH_(2 * (q0 + l - 1)) = n2 * cpp;
+        SH_(2 * (q0 + l - 1) + 1) = n2 * spp;
+        const int qpp = (l - 2) * (l - 1) / 2;  // row l-2
+#pragma unroll 1
+        for (int m = 0; m + 2 <= l; ++m) {
+            const float a = c_shrec[l][m][0] * n2, b = c_shrec[l][m][1];
+            SH_(2 * (q0 + m)) = a * SH_(2 * (qp + m)) - b * SH_(2 * (qpp + m));
+            SH_(2 * (q0 + m) + 1) = a * SH_(2 * (qp + m) + 1) - b * SH_(2 * (qpp + m) + 1);
+        }
+    }
+    RadialBasis<float> B;
+    radial_basis<float>(E, s_log(r), B);
+    const float idu = (float)E.inv_du;
+    float S1 = 0.0f, V0 = 0.0f, V1 = 0.0f, V2 = 0.0f;
+#pragma unroll 2
+    for (int j = 0; j < nt; ++j) {
+        const short4 i0 = c_shterm_i[j][0], i1 = c_shterm_i[j][1];
+        float f, fs, fss;
+        radial_term<float>(E, B, nt, j, f, fs, fss);
+        const float a1 = fs * idu * ir;
+        const float G1 = a1 - (float)i1.z * f * ir;
+        S1 = fmaf(G1, c_shterm_f[j][0] * SH_(i0.x), S1);
+        const float gx = c_shterm_f[j][1] * SH_(i0.y) + c_shterm_f[j][2] * SH_(i0.z);
+        const float gy = c_shterm_f[j][3] * SH_(i0.w) + c_shterm_f[j][4] * SH_(i1.x);
+        const float gz = c_shterm_f[j][5] * SH_(i1.y);
+        V0 = fmaf(f, gx, V0);
+        V1 = fmaf(f, gy, V1);
+        V2 = fmaf(f, gz, V2);
+    }
+#undef SH_
+    return Vec3<float>{scale * (S1 * n0 + V0 * ir), scale * (S1 * n1 + V1 * ir), scale * (S1 * n2 + V2 * ir)};
+}
+
+// Straight-line FP32 form for a compile-time degree L (the stream's common
+// case, l_max = 8, with the FP32 interval table): every harmonic and term
+// index is a compile-time constant, so the rows live in registers and each
+// term is one float4 load plus ~30 FP32 operations.
+template <int L>
+static __device__ __noinline__ Vec3<float> shexp_grad_fixed(const ExpDev E, float scale, float x0, float x1, float x2) {
+    constexpr int nt = (L + 1) * (L + 1);
+    const float r2 = x0 * x0 + x1 * x1 + x2 * x2;
+    const float ir = s_rsqrt(r2);
+    const float r = r2 * ir;
+    const float n[3] = {x0 * ir, x1 * ir, x2 * ir};
+    RadialBasis<float> B;
+    radial_basis<float>(E, s_log(r), B);
+    const float4* tab = E.tab32 + (size_t)B.k * nt;
+    const float idu = (float)E.inv_du;
+    float R0c[L + 1], R0s[L + 1], R1c[L + 1], R1s[L + 1], R2c[L + 1], R2s[L + 1];
+#pragma unroll
+    for (int m = 0; m <= L; ++m) R0c[m] = R0s[m] = R1c[m] = R1s[m] = R2c[m] = R2s[m] = 0.0f;
+    R0c[0] = 1.0f;
+    float S1 = 0.0f, V0 = 0.0f, V1 = 0.0f, V2 = 0.0f;
+#pragma unroll
+    for (int l = 0; l <= L; ++l) {
+        if (l > 0) {
+#pragma unroll
+            for (int m = 0; m < l; ++m) {
+                R2c[m] = R1c[m];
+                R2s[m] = R1s[m];
+                R1c[m] = R0c[m];
+                R1s[m] = R0s[m];
+            }
+#pragma unroll
+            for (int m = 0; m + 2 <= l; ++m) {
+                const float a = (float)((2.0 * l - 1.0) / ((double)(l - m) * (l + m)));
+                const float b = (float)(1.0 / ((double)(l - m) * (l + m)));
+                R0c[m] = a * n[2] * R1c[m] - b * R2c[m];
+                R0s[m] = a * n[2] * R1s[m] - b * R2s[m];
+            }
+            R0c[l - 1] = n[2] * R1c[l - 1];
+            R0s[l - 1] = n[2] * R1s[l - 1];
+            const float f = (float)(1.0 / (2.0 * l));
+            R0c[l] = (n[0] * R1c[l - 1] - n[1] * R1s[l - 1]) * f;
+            R0s[l] = (n[0] * R1s[l - 1] + n[1] * R1c[l - 1]) * f;
+        }
+        // {Re, Im} of the degree-(l-1) row at any m (R^{-m} = (-1)^m conj R^m)
+        auto c1 = [&](int m) -> float {
+            if (m > l - 1 || -m > l - 1) return 0.0f;
+            return m >= 0 ? R1c[m] : ((m & 1) ? -R1c[-m] : R1c[-m]);
+        };
+        auto s1 = [&](int m) -> float {
+            if (m > l - 1 || -m > l - 1) return 0.0f;
+            return m >= 0 ? R1s[m] : ((m & 1) ? R1s[-m] : -R1s[-m]);
+        };
+        const float fl = (float)l;
+#pragma unroll
+        for (int mm = -l; mm <= l; ++mm) {
+            const int m = mm < 0 ? -mm : mm;
+            const float N = (float)shnorm_ct(l, m);
+            const float4 t = __ldg(tab + (l * l + l + mm));
+            const float fs = B.hs[0] * t.x + B.hs[1] * t.y + B.hs[2] * t.z + B.hs[3] * t.w;
+            const float f = B.h[0] * t.x + B.h[1] * t.y + B.h[2] * t.z + B.h[3] * t.w + B.e * fs;
+            const float G1 = (fs * idu - fl * f) * ir;
+            float K, g0, g1, g2;
+            if (mm >= 0) {
+                K = R0c[m];
+                g0 = 0.5f * (c1(m - 1) - c1(m + 1));
+                g1 = -0.5f * (s1(m + 1) + s1(m - 1));
+                g2 = c1(m);
+            } else {
+                K = R0s[m];
+                g0 = 0.5f * (s1(m - 1) - s1(m + 1));
+                g1 = 0.5f * (c1(m + 1) + c1(m - 1));
+                g2 = s1(m);
+            }
+            const float fN = f * N;
+            S1 = fmaf(G1 * N, K, S1);
+            V0 = fmaf(fN, g0, V0);
+            V1 = fmaf(fN, g1, V1);
+            V2 = fmaf(fN, g2, V2);
+        }
+    }
+    return Vec3<float>{scale * (S1 * n[0] + V0 * ir), scale * (S1 * n[1] + V1 * ir), scale * (S1 * n[2] + V2 * ir)};
+}
+
 template <class T, class R, bool HESS>
 __device__ __noinline__ void shexp_grad_ref(const ExpDev& E, const R scale, const T x[3], T grad[3], T H[6]) {
     shexp_grad_impl<T, R, HESS>(E, scale, x, grad, H);
@@ -713,7 +1052,21 @@ __device__ __noinline__ void shexp_grad_ref(const ExpDev& E, const R scale, cons
 
 template <class T, class R, bool HESS>
 __device__ __forceinline__ void shexp_grad(const ExpDev& E, const R scale, const T x[3], T grad[3], T H[6]) {
-    if constexpr (std::is_floating_point<T>::value && std::is_same<T, R>::value && !HESS) {
+    if constexpr (std::is_same<T, float>::value && std::is_same<T, R>::value && !HESS) {
+        if (E.lmax == SS_SHEXP_LMAX && E.tab32 != nullptr) {
+            const Vec3<float> g = shexp_grad_fixed<SS_SHEXP_LMAX>(E, scale, x[0], x[1], x[2]);
+            grad[0] += g.x;
+            grad[1] += g.y;
+            grad[2] += g.z;
+        } else if (blockDim.x <= SH_COLS) {
+            const Vec3<float> g = shexp_grad_smem(E, scale, x[0], x[1], x[2]);
+            grad[0] += g.x;
+            grad[1] += g.y;
+            grad[2] += g.z;
+        } else {
+            shexp_grad_ref<T, R, HESS>(E, scale, x, grad, H);
+        }
+    } else if constexpr (std::is_floating_point<T>::value && std::is_same<T, R>::value && !HESS) {
         const Vec3<T> g = shexp_grad_value<T>(E, scale, x[0], x[1], x[2]);
         grad[0] += g.x;
         grad[1] += g.y;

@@ -1,10 +1,12 @@
 // ss_mlp_stream.cu — particle-spray stream whose force is the learned
 // surrogate, evaluated on the 5th-generation tensor cores.
 //
-// One CTA = one warpgroup (128 threads) = a tile of 128 particles, persistent
-// over tiles.  The CTA integrates its tile with the FP32-compensated Dopri5
-// step of the plain stream (step_f32k); every stage's force is one
-// CTA-collective network evaluation:
+// One CTA = two warpgroups (256 threads); each warpgroup owns its own tile
+// of 128 particles (one per thread) and runs independently of the other, so
+// one warpgroup's epilogue math overlaps the other's tensor-core GEMMs.  A
+// warpgroup integrates its tile with the FP32-compensated Dopri5 step of the
+// plain stream (step_f32k); every stage's force is one warpgroup-collective
+// network evaluation:
 //   layer 1 (4 -> 128) on CUDA cores in FP32 (keeps the input precision),
 //   layers 2-4 as tcgen05.mma 128 x 128 x 128 BF16 GEMMs with FP32
 //   accumulators in tensor memory (TMEM),
@@ -13,15 +15,17 @@
 //   product on CUDA cores.
 // Shared memory holds W2..W4 as BF16 in the no-swizzle core-matrix layout
 // (8 rows x 16 bytes per core matrix; element (o, i) of W at byte
-// (o/8)*2048 + (i/8)*128 + (o%8)*16 + (i%8)*2), the activation/delta tile
-// A [128 particles x 128] in the same layout, and W1, biases and w5 in FP32.
-// TMEM (512 columns x 128 lanes, lane = particle): R1..R3 keep s'(z1..z3)
-// for the backward chain, R4 is the accumulator of layer 4 and of the three
-// backward GEMMs.  One thread issues the MMAs; completion is signalled by
-// tcgen05.commit on an mbarrier; each evaluation waits six times, so the
-// wait parities are 0,1,0,1,0,1 in every evaluation.  Every wait is bounded:
-// on a timeout the CTA records SS_STATUS_ABORTED for its particles, stops
-// issuing MMAs and releases its TMEM.
+// (o/8)*2048 + (i/8)*128 + (o%8)*16 + (i%8)*2), one activation/delta tile A
+// [128 particles x 128] per warpgroup in the same layout, and W1, biases and
+// w5 in FP32.  TMEM (512 columns x 128 lanes, lane = particle): per
+// warpgroup 256 columns = s'(z2), s'(z3) as packed BF16 pairs (64 columns
+// each) for the backward chain and one FP32 accumulator (128 columns);
+// s'(z1) is recomputed from the inputs.  One thread per warpgroup issues the
+// MMAs; completion is signalled by tcgen05.commit on the warpgroup's
+// mbarrier; each evaluation waits six times, so the wait parities are
+// 0,1,0,1,0,1 in every evaluation.  Every wait is bounded: on a timeout the
+// warpgroup records SS_STATUS_ABORTED for its particles, stops issuing MMAs
+// and the CTA releases its TMEM.
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -40,19 +44,20 @@ static constexpr int64_t P_W1 = 0, P_B1 = 512, P_W2 = 640, P_B2 = P_W2 + 16384, 
 static_assert(P_B5 + 1 == SS_MLP_NPARAM, "parameter packing");
 
 // shared-memory map (bytes from a 1024-aligned base)
-static constexpr uint32_t SM_W2 = 0, SM_W3 = 32768, SM_W4 = 65536, SM_A = 98304;
-static constexpr uint32_t SM_W1 = 131072;             // float [128][4]
+static constexpr uint32_t SM_W2 = 0, SM_W3 = 32768, SM_W4 = 65536, SM_A = 98304;  // A tiles: 2 x 32 KB
+static constexpr uint32_t SM_W1 = SM_A + 65536;       // float [128][4]
 static constexpr uint32_t SM_B = SM_W1 + 2048;        // float b1..b4 [4][128]
 static constexpr uint32_t SM_W5 = SM_B + 2048;        // float [128]
-static constexpr uint32_t SM_BAR = SM_W5 + 512;       // mbarrier (8 B)
-static constexpr uint32_t SM_TMEM = SM_BAR + 8;       // TMEM base address
-static constexpr uint32_t SM_ABORT = SM_TMEM + 4;     // abort flag
-static constexpr uint32_t SM_START = SM_ABORT + 4;    // tile start step
-static constexpr uint32_t SM_BYTES = SM_START + 4;
+static constexpr uint32_t SM_BAR = SM_W5 + 512;       // 2 mbarriers (8 B each)
+static constexpr uint32_t SM_TMEM = SM_BAR + 16;      // TMEM base address
+static constexpr uint32_t SM_ABORT = SM_TMEM + 4;     // 2 abort flags
+static constexpr uint32_t SM_START = SM_ABORT + 8;    // 2 tile start steps
+static constexpr uint32_t SM_BYTES = SM_START + 8;
 static constexpr uint32_t SM_ALLOC = SM_BYTES + 1024;  // slack for the 1024-byte alignment
 
-// TMEM columns
-static constexpr uint32_t T_R1 = 0, T_R2 = 128, T_R3 = 256, T_R4 = 384;
+// TMEM columns within a warpgroup's 256
+static constexpr uint32_t T_S2 = 0, T_S3 = 64, T_ACC = 128;
+static constexpr int MLP_THREADS = 256;
 
 // MN-major B operand, no swizzle: SBO = stride between core matrices along
 // N (the contiguous 16 bytes), LBO = stride along K.
@@ -134,6 +139,22 @@ __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.a
                  "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])                 \
                  : "memory")
 
+#define SS_TMEM_LD16(r, taddr)                                                                                     \
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, " \
+                 "[%16];"                                                                                          \
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), \
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),        \
+                   "=r"(r[15])                                                                                      \
+                 : "r"(taddr)                                                                                       \
+                 : "memory")
+
+#define SS_TMEM_ST16(taddr, r)                                                                                      \
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"    \
+                 "%15,%16};" ::"r"(taddr),                                                                          \
+                 "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), \
+                 "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])                  \
+                 : "memory")
+
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
@@ -149,9 +170,67 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
     return *reinterpret_cast<uint32_t*>(&v);
 }
 
-// 32 consecutive features (8-aligned chunk c of row t) into the A tile.
-__device__ __forceinline__ void store_row32(uint8_t* sm, int t, int c, const float v[32]) {
-    uint8_t* row = sm + SM_A + (t >> 3) * 2048 + (t & 7) * 16;
+struct MlpCta {
+    uint32_t tmem;      // this warpgroup's TMEM base (lane 0, its first column)
+    uint32_t lane_off;  // this warp's lane offset << 16
+    uint32_t bar;       // this warpgroup's mbarrier (shared address)
+    uint32_t base;      // shared address of the aligned base
+    uint32_t a_off;     // this warpgroup's A tile (offset from the base)
+    int wg;             // warpgroup 0 or 1
+};
+
+// barrier over one warpgroup (named barrier 1 + wg, 128 threads)
+__device__ __forceinline__ void wg_sync(int wg) { asm volatile("bar.sync %0, 128;" ::"r"(1 + wg) : "memory"); }
+
+// barrier over one warpgroup that also ORs a flag across it
+__device__ __forceinline__ bool wg_sync_or(int wg, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n.reg .pred p, q;\nsetp.ne.u32 q, %1, 0;\nbar.red.or.pred p, %2, 128, q;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(1 + wg)
+        : "memory");
+    return r != 0;
+}
+
+// Issue one 128x128x128 GEMM of this warpgroup into its accumulator and
+// wait for it.  wsm: weight tile offset; b_mn: 0 = z = A W^T (forward),
+// 1 = u = A W (backward).  Returns false on a wait timeout (abort).
+__device__ __forceinline__ bool gemm_layer(const MlpCta& cx, uint32_t wsm, uint32_t b_mn, uint32_t parity,
+                                           volatile uint32_t* abort) {
+    tmem_wait_st();
+    fence_async_smem();
+    fence_before();
+    wg_sync(cx.wg);
+    if (*abort) return false;
+    if ((threadIdx.x & 127) == 0) {
+        fence_after();
+        const uint32_t id = idesc_bf16(b_mn);
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk) {
+            const uint64_t ad = smem_desc(cx.base + cx.a_off + kk * 256, 128, 2048);
+            const uint64_t bd = b_mn ? smem_desc(cx.base + wsm + kk * 4096, MN_LBO, MN_SBO)
+                                     : smem_desc(cx.base + wsm + kk * 256, 128, 2048);
+            mma_bf16(cx.tmem + T_ACC, ad, bd, id, kk > 0 ? 1u : 0u);
+        }
+        mma_commit(cx.bar);
+    }
+    const bool ok = mbar_wait(cx.bar, parity);
+    fence_after();
+    // every thread of the warpgroup takes the same path after a timeout
+    if (wg_sync_or(cx.wg, !ok)) {
+        *abort = 1u;
+        return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ float bf_lo(uint32_t u) { return __uint_as_float(u << 16); }
+__device__ __forceinline__ float bf_hi(uint32_t u) { return __uint_as_float(u & 0xffff0000u); }
+
+// store 32 consecutive features of one particle row into an A tile
+__device__ __forceinline__ void store_row32_at(uint8_t* tile, int row, int c, const float v[32]) {
+    uint8_t* r = tile + (row >> 3) * 2048 + (row & 7) * 16;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         uint4 w;
@@ -159,150 +238,122 @@ __device__ __forceinline__ void store_row32(uint8_t* sm, int t, int c, const flo
         w.y = pack_bf16(v[8 * q + 2], v[8 * q + 3]);
         w.z = pack_bf16(v[8 * q + 4], v[8 * q + 5]);
         w.w = pack_bf16(v[8 * q + 6], v[8 * q + 7]);
-        *reinterpret_cast<uint4*>(row + (4 * c + q) * 128) = w;
+        *reinterpret_cast<uint4*>(r + (4 * c + q) * 128) = w;
     }
 }
 
-struct MlpCta {
-    uint32_t tmem;      // TMEM base (lane 0, column 0)
-    uint32_t lane_off;  // this warp's lane offset << 16
-    uint32_t bar;       // mbarrier shared address
-    uint32_t base;      // shared address of the aligned base
-};
-
-// Issue one 128x128x128 GEMM into TMEM column `dcol` and wait for it.
-// wsm: weight tile offset; b_mn: 0 = z = A W^T (forward), 1 = u = A W
-// (backward).  Returns false on a wait timeout (abort).
-__device__ __forceinline__ bool gemm_layer(const MlpCta& cx, uint32_t wsm, uint32_t b_mn, uint32_t dcol,
-                                           uint32_t parity, volatile uint32_t* abort) {
-    tmem_wait_st();
-    fence_async_smem();
-    fence_before();
-    __syncthreads();
-    if (*abort) return false;
-    if (threadIdx.x == 0) {
-        fence_after();
-        const uint32_t id = idesc_bf16(b_mn);
-#pragma unroll
-        for (int kk = 0; kk < 8; ++kk) {
-            const uint64_t ad = smem_desc(cx.base + SM_A + kk * 256, 128, 2048);
-            const uint64_t bd = b_mn ? smem_desc(cx.base + wsm + kk * 4096, MN_LBO, MN_SBO)
-                                     : smem_desc(cx.base + wsm + kk * 256, 128, 2048);
-            mma_bf16(cx.tmem + dcol, ad, bd, id, kk > 0 ? 1u : 0u);
-        }
-        mma_commit(cx.bar);
-    }
-    const bool ok = mbar_wait(cx.bar, parity);
-    fence_after();
-    // every thread takes the same path after a timeout in any of them
-    if (__syncthreads_or(!ok)) {
-        *abort = 1u;
-        return false;
-    }
-    return true;
-}
-
-// grad Phi at X (FP32) for every thread of the CTA (collective).
-__device__ __noinline__ void mlp_grad_cta(const MlpDev& M, const MlpCta& cx, float X0, float X1, float X2, float& g0,
-                                          float& g1, float& g2) {
+// grad Phi at X (FP32) for every thread of one warpgroup (collective).
+__device__ __noinline__ void mlp_grad_wg(const MlpDev& M, const MlpCta& cx, float X0, float X1, float X2, float& g0,
+                                         float& g1, float& g2) {
     uint8_t* sm = mlp_smem();
-    volatile uint32_t* abort = reinterpret_cast<volatile uint32_t*>(sm + SM_ABORT);
+    volatile uint32_t* abort = reinterpret_cast<volatile uint32_t*>(sm + SM_ABORT) + cx.wg;
     const float* W1 = reinterpret_cast<const float*>(sm + SM_W1);
     const float* Bb = reinterpret_cast<const float*>(sm + SM_B);
     const float* w5 = reinterpret_cast<const float*>(sm + SM_W5);
-    const int t = threadIdx.x;
+    uint8_t* tile = sm + cx.a_off;
+    const int row = threadIdx.x & 127;
     const uint32_t tl = cx.tmem + cx.lane_off;
     g0 = g1 = g2 = 0.0f;
     if (*abort) return;
     const float r2 = X0 * X0 + X1 * X1 + X2 * X2;
     const float u0 = (X0 - M.s[0]) * M.c[0], u1 = (X1 - M.s[1]) * M.c[1], u2 = (X2 - M.s[2]) * M.c[2];
     const float u3 = (0.5f * logf(r2) - M.s[3]) * M.c[3];
-    // layer 1 on CUDA cores: a1 -> A tile, s'(z1) -> TMEM R1
+    // layer 1 on CUDA cores: a1 -> A tile (s'(z1) is recomputed in the backward pass)
 #pragma unroll 1
     for (int c = 0; c < 4; ++c) {
         float a[32];
-        uint32_t sp[32];
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
             const int f = 32 * c + j;
             const float4 w = *reinterpret_cast<const float4*>(W1 + 4 * f);
             const float z = fmaf(w.x, u0, fmaf(w.y, u1, fmaf(w.z, u2, fmaf(w.w, u3, Bb[f]))));
-            const float s = sigm(z);
-            a[j] = z * s;
-            sp[j] = __float_as_uint(s * fmaf(z, 1.0f - s, 1.0f));
+            a[j] = z * sigm(z);
         }
-        store_row32(sm, t, c, a);
-        SS_TMEM_ST32(tl + T_R1 + 32 * c, sp);
+        store_row32_at(tile, row, c, a);
     }
-    // layers 2 and 3: z = a W^T + b, a = SiLU(z) -> A tile, s'(z) -> TMEM
+    // layers 2 and 3: z = a W^T + b, a = SiLU(z) -> A tile, s'(z) -> S2 / S3 (packed BF16)
 #pragma unroll 1
     for (int k = 2; k <= 3; ++k) {
-        const uint32_t col = k == 2 ? T_R2 : T_R3;
-        if (!gemm_layer(cx, k == 2 ? SM_W2 : SM_W3, 0, col, k == 2 ? 0u : 1u, abort)) return;
+        if (!gemm_layer(cx, k == 2 ? SM_W2 : SM_W3, 0, k == 2 ? 0u : 1u, abort)) return;
         const float* bk = Bb + (k - 1) * MLP_W;
+        const uint32_t sc = k == 2 ? T_S2 : T_S3;
 #pragma unroll 1
         for (int c = 0; c < 4; ++c) {
-            uint32_t r[32];
+            uint32_t r[32], sp[16];
             float a[32];
-            SS_TMEM_LD32(r, tl + col + 32 * c);
+            SS_TMEM_LD32(r, tl + T_ACC + 32 * c);
             tmem_wait_ld();
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                const float z = __uint_as_float(r[j]) + bk[32 * c + j];
-                const float s = sigm(z);
-                a[j] = z * s;
-                r[j] = __float_as_uint(s * fmaf(z, 1.0f - s, 1.0f));
+            for (int j = 0; j < 32; j += 2) {
+                float s2[2];
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const float z = __uint_as_float(r[j + e]) + bk[32 * c + j + e];
+                    const float sg = sigm(z);
+                    a[j + e] = z * sg;
+                    s2[e] = sg * fmaf(z, 1.0f - sg, 1.0f);
+                }
+                sp[j / 2] = pack_bf16(s2[0], s2[1]);
             }
-            store_row32(sm, t, c, a);
-            SS_TMEM_ST32(tl + col + 32 * c, r);
+            store_row32_at(tile, row, c, a);
+            SS_TMEM_ST16(tl + sc + 16 * c, sp);
         }
     }
     // layer 4: only s'(z4) is needed: d4 = w5 s'(z4) -> A tile
-    if (!gemm_layer(cx, SM_W4, 0, T_R4, 0u, abort)) return;
+    if (!gemm_layer(cx, SM_W4, 0, 0u, abort)) return;
     {
         const float* b4 = Bb + 3 * MLP_W;
 #pragma unroll 1
         for (int c = 0; c < 4; ++c) {
             uint32_t r[32];
             float d[32];
-            SS_TMEM_LD32(r, tl + T_R4 + 32 * c);
+            SS_TMEM_LD32(r, tl + T_ACC + 32 * c);
             tmem_wait_ld();
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
-                const float z = __uint_as_float(r[j]) + b4[32 * c + j];
-                const float s = sigm(z);
-                d[j] = w5[32 * c + j] * (s * fmaf(z, 1.0f - s, 1.0f));
+                const int f = 32 * c + j;
+                const float z = __uint_as_float(r[j]) + b4[f];
+                const float sg = sigm(z);
+                d[j] = w5[f] * (sg * fmaf(z, 1.0f - sg, 1.0f));
             }
-            store_row32(sm, t, c, d);
+            store_row32_at(tile, row, c, d);
         }
     }
     // backward: u = d W_k (MN-major B), d_{k-1} = u s'(z_{k-1})
     const uint32_t wk[3] = {SM_W4, SM_W3, SM_W2};
-    const uint32_t sk[3] = {T_R3, T_R2, T_R1};
     float gi[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll 1
     for (int q = 0; q < 3; ++q) {
-        if (!gemm_layer(cx, wk[q], 1, T_R4, q == 1 ? 0u : 1u, abort)) return;
+        if (!gemm_layer(cx, wk[q], 1, q == 1 ? 0u : 1u, abort)) return;
 #pragma unroll 1
         for (int c = 0; c < 4; ++c) {
-            uint32_t r[32], s[32];
-            SS_TMEM_LD32(r, tl + T_R4 + 32 * c);
-            SS_TMEM_LD32(s, tl + sk[q] + 32 * c);
-            tmem_wait_ld();
+            uint32_t r[32];
             float d[32];
-#pragma unroll
-            for (int j = 0; j < 32; ++j) d[j] = __uint_as_float(r[j]) * __uint_as_float(s[j]);
+            SS_TMEM_LD32(r, tl + T_ACC + 32 * c);
             if (q < 2) {
-                store_row32(sm, t, c, d);
+                uint32_t sv[16];
+                SS_TMEM_LD16(sv, tl + (q == 0 ? T_S3 : T_S2) + 16 * c);
+                tmem_wait_ld();
+#pragma unroll
+                for (int j = 0; j < 32; j += 2) {
+                    d[j] = __uint_as_float(r[j]) * bf_lo(sv[j / 2]);
+                    d[j + 1] = __uint_as_float(r[j + 1]) * bf_hi(sv[j / 2]);
+                }
+                store_row32_at(tile, row, c, d);
             } else {
-                // g = W1^T d1 (FP32)
+                tmem_wait_ld();
+                // d1 = u1 s'(z1) with s'(z1) recomputed; g = W1^T d1 (FP32)
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
-                    const float4 w = *reinterpret_cast<const float4*>(W1 + 4 * (32 * c + j));
-                    gi[0] = fmaf(w.x, d[j], gi[0]);
-                    gi[1] = fmaf(w.y, d[j], gi[1]);
-                    gi[2] = fmaf(w.z, d[j], gi[2]);
-                    gi[3] = fmaf(w.w, d[j], gi[3]);
+                    const int f = 32 * c + j;
+                    const float4 w = *reinterpret_cast<const float4*>(W1 + 4 * f);
+                    const float z = fmaf(w.x, u0, fmaf(w.y, u1, fmaf(w.z, u2, fmaf(w.w, u3, Bb[f]))));
+                    const float sg = sigm(z);
+                    const float d1 = __uint_as_float(r[j]) * (sg * fmaf(z, 1.0f - sg, 1.0f));
+                    gi[0] = fmaf(w.x, d1, gi[0]);
+                    gi[1] = fmaf(w.y, d1, gi[1]);
+                    gi[2] = fmaf(w.z, d1, gi[2]);
+                    gi[3] = fmaf(w.w, d1, gi[3]);
                 }
             }
         }
@@ -336,12 +387,14 @@ template <class T, class R, bool HESS>
 __device__ __forceinline__ void MlpComp::grad(const PotDev<R>&, const T x[3], const T*, T g[3], T*) {
     uint8_t* sm = mlp_smem();
     MlpCta cx;
-    cx.tmem = *reinterpret_cast<volatile uint32_t*>(sm + SM_TMEM);
-    cx.lane_off = (uint32_t)(32 * (threadIdx.x >> 5)) << 16;
-    cx.bar = smem_u32(sm + SM_BAR);
+    cx.wg = threadIdx.x >> 7;
+    cx.tmem = *reinterpret_cast<volatile uint32_t*>(sm + SM_TMEM) + 256u * cx.wg;
+    cx.lane_off = (uint32_t)(32 * ((threadIdx.x >> 5) & 3)) << 16;
+    cx.bar = smem_u32(sm + SM_BAR + 8 * cx.wg);
     cx.base = smem_u32(sm);
+    cx.a_off = SM_A + 32768u * cx.wg;
     const MlpKernelArgs* ka = mlp_args_ptr();
-    mlp_grad_cta(ka->M, cx, x[0], x[1], x[2], g[0], g[1], g[2]);
+    mlp_grad_wg(ka->M, cx, x[0], x[1], x[2], g[0], g[1], g[2]);
 }
 
 // CTA prologue: weights -> shared memory (BF16 core-matrix tiles, FP32
@@ -350,7 +403,7 @@ __device__ __forceinline__ void mlp_cta_setup(const MlpKernelArgs& ka) {
     uint8_t* sm = mlp_smem();
     const int t = threadIdx.x;
     const float* prm = ka.M.params;
-    for (int e = t; e < 3 * 16384; e += 128) {
+    for (int e = t; e < 3 * 16384; e += blockDim.x) {
         const int k = e / 16384, idx = e % 16384, o = idx / 128, i = idx % 128;
         const float w = prm[(k == 0 ? P_W2 : k == 1 ? P_W3 : P_W4) + idx];
         __nv_bfloat16 b = __float2bfloat16_rn(w);
@@ -360,8 +413,8 @@ __device__ __forceinline__ void mlp_cta_setup(const MlpKernelArgs& ka) {
     float* W1 = reinterpret_cast<float*>(sm + SM_W1);
     float* Bb = reinterpret_cast<float*>(sm + SM_B);
     float* w5 = reinterpret_cast<float*>(sm + SM_W5);
-    for (int e = t; e < 512; e += 128) W1[e] = prm[P_W1 + e];
-    for (int e = t; e < 128; e += 128) {
+    for (int e = t; e < 512; e += blockDim.x) W1[e] = prm[P_W1 + e];
+    for (int e = t; e < 128; e += blockDim.x) {
         Bb[e] = prm[P_B1 + e];
         Bb[128 + e] = prm[P_B2 + e];
         Bb[256 + e] = prm[P_B3 + e];
@@ -370,8 +423,10 @@ __device__ __forceinline__ void mlp_cta_setup(const MlpKernelArgs& ka) {
     }
     if (t == 0) {
         mlp_args_ptr() = &ka;
-        *reinterpret_cast<uint32_t*>(sm + SM_ABORT) = 0u;
+        reinterpret_cast<uint32_t*>(sm + SM_ABORT)[0] = 0u;
+        reinterpret_cast<uint32_t*>(sm + SM_ABORT)[1] = 0u;
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(sm + SM_BAR)), "r"(1));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(sm + SM_BAR + 8)), "r"(1));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if ((t >> 5) == 0) {
@@ -385,19 +440,19 @@ __device__ __forceinline__ void mlp_cta_setup(const MlpKernelArgs& ka) {
     fence_after();
 }
 
-// CTA epilogue: release TMEM (after a timeout, first give the outstanding
-// commit a bounded wait).
+// CTA epilogue: release TMEM (after a timeout, the warpgroup first gives
+// its outstanding commit a bounded wait).
 __device__ __forceinline__ void mlp_cta_teardown() {
     uint8_t* sm = mlp_smem();
     volatile uint32_t* abort = reinterpret_cast<volatile uint32_t*>(sm + SM_ABORT);
+    const int wg = threadIdx.x >> 7;
+    if (abort[wg] && (threadIdx.x & 127) == 0) {
+        mbar_wait(smem_u32(sm + SM_BAR + 8 * wg), 0u);
+        mbar_wait(smem_u32(sm + SM_BAR + 8 * wg), 1u);
+    }
     fence_before();
     __syncthreads();
     fence_after();
-    if (*abort && threadIdx.x == 0) {
-        mbar_wait(smem_u32(sm + SM_BAR), 0u);
-        mbar_wait(smem_u32(sm + SM_BAR), 1u);
-    }
-    __syncthreads();
     if ((threadIdx.x >> 5) == 0) {
         const uint32_t tm = *reinterpret_cast<volatile uint32_t*>(sm + SM_TMEM);
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(512));
@@ -405,16 +460,18 @@ __device__ __forceinline__ void mlp_cta_teardown() {
 }
 
 // grad Phi of the surrogate at points xyz [n,3] (tensor-core path; tests)
-__global__ void __launch_bounds__(128, 1) mlp_grad_kernel(const __grid_constant__ MlpKernelArgs ka, const double* xyz,
-                                                          int64_t n, double* grad, int32_t* status) {
+__global__ void __launch_bounds__(MLP_THREADS, 1) mlp_grad_kernel(const __grid_constant__ MlpKernelArgs ka, const double* xyz,
+                                                                  int64_t n, double* grad, int32_t* status) {
     mlp_cta_setup(ka);
     uint8_t* sm = mlp_smem();
-    volatile uint32_t* abort = reinterpret_cast<volatile uint32_t*>(sm + SM_ABORT);
+    const int wg = threadIdx.x >> 7;
+    volatile uint32_t* abort = reinterpret_cast<volatile uint32_t*>(sm + SM_ABORT) + wg;
     PotDev<float> P;
     P.n = 0;
     P.has_track = 0;
-    for (int64_t tile = blockIdx.x; tile < (n + 127) / 128; tile += gridDim.x) {
-        const int64_t p = tile * 128 + threadIdx.x;
+    const int64_t n_tiles = (n + 127) / 128;
+    for (int64_t tile = 2 * (int64_t)blockIdx.x + wg; tile < n_tiles; tile += 2 * (int64_t)gridDim.x) {
+        const int64_t p = tile * 128 + (threadIdx.x & 127);
         const int64_t q = p < n ? p : 0;
         const float x[3] = {(float)xyz[3 * q], (float)xyz[3 * q + 1], (float)xyz[3 * q + 2]};
         float g[3];
@@ -428,29 +485,31 @@ __global__ void __launch_bounds__(128, 1) mlp_grad_kernel(const __grid_constant_
     mlp_cta_teardown();
 }
 
-__global__ void __launch_bounds__(128, 1) stream_mlp_kernel(const __grid_constant__ MlpKernelArgs ka) {
+__global__ void __launch_bounds__(MLP_THREADS, 1) stream_mlp_kernel(const __grid_constant__ MlpKernelArgs ka) {
     mlp_cta_setup(ka);
     uint8_t* sm = mlp_smem();
-    const int t = threadIdx.x;
+    const int t = threadIdx.x & 127, wg = threadIdx.x >> 7;
     const StreamArgs& a = ka.a;
-    volatile uint32_t* abort = reinterpret_cast<volatile uint32_t*>(sm + SM_ABORT);
+    volatile uint32_t* abort = reinterpret_cast<volatile uint32_t*>(sm + SM_ABORT) + wg;
+    int* s_start = reinterpret_cast<int*>(sm + SM_START) + wg;
     PotDev<float> P;  // unused by MlpComp (no track, no subhalos)
     P.n = 0;
     P.has_track = 0;
-    for (int64_t tile = blockIdx.x; tile < ka.n_tiles; tile += gridDim.x) {
+    // warpgroups take alternate tiles and run independently
+    for (int64_t tile = 2 * (int64_t)blockIdx.x + wg; tile < ka.n_tiles; tile += 2 * (int64_t)gridDim.x) {
         const int64_t p = tile * 128 + t;
         const bool valid = p < a.N;
         const int start = valid ? (int)((p / a.ppr) * (int64_t)a.spr) : a.n_steps;
         // the tile steps from its earliest start; particles not yet released
         // step a copy (their rows of the GEMMs are independent)
-        int* s_start = reinterpret_cast<int*>(sm + SM_START);
         if (t == 0) *s_start = a.n_steps;
-        __syncthreads();
+        wg_sync(wg);
         atomicMin(s_start, start);
-        __syncthreads();
+        wg_sync(wg);
         const int tstart = *s_start;
+        wg_sync(wg);
         float xh[3], xl[3], vh[3], vl[3];
-        const int64_t q = valid ? p : (a.N > 0 ? (int64_t)0 : 0);
+        const int64_t q = valid ? p : 0;
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             const double xd = a.ics[6 * q + i], vd = a.ics[6 * q + 3 + i];
@@ -535,8 +594,8 @@ int ss_mlp_grad_bf16(const ss_mlp* mlp, const double* xyz, int64_t n, double* gr
     SS_CUDA_TRY(cudaGetDevice(&dev));
     SS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     SS_CUDA_TRY(cudaFuncSetAttribute(mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM_ALLOC));
-    const int64_t tiles = (n + 127) / 128;
-    mlp_grad_kernel<<<(unsigned)(tiles < sms ? tiles : sms), 128, SM_ALLOC, (cudaStream_t)stream>>>(ka, xyz, n, grad,
+    const int64_t pairs = ((n + 127) / 128 + 1) / 2;
+    mlp_grad_kernel<<<(unsigned)(pairs < sms ? pairs : sms), MLP_THREADS, SM_ALLOC, (cudaStream_t)stream>>>(ka, xyz, n, grad,
                                                                                                       status);
     SS_LAUNCH_CHECK();
     return SS_OK;
@@ -585,8 +644,9 @@ int ss_stream_mlp_bf16(const ss_mlp* mlp, const ss_stream_cfg* cfg, const double
     SS_CUDA_TRY(cudaGetDevice(&dev));
     SS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     SS_CUDA_TRY(cudaFuncSetAttribute(stream_mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM_ALLOC));
-    const int64_t grid = ka.n_tiles < sms ? ka.n_tiles : sms;
-    stream_mlp_kernel<<<(unsigned)grid, 128, SM_ALLOC, (cudaStream_t)stream>>>(ka);
+    const int64_t pairs = (ka.n_tiles + 1) / 2;
+    const int64_t grid = pairs < sms ? pairs : sms;
+    stream_mlp_kernel<<<(unsigned)grid, MLP_THREADS, SM_ALLOC, (cudaStream_t)stream>>>(ka);
     SS_LAUNCH_CHECK();
     return SS_OK;
 }

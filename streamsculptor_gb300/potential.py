@@ -298,6 +298,18 @@ class SubhaloLinePotential_Custom(_SubhaloLines):
         self._kind = kind
 
 
+class SubhaloLinePotentialCustom_fromFunc(SubhaloLinePotential_Custom):
+    """Subhalos on lines with the profile class `func` (PlummerPotential or
+    HernquistPotential) built from arrays m, r_s (potential.py:1161-1213)."""
+
+    def __init__(self, func, m, r_s, subhalo_x0, subhalo_v, subhalo_t0, t_window, units=None):
+        if func not in (PlummerPotential, HernquistPotential):
+            raise NotImplementedError("SubhaloLinePotentialCustom_fromFunc supports PlummerPotential and "
+                                      "HernquistPotential")
+        super().__init__(func(m=m, r_s=r_s, units=units), subhalo_x0, subhalo_v, subhalo_t0, t_window, units=units)
+        self.func = func
+
+
 class CustomPotential(Potential):
     """Arbitrary Python potential_func(xyz, t): no GPU implementation."""
 

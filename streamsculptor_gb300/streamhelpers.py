@@ -220,7 +220,53 @@ def gen_stream_vmapped_Chen25(pot_base, ts, prog_w0, Msat, key, solver=None, rto
                       n_particles_per_release=n_particles_per_release, throw=throw)
 
 
+def gen_stream_ics_pert_Chen25(pot_base=None, pot_pert=None, ts=None, prog_w0=None, Msat=None, key=None, solver=None,
+                               rtol=1e-7, atol=1e-7, dtmin=0.3, dtmax=None, max_steps=10_000, *, dt=None,
+                               normals=None):
+    """Chen+25 release in the smooth potential from a progenitor orbit
+    integrated in base + perturbation (streamhelpers.py:462-489)."""
+    from .main import Solution
+    ts_h = host64(ts).reshape(-1)
+    total = _pot.Potential_Combine([pot_base, pot_pert], units=pot_base.units)
+    ws, _, _ = total._prog_orbit(ts_h, prog_w0, dt, dtmin, dtmax)
+    if normals is None:
+        normals = release_normals(int(np.asarray(key).ravel()[-1]), len(ts_h), 1, 6)
+    ics, _ = pot_base._release(ws, ts_h, Msat, normals, model=_abi.SS_RELEASE_CHEN25,
+                               chen=(CHEN25_MEAN, chen25_factor()))
+    return list(_split_ics(ics, 1)), Solution(torch.as_tensor(ts_h, device=ws.device), ws)
+
+
+def gen_stream_vmapped_with_pert_Chen25(pot_base=None, pot_pert=None, prog_pot=None, ts=None, prog_w0=None, Msat=None,
+                                        key=None, solver=None, max_steps=10_000, rtol=1e-7, atol=1e-7, dtmin=0.1, *,
+                                        dt=None, precision="f64", normals=None, n_particles_per_release=2,
+                                        snapshot_every=None):
+    """Chen+25 perturbed stream: progenitor orbit in base + perturbation,
+    particles in base + perturbation + the progenitor's potential moving on
+    that orbit (streamhelpers.py:546-598)."""
+    if prog_pot is None:
+        prog_pot = _pot.PlummerPotential(m=0.0, r_s=1.0, units=pot_base.units)
+    seed = None if key is None else int(np.asarray(key).ravel()[-1])
+    return gen_stream(pot_base, ts, prog_w0, Msat, seed, solver=solver, dt=dt, release="chen25", prog_pot=prog_pot,
+                      pot_pert=pot_pert, prog_in_pert=True, precision=precision, normals=normals,
+                      n_particles_per_release=n_particles_per_release, snapshot_every=snapshot_every)
+
+
+def gen_stream_vmapped_with_pert_Chen25_fixed_prog(pot_base=None, pot_pert=None, prog_pot=None, ts=None, prog_w0=None,
+                                                   Msat=None, key=None, solver=None, max_steps=10_000, rtol=1e-7,
+                                                   atol=1e-7, dtmin=0.1, *, dt=None, precision="f64", normals=None,
+                                                   n_particles_per_release=2, snapshot_every=None):
+    """Chen+25 perturbed stream with the unperturbed progenitor orbit (its
+    potential still moves on that orbit) (streamhelpers.py:601-653)."""
+    if prog_pot is None:
+        prog_pot = _pot.PlummerPotential(m=0.0, r_s=1.0, units=pot_base.units)
+    seed = None if key is None else int(np.asarray(key).ravel()[-1])
+    return gen_stream(pot_base, ts, prog_w0, Msat, seed, solver=solver, dt=dt, release="chen25", prog_pot=prog_pot,
+                      pot_pert=pot_pert, prog_in_pert=False, precision=precision, normals=normals,
+                      n_particles_per_release=n_particles_per_release, snapshot_every=snapshot_every)
+
+
 __all__ = ["gen_stream", "eval_dense_stream", "eval_dense_stream_id", "gen_stream_ics_pert",
            "gen_stream_vmapped_with_pert", "gen_stream_vmapped_with_pert_fixed_prog", "gen_stream_scan_with_pert",
            "custom_release_model", "computed_binned_track", "release_model_Chen25", "gen_stream_ics_Chen25",
-           "gen_stream_vmapped_Chen25", "chen25_factor", "CHEN25_MEAN", "CHEN25_COV"]
+           "gen_stream_vmapped_Chen25", "gen_stream_ics_pert_Chen25", "gen_stream_vmapped_with_pert_Chen25",
+           "gen_stream_vmapped_with_pert_Chen25_fixed_prog", "chen25_factor", "CHEN25_MEAN", "CHEN25_COV"]

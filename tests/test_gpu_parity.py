@@ -212,6 +212,40 @@ def test_nonlinear_subhalo_stream_parity(ss, oracle):
     assert phase_err(np64(trail), final[:, 1]) <= 1e-10
 
 
+@pytest.mark.parametrize("fixed", [True, False])
+def test_chen25_perturbed_stream_parity(ss, oracle, fixed):
+    """gen_stream_vmapped_with_pert_Chen25[_fixed_prog] (streamhelpers.py:546-653):
+    Chen25 release, Hernquist subhalos on lines, moving Plummer progenitor;
+    the progenitor orbit in base + perturbation unless fixed."""
+    from streamsculptor_gb300 import potential as P
+    from streamsculptor_gb300 import streamhelpers as H
+    n_rel, dt = 300, 1.0
+    orc_base = oracle.HostModel(oracle.mw3())
+    back = oracle.orbit(orc_base, PROG_WF, 0.0, -dt, n_rel, n_rel)[0, -1]
+    ts = -n_rel * dt + np.arange(n_rel + 1) * dt
+    rng = np.random.default_rng(12)
+    sh = dict(m=np.array([4e7, 2e6]), a=np.array([0.6, 0.3]), x0=rng.normal(0, 8, (2, 3)),
+              v=rng.normal(0, 0.15, (2, 3)), t0=np.array([-200.0, -80.0]), t_window=150.0)
+    pert = P.SubhaloLinePotential_Custom(P.HernquistPotential(m=sh["m"], r_s=sh["a"], units=ss.usys), sh["x0"],
+                                         sh["v"], sh["t0"], sh["t_window"], units=ss.usys)
+    normals = rng.standard_normal((n_rel + 1, 1, 6))
+    prog = P.PlummerPotential(m=2e4, r_s=0.01, units=ss.usys)
+    fn = H.gen_stream_vmapped_with_pert_Chen25_fixed_prog if fixed else H.gen_stream_vmapped_with_pert_Chen25
+    lead, trail = fn(pot_base=mw3_gpu(ss), pot_pert=pert, prog_pot=prog, ts=ts, prog_w0=back, Msat=2e4,
+                     normals=normals)
+    orc_total = oracle.HostModel(oracle.mw3(), subhalos=dict(sh, kind=2))
+    ws = oracle.orbit(orc_base if fixed else orc_total, back, ts[0], dt, n_rel, 1)[0]
+    from streamsculptor_gb300.streamhelpers import CHEN25_MEAN, chen25_factor
+    ics, _ = oracle.release(orc_base, ws, ts, 2e4, normals, model_kind=1, chen=(CHEN25_MEAN, chen25_factor()))
+    integ = oracle.HostModel(oracle.mw3() + [(_abi.SS_PLUMMER, 1, (2e4, 0.01))], track=(ts[0], dt, ws[:, :3]),
+                             subhalos=dict(sh, kind=2))
+    final, _, st = oracle.stream(integ, ts[0], dt, n_rel, ics[:-1].reshape(-1, 6), 2, 1)
+    final = final.reshape(n_rel, 2, 6)
+    assert (st == 0).all()
+    assert phase_err(np64(lead), final[:, 0]) <= 1e-10
+    assert phase_err(np64(trail), final[:, 1]) <= 1e-10
+
+
 def _pert_case(oracle, N=24, nsh=7, n_steps=120, seed=4):
     rng = np.random.default_rng(seed)
     sh = dict(kind=1, m=10 ** rng.uniform(5, 8, nsh), a=rng.uniform(0.1, 1.0, nsh), x0=rng.normal(0, 10, (nsh, 3)),
