@@ -322,18 +322,15 @@ def gpu_arm(args, wl):
 
     # --- e2e through the public API with host buffers
     n_snap = n_steps // snap if snap else 0
-    pin_snaps = torch.empty((n_snap, n_rel, ppr // 2, 2, 6), dtype=torch.float32, pin_memory=True) if snap else None
-    pin_final = torch.empty((2, n_rel, ppr // 2, 6), dtype=torch.float64, pin_memory=True)
 
     def e2e_step():
+        # public API with host inputs and host outputs: gen_stream(out="host")
+        # integrates in particle sub-ranges and copies each one to pinned host
+        # memory while the next integrates
         sol = pot.integrate_orbit(w0=WF, ts=np.array([0.0, -T]), t0=0.0, t1=-T, dt=dt)
         out = gen_stream(pot, ts, sol.ys[-1], MSAT, normals=normals_h, dt=dt, prog_pot=prog,
-                         n_particles_per_release=ppr, precision="f32k", snapshot_every=snap or None)
-        lead, trail = out[0], out[1]
-        pin_final[0].copy_(lead.reshape(n_rel, ppr // 2, 6), non_blocking=True)
-        pin_final[1].copy_(trail.reshape(n_rel, ppr // 2, 6), non_blocking=True)
-        if snap:
-            pin_snaps.copy_(out[2], non_blocking=True)
+                         n_particles_per_release=ppr, precision="f32k", snapshot_every=snap or None, out="host")
+        assert not out[0].is_cuda
         torch.cuda.synchronize()
 
     for _ in range(2):
@@ -354,7 +351,7 @@ def gpu_arm(args, wl):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     h2d = normals_h.nbytes + ts.nbytes + WF.nbytes + 2 * 8
-    d2h = pin_final.numel() * 8 + (pin_snaps.numel() * 4 if snap else 0)
+    d2h = n_rel * ppr * 6 * 8 + (n_snap * n_rel * ppr * 6 * 4 if snap else 0)  # final states + snapshots
 
     # --- roofline of the dominant kernel (stream_f32k_kernel)
     flat = P.Potential_Combine([pot] + ([P.TimeDepTranslatingPotential(prog, _core.CenterTrack(0.0, 1.0, wf_d.reshape(2, 3)))]
@@ -397,8 +394,8 @@ def gpu_arm(args, wl):
               "cpu_baseline": cpu,
               "e2e": {"value": world * work / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                       "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
-                      "path": "integrate_orbit + streamhelpers.gen_stream with host numpy inputs; results "
-                              "copied to pinned host memory"},
+                      "path": "integrate_orbit + streamhelpers.gen_stream(out='host') with host numpy inputs: "
+                              "particle sub-ranges copied to pinned host memory while the next integrates"},
               "clocks": clk, "gpu_launches": r32["launches"],
               "gpu_launches_per_step": r32["launches"] / args.steps})
     if world > 1:
@@ -557,7 +554,7 @@ def c4_arm(args):
     lib = _abi.load()
     u = ss.usys
     pot = P.seeded_triaxial_expansion(units=u)
-    n_rel, ppr, dt = C4["n_rel"], C4["ppr"], C4["dt"]
+    n_rel, ppr, dt = args.c4_releases, C4["ppr"], C4["dt"]
     T = n_rel * dt
     ts = -T + np.arange(n_rel + 1) * dt
     work = particle_steps(n_rel, ppr, 1)
@@ -622,6 +619,36 @@ def c4_arm(args):
     ex = torch.linalg.norm(a[:, :3] - b[:, :3], dim=1) / torch.linalg.norm(b[:, :3], dim=1)
     ev = torch.linalg.norm(a[:, 3:] - b[:, 3:], dim=1) / torch.linalg.norm(b[:, 3:], dim=1)
     e = torch.maximum(ex, ev)
+    # FP64 exact expansion on a 600-release sub-workload (600 steps): its rate,
+    # and the surrogate's and the FP32 path's final-state errors against it
+    n_s = min(600, n_rel)
+    T_s = n_s * dt
+    back_s = pot.integrate_orbit(w0=WF, ts=np.array([0.0, -T_s]), t0=0.0, t1=-T_s, dt=dt).ys[-1]
+    ts_s = -T_s + np.arange(n_s + 1) * dt
+    nrm_s = normals_d[:n_s + 1].contiguous()
+
+    def sub(precision):
+        return gen_stream(pot, ts_s, back_s, MSAT, normals=nrm_s, dt=dt, n_particles_per_release=ppr,
+                          precision=precision, force_surrogate=sur if precision == "mlp" else None)
+
+    sub("f64")
+    kev64 = []
+    _core.STREAM_EVENTS = kev64
+    r64 = sub("f64")
+    torch.cuda.synchronize()
+    _core.STREAM_EVENTS = None
+    k64_ms = kev64[0][0].elapsed_time(kev64[0][1])
+    work_s = particle_steps(n_s, ppr, 1)
+    b64 = torch.stack([r64[0], r64[1]]).reshape(-1, 6)
+
+    def err_vs(o):
+        q = torch.stack([o[0], o[1]]).reshape(-1, 6)
+        ex_ = torch.linalg.norm(q[:, :3] - b64[:, :3], dim=1) / torch.linalg.norm(b64[:, :3], dim=1)
+        ev_ = torch.linalg.norm(q[:, 3:] - b64[:, 3:], dim=1) / torch.linalg.norm(b64[:, 3:], dim=1)
+        e_ = torch.maximum(ex_, ev_)
+        return {"median": float(e_.median()), "p99": float(torch.quantile(e_.float(), 0.99)), "max": float(e_.max())}
+
+    sub_errs = {"f32k": err_vs(sub("f32k")), "mlp": err_vs(sub("mlp"))}
     # e2e: host normals in, final states to pinned host memory
     pin = torch.empty((2, n_rel, ppr // 2, 6), dtype=torch.float64, pin_memory=True)
     torch.cuda.synchronize()
@@ -639,11 +666,17 @@ def c4_arm(args):
           "scaling": "weak", "vs_baseline": None, "dtype": "bf16 tensor-core force (FP32 accumulation), f32 "
           "compensated state, f64 progenitor and release",
           "data": "synthetic (seeded expansion, PCG64 draws; training points along orbits of the exact expansion)",
-          "config": {"workload": C4["name"], "particles": n_rel * ppr, "n_steps": n_rel, "particle_steps_per_step":
+          "config": {"workload": C4["name"] if n_rel == C4["n_rel"] else
+                     f"profiling case shaped like the surrogate workload: {n_rel} releases x {ppr} particles",
+                     "particles": n_rel * ppr, "n_steps": n_rel, "particle_steps_per_step":
                      work, "l2": "512 MB buffer zeroed between timed steps"},
           "exact_expansion_f32k": {"value": work / (rx["ms_per_step"] * 1e-3), "ms_per_step": rx["ms_per_step"],
                                    "kernel_ms": rx["kernel_ms"]},
           "speedup_vs_exact_expansion": rx["ms_per_step"] / rm["ms_per_step"],
+          "exact_expansion_f64": {"value": work_s / (k64_ms * 1e-3), "kernel_ms": k64_ms,
+                                  "sample": f"{n_s} releases x {ppr} particles, {n_s} steps ({work_s} particle-steps)",
+                                  "note": "stream kernel time only"},
+          "error_vs_exact_f64_sample": sub_errs,
           "surrogate": {"train_points": int(args.c4_points), "train_steps": args.c4_train_steps, "batch": 8192,
                         "sample_s": t1 - t0, "train_s": t2 - t1, "loss_history": sur.history,
                         "force_rel_err_fp32": {"median": float(e32.median()), "p99": float(torch.quantile(e32.float(), 0.99))},
@@ -690,6 +723,7 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["c3", "c3s", "c4", "c5"], default="c2")
     ap.add_argument("--c4-points", type=int, default=1 << 22, help="surrogate training points (c4)")
     ap.add_argument("--c4-train-steps", type=int, default=6000, help="surrogate Adam steps (c4)")
+    ap.add_argument("--c4-releases", type=int, default=C4["n_rel"], help="release times (c4; smaller for profiling)")
     ap.add_argument("--f64-steps", type=int, default=2)
     ap.add_argument("--f64-warmup", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")

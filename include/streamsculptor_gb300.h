@@ -151,6 +151,13 @@ typedef struct ss_stream_cfg {
     int32_t steps_per_release;
     int32_t snap_stride;       /* 0 = final state only; else snapshot after every snap_stride global steps */
     int32_t reserved;
+    /* Sub-range runs: the n_particles given are particles first_particle ..
+     * first_particle + n_particles - 1 of a larger stream (their release
+     * steps follow from those global indices); ics/final_w/status are indexed
+     * from first_particle, snapshots are rows of snap_pitch particles
+     * (0 = n_particles) written at the global index.  Zero for whole runs. */
+    int64_t first_particle;
+    int64_t snap_pitch;
 } ss_stream_cfg;
 
 typedef enum ss_release_model { SS_RELEASE_FARDAL = 0, SS_RELEASE_CHEN25 = 1 } ss_release_model;
@@ -360,6 +367,14 @@ int ss_binned_sums(const double* values, const double* key, int64_t n, int32_t n
  * *out_flops = flops the launch executes; sink: device buffer of >= 512
  * floats (never written in practice). */
 int ss_peak_fma(int precision, int64_t iters, double* out_flops, float* sink, void* stream);
+
+/* Strided copy of `rows` rows of `width_bytes` starting `offset_bytes`
+ * into each row of pitch `pitch_bytes` (cudaMemcpy2DAsync, same offset and
+ * pitch on both sides): moves a particle sub-range of snapshots
+ * [n_snap, N, 6] between device and pinned host memory on `stream`.
+ * kind: 0 device -> host, 1 host -> device, 2 device -> device. */
+int ss_copy_rows_async(void* dst, const void* src, int64_t rows, int64_t pitch_bytes, int64_t offset_bytes,
+                       int64_t width_bytes, int kind, void* stream);
 
 /* ---------------------------------------------------- MLP force surrogate
  * A learned potential for expensive expansion potentials:

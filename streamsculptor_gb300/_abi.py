@@ -70,7 +70,8 @@ class ss_potential(C.Structure):
 class ss_stream_cfg(C.Structure):
     _fields_ = [("t0", C.c_double), ("dt", C.c_double), ("n_steps", C.c_int64),
                 ("n_particles", C.c_int64), ("particles_per_release", C.c_int32),
-                ("steps_per_release", C.c_int32), ("snap_stride", C.c_int32), ("reserved", C.c_int32)]
+                ("steps_per_release", C.c_int32), ("snap_stride", C.c_int32), ("reserved", C.c_int32),
+                ("first_particle", C.c_int64), ("snap_pitch", C.c_int64)]
 
 
 class ss_release_cfg(C.Structure):
@@ -131,6 +132,7 @@ SIGNATURES = {
                                        VP, C.c_int64, VP]),
     "ss_binned_sums": (C.c_int, [VP, VP, C.c_int64, C.c_int32, VP, C.c_int32, VP, VP, VP]),
     "ss_peak_fma": (C.c_int, [C.c_int, C.c_int64, DP, VP, VP]),
+    "ss_copy_rows_async": (C.c_int, [VP, VP, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int, VP]),
     "ss_mlp_eval_workspace_bytes": (C.c_int64, [C.c_int64]),
     "ss_mlp_eval": (C.c_int, [C.POINTER(ss_mlp), VP, C.c_int64, VP, VP, VP, C.c_int64, VP]),
     "ss_mlp_train_workspace_bytes": (C.c_int64, [C.c_int64]),

@@ -373,6 +373,83 @@ def stream(P, cfg, ics: torch.Tensor, precision: str, want_final=True, snaps=Non
     return final, st
 
 
+_AUX_STREAMS = {}
+
+
+def _aux_stream(dev: torch.device, name: str) -> torch.cuda.Stream:
+    key = (dev.type, dev.index, name)
+    if key not in _AUX_STREAMS:
+        _AUX_STREAMS[key] = torch.cuda.Stream(device=dev)
+    return _AUX_STREAMS[key]
+
+
+def stream_to_host(P, cfg, ics: torch.Tensor, precision: str, snap_every: int = 0, mlp=None, n_chunks: int = 4):
+    """The stream in particle sub-ranges whose results are copied to pinned
+    host memory while later sub-ranges integrate: sub-range kernels alternate
+    between two CUDA streams (so one's last wave overlaps the next one's
+    first), each followed by its copies on a third stream (snapshots move as
+    strided row blocks with ss_copy_rows_async).  Returns pinned host (final
+    [N,6] float64, snapshots [n_snap,N,6] float32 or None) and the device
+    status [N]; the host buffers are complete once the current stream is
+    synchronised."""
+    import copy as _cp
+    N = int(cfg.n_particles)
+    dev = ics.device
+    n_snap = int(cfg.n_steps) // snap_every if snap_every else 0
+    final_d = torch.empty(N, 6, dtype=torch.float64, device=dev)
+    status_d = torch.empty(N, dtype=torch.int32, device=dev)
+    snaps_d = torch.empty(n_snap, N, 6, dtype=torch.float32, device=dev) if n_snap else None
+    final_h = torch.empty(N, 6, dtype=torch.float64, pin_memory=True)
+    snaps_h = torch.empty(n_snap, N, 6, dtype=torch.float32, pin_memory=True) if n_snap else None
+    main = torch.cuda.current_stream(dev)
+    comp = [_aux_stream(dev, "compute0"), _aux_stream(dev, "compute1")]
+    side = _aux_stream(dev, "copy")
+    for st in comp + [side]:
+        st.wait_stream(main)  # inputs and buffers are ready on the main stream
+    lib = _abi.load()
+    per = max(128, -(-N // max(1, n_chunks) // 128) * 128)
+    for c_idx, p0 in enumerate(range(0, N, per)):
+        p1 = min(N, p0 + per)
+        c = _cp.copy(cfg)
+        c.first_particle, c.n_particles = p0, p1 - p0
+        c.snap_pitch = N if n_snap else 0
+        c.snap_stride = snap_every if n_snap else 0
+        sub_ics, fin, stt = ics[p0:p1], final_d[p0:p1], status_d[p0:p1]
+        cs = comp[c_idx % 2]
+        h = C.c_void_p(cs.cuda_stream)
+        if precision == "f64":
+            _abi.call("ss_stream_f64", C.byref(P), C.byref(c), ptr(sub_ics), ptr(fin), ptr(snaps_d), ptr(stt), h)
+        elif precision == "f32k":
+            need = lib.ss_stream_workspace_bytes(C.byref(P), C.byref(c))
+            if need < 0:
+                raise _abi.SSError("ss_stream_workspace_bytes", need, lib.ss_last_error().decode())
+            ws, nb = aligned_ptr(Workspace.get(need, dev, slot=f"compute{c_idx % 2}"))
+            _abi.call("ss_stream_f32k", C.byref(P), C.byref(c), ptr(sub_ics), ptr(fin), ptr(snaps_d), ptr(stt), ws,
+                      nb, h)
+        elif precision == "mlp":
+            m = mlp.struct()
+            _abi.call("ss_stream_mlp_bf16", C.byref(m), C.byref(c), ptr(sub_ics), ptr(fin), ptr(snaps_d), ptr(stt),
+                      None, 0, h)
+        else:
+            raise ValueError("precision must be 'f64', 'f32k' or 'mlp'")
+        ev = torch.cuda.Event()
+        ev.record(cs)
+        side.wait_event(ev)
+        hs = C.c_void_p(side.cuda_stream)
+        _abi.call("ss_copy_rows_async", C.c_void_p(final_h.data_ptr()), ptr(final_d), 1, N * 48, p0 * 48,
+                  (p1 - p0) * 48, 0, hs)
+        if n_snap:
+            _abi.call("ss_copy_rows_async", C.c_void_p(snaps_h.data_ptr()), ptr(snaps_d), n_snap, N * 24, p0 * 24,
+                      (p1 - p0) * 24, 0, hs)
+    for st in comp + [side]:
+        main.wait_stream(st)
+    for t in (final_d, status_d, snaps_d, ics):
+        if t is not None:
+            for st in comp + [side]:
+                t.record_stream(st)
+    return final_h, snaps_h, status_d
+
+
 def subhalo_eval(table: SubhaloTable, G: float, xyz: torch.Tensor, t: float):
     n, ns = xyz.shape[0], int(table.m.shape[0])
     dev = xyz.device

@@ -362,6 +362,20 @@ int64_t ss_kernel_launches(void) { return (int64_t)g_launches.load(std::memory_o
 
 const char* ss_last_error(void) { return ssg::last_error(); }
 
+int ss_copy_rows_async(void* dst, const void* src, int64_t rows, int64_t pitch_bytes, int64_t offset_bytes,
+                       int64_t width_bytes, int kind, void* stream) {
+    SS_CHECK_ARG(dst != nullptr && src != nullptr, "NULL buffer");
+    SS_CHECK_ARG(rows >= 0 && width_bytes >= 0 && offset_bytes >= 0 && offset_bytes + width_bytes <= pitch_bytes,
+                 "bad rows/pitch/offset/width");
+    SS_CHECK_ARG(kind >= 0 && kind <= 2, "kind must be 0 (D2H), 1 (H2D) or 2 (D2D)");
+    if (rows == 0 || width_bytes == 0) return SS_OK;
+    const cudaMemcpyKind k = kind == 0 ? cudaMemcpyDeviceToHost : kind == 1 ? cudaMemcpyHostToDevice
+                                                                             : cudaMemcpyDeviceToDevice;
+    SS_CUDA_TRY(cudaMemcpy2DAsync((char*)dst + offset_bytes, (size_t)pitch_bytes, (const char*)src + offset_bytes,
+                                  (size_t)pitch_bytes, (size_t)width_bytes, (size_t)rows, k, (cudaStream_t)stream));
+    return SS_OK;
+}
+
 int64_t ss_abi_sizeof(int which) {
     switch (which) {
         case 0: return (int64_t)sizeof(ss_potential);

@@ -499,7 +499,7 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) stream_mlp_kernel(const __grid
     for (int64_t tile = 2 * (int64_t)blockIdx.x + wg; tile < ka.n_tiles; tile += 2 * (int64_t)gridDim.x) {
         const int64_t p = tile * 128 + t;
         const bool valid = p < a.N;
-        const int start = valid ? (int)((p / a.ppr) * (int64_t)a.spr) : a.n_steps;
+        const int start = valid ? (int)(((p + a.p_off) / a.ppr) * (int64_t)a.spr) : a.n_steps;
         // the tile steps from its earliest start; particles not yet released
         // step a copy (their rows of the GEMMs are independent)
         if (t == 0) *s_start = a.n_steps;
@@ -521,7 +521,7 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) stream_mlp_kernel(const __grid
         if (a.snaps && valid) {
             const float y[6] = {xh[0], xh[1], xh[2], vh[0], vh[1], vh[2]};
             for (int64_t k = 0; (k + 1) * (int64_t)a.stride <= tstart; ++k)
-                write_snap<float>(a.snaps, a.N, k, p, (k + 1) * (int64_t)a.stride >= start, y);
+                write_snap<float>(a.snaps, a.snap_pitch, k, p + a.p_off, (k + 1) * (int64_t)a.stride >= start, y);
         }
         for (int n = tstart; n < a.n_steps; ++n) {
             if (*abort) break;
@@ -545,7 +545,7 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) stream_mlp_kernel(const __grid
             }
             if (a.snaps && (n + 1) % a.stride == 0 && valid) {
                 const float y[6] = {xh[0], xh[1], xh[2], vh[0], vh[1], vh[2]};
-                write_snap<float>(a.snaps, a.N, (n + 1) / a.stride - 1, p, n + 1 >= start, y);
+                write_snap<float>(a.snaps, a.snap_pitch, (n + 1) / a.stride - 1, p + a.p_off, n + 1 >= start, y);
             }
         }
         if (valid) {
@@ -617,7 +617,11 @@ int ss_stream_mlp_bf16(const ss_mlp* mlp, const ss_stream_cfg* cfg, const double
     SS_CHECK_ARG(cfg->particles_per_release >= 1 && cfg->steps_per_release >= 0, "bad release layout");
     SS_CHECK_ARG(std::isfinite(cfg->dt) && cfg->dt > 0.0 && std::isfinite(cfg->t0), "dt must be finite and > 0");
     SS_CHECK_ARG(cfg->snap_stride >= 0, "snap_stride < 0");
-    const int64_t n_rel = (cfg->n_particles + cfg->particles_per_release - 1) / cfg->particles_per_release;
+    SS_CHECK_ARG(cfg->first_particle >= 0 && cfg->snap_pitch >= 0, "first_particle and snap_pitch must be >= 0");
+    SS_CHECK_ARG(cfg->snap_pitch == 0 || cfg->snap_pitch >= cfg->first_particle + cfg->n_particles,
+                 "snap_pitch must cover first_particle + n_particles");
+    const int64_t n_rel =
+        (cfg->first_particle + cfg->n_particles + cfg->particles_per_release - 1) / cfg->particles_per_release;
     SS_CHECK_ARG(n_rel == 0 || (n_rel - 1) * (int64_t)cfg->steps_per_release <= cfg->n_steps,
                  "last release starts after n_steps");
     if (cfg->n_particles == 0) return SS_OK;
@@ -639,6 +643,8 @@ int ss_stream_mlp_bf16(const ss_mlp* mlp, const ss_stream_cfg* cfg, const double
     a.dt = cfg->dt;
     a.h_hi = (float)cfg->dt;
     a.h_lo = (float)(cfg->dt - (double)a.h_hi);
+    a.p_off = cfg->first_particle;
+    a.snap_pitch = cfg->snap_pitch > 0 ? cfg->snap_pitch : cfg->n_particles;
     ka.n_tiles = (cfg->n_particles + 127) / 128;
     int dev = 0, sms = 0;
     SS_CUDA_TRY(cudaGetDevice(&dev));

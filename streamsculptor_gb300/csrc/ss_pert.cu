@@ -121,9 +121,29 @@ __global__ void __launch_bounds__(64) pert_base_kernel(PotDev<double> P, PertArg
 
 // ------------------------------------------------------------- phase 2
 // derivative of one ncol-state at a stage: K = (v1, a1 + T x1 [, v1r, a1r + T x1r])
+// one stage record (x0[3], T[6]) from the 16-byte aligned shared-memory copy
+__device__ __forceinline__ void load_stage(const float* p, float r[9]) {
+    const float4 a = *reinterpret_cast<const float4*>(p);
+    const float4 b = *reinterpret_cast<const float4*>(p + 4);
+    r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
+    r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
+    r[8] = p[8];
+}
+__device__ __forceinline__ void load_stage(const double* p, double r[9]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const double2 v = *reinterpret_cast<const double2*>(p + 2 * i);
+        r[2 * i] = v.x;
+        r[2 * i + 1] = v.y;
+    }
+    r[8] = p[8];
+}
+
 template <class R, int NCOL>
-__device__ __forceinline__ void pert_rhs(const R* rec, const R U[NCOL], int kind, R Gm, R a, const R P0[3], const R V[3],
-                                         R trel, R tau0, R window, R K[NCOL]) {
+__device__ __forceinline__ void pert_rhs(const R* recp, const R U[NCOL], int kind, R Gm, R a, const R P0[3],
+                                         const R V[3], R trel, R tau0, R window, R K[NCOL]) {
+    R rec[9];
+    load_stage(recp, rec);
     R rel[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) rel[i] = rec[i] - (P0[i] + V[i] * trel);
@@ -146,12 +166,22 @@ __device__ __forceinline__ void pert_rhs(const R* rec, const R U[NCOL], int kind
     }
 }
 
+// The block's threads share one particle, so its base-track records are
+// staged in shared memory PERT_STEPS_STAGED steps at a time (coalesced global loads,
+// stage records padded to 12 values for vector loads); threads past the last
+// subhalo run on subhalo 0 and discard their result so that every thread
+// reaches the block barriers.
+static constexpr int PERT_STEPS_STAGED = 16;
+
 template <class R, int NCOL>
 __global__ void __launch_bounds__(128) pert_response_kernel(ShDev sh, PertArgs a, int sblocks) {
+    __shared__ __align__(16) R srec[PERT_STEPS_STAGED][6][12];
     const int64_t i = blockIdx.x / sblocks;          // particle within the chunk
     const int sb = blockIdx.x - (int)(i * sblocks);
-    const int s = sb * blockDim.x + threadIdx.x;     // subhalo
-    if (i >= a.np || s >= sh.n) return;
+    const int s_raw = sb * blockDim.x + threadIdx.x;  // subhalo
+    if (i >= a.np) return;                           // whole block
+    const bool active = s_raw < sh.n;
+    const int s = active ? s_raw : 0;
     const int64_t p = a.p0 + i;
     const int start = (int)pert_start(p, a.ppr, a.spr);
     const R* rec = reinterpret_cast<const R*>(a.table) +
@@ -173,6 +203,7 @@ __global__ void __launch_bounds__(128) pert_response_kernel(ShDev sh, PertArgs a
     for (int c = 0; c < NCOL; ++c) u[c] = ic ? ic[(p * nsh + s) * NCOL + c] : R(0);
     R* out = reinterpret_cast<R*>(a.pert_out);
     auto save = [&](int slot) {
+        if (!active) return;
         R* o = out + (((int64_t)slot * a.N + p) * nsh + s) * NCOL;
 #pragma unroll
         for (int c = 0; c < NCOL; ++c) o[c] = u[c];
@@ -182,7 +213,16 @@ __global__ void __launch_bounds__(128) pert_response_kernel(ShDev sh, PertArgs a
     }
     const R h = (R)a.dt;
     const R cs[6] = {R(0), R(SS_C2), R(SS_C3), R(SS_C4), R(SS_C5), R(1)};
-    for (int n = start; n < a.n_steps; ++n, rec += REC) {
+    for (int n0 = start; n0 < a.n_steps; n0 += PERT_STEPS_STAGED, rec += PERT_STEPS_STAGED * REC) {
+      const int cnt = min(PERT_STEPS_STAGED, a.n_steps - n0);
+      __syncthreads();  // the previous chunk has been consumed
+      for (int e = threadIdx.x; e < cnt * 54; e += blockDim.x) {
+          const int j = e / 54, r = e - 54 * j, st = r / 9, q = r - 9 * st;
+          srec[j][st][q] = rec[(int64_t)j * REC + r];
+      }
+      __syncthreads();
+      for (int j = 0; j < cnt; ++j) {
+        const int n = n0 + j;
         const R tn = (R)n * h;
         R k[6][NCOL];
         R U[NCOL];
@@ -200,13 +240,14 @@ __global__ void __launch_bounds__(128) pert_response_kernel(ShDev sh, PertArgs a
                           R(SS_A65) * k[4][c];
                 U[c] = st == 0 ? u[c] : u[c] + h * acc;
             }
-            pert_rhs<R, NCOL>(rec + 9 * st, U, sh.kind, Gm, am, P0, V, tn + cs[st] * h, tau0, window, k[st]);
+            pert_rhs<R, NCOL>(&srec[j][st][0], U, sh.kind, Gm, am, P0, V, tn + cs[st] * h, tau0, window, k[st]);
         }
 #pragma unroll
         for (int c = 0; c < NCOL; ++c)
             u[c] = u[c] + h * (R(SS_B1) * k[0][c] + R(SS_B3) * k[2][c] + R(SS_B4) * k[3][c] + R(SS_B5) * k[4][c] +
                                R(SS_B6) * k[5][c]);
         if (a.save_stride > 0 && (n + 1) % a.save_stride == 0) save((n + 1) / a.save_stride);
+      }
     }
     if (a.save_stride == 0) save(0);
 }

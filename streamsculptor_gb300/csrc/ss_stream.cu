@@ -72,7 +72,11 @@ static int check_stream_cfg(const ss_stream_cfg* cfg) {
     SS_CHECK_ARG(cfg->particles_per_release >= 1 && cfg->steps_per_release >= 0, "bad release layout");
     SS_CHECK_ARG(std::isfinite(cfg->dt) && cfg->dt > 0.0 && std::isfinite(cfg->t0), "dt must be finite and > 0");
     SS_CHECK_ARG(cfg->snap_stride >= 0, "snap_stride < 0");
-    int64_t n_rel = (cfg->n_particles + cfg->particles_per_release - 1) / cfg->particles_per_release;
+    SS_CHECK_ARG(cfg->first_particle >= 0 && cfg->snap_pitch >= 0, "first_particle and snap_pitch must be >= 0");
+    SS_CHECK_ARG(cfg->snap_pitch == 0 || cfg->snap_pitch >= cfg->first_particle + cfg->n_particles,
+                 "snap_pitch must cover first_particle + n_particles");
+    int64_t n_rel =
+        (cfg->first_particle + cfg->n_particles + cfg->particles_per_release - 1) / cfg->particles_per_release;
     SS_CHECK_ARG(n_rel == 0 || (n_rel - 1) * (int64_t)cfg->steps_per_release <= cfg->n_steps,
                  "last release starts after n_steps");
     return SS_OK;
@@ -95,6 +99,8 @@ static StreamArgs make_args(const ss_stream_cfg* cfg, const double* ics, double*
     a.dt = cfg->dt;
     a.h_hi = (float)cfg->dt;
     a.h_lo = (float)(cfg->dt - (double)a.h_hi);
+    a.p_off = cfg->first_particle;
+    a.snap_pitch = cfg->snap_pitch > 0 ? cfg->snap_pitch : cfg->n_particles;
     return a;
 }
 

@@ -33,6 +33,9 @@ struct StreamArgs {
     // steps: [n_seg, N, 3] float4 = (xh, vh.x), (vh.yz, xl.xy), (xl.z, vl)
     float4* ckpt;
     int32_t ckpt_stride;
+    // sub-range runs: global index of local particle 0, snapshot row pitch
+    int64_t p_off;
+    int64_t snap_pitch;
 };
 
 // Write the snapshot k for lane state y (or NaN when not yet released).
@@ -56,7 +59,7 @@ template <class C>
 __global__ void __launch_bounds__(64) stream_f64_kernel(PotDev<double> P, StreamArgs a) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p < a.N;
-    const int start = valid ? (int)((p / a.ppr) * (int64_t)a.spr) : a.n_steps;
+    const int start = valid ? (int)(((p + a.p_off) / a.ppr) * (int64_t)a.spr) : a.n_steps;
     const int wstart = (int)__reduce_min_sync(0xffffffffu, (unsigned)start);
     double y[6];
     if (valid) {
@@ -69,13 +72,13 @@ __global__ void __launch_bounds__(64) stream_f64_kernel(PotDev<double> P, Stream
     if (a.snaps && valid) {
         for (int64_t k = 0; (k + 1) * (int64_t)a.stride <= wstart; ++k) {
             int64_t step = (k + 1) * (int64_t)a.stride;
-            write_snap<double>(a.snaps, a.N, k, p, step >= start, y);
+            write_snap<double>(a.snaps, a.snap_pitch, k, p + a.p_off, step >= start, y);
         }
     }
     for (int n = wstart; n < a.n_steps; ++n) {
         if (valid && n >= start) dopri5_step_f64<C>(P, a.t0 + (double)n * a.dt, a.dt, y);
         if (a.snaps && (n + 1) % a.stride == 0 && valid)
-            write_snap<double>(a.snaps, a.N, (n + 1) / a.stride - 1, p, n + 1 >= start, y);
+            write_snap<double>(a.snaps, a.snap_pitch, (n + 1) / a.stride - 1, p + a.p_off, n + 1 >= start, y);
     }
     if (!valid) return;
     bool ok = true;
@@ -217,7 +220,7 @@ template <class C>
 __global__ void __launch_bounds__(128) stream_f32k_kernel(PotDev<float> P, StreamArgs a) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p < a.N;
-    const int start = valid ? (int)((p / a.ppr) * (int64_t)a.spr) : a.n_steps;
+    const int start = valid ? (int)(((p + a.p_off) / a.ppr) * (int64_t)a.spr) : a.n_steps;
     const int wstart = (int)__reduce_min_sync(0xffffffffu, (unsigned)start);
     float xh[3], xl[3], vh[3], vl[3];
 #pragma unroll
@@ -233,7 +236,7 @@ __global__ void __launch_bounds__(128) stream_f32k_kernel(PotDev<float> P, Strea
         float y[6] = {xh[0], xh[1], xh[2], vh[0], vh[1], vh[2]};
         for (int64_t k = 0; (k + 1) * (int64_t)a.stride <= wstart; ++k) {
             int64_t step = (k + 1) * (int64_t)a.stride;
-            write_snap<float>(a.snaps, a.N, k, p, step >= start, y);
+            write_snap<float>(a.snaps, a.snap_pitch, k, p + a.p_off, step >= start, y);
         }
     }
     for (int n = wstart; n < a.n_steps; ++n) {
@@ -248,7 +251,7 @@ __global__ void __launch_bounds__(128) stream_f32k_kernel(PotDev<float> P, Strea
         }
         if (a.snaps && (n + 1) % a.stride == 0 && valid) {
             float y[6] = {xh[0], xh[1], xh[2], vh[0], vh[1], vh[2]};
-            write_snap<float>(a.snaps, a.N, (n + 1) / a.stride - 1, p, n + 1 >= start, y);
+            write_snap<float>(a.snaps, a.snap_pitch, (n + 1) / a.stride - 1, p + a.p_off, n + 1 >= start, y);
         }
     }
     if (!valid) return;

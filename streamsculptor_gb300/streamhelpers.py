@@ -40,7 +40,7 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
                kval_arr=1.0, dt=None, dtmax=None, n_particles_per_release=2, normals=None, precision="f64",
                snapshot_every=None, throw=False, release="fardal", prog_pot: Optional[Potential] = None,
                pot_pert: Optional[Potential] = None, prog_in_pert=False, return_ics=False, prog_method="auto",
-               force_surrogate=None):
+               force_surrogate=None, out="device"):
     """Generate a particle-spray stream on the GPU.
 
     pot_base    smooth potential (release model and integration)
@@ -54,6 +54,9 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
     prog_method progenitor orbit solver (FP64 either way): 'serial', 'shoot'
                 (parallel in time, multiple shooting) or 'auto' (shoot when the
                 progenitor's potential is static)
+    out         'device' (CUDA tensors) or 'host': pinned host tensors, the stream
+                run in particle sub-ranges whose results are copied while the
+                next sub-range integrates (ready when the call returns)
     precision   'f64', 'f32k' (FP32 compensated) or 'mlp': the particles move
                 in the force of `force_surrogate` (surrogate.MLPSurrogate, BF16
                 tensor cores) while the progenitor orbit and the release use
@@ -94,14 +97,21 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
     cfg.steps_per_release = spr
     cfg.snap_stride = int(snapshot_every or 0)
     snaps = None
-    if snapshot_every:
-        n_snap = cfg.n_steps // int(snapshot_every)
-        snaps = torch.empty(n_snap, N, 6, dtype=torch.float32, device=ws.device)
     stream_ics = ics[:n_rel].reshape(N, 6).contiguous()
     if precision == "mlp" and (integ is not pot_base or force_surrogate is None):
         raise NotImplementedError("precision='mlp' integrates in the surrogate alone: give force_surrogate and no "
                                   "prog_pot / pot_pert")
-    final, status = _core.stream(integ._desc(), cfg, stream_ics, precision, snaps=snaps, mlp=force_surrogate)
+    if out == "host":
+        final, snaps, status = _core.stream_to_host(integ._desc(), cfg, stream_ics, precision,
+                                                    int(snapshot_every or 0), mlp=force_surrogate)
+        torch.cuda.current_stream().synchronize()
+    elif out == "device":
+        if snapshot_every:
+            n_snap = cfg.n_steps // int(snapshot_every)
+            snaps = torch.empty(n_snap, N, 6, dtype=torch.float32, device=ws.device)
+        final, status = _core.stream(integ._desc(), cfg, stream_ics, precision, snaps=snaps, mlp=force_surrogate)
+    else:
+        raise ValueError("out must be 'device' or 'host'")
     if throw and bool((status != 0).any()):
         raise RuntimeError("gen_stream: non-finite particle state")
     final = final.reshape(n_rel, n_draw, 2, 6)

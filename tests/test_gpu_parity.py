@@ -421,3 +421,21 @@ def test_orbit_parallel_in_time_vs_oracle(ss, oracle):
     w3, _, _ = gpu._prog_orbit(np.arange(0.0, 41.0, 2.0) - 20.0, PROG_WF, 0.5, method="shoot")
     ref3 = oracle.orbit(orc, PROG_WF, -20.0, 0.5, 80, 4)[0]
     assert phase_err(np64(w3), ref3) < 1e-11
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32k"])
+def test_host_output_matches_device(ss, oracle, precision):
+    """gen_stream(out='host') runs the stream in particle sub-ranges
+    (first_particle / snap_pitch) with overlapped copies; every particle's
+    arithmetic is unchanged, so the results equal the one-launch run."""
+    from streamsculptor_gb300.streamhelpers import gen_stream
+    orc_mov, back, ts, normals, ics, prog, c = _moving_prog_case(ss, oracle, n_rel=150, ppr=12)
+    kw = dict(normals=normals, dt=c["dt"], prog_pot=prog, n_particles_per_release=c["ppr"], precision=precision,
+              snapshot_every=20)
+    d = gen_stream(mw3_gpu(ss), ts, back, 2e4, **kw)
+    h = gen_stream(mw3_gpu(ss), ts, back, 2e4, out="host", **kw)
+    assert not h[0].is_cuda and h[0].is_pinned()
+    for a, b in zip(d, h):
+        a, b = a.cpu().numpy(), b.numpy()
+        assert a.shape == b.shape
+        assert np.array_equal(a, b, equal_nan=True)
