@@ -6,14 +6,18 @@
 // the orbit is solved by multiple shooting with Newton's method:
 //   * split the n_steps fixed Dopri5 steps into S slices of M steps;
 //   * guess the slice starts U_n with a cheap FP32 integration (coarse steps);
-//   * iterate: integrate every slice in parallel in FP64 from U_n, together
-//     with its 6x6 Jacobian (six forward-mode tangent lanes per slice),
-//     giving F_n = F(U_n) and J_n; then one serial sweep
-//     U_{n+1} <- F_n + J_n (U_n^new - U_n^old) (6x6 matrix-vector products);
-//   * Newton converges quadratically: after the sweep changes U by less than
-//     `tol` (relative), the starts satisfy U_{n+1} = F(U_n) to round-off;
-//   * a last parallel pass integrates each slice in FP64 from its converged
-//     start and writes the saved states.
+//   * iterate: integrate every slice in parallel in FP64 from U_n (its end
+//     F_n = F(U_n), and the saved states of its steps), and its 6x6 Jacobian
+//     J_n in FP32 (six forward-mode tangent lanes per slice); then the Newton
+//     update of the joins, e_{n+1} = J_n e_n + (F_n - U_{n+1}) with e_0 = 0,
+//     U_{n+1} += e_{n+1}, an affine recurrence solved as a parallel prefix
+//     scan over the slices (composition (A2,b2) o (A1,b1) = (A2 A1, A2 b1 + b2));
+//   * an FP32 Jacobian makes the iteration converge linearly with a factor
+//     ~1e-6 instead of quadratically, which still reaches the FP64 round-off
+//     floor in a few iterations; the iteration stops when the largest relative
+//     update is below `tol` or stops shrinking below 1e-11 (the round-off floor);
+//   * the last slice pass wrote the saved states (its starts differ from the
+//     final ones by less than the last update).
 // The result is the serial fixed-step FP64 Dopri5 orbit (the same step map
 // composed n_steps times) up to round-off in the slice joins.  Static
 // potentials (no center track, no subhalos) only; the entry point falls back
@@ -40,8 +44,8 @@ struct ShootArgs {
     int32_t n_save;
     double* U;        // [S + 1, 6] slice starts
     double* F;        // [S, 6] slice ends
-    double* J;        // [S, 36] dF_i/dU_j at [i * 6 + j]
-    int32_t* flag;    // [0] converged, [1] Newton sweeps done
+    double* J;        // [S, 36] floats dF_i/dU_j at [i * 6 + j] (space for 36 S doubles)
+    int32_t* flag;    // [0] converged, [1] Newton sweeps done, [2] last update (float bits)
     double tol;
     double* out;      // [n_save, 6]
 };
@@ -102,127 +106,208 @@ __global__ void shoot_guess_kernel(PotDev<float> P, ShootArgs a) {
     }
 }
 
-// Every slice from its start, with its Jacobian: lane 6 n + i carries the
-// tangent along U_j = e_i.
+// Every slice from its start in FP64: its end F_n and (when saving) the
+// states of its steps.
 template <class C>
-__global__ void __launch_bounds__(96) shoot_slice_kernel(PotDev<double> P, ShootArgs a) {
+__global__ void __launch_bounds__(64) shoot_f64_kernel(PotDev<double> P, ShootArgs a) {
     if (a.flag[0]) return;
-    const int lane = blockIdx.x * blockDim.x + threadIdx.x;
-    const int n = lane / 6, i = lane % 6;
-    if (n >= a.S) return;
-    typedef D1<double> T;
-    PotDev<T> Q;
-    Q.n = P.n;
-    Q.has_track = 0;
-    Q.ex = P.ex;
-#pragma unroll
-    for (int c = 0; c < C::n; ++c) {
-        Q.c[c].kind = P.c[c].kind;
-        Q.c[c].center = P.c[c].center;
-#pragma unroll
-        for (int j = 0; j < 6; ++j) Q.c[c].q[j] = T(P.c[c].q[j], 0.0);
-    }
-    T y[6];
-#pragma unroll
-    for (int j = 0; j < 6; ++j) y[j] = T(a.U[6 * n + j], j == i ? 1.0 : 0.0);
-    const T h(a.dt, 0.0);
-    const int len = slice_len(a, n);
-    for (int s = 0; s < len; ++s) dopri5_step_dual<C, double>(Q, h, y);
-#pragma unroll
-    for (int j = 0; j < 6; ++j) a.J[36 * n + 6 * j + i] = y[j].d;
-    if (i == 0)
-#pragma unroll
-        for (int j = 0; j < 6; ++j) a.F[6 * n + j] = y[j].v;
-}
-
-// Newton sweep over the slice joins.  The recurrence is serial and its
-// FP64 FMA chain (6 deep per slice) is latency-bound, so the block stages
-// chunks of J, F and U in shared memory with coalesced loads and one thread
-// runs the chain from there; the convergence test compares squares (no
-// division or square root on the serial path).
-static constexpr int SWEEP_CHUNK = 64;
-static constexpr int SWEEP_THREADS = 128;
-
-__global__ void __launch_bounds__(SWEEP_THREADS) shoot_sweep_kernel(ShootArgs a) {
-    if (a.flag[0]) return;
-    __shared__ double sJ[SWEEP_CHUNK * 36];
-    __shared__ double sF[SWEEP_CHUNK * 6];
-    __shared__ double sU[SWEEP_CHUNK * 6];
-    double d[6] = {0, 0, 0, 0, 0, 0};  // U_n^new - U_n^old (zero at n = 0)
-    const double tol2 = a.tol * a.tol;
-    bool ok = true;
-    for (int base = 0; base < a.S; base += SWEEP_CHUNK) {
-        const int cnt = min(SWEEP_CHUNK, a.S - base);
-        __syncthreads();
-        for (int k = threadIdx.x; k < cnt * 36; k += blockDim.x) sJ[k] = a.J[36 * base + k];
-        for (int k = threadIdx.x; k < cnt * 6; k += blockDim.x) {
-            sF[k] = a.F[6 * base + k];
-            sU[k] = a.U[6 * (base + 1) + k];
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            for (int n = 0; n < cnt; ++n) {
-                double unew[6];
-#pragma unroll
-                for (int r = 0; r < 6; ++r) {
-                    double s = sF[6 * n + r];
-#pragma unroll
-                    for (int c = 0; c < 6; ++c) s = fma(sJ[36 * n + 6 * r + c], d[c], s);
-                    unew[r] = s;
-                }
-                double dx = 0.0, dv = 0.0, nx = 0.0, nv = 0.0;
-#pragma unroll
-                for (int r = 0; r < 6; ++r) {
-                    d[r] = unew[r] - sU[6 * n + r];
-                    sU[6 * n + r] = unew[r];
-                }
-#pragma unroll
-                for (int r = 0; r < 3; ++r) {
-                    dx = fma(d[r], d[r], dx);
-                    dv = fma(d[3 + r], d[3 + r], dv);
-                    nx = fma(unew[r], unew[r], nx);
-                    nv = fma(unew[3 + r], unew[3 + r], nv);
-                }
-                ok = ok && dx <= tol2 * nx && dv <= tol2 * nv;
-            }
-        }
-        __syncthreads();
-        for (int k = threadIdx.x; k < cnt * 6; k += blockDim.x) a.U[6 * (base + 1) + k] = sU[k];
-    }
-    if (threadIdx.x == 0) {
-        a.flag[1] += 1;
-        if (ok) a.flag[0] = 1;
-    }
-}
-
-// Converged starts -> saved states (plain FP64 steps, the serial step map).
-template <class C>
-__global__ void __launch_bounds__(64) shoot_save_kernel(PotDev<double> P, ShootArgs a) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= a.S) return;
     double y[6];
+#pragma unroll
     for (int j = 0; j < 6; ++j) y[j] = a.U[6 * n + j];
-    if (n == 0)
+    if (a.out && n == 0)
         for (int j = 0; j < 6; ++j) a.out[j] = y[j];
     const int len = slice_len(a, n);
     for (int s = 0; s < len; ++s) {
         dopri5_step_f64<C>(P, 0.0, a.dt, y);
         const int g = n * SHOOT_M + s + 1;
-        if (g % a.save_every == 0 && g / a.save_every < a.n_save)
+        if (a.out && g % a.save_every == 0 && g / a.save_every < a.n_save)
             for (int j = 0; j < 6; ++j) a.out[6 * (g / a.save_every) + j] = y[j];
+    }
+#pragma unroll
+    for (int j = 0; j < 6; ++j) a.F[6 * n + j] = y[j];
+}
+
+// The slices' Jacobians in FP32: lane 6 n + i carries the tangent along
+// U_j = e_i; J_n is stored as floats [S, 36] at a.J.
+template <class C>
+__global__ void __launch_bounds__(96) shoot_jac_kernel(PotDev<float> P32, ShootArgs a) {
+    if (a.flag[0]) return;
+    const int lane = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = lane / 6, i = lane % 6;
+    if (n >= a.S) return;
+    typedef D1<float> T;
+    PotDev<T> Q;
+    Q.n = P32.n;
+    Q.has_track = 0;
+    Q.ex = P32.ex;
+#pragma unroll
+    for (int c = 0; c < C::n; ++c) {
+        Q.c[c].kind = P32.c[c].kind;
+        Q.c[c].center = P32.c[c].center;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) Q.c[c].q[j] = T(P32.c[c].q[j], 0.0f);
+    }
+    T y[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) y[j] = T((float)a.U[6 * n + j], j == i ? 1.0f : 0.0f);
+    const T h((float)a.dt, 0.0f);
+    const int len = slice_len(a, n);
+    for (int s = 0; s < len; ++s) dopri5_step_dual<C, float>(Q, h, y);
+    float* J = reinterpret_cast<float*>(a.J);
+#pragma unroll
+    for (int j = 0; j < 6; ++j) J[36 * n + 6 * j + i] = y[j].d;
+}
+
+// Newton update of the joins as a parallel prefix scan of the affine maps
+// e -> J_n e + r_n (r_n = F_n - U_{n+1}, FP32; e_0 = 0): each thread composes
+// a contiguous segment, a Hillis-Steele scan combines the segments, each
+// thread replays its segment from its entry value and adds e to U (FP64).
+static constexpr int SCAN_T = 256;
+
+__device__ __forceinline__ void mat6_mul(const float A[36], const float B[36], float C_[36]) {
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            float s = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) s = fmaf(A[6 * r + k], B[6 * k + c], s);
+            C_[6 * r + c] = s;
+        }
+}
+
+__global__ void __launch_bounds__(SCAN_T) shoot_scan_kernel(ShootArgs a) {
+    if (a.flag[0]) return;
+    __shared__ float sA[SCAN_T * 36];
+    __shared__ float sb[SCAN_T * 6];
+    __shared__ float sw[SCAN_T];
+    const int t = threadIdx.x, S = a.S;
+    const int seg = (S + SCAN_T - 1) / SCAN_T;
+    const int n0 = min(S, t * seg), n1 = min(S, n0 + seg);
+    const float* J = reinterpret_cast<const float*>(a.J);
+    // segment composition
+    float A[36], b[6];
+#pragma unroll
+    for (int k = 0; k < 36; ++k) A[k] = (k % 7 == 0) ? 1.0f : 0.0f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) b[k] = 0.0f;
+    for (int n = n0; n < n1; ++n) {
+        float Jn[36], r[6], T2[36], b2[6];
+#pragma unroll
+        for (int k = 0; k < 36; ++k) Jn[k] = J[36 * n + k];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) r[k] = (float)(a.F[6 * n + k] - a.U[6 * (n + 1) + k]);
+        mat6_mul(Jn, A, T2);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            float s = r[q];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) s = fmaf(Jn[6 * q + k], b[k], s);
+            b2[q] = s;
+        }
+#pragma unroll
+        for (int k = 0; k < 36; ++k) A[k] = T2[k];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) b[k] = b2[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 36; ++k) sA[36 * t + k] = A[k];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) sb[6 * t + k] = b[k];
+    __syncthreads();
+    // inclusive scan over the segments: (A_t, b_t) <- (A_t, b_t) o (A_{t-s}, b_{t-s})
+    for (int st = 1; st < SCAN_T; st <<= 1) {
+        float Ap[36], bp[6];
+        const bool take = t >= st;
+        if (take) {
+#pragma unroll
+            for (int k = 0; k < 36; ++k) Ap[k] = sA[36 * (t - st) + k];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) bp[k] = sb[6 * (t - st) + k];
+        }
+        __syncthreads();
+        if (take) {
+            float T2[36], b2[6];
+            mat6_mul(A, Ap, T2);
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                float s = b[q];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) s = fmaf(A[6 * q + k], bp[k], s);
+                b2[q] = s;
+            }
+#pragma unroll
+            for (int k = 0; k < 36; ++k) A[k] = T2[k];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) b[k] = b2[k];
+#pragma unroll
+            for (int k = 0; k < 36; ++k) sA[36 * t + k] = A[k];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) sb[6 * t + k] = b[k];
+        }
+        __syncthreads();
+    }
+    // replay the segment from its entry value e (the previous prefix's b)
+    float e[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) e[k] = t > 0 ? sb[6 * (t - 1) + k] : 0.0f;
+    float worst = 0.0f;
+    for (int n = n0; n < n1; ++n) {
+        float e2[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            float s = (float)(a.F[6 * n + q] - a.U[6 * (n + 1) + q]);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) s = fmaf(J[36 * n + 6 * q + k], e[k], s);
+            e2[q] = s;
+        }
+        float ex = 0.0f, ev = 0.0f, nx = 0.0f, nv = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            e[q] = e2[q];
+            const double u = a.U[6 * (n + 1) + q] + (double)e2[q];
+            a.U[6 * (n + 1) + q] = u;
+            const float uf = (float)u;
+            if (q < 3) {
+                ex = fmaf(e2[q], e2[q], ex);
+                nx = fmaf(uf, uf, nx);
+            } else {
+                ev = fmaf(e2[q], e2[q], ev);
+                nv = fmaf(uf, uf, nv);
+            }
+        }
+        worst = fmaxf(worst, fmaxf(ex / fmaxf(nx, 1e-30f), ev / fmaxf(nv, 1e-30f)));
+    }
+    sw[t] = worst;
+    __syncthreads();
+    for (int st = SCAN_T / 2; st > 0; st >>= 1) {
+        if (t < st) sw[t] = fmaxf(sw[t], sw[t + st]);
+        __syncthreads();
+    }
+    if (t == 0) {
+        const float w = sqrtf(sw[0]);  // largest relative update
+        const float prev = __int_as_float(a.flag[2]);
+        a.flag[1] += 1;
+        const bool floor_reached = a.flag[1] > 1 && w < 1e-11f && w > 0.5f * prev;
+        if (w < (float)a.tol || floor_reached) a.flag[0] = 1;
+        a.flag[2] = __float_as_int(w);
     }
 }
 
 // Guess + Newton iterations of one orbit (slice starts in a.U); returns
-// the number of kernels launched.
+// the number of kernels launched.  With a.out set, the last slice pass
+// writes the saved states.
 template <class C>
 static int launch_shoot(const PotDev<double>& P, const PotDev<float>& P32, const ShootArgs& a, cudaStream_t st) {
     shoot_guess_kernel<C><<<1, 32, 0, st>>>(P32, a);
     for (int it = 0; it < SHOOT_ITERS; ++it) {
-        shoot_slice_kernel<C><<<(unsigned)((6 * a.S + 95) / 96), 96, 0, st>>>(P, a);
-        shoot_sweep_kernel<<<1, SWEEP_THREADS, 0, st>>>(a);
+        shoot_f64_kernel<C><<<(unsigned)((a.S + 63) / 64), 64, 0, st>>>(P, a);
+        shoot_jac_kernel<C><<<(unsigned)((6 * a.S + 95) / 96), 96, 0, st>>>(P32, a);
+        shoot_scan_kernel<<<1, SCAN_T, 0, st>>>(a);
     }
-    return 1 + 2 * SHOOT_ITERS;
+    return 1 + 3 * SHOOT_ITERS;
 }
 
 // ------------------------------------------------------------ sensitivities
@@ -346,7 +431,7 @@ extern "C" {
 int64_t ss_orbit_shoot_workspace_bytes(int64_t n_steps) {
     if (n_steps < 0) return set_error(SS_ERR_INVALID_ARGUMENT, "n_steps < 0");
     const int64_t S = (n_steps + SHOOT_M - 1) / SHOOT_M;
-    return (6 * (S + 1) + 6 * S + 36 * S) * (int64_t)sizeof(double) + 2 * (int64_t)sizeof(int32_t) + 256;
+    return (6 * (S + 1) + 6 * S + 36 * S) * (int64_t)sizeof(double) + 4 * (int64_t)sizeof(int32_t) + 256;
 }
 
 int ss_orbit_shoot_f64(const ss_potential* pot, const double* w0, double t0, double dt, int64_t n_steps,
@@ -384,15 +469,11 @@ int ss_orbit_shoot_f64(const ss_potential* pot, const double* w0, double t0, dou
         a.flag = (int32_t*)(a.J + 36 * S);
         a.tol = tol;
         a.out = out;
-        SS_CUDA_TRY(cudaMemsetAsync(a.flag, 0, 2 * sizeof(int32_t), st));
+        SS_CUDA_TRY(cudaMemsetAsync(a.flag, 0, 4 * sizeof(int32_t), st));
         int launched = 0;
         dispatch_comp(P, [&](auto comp) {
             using C = decltype(comp);
-            if constexpr (!std::is_same<C, GenericComp>::value) {
-                launched = launch_shoot<C>(P, P32, a, st);
-                shoot_save_kernel<C><<<(unsigned)((S + 63) / 64), 64, 0, st>>>(P, a);
-                launched += 1;
-            }
+            if constexpr (!std::is_same<C, GenericComp>::value) launched = launch_shoot<C>(P, P32, a, st);
             return 0;
         });
         for (int i = 1; i < launched; ++i) count_launch();
@@ -409,7 +490,7 @@ int64_t ss_prog_tangents_workspace_bytes(int64_t n_steps, int32_t n_comp) {
     if (n_steps < 0 || n_comp < 1) return set_error(SS_ERR_INVALID_ARGUMENT, "bad arguments");
     const int64_t S = (n_steps + SHOOT_M - 1) / SHOOT_M;
     const int64_t NS = 6 * n_comp, nd = NS + 6;
-    const int64_t leg = 6 * (S + 1) + 6 * S + 36 * S + 1;  // U, F, J, flags (one double)
+    const int64_t leg = 6 * (S + 1) + 6 * S + 36 * S + 2;  // U, F, J, flags (two doubles)
     return (2 * leg + 2 * S * 6 * (6 + NS) + (S + 1) * nd * 6) * (int64_t)sizeof(double) + 256;
 }
 
@@ -433,7 +514,7 @@ int ss_prog_tangents_f64(const ss_potential* pot, const double* raw_params, cons
     const int S = (n_steps + SHOOT_M - 1) / SHOOT_M;
     const int NS = 6 * P.n, nd = NS + 6;
     double* ws = (double*)workspace;
-    const int64_t leg = 6 * (S + 1) + 6 * S + 36 * S + 1;
+    const int64_t leg = 6 * (S + 1) + 6 * S + 36 * S + 2;
     auto leg_args = [&](double* base, const double* start, double h) {
         ShootArgs a;
         a.w0 = start;
@@ -469,8 +550,8 @@ int ss_prog_tangents_f64(const ss_potential* pot, const double* raw_params, cons
     t.W = t.Mf + (int64_t)S * 6 * (6 + NS);
     t.states = states;
     t.tangents = tangents;
-    SS_CUDA_TRY(cudaMemsetAsync(ab.flag, 0, 2 * sizeof(int32_t), st));
-    SS_CUDA_TRY(cudaMemsetAsync(af.flag, 0, 2 * sizeof(int32_t), st));
+    SS_CUDA_TRY(cudaMemsetAsync(ab.flag, 0, 4 * sizeof(int32_t), st));
+    SS_CUDA_TRY(cudaMemsetAsync(af.flag, 0, 4 * sizeof(int32_t), st));
     int launched = 0;
     dispatch_comp(P, [&](auto comp) {
         using C = decltype(comp);
