@@ -300,25 +300,38 @@ def gpu_arm(args, wl):
     err = {"max": float(e.max()), "p99": float(torch.quantile(e.float(), 0.99)), "median": float(e.median()),
            "frac_above_1e-5": float((e > 1e-5).double().mean()),
            "measure": "per particle max(|dx|/|x|, |dv|/|v|) of final states, FP32-compensated vs FP64 GPU path"}
-    # Sensitivity of each FP64 track to a 1e-12 relative change of the
-    # progenitor state (growth = final change / 1e-12): particles on chaotic
-    # tracks (close passages by the progenitor) amplify any rounding, FP64's
-    # included, so the FP32 error is also quoted on the regular tracks.
-    eps = 1e-12
-    wf_p = wf_d + eps * torch.cat([wf_d[:3].norm().expand(3), wf_d[3:].norm().expand(3)])
-    l64p, t64p = step("f64", wf_p, normals_d)[:2]
-    bp = torch.stack([l64p, t64p]).reshape(-1, 6)
-    gx = torch.linalg.norm(bp[:, :3] - b[:, :3], dim=1) / torch.linalg.norm(b[:, :3], dim=1)
-    gv = torch.linalg.norm(bp[:, 3:] - b[:, 3:], dim=1) / torch.linalg.norm(b[:, 3:], dim=1)
-    growth = torch.maximum(gx, gv) / eps
+    # Sensitivity of each FP64 track to a tiny independent change of its own
+    # initial state (release draws moved by 1e-9): growth = relative change
+    # of the final state / relative change of the initial state.  Tracks
+    # with close passages by the progenitor amplify any rounding, FP64's
+    # included, so the FP32 error is also quoted on the tracks whose growth
+    # stays below 1e3.
+    def with_ics(nrm):
+        back = pot.integrate_orbit(w0=wf_d, ts=np.array([0.0, -T]), t0=0.0, t1=-T, dt=dt).ys[-1]
+        o = gen_stream(pot, ts, back, MSAT, normals=nrm, dt=dt, prog_pot=prog, n_particles_per_release=ppr,
+                       precision="f64", return_ics=True)
+        # particle order (arm, release, draw) as in the error above
+        return torch.stack([o[0], o[1]]).reshape(-1, 6), o[2][:n_rel].permute(2, 0, 1, 3).reshape(-1, 6)
+
+    gen = torch.Generator(device=dev).manual_seed(77)
+    nrm_p = normals_d + 1e-9 * torch.randn(normals_d.shape, generator=gen, device=dev, dtype=normals_d.dtype)
+    b0, ic0 = with_ics(normals_d)
+    bp, icp = with_ics(nrm_p)
+
+    def prel(u, v):
+        return torch.maximum(torch.linalg.norm(u[:, :3] - v[:, :3], dim=1) / torch.linalg.norm(v[:, :3], dim=1),
+                             torch.linalg.norm(u[:, 3:] - v[:, 3:], dim=1) / torch.linalg.norm(v[:, 3:], dim=1))
+
+    growth = prel(bp, b0) / prel(icp, ic0).clamp_min(1e-300)
     regular = growth <= 1e3
     err["fp64_sensitivity"] = {
-        "perturbation": eps, "growth_median": float(growth.median()),
-        "growth_p99": float(torch.quantile(growth.float(), 0.99)), "growth_max": float(growth.max()),
-        "frac_growth_above_1e3": float((~regular).double().mean()),
+        "perturbation": "release draws + 1e-9 N(0,1) (independent per particle)",
+        "growth_median": float(growth.median()), "growth_p99": float(torch.quantile(growth.float(), 0.99)),
+        "growth_max": float(growth.max()), "frac_growth_above_1e3": float((~regular).double().mean()),
         "max_err_growth_le_1e3": float(e[regular].max()) if bool(regular.any()) else None,
-        "p99_err_growth_le_1e3": float(torch.quantile(e[regular].float(), 0.99)) if bool(regular.any()) else None}
-    del l32, t32, l64, t64, a, b, l64p, t64p, bp
+        "p99_err_growth_le_1e3": float(torch.quantile(e[regular].float(), 0.99)) if bool(regular.any()) else None,
+        "frac_err_above_1e-5_growth_le_1e3": float(((e > 1e-5) & regular).double().mean())}
+    del l32, t32, l64, t64, a, b, bp, b0, ic0, icp
 
     # --- e2e through the public API with host buffers
     n_snap = n_steps // snap if snap else 0

@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define SS_ABI_VERSION 1
+#define SS_ABI_VERSION 2
 #define SS_MAX_COMPONENTS 16
 
 /* ---------------------------------------------------------------- status */
@@ -33,7 +33,7 @@ typedef enum ss_status {
     SS_ERR_CUDA = -2,             /* a CUDA runtime call failed */
     SS_ERR_NONFINITE = -3,        /* integration produced inf/nan (per-item status set) */
     SS_ERR_WORKSPACE = -4,        /* caller workspace too small */
-    SS_ERR_UNSUPPORTED = -5       /* valid request outside what this build implements */
+    SS_ERR_UNSUPPORTED = -5       /* valid request outside what this library implements */
 } ss_status;
 
 /* ------------------------------------------------------ potential model */
@@ -195,8 +195,9 @@ typedef struct ss_pert_cfg {
 /* Library / ABI identity. */
 int ss_abi_version(void);
 const char* ss_last_error(void);
-/* sizeof of the ABI structs in this build: which = 0 ss_potential, 1 ss_stream_cfg,
- * 2 ss_release_cfg, 3 ss_pert_cfg, 4 ss_component, 5 ss_track, 6 ss_subhalos. */
+/* sizeof of the ABI structs in this library: which = 0 ss_potential, 1 ss_stream_cfg,
+ * 2 ss_release_cfg, 3 ss_pert_cfg, 4 ss_component, 5 ss_track, 6 ss_subhalos,
+ * 7 ss_expansion, 8 ss_mlp. */
 int64_t ss_abi_sizeof(int which);
 /* Number of kernels this library has launched in the process so far. */
 int64_t ss_kernel_launches(void);
@@ -346,11 +347,16 @@ int ss_release_vjp(const ss_potential* pot, const ss_release_cfg* cfg, const dou
  * forward-mode tangents along every raw parameter and every component of w0
  * (n_dir = 6 n_comp + 6): states [n_steps/save_every + 1, 6] and tangents
  * [n_steps/save_every + 1, n_dir, 6] on the forward leg.  workspace >=
- * ss_prog_tangents_workspace_bytes(n_steps, n_comp). */
+ * ss_prog_tangents_workspace_bytes(n_steps, n_comp).  starts_back and
+ * starts_fwd (optional, [S + 1, 6], S = ceil(n_steps / 16)) are the
+ * converged slice starts of the two legs from earlier ss_orbit_shoot_f64
+ * calls on the same potential (the first 6 (S + 1) doubles of their
+ * workspaces); given, the legs are not solved again. */
 int64_t ss_prog_tangents_workspace_bytes(int64_t n_steps, int32_t n_comp);
 int ss_prog_tangents_f64(const ss_potential* pot, const double* raw_params, const double* w0,
                          double dt, int32_t n_steps, int32_t save_every, double* states,
-                         double* tangents, void* workspace, int64_t workspace_bytes, void* stream);
+                         double* tangents, const double* starts_back, const double* starts_fwd,
+                         void* workspace, int64_t workspace_bytes, void* stream);
 
 /* Binned mean track (computed_binned_track, streamhelpers.py:201-228).
  * values [n, ncomp] FP64, key [n] FP64, edges [n_edges] ascending.

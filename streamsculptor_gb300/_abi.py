@@ -10,7 +10,7 @@ import ctypes as C
 import os
 import threading
 
-SS_ABI_VERSION = 1
+SS_ABI_VERSION = 2
 SS_MAX_COMPONENTS = 16
 
 SS_OK = 0
@@ -129,7 +129,7 @@ SIGNATURES = {
                                  VP]),
     "ss_prog_tangents_workspace_bytes": (C.c_int64, [C.c_int64, C.c_int32]),
     "ss_prog_tangents_f64": (C.c_int, [C.POINTER(ss_potential), VP, VP, C.c_double, C.c_int32, C.c_int32, VP, VP,
-                                       VP, C.c_int64, VP]),
+                                       VP, VP, VP, C.c_int64, VP]),
     "ss_binned_sums": (C.c_int, [VP, VP, C.c_int64, C.c_int32, VP, C.c_int32, VP, VP, VP]),
     "ss_peak_fma": (C.c_int, [C.c_int, C.c_int64, DP, VP, VP]),
     "ss_copy_rows_async": (C.c_int, [VP, VP, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int, VP]),

@@ -272,7 +272,7 @@ SHOOT_TOL = 1e-14
 
 
 def orbit(P, w0: torch.Tensor, t0: float, dt: float, n_steps: int, save_every: int,
-          method: str = "auto") -> torch.Tensor:
+          method: str = "auto", keep_starts: bool = False):
     """Fixed-step FP64 Dopri5 orbits.  method: 'serial' (one thread per
     orbit), 'shoot' (one orbit, parallel in time by multiple shooting; the
     serial orbit up to round-off) or 'auto' (shoot for a single long orbit in
@@ -285,14 +285,23 @@ def orbit(P, w0: torch.Tensor, t0: float, dt: float, n_steps: int, save_every: i
         if n != 1:
             raise ValueError("the parallel-in-time orbit integrates one orbit")
         need = _abi.load().ss_orbit_shoot_workspace_bytes(int(n_steps))
-        ws, nb = aligned_ptr(Workspace.get(int(need), w0.device, slot="shoot"))
+        buf = Workspace.get(int(need), w0.device, slot="shoot")
+        ws, nb = aligned_ptr(buf)
         _abi.call("ss_orbit_shoot_f64", C.byref(P), ptr(w0), float(t0), float(dt), int(n_steps), int(save_every),
                   ptr(out), ws, nb, SHOOT_TOL, stream_handle())
+        if keep_starts:
+            # converged slice starts: the first 6 (S + 1) doubles of the workspace
+            S = (int(n_steps) + 15) // 16
+            off = ws.value - buf.data_ptr()
+            starts = buf[off:off + 48 * (S + 1)].view(torch.float64).reshape(S + 1, 6).clone()
+            return out, starts
     elif method == "serial":
         _abi.call("ss_orbit_f64", C.byref(P), ptr(w0), n, float(t0), float(dt), int(n_steps), int(save_every),
                   ptr(out), stream_handle())
     else:
         raise ValueError("method must be 'auto', 'serial' or 'shoot'")
+    if keep_starts:
+        return out, None
     return out
 
 

@@ -111,8 +111,10 @@ def forward_stream(model, theta: np.ndarray, setup: StreamSetup, keep=False):
     dev = _core.device()
     P = model.struct(theta)
     w_obs = f64(np.asarray(theta[-6:], dtype=np.float64).reshape(1, 6), dev)
-    back = _core.orbit(P, w_obs, 0.0, -setup.dt, setup.n_steps, setup.n_steps)[:, -1].contiguous()
-    ws = _core.orbit(P, back, setup.t0, setup.dt, setup.n_steps, setup.spr)[0]
+    ob, starts_back = _core.orbit(P, w_obs, 0.0, -setup.dt, setup.n_steps, setup.n_steps, keep_starts=True)
+    back = ob[:, -1].contiguous()
+    of, starts_fwd = _core.orbit(P, back, setup.t0, setup.dt, setup.n_steps, setup.spr, keep_starts=True)
+    ws = of[0]
     ts = setup.t0 + np.arange(setup.n_rel + 1) * setup.spr * setup.dt
     normals = f64(setup.normals, dev)
     rcfg = _release_cfg(setup, setup.n_rel + 1)
@@ -130,7 +132,8 @@ def forward_stream(model, theta: np.ndarray, setup: StreamSetup, keep=False):
               ptr(ckpt), CKPT, stream_handle())
     if not keep:
         return final
-    return final, dict(P=P, ws=ws, t_rel=t_rel, msat=msat, normals=normals, ckpt=ckpt, cfg=cfg)
+    return final, dict(P=P, ws=ws, t_rel=t_rel, msat=msat, normals=normals, ckpt=ckpt, cfg=cfg,
+                       starts=(starts_back, starts_fwd))
 
 
 def backward_stream(model, theta: np.ndarray, setup: StreamSetup, saved: dict, lam_final: torch.Tensor):
@@ -159,8 +162,11 @@ def backward_stream(model, theta: np.ndarray, setup: StreamSetup, saved: dict, l
     tang = torch.empty(n_save, n_dir, 6, dtype=torch.float64, device=dev)
     need = _abi.load().ss_prog_tangents_workspace_bytes(int(setup.n_steps), int(model.n_comp))
     ws, nb = _core.aligned_ptr(_core.Workspace.get(int(need), dev, slot="tangents"))
+    sb, sf = saved.get("starts", (None, None))
+    if sb is None or sf is None:
+        sb = sf = None
     _abi.call("ss_prog_tangents_f64", C.byref(P), ptr(raw), ptr(w_obs), float(setup.dt), int(setup.n_steps),
-              int(setup.spr), ptr(states), ptr(tang), ws, nb, stream_handle())
+              int(setup.spr), ptr(states), ptr(tang), ptr(sb), ptr(sf), ws, nb, stream_handle())
     g_dir = torch.einsum("ri,rki->k", g_prog, tang)
     g_slot = g_slot + g_dir[:ns]
     g = torch.empty(len(theta), dtype=torch.float64, device=dev)

@@ -15,7 +15,7 @@
 //   * an FP32 Jacobian makes the iteration converge linearly with a factor
 //     ~1e-6 instead of quadratically, which still reaches the FP64 round-off
 //     floor in a few iterations; the iteration stops when the largest relative
-//     update is below `tol` or stops shrinking below 1e-11 (the round-off floor);
+//     update is below `tol` or stops shrinking below 1e-12 (the round-off floor);
 //   * the last slice pass wrote the saved states (its starts differ from the
 //     final ones by less than the last update).
 // The result is the serial fixed-step FP64 Dopri5 orbit (the same step map
@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(SCAN_T) shoot_scan_kernel(ShootArgs a) {
         const float w = sqrtf(sw[0]);  // largest relative update
         const float prev = __int_as_float(a.flag[2]);
         a.flag[1] += 1;
-        const bool floor_reached = a.flag[1] > 1 && w < 1e-11f && w > 0.5f * prev;
+        const bool floor_reached = a.flag[1] > 1 && w < 1e-12f && w > 0.5f * prev;
         if (w < (float)a.tol || floor_reached) a.flag[0] = 1;
         a.flag[2] = __float_as_int(w);
     }
@@ -495,7 +495,8 @@ int64_t ss_prog_tangents_workspace_bytes(int64_t n_steps, int32_t n_comp) {
 }
 
 int ss_prog_tangents_f64(const ss_potential* pot, const double* raw_params, const double* w0, double dt,
-                         int32_t n_steps, int32_t save_every, double* states, double* tangents, void* workspace,
+                         int32_t n_steps, int32_t save_every, double* states, double* tangents,
+                         const double* starts_back, const double* starts_fwd, void* workspace,
                          int64_t workspace_bytes, void* stream) {
     PotDev<double> P;
     int rc = prepare_potential<double>(pot, &P, false);
@@ -552,12 +553,22 @@ int ss_prog_tangents_f64(const ss_potential* pot, const double* raw_params, cons
     t.tangents = tangents;
     SS_CUDA_TRY(cudaMemsetAsync(ab.flag, 0, 4 * sizeof(int32_t), st));
     SS_CUDA_TRY(cudaMemsetAsync(af.flag, 0, 4 * sizeof(int32_t), st));
+    SS_CHECK_ARG((starts_back == nullptr) == (starts_fwd == nullptr), "give both leg starts or neither");
+    const bool reuse = starts_back != nullptr;
+    if (reuse) {
+        SS_CUDA_TRY(cudaMemcpyAsync(ab.U, starts_back, 6 * (size_t)(S + 1) * sizeof(double), cudaMemcpyDeviceToDevice,
+                                    st));
+        SS_CUDA_TRY(cudaMemcpyAsync(af.U, starts_fwd, 6 * (size_t)(S + 1) * sizeof(double), cudaMemcpyDeviceToDevice,
+                                    st));
+    }
     int launched = 0;
     dispatch_comp(P, [&](auto comp) {
         using C = decltype(comp);
         if constexpr (!std::is_same<C, GenericComp>::value) {
-            launched += launch_shoot<C>(P, P32, ab, st);
-            launched += launch_shoot<C>(P, P32, af, st);
+            if (!reuse) {
+                launched += launch_shoot<C>(P, P32, ab, st);
+                launched += launch_shoot<C>(P, P32, af, st);
+            }
             const int lanes = S * (6 + NS);
             shoot_sens_kernel<C><<<(unsigned)((lanes + 63) / 64), 64, 0, st>>>(P, t, 1);
             shoot_sens_kernel<C><<<(unsigned)((lanes + 63) / 64), 64, 0, st>>>(P, t, 0);

@@ -5,7 +5,7 @@ value + force loss differentiated through the network's input gradient;
 ss_mlp_adam), evaluated in FP32 on CUDA cores (ss_mlp_eval) or with BF16
 weights on the tensor cores inside the stream integrator
 (ss_stream_mlp_bf16).  The exact potential stays the reference: it makes
-the training set and judges the surrogate's error.
+the training set and measures the surrogate's error.
 """
 from __future__ import annotations
 
