@@ -306,6 +306,21 @@ int ss_pert_response(const ss_potential* base, const ss_subhalos* sh, const ss_p
                      double* base_out, void* pert_out,
                      void* workspace, int64_t workspace_bytes, void* stream);
 
+/* The same response along a stored base track, for many subhalo batches
+ * (fields.MassRadiusPerturbation_Interp, fields.py:208-257, and
+ * GenerateMassRadiusPerturbation.compute_perturbation_Interp,
+ * perturbative.py:178-221: the base stream is computed once, each batch only
+ * integrates its response).  ss_pert_base_track fills `track` (device,
+ * >= ss_pert_track_bytes(cfg, precision) bytes: every particle's stage
+ * positions and tidal tensors) and base_out (nullable); ss_pert_response_track
+ * integrates the response of the subhalos `sh` (G: the base potential's G)
+ * along it.  The results equal ss_pert_response's with the same cfg. */
+int64_t ss_pert_track_bytes(const ss_pert_cfg* cfg, int precision);
+int ss_pert_base_track(const ss_potential* base, const ss_pert_cfg* cfg, int precision, const double* base_ics,
+                       double* base_out, void* track, int64_t track_bytes, void* stream);
+int ss_pert_response_track(const ss_subhalos* sh, double G, const ss_pert_cfg* cfg, int precision,
+                           const void* track, const void* pert_ics, void* pert_out, void* stream);
+
 /* Per-subhalo potential, gradient, dPhi/da and its gradient at n points
  * (device): phi [n, sh->n], grad [n, sh->n, 3], dphi_da [n, sh->n],
  * grad_dphi_da [n, sh->n, 3] (any may be NULL); zero outside the window.

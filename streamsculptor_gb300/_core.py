@@ -495,6 +495,35 @@ def pert_response(P, table: SubhaloTable, cfg, precision: int, base_ics, pert_ic
     return base_out, out
 
 
+def pert_base_track(P, cfg, precision: int, base_ics):
+    """Stored base track of every particle (ss_pert_base_track): (track
+    buffer, final base states [N, 6])."""
+    dev = base_ics.device
+    nb = _abi.load().ss_pert_track_bytes(C.byref(cfg), int(precision))
+    if nb < 0:
+        raise _abi.SSError("ss_pert_track_bytes", nb, _abi.load().ss_last_error().decode())
+    track = torch.empty(max(int(nb), 16) // 16 * 16 + 16, dtype=torch.uint8, device=dev)
+    base_out = torch.empty(cfg.n_particles, 6, dtype=torch.float64, device=dev)
+    _abi.call("ss_pert_base_track", C.byref(P), C.byref(cfg), int(precision), ptr(base_ics), ptr(base_out),
+              ptr(track), track.numel(), stream_handle())
+    return track, base_out
+
+
+def pert_response_track(table: SubhaloTable, G: float, cfg, precision: int, track, pert_ics):
+    """Response of the subhalos `table` along a stored base track."""
+    dev = track.device
+    dtype = torch.float64 if precision == 64 else torch.float32
+    N, ns, ncol = cfg.n_particles, int(table.m.shape[0]), cfg.ncol
+    n_saves = cfg.n_steps // cfg.save_stride + 1 if cfg.save_stride > 0 else 1
+    out = torch.empty(n_saves, N, ns, ncol, dtype=dtype, device=dev)
+    S = table.struct()
+    if pert_ics is not None:
+        pert_ics = pert_ics.to(dtype).contiguous()
+    _abi.call("ss_pert_response_track", C.byref(S), float(G), C.byref(cfg), int(precision), ptr(track),
+              ptr(pert_ics), ptr(out), stream_handle())
+    return out
+
+
 def binned_sums(values: torch.Tensor, key: torch.Tensor, edges: torch.Tensor):
     n, ncomp = values.shape
     nb = edges.shape[0] - 1

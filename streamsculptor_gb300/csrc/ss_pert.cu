@@ -326,6 +326,54 @@ int64_t ss_pert_workspace_bytes(const ss_pert_cfg* cfg, int precision, int64_t p
     return particles_per_chunk * cfg->n_steps * REC * (precision == 64 ? 8 : 4);
 }
 
+static int pert_args(const ss_pert_cfg* cfg, int precision, PertArgs* a) {
+    SS_CHECK_ARG(cfg != nullptr, "cfg is NULL");
+    SS_CHECK_ARG(precision == 32 || precision == 64, "precision must be 32 or 64");
+    SS_CHECK_ARG(cfg->ncol == 6 || cfg->ncol == 12, "ncol must be 6 or 12");
+    SS_CHECK_ARG(cfg->n_particles >= 0 && cfg->n_steps >= 0 && cfg->n_steps < (1LL << 30), "bad sizes");
+    SS_CHECK_ARG(cfg->particles_per_release >= 1 && cfg->steps_per_release >= 0, "bad release layout");
+    SS_CHECK_ARG(std::isfinite(cfg->dt) && cfg->dt != 0.0 && std::isfinite(cfg->t0), "dt must be finite, non-zero");
+    SS_CHECK_ARG(cfg->save_stride >= 0, "save_stride < 0");
+    const int64_t n_rel = (cfg->n_particles + cfg->particles_per_release - 1) / cfg->particles_per_release;
+    SS_CHECK_ARG(n_rel == 0 || (n_rel - 1) * (int64_t)cfg->steps_per_release <= cfg->n_steps,
+                 "last release starts after n_steps");
+    memset(a, 0, sizeof(*a));
+    a->N = cfg->n_particles;
+    a->ppr = cfg->particles_per_release;
+    a->spr = cfg->steps_per_release;
+    a->n_steps = (int32_t)cfg->n_steps;
+    a->ncol = cfg->ncol;
+    a->save_stride = cfg->save_stride;
+    a->n_saves = cfg->save_stride > 0 ? (int32_t)(cfg->n_steps / cfg->save_stride + 1) : 1;
+    a->t0 = cfg->t0;
+    a->dt = cfg->dt;
+    return SS_OK;
+}
+
+// response kernels over [0, N) in grid-sized chunks; a.table = the records of particle 0
+static int pert_response_launch(const ShDev& S, PertArgs a, int precision, cudaStream_t st) {
+    const int sblock = 128;
+    const int sblocks = (int)((S.n + sblock - 1) / sblock);
+    const int64_t max_np = ((1LL << 31) - 1) / sblocks;
+    const int64_t esz = precision == 64 ? 8 : 4;
+    char* table0 = (char*)a.table;
+    for (int64_t p0 = 0; p0 < a.N; p0 += max_np) {
+        a.p0 = p0;
+        a.np = a.N - p0 < max_np ? a.N - p0 : max_np;
+        a.table = table0 + pert_offset(p0, a.ppr, a.spr, a.n_steps) * REC * esz;
+        const unsigned g2 = (unsigned)(a.np * sblocks);
+        if (precision == 64) {
+            if (a.ncol == 12) pert_response_kernel<double, 12><<<g2, sblock, 0, st>>>(S, a, sblocks);
+            else pert_response_kernel<double, 6><<<g2, sblock, 0, st>>>(S, a, sblocks);
+        } else {
+            if (a.ncol == 12) pert_response_kernel<float, 12><<<g2, sblock, 0, st>>>(S, a, sblocks);
+            else pert_response_kernel<float, 6><<<g2, sblock, 0, st>>>(S, a, sblocks);
+        }
+        SS_LAUNCH_CHECK();
+    }
+    return SS_OK;
+}
+
 int ss_pert_response(const ss_potential* base, const ss_subhalos* sh, const ss_pert_cfg* cfg, int precision,
                      const double* base_ics, const void* pert_ics, double* base_out, void* pert_out, void* workspace,
                      int64_t workspace_bytes, void* stream) {
@@ -405,6 +453,57 @@ int ss_pert_response(const ss_potential* base, const ss_subhalos* sh, const ss_p
         p0 = p1;
     }
     return SS_OK;
+}
+
+int64_t ss_pert_track_bytes(const ss_pert_cfg* cfg, int precision) {
+    PertArgs a;
+    int rc = pert_args(cfg, precision, &a);
+    if (rc) return rc;
+    return pert_offset(a.N, a.ppr, a.spr, a.n_steps) * REC * (precision == 64 ? 8 : 4);
+}
+
+int ss_pert_base_track(const ss_potential* base, const ss_pert_cfg* cfg, int precision, const double* base_ics,
+                       double* base_out, void* track, int64_t track_bytes, void* stream) {
+    PotDev<double> P;
+    int rc = prepare_potential<double>(base, &P, false);
+    if (rc) return rc;
+    PertArgs a;
+    rc = pert_args(cfg, precision, &a);
+    if (rc) return rc;
+    if (a.N == 0) return SS_OK;
+    SS_CHECK_ARG(base_ics != nullptr, "base_ics is NULL");
+    const int64_t need = ss_pert_track_bytes(cfg, precision);
+    SS_CHECK_ARG(track != nullptr && track_bytes >= need && ((uintptr_t)track % 16) == 0,
+                 "track of %lld bytes (16-byte aligned) needed", (long long)need);
+    a.base_ics = base_ics;
+    a.base_out = base_out;
+    a.table = track;
+    a.p0 = 0;
+    a.np = a.N;
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned g1 = (unsigned)((a.N + 63) / 64);
+    if (precision == 64) pert_base_kernel<double><<<g1, 64, 0, st>>>(P, a);
+    else pert_base_kernel<float><<<g1, 64, 0, st>>>(P, a);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
+int ss_pert_response_track(const ss_subhalos* sh, double G, const ss_pert_cfg* cfg, int precision,
+                           const void* track, const void* pert_ics, void* pert_out, void* stream) {
+    ShDev S;
+    SS_CHECK_ARG(std::isfinite(G) && G > 0.0, "G must be finite and > 0");
+    int rc = prepare_subhalos(sh, G, &S);
+    if (rc) return rc;
+    PertArgs a;
+    rc = pert_args(cfg, precision, &a);
+    if (rc) return rc;
+    if (a.N == 0) return SS_OK;
+    SS_CHECK_ARG(track != nullptr && pert_out != nullptr, "NULL buffer");
+    SS_CHECK_ARG(((uintptr_t)track % 16) == 0, "track must be 16-byte aligned");
+    a.pert_ics = pert_ics;
+    a.pert_out = pert_out;
+    a.table = const_cast<void*>(track);
+    return pert_response_launch(S, a, precision, (cudaStream_t)stream);
 }
 
 }  // extern "C"

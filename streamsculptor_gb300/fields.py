@@ -52,6 +52,26 @@ class MassRadiusPerturbation_OTF:
         return [out0, torch.cat([v1, dp, dv1, dpr], dim=1)]
 
 
+class MassRadiusPerturbation_Interp(MassRadiusPerturbation_OTF):
+    """The response field along the stored base stream (fields.py:208-257):
+    coords = derivs [N_sh, 12]; args = {'idx': release index, 'tail_bool':
+    True for the leading arm}.  The base state at t is the particle's fixed-
+    step FP64 orbit from its release (the reference interpolates its dense
+    base stream there)."""
+
+    def term(self, t, coords, args):
+        g = self.pertgen
+        b = g.base_stream
+        idx, lead = int(args["idx"]), bool(args["tail_bool"])
+        ics = g.base_realspace_ICs_lead if lead else g.base_realspace_ICs_trail
+        t_rel, t = float(b._ts_h[idx]), float(host64(t))
+        h, nst = _core.fixed_step(t - t_rel, b._h)
+        w = f64(ics[idx]).reshape(1, 6)
+        if nst > 0:
+            w = _core.orbit(g.potential_base._desc(), w, t_rel, h, nst, nst)[:, -1]
+        return super().term(t, [w.reshape(6), coords], args)[1]
+
+
 def _t_span(ts_h, backwards_int, t0, t1):
     """t0/t1 selection of integrate_field (fields.py:58-80)."""
     if float(t0) != float(t1):

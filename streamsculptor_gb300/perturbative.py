@@ -128,6 +128,40 @@ class GenerateMassRadiusPerturbation(Potential):
         d = out[0].reshape(nrel, 2, self.num_pert, self._ncol)
         return [base_out[:, 0], d[:, 0]], [base_out[:, 1], d[:, 1]]
 
+    def _stream_pert_cfg(self):
+        b = self.base_stream
+        nrel = len(b._ts_h) - 1
+        cfg = _abi.ss_pert_cfg()
+        cfg.t0, cfg.dt = float(b._ts_h[0]), float(b._h)
+        cfg.n_steps, cfg.n_particles = b._spr * nrel, 2 * nrel
+        cfg.particles_per_release, cfg.steps_per_release = 2, b._spr
+        cfg.ncol, cfg.save_stride = self._ncol, 0
+        return cfg, nrel
+
+    def compute_perturbation_Interp(self, cpu=True, solver=None, rtol=1e-6, atol=1e-6, dtmin=0.05, dtmax=None, *,
+                                    precision=None):
+        """The response along the stored base stream (perturbative.py:178-221):
+        the base track (stage positions and tidal tensors of every particle)
+        is computed once per BaseStreamModel and precision and reused by every
+        perturbation generator built on it, so each subhalo batch only
+        integrates its response.  Same results as compute_perturbation_OTF."""
+        _core.check_solver(solver)
+        prec = int(precision or self.precision)
+        b = self.base_stream
+        cfg, nrel = self._stream_pert_cfg()
+        cache = b.__dict__.setdefault("_pert_tracks", {})
+        if prec not in cache:
+            base = torch.stack([self.base_realspace_ICs_lead[:nrel], self.base_realspace_ICs_trail[:nrel]], dim=1)
+            cache[prec] = _core.pert_base_track(self.potential_base._desc(), cfg, prec,
+                                                base.reshape(2 * nrel, 6).contiguous())
+        track, base_out = cache[prec]
+        pert = torch.stack([self.perturbation_ICs_lead[:nrel], self.perturbation_ICs_trail[:nrel]], dim=1)
+        out = _core.pert_response_track(self.sh_table, self.potential_base._G, cfg, prec, track,
+                                        pert.reshape(2 * nrel, self.num_pert, self._ncol))
+        base_out = base_out.reshape(nrel, 2, 6)
+        d = out[0].reshape(nrel, 2, self.num_pert, self._ncol)
+        return [base_out[:, 0], d[:, 0]], [base_out[:, 1], d[:, 1]]
+
 
 class BaseStreamModelChen25(Potential):
     """Chen+25 base stream with the progenitor's own potential moving on its

@@ -439,3 +439,34 @@ def test_host_output_matches_device(ss, oracle, precision):
         a, b = a.cpu().numpy(), b.numpy()
         assert a.shape == b.shape
         assert np.array_equal(a, b, equal_nan=True)
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_interp_response_equals_otf_for_several_batches(ss, oracle, precision):
+    """compute_perturbation_Interp (stored base track, perturbative.py:178-221)
+    gives the OTF results for every subhalo batch built on one base stream,
+    and the Interp field term equals the OTF term at the stored base state."""
+    from streamsculptor_gb300 import fields, perturbative, potential as P
+    n_rel = 120
+    orc, back, ts, normals = _c1_setup(oracle, n_rel=n_rel)
+    base_pot = mw3_gpu(ss)
+    bsm = perturbative.BaseStreamModel(base_pot, back, ts, 2e4, 0, normals=normals)
+    rng = np.random.default_rng(21)
+    for batch in range(2):
+        nsh = 5 + 3 * batch
+        args = (10 ** rng.uniform(5, 7, nsh), rng.uniform(0.1, 0.5, nsh), rng.normal(0, 8, (nsh, 3)),
+                rng.normal(0, 0.1, (nsh, 3)), rng.uniform(ts[0], ts[-1], nsh), 1e9)
+        gen = perturbative.GenerateMassRadiusPerturbation(base_pot, P.SubhaloLinePotential(*args, units=ss.usys),
+                                                          P.SubhaloLinePotential_dRadius(*args, units=ss.usys), bsm,
+                                                          precision=precision)
+        (lo, ldo), (to, tdo) = gen.compute_perturbation_OTF()
+        (li, ldi), (ti, tdi) = gen.compute_perturbation_Interp()
+        for a, b in ((lo, li), (ldo, ldi), (to, ti), (tdo, tdi)):
+            assert torch.equal(a, b)
+    # the Interp field at a stored state equals the OTF field there
+    f_i = fields.MassRadiusPerturbation_Interp(gen)
+    f_o = fields.MassRadiusPerturbation_OTF(gen)
+    d = torch.as_tensor(rng.normal(0, 1e-3, (gen.num_pert, 12)), device="cuda")
+    out_i = f_i.term(ts[-1], d, {"idx": 10, "tail_bool": True})
+    out_o = f_o.term(ts[-1], [lo[10], d])[1]
+    assert rel_err(np64(out_i), np64(out_o)) < 1e-12
