@@ -178,7 +178,11 @@ typedef struct ss_release_cfg {
 
 /* First-order response to subhalos (MassRadiusPerturbation_OTF,
  * fields.py:159-206).  Per particle: base state (6) and, per subhalo, ncol
- * columns: d(x,v)/d(eps) (6) and, when ncol == 12, d^2(x,v)/d(eps)d(r_s) (6). */
+ * columns: d(x,v)/d(eps) (6), when ncol >= 12 d^2(x,v)/d(eps)d(r_s) (6) and,
+ * when ncol == 18, the second-order mass response (x2, v2) of
+ * MassRadiusPerturbation_OTF_SecondOrder (fields.py:260-320):
+ *   d(x2)/dt = v2,  d(v2)/dt = T x2 + (d2a/dx2 : x1 x1) - Hessian(Phi_s) x1,
+ * the reference's equation as written (no factor 1/2 on either source). */
 typedef struct ss_pert_cfg {
     double t0;
     double dt;                 /* signed: < 0 integrates backwards in time */
@@ -186,7 +190,7 @@ typedef struct ss_pert_cfg {
     int64_t n_particles;
     int32_t particles_per_release;
     int32_t steps_per_release;
-    int32_t ncol;              /* 6 or 12 */
+    int32_t ncol;              /* 6, 12 or 18 */
     int32_t save_stride;       /* 0 = final only; else save at steps 0, s, 2s, ... n_steps */
 } ss_pert_cfg;
 
@@ -320,6 +324,13 @@ int ss_pert_base_track(const ss_potential* base, const ss_pert_cfg* cfg, int pre
                        double* base_out, void* track, int64_t track_bytes, void* stream);
 int ss_pert_response_track(const ss_subhalos* sh, double G, const ss_pert_cfg* cfg, int precision,
                            const void* track, const void* pert_ics, void* pert_out, void* stream);
+
+/* The response field at one point (fields.MassRadiusPerturbation_OTF.term,
+ * fields.py:174-206, and MassRadiusPerturbation_OTF_SecondOrder.term,
+ * fields.py:284-320): y = [x0v0 (6), sh->n x ncol] (device, FP64) at time t,
+ * dy (device) receives d/dt of the same layout.  ncol: 6, 12 or 18. */
+int ss_pert_term(const ss_potential* base, const ss_subhalos* sh, int ncol, double t, const double* y, double* dy,
+                 void* stream);
 
 /* Per-subhalo potential, gradient, dPhi/da and its gradient at n points
  * (device): phi [n, sh->n], grad [n, sh->n, 3], dphi_da [n, sh->n],

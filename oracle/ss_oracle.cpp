@@ -558,6 +558,18 @@ struct PertRHS {
         double T[3][3];
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j) T[i][j] = -H[i][j];
+        // second order (MassRadiusPerturbation_OTF_SecondOrder, fields.py:260-320):
+        // d2a_dx2[i][j][k] = d^2 a_i / dx_j dx_k = -d^3 Phi, by AD of the Hessian
+        double d2a[3][3][3] = {};
+        if (ncol == 18) {
+            typedef Dual<double, 3> D3;
+            D3 xd[3], ph, gg[3], HH[3][3];
+            for (int i = 0; i < 3; ++i) xd[i] = D3::var(x0[i], i);
+            hess_total<D3>(*P, xd, t, &ph, gg, HH);
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j)
+                    for (int k = 0; k < 3; ++k) d2a[i][j][k] = -HH[i][j].d[k];
+        }
         for (int64_t s = 0; s < sh->n; ++s) {
             // -jacfwd(potential_per_SH) and -jacfwd(structural potential_per_SH)
             // for subhalo s (perturbative.py:40-41): gradient in x of Phi_s and
@@ -582,12 +594,31 @@ struct PertRHS {
                 for (int j = 0; j < 3; ++j) acc += T[i][j] * u[j];
                 du[3 + i] = acc;
             }
-            if (ncol == 12) {
+            if (ncol >= 12) {
                 for (int i = 0; i < 3; ++i) {
                     du[6 + i] = u[9 + i];
                     double acc = a1r[i];
                     for (int j = 0; j < 3; ++j) acc += T[i][j] * u[6 + j];
                     du[9 + i] = acc;
+                }
+            }
+            if (ncol == 18) {
+                // dapert_dx = -(Hessian of Phi_s), by nested AD in x
+                typedef Dual<double, 3> I3;
+                typedef Dual<I3, 3> O3;
+                O3 xs2[3];
+                for (int i = 0; i < 3; ++i) xs2[i] = O3::var(I3::var(x0[i], i), i);
+                O3 fs = phi_subhalo<O3>(sh->kind, P->G, sh->m[s], O3(sh->a[s]), sh->x0 + 3 * s, sh->v + 3 * s,
+                                        sh->t0[s], sh->t_window, xs2, t);
+                // d2a = T x2 + einsum('ikj,nk->nij') contracted with x1 + dapert_dx x1
+                for (int i = 0; i < 3; ++i) {
+                    du[12 + i] = u[15 + i];
+                    double acc = 0.0;
+                    for (int j = 0; j < 3; ++j) acc += T[i][j] * u[12 + j];
+                    for (int k = 0; k < 3; ++k)
+                        for (int j = 0; j < 3; ++j) acc += d2a[i][k][j] * u[k] * u[j];
+                    for (int j = 0; j < 3; ++j) acc += -fs.d[i].d[j] * u[j];
+                    du[15 + i] = acc;
                 }
             }
         }

@@ -118,6 +118,7 @@ SIGNATURES = {
     "ss_stream_f32k_noalloc": (C.c_int, [C.POINTER(ss_potential), C.POINTER(ss_stream_cfg), VP, VP, VP, VP, VP]),
     "ss_subhalo_eval": (C.c_int, [C.POINTER(ss_subhalos), C.c_double, VP, C.c_int64, C.c_double, VP, VP, VP,
                                   VP, VP]),
+    "ss_pert_term": (C.c_int, [C.POINTER(ss_potential), C.POINTER(ss_subhalos), C.c_int, C.c_double, VP, VP, VP]),
     "ss_pert_workspace_bytes": (C.c_int64, [C.POINTER(ss_pert_cfg), C.c_int, C.c_int64]),
     "ss_pert_response": (C.c_int, [C.POINTER(ss_potential), C.POINTER(ss_subhalos), C.POINTER(ss_pert_cfg),
                                    C.c_int, VP, VP, VP, VP, VP, C.c_int64, VP]),

@@ -472,6 +472,15 @@ def subhalo_eval(table: SubhaloTable, G: float, xyz: torch.Tensor, t: float):
     return phi, grad, dphi, gdphi
 
 
+def pert_term(P, table: SubhaloTable, ncol: int, t: float, y: torch.Tensor) -> torch.Tensor:
+    """d/dt of y = [x0v0 (6), n_sh x ncol] (FP64, device) at time t."""
+    y = y.contiguous()
+    dy = torch.empty_like(y)
+    S = table.struct()
+    _abi.call("ss_pert_term", C.byref(P), C.byref(S), int(ncol), float(t), ptr(y), ptr(dy), stream_handle())
+    return dy
+
+
 def pert_response(P, table: SubhaloTable, cfg, precision: int, base_ics, pert_ics, chunk_particles=None):
     dev = base_ics.device
     dtype = torch.float64 if precision == 64 else torch.float32
@@ -481,7 +490,7 @@ def pert_response(P, table: SubhaloTable, cfg, precision: int, base_ics, pert_ic
     base_out = torch.empty(N, 6, dtype=torch.float64, device=dev)
     if chunk_particles is None:
         # about 2 GB of base-track records per chunk
-        per = max(1, cfg.n_steps) * 56 * (8 if precision == 64 else 4)
+        per = max(1, cfg.n_steps) * (120 if ncol == 18 else 56) * (8 if precision == 64 else 4)
         chunk_particles = max(1, min(N, (2 << 30) // per))
     need = _abi.load().ss_pert_workspace_bytes(C.byref(cfg), precision, int(chunk_particles))
     if need < 0:

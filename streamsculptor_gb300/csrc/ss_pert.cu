@@ -30,7 +30,13 @@
 
 namespace ssg {
 
-static constexpr int REC = 56;  // 6 stages x (x0[3], T[6]) + 2 pad
+// Base-track records per step: first order 6 stages x (x0[3], T[6]) + 2 pad;
+// second order (ncol = 18) adds the 10 independent third derivatives of the
+// base acceleration per stage: 6 x 19 + 6 pad.
+static constexpr int REC = 56;
+static constexpr int REC2 = 120;
+__host__ __device__ constexpr int rec_len(int ord) { return ord == 2 ? REC2 : REC; }
+__host__ __device__ constexpr int stage_len(int ord) { return ord == 2 ? 19 : 9; }
 
 struct PertArgs {
     int64_t N;       // particles in the whole run
@@ -61,19 +67,55 @@ __host__ __device__ inline int64_t pert_offset(int64_t p, int32_t ppr, int32_t s
 }
 
 // ------------------------------------------------------------- phase 1
-template <class R>
+// One stage record of the base track at (x, t): x0, T = -Hessian(Phi)
+// (xx yy zz xy xz yz) and, for the second order, d2a/dx dx = -(third
+// derivatives of Phi) by forward-mode differentiation of the analytic
+// Hessian, ordered xxx xxy xxz xyy xyz xzz yyy yyz yzz zzz.  g = grad Phi.
+template <int ORD>
+__device__ __forceinline__ void base_stage(const PotDev<double>& P, const double x[3], double t, double g[3],
+                                           double r[19]) {
+    double cc[3] = {0.0, 0.0, 0.0};
+    if (P.has_track) track_eval(P.track, t, cc);
+    double H[6];
+    const double xs[3] = {x[0] - cc[0], x[1] - cc[1], x[2] - cc[2]};
+    pot_grad<double, double, true>(P, x, xs, g, H);
+    r[0] = x[0];
+    r[1] = x[1];
+    r[2] = x[2];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) r[3 + c] = -H[c];
+    if constexpr (ORD == 2) {
+        Dual<3> xd[3], xsd[3], gd[3], Hd[6];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            xd[c] = Dual<3>(x[c]);
+            xd[c].d[c] = 1.0;
+            xsd[c] = Dual<3>(xs[c]);
+            xsd[c].d[c] = 1.0;
+        }
+        pot_grad<Dual<3>, double, true>(P, xd, xsd, gd, Hd);
+        // H order xx yy zz xy xz yz; D_abc = d H_ab / d x_c
+        const double D[10] = {Hd[0].d[0], Hd[0].d[1], Hd[0].d[2], Hd[1].d[0], Hd[3].d[2],
+                              Hd[2].d[0], Hd[1].d[1], Hd[1].d[2], Hd[2].d[1], Hd[2].d[2]};
+#pragma unroll
+        for (int c = 0; c < 10; ++c) r[9 + c] = -D[c];
+    }
+}
+
+template <class R, int ORD>
 __global__ void __launch_bounds__(64) pert_base_kernel(PotDev<double> P, PertArgs a) {
+    constexpr int RL = rec_len(ORD), SL = stage_len(ORD);
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.np) return;
     const int64_t p = a.p0 + i;
     const int start = (int)pert_start(p, a.ppr, a.spr);
     R* rec = reinterpret_cast<R*>(a.table) +
-             (pert_offset(p, a.ppr, a.spr, a.n_steps) - pert_offset(a.p0, a.ppr, a.spr, a.n_steps)) * REC;
+             (pert_offset(p, a.ppr, a.spr, a.n_steps) - pert_offset(a.p0, a.ppr, a.spr, a.n_steps)) * RL;
     double y[6];
     for (int k = 0; k < 6; ++k) y[k] = a.base_ics[6 * p + k];
     const double h = a.dt;
     const double cs[6] = {0.0, SS_C2, SS_C3, SS_C4, SS_C5, 1.0};
-    for (int n = start; n < a.n_steps; ++n, rec += REC) {
+    for (int n = start; n < a.n_steps; ++n, rec += RL) {
         const double t = a.t0 + (double)n * h;
         double k[6][6];
         double ys[6];
@@ -91,25 +133,17 @@ __global__ void __launch_bounds__(64) pert_base_kernel(PotDev<double> P, PertArg
                     acc = SS_A61 * k[0][c] + SS_A62 * k[1][c] + SS_A63 * k[2][c] + SS_A64 * k[3][c] + SS_A65 * k[4][c];
                 ys[c] = s == 0 ? y[c] : y[c] + h * acc;
             }
-            const double ts = t + cs[s] * h;
-            double cc[3] = {0.0, 0.0, 0.0};
-            if (P.has_track) track_eval(P.track, ts, cc);
-            double g[3], H[6];
-            const double xs[3] = {ys[0] - cc[0], ys[1] - cc[1], ys[2] - cc[2]};
-            pot_grad<double, double, true>(P, ys, xs, g, H);
+            double g[3], r[19];
+            base_stage<ORD>(P, ys, t + cs[s] * h, g, r);
             k[s][0] = ys[3];
             k[s][1] = ys[4];
             k[s][2] = ys[5];
             k[s][3] = -g[0];
             k[s][4] = -g[1];
             k[s][5] = -g[2];
-            R* r = rec + 9 * s;
-            r[0] = (R)ys[0];
-            r[1] = (R)ys[1];
-            r[2] = (R)ys[2];
-            // tidal tensor T = -H  (xx, yy, zz, xy, xz, yz)
+            R* o = rec + SL * s;
 #pragma unroll
-            for (int c = 0; c < 6; ++c) r[3 + c] = (R)(-H[c]);
+            for (int c = 0; c < SL; ++c) o[c] = (R)r[c];
         }
 #pragma unroll
         for (int c = 0; c < 6; ++c)
@@ -139,6 +173,30 @@ __device__ __forceinline__ void load_stage(const double* p, double r[9]) {
     r[8] = p[8];
 }
 
+// Hessian of one subhalo's potential at rel (xx yy zz xy xz yz)
+template <class R>
+__device__ __forceinline__ void subhalo_hess(int kind, R Gm, R a, const R rel[3], R Hs[6]) {
+    const R r2 = rel[0] * rel[0] + rel[1] * rel[1] + rel[2] * rel[2];
+    R g, gr;  // grad = g rel, H = g I + gr rel rel^T
+    if (kind == SS_SH_PLUMMER) {
+        const R id = s_rsqrt(r2 + a * a);
+        const R id2 = id * id, id3 = id2 * id;
+        g = Gm * id3;
+        gr = R(-3) * Gm * id3 * id2;
+    } else {
+        const R r = s_sqrt(r2);
+        const R ir = s_rcp(r), ira = s_rcp(r + a);
+        g = Gm * ir * ira * ira;
+        gr = -Gm * (R(3) * r + a) * ir * ir * ir * ira * ira * ira;
+    }
+    Hs[0] = g + gr * rel[0] * rel[0];
+    Hs[1] = g + gr * rel[1] * rel[1];
+    Hs[2] = g + gr * rel[2] * rel[2];
+    Hs[3] = gr * rel[0] * rel[1];
+    Hs[4] = gr * rel[0] * rel[2];
+    Hs[5] = gr * rel[1] * rel[2];
+}
+
 template <class R, int NCOL>
 __device__ __forceinline__ void pert_rhs(const R* recp, const R U[NCOL], int kind, R Gm, R a, const R P0[3],
                                          const R V[3], R trel, R tau0, R window, R K[NCOL]) {
@@ -148,13 +206,34 @@ __device__ __forceinline__ void pert_rhs(const R* recp, const R U[NCOL], int kin
 #pragma unroll
     for (int i = 0; i < 3; ++i) rel[i] = rec[i] - (P0[i] + V[i] * trel);
     R gphi[3], gdphi[3];
-    subhalo_grad<R, NCOL == 12>(kind, Gm, a, rel, gphi, gdphi);
+    subhalo_grad<R, NCOL >= 12>(kind, Gm, a, rel, gphi, gdphi);
     // window: |t - t0_s| < t_window
     R on = fabs(trel - tau0) < window ? R(1) : R(0);
     const R* T = rec + 3;
+    if constexpr (NCOL == 18) {
+        // second order in the subhalo mass (fields.py:260-320):
+        //   d(x2)/dt = v2,  d(v2)/dt = T x2 + x1^T (d2a/dx2) x1 - H_s x1
+        const R* D = recp + 9;  // d2a: xxx xxy xxz xyy xyz xzz yyy yyz yzz zzz
+        const R* x1 = U;
+        const R* x2 = U + 12;
+        R Hs[6];
+        subhalo_hess<R>(kind, Gm, a, rel, Hs);
+        const R x0s = x1[0] * x1[0], x1s = x1[1] * x1[1], x2s = x1[2] * x1[2];
+        const R x01 = x1[0] * x1[1], x02 = x1[0] * x1[2], x12 = x1[1] * x1[2];
+        // Q_i = sum_jk d2a_ijk x1_j x1_k with d2a symmetric
+        const R Qx = D[0] * x0s + D[3] * x1s + D[5] * x2s + R(2) * (D[1] * x01 + D[2] * x02 + D[4] * x12);
+        const R Qy = D[1] * x0s + D[6] * x1s + D[8] * x2s + R(2) * (D[3] * x01 + D[4] * x02 + D[7] * x12);
+        const R Qz = D[2] * x0s + D[7] * x1s + D[9] * x2s + R(2) * (D[4] * x01 + D[5] * x02 + D[8] * x12);
+        K[12] = U[15];
+        K[13] = U[16];
+        K[14] = U[17];
+        K[15] = Qx + (T[0] * x2[0] + T[3] * x2[1] + T[4] * x2[2]) - on * (Hs[0] * x1[0] + Hs[3] * x1[1] + Hs[4] * x1[2]);
+        K[16] = Qy + (T[3] * x2[0] + T[1] * x2[1] + T[5] * x2[2]) - on * (Hs[3] * x1[0] + Hs[1] * x1[1] + Hs[5] * x1[2]);
+        K[17] = Qz + (T[4] * x2[0] + T[5] * x2[1] + T[2] * x2[2]) - on * (Hs[4] * x1[0] + Hs[5] * x1[1] + Hs[2] * x1[2]);
+    }
     // T: xx yy zz xy xz yz
 #pragma unroll
-    for (int b = 0; b < NCOL / 6; ++b) {
+    for (int b = 0; b < (NCOL == 18 ? 2 : NCOL / 6); ++b) {
         const R* x1 = U + 6 * b;
         K[6 * b + 0] = U[6 * b + 3];
         K[6 * b + 1] = U[6 * b + 4];
@@ -175,7 +254,9 @@ static constexpr int PERT_STEPS_STAGED = 16;
 
 template <class R, int NCOL>
 __global__ void __launch_bounds__(128) pert_response_kernel(ShDev sh, PertArgs a, int sblocks) {
-    __shared__ __align__(16) R srec[PERT_STEPS_STAGED][6][12];
+    constexpr int ORD = NCOL == 18 ? 2 : 1;
+    constexpr int RL = rec_len(ORD), SL = stage_len(ORD), SW = ORD == 2 ? 20 : 12;
+    __shared__ __align__(16) R srec[PERT_STEPS_STAGED][6][SW];
     const int64_t i = blockIdx.x / sblocks;          // particle within the chunk
     const int sb = blockIdx.x - (int)(i * sblocks);
     const int s_raw = sb * blockDim.x + threadIdx.x;  // subhalo
@@ -185,7 +266,7 @@ __global__ void __launch_bounds__(128) pert_response_kernel(ShDev sh, PertArgs a
     const int64_t p = a.p0 + i;
     const int start = (int)pert_start(p, a.ppr, a.spr);
     const R* rec = reinterpret_cast<const R*>(a.table) +
-                   (pert_offset(p, a.ppr, a.spr, a.n_steps) - pert_offset(a.p0, a.ppr, a.spr, a.n_steps)) * REC;
+                   (pert_offset(p, a.ppr, a.spr, a.n_steps) - pert_offset(a.p0, a.ppr, a.spr, a.n_steps)) * RL;
     // subhalo line relative to the run start t0: P0 + V (t - t0)
     const double tau = a.t0 - sh.t0[s];
     const R P0[3] = {(R)(sh.x0[3 * s] + sh.v[3 * s] * tau), (R)(sh.x0[3 * s + 1] + sh.v[3 * s + 1] * tau),
@@ -213,12 +294,12 @@ __global__ void __launch_bounds__(128) pert_response_kernel(ShDev sh, PertArgs a
     }
     const R h = (R)a.dt;
     const R cs[6] = {R(0), R(SS_C2), R(SS_C3), R(SS_C4), R(SS_C5), R(1)};
-    for (int n0 = start; n0 < a.n_steps; n0 += PERT_STEPS_STAGED, rec += PERT_STEPS_STAGED * REC) {
+    for (int n0 = start; n0 < a.n_steps; n0 += PERT_STEPS_STAGED, rec += PERT_STEPS_STAGED * RL) {
       const int cnt = min(PERT_STEPS_STAGED, a.n_steps - n0);
       __syncthreads();  // the previous chunk has been consumed
-      for (int e = threadIdx.x; e < cnt * 54; e += blockDim.x) {
-          const int j = e / 54, r = e - 54 * j, st = r / 9, q = r - 9 * st;
-          srec[j][st][q] = rec[(int64_t)j * REC + r];
+      for (int e = threadIdx.x; e < cnt * 6 * SL; e += blockDim.x) {
+          const int j = e / (6 * SL), r = e - 6 * SL * j, st = r / SL, q = r - SL * st;
+          srec[j][st][q] = rec[(int64_t)j * RL + r];
       }
       __syncthreads();
       for (int j = 0; j < cnt; ++j) {
@@ -280,6 +361,41 @@ __global__ void subhalo_eval_kernel(ShDev sh, const double* __restrict__ xyz, in
     }
 }
 
+// The field itself at one point (MassRadiusPerturbation_OTF.term,
+// fields.py:174-206, and MassRadiusPerturbation_OTF_SecondOrder.term,
+// fields.py:284-320): y = [x0v0 (6), n_sh x ncol], dy the same layout.
+// One thread per subhalo evaluates the stage record at x0 and the same
+// pert_rhs as the response kernels; thread 0 writes the base derivative.
+template <int NCOL>
+__global__ void __launch_bounds__(128) pert_term_kernel(PotDev<double> P, ShDev sh, double t,
+                                                        const double* __restrict__ y, double* __restrict__ dy) {
+    constexpr int ORD = NCOL == 18 ? 2 : 1;
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= sh.n) return;
+    __align__(16) double r[20];
+    double g[3];
+    base_stage<ORD>(P, y, t, g, r);
+    if (s == 0) {
+        dy[0] = y[3];
+        dy[1] = y[4];
+        dy[2] = y[5];
+        dy[3] = -g[0];
+        dy[4] = -g[1];
+        dy[5] = -g[2];
+    }
+    // subhalo line relative to t: P0 + V (t' - t), evaluated at t' = t
+    const double tau = t - sh.t0[s];
+    const double P0[3] = {sh.x0[3 * s] + sh.v[3 * s] * tau, sh.x0[3 * s + 1] + sh.v[3 * s + 1] * tau,
+                          sh.x0[3 * s + 2] + sh.v[3 * s + 2] * tau};
+    const double V[3] = {sh.v[3 * s], sh.v[3 * s + 1], sh.v[3 * s + 2]};
+    double U[NCOL], K[NCOL];
+#pragma unroll
+    for (int c = 0; c < NCOL; ++c) U[c] = y[6 + s * NCOL + c];
+    pert_rhs<double, NCOL>(r, U, sh.kind, sh.G * sh.m[s], sh.a[s], P0, V, 0.0, sh.t0[s] - t, sh.t_window, K);
+#pragma unroll
+    for (int c = 0; c < NCOL; ++c) dy[6 + s * NCOL + c] = K[c];
+}
+
 static int prepare_subhalos(const ss_subhalos* in, double G, ShDev* out) {
     SS_CHECK_ARG(in != nullptr, "subhalos is NULL");
     SS_CHECK_ARG(in->n >= 1 && in->n <= (1 << 30), "subhalos: n must be in [1, 2^30]");
@@ -323,13 +439,13 @@ int64_t ss_pert_workspace_bytes(const ss_pert_cfg* cfg, int precision, int64_t p
     if (!cfg || (precision != 32 && precision != 64) || particles_per_chunk < 1 || cfg->n_steps < 0)
         return set_error(SS_ERR_INVALID_ARGUMENT, "bad arguments");
     // the first particles are the longest: n_steps records each
-    return particles_per_chunk * cfg->n_steps * REC * (precision == 64 ? 8 : 4);
+    return particles_per_chunk * cfg->n_steps * rec_len(cfg->ncol == 18 ? 2 : 1) * (precision == 64 ? 8 : 4);
 }
 
 static int pert_args(const ss_pert_cfg* cfg, int precision, PertArgs* a) {
     SS_CHECK_ARG(cfg != nullptr, "cfg is NULL");
     SS_CHECK_ARG(precision == 32 || precision == 64, "precision must be 32 or 64");
-    SS_CHECK_ARG(cfg->ncol == 6 || cfg->ncol == 12, "ncol must be 6 or 12");
+    SS_CHECK_ARG(cfg->ncol == 6 || cfg->ncol == 12 || cfg->ncol == 18, "ncol must be 6, 12 or 18");
     SS_CHECK_ARG(cfg->n_particles >= 0 && cfg->n_steps >= 0 && cfg->n_steps < (1LL << 30), "bad sizes");
     SS_CHECK_ARG(cfg->particles_per_release >= 1 && cfg->steps_per_release >= 0, "bad release layout");
     SS_CHECK_ARG(std::isfinite(cfg->dt) && cfg->dt != 0.0 && std::isfinite(cfg->t0), "dt must be finite, non-zero");
@@ -351,6 +467,30 @@ static int pert_args(const ss_pert_cfg* cfg, int precision, PertArgs* a) {
 }
 
 // response kernels over [0, N) in grid-sized chunks; a.table = the records of particle 0
+// response kernel for the run's precision and column count
+static void launch_response(const ShDev& S, const PertArgs& a, int precision, unsigned g2, int sblock, int sblocks,
+                            cudaStream_t st) {
+    if (precision == 64) {
+        if (a.ncol == 18) pert_response_kernel<double, 18><<<g2, sblock, 0, st>>>(S, a, sblocks);
+        else if (a.ncol == 12) pert_response_kernel<double, 12><<<g2, sblock, 0, st>>>(S, a, sblocks);
+        else pert_response_kernel<double, 6><<<g2, sblock, 0, st>>>(S, a, sblocks);
+    } else {
+        if (a.ncol == 18) pert_response_kernel<float, 18><<<g2, sblock, 0, st>>>(S, a, sblocks);
+        else if (a.ncol == 12) pert_response_kernel<float, 12><<<g2, sblock, 0, st>>>(S, a, sblocks);
+        else pert_response_kernel<float, 6><<<g2, sblock, 0, st>>>(S, a, sblocks);
+    }
+}
+
+static void launch_base(const PotDev<double>& P, const PertArgs& a, int precision, unsigned g1, cudaStream_t st) {
+    if (precision == 64) {
+        if (a.ncol == 18) pert_base_kernel<double, 2><<<g1, 64, 0, st>>>(P, a);
+        else pert_base_kernel<double, 1><<<g1, 64, 0, st>>>(P, a);
+    } else {
+        if (a.ncol == 18) pert_base_kernel<float, 2><<<g1, 64, 0, st>>>(P, a);
+        else pert_base_kernel<float, 1><<<g1, 64, 0, st>>>(P, a);
+    }
+}
+
 static int pert_response_launch(const ShDev& S, PertArgs a, int precision, cudaStream_t st) {
     const int sblock = 128;
     const int sblocks = (int)((S.n + sblock - 1) / sblock);
@@ -360,15 +500,8 @@ static int pert_response_launch(const ShDev& S, PertArgs a, int precision, cudaS
     for (int64_t p0 = 0; p0 < a.N; p0 += max_np) {
         a.p0 = p0;
         a.np = a.N - p0 < max_np ? a.N - p0 : max_np;
-        a.table = table0 + pert_offset(p0, a.ppr, a.spr, a.n_steps) * REC * esz;
-        const unsigned g2 = (unsigned)(a.np * sblocks);
-        if (precision == 64) {
-            if (a.ncol == 12) pert_response_kernel<double, 12><<<g2, sblock, 0, st>>>(S, a, sblocks);
-            else pert_response_kernel<double, 6><<<g2, sblock, 0, st>>>(S, a, sblocks);
-        } else {
-            if (a.ncol == 12) pert_response_kernel<float, 12><<<g2, sblock, 0, st>>>(S, a, sblocks);
-            else pert_response_kernel<float, 6><<<g2, sblock, 0, st>>>(S, a, sblocks);
-        }
+        a.table = table0 + pert_offset(p0, a.ppr, a.spr, a.n_steps) * rec_len(a.ncol == 18 ? 2 : 1) * esz;
+        launch_response(S, a, precision, (unsigned)(a.np * sblocks), sblock, sblocks, st);
         SS_LAUNCH_CHECK();
     }
     return SS_OK;
@@ -385,7 +518,7 @@ int ss_pert_response(const ss_potential* base, const ss_subhalos* sh, const ss_p
     if (rc) return rc;
     SS_CHECK_ARG(cfg != nullptr, "cfg is NULL");
     SS_CHECK_ARG(precision == 32 || precision == 64, "precision must be 32 or 64");
-    SS_CHECK_ARG(cfg->ncol == 6 || cfg->ncol == 12, "ncol must be 6 or 12");
+    SS_CHECK_ARG(cfg->ncol == 6 || cfg->ncol == 12 || cfg->ncol == 18, "ncol must be 6, 12 or 18");
     SS_CHECK_ARG(cfg->n_particles >= 0 && cfg->n_steps >= 0 && cfg->n_steps < (1LL << 30), "bad sizes");
     SS_CHECK_ARG(cfg->particles_per_release >= 1 && cfg->steps_per_release >= 0, "bad release layout");
     SS_CHECK_ARG(std::isfinite(cfg->dt) && cfg->dt != 0.0 && std::isfinite(cfg->t0), "dt must be finite, non-zero");
@@ -395,7 +528,7 @@ int ss_pert_response(const ss_potential* base, const ss_subhalos* sh, const ss_p
     int64_t n_rel = (cfg->n_particles + cfg->particles_per_release - 1) / cfg->particles_per_release;
     SS_CHECK_ARG((n_rel - 1) * (int64_t)cfg->steps_per_release <= cfg->n_steps, "last release starts after n_steps");
     const int64_t esz = precision == 64 ? 8 : 4;
-    const int64_t rec_bytes = REC * esz;
+    const int64_t rec_bytes = rec_len(cfg->ncol == 18 ? 2 : 1) * esz;
     const int64_t cap_records = workspace ? workspace_bytes / rec_bytes : 0;
     if (cfg->n_steps > 0 && cap_records < cfg->n_steps)
         return set_error(SS_ERR_WORKSPACE, "workspace of >= %lld bytes needed (one particle), %lld given",
@@ -438,17 +571,9 @@ int ss_pert_response(const ss_potential* base, const ss_subhalos* sh, const ss_p
         a.np = p1 - p0;
         unsigned g1 = (unsigned)((a.np + 63) / 64);
         unsigned g2 = (unsigned)(a.np * sblocks);
-        if (precision == 64) {
-            pert_base_kernel<double><<<g1, 64, 0, st>>>(P, a);
-            SS_LAUNCH_CHECK();
-            if (a.ncol == 12) pert_response_kernel<double, 12><<<g2, sblock, 0, st>>>(S, a, sblocks);
-            else pert_response_kernel<double, 6><<<g2, sblock, 0, st>>>(S, a, sblocks);
-        } else {
-            pert_base_kernel<float><<<g1, 64, 0, st>>>(P, a);
-            SS_LAUNCH_CHECK();
-            if (a.ncol == 12) pert_response_kernel<float, 12><<<g2, sblock, 0, st>>>(S, a, sblocks);
-            else pert_response_kernel<float, 6><<<g2, sblock, 0, st>>>(S, a, sblocks);
-        }
+        launch_base(P, a, precision, g1, st);
+        SS_LAUNCH_CHECK();
+        launch_response(S, a, precision, g2, sblock, sblocks, st);
         SS_LAUNCH_CHECK();
         p0 = p1;
     }
@@ -459,7 +584,7 @@ int64_t ss_pert_track_bytes(const ss_pert_cfg* cfg, int precision) {
     PertArgs a;
     int rc = pert_args(cfg, precision, &a);
     if (rc) return rc;
-    return pert_offset(a.N, a.ppr, a.spr, a.n_steps) * REC * (precision == 64 ? 8 : 4);
+    return pert_offset(a.N, a.ppr, a.spr, a.n_steps) * rec_len(a.ncol == 18 ? 2 : 1) * (precision == 64 ? 8 : 4);
 }
 
 int ss_pert_base_track(const ss_potential* base, const ss_pert_cfg* cfg, int precision, const double* base_ics,
@@ -482,8 +607,7 @@ int ss_pert_base_track(const ss_potential* base, const ss_pert_cfg* cfg, int pre
     a.np = a.N;
     cudaStream_t st = (cudaStream_t)stream;
     const unsigned g1 = (unsigned)((a.N + 63) / 64);
-    if (precision == 64) pert_base_kernel<double><<<g1, 64, 0, st>>>(P, a);
-    else pert_base_kernel<float><<<g1, 64, 0, st>>>(P, a);
+    launch_base(P, a, precision, g1, st);
     SS_LAUNCH_CHECK();
     return SS_OK;
 }
@@ -504,6 +628,26 @@ int ss_pert_response_track(const ss_subhalos* sh, double G, const ss_pert_cfg* c
     a.pert_out = pert_out;
     a.table = const_cast<void*>(track);
     return pert_response_launch(S, a, precision, (cudaStream_t)stream);
+}
+
+int ss_pert_term(const ss_potential* base, const ss_subhalos* sh, int ncol, double t, const double* y, double* dy,
+                 void* stream) {
+    PotDev<double> P;
+    int rc = prepare_potential<double>(base, &P, false);
+    if (rc) return rc;
+    ShDev S;
+    rc = prepare_subhalos(sh, base->G, &S);
+    if (rc) return rc;
+    SS_CHECK_ARG(ncol == 6 || ncol == 12 || ncol == 18, "ncol must be 6, 12 or 18");
+    SS_CHECK_ARG(std::isfinite(t), "t must be finite");
+    SS_CHECK_ARG(y != nullptr && dy != nullptr, "NULL buffer");
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned g = (unsigned)((S.n + 127) / 128);
+    if (ncol == 18) pert_term_kernel<18><<<g, 128, 0, st>>>(P, S, t, y, dy);
+    else if (ncol == 12) pert_term_kernel<12><<<g, 128, 0, st>>>(P, S, t, y, dy);
+    else pert_term_kernel<6><<<g, 128, 0, st>>>(P, S, t, y, dy);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
 }
 
 }  // extern "C"

@@ -1,7 +1,8 @@
 """Vector fields and their integrator — the reference's fields.py API.
 
 Supported fields (jnibauer/streamsculptor fields.py): hamiltonian_field
-(101-113) and MassRadiusPerturbation_OTF (159-206).  `term` evaluates the
+(101-113), MassRadiusPerturbation_OTF (159-206), MassRadiusPerturbation_Interp
+(208-257) and MassRadiusPerturbation_OTF_SecondOrder (260-320).  `term` evaluates the
 field on the GPU; `integrate_field` (35-99) dispatches to the fixed-step
 Dopri5 kernels (ss_orbit_f64 / ss_pert_response).  Other fields (N-body,
 MW-LMC, custom Python callables) have no GPU implementation and raise.
@@ -72,6 +73,31 @@ class MassRadiusPerturbation_Interp(MassRadiusPerturbation_OTF):
         return super().term(t, [w.reshape(6), coords], args)[1]
 
 
+class MassRadiusPerturbation_OTF_SecondOrder:
+    """Second order in subhalo mass with the first-order radius response
+    (fields.py:260-320).  coords = [x0v0 (6), first (N_sh, 12), second
+    (N_sh, 6)]; term returns the same pytree:
+      d(x2)/dt = v2,  d(v2)/dt = T x2 + (d2a/dx2 : x1 x1) + dapert/dx x1,
+    with dapert/dx = -Hessian of each subhalo's potential, as the reference
+    writes it.  Evaluated on the GPU by ss_pert_term (FP64, third
+    derivatives of the base potential by forward-mode differentiation of its
+    analytic Hessian)."""
+
+    def __init__(self, perturbation_generator):
+        self.pertgen = perturbation_generator
+        self.potential_base = perturbation_generator.potential_base
+
+    def term(self, t, coords, args=None):
+        g = self.pertgen
+        x0v0 = f64(coords[0]).reshape(6)
+        ns = int(g.sh_table.m.shape[0])
+        d = torch.cat([f64(coords[1]).reshape(ns, 12), f64(coords[2]).reshape(ns, 6)], dim=1)
+        y = torch.cat([x0v0, d.reshape(-1)])
+        dy = _core.pert_term(g.potential_base._desc(), g.sh_table, 18, float(host64(t)), y)
+        r = dy[6:].reshape(ns, 18)
+        return [dy[:6], r[:, :12], r[:, 12:]]
+
+
 def _t_span(ts_h, backwards_int, t0, t1):
     """t0/t1 selection of integrate_field (fields.py:58-80)."""
     if float(t0) != float(t1):
@@ -100,14 +126,17 @@ def integrate_field(w0=None, ts=None, dense=False, solver=None, field=None, args
         out = _core.orbit(field.pot._desc(), w.reshape(-1, 6).contiguous(), ta, h, n, 1)
         ys = out[:, torch.as_tensor(idx, device=out.device)]
         return Solution(torch.as_tensor(ts_h, device=ys.device), ys[0] if single else ys)
-    if isinstance(field, MassRadiusPerturbation_OTF):
+    if isinstance(field, (MassRadiusPerturbation_OTF, MassRadiusPerturbation_OTF_SecondOrder)):
         g = field.pertgen
         base = f64(w0[0]).reshape(-1, 6).contiguous()
+        second = isinstance(field, MassRadiusPerturbation_OTF_SecondOrder)
         pert = f64(w0[1])
         single = pert.ndim == 2
         N = base.shape[0]
         ns = int(g.sh_table.m.shape[0])
         pert = pert.reshape(N, ns, -1)
+        if second:
+            pert = torch.cat([pert, f64(w0[2]).reshape(N, ns, 6)], dim=2).contiguous()
         cfg = _abi.ss_pert_cfg()
         cfg.t0, cfg.dt, cfg.n_steps, cfg.n_particles = ta, h, n, N
         cfg.particles_per_release, cfg.steps_per_release = 1, 0
@@ -116,9 +145,9 @@ def integrate_field(w0=None, ts=None, dense=False, solver=None, field=None, args
         _, out = _core.pert_response(g.potential_base._desc(), g.sh_table, cfg, int(precision), base, pert)
         pys = out[torch.as_tensor(idx, device=out.device)]  # [len(ts), N, ns, ncol]
         bys = _core.orbit(g.potential_base._desc(), base, ta, h, n, 1)[:, torch.as_tensor(idx, device=out.device)]
-        if single:
-            return Solution(torch.as_tensor(ts_h, device=out.device), [bys[0], pys[:, 0]])
-        return Solution(torch.as_tensor(ts_h, device=out.device), [bys, pys.transpose(0, 1)])
+        pys = pys[:, 0] if single else pys.transpose(0, 1)
+        parts = [pys[..., :12], pys[..., 12:]] if second else [pys]
+        return Solution(torch.as_tensor(ts_h, device=out.device), [bys[0] if single else bys] + parts)
     raise NotImplementedError(f"field {type(field).__name__} has no GPU implementation")
 
 
@@ -129,4 +158,5 @@ class CustomField:
         self.term = term
 
 
-__all__ = ["integrate_field", "hamiltonian_field", "MassRadiusPerturbation_OTF", "CustomField"]
+__all__ = ["integrate_field", "hamiltonian_field", "MassRadiusPerturbation_OTF", "MassRadiusPerturbation_Interp",
+           "MassRadiusPerturbation_OTF_SecondOrder", "CustomField"]

@@ -240,6 +240,153 @@ class GenerateMassRadiusPerturbation_Chen25(Potential):
         return torch.cat([lead, trail], dim=0)
 
 
+class CustomBaseStreamModel(Potential):
+    """Base stream with a caller-given release (perturbative.py:299-364):
+    particle i starts at the progenitor's state at ts[i] plus (pos_rel[i],
+    vel_rel[i]) (custom_release_model, streamhelpers.py:187-198), so the
+    release Jacobian d(ICs)/d(progenitor w) is the identity."""
+
+    def __init__(self, potential_base=None, prog_w0=None, ts=None, pos_rel=None, vel_rel=None, solver=None,
+                 units=None, dense=False, cpu=True, *, dt=None, **kwargs):
+        super().__init__(units, {"potential_base": potential_base, "prog_w0": prog_w0, "ts": ts, "pos_rel": pos_rel,
+                                 "vel_rel": vel_rel, "solver": solver, "dense": dense, "cpu": cpu})
+        if dense:
+            raise NotImplementedError("dense stream interpolants are replaced by snapshots")
+        _core.check_solver(solver)
+        self.potential_base = potential_base
+        ts_h = host64(ts).reshape(-1)
+        self._ts_h = ts_h
+        ws, self._h, self._spr = potential_base._prog_orbit(ts_h, prog_w0, dt)
+        self.prog_at_ts = ws
+        self.prog_loc_fwd = ws
+        rel = torch.cat([f64(pos_rel).reshape(-1, 3), f64(vel_rel).reshape(-1, 3)], dim=1).to(ws.device)
+        if rel.shape[0] != len(ts_h):
+            raise ValueError("pos_rel / vel_rel need one row per release time")
+        self.streamICs = (ws + rel).contiguous()  # [len(ts), 6]
+        self.IDs = torch.arange(len(ts_h), device=ws.device)
+        self.dRel_dIC = self.release_func_jacobian()
+        self.stream_interp = None
+
+    def release_func_jacobian(self):
+        """[len(ts), 6, 6]: identity (perturbative.py:348-364)."""
+        n = len(self._ts_h)
+        return torch.eye(6, dtype=torch.float64, device=self.streamICs.device).expand(n, 6, 6).contiguous()
+
+    def gen_stream(self, *, precision="f64"):
+        """Particles 0..len(ts)-2 from their release to ts[-1] (perturbative.py:336-345): [len(ts)-1, 6]."""
+        n_rel = len(self._ts_h) - 1
+        cfg = _abi.ss_stream_cfg()
+        cfg.t0, cfg.dt = float(self._ts_h[0]), float(self._h)
+        cfg.n_steps, cfg.n_particles = self._spr * n_rel, n_rel
+        cfg.particles_per_release, cfg.steps_per_release = 1, self._spr
+        final, _ = _core.stream(self.potential_base._desc(), cfg, self.streamICs[:n_rel].contiguous(), precision)
+        return final
+
+
+class GenerateMassRadiusPerturbation_CustomBase(Potential):
+    """First-order mass / radius response of a CustomBaseStreamModel stream
+    (perturbative.py:367-487): one particle per release time, perturbation
+    ICs = dRel_dIC @ the progenitor's backward response."""
+
+    _ncol = 12
+
+    def __init__(self, potential_base, potential_perturbation, potential_structural, BaseStreamModel=None, units=None,
+                 *, precision=64, **kwargs):
+        super().__init__(units, {"potential_base": potential_base, "potential_perturbation": potential_perturbation,
+                                 "potential_structural": potential_structural, "BaseStreamModel": BaseStreamModel})
+        self.potential_base = potential_base
+        self.potential_perturbation = potential_perturbation
+        self.gradientPotentialBase = potential_base.gradient
+        self.gradientPotentialPerturbation_per_SH = potential_perturbation.gradient_per_SH
+        self.gradientPotentialStructural_per_SH = potential_structural.gradient_per_SH
+        self.sh_table = potential_perturbation.table()
+        if not self.sh_table.same_lines(potential_structural.table()):
+            raise NotImplementedError("perturbation and structural potentials must share one subhalo table")
+        self.precision = int(precision)
+        self.base_stream = BaseStreamModel
+        self.num_pert = int(self.sh_table.m.shape[0])
+        self.jump_ts = None
+        self.prog_fieldICs_all = self._prog_response()
+        self.prog_fieldICs = self.prog_fieldICs_all[:, :, :12]
+        self.perturbation_ICs = self.compute_perturbation_ICs()
+        self.base_realspace_ICs = BaseStreamModel.streamICs
+
+    def _prog_response(self):
+        """Progenitor response backwards from the observation time, zero there
+        (perturbative.py:389-397): [len(ts), N_sh, ncol], time increasing."""
+        b = self.base_stream
+        n = len(b._ts_h)
+        cfg = _abi.ss_pert_cfg()
+        cfg.t0, cfg.dt = float(b._ts_h[-1]), -float(b._h)
+        cfg.n_steps, cfg.n_particles = b._spr * (n - 1), 1
+        cfg.particles_per_release, cfg.steps_per_release = 1, 0
+        cfg.ncol, cfg.save_stride = self._ncol, b._spr
+        _, out = _core.pert_response(self.potential_base._desc(), self.sh_table, cfg, 64,
+                                     b.prog_loc_fwd[-1:].contiguous(), None)
+        return torch.flip(out[:, 0], dims=[0])
+
+    def compute_perturbation_ICs(self):
+        """perturbative.py:410-420: [N_star, N_sh, 12]."""
+        J = self.base_stream.dRel_dIC
+        pf = self.prog_fieldICs_all
+        return torch.cat([torch.einsum("ijk,ilk->ilj", J, pf[:, :, 0:6]),
+                          torch.einsum("ijk,ilk->ilj", J, pf[:, :, 6:12])], dim=2)
+
+    def compute_base_stream(self, cpu=True):
+        return self.base_stream.gen_stream()
+
+    def _response(self, pert, prec):
+        b = self.base_stream
+        nrel = len(b._ts_h) - 1
+        cfg = _abi.ss_pert_cfg()
+        cfg.t0, cfg.dt = float(b._ts_h[0]), float(b._h)
+        cfg.n_steps, cfg.n_particles = b._spr * nrel, nrel
+        cfg.particles_per_release, cfg.steps_per_release = 1, b._spr
+        cfg.ncol, cfg.save_stride = self._ncol, 0
+        base_out, out = _core.pert_response(self.potential_base._desc(), self.sh_table, cfg, prec,
+                                            self.base_realspace_ICs[:nrel].contiguous(), pert[:nrel].contiguous())
+        return base_out, out[0]
+
+    def compute_perturbation_OTF(self, cpu=True, solver=None, rtol=1e-6, atol=1e-6, dtmin=0.05, max_steps=10_000,
+                                 dtmax=None, *, precision=None):
+        """perturbative.py:424-456: [x0v0 [len(ts)-1, 6], derivs [len(ts)-1, N_sh, 12]]."""
+        _core.check_solver(solver)
+        base_out, d = self._response(self.perturbation_ICs, int(precision or self.precision))
+        return [base_out, d]
+
+
+class GenerateMassRadiusPerturbation_CustomBase_SecondOrder(GenerateMassRadiusPerturbation_CustomBase):
+    """Second order in the subhalo mass with the first-order radius response
+    (perturbative.py:491-585, field fields.py:260-320).  The progenitor's
+    response and every particle's carry 18 columns per subhalo: the 12
+    first-order ones and (x2, v2).  compute_perturbation_OTF returns
+    [x0v0 [len(ts)-1, 6], first [len(ts)-1, N_sh, 12], second [len(ts)-1, N_sh, 6]]."""
+
+    _ncol = 18
+
+    def __init__(self, potential_base, potential_perturbation, potential_structural, BaseStreamModel=None, units=None,
+                 **kwargs):
+        super().__init__(potential_base, potential_perturbation, potential_structural, BaseStreamModel, units,
+                         **kwargs)
+        self.prog_fieldICs_first_order_mass = self.prog_fieldICs_all[:, :, :12]
+        self.prog_fieldICs_second_order_mass = self.prog_fieldICs_all[:, :, 12:]
+
+    def compute_perturbation_ICs(self):
+        """perturbative.py:537-550: [[N_star, N_sh, 12], [N_star, N_sh, 6]]."""
+        J = self.base_stream.dRel_dIC
+        pf = self.prog_fieldICs_all
+        first = torch.cat([torch.einsum("ijk,ilk->ilj", J, pf[:, :, 0:6]),
+                           torch.einsum("ijk,ilk->ilj", J, pf[:, :, 6:12])], dim=2)
+        return [first, torch.einsum("ijk,ilk->ilj", J, pf[:, :, 12:18])]
+
+    def compute_perturbation_OTF(self, cpu=False, solver=None, rtol=1e-8, atol=1e-8, dtmin=0.05, max_steps=10_000,
+                                 dtmax=None, *, precision=None):
+        _core.check_solver(solver)
+        pert = torch.cat(self.perturbation_ICs, dim=2)
+        base_out, d = self._response(pert, int(precision or self.precision))
+        return [base_out, d[:, :, :12], d[:, :, 12:]]
+
+
 class GenerateMassPerturbation(GenerateMassRadiusPerturbation):
     """Mass-only response (6 columns per subhalo) at fixed subhalo radius
     (perturbative.py:224-241; the reference's constructor references an
@@ -252,4 +399,5 @@ class GenerateMassPerturbation(GenerateMassRadiusPerturbation):
 
 
 __all__ = ["BaseStreamModel", "GenerateMassRadiusPerturbation", "GenerateMassPerturbation", "BaseStreamModelChen25",
-           "GenerateMassRadiusPerturbation_Chen25"]
+           "GenerateMassRadiusPerturbation_Chen25", "CustomBaseStreamModel", "GenerateMassRadiusPerturbation_CustomBase",
+           "GenerateMassRadiusPerturbation_CustomBase_SecondOrder"]

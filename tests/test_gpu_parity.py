@@ -252,12 +252,15 @@ def _pert_case(oracle, N=24, nsh=7, n_steps=120, seed=4):
               v=rng.normal(0, 0.12, (nsh, 3)), t0=rng.uniform(0, 100, nsh), t_window=60.0)
     orc = oracle.HostModel(oracle.mw3(), subhalos=sh)
     base = PROG_WF + rng.normal(0, 0.3, (N, 6)) * np.array([1, 1, 1, 0.01, 0.01, 0.01])
-    pert = rng.normal(0, 1e-3, (N, nsh, 12))
+    pert = rng.normal(0, 1e-3, (N, nsh, 18))
     return sh, orc, base, pert
 
 
-@pytest.mark.parametrize("ncol", [12, 6])
+@pytest.mark.parametrize("ncol", [12, 6, 18])
 def test_pert_response_f64_and_f32(ss, oracle, ncol):
+    """First-order response (6 mass or 12 mass + radius columns) and the
+    second-order mass response (18 columns: + x2, v2 of
+    MassRadiusPerturbation_OTF_SecondOrder, fields.py:260-320)."""
     from streamsculptor_gb300 import _core
     sh, orc, base, pert = _pert_case(oracle)
     pert = np.ascontiguousarray(pert[:, :, :ncol])
@@ -286,10 +289,78 @@ def test_pert_field_term_matches_oracle(ss, oracle):
     gen = perturbative.GenerateMassRadiusPerturbation(mw3_gpu(ss), pot_sh, pot_st)
     f = fields.MassRadiusPerturbation_OTF(gen)
     for t in (10.0, 55.0):
-        d0, d1 = f.term(t, [base[0], pert[0]])
-        o0, o1 = oracle.pert_term(orc, t, base[0], pert[0])
+        d0, d1 = f.term(t, [base[0], pert[0][:, :12]])
+        o0, o1 = oracle.pert_term(orc, t, base[0], pert[0][:, :12])
         assert rel_err(np64(d0), o0) < 1e-12
         assert rel_err(np64(d1), o1) < 1e-11
+
+
+@pytest.mark.parametrize("ncol", [6, 12, 18])
+def test_pert_term_kernel_matches_oracle(ss, oracle, ncol):
+    """ss_pert_term (the field at one point) for the first- and second-order
+    layouts, and the second-order field class built on it."""
+    from types import SimpleNamespace
+
+    from streamsculptor_gb300 import _core, fields
+    sh, orc, base, pert = _pert_case(oracle, N=1)
+    table = _core.SubhaloTable(1, *(_core.f64(sh[k]) for k in ("m", "a")), _core.f64(sh["x0"]), _core.f64(sh["v"]),
+                               _core.f64(sh["t0"]), sh["t_window"])
+    pot = mw3_gpu(ss)
+    u = pert[0][:, :ncol]
+    for t in (10.0, 55.0):
+        dy = np64(_core.pert_term(pot._desc(), table, ncol, t, _core.f64(np.concatenate([base[0], u.ravel()]))))
+        o0, o1 = oracle.pert_term(orc, t, base[0], u, ncol=ncol)
+        assert rel_err(dy[:6], o0) < 1e-12
+        d1 = dy[6:].reshape(-1, ncol)
+        assert rel_err(d1[:, :6], o1[:, :6]) < 1e-11
+        if ncol >= 12:
+            assert rel_err(d1[:, 6:12], o1[:, 6:12]) < 1e-11
+        if ncol == 18:
+            assert rel_err(d1[:, 12:], o1[:, 12:]) < 1e-11
+            f = fields.MassRadiusPerturbation_OTF_SecondOrder(SimpleNamespace(potential_base=pot, sh_table=table))
+            c0, c1, c2 = f.term(t, [base[0], u[:, :12], u[:, 12:]])
+            assert rel_err(np64(c1), o1[:, :12]) < 1e-11 and rel_err(np64(c2), o1[:, 12:]) < 1e-11
+
+
+def test_custom_base_second_order_matches_oracle(ss, oracle):
+    """GenerateMassRadiusPerturbation_CustomBase(_SecondOrder) on a
+    CustomBaseStreamModel (perturbative.py:299-585): the progenitor's 18-column
+    response integrated backwards from zero at t_obs, the identity release
+    Jacobian, every particle's response forward to t_obs; the first-order
+    generator gives the same 12 columns."""
+    from streamsculptor_gb300 import perturbative, potential as P
+    n_rel = 60
+    orc, back, ts, _ = _c1_setup(oracle, n_rel=n_rel)
+    rng = np.random.default_rng(31)
+    pos_rel = rng.normal(0, 0.05, (n_rel + 1, 3))
+    vel_rel = rng.normal(0, 0.002, (n_rel + 1, 3))
+    ws = oracle.orbit(orc, back, ts[0], 1.0, n_rel, 1)[0]
+    sh = dict(kind=1, m=np.array([3e6, 2e7, 8e6]), a=np.array([0.3, 0.6, 0.4]),
+              x0=ws[[20, 40, 50], :3] + rng.normal(0, 0.5, (3, 3)), v=rng.normal(0, 0.1, (3, 3)),
+              t0=np.array([ts[20], ts[40], ts[50]]), t_window=30.0)
+    args = (sh["m"], sh["a"], sh["x0"], sh["v"], sh["t0"], sh["t_window"])
+    pot_sh = P.SubhaloLinePotential(*args, units=ss.usys)
+    pot_st = P.SubhaloLinePotential_dRadius(*args, units=ss.usys)
+    bsm = perturbative.CustomBaseStreamModel(mw3_gpu(ss), back, ts, pos_rel, vel_rel)
+    gen2 = perturbative.GenerateMassRadiusPerturbation_CustomBase_SecondOrder(mw3_gpu(ss), pot_sh, pot_st, bsm)
+    base, d1, d2 = gen2.compute_perturbation_OTF()
+    gen1 = perturbative.GenerateMassRadiusPerturbation_CustomBase(mw3_gpu(ss), pot_sh, pot_st, bsm)
+    b1, e1 = gen1.compute_perturbation_OTF()
+    ics = ws + np.concatenate([pos_rel, vel_rel], axis=1)
+    orc_sh = oracle.HostModel(oracle.mw3(), subhalos=sh)
+    _, prog = oracle.pert_response(orc_sh, ts[-1], -1.0, n_rel, ws[-1:], None, 1, 0, ncol=18, save_stride=1)
+    pf = np.ascontiguousarray(prog[::-1, 0])  # [n_rel + 1, n_sh, 18], time increasing
+    assert rel_err(np64(gen2.prog_fieldICs_all), pf) <= 1e-10
+    bo, po = oracle.pert_response(orc_sh, ts[0], 1.0, n_rel, ics[:-1], pf[:-1], 1, 1, ncol=18)
+    assert base.shape == (n_rel, 6) and d1.shape == (n_rel, 3, 12) and d2.shape == (n_rel, 3, 6)
+    assert phase_err(np64(base), bo) <= 1e-10
+    assert rel_err(np64(d1), po[0][..., :12]) <= 1e-9
+    assert rel_err(np64(d2), po[0][..., 12:]) <= 1e-9
+    assert np.abs(np64(d2)).max() > 0
+    assert phase_err(np64(b1), np64(base)) <= 1e-14
+    assert rel_err(np64(e1), np64(d1)) <= 1e-12
+    s0 = bsm.gen_stream()
+    assert phase_err(np64(s0), bo) <= 1e-10
 
 
 def test_linear_response_matches_nonlinear_difference(ss, oracle):

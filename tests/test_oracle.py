@@ -170,3 +170,38 @@ def test_track_slopes_restatement(oracle):
     s = oracle.track_slopes(knots, 0.5)
     assert np.allclose(s[1:-1], (knots[2:] - knots[:-2]) / 1.0)
     assert np.allclose(s[0], (knots[1] - knots[0]) / 0.5) and np.allclose(s[-1], (knots[-1] - knots[-2]) / 0.5)
+
+
+def test_second_order_term_matches_finite_differences(oracle):
+    """The 18-column term (MassRadiusPerturbation_OTF_SecondOrder.term,
+    fields.py:284-320): columns 0-11 equal the first-order term, dx2/dt = v2
+    and dv2/dt = T x2 + (d2a/dx2 : x1 x1) - Hess(Phi_s) x1, the third
+    derivatives and the subhalo Hessian checked against central differences
+    of the oracle's analytic Hessian and subhalo gradient."""
+    rng = np.random.default_rng(8)
+    nsh = 5
+    sh = dict(kind=1, m=10 ** rng.uniform(6, 8, nsh), a=rng.uniform(0.3, 1.0, nsh),
+              x0=PROG_WF[:3] + rng.normal(0, 2.0, (nsh, 3)), v=rng.normal(0, 0.12, (nsh, 3)),
+              t0=rng.uniform(0, 20, nsh), t_window=60.0)
+    m = oracle.HostModel(oracle.mw3(), subhalos=sh)
+    base = PROG_WF.copy()
+    u = rng.normal(0, 1.0, (nsh, 18))
+    t = 12.0
+    d0, d1 = oracle.pert_term(m, t, base, u, ncol=18)
+    e0, e1 = oracle.pert_term(m, t, base, u[:, :12], ncol=12)
+    assert np.array_equal(d0, e0) and np.array_equal(d1[:, :12], e1)
+    assert np.array_equal(d1[:, 12:15], u[:, 15:18])
+    mb = oracle.HostModel(oracle.mw3())  # the base potential alone
+    _, _, T0 = oracle.potential_eval(mb, base[None, :3], t)
+    T0 = -T0[0]
+    h = 1e-3
+    for s in range(nsh):
+        x1 = u[s, 0:3]
+        _, _, Hp = oracle.potential_eval(mb, (base[:3] + h * x1)[None], t)
+        _, _, Hm = oracle.potential_eval(mb, (base[:3] - h * x1)[None], t)
+        third = -(Hp[0] - Hm[0]) / (2 * h) @ x1
+        _, gp, _, _ = oracle.subhalo_eval(m, (base[:3] + h * x1)[None], t)
+        _, gm, _, _ = oracle.subhalo_eval(m, (base[:3] - h * x1)[None], t)
+        hs = (gp[0, s] - gm[0, s]) / (2 * h)
+        want = T0 @ u[s, 12:15] + third - hs
+        assert np.max(np.abs(d1[s, 15:18] - want)) <= 1e-6 * np.max(np.abs(want)), s
