@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define SS_ABI_VERSION 2
+#define SS_ABI_VERSION 3
 #define SS_MAX_COMPONENTS 16
 
 /* ---------------------------------------------------------------- status */
@@ -158,6 +158,18 @@ typedef struct ss_stream_cfg {
      * (0 = n_particles) written at the global index.  Zero for whole runs. */
     int64_t first_particle;
     int64_t snap_pitch;
+    /* Ensembles of independent streams (jax.vmap of gen_stream_vmapped_with_pert
+     * over subhalo parameters, examples/GD1_and_SubhaloFitting_GPU.ipynb):
+     * with stream_particles > 0 the particles form consecutive streams of
+     * stream_particles each, and the release layout above restarts in every
+     * stream (global particle q is particle q % stream_particles of stream
+     * q / stream_particles).  With subhalos_per_stream = k > 0, stream g feels
+     * only the rows [g k, (g + 1) k) of the potential's subhalo table.  Zero
+     * for a single stream.  The checkpoint / adjoint and surrogate paths take
+     * single streams only. */
+    int64_t stream_particles;
+    int32_t subhalos_per_stream;
+    int32_t reserved2;
 } ss_stream_cfg;
 
 typedef enum ss_release_model { SS_RELEASE_FARDAL = 0, SS_RELEASE_CHEN25 = 1 } ss_release_model;
@@ -222,6 +234,19 @@ int ss_potential_eval(const ss_potential* pot, const double* xyz, int64_t n,
 int ss_orbit_f64(const ss_potential* pot, const double* w0, int64_t n_orbits,
                  double t0, double dt, int64_t n_steps, int64_t save_every,
                  double* out, void* stream);
+
+/* Ensembles of orbits that differ in step or perturbation, one thread per
+ * orbit: orbit i starts at t0 from w0[i] and takes n_steps fixed Dopri5
+ * steps of dt[i] (dt_all when dt is NULL; either sign), and with
+ * subhalos_per_orbit = k > 0 feels only the rows [i k, (i + 1) k) of the
+ * potential's subhalo table.  out as ss_orbit_f64.  Replaces jax.vmap of
+ * integrate_orbit over orbits with their own end times (the back-integration
+ * of stream patches to each impact time, GenerateImpactParams.py:179) or
+ * their own subhalo (one perturbed progenitor per sample,
+ * examples/GD1_and_SubhaloFitting_GPU.ipynb). */
+int ss_orbit_ensemble_f64(const ss_potential* pot, const double* w0, int64_t n_orbits, double t0,
+                          const double* dt, double dt_all, int64_t n_steps, int64_t save_every,
+                          int32_t subhalos_per_orbit, double* out, void* stream);
 
 /* One orbit, parallel in time (multiple shooting with Newton's method): the
  * n_steps fixed Dopri5 steps are split into slices that are integrated in

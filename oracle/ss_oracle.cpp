@@ -751,9 +751,23 @@ void or_stream(const ss_potential* P, const ss_stream_cfg* cfg, const double* ic
     const float fnan = std::numeric_limits<float>::quiet_NaN();
 #pragma omp parallel for schedule(dynamic, 8)
     for (int64_t p = 0; p < N; ++p) {
-        HamRHS f{P};
+        // ensembles: particle p is particle p % stream_particles of stream
+        // p / stream_particles, which feels its own subhalo rows
+        const int64_t grp = cfg->stream_particles;
+        const int64_t pl = grp > 0 ? p % grp : p;
+        ss_potential Pl = *P;
+        if (cfg->subhalos_per_stream > 0) {
+            const int64_t k = cfg->subhalos_per_stream, o = (p / grp) * k;
+            Pl.subhalos.n = k;
+            Pl.subhalos.m += o;
+            Pl.subhalos.a += o;
+            Pl.subhalos.x0 += 3 * o;
+            Pl.subhalos.v += 3 * o;
+            Pl.subhalos.t0 += o;
+        }
+        HamRHS f{&Pl};
         std::vector<double> w;
-        int64_t start = (p / cfg->particles_per_release) * (int64_t)cfg->steps_per_release;
+        int64_t start = (pl / cfg->particles_per_release) * (int64_t)cfg->steps_per_release;
         double y[6];
         for (int i = 0; i < 6; ++i) y[i] = ics[6 * p + i];
         if (snaps) {

@@ -10,7 +10,7 @@ import ctypes as C
 import os
 import threading
 
-SS_ABI_VERSION = 2
+SS_ABI_VERSION = 3
 SS_MAX_COMPONENTS = 16
 
 SS_OK = 0
@@ -71,7 +71,8 @@ class ss_stream_cfg(C.Structure):
     _fields_ = [("t0", C.c_double), ("dt", C.c_double), ("n_steps", C.c_int64),
                 ("n_particles", C.c_int64), ("particles_per_release", C.c_int32),
                 ("steps_per_release", C.c_int32), ("snap_stride", C.c_int32), ("reserved", C.c_int32),
-                ("first_particle", C.c_int64), ("snap_pitch", C.c_int64)]
+                ("first_particle", C.c_int64), ("snap_pitch", C.c_int64),
+                ("stream_particles", C.c_int64), ("subhalos_per_stream", C.c_int32), ("reserved2", C.c_int32)]
 
 
 class ss_release_cfg(C.Structure):
@@ -106,6 +107,8 @@ SIGNATURES = {
     "ss_potential_eval": (C.c_int, [C.POINTER(ss_potential), VP, C.c_int64, VP, C.c_double, VP, VP, VP, VP]),
     "ss_orbit_f64": (C.c_int, [C.POINTER(ss_potential), VP, C.c_int64, C.c_double, C.c_double, C.c_int64,
                                C.c_int64, VP, VP]),
+    "ss_orbit_ensemble_f64": (C.c_int, [C.POINTER(ss_potential), VP, C.c_int64, C.c_double, VP, C.c_double,
+                                        C.c_int64, C.c_int64, C.c_int32, VP, VP]),
     "ss_orbit_shoot_workspace_bytes": (C.c_int64, [C.c_int64]),
     "ss_orbit_shoot_f64": (C.c_int, [C.POINTER(ss_potential), VP, C.c_double, C.c_double, C.c_int64, C.c_int64, VP,
                                      VP, C.c_int64, C.c_double, VP]),

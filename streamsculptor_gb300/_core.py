@@ -305,6 +305,24 @@ def orbit(P, w0: torch.Tensor, t0: float, dt: float, n_steps: int, save_every: i
     return out
 
 
+def orbit_ensemble(P, w0: torch.Tensor, t0: float, dt, n_steps: int, save_every: int = 0,
+                   subhalos_per_orbit: int = 0) -> torch.Tensor:
+    """Orbits with their own step (dt: a float, or [n] steps) and, for
+    subhalos_per_orbit = k > 0, their own subhalo rows [i k, (i + 1) k):
+    [n, n_steps // save_every + 1, 6] (save_every 0: start and end only)."""
+    n = w0.shape[0]
+    every = int(save_every) if save_every else max(int(n_steps), 1)
+    out = torch.empty(n, int(n_steps) // every + 1, 6, dtype=torch.float64, device=w0.device)
+    if torch.is_tensor(dt) or np.ndim(dt) > 0:
+        dts = f64(dt).reshape(n).contiguous()
+        dptr, dall = ptr(dts), 0.0
+    else:
+        dts, dptr, dall = None, None, float(dt)
+    _abi.call("ss_orbit_ensemble_f64", C.byref(P), ptr(w0.contiguous()), n, float(t0), dptr, dall, int(n_steps),
+              every, int(subhalos_per_orbit), ptr(out), stream_handle())
+    return out
+
+
 def is_static(P) -> bool:
     """True when the descriptor has no center-track component and no subhalos."""
     return P.subhalos.n == 0 and all(P.comp[i].center == _abi.SS_CENTER_ORIGIN for i in range(P.n_components))

@@ -415,8 +415,8 @@ int ss_stream_f32k_ckpt(const ss_potential* pot, const ss_stream_cfg* cfg, const
     PotDev<float> P;
     int rc = prepare_potential<float>(pot, &P, false);
     if (rc) return rc;
-    SS_CHECK_ARG(cfg != nullptr && cfg->first_particle == 0 && cfg->snap_pitch == 0,
-                 "the adjoint path runs whole streams (first_particle = snap_pitch = 0)");
+    SS_CHECK_ARG(cfg != nullptr && cfg->first_particle == 0 && cfg->snap_pitch == 0 && cfg->stream_particles == 0,
+                 "the adjoint path runs whole single streams (first_particle = snap_pitch = stream_particles = 0)");
     SS_CHECK_ARG(!P.has_track, "the adjoint supports static potentials (no center track) only");
     SS_CHECK_ARG(cfg && cfg->n_particles >= 0 && cfg->n_steps >= 0 && cfg->n_steps < (1LL << 30), "bad cfg");
     SS_CHECK_ARG(cfg->particles_per_release >= 1 && cfg->steps_per_release >= 0, "bad release layout");
@@ -455,8 +455,8 @@ int ss_stream_adjoint_f32(const ss_potential* pot, const ss_stream_cfg* cfg, con
     PotDev<float> P;
     int rc = prepare_potential<float>(pot, &P, false);
     if (rc) return rc;
-    SS_CHECK_ARG(cfg != nullptr && cfg->first_particle == 0 && cfg->snap_pitch == 0,
-                 "the adjoint path runs whole streams (first_particle = snap_pitch = 0)");
+    SS_CHECK_ARG(cfg != nullptr && cfg->first_particle == 0 && cfg->snap_pitch == 0 && cfg->stream_particles == 0,
+                 "the adjoint path runs whole single streams (first_particle = snap_pitch = stream_particles = 0)");
     for (int k = 0; k < P.n; ++k)
         SS_CHECK_ARG(P.c[k].kind != SS_SH_EXPANSION, "component %d: SS_SH_EXPANSION has no adjoint", k);
     SS_CHECK_ARG(!P.has_track, "the adjoint supports static potentials (no center track) only");

@@ -234,6 +234,31 @@ __global__ void __launch_bounds__(64) orbit_f64_kernel(PotDev<double> P, const d
     }
 }
 
+// Orbit o with its own step (dts[o], or dt_all) and, for k > 0, its own
+// subhalo rows [o k, (o + 1) k).
+template <class C>
+__global__ void __launch_bounds__(64) orbit_ensemble_kernel(PotDev<double> P, const double* __restrict__ w0,
+                                                            int64_t n_orbits, double t0, const double* __restrict__ dts,
+                                                            double dt_all, int64_t n_steps, int64_t save_every,
+                                                            int32_t k, double* __restrict__ out) {
+    int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= n_orbits) return;
+    const double dt = dts ? dts[o] : dt_all;
+    const ShDev sh = subhalo_slice(P.sh, o, k);
+    const int64_t n_save = n_steps / save_every + 1;
+    double y[6];
+    for (int i = 0; i < 6; ++i) y[i] = w0[6 * o + i];
+    double* base = out + o * n_save * 6;
+    for (int i = 0; i < 6; ++i) base[i] = y[i];
+    for (int64_t n = 0; n < n_steps; ++n) {
+        dopri5_step_f64<C>(P, sh, t0 + (double)n * dt, dt, y);
+        if ((n + 1) % save_every == 0) {
+            double* b = base + 6 * ((n + 1) / save_every);
+            for (int i = 0; i < 6; ++i) b[i] = y[i];
+        }
+    }
+}
+
 // ------------------------------------------------------------- track
 // Knot slopes as interpax 'cubic' defines them: mean of the adjacent
 // secants, one-sided at the ends.
@@ -418,6 +443,30 @@ int ss_orbit_f64(const ss_potential* pot, const double* w0, int64_t n_orbits, do
     dispatch_comp(P, [&](auto comp) {
         orbit_f64_kernel<decltype(comp)><<<grid_for(n_orbits, 64), 64, 0, (cudaStream_t)stream>>>(
             P, w0, n_orbits, t0, dt, n_steps, save_every, out);
+        return 0;
+    });
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
+int ss_orbit_ensemble_f64(const ss_potential* pot, const double* w0, int64_t n_orbits, double t0, const double* dt,
+                          double dt_all, int64_t n_steps, int64_t save_every, int32_t subhalos_per_orbit, double* out,
+                          void* stream) {
+    PotDev<double> P;
+    int rc = prepare_potential<double>(pot, &P, true);
+    if (rc) return rc;
+    SS_CHECK_ARG(n_orbits >= 0 && n_steps >= 0, "negative size");
+    SS_CHECK_ARG(save_every >= 1, "save_every must be >= 1");
+    SS_CHECK_ARG(std::isfinite(t0), "t0 must be finite");
+    SS_CHECK_ARG(dt != nullptr || (std::isfinite(dt_all) && dt_all != 0.0), "dt_all must be finite and non-zero");
+    SS_CHECK_ARG(subhalos_per_orbit >= 0, "subhalos_per_orbit < 0");
+    SS_CHECK_ARG(subhalos_per_orbit == 0 || pot->subhalos.n >= n_orbits * (int64_t)subhalos_per_orbit,
+                 "the subhalo table needs subhalos_per_orbit rows for each of the %lld orbits", (long long)n_orbits);
+    if (n_orbits == 0) return SS_OK;
+    SS_CHECK_ARG(w0 && out, "NULL buffer");
+    dispatch_comp(P, [&](auto comp) {
+        orbit_ensemble_kernel<decltype(comp)><<<grid_for(n_orbits, 64), 64, 0, (cudaStream_t)stream>>>(
+            P, w0, n_orbits, t0, dt, dt_all, n_steps, save_every, subhalos_per_orbit, out);
         return 0;
     });
     SS_LAUNCH_CHECK();

@@ -77,15 +77,17 @@ int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalo
 
 // FP64 acceleration of the full potential (components + track + subhalos)
 // at time t: velocity_acceleration, main.py:116-120.
-// C: the composition (Comp<...> or GenericComp).
+// C: the composition (Comp<...> or GenericComp); sh: the subhalo rows this
+// particle feels (P.sh, or one stream's slice of it in an ensemble run).
 template <class C>
-__device__ __forceinline__ void accel_f64(const PotDev<double>& P, const double x[3], double t, double a[3]) {
+__device__ __forceinline__ void accel_f64(const PotDev<double>& P, const ShDev& sh, const double x[3], double t,
+                                          double a[3]) {
     double c[3] = {0.0, 0.0, 0.0};
     if (P.has_track) track_eval(P.track, t, c);
     const double xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
     double g[3];
     C::template grad<double, double, false>(P, x, xs, g, nullptr);
-    if (P.sh.n > 0) subhalo_sum_grad<double>(P.sh, x, t, g);
+    if (sh.n > 0) subhalo_sum_grad<double>(sh, x, t, g);
     a[0] = -g[0];
     a[1] = -g[1];
     a[2] = -g[2];
@@ -93,36 +95,58 @@ __device__ __forceinline__ void accel_f64(const PotDev<double>& P, const double 
 
 // One fixed Dopri5 step of the Hamiltonian flow (x, v) in FP64.
 template <class C>
-__device__ __forceinline__ void dopri5_step_f64(const PotDev<double>& P, double t, double h, double y[6]) {
+__device__ __forceinline__ void dopri5_step_f64(const PotDev<double>& P, const ShDev& sh, double t, double h,
+                                                double y[6]) {
     double k1[6], k2[6], k3[6], k4[6], k5[6], k6[6], ys[6];
     // stage 1
     k1[0] = y[3]; k1[1] = y[4]; k1[2] = y[5];
-    accel_f64<C>(P, y, t, k1 + 3);
+    accel_f64<C>(P, sh, y, t, k1 + 3);
 #pragma unroll
     for (int i = 0; i < 6; ++i) ys[i] = y[i] + h * (SS_A21 * k1[i]);
     k2[0] = ys[3]; k2[1] = ys[4]; k2[2] = ys[5];
-    accel_f64<C>(P, ys, t + SS_C2 * h, k2 + 3);
+    accel_f64<C>(P, sh, ys, t + SS_C2 * h, k2 + 3);
 #pragma unroll
     for (int i = 0; i < 6; ++i) ys[i] = y[i] + h * (SS_A31 * k1[i] + SS_A32 * k2[i]);
     k3[0] = ys[3]; k3[1] = ys[4]; k3[2] = ys[5];
-    accel_f64<C>(P, ys, t + SS_C3 * h, k3 + 3);
+    accel_f64<C>(P, sh, ys, t + SS_C3 * h, k3 + 3);
 #pragma unroll
     for (int i = 0; i < 6; ++i) ys[i] = y[i] + h * (SS_A41 * k1[i] + SS_A42 * k2[i] + SS_A43 * k3[i]);
     k4[0] = ys[3]; k4[1] = ys[4]; k4[2] = ys[5];
-    accel_f64<C>(P, ys, t + SS_C4 * h, k4 + 3);
+    accel_f64<C>(P, sh, ys, t + SS_C4 * h, k4 + 3);
 #pragma unroll
     for (int i = 0; i < 6; ++i)
         ys[i] = y[i] + h * (SS_A51 * k1[i] + SS_A52 * k2[i] + SS_A53 * k3[i] + SS_A54 * k4[i]);
     k5[0] = ys[3]; k5[1] = ys[4]; k5[2] = ys[5];
-    accel_f64<C>(P, ys, t + SS_C5 * h, k5 + 3);
+    accel_f64<C>(P, sh, ys, t + SS_C5 * h, k5 + 3);
 #pragma unroll
     for (int i = 0; i < 6; ++i)
         ys[i] = y[i] + h * (SS_A61 * k1[i] + SS_A62 * k2[i] + SS_A63 * k3[i] + SS_A64 * k4[i] + SS_A65 * k5[i]);
     k6[0] = ys[3]; k6[1] = ys[4]; k6[2] = ys[5];
-    accel_f64<C>(P, ys, t + h, k6 + 3);
+    accel_f64<C>(P, sh, ys, t + h, k6 + 3);
 #pragma unroll
     for (int i = 0; i < 6; ++i)
         y[i] = y[i] + h * (SS_B1 * k1[i] + SS_B3 * k3[i] + SS_B4 * k4[i] + SS_B5 * k5[i] + SS_B6 * k6[i]);
+}
+
+template <class C>
+__device__ __forceinline__ void dopri5_step_f64(const PotDev<double>& P, double t, double h, double y[6]) {
+    dopri5_step_f64<C>(P, P.sh, t, h, y);
+}
+
+// The subhalo rows [g k, (g + 1) k) of sh (one stream or orbit of an
+// ensemble); k <= 0 keeps the whole table.
+__device__ __forceinline__ ShDev subhalo_slice(const ShDev& sh, int64_t g, int32_t k) {
+    ShDev s = sh;
+    if (k > 0 && sh.n > 0) {
+        const int64_t o = g * (int64_t)k;
+        s.m += o;
+        s.a += o;
+        s.x0 += 3 * o;
+        s.v += 3 * o;
+        s.t0 += o;
+        s.n = k;
+    }
+    return s;
 }
 
 }  // namespace ssg

@@ -618,6 +618,7 @@ int ss_stream_mlp_bf16(const ss_mlp* mlp, const ss_stream_cfg* cfg, const double
     SS_CHECK_ARG(std::isfinite(cfg->dt) && cfg->dt > 0.0 && std::isfinite(cfg->t0), "dt must be finite and > 0");
     SS_CHECK_ARG(cfg->snap_stride >= 0, "snap_stride < 0");
     SS_CHECK_ARG(cfg->first_particle >= 0 && cfg->snap_pitch >= 0, "first_particle and snap_pitch must be >= 0");
+    SS_CHECK_ARG(cfg->stream_particles == 0, "the surrogate stream runs single streams (stream_particles = 0)");
     SS_CHECK_ARG(cfg->snap_pitch == 0 || cfg->snap_pitch >= cfg->first_particle + cfg->n_particles,
                  "snap_pitch must cover first_particle + n_particles");
     const int64_t n_rel =

@@ -65,7 +65,7 @@ __global__ void subhalo_table_kernel(ShDev sh, double t0, float4* tab) {
     tab[3 * j + 2] = make_float4((float)(sh.t0[j] - t0), win, 0.f, 0.f);
 }
 
-static int check_stream_cfg(const ss_stream_cfg* cfg) {
+static int check_stream_cfg(const ss_stream_cfg* cfg, const ss_potential* pot) {
     SS_CHECK_ARG(cfg != nullptr, "cfg is NULL");
     SS_CHECK_ARG(cfg->n_particles >= 0, "n_particles < 0");
     SS_CHECK_ARG(cfg->n_steps >= 0 && cfg->n_steps < (1LL << 30), "n_steps outside [0, 2^30)");
@@ -75,10 +75,21 @@ static int check_stream_cfg(const ss_stream_cfg* cfg) {
     SS_CHECK_ARG(cfg->first_particle >= 0 && cfg->snap_pitch >= 0, "first_particle and snap_pitch must be >= 0");
     SS_CHECK_ARG(cfg->snap_pitch == 0 || cfg->snap_pitch >= cfg->first_particle + cfg->n_particles,
                  "snap_pitch must cover first_particle + n_particles");
-    int64_t n_rel =
-        (cfg->first_particle + cfg->n_particles + cfg->particles_per_release - 1) / cfg->particles_per_release;
+    SS_CHECK_ARG(cfg->stream_particles >= 0 && cfg->subhalos_per_stream >= 0,
+                 "stream_particles and subhalos_per_stream must be >= 0");
+    SS_CHECK_ARG(cfg->subhalos_per_stream == 0 || cfg->stream_particles > 0,
+                 "subhalos_per_stream needs stream_particles > 0");
+    const int64_t end = cfg->first_particle + cfg->n_particles;
+    const int64_t per_stream = cfg->stream_particles > 0 && cfg->stream_particles < end ? cfg->stream_particles : end;
+    int64_t n_rel = (per_stream + cfg->particles_per_release - 1) / cfg->particles_per_release;
     SS_CHECK_ARG(n_rel == 0 || (n_rel - 1) * (int64_t)cfg->steps_per_release <= cfg->n_steps,
                  "last release starts after n_steps");
+    if (cfg->subhalos_per_stream > 0) {
+        const int64_t n_streams = (end + cfg->stream_particles - 1) / cfg->stream_particles;
+        SS_CHECK_ARG(pot != nullptr && pot->subhalos.n >= n_streams * (int64_t)cfg->subhalos_per_stream,
+                     "the subhalo table needs subhalos_per_stream rows for each of the %lld streams",
+                     (long long)n_streams);
+    }
     return SS_OK;
 }
 
@@ -101,6 +112,8 @@ static StreamArgs make_args(const ss_stream_cfg* cfg, const double* ics, double*
     a.h_lo = (float)(cfg->dt - (double)a.h_hi);
     a.p_off = cfg->first_particle;
     a.snap_pitch = cfg->snap_pitch > 0 ? cfg->snap_pitch : cfg->n_particles;
+    a.grp = cfg->stream_particles;
+    a.sh_per_grp = cfg->subhalos_per_stream;
     return a;
 }
 
@@ -150,7 +163,7 @@ int ss_stream_f64(const ss_potential* pot, const ss_stream_cfg* cfg, const doubl
     PotDev<double> P;
     int rc = prepare_potential<double>(pot, &P, true);
     if (rc) return rc;
-    rc = check_stream_cfg(cfg);
+    rc = check_stream_cfg(cfg, pot);
     if (rc) return rc;
     if (cfg->n_particles == 0) return SS_OK;
     SS_CHECK_ARG(ics != nullptr, "ics is NULL");
@@ -175,7 +188,7 @@ int ss_stream_f32k(const ss_potential* pot, const ss_stream_cfg* cfg, const doub
     PotDev<float> P;
     int rc = prepare_potential<float>(pot, &P, true);
     if (rc) return rc;
-    rc = check_stream_cfg(cfg);
+    rc = check_stream_cfg(cfg, pot);
     if (rc) return rc;
     if (cfg->n_particles == 0) return SS_OK;
     SS_CHECK_ARG(ics != nullptr, "ics is NULL");

@@ -36,7 +36,18 @@ struct StreamArgs {
     // sub-range runs: global index of local particle 0, snapshot row pitch
     int64_t p_off;
     int64_t snap_pitch;
+    // ensembles: particles per stream (0 = one stream) and subhalo rows per
+    // stream (0 = every particle feels the whole table)
+    int64_t grp;
+    int32_t sh_per_grp;
 };
+
+// Release step of global particle q (its index within its stream picks the
+// release when the run is an ensemble of streams).
+__device__ __forceinline__ int stream_start(const StreamArgs& a, int64_t q) {
+    const int64_t ql = a.grp > 0 ? q % a.grp : q;
+    return (int)((ql / a.ppr) * (int64_t)a.spr);
+}
 
 // Write the snapshot k for lane state y (or NaN when not yet released).
 template <class T>
@@ -59,8 +70,9 @@ template <class C>
 __global__ void __launch_bounds__(64) stream_f64_kernel(PotDev<double> P, StreamArgs a) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p < a.N;
-    const int start = valid ? (int)(((p + a.p_off) / a.ppr) * (int64_t)a.spr) : a.n_steps;
+    const int start = valid ? stream_start(a, p + a.p_off) : a.n_steps;
     const int wstart = (int)__reduce_min_sync(0xffffffffu, (unsigned)start);
+    const ShDev sh = a.sh_per_grp > 0 ? subhalo_slice(P.sh, (p + a.p_off) / a.grp, a.sh_per_grp) : P.sh;
     double y[6];
     if (valid) {
 #pragma unroll
@@ -76,7 +88,7 @@ __global__ void __launch_bounds__(64) stream_f64_kernel(PotDev<double> P, Stream
         }
     }
     for (int n = wstart; n < a.n_steps; ++n) {
-        if (valid && n >= start) dopri5_step_f64<C>(P, a.t0 + (double)n * a.dt, a.dt, y);
+        if (valid && n >= start) dopri5_step_f64<C>(P, sh, a.t0 + (double)n * a.dt, a.dt, y);
         if (a.snaps && (n + 1) % a.stride == 0 && valid)
             write_snap<double>(a.snaps, a.snap_pitch, (n + 1) / a.stride - 1, p + a.p_off, n + 1 >= start, y);
     }
@@ -110,7 +122,7 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 // difference is exact and the separation keeps its relative precision.
 template <class C>
 __device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamArgs& a, const float xh[3],
-                                          const float d[3], int slot, float trel, float A[3]) {
+                                          const float d[3], int slot, float trel, float A[3], int shb, int she) {
     const float X[3] = {xh[0] + d[0], xh[1] + d[1], xh[2] + d[2]};
     float xs[3] = {X[0], X[1], X[2]};
     if (P.has_track) {
@@ -123,7 +135,7 @@ __device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamAr
     float g[3];
     C::template grad<float, float, false>(P, X, xs, g, nullptr);
 #pragma unroll 1
-    for (int j = 0; j < a.n_sh; ++j) {
+    for (int j = shb; j < she; ++j) {
         float4 s0 = __ldg(a.shtab + 3 * j);
         float4 s1 = __ldg(a.shtab + 3 * j + 1);
         float4 s2 = __ldg(a.shtab + 3 * j + 2);
@@ -144,9 +156,12 @@ __device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamAr
 // One compensated step.  V_i = vh + d_i and sum_j a_ij = c_i, sum_i b_i = 1
 // are used exactly, so only the small parts d_i and A_i - A_1 see the
 // rounded tableau.
+// shb, she: the subhalo rows [shb, she) of the table this particle feels
+// (she < 0: all of them).
 template <class C>
 __device__ __forceinline__ void step_f32k(const PotDev<float>& P, const StreamArgs& a, int n, float xh[3],
-                                          float xl[3], float vh[3], float vl[3]) {
+                                          float xl[3], float vh[3], float vl[3], int shb = 0, int she = -1) {
+    if (she < 0) she = a.n_sh;
     const float h = a.h_hi;
     const float tn = (float)n * h;  // time since global step 0 (subhalo lines)
     const int s0 = 5 * n;
@@ -158,32 +173,32 @@ __device__ __forceinline__ void step_f32k(const PotDev<float>& P, const StreamAr
         D[i] = xl[i];
         d1[i] = vl[i];
     }
-    accel_f32<C>(P, a, xh, D, s0, tn, A1);
+    accel_f32<C>(P, a, xh, D, s0, tn, A1, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d2[i] = vl[i] + h * (F_(SS_A21) * A1[i]);
         D[i] = xl[i] + h * (F_C2 * vh[i] + F_(SS_A21) * d1[i]);
     }
-    accel_f32<C>(P, a, xh, D, s0 + 1, tn + F_C2 * h, A2);
+    accel_f32<C>(P, a, xh, D, s0 + 1, tn + F_C2 * h, A2, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d3[i] = vl[i] + h * (F_(SS_A31) * A1[i] + F_(SS_A32) * A2[i]);
         D[i] = xl[i] + h * (F_C3 * vh[i] + F_(SS_A31) * d1[i] + F_(SS_A32) * d2[i]);
     }
-    accel_f32<C>(P, a, xh, D, s0 + 2, tn + F_C3 * h, A3);
+    accel_f32<C>(P, a, xh, D, s0 + 2, tn + F_C3 * h, A3, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d4[i] = vl[i] + h * (F_(SS_A41) * A1[i] + F_(SS_A42) * A2[i] + F_(SS_A43) * A3[i]);
         D[i] = xl[i] + h * (F_C4 * vh[i] + F_(SS_A41) * d1[i] + F_(SS_A42) * d2[i] + F_(SS_A43) * d3[i]);
     }
-    accel_f32<C>(P, a, xh, D, s0 + 3, tn + F_C4 * h, A4);
+    accel_f32<C>(P, a, xh, D, s0 + 3, tn + F_C4 * h, A4, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d5[i] = vl[i] + h * (F_(SS_A51) * A1[i] + F_(SS_A52) * A2[i] + F_(SS_A53) * A3[i] + F_(SS_A54) * A4[i]);
         D[i] = xl[i] + h * (F_C5 * vh[i] + F_(SS_A51) * d1[i] + F_(SS_A52) * d2[i] + F_(SS_A53) * d3[i] +
                             F_(SS_A54) * d4[i]);
     }
-    accel_f32<C>(P, a, xh, D, s0 + 4, tn + F_C5 * h, A5);
+    accel_f32<C>(P, a, xh, D, s0 + 4, tn + F_C5 * h, A5, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d6[i] = vl[i] + h * (F_(SS_A61) * A1[i] + F_(SS_A62) * A2[i] + F_(SS_A63) * A3[i] + F_(SS_A64) * A4[i] +
@@ -191,7 +206,7 @@ __device__ __forceinline__ void step_f32k(const PotDev<float>& P, const StreamAr
         D[i] = xl[i] + h * (vh[i] + F_(SS_A61) * d1[i] + F_(SS_A62) * d2[i] + F_(SS_A63) * d3[i] +
                             F_(SS_A64) * d4[i] + F_(SS_A65) * d5[i]);
     }
-    accel_f32<C>(P, a, xh, D, s0 + 5, tn + h, A6);
+    accel_f32<C>(P, a, xh, D, s0 + 5, tn + h, A6, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         // position: h * (vh + Db), Db = sum b_i d_i
@@ -220,8 +235,10 @@ template <class C>
 __global__ void __launch_bounds__(128) stream_f32k_kernel(PotDev<float> P, StreamArgs a) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p < a.N;
-    const int start = valid ? (int)(((p + a.p_off) / a.ppr) * (int64_t)a.spr) : a.n_steps;
+    const int start = valid ? stream_start(a, p + a.p_off) : a.n_steps;
     const int wstart = (int)__reduce_min_sync(0xffffffffu, (unsigned)start);
+    const int shb = a.sh_per_grp > 0 ? (int)((p + a.p_off) / a.grp) * a.sh_per_grp : 0;
+    const int she = a.sh_per_grp > 0 ? shb + a.sh_per_grp : a.n_sh;
     float xh[3], xl[3], vh[3], vl[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -247,7 +264,7 @@ __global__ void __launch_bounds__(128) stream_f32k_kernel(PotDev<float> P, Strea
                 c[1] = make_float4(vh[1], vh[2], xl[0], xl[1]);
                 c[2] = make_float4(xl[2], vl[0], vl[1], vl[2]);
             }
-            step_f32k<C>(P, a, n, xh, xl, vh, vl);
+            step_f32k<C>(P, a, n, xh, xl, vh, vl, shb, she);
         }
         if (a.snaps && (n + 1) % a.stride == 0 && valid) {
             float y[6] = {xh[0], xh[1], xh[2], vh[0], vh[1], vh[2]};

@@ -68,9 +68,13 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
     ts_h = host64(ts).reshape(-1)
     if len(ts_h) < 2:
         raise ValueError("need at least two release times")
+    ts_grid, t_end = _split_tail(ts_h)
+    if t_end is not None and (prog_pot is not None or snapshot_every or out != "device"):
+        raise NotImplementedError("ts with a last interval off the release grid: no moving progenitor, snapshots or "
+                                  "host output")
     total = pot_base if pot_pert is None else _pot.Potential_Combine([pot_base, pot_pert], units=pot_base.units)
     prog_src = total if (pot_pert is not None and prog_in_pert) else pot_base
-    ws, h, spr = prog_src._prog_orbit(ts_h, prog_w0, dt, None, dtmax, method=prog_method)
+    ws, h, spr = prog_src._prog_orbit(ts_grid, prog_w0, dt, None, dtmax, method=prog_method)
     n_draw = _n_draw(n_particles_per_release)
     model = _abi.SS_RELEASE_CHEN25 if release == "chen25" else _abi.SS_RELEASE_FARDAL
     if release not in ("fardal", "chen25"):
@@ -79,7 +83,10 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
     if normals is None:
         normals = release_normals(seed_num, len(ts_h), n_draw, nz)
     chen = (CHEN25_MEAN, chen25_factor()) if model == _abi.SS_RELEASE_CHEN25 else None
-    ics, _ = pot_base._release(ws, ts_h, Msat, normals, kval_arr, model=model, chen=chen)
+    if t_end is not None:
+        normals = np.asarray(host64(normals)) if not torch.is_tensor(normals) else normals
+        normals = normals[:len(ts_grid)]
+    ics, _ = pot_base._release(ws, ts_grid, Msat, normals, kval_arr, model=model, chen=chen)
     integ = total
     if prog_pot is not None:
         track = CenterTrack.from_samples(ts_h, ws[:, :3])
@@ -91,7 +98,8 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
     cfg = _abi.ss_stream_cfg()
     cfg.t0 = float(ts_h[0])
     cfg.dt = float(h)
-    cfg.n_steps = spr * n_rel
+    # with a last interval off the grid, the grid part ends at the last release
+    cfg.n_steps = spr * (n_rel if t_end is None else n_rel - 1)
     cfg.n_particles = N
     cfg.particles_per_release = ppr
     cfg.steps_per_release = spr
@@ -110,6 +118,9 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
             n_snap = cfg.n_steps // int(snapshot_every)
             snaps = torch.empty(n_snap, N, 6, dtype=torch.float32, device=ws.device)
         final, status = _core.stream(integ._desc(), cfg, stream_ics, precision, snaps=snaps, mlp=force_surrogate)
+        if t_end is not None:
+            final, status = _tail_phase(integ, cfg, final, status, float(ts_grid[-1]), float(t_end), h, precision,
+                                        force_surrogate)
     else:
         raise ValueError("out must be 'device' or 'host'")
     if throw and bool((status != 0).any()):
@@ -124,6 +135,104 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
         out = out + (snaps.reshape(-1, n_rel, n_draw, 2, 6),)
     if return_ics:
         out = out + (ics, ws)
+    return out
+
+
+def _split_tail(ts_h: np.ndarray):
+    """(release grid, end time): the reference integrates every release
+    ts[i], i < len(ts) - 1, to ts[-1], and its notebooks end on a time off
+    the release grid (ts = [linspace(-t_age, t_dissolve, n), 0]).  When ts is
+    uniform the grid is ts and the end None; when only ts[:-1] is, the grid
+    is ts[:-1] (every point a release) and the end ts[-1]."""
+    if len(ts_h) < 4 or _grid_spacing(ts_h) is not None:
+        return ts_h, None
+    head = ts_h[:-1]
+    if _grid_spacing(head) is None or not ts_h[-1] > ts_h[-2] or not head[1] > head[0]:
+        return ts_h, None
+    return head, float(ts_h[-1])
+
+
+def _tail_phase(integ, cfg, final, status, t_last, t_end, h, precision, force_surrogate=None):
+    """Every particle from the last release time to t_end in equal steps no
+    longer than h (one more stream-kernel launch, all particles starting at
+    its first step)."""
+    span = t_end - t_last
+    m = int(np.ceil(span / h - 1e-9))
+    cfg2 = _abi.ss_stream_cfg()
+    cfg2.t0, cfg2.dt, cfg2.n_steps = t_last, span / m, m
+    cfg2.n_particles = cfg.n_particles
+    cfg2.particles_per_release, cfg2.steps_per_release = max(int(cfg.n_particles), 1), 0
+    cfg2.stream_particles, cfg2.subhalos_per_stream = cfg.stream_particles, cfg.subhalos_per_stream
+    final2, status2 = _core.stream(integ._desc(), cfg2, final.contiguous(), precision, mlp=force_surrogate)
+    return final2, torch.maximum(status, status2)
+
+
+def gen_stream_ensemble(pot_base: Potential, pot_pert: Potential, subhalos_per_stream: int, ts=None, prog_w0=None,
+                        Msat=None, seed_num=None, *, solver=None, kval_arr=1.0, dt=None, normals=None,
+                        prog_in_pert=True, precision="f64", return_ics=False):
+    """B independent perturbed streams in one pass: jax.vmap of
+    gen_stream_vmapped_with_pert (streamhelpers.py:89-116; _fixed_prog,
+    :119-146, with prog_in_pert=False) over subhalo parameters, as the
+    reference's GD-1 fitting notebook runs hundreds of samples at once.
+
+    pot_pert  SubhaloLinePotential(-like) with B * subhalos_per_stream rows;
+              stream b feels rows [b k, (b + 1) k) only
+    prog_w0   [6] (every stream) or [B, 6]: the progenitor at ts[0]
+    normals   release draws [len(ts), 1, 4] shared by every stream (the
+              reference reuses seed_num for every sample) or [B, len(ts), 1, 4]
+    ts        uniform, or uniform release times followed by a later end time
+    Every stream's progenitor orbit (in base + its own subhalos when
+    prog_in_pert) runs in one ensemble orbit launch, the releases in one
+    release launch, and all B streams in one stream launch.
+    Returns (lead, trail), each [B, n_rel, 6]."""
+    _core.check_solver(solver)
+    k = int(subhalos_per_stream)
+    table = pot_pert.table()
+    n_sh = int(table.m.shape[0])
+    if k < 1 or n_sh % k:
+        raise ValueError("the subhalo table must hold subhalos_per_stream rows per stream")
+    B = n_sh // k
+    ts_h = host64(ts).reshape(-1)
+    ts_grid, t_end = _split_tail(ts_h)
+    grid = _grid_spacing(ts_grid)
+    if grid is None or ts_grid[1] < ts_grid[0]:
+        raise NotImplementedError("release times must be uniformly spaced and increasing")
+    h, spr = _core.fixed_step(grid, dt=dt if dt is not None else grid)
+    n_grid = len(ts_grid)
+    w0 = f64(prog_w0).reshape(-1, 6)
+    if w0.shape[0] == 1:
+        w0 = w0.expand(B, 6).contiguous()
+    if w0.shape[0] != B:
+        raise ValueError("prog_w0 must be [6] or [B, 6]")
+    total = _pot.Potential_Combine([pot_base, pot_pert], units=pot_base.units)
+    src = total if prog_in_pert else pot_base
+    ws = _core.orbit_ensemble(src._desc(), w0, float(ts_grid[0]), h, spr * (n_grid - 1), spr,
+                              k if prog_in_pert else 0)  # [B, n_grid, 6]
+    if normals is None:
+        normals = release_normals(seed_num, len(ts_h), 1, 4)
+    nrm = f64(normals)
+    if nrm.ndim == 3:
+        nrm = nrm.unsqueeze(0).expand(B, *nrm.shape)
+    nrm = nrm[:, :n_grid].reshape(B * n_grid, -1, 4).contiguous()
+    t_rel = np.tile(ts_grid, B)
+    ics, _ = pot_base._release(ws.reshape(B * n_grid, 6), t_rel, Msat, nrm, kval_arr)  # [B n_grid, 1, 2, 6]
+    n_rel = len(ts_h) - 1
+    ics = ics.reshape(B, n_grid, 2, 6)[:, :n_rel]
+    N = 2 * n_rel
+    cfg = _abi.ss_stream_cfg()
+    cfg.t0, cfg.dt = float(ts_grid[0]), float(h)
+    cfg.n_steps = spr * (n_rel if t_end is None else n_rel - 1)
+    cfg.n_particles = B * N
+    cfg.particles_per_release, cfg.steps_per_release = 2, spr
+    cfg.stream_particles, cfg.subhalos_per_stream = N, k
+    stream_ics = ics.reshape(B * N, 6).contiguous()
+    final, status = _core.stream(total._desc(), cfg, stream_ics, precision)
+    if t_end is not None:
+        final, status = _tail_phase(total, cfg, final, status, float(ts_grid[-1]), float(t_end), h, precision)
+    final = final.reshape(B, n_rel, 2, 6)
+    out = (final[:, :, 0], final[:, :, 1])
+    if return_ics:
+        out = out + (stream_ics.reshape(B, n_rel, 2, 6), ws)
     return out
 
 
@@ -277,6 +386,6 @@ def gen_stream_vmapped_with_pert_Chen25_fixed_prog(pot_base=None, pot_pert=None,
 
 __all__ = ["gen_stream", "eval_dense_stream", "eval_dense_stream_id", "gen_stream_ics_pert",
            "gen_stream_vmapped_with_pert", "gen_stream_vmapped_with_pert_fixed_prog", "gen_stream_scan_with_pert",
-           "custom_release_model", "computed_binned_track", "release_model_Chen25", "gen_stream_ics_Chen25",
+           "custom_release_model", "computed_binned_track", "gen_stream_ensemble", "release_model_Chen25", "gen_stream_ics_Chen25",
            "gen_stream_vmapped_Chen25", "gen_stream_ics_pert_Chen25", "gen_stream_vmapped_with_pert_Chen25",
            "gen_stream_vmapped_with_pert_Chen25_fixed_prog", "chen25_factor", "CHEN25_MEAN", "CHEN25_COV"]

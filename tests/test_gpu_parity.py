@@ -212,6 +212,82 @@ def test_nonlinear_subhalo_stream_parity(ss, oracle):
     assert phase_err(np64(trail), final[:, 1]) <= 1e-10
 
 
+def _ensemble_oracle(oracle, sh, b, back, ts_grid, t_end, normals, prog_in_pert, dt=1.0):
+    """Stream b of an ensemble on the oracle: its progenitor orbit (in base +
+    its own subhalo when prog_in_pert), the release in the base potential,
+    the particles in base + subhalo to the last release and then to t_end."""
+    row = {k: (v[b:b + 1] if isinstance(v, np.ndarray) else v) for k, v in sh.items()}
+    tot = oracle.HostModel(oracle.mw3(), subhalos=dict(row, kind=1))
+    base = oracle.HostModel(oracle.mw3())
+    n_grid = len(ts_grid)
+    ws = oracle.orbit(tot if prog_in_pert else base, back, ts_grid[0], dt, n_grid - 1, 1)[0]
+    ics, _ = oracle.release(base, ws, ts_grid, 2e4, normals[:n_grid])
+    if t_end is None:
+        final, _, _ = oracle.stream(tot, ts_grid[0], dt, n_grid - 1, ics[:-1].reshape(-1, 6), 2, 1)
+        return final.reshape(n_grid - 1, 2, 6)
+    f1, _, _ = oracle.stream(tot, ts_grid[0], dt, n_grid - 1, ics.reshape(-1, 6), 2, 1)
+    span = t_end - ts_grid[-1]
+    m = int(np.ceil(span / dt - 1e-9))
+    f2, _, _ = oracle.stream(tot, ts_grid[-1], span / m, m, f1, f1.shape[0], 0)
+    return f2.reshape(n_grid, 2, 6)
+
+
+@pytest.mark.parametrize("tail,prog_in_pert", [(False, True), (True, True), (True, False)])
+def test_stream_ensemble_parity(ss, oracle, tail, prog_in_pert):
+    """gen_stream_ensemble: B streams, each with its own subhalo, in one
+    orbit launch, one release launch and one stream launch (FP64 and FP32
+    compensated) against the oracle stream by stream; with `tail` the release
+    times are followed by an end time off their grid (the reference notebooks'
+    ts = [linspace(-t_age, t_dissolve, n), 0])."""
+    from streamsculptor_gb300 import potential as P
+    from streamsculptor_gb300.streamhelpers import gen_stream_ensemble, gen_stream_vmapped_with_pert
+    n = 120
+    orc, back, ts, normals = _c1_setup(oracle, n_rel=n)
+    if tail:
+        ts = np.concatenate([ts[:-1], [ts[-1] + 17.4]])
+    rng = np.random.default_rng(12)
+    B = 4
+    ws = oracle.orbit(orc, back, ts[0], 1.0, n - 1, 1)[0]
+    sh = dict(m=10 ** rng.uniform(6.5, 7.7, B), a=rng.uniform(0.2, 0.8, B),
+              x0=ws[rng.integers(30, 100, B), :3] + rng.normal(0, 0.6, (B, 3)), v=rng.normal(0, 0.15, (B, 3)),
+              t0=ts[0] + rng.uniform(30, 100, B), t_window=60.0)
+    pert = P.SubhaloLinePotential(sh["m"], sh["a"], sh["x0"], sh["v"], sh["t0"], sh["t_window"], units=ss.usys)
+    ts_grid = ts[:-1] if tail else ts
+    t_end = float(ts[-1]) if tail else None
+    for precision, tol in (("f64", 1e-10), ("f32k", 1e-5)):
+        lead, trail = gen_stream_ensemble(mw3_gpu(ss), pert, 1, ts=ts, prog_w0=back, Msat=2e4, normals=normals,
+                                          prog_in_pert=prog_in_pert, precision=precision)
+        assert lead.shape == (B, n, 6)
+        for b in range(B):
+            o = _ensemble_oracle(oracle, sh, b, back, ts_grid, t_end, normals, prog_in_pert)
+            assert phase_err(np64(lead[b]), o[:, 0]) <= tol, (precision, b)
+            assert phase_err(np64(trail[b]), o[:, 1]) <= tol, (precision, b)
+    if prog_in_pert:
+        # the single-stream generator on one row gives the ensemble's stream
+        b = 2
+        one = P.SubhaloLinePotential(sh["m"][b:b + 1], sh["a"][b:b + 1], sh["x0"][b:b + 1], sh["v"][b:b + 1],
+                                     sh["t0"][b:b + 1], sh["t_window"], units=ss.usys)
+        l1, t1 = gen_stream_vmapped_with_pert(mw3_gpu(ss), one, ts=ts, prog_w0=back, Msat=2e4, normals=normals,
+                                              prog_method="serial")
+        lead, trail = gen_stream_ensemble(mw3_gpu(ss), pert, 1, ts=ts, prog_w0=back, Msat=2e4, normals=normals)
+        assert phase_err(np64(l1), np64(lead[b])) <= 1e-13 and phase_err(np64(t1), np64(trail[b])) <= 1e-13
+
+
+def test_orbit_ensemble_own_steps(ss, oracle):
+    """ss_orbit_ensemble_f64: every orbit with its own step and end time,
+    against the oracle orbit of each."""
+    from streamsculptor_gb300 import _core
+    orc = oracle.HostModel(oracle.mw3())
+    rng = np.random.default_rng(3)
+    w0 = PROG_WF + rng.normal(0, 0.5, (7, 6)) * np.array([1, 1, 1, 0.01, 0.01, 0.01])
+    t1 = -rng.uniform(100, 900, 7)
+    n = 600
+    out = np64(_core.orbit_ensemble(mw3_gpu(ss)._desc(), _core.f64(w0), 0.0, _core.f64(t1 / n), n))
+    for i in range(7):
+        ref = oracle.orbit(orc, w0[i], 0.0, t1[i] / n, n, n)[0, -1]
+        assert phase_err(out[i, -1], ref) <= 1e-11
+
+
 @pytest.mark.parametrize("fixed", [True, False])
 def test_chen25_perturbed_stream_parity(ss, oracle, fixed):
     """gen_stream_vmapped_with_pert_Chen25[_fixed_prog] (streamhelpers.py:546-653):

@@ -205,3 +205,22 @@ def test_second_order_term_matches_finite_differences(oracle):
         hs = (gp[0, s] - gm[0, s]) / (2 * h)
         want = T0 @ u[s, 12:15] + third - hs
         assert np.max(np.abs(d1[s, 15:18] - want)) <= 1e-6 * np.max(np.abs(want)), s
+
+
+def test_stream_ensemble_mode_equals_separate_streams(oracle):
+    """ss_stream_cfg.stream_particles / subhalos_per_stream on the oracle:
+    an ensemble run equals the streams run one by one with their own
+    subhalo row (release layout restarting in every stream)."""
+    rng = np.random.default_rng(5)
+    B, n_rel, ppr = 3, 20, 2
+    sh = dict(kind=1, m=10 ** rng.uniform(6, 8, B), a=rng.uniform(0.2, 0.8, B),
+              x0=PROG_WF[:3] + rng.normal(0, 1.0, (B, 3)), v=rng.normal(0, 0.1, (B, 3)),
+              t0=rng.uniform(0, 30, B), t_window=40.0)
+    ics = PROG_WF + rng.normal(0, 0.2, (B, n_rel * ppr, 6)) * np.array([1, 1, 1, 0.01, 0.01, 0.01])
+    full, _, st = oracle.stream(oracle.HostModel(oracle.mw3(), subhalos=sh), 0.0, 1.0, n_rel, ics.reshape(-1, 6),
+                                ppr, 1, stream_particles=n_rel * ppr, subhalos_per_stream=1)
+    assert (st == 0).all()
+    for b in range(B):
+        row = {k: (v[b:b + 1] if isinstance(v, np.ndarray) else v) for k, v in sh.items()}
+        one, _, _ = oracle.stream(oracle.HostModel(oracle.mw3(), subhalos=row), 0.0, 1.0, n_rel, ics[b], ppr, 1)
+        assert np.array_equal(full.reshape(B, -1, 6)[b], one)
