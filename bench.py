@@ -706,6 +706,138 @@ def c4_arm(args):
           "clocks": rm["clocks"], "gpu_launches": rm["launches"]})
 
 
+# ------------------------------------------------------------ GD-1 batch
+GD1 = dict(n_samples=700, n_rel=2000, t_age=2500.0, t_dissolve=-300.0, msat=1e4, seed=532, t_window=100.0,
+           wtoday=np.array([-4.0, 1.0, 13.0, -0.20, -0.12, 0.04]),
+           name="batch of 700 perturbed streams (the reference's GD-1 subhalo-fitting batch): Gala Milky Way "
+                "(NFW + Miyamoto-Nagai + two Hernquist), ts = [linspace(-2500, -300, 2000), 0] Myr, 4000 "
+                "particles per stream, one Plummer subhalo per stream (t_window 100 Myr) placed on the "
+                "unperturbed stream by ImpactGenerator from the notebook's prior, each progenitor integrated "
+                "back 2.5 Gyr and forward in base + its own subhalo; fixed dt = 1.1 Myr")
+
+
+def gd1_setup(n_samples):
+    """Unperturbed stream, its phi1, and n_samples subhalos drawn from the
+    notebook's prior and placed on the stream by ImpactGenerator."""
+    import torch
+
+    import streamsculptor_gb300 as ss
+    from streamsculptor_gb300 import potential as P
+    from streamsculptor_gb300.GenerateImpactParams import ImpactGenerator
+    from streamsculptor_gb300.streamhelpers import gen_stream
+
+    u = ss.usys
+    pot = P.GalaMilkyWayPotential(units=u)
+    ts = np.concatenate([np.linspace(-GD1["t_age"], GD1["t_dissolve"], GD1["n_rel"]), [0.0]])
+    h = float(ts[1] - ts[0])
+    n_back = int(np.ceil(GD1["t_age"] / h))
+    ic = pot.integrate_orbit(w0=GD1["wtoday"], ts=np.array([-GD1["t_age"]]), t0=0.0, t1=-GD1["t_age"],
+                             dt=GD1["t_age"] / n_back).ys[0]
+    normals = np.random.Generator(np.random.PCG64(GD1["seed"])).standard_normal((len(ts), 1, 4))
+    lead, trail = gen_stream(pot, ts, ic, GD1["msat"], normals=normals)
+    stream = torch.cat([lead, trail]).double()
+    w = torch.as_tensor(GD1["wtoday"], device=stream.device)
+    e1 = w[:3] / torch.linalg.norm(w[:3])
+    L = torch.linalg.cross(w[:3], w[3:], dim=0)
+    e2 = torch.linalg.cross(L / torch.linalg.norm(L), e1, dim=0)
+    phi1 = torch.rad2deg(torch.atan2(stream[:, :3] @ e2, stream[:, :3] @ e1))
+    tstrip = np.concatenate([ts[:-1], ts[:-1]])
+    rng = np.random.Generator(np.random.PCG64(8942))
+    p1 = phi1.cpu().numpy()
+    lo, hi = np.percentile(p1, 10), np.percentile(p1, 90)
+    gen = ImpactGenerator(pot=pot, tobs=0.0, stream=stream, stream_phi1=phi1, stripping_times=tstrip,
+                          prog_today=GD1["wtoday"], phi1window=0.8, NumImpacts=n_samples,
+                          tImpactBounds=[-GD1["t_age"], 0.0], seednum=4)
+    log10_m = rng.uniform(6.0, 7.0, n_samples)
+    log10_a = rng.uniform(np.log10(0.01), np.log10(0.2), n_samples)
+    phi1_0 = rng.uniform(lo, hi, n_samples)
+    t_imp = -10 ** rng.uniform(1.0, np.log10(2000.0), n_samples)
+    b_imp = 10 ** rng.uniform(-5.0, np.log10(0.5), n_samples)
+    perp = rng.uniform(0.0, 2 * np.pi, n_samples)
+    means, tm = gen.get_particle_mean(phi1_0)
+    xv, _ = gen._get_subhalo_ImpactParamsCartesian(0.0, means, tm, t_imp, b_imp, perp, np.arange(n_samples))
+    xv = xv.cpu().numpy()
+    pert = P.SubhaloLinePotential(10 ** log10_m, 10 ** log10_a, xv[:, :3], xv[:, 3:], t_imp, GD1["t_window"],
+                                  units=u)
+    return pot, pert, ts, normals, n_back
+
+
+def gd1_batch(pot, pert, ts, normals, n_back, precision):
+    """One batch: every sample's progenitor back 2.5 Gyr in base + its
+    subhalo (one ensemble orbit launch), then the 700 streams."""
+    import streamsculptor_gb300 as ss
+    from streamsculptor_gb300 import _core, potential as P
+    from streamsculptor_gb300.streamhelpers import gen_stream_ensemble
+
+    B = int(pert.table().m.shape[0])
+    total = P.Potential_Combine([pot, pert], units=ss.usys)
+    w = _core.f64(GD1["wtoday"]).reshape(1, 6).expand(B, 6).contiguous()
+    ic = _core.orbit_ensemble(total._desc(), w, 0.0, -GD1["t_age"] / n_back, n_back, 0, 1)[:, -1].contiguous()
+    return gen_stream_ensemble(pot, pert, 1, ts=ts, prog_w0=ic, Msat=GD1["msat"], normals=normals,
+                               precision=precision)
+
+
+def gd1_arm(args):
+    import torch
+
+    from streamsculptor_gb300 import _abi
+
+    torch.cuda.set_device(0)
+    B = GD1["n_samples"]
+    pot, pert, ts, normals, n_back = gd1_setup(B)
+    n_rel = GD1["n_rel"]
+    tail = int(np.ceil((ts[-1] - ts[-2]) / (ts[1] - ts[0]) - 1e-9))
+    per_stream = 2 * ((n_rel - 1) * n_rel // 2) + 2 * n_rel * tail
+    work = B * per_stream
+    res = {}
+    outs = {}
+    for prec, steps, warm in (("f32k", args.steps, args.warmup), ("f64", args.f64_steps, 1)):
+        if prec not in args.precisions.split(","):
+            continue
+        for _ in range(warm):
+            gd1_batch(pot, pert, ts, normals, n_back, prec)
+        torch.cuda.synchronize()
+        l0 = _abi.load().ss_kernel_launches()
+        clocks = ClockSampler(gpu_id_for(0))
+        clocks.start()
+        ms = 0.0
+        for _ in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            out = gd1_batch(pot, pert, ts, normals, n_back, prec)
+            e1.record()
+            torch.cuda.synchronize()
+            ms += e0.elapsed_time(e1)
+        res[prec] = dict(ms=ms / steps, clocks=clocks.stop(), launches=_abi.load().ss_kernel_launches() - l0)
+        outs[prec] = torch.stack(out, dim=2).cpu().numpy()  # [B, n_rel, 2, 6]
+    r = res["f32k"]
+    line = {"metric": "particle-steps/s, batches of 700 perturbed streams", "value": work / (r["ms"] * 1e-3),
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (compensated) streams; FP64 progenitor orbits and release",
+            "data": "synthetic (seeded): a GD-1-like progenitor state and the notebook's subhalo prior",
+            "config": {"workload": GD1["name"], "streams": B, "particles_per_stream": 2 * n_rel,
+                       "particle_steps_per_step": work},
+            "s_per_batch": r["ms"] * 1e-3, "clocks": r["clocks"], "gpu_launches": r["launches"],
+            "reference_published": {"value": 11.30, "unit": "s per batch of 700 perturbed GD-1 streams",
+                                    "hardware": "NVIDIA A100",
+                                    "source": "examples/GD1_and_SubhaloFitting_GPU.ipynb:754",
+                                    "note": "adaptive Dopri5 (rtol = atol = 1e-6) in FP64 under jax.vmap, and it "
+                                            "includes the KDE likelihood of each stream; not the same step "
+                                            "sequence"}}
+    if "f64" in res:
+        f = res["f64"]
+        line["f64"] = {"value": work / (f["ms"] * 1e-3), "unit": UNIT, "s_per_batch": f["ms"] * 1e-3,
+                       "clocks": f["clocks"], "gpu_launches": f["launches"]}
+        a, b = outs["f32k"].reshape(-1, 6), outs["f64"].reshape(-1, 6)
+        ex = np.linalg.norm(a[:, :3] - b[:, :3], axis=1) / np.linalg.norm(b[:, :3], axis=1)
+        ev = np.linalg.norm(a[:, 3:] - b[:, 3:], axis=1) / np.linalg.norm(b[:, 3:], axis=1)
+        e = np.maximum(ex, ev)
+        line["error_vs_f64"] = {"median": float(np.median(e)), "p99": float(np.percentile(e, 99)),
+                                "max": float(e.max()), "frac_above_1e-5": float((e > 1e-5).mean())}
+    emit(line)
+
+
 def _measured_bf16():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -733,7 +865,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["c3", "c3s", "c4", "c5"], default="c2")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["c3", "c3s", "c4", "c5", "gd1"], default="c2")
     ap.add_argument("--c4-points", type=int, default=1 << 22, help="surrogate training points (c4)")
     ap.add_argument("--c4-train-steps", type=int, default=6000, help="surrogate Adam steps (c4)")
     ap.add_argument("--c4-releases", type=int, default=C4["n_rel"], help="release times (c4; smaller for profiling)")
@@ -750,6 +882,9 @@ def main():
         return
     if args.workload == "c4":
         c4_arm(args)
+        return
+    if args.workload == "gd1":
+        gd1_arm(args)
         return
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":

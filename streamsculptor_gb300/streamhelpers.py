@@ -300,6 +300,49 @@ def computed_binned_track(stream, phi1, bins=20):
     return torch.where(mean == 0, torch.full_like(mean, float("nan")), mean)
 
 
+def compute_stream_length(stream, phi1, bins=20):
+    """Length of the stream's binned mean track (streamhelpers.py:230-243):
+    the summed distances between consecutive bin means (positions), NaN
+    bins skipped."""
+    m = computed_binned_track(stream, phi1, bins)[:, :3]
+    seg = torch.linalg.norm(m[1:] - m[:-1], dim=1)
+    return torch.nansum(seg)
+
+
+def compute_length_oscillations(pot, prog_today, first_stripped_lead, first_stripped_trail, t_age, length_today, *,
+                                dt=None, n_samples=2_000):
+    """Stream length through time from orbital oscillations
+    (streamhelpers.py:246-303): the progenitor and the first stripped leading
+    and trailing stars are integrated back t_age from t = 0 (one ensemble of
+    three FP64 orbits, saved at 2000 times); the length is length_today times
+    the quadrature sum of the two arm separations relative to today's.
+    Returns dict(ts [increasing], length_func)."""
+    t_age = float(host64(t_age))
+    ts = np.linspace(0.0, -t_age, int(n_samples))
+    w = torch.stack([f64(first_stripped_lead).reshape(6), f64(first_stripped_trail).reshape(6),
+                     f64(prog_today).reshape(6)])
+    ys = pot.integrate_orbit(w0=w, ts=ts, t0=0.0, t1=-t_age, dt=dt).ys  # [3, n, 6]
+    diff = torch.sqrt(torch.sum((ys[0, :, :3] - ys[2, :, :3]) ** 2 + (ys[1, :, :3] - ys[2, :, :3]) ** 2, dim=1))
+    diff_flip = torch.flip(diff, dims=[0])
+    amp = diff_flip / diff_flip[-1]
+    return dict(ts=torch.as_tensor(ts[::-1].copy(), device=diff.device), length_func=float(host64(length_today)) * amp)
+
+
+def sample_from_1D_pdf(x, y, key, num_samples):
+    """Inverse-CDF samples of the density y(x) (streamhelpers.py:306-349):
+    y normalised by its trapezoid integral, CDF = cumulative sum normalised
+    to 1, samples = interp(u, CDF, x) for u ~ U(0, 1) (numpy PCG64 seeded
+    from `key`)."""
+    from .subhalostatistics import seed_of
+    xh = np.asarray(host64(x), dtype=np.float64).reshape(-1)
+    yh = np.asarray(host64(y), dtype=np.float64).reshape(-1)
+    pdf = yh / np.trapezoid(yh, xh)
+    cdf = np.cumsum(pdf)
+    cdf = cdf / cdf[-1]
+    u = np.random.default_rng(seed_of(key)).uniform(size=int(num_samples))
+    return np.interp(u, cdf, xh)
+
+
 def release_model_Chen25(pot_base, key, x, v, Msat, t, normals=None):
     """Chen+25 6-D Gaussian release at one time (streamhelpers.py:352-432).
 
@@ -386,6 +429,7 @@ def gen_stream_vmapped_with_pert_Chen25_fixed_prog(pot_base=None, pot_pert=None,
 
 __all__ = ["gen_stream", "eval_dense_stream", "eval_dense_stream_id", "gen_stream_ics_pert",
            "gen_stream_vmapped_with_pert", "gen_stream_vmapped_with_pert_fixed_prog", "gen_stream_scan_with_pert",
-           "custom_release_model", "computed_binned_track", "gen_stream_ensemble", "release_model_Chen25", "gen_stream_ics_Chen25",
+           "custom_release_model", "computed_binned_track", "gen_stream_ensemble", "compute_stream_length",
+           "compute_length_oscillations", "sample_from_1D_pdf", "release_model_Chen25", "gen_stream_ics_Chen25",
            "gen_stream_vmapped_Chen25", "gen_stream_ics_pert_Chen25", "gen_stream_vmapped_with_pert_Chen25",
            "gen_stream_vmapped_with_pert_Chen25_fixed_prog", "chen25_factor", "CHEN25_MEAN", "CHEN25_COV"]
