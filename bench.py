@@ -716,9 +716,9 @@ GD1 = dict(n_samples=700, n_rel=2000, t_age=2500.0, t_dissolve=-300.0, msat=1e4,
                 "back 2.5 Gyr and forward in base + its own subhalo; fixed dt = 1.1 Myr")
 
 
-def gd1_setup(n_samples):
-    """Unperturbed stream, its phi1, and n_samples subhalos drawn from the
-    notebook's prior and placed on the stream by ImpactGenerator."""
+def gd1_setup(n_samples, n_batches):
+    """Unperturbed stream, its phi1, and n_batches x n_samples subhalos drawn
+    from the notebook's prior and placed on the stream by ImpactGenerator."""
     import torch
 
     import streamsculptor_gb300 as ss
@@ -748,77 +748,87 @@ def gd1_setup(n_samples):
     gen = ImpactGenerator(pot=pot, tobs=0.0, stream=stream, stream_phi1=phi1, stripping_times=tstrip,
                           prog_today=GD1["wtoday"], phi1window=0.8, NumImpacts=n_samples,
                           tImpactBounds=[-GD1["t_age"], 0.0], seednum=4)
-    log10_m = rng.uniform(6.0, 7.0, n_samples)
-    log10_a = rng.uniform(np.log10(0.01), np.log10(0.2), n_samples)
-    phi1_0 = rng.uniform(lo, hi, n_samples)
-    t_imp = -10 ** rng.uniform(1.0, np.log10(2000.0), n_samples)
-    b_imp = 10 ** rng.uniform(-5.0, np.log10(0.5), n_samples)
-    perp = rng.uniform(0.0, 2 * np.pi, n_samples)
-    means, tm = gen.get_particle_mean(phi1_0)
-    xv, _ = gen._get_subhalo_ImpactParamsCartesian(0.0, means, tm, t_imp, b_imp, perp, np.arange(n_samples))
-    xv = xv.cpu().numpy()
-    pert = P.SubhaloLinePotential(10 ** log10_m, 10 ** log10_a, xv[:, :3], xv[:, 3:], t_imp, GD1["t_window"],
-                                  units=u)
-    return pot, pert, ts, normals, n_back
-
-
-def gd1_batch(pot, pert, ts, normals, n_back, precision):
-    """One batch: every sample's progenitor back 2.5 Gyr in base + its
-    subhalo (one ensemble orbit launch), then the 700 streams."""
-    import streamsculptor_gb300 as ss
-    from streamsculptor_gb300 import _core, potential as P
-    from streamsculptor_gb300.streamhelpers import gen_stream_ensemble
-
-    B = int(pert.table().m.shape[0])
-    total = P.Potential_Combine([pot, pert], units=ss.usys)
-    w = _core.f64(GD1["wtoday"]).reshape(1, 6).expand(B, 6).contiguous()
-    ic = _core.orbit_ensemble(total._desc(), w, 0.0, -GD1["t_age"] / n_back, n_back, 0, 1)[:, -1].contiguous()
-    return gen_stream_ensemble(pot, pert, 1, ts=ts, prog_w0=ic, Msat=GD1["msat"], normals=normals,
-                               precision=precision)
+    perts = []
+    for _ in range(n_batches):
+        log10_m = rng.uniform(6.0, 7.0, n_samples)
+        log10_a = rng.uniform(np.log10(0.01), np.log10(0.2), n_samples)
+        phi1_0 = rng.uniform(lo, hi, n_samples)
+        t_imp = -10 ** rng.uniform(1.0, np.log10(2000.0), n_samples)
+        b_imp = 10 ** rng.uniform(-5.0, np.log10(0.5), n_samples)
+        perp = rng.uniform(0.0, 2 * np.pi, n_samples)
+        means, tm = gen.get_particle_mean(phi1_0)
+        xv, _ = gen._get_subhalo_ImpactParamsCartesian(0.0, means, tm, t_imp, b_imp, perp, np.arange(n_samples))
+        xv = xv.cpu().numpy()
+        perts.append(P.SubhaloLinePotential(10 ** log10_m, 10 ** log10_a, xv[:, :3], xv[:, 3:], t_imp,
+                                            GD1["t_window"], units=u))
+    return pot, perts, ts, normals
 
 
 def gd1_arm(args):
+    """Batches of 700 perturbed streams: each sample's progenitor is
+    integrated back 2.5 Gyr from today and forward in base + its own subhalo
+    (FP64 ensemble orbits), released (FP64) and its 4000 particles
+    integrated (FP32 compensated; FP64 beside it).  Timed: K batches through
+    gen_stream_ensemble_batches, which overlaps batch i + 1's latency-bound
+    orbits with batch i's streams; the latency of one batch alone is
+    reported beside it."""
     import torch
 
     from streamsculptor_gb300 import _abi
+    from streamsculptor_gb300 import streamhelpers as H
+    from streamsculptor_gb300.streamhelpers import gen_stream_ensemble, gen_stream_ensemble_batches
 
     torch.cuda.set_device(0)
     B = GD1["n_samples"]
-    pot, pert, ts, normals, n_back = gd1_setup(B)
+    K, W = args.steps, args.warmup
+    pot, perts, ts, normals = gd1_setup(B, max(K, args.f64_steps) + 1)
     n_rel = GD1["n_rel"]
     tail = int(np.ceil((ts[-1] - ts[-2]) / (ts[1] - ts[0]) - 1e-9))
     per_stream = 2 * ((n_rel - 1) * n_rel // 2) + 2 * n_rel * tail
     work = B * per_stream
-    res = {}
-    outs = {}
-    for prec, steps, warm in (("f32k", args.steps, args.warmup), ("f64", args.f64_steps, 1)):
+    kw = dict(Msat=GD1["msat"], normals=normals, prog_w0_at="end")
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), out
+
+    res, outs = {}, {}
+    for prec, k in (("f32k", K), ("f64", args.f64_steps)):
         if prec not in args.precisions.split(","):
             continue
-        for _ in range(warm):
-            gd1_batch(pot, pert, ts, normals, n_back, prec)
-        torch.cuda.synchronize()
+        for _ in range(W if prec == "f32k" else 1):
+            gen_stream_ensemble_batches(pot, perts[:2], 1, ts, GD1["wtoday"], precision=prec, **kw)
         l0 = _abi.load().ss_kernel_launches()
         clocks = ClockSampler(gpu_id_for(0))
         clocks.start()
-        ms = 0.0
-        for _ in range(steps):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            out = gd1_batch(pot, pert, ts, normals, n_back, prec)
-            e1.record()
-            torch.cuda.synchronize()
-            ms += e0.elapsed_time(e1)
-        res[prec] = dict(ms=ms / steps, clocks=clocks.stop(), launches=_abi.load().ss_kernel_launches() - l0)
-        outs[prec] = torch.stack(out, dim=2).cpu().numpy()  # [B, n_rel, 2, 6]
+        ms, out = timed(lambda: gen_stream_ensemble_batches(pot, perts[1:k + 1], 1, ts, GD1["wtoday"],
+                                                            precision=prec, **kw))
+        ck = clocks.stop()
+        launches = _abi.load().ss_kernel_launches() - l0
+        one_ms, _ = timed(lambda: gen_stream_ensemble(pot, perts[0], 1, ts, GD1["wtoday"], precision=prec, **kw))
+        # the two halves of one batch alone: FP64 orbits + release, then the streams
+        prep_ms, prep = timed(lambda: H._ensemble_prepare(pot, perts[0], 1, ts, GD1["wtoday"], GD1["msat"], None,
+                                                          1.0, None, normals, True, "end"))
+        run_ms, _ = timed(lambda: H._ensemble_run(prep, prec, False))
+        res[prec] = dict(ms=ms / k, one_ms=one_ms, prep_ms=prep_ms, run_ms=run_ms, clocks=ck, launches=launches, k=k)
+        outs[prec] = torch.stack(out[0], dim=2).cpu().numpy()  # batch perts[1]: [B, n_rel, 2, 6]
     r = res["f32k"]
     line = {"metric": "particle-steps/s, batches of 700 perturbed streams", "value": work / (r["ms"] * 1e-3),
-            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"],
+            "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": W, "ms_per_step": r["ms"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (compensated) streams; FP64 progenitor orbits and release",
             "data": "synthetic (seeded): a GD-1-like progenitor state and the notebook's subhalo prior",
             "config": {"workload": GD1["name"], "streams": B, "particles_per_stream": 2 * n_rel,
-                       "particle_steps_per_step": work},
-            "s_per_batch": r["ms"] * 1e-3, "clocks": r["clocks"], "gpu_launches": r["launches"],
+                       "particle_steps_per_step": work, "step": "one batch of 700 streams",
+                       "l2": "1.3e8 B of particle state per batch, larger than L2"},
+            "s_per_batch": r["ms"] * 1e-3, "s_one_batch_alone": r["one_ms"] * 1e-3,
+            "one_batch_split_ms": {"orbits_and_release": r["prep_ms"], "streams": r["run_ms"]},
+            "clocks": r["clocks"], "gpu_launches": r["launches"],
             "reference_published": {"value": 11.30, "unit": "s per batch of 700 perturbed GD-1 streams",
                                     "hardware": "NVIDIA A100",
                                     "source": "examples/GD1_and_SubhaloFitting_GPU.ipynb:754",
@@ -828,7 +838,8 @@ def gd1_arm(args):
     if "f64" in res:
         f = res["f64"]
         line["f64"] = {"value": work / (f["ms"] * 1e-3), "unit": UNIT, "s_per_batch": f["ms"] * 1e-3,
-                       "clocks": f["clocks"], "gpu_launches": f["launches"]}
+                       "s_one_batch_alone": f["one_ms"] * 1e-3, "batches": f["k"], "clocks": f["clocks"],
+                       "gpu_launches": f["launches"]}
         a, b = outs["f32k"].reshape(-1, 6), outs["f64"].reshape(-1, 6)
         ex = np.linalg.norm(a[:, :3] - b[:, :3], axis=1) / np.linalg.norm(b[:, :3], axis=1)
         ev = np.linalg.norm(a[:, 3:] - b[:, 3:], axis=1) / np.linalg.norm(b[:, 3:], axis=1)

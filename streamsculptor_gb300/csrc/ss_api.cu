@@ -430,6 +430,17 @@ int ss_potential_eval(const ss_potential* pot, const double* xyz, int64_t n, con
     return SS_OK;
 }
 
+// Threads per block of the one-thread-per-orbit kernels.  An SM's warps
+// share its FP64 pipe, so while the orbits fit one warp per SM they are
+// spread that way (32-thread blocks); larger batches use 64.
+static int orbit_block(int64_t n_orbits) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess)
+        return 64;
+    return n_orbits <= 32 * (int64_t)sms ? 32 : 64;
+}
+
 int ss_orbit_f64(const ss_potential* pot, const double* w0, int64_t n_orbits, double t0, double dt,
                  int64_t n_steps, int64_t save_every, double* out, void* stream) {
     PotDev<double> P;
@@ -441,7 +452,8 @@ int ss_orbit_f64(const ss_potential* pot, const double* w0, int64_t n_orbits, do
     if (n_orbits == 0) return SS_OK;
     SS_CHECK_ARG(w0 && out, "NULL buffer");
     dispatch_comp(P, [&](auto comp) {
-        orbit_f64_kernel<decltype(comp)><<<grid_for(n_orbits, 64), 64, 0, (cudaStream_t)stream>>>(
+        const int bs = orbit_block(n_orbits);
+        orbit_f64_kernel<decltype(comp)><<<grid_for(n_orbits, bs), bs, 0, (cudaStream_t)stream>>>(
             P, w0, n_orbits, t0, dt, n_steps, save_every, out);
         return 0;
     });
@@ -465,7 +477,8 @@ int ss_orbit_ensemble_f64(const ss_potential* pot, const double* w0, int64_t n_o
     if (n_orbits == 0) return SS_OK;
     SS_CHECK_ARG(w0 && out, "NULL buffer");
     dispatch_comp(P, [&](auto comp) {
-        orbit_ensemble_kernel<decltype(comp)><<<grid_for(n_orbits, 64), 64, 0, (cudaStream_t)stream>>>(
+        const int bs = orbit_block(n_orbits);
+        orbit_ensemble_kernel<decltype(comp)><<<grid_for(n_orbits, bs), bs, 0, (cudaStream_t)stream>>>(
             P, w0, n_orbits, t0, dt, dt_all, n_steps, save_every, subhalos_per_orbit, out);
         return 0;
     });

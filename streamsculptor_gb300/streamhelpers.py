@@ -15,7 +15,7 @@ import torch
 
 from . import _abi, _core
 from ._core import CenterTrack, f64, host64
-from .main import Potential, _grid_spacing, _n_draw, _split_ics, release_normals
+from .main import Potential, _grid_spacing, _kvals, _n_draw, _split_ics, release_normals
 from . import potential as _pot
 
 # release_model_Chen25 mean and covariance (streamhelpers.py:360-369)
@@ -169,55 +169,162 @@ def _tail_phase(integ, cfg, final, status, t_last, t_end, h, precision, force_su
 
 def gen_stream_ensemble(pot_base: Potential, pot_pert: Potential, subhalos_per_stream: int, ts=None, prog_w0=None,
                         Msat=None, seed_num=None, *, solver=None, kval_arr=1.0, dt=None, normals=None,
-                        prog_in_pert=True, precision="f64", return_ics=False):
+                        prog_in_pert=True, precision="f64", prog_w0_at="start", return_ics=False):
     """B independent perturbed streams in one pass: jax.vmap of
     gen_stream_vmapped_with_pert (streamhelpers.py:89-116; _fixed_prog,
     :119-146, with prog_in_pert=False) over subhalo parameters, as the
     reference's GD-1 fitting notebook runs hundreds of samples at once.
 
-    pot_pert  SubhaloLinePotential(-like) with B * subhalos_per_stream rows;
-              stream b feels rows [b k, (b + 1) k) only
-    prog_w0   [6] (every stream) or [B, 6]: the progenitor at ts[0]
-    normals   release draws [len(ts), 1, 4] shared by every stream (the
-              reference reuses seed_num for every sample) or [B, len(ts), 1, 4]
-    ts        uniform, or uniform release times followed by a later end time
-    Every stream's progenitor orbit (in base + its own subhalos when
-    prog_in_pert) runs in one ensemble orbit launch, the releases in one
-    release launch, and all B streams in one stream launch.
+    pot_pert    SubhaloLinePotential(-like) with B * subhalos_per_stream rows;
+                stream b feels rows [b k, (b + 1) k) only
+    prog_w0     [6] (every stream) or [B, 6]: the progenitor at ts[0], or at
+                ts[-1] with prog_w0_at="end" (then each stream's progenitor is
+                first integrated back to ts[0], in base + its own subhalos
+                when prog_in_pert, as the notebook does per sample)
+    normals     release draws [len(ts), 1, 4] shared by every stream (the
+                reference reuses seed_num for every sample) or [B, len(ts), 1, 4]
+    ts          uniform, or uniform release times followed by a later end time
+    Every stream's progenitor orbit runs in one ensemble orbit launch, the
+    releases in one release launch, and all B streams in one stream launch.
     Returns (lead, trail), each [B, n_rel, 6]."""
     _core.check_solver(solver)
-    k = int(subhalos_per_stream)
-    table = pot_pert.table()
-    n_sh = int(table.m.shape[0])
-    if k < 1 or n_sh % k:
-        raise ValueError("the subhalo table must hold subhalos_per_stream rows per stream")
-    B = n_sh // k
+    prep = _ensemble_prepare(pot_base, pot_pert, subhalos_per_stream, ts, prog_w0, Msat, seed_num, kval_arr, dt,
+                             normals, prog_in_pert, prog_w0_at)
+    return _ensemble_run(prep, precision, return_ics)
+
+
+def gen_stream_ensemble_batches(pot_base: Potential, pot_perts, subhalos_per_stream: int, ts=None, prog_w0=None,
+                                Msat=None, seed_num=None, *, solver=None, kval_arr=1.0, dt=None, normals=None,
+                                prog_in_pert=True, precision="f64", prog_w0_at="start", lookahead=2):
+    """gen_stream_ensemble over a sequence of subhalo batches (the notebook's
+    loop of vmapped batches), pipelined on several CUDA streams: the FP64
+    progenitor orbits and releases of the next `lookahead` batches (a few
+    hundred threads each, bound by the FP64 issue rate of their warps, not
+    by the GPU's capacity) run concurrently while the streams of the current
+    batch fill the GPU.  Every host-to-device copy is made before the first
+    launch, so the host never waits on the GPU inside the loop.  prog_w0 is
+    one state / [B, 6] for every batch or a list with one per batch.
+    Returns a list of (lead, trail), ready on the current stream."""
+    _core.check_solver(solver)
+    perts = list(pot_perts)
+    if not perts:
+        return []
+    w0s = prog_w0 if isinstance(prog_w0, (list, tuple)) else [prog_w0] * len(perts)
+    main = torch.cuda.current_stream()
+    # device tables and inputs of every batch, made on the main stream up front
+    totals = []
+    for pert in perts:
+        total = _pot.Potential_Combine([pot_base, pert], units=pot_base.units)
+        total._desc()
+        totals.append(total)
+    pot_base._desc()
+    shared = isinstance(prog_w0, (list, tuple)) is False
+    inputs = [None] * len(perts)
+    for i, pert in enumerate(perts):
+        if i == 0 or not shared or int(pert.table().m.shape[0]) != int(perts[0].table().m.shape[0]):
+            inputs[i] = _ensemble_inputs(pert, subhalos_per_stream, ts, w0s[i], Msat, seed_num, kval_arr, dt,
+                                         normals)
+        else:
+            inputs[i] = inputs[0]
+    depth = max(1, int(lookahead))
+    # high priority: their few orbit blocks go first when the streams free a slot
+    sides = [torch.cuda.Stream(priority=-1) for _ in range(depth)]
+    for sd in sides:
+        sd.wait_stream(main)
+
+    def prepare(i):
+        side = sides[i % depth]
+        with torch.cuda.stream(side):
+            prep = _ensemble_prepare(pot_base, perts[i], subhalos_per_stream, ts, None, Msat, seed_num, kval_arr, dt,
+                                     normals, prog_in_pert, prog_w0_at, totals[i], inputs[i])
+            ev = torch.cuda.Event()
+            ev.record(side)
+        for t in (prep["ics"], prep["ws"]):
+            t.record_stream(main)
+        return prep, ev
+
+    outs = []
+    ready = {}
+    for i in range(len(perts)):
+        for j in range(i, min(i + depth + 1, len(perts))):
+            if j not in ready:
+                ready[j] = prepare(j)
+        prep, ev = ready.pop(i)
+        main.wait_event(ev)
+        outs.append(_ensemble_run(prep, precision, False))
+    return outs
+
+
+def _ensemble_grid(ts, dt):
     ts_h = host64(ts).reshape(-1)
     ts_grid, t_end = _split_tail(ts_h)
     grid = _grid_spacing(ts_grid)
     if grid is None or ts_grid[1] < ts_grid[0]:
         raise NotImplementedError("release times must be uniformly spaced and increasing")
     h, spr = _core.fixed_step(grid, dt=dt if dt is not None else grid)
+    return ts_h, ts_grid, t_end, h, spr
+
+
+def _ensemble_inputs(pot_pert, subhalos_per_stream, ts, prog_w0, Msat, seed_num, kval_arr, dt, normals):
+    """Device copies of an ensemble's inputs (progenitor states, release
+    times, satellite masses, release draws) and its release config."""
+    k = int(subhalos_per_stream)
+    n_sh = int(pot_pert.table().m.shape[0])
+    if k < 1 or n_sh % k:
+        raise ValueError("the subhalo table must hold subhalos_per_stream rows per stream")
+    B = n_sh // k
+    ts_h, ts_grid, _, _, _ = _ensemble_grid(ts, dt)
     n_grid = len(ts_grid)
     w0 = f64(prog_w0).reshape(-1, 6)
     if w0.shape[0] == 1:
         w0 = w0.expand(B, 6).contiguous()
     if w0.shape[0] != B:
         raise ValueError("prog_w0 must be [6] or [B, 6]")
-    total = _pot.Potential_Combine([pot_base, pot_pert], units=pot_base.units)
-    src = total if prog_in_pert else pot_base
-    ws = _core.orbit_ensemble(src._desc(), w0, float(ts_grid[0]), h, spr * (n_grid - 1), spr,
-                              k if prog_in_pert else 0)  # [B, n_grid, 6]
     if normals is None:
         normals = release_normals(seed_num, len(ts_h), 1, 4)
     nrm = f64(normals)
     if nrm.ndim == 3:
         nrm = nrm.unsqueeze(0).expand(B, *nrm.shape)
     nrm = nrm[:, :n_grid].reshape(B * n_grid, -1, 4).contiguous()
-    t_rel = np.tile(ts_grid, B)
-    ics, _ = pot_base._release(ws.reshape(B * n_grid, 6), t_rel, Msat, nrm, kval_arr)  # [B n_grid, 1, 2, 6]
+    m = host64(Msat)
+    msat = np.full(n_grid, float(m)) if m.ndim == 0 else m.reshape(-1)[:n_grid]
+    rcfg = _abi.ss_release_cfg()
+    rcfg.n_release, rcfg.n_draw, rcfg.model = B * n_grid, nrm.shape[1], _abi.SS_RELEASE_FARDAL
+    for i, kv in enumerate(_kvals(kval_arr)):
+        rcfg.kvals[i] = kv
+    return dict(w0=w0, nrm=nrm, t_rel=f64(np.tile(ts_grid, B)), msat=f64(np.tile(np.asarray(msat, np.float64), B)),
+                rcfg=rcfg, B=B)
+
+
+def _ensemble_prepare(pot_base, pot_pert, subhalos_per_stream, ts, prog_w0, Msat, seed_num, kval_arr, dt, normals,
+                      prog_in_pert, prog_w0_at, total=None, inputs=None):
+    """Progenitor orbits (one ensemble launch, two with prog_w0_at="end")
+    and the releases (one launch) of an ensemble, on the current stream;
+    with `inputs` (from _ensemble_inputs) nothing here copies between host
+    and device."""
+    k = int(subhalos_per_stream)
+    if prog_w0_at not in ("start", "end"):
+        raise ValueError("prog_w0_at must be 'start' or 'end'")
+    if inputs is None:
+        inputs = _ensemble_inputs(pot_pert, k, ts, prog_w0, Msat, seed_num, kval_arr, dt, normals)
+    B = inputs["B"]
+    ts_h, ts_grid, t_end, h, spr = _ensemble_grid(ts, dt)
+    n_grid = len(ts_grid)
+    w0 = inputs["w0"]
+    if total is None:
+        total = _pot.Potential_Combine([pot_base, pot_pert], units=pot_base.units)
+    src = total if prog_in_pert else pot_base
+    kk = k if prog_in_pert else 0
+    if prog_w0_at == "end":
+        span = float(ts_h[-1] - ts_h[0])
+        n_back = max(1, int(np.ceil(span / h - 1e-9)))
+        w0 = _core.orbit_ensemble(src._desc(), w0, float(ts_h[-1]), -span / n_back, n_back, 0, kk)[:, -1]
+        w0 = w0.contiguous()
+    ws = _core.orbit_ensemble(src._desc(), w0, float(ts_grid[0]), h, spr * (n_grid - 1), spr, kk)  # [B, n_grid, 6]
+    ics, _ = _core.release(pot_base._desc(), inputs["rcfg"], ws.reshape(B * n_grid, 6), inputs["t_rel"],
+                           inputs["msat"], inputs["nrm"])  # [B n_grid, 1, 2, 6]
     n_rel = len(ts_h) - 1
-    ics = ics.reshape(B, n_grid, 2, 6)[:, :n_rel]
+    ics = ics.reshape(B, n_grid, 2, 6)[:, :n_rel].reshape(B * 2 * n_rel, 6).contiguous()
     N = 2 * n_rel
     cfg = _abi.ss_stream_cfg()
     cfg.t0, cfg.dt = float(ts_grid[0]), float(h)
@@ -225,14 +332,19 @@ def gen_stream_ensemble(pot_base: Potential, pot_pert: Potential, subhalos_per_s
     cfg.n_particles = B * N
     cfg.particles_per_release, cfg.steps_per_release = 2, spr
     cfg.stream_particles, cfg.subhalos_per_stream = N, k
-    stream_ics = ics.reshape(B * N, 6).contiguous()
-    final, status = _core.stream(total._desc(), cfg, stream_ics, precision)
-    if t_end is not None:
-        final, status = _tail_phase(total, cfg, final, status, float(ts_grid[-1]), float(t_end), h, precision)
+    return dict(total=total, cfg=cfg, ics=ics, ws=ws, B=B, n_rel=n_rel, t_last=float(ts_grid[-1]), t_end=t_end, h=h)
+
+
+def _ensemble_run(prep, precision, return_ics):
+    """The stream launches of a prepared ensemble, on the current stream."""
+    total, cfg, B, n_rel = prep["total"], prep["cfg"], prep["B"], prep["n_rel"]
+    final, status = _core.stream(total._desc(), cfg, prep["ics"], precision)
+    if prep["t_end"] is not None:
+        final, status = _tail_phase(total, cfg, final, status, prep["t_last"], prep["t_end"], prep["h"], precision)
     final = final.reshape(B, n_rel, 2, 6)
     out = (final[:, :, 0], final[:, :, 1])
     if return_ics:
-        out = out + (stream_ics.reshape(B, n_rel, 2, 6), ws)
+        out = out + (prep["ics"].reshape(B, n_rel, 2, 6), prep["ws"])
     return out
 
 
@@ -429,7 +541,8 @@ def gen_stream_vmapped_with_pert_Chen25_fixed_prog(pot_base=None, pot_pert=None,
 
 __all__ = ["gen_stream", "eval_dense_stream", "eval_dense_stream_id", "gen_stream_ics_pert",
            "gen_stream_vmapped_with_pert", "gen_stream_vmapped_with_pert_fixed_prog", "gen_stream_scan_with_pert",
-           "custom_release_model", "computed_binned_track", "gen_stream_ensemble", "compute_stream_length",
+           "custom_release_model", "computed_binned_track", "gen_stream_ensemble", "gen_stream_ensemble_batches",
+           "compute_stream_length",
            "compute_length_oscillations", "sample_from_1D_pdf", "release_model_Chen25", "gen_stream_ics_Chen25",
            "gen_stream_vmapped_Chen25", "gen_stream_ics_pert_Chen25", "gen_stream_vmapped_with_pert_Chen25",
            "gen_stream_vmapped_with_pert_Chen25_fixed_prog", "chen25_factor", "CHEN25_MEAN", "CHEN25_COV"]

@@ -273,6 +273,44 @@ def test_stream_ensemble_parity(ss, oracle, tail, prog_in_pert):
         assert phase_err(np64(l1), np64(lead[b])) <= 1e-13 and phase_err(np64(t1), np64(trail[b])) <= 1e-13
 
 
+def test_ensemble_batches_pipelined(ss, oracle):
+    """gen_stream_ensemble_batches (two CUDA streams, batch i + 1's orbits
+    under batch i's streams) gives every batch exactly what
+    gen_stream_ensemble gives it alone; with prog_w0_at="end" each
+    progenitor is first integrated back in base + its own subhalo (checked
+    against the oracle for one stream)."""
+    from streamsculptor_gb300 import potential as P
+    from streamsculptor_gb300.streamhelpers import gen_stream_ensemble, gen_stream_ensemble_batches
+    n = 80
+    orc, back, ts, normals = _c1_setup(oracle, n_rel=n)
+    ts = np.concatenate([ts[:-1], [ts[-1] + 6.5]])
+    rng = np.random.default_rng(2)
+    perts, shs = [], []
+    for _ in range(3):
+        sh = dict(m=10 ** rng.uniform(6.5, 7.5, 3), a=rng.uniform(0.2, 0.6, 3), x0=rng.normal(0, 9, (3, 3)),
+                  v=rng.normal(0, 0.15, (3, 3)), t0=ts[0] + rng.uniform(10, 70, 3), t_window=50.0)
+        shs.append(sh)
+        perts.append(P.SubhaloLinePotential(sh["m"], sh["a"], sh["x0"], sh["v"], sh["t0"], sh["t_window"],
+                                            units=ss.usys))
+    kw = dict(ts=ts, prog_w0=PROG_WF, Msat=2e4, normals=normals, prog_w0_at="end")
+    for precision in ("f64", "f32k"):
+        outs = gen_stream_ensemble_batches(mw3_gpu(ss), perts, 1, precision=precision, **kw)
+        for i, pert in enumerate(perts):
+            lead, trail = gen_stream_ensemble(mw3_gpu(ss), pert, 1, precision=precision, **kw)
+            assert torch.equal(outs[i][0], lead) and torch.equal(outs[i][1], trail)
+    # stream 1 of batch 2 on the oracle: back from t_end in base + its subhalo, then as usual
+    sh, b = shs[2], 1
+    row = {k: (v[b:b + 1] if isinstance(v, np.ndarray) else v) for k, v in sh.items()}
+    tot = oracle.HostModel(oracle.mw3(), subhalos=dict(row, kind=1))
+    span = ts[-1] - ts[0]
+    n_back = int(np.ceil(span / 1.0 - 1e-9))
+    start = oracle.orbit(tot, PROG_WF, ts[-1], -span / n_back, n_back, n_back)[0, -1]
+    o = _ensemble_oracle(oracle, sh, b, start, ts[:-1], float(ts[-1]), normals, True)
+    assert phase_err(np64(outs[2][0][b]), o[:, 0]) <= 1e-5  # outs holds the f32k run
+    lead64, _ = gen_stream_ensemble(mw3_gpu(ss), perts[2], 1, precision="f64", **kw)
+    assert phase_err(np64(lead64[b]), o[:, 0]) <= 1e-10
+
+
 def test_orbit_ensemble_own_steps(ss, oracle):
     """ss_orbit_ensemble_f64: every orbit with its own step and end time,
     against the oracle orbit of each."""
