@@ -1,4 +1,4 @@
-// ss_pert.cu — first-order response of stream tracks to many subhalos.
+// ss_pert.cu — response of stream tracks to many subhalos.
 //
 // Reference: MassRadiusPerturbation_OTF.term (fields.py:174-206) integrated
 // per particle by GenerateMassRadiusPerturbation.compute_perturbation_OTF
@@ -7,6 +7,10 @@
 // tidal tensor T = -Hessian(Phi_base)(x0) and, per subhalo s,
 //   d/dt (x1, v1)   = (v1,  -grad Phi_s(x0)        + T x1)
 //   d/dt (x1r, v1r) = (v1r, -grad dPhi_s/da_s(x0)  + T x1r)
+// With 18 columns the second-order mass response of
+// MassRadiusPerturbation_OTF_SecondOrder (fields.py:260-320) follows:
+//   d/dt (x2, v2)   = (v2,  T x2 + x1^T (d2a/dx2) x1 - Hessian(Phi_s) x1),
+// which needs the third derivatives of Phi_base on the base track.
 //
 // The base track does not depend on the subhalos, so it is computed once per
 // particle instead of once per (particle, subhalo):
