@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define SS_ABI_VERSION 3
+#define SS_ABI_VERSION 4
 #define SS_MAX_COMPONENTS 16
 
 /* ---------------------------------------------------------------- status */
@@ -48,6 +48,12 @@ typedef enum ss_status {
  *   SS_SH_EXPANSION   p = {scale}                  the potential's ss_expansion table times scale
  *                     (a multipole expansion in place of the reference's optional bfeax
  *                     package; at most one expansion per potential)
+ *   SS_BAR            p = {m, a, b, c, Omega}      BarPotential (Long & Murali 1992), rotating
+ *                                                  about z at Omega           potential.py:178-198
+ *   SS_DEHNEN_BAR     p = {alpha, v0, R0, Rb, phib, Omega}  DehnenBarPotential  potential.py:200-222
+ *                     (the rotating components of one potential share one Omega)
+ *   SS_UNIFORM_ACCEL  p = {}                       UniformAcceleration: gradient dv/dt of the
+ *                     potential's frame_velocity track, no potential value (0)  potential.py:480-502
  * A component with center = SS_CENTER_TRACK is evaluated at x - c(t), where
  * c(t) is the potential's center track: TimeDepTranslatingPotential,
  * potential.py:448-462.  Components are summed in list order
@@ -59,7 +65,10 @@ typedef enum ss_kind {
     SS_HERNQUIST = 4,
     SS_PLUMMER = 5,
     SS_ISOCHRONE = 6,
-    SS_SH_EXPANSION = 7
+    SS_SH_EXPANSION = 7,
+    SS_BAR = 8,
+    SS_DEHNEN_BAR = 9,
+    SS_UNIFORM_ACCEL = 10
 } ss_kind;
 
 /* Largest degree of a spherical-harmonic expansion. */
@@ -81,10 +90,14 @@ typedef struct ss_component {
  * pointers for device entry points. */
 typedef struct ss_track {
     const double* knots;  /* [n_knots, 3] */
-    const double* slopes; /* [n_knots, 3] */
+    const double* slopes; /* [n_knots, 3] (unused when linear) */
     double t0;
     double dt;            /* knot spacing, > 0 */
     int64_t n_knots;      /* >= 2 when any component uses the track */
+    int32_t linear;       /* 1: piecewise-linear through the knots, the end
+                           * segments continued (RegularGridInterpolator(method=
+                           * 'linear', fill_value=None), potential.py:575-590) */
+    int32_t reserved;
 } ss_track;
 
 /* Subhalos moving on straight lines x0 + v (t - t0), active while
@@ -134,6 +147,10 @@ typedef struct ss_potential {
     ss_subhalos subhalos;
     /* Table of the SS_SH_EXPANSION component (unused otherwise). */
     ss_expansion expansion;
+    /* Velocity of the frame through time for SS_UNIFORM_ACCEL (its gradient
+     * is d/dt of this track, a linear track's segment slopes; unused
+     * otherwise): the MW's reflex motion of MW_LMC_Potential, potential.py:555-662. */
+    ss_track frame_velocity;
 } ss_potential;
 
 /* ------------------------------------------------------------- configs */

@@ -76,10 +76,22 @@ class HostModel:
 
     comps: List[Tuple[int, int, Sequence[float]]]
     G: float = G_KPC
-    track: Optional[Tuple[float, float, np.ndarray]] = None  # (t0, dt, knots [n,3])
+    track: Optional[tuple] = None  # (t0, dt, knots [n,3]) or (t0, dt, knots, "linear")
     subhalos: Optional[dict] = None  # kind, m, a, x0, v, t0, t_window
     expansion: Optional[tuple] = None  # (l_max, log_r0, dlog_r, coef [n_knots, (l_max+1)^2, 2])
+    frame_velocity: Optional[tuple] = None  # (t0, dt, velocities [n,3]) or (..., "linear")
     _keep: list = field(default_factory=list)
+
+    def _track(self, spec) -> _abi.ss_track:
+        t0, dt, knots = spec[:3]
+        linear = len(spec) > 3 and spec[3] == "linear"
+        knots = f8(knots)
+        slopes = track_slopes(knots, dt)
+        self._keep += [knots, slopes]
+        tr = _abi.ss_track()
+        tr.knots, tr.slopes = knots.ctypes.data, slopes.ctypes.data
+        tr.t0, tr.dt, tr.n_knots, tr.linear = t0, dt, knots.shape[0], int(linear)
+        return tr
 
     def struct(self) -> _abi.ss_potential:
         P = _abi.ss_potential()
@@ -91,15 +103,9 @@ class HostModel:
             for j, v in enumerate(params):
                 P.comp[i].p[j] = float(v)
         if self.track is not None:
-            t0, dt, knots = self.track
-            knots = f8(knots)
-            slopes = track_slopes(knots, dt)
-            self._keep += [knots, slopes]
-            P.track.knots = knots.ctypes.data
-            P.track.slopes = slopes.ctypes.data
-            P.track.t0 = t0
-            P.track.dt = dt
-            P.track.n_knots = knots.shape[0]
+            P.track = self._track(self.track)
+        if self.frame_velocity is not None:
+            P.frame_velocity = self._track(self.frame_velocity)
         if self.subhalos is not None:
             P.subhalos = self.sh_struct()
         if self.expansion is not None:

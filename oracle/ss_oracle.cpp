@@ -138,6 +138,27 @@ template <class T, int N>
 Dual<T, N> pow_(const Dual<T, N>& x, double p) {
     return chain(x, pow_(x.v, p), p * pow_(x.v, p - 1.0));
 }
+inline double cos_(double x) { return std::cos(x); }
+inline double sin_(double x) { return std::sin(x); }
+inline double atan2_(double y, double x) { return std::atan2(y, x); }
+template <class T, int N>
+Dual<T, N> cos_(const Dual<T, N>& x) {
+    return chain(x, cos_(x.v), -sin_(x.v));
+}
+template <class T, int N>
+Dual<T, N> sin_(const Dual<T, N>& x) {
+    return chain(x, sin_(x.v), cos_(x.v));
+}
+// atan2 with d/dy = x / (x^2 + y^2), d/dx = -y / (x^2 + y^2)
+template <class T, int N>
+Dual<T, N> atan2_(const Dual<T, N>& y, const Dual<T, N>& x) {
+    Dual<T, N> r;
+    r.v = atan2_(y.v, x.v);
+    T den = x.v * x.v + y.v * y.v;
+    T a = x.v / den, b = -y.v / den;
+    for (int i = 0; i < N; ++i) r.d[i] = a * y.d[i] + b * x.d[i];
+    return r;
+}
 template <class T, int N>
 double value(const Dual<T, N>& x) {
     return value(x.v);
@@ -172,6 +193,10 @@ static void track_eval(const ss_track& tr, double t, double c[3]) {
     if (k < 0) k = 0;
     if (k > tr.n_knots - 2) k = tr.n_knots - 2;
     double s = u - (double)k;
+    if (tr.linear) {  // RegularGridInterpolator(method='linear', fill_value=None)
+        for (int i = 0; i < 3; ++i) c[i] = tr.knots[3 * k + i] + s * (tr.knots[3 * (k + 1) + i] - tr.knots[3 * k + i]);
+        return;
+    }
     double s2 = s * s, s3 = s2 * s;
     double h00 = 2 * s3 - 3 * s2 + 1;
     double h10 = s3 - 2 * s2 + s;
@@ -181,6 +206,29 @@ static void track_eval(const ss_track& tr, double t, double c[3]) {
         double p0 = tr.knots[3 * k + i], p1 = tr.knots[3 * (k + 1) + i];
         double m0 = tr.slopes[3 * k + i], m1 = tr.slopes[3 * (k + 1) + i];
         c[i] = h00 * p0 + h10 * tr.dt * m0 + h01 * p1 + h11 * tr.dt * m1;
+    }
+}
+
+// d/dt of a track by central differences of track_eval inside the segment
+// holding t (exact for the linear form; the cubic form's derivative to
+// round-off of the difference), jax.jacfwd of the velocity spline in
+// UniformAcceleration.gradient (potential.py:497-499).
+static void track_deriv(const ss_track& tr, double t, double d[3]) {
+    double u = (t - tr.t0) / tr.dt;
+    int64_t k = (int64_t)std::floor(u);
+    if (k < 0) k = 0;
+    if (k > tr.n_knots - 2) k = tr.n_knots - 2;
+    if (tr.linear) {
+        for (int i = 0; i < 3; ++i) d[i] = (tr.knots[3 * (k + 1) + i] - tr.knots[3 * k + i]) / tr.dt;
+        return;
+    }
+    double s = u - (double)k;
+    for (int i = 0; i < 3; ++i) {
+        double p0 = tr.knots[3 * k + i], p1 = tr.knots[3 * (k + 1) + i];
+        double m0 = tr.slopes[3 * k + i], m1 = tr.slopes[3 * (k + 1) + i];
+        // derivative of the Hermite basis, chain factor 1/dt
+        d[i] = ((6 * s * s - 6 * s) * p0 + (3 * s * s - 4 * s + 1) * tr.dt * m0 + (-6 * s * s + 6 * s) * p1 +
+                (3 * s * s - 2 * s) * tr.dt * m1) / tr.dt;
     }
 }
 
@@ -220,6 +268,39 @@ S phi_component(const ss_component& c, double G, const S x[3]) {
         }
         default:
             return S(std::numeric_limits<double>::quiet_NaN());
+    }
+}
+
+// Time-dependent components.
+template <class S>
+S phi_component_t(const ss_component& c, double G, const S x[3], double t, const ss_track& fvel) {
+    const double* p = c.p;
+    switch (c.kind) {
+        case SS_BAR: {  // BarPotential.potential, potential.py:185-198: rotate by ang = -Omega t
+            double ang = -p[4] * t;
+            double R00 = std::cos(ang), R01 = -std::sin(ang), R10 = std::sin(ang), R11 = std::cos(ang);
+            S xc = R00 * x[0] + R01 * x[1], yc = R10 * x[0] + R11 * x[1], zc = x[2];
+            S bz = p[2] + sqrt_(p[3] * p[3] + zc * zc);
+            S Tp = sqrt_((p[1] + xc) * (p[1] + xc) + yc * yc + bz * bz);
+            S Tm = sqrt_((p[1] - xc) * (p[1] - xc) + yc * yc + bz * bz);
+            return (G * p[0] / (2.0 * p[1])) * log_((xc - p[1] + Tm) / (xc + p[1] + Tp));
+        }
+        case SS_DEHNEN_BAR: {  // DehnenBarPotential.potential, potential.py:205-222
+            S phi = atan2_(x[1], x[0]);
+            S R2 = x[0] * x[0] + x[1] * x[1];
+            S r2 = R2 + x[2] * x[2];
+            S r = sqrt_(r2);
+            S U = value(r) >= p[3] ? -pow_(r / p[3], -3.0) : pow_(r / p[3], 3.0) - 2.0;
+            double pref = p[0] * (p[1] * p[1] / 3.0) * std::pow(p[2] / p[3], 3.0);
+            return pref * (R2 / r2) * U * cos_(2.0 * (phi - p[4] - p[5] * t));
+        }
+        case SS_UNIFORM_ACCEL: {  // gradient dv/dt (potential.py:497-499): Phi = (dv/dt) . x
+            double d[3];
+            track_deriv(fvel, t, d);
+            return d[0] * x[0] + d[1] * x[1] + d[2] * x[2];
+        }
+        default:
+            return phi_component(c, G, x);
     }
 }
 
@@ -317,10 +398,10 @@ S phi_total(const ss_potential& P, const S x[3], double t) {
             }
             S xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
             acc = acc + (comp.kind == SS_SH_EXPANSION ? phi_expansion(P.expansion, comp.p[0], xs)
-                                                      : phi_component(comp, P.G, xs));
+                                                      : phi_component_t(comp, P.G, xs, t, P.frame_velocity));
         } else {
             acc = acc + (comp.kind == SS_SH_EXPANSION ? phi_expansion(P.expansion, comp.p[0], x)
-                                                      : phi_component(comp, P.G, x));
+                                                      : phi_component_t(comp, P.G, x, t, P.frame_velocity));
         }
     }
     const ss_subhalos& sh = P.subhalos;

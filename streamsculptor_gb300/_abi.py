@@ -10,7 +10,7 @@ import ctypes as C
 import os
 import threading
 
-SS_ABI_VERSION = 3
+SS_ABI_VERSION = 4
 SS_MAX_COMPONENTS = 16
 
 SS_OK = 0
@@ -27,6 +27,9 @@ SS_HERNQUIST = 4
 SS_PLUMMER = 5
 SS_ISOCHRONE = 6
 SS_SH_EXPANSION = 7
+SS_BAR = 8
+SS_DEHNEN_BAR = 9
+SS_UNIFORM_ACCEL = 10
 SS_SHEXP_LMAX = 8
 
 SS_CENTER_ORIGIN = 0
@@ -48,7 +51,7 @@ class ss_component(C.Structure):
 
 class ss_track(C.Structure):
     _fields_ = [("knots", VP), ("slopes", VP), ("t0", C.c_double), ("dt", C.c_double),
-                ("n_knots", C.c_int64)]
+                ("n_knots", C.c_int64), ("linear", C.c_int32), ("reserved", C.c_int32)]
 
 
 class ss_subhalos(C.Structure):
@@ -64,7 +67,7 @@ class ss_expansion(C.Structure):
 class ss_potential(C.Structure):
     _fields_ = [("G", C.c_double), ("n_components", C.c_int32), ("reserved", C.c_int32),
                 ("comp", ss_component * SS_MAX_COMPONENTS), ("track", ss_track),
-                ("subhalos", ss_subhalos), ("expansion", ss_expansion)]
+                ("subhalos", ss_subhalos), ("expansion", ss_expansion), ("frame_velocity", ss_track)]
 
 
 class ss_stream_cfg(C.Structure):

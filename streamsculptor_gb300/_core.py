@@ -97,6 +97,23 @@ class CenterTrack:
     dt: float
     knots: torch.Tensor  # [n, 3] float64 (device)
     slopes: Optional[torch.Tensor] = None
+    # piecewise-linear through the knots instead (the reference's
+    # RegularGridInterpolator(method='linear') tracks, potential.py:575-590)
+    linear: bool = False
+
+    @staticmethod
+    def linear_from_samples(ts, values) -> "CenterTrack":
+        t = CenterTrack.from_samples(ts, values)
+        t.linear = True
+        return t
+
+    def struct(self) -> _abi.ss_track:
+        tr = _abi.ss_track()
+        tr.knots = self.knots.data_ptr()
+        if not self.linear:
+            tr.slopes = self.ensure_slopes().data_ptr()
+        tr.t0, tr.dt, tr.n_knots, tr.linear = self.t0, self.dt, self.knots.shape[0], int(self.linear)
+        return tr
 
     @staticmethod
     def from_samples(ts, positions) -> "CenterTrack":
@@ -170,6 +187,7 @@ class Flat:
     track: Optional[CenterTrack] = None
     subhalos: Optional[SubhaloTable] = None
     expansion: Optional[ExpansionTable] = None
+    frame_velocity: Optional[CenterTrack] = None
 
     def extend(self, other: "Flat"):
         self.comps.extend(other.comps)
@@ -185,6 +203,10 @@ class Flat:
             if self.expansion is not None and self.expansion is not other.expansion:
                 raise NotImplementedError("at most one spherical-harmonic expansion per potential")
             self.expansion = other.expansion
+        if other.frame_velocity is not None:
+            if self.frame_velocity is not None and self.frame_velocity is not other.frame_velocity:
+                raise NotImplementedError("at most one uniform frame acceleration per potential")
+            self.frame_velocity = other.frame_velocity
 
 
 def make_struct(flat: Flat, G: float) -> _abi.ss_potential:
@@ -199,12 +221,9 @@ def make_struct(flat: Flat, G: float) -> _abi.ss_potential:
         for j, v in enumerate(params):
             P.comp[i].p[j] = float(v)
     if flat.track is not None:
-        flat.track.ensure_slopes()
-        P.track.knots = flat.track.knots.data_ptr()
-        P.track.slopes = flat.track.slopes.data_ptr()
-        P.track.t0 = flat.track.t0
-        P.track.dt = flat.track.dt
-        P.track.n_knots = flat.track.knots.shape[0]
+        P.track = flat.track.struct()
+    if flat.frame_velocity is not None:
+        P.frame_velocity = flat.frame_velocity.struct()
     if flat.subhalos is not None:
         P.subhalos = flat.subhalos.struct()
     if flat.expansion is not None:
@@ -323,9 +342,14 @@ def orbit_ensemble(P, w0: torch.Tensor, t0: float, dt, n_steps: int, save_every:
     return out
 
 
+TIME_DEPENDENT_KINDS = (_abi.SS_BAR, _abi.SS_DEHNEN_BAR, _abi.SS_UNIFORM_ACCEL)
+
+
 def is_static(P) -> bool:
-    """True when the descriptor has no center-track component and no subhalos."""
-    return P.subhalos.n == 0 and all(P.comp[i].center == _abi.SS_CENTER_ORIGIN for i in range(P.n_components))
+    """True when the descriptor has no center-track, rotating or frame-
+    acceleration component and no subhalos."""
+    return P.subhalos.n == 0 and all(P.comp[i].center == _abi.SS_CENTER_ORIGIN and
+                                     P.comp[i].kind not in TIME_DEPENDENT_KINDS for i in range(P.n_components))
 
 
 def release(P, cfg, prog_w, t_rel, msat, normals, jac=False):

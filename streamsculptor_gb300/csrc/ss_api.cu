@@ -97,6 +97,39 @@ int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalo
                 out->ex.lmax = e.l_max;
                 break;
             }
+            case SS_BAR:
+            case SS_DEHNEN_BAR: {
+                const double om = c.kind == SS_BAR ? p[4] : p[5];
+                SS_CHECK_ARG(!out->has_rot || out->omega == om,
+                             "component %d: the rotating components of one potential need one pattern speed", k);
+                out->has_rot = 1;
+                out->omega = om;
+                if (c.kind == SS_BAR) {
+                    SS_CHECK_ARG(p[1] > 0.0 && p[2] >= 0.0 && p[3] >= 0.0, "component %d (Bar): need a > 0, b, c >= 0",
+                                 k);
+                    d.q[0] = R(G * p[0] / (2.0 * p[1])); d.q[1] = R(p[1]); d.q[2] = R(p[2]); d.q[3] = R(p[3] * p[3]);
+                } else {
+                    SS_CHECK_ARG(p[3] > 0.0, "component %d (DehnenBar): need Rb > 0", k);
+                    const double rr = p[2] / p[3];
+                    d.q[0] = R(p[0] * p[1] * p[1] / 3.0 * rr * rr * rr); d.q[1] = R(p[3]);
+                    d.q[2] = R(cos(2.0 * p[4])); d.q[3] = R(sin(2.0 * p[4]));
+                }
+                break;
+            }
+            case SS_UNIFORM_ACCEL: {
+                const ss_track& fv = in->frame_velocity;
+                SS_CHECK_ARG(fv.knots != nullptr && fv.n_knots >= 2 && std::isfinite(fv.dt) && fv.dt > 0.0 &&
+                                 std::isfinite(fv.t0) && (fv.linear || fv.slopes != nullptr),
+                             "component %d (UniformAcceleration): frame_velocity track needs >= 2 knots, dt > 0", k);
+                out->has_facc = 1;
+                out->fvel.knots = fv.knots;
+                out->fvel.slopes = fv.slopes;
+                out->fvel.t0 = fv.t0;
+                out->fvel.dt = fv.dt;
+                out->fvel.n = fv.n_knots;
+                out->fvel.linear = fv.linear ? 1 : 0;
+                break;
+            }
             default:
                 return set_error(SS_ERR_INVALID_ARGUMENT, "component %d: unknown kind %d", k, c.kind);
         }
@@ -104,7 +137,7 @@ int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalo
     out->has_track = need_track ? 1 : 0;
     if (need_track) {
         const ss_track& tr = in->track;
-        SS_CHECK_ARG(tr.knots != nullptr && tr.slopes != nullptr, "center track: knots/slopes NULL");
+        SS_CHECK_ARG(tr.knots != nullptr && (tr.linear || tr.slopes != nullptr), "center track: knots/slopes NULL");
         SS_CHECK_ARG(tr.n_knots >= 2, "center track: need >= 2 knots");
         SS_CHECK_ARG(std::isfinite(tr.dt) && tr.dt > 0.0 && std::isfinite(tr.t0), "center track: need dt > 0");
         out->track.knots = tr.knots;
@@ -112,6 +145,7 @@ int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalo
         out->track.t0 = tr.t0;
         out->track.dt = tr.dt;
         out->track.n = tr.n_knots;
+        out->track.linear = tr.linear ? 1 : 0;
     }
     const ss_subhalos& sh = in->subhalos;
     SS_CHECK_ARG(sh.n >= 0 && sh.n <= (int64_t)1 << 30, "subhalos: bad n");
@@ -137,10 +171,28 @@ template int prepare_potential<double>(const ss_potential*, PotDev<double>*, boo
 template int prepare_potential<float>(const ss_potential*, PotDev<float>*, bool);
 
 // ------------------------------------------------------------- Phi (FP64)
-__device__ double comp_phi(const PotDev<double>& P, const CompDev<double>& c, const double x[3]) {
+__device__ double comp_phi(const PotDev<double>& P, const CompDev<double>& c, const double xin[3],
+                           const TimeDep<double>& td = TimeDep<double>()) {
     const double* q = c.q;
+    // rotating components: their corotating-frame position
+    const bool rot = c.kind == SS_BAR || c.kind == SS_DEHNEN_BAR;
+    const double x[3] = {rot ? td.c * xin[0] + td.s * xin[1] : xin[0], rot ? td.c * xin[1] - td.s * xin[0] : xin[1],
+                         xin[2]};
     double r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
     switch (c.kind) {
+        case SS_BAR: {
+            const double B = q[2] + sqrt(q[3] + x[2] * x[2]);
+            const double rho2 = x[1] * x[1] + B * B;
+            const double wm = x[0] - q[1], wp = x[0] + q[1];
+            return q[0] * log((wm + sqrt(wm * wm + rho2)) / (wp + sqrt(wp * wp + rho2)));
+        }
+        case SS_DEHNEN_BAR: {
+            const double r = sqrt(r2), Rb = q[1];
+            const double W = r >= Rb ? -Rb * Rb * Rb / (r2 * r2 * r) : r / (Rb * Rb * Rb) - 2.0 / r2;
+            return q[0] * W * ((x[0] * x[0] - x[1] * x[1]) * q[2] + 2.0 * x[0] * x[1] * q[3]);
+        }
+        case SS_UNIFORM_ACCEL:
+            return 0.0;  // a force without a potential (UniformAcceleration.potential raises)
         case SS_SH_EXPANSION:
             return shexp_phi(P.ex, q[0], x);
         case SS_NFW: {
@@ -176,14 +228,15 @@ __global__ void potential_eval_kernel(PotDev<double> P, const double* __restrict
     double x[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
     double c[3] = {0.0, 0.0, 0.0};
     if (P.has_track) track_eval(P.track, t, c);
+    const TimeDep<double> td = time_dep(P, t);
     if (phi) {
         double f = 0.0;
         for (int k = 0; k < P.n; ++k) {
             if (P.c[k].center == SS_CENTER_TRACK) {
                 double xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
-                f += comp_phi(P, P.c[k], xs);
+                f += comp_phi(P, P.c[k], xs, td);
             } else {
-                f += comp_phi(P, P.c[k], x);
+                f += comp_phi(P, P.c[k], x, td);
             }
         }
         for (int j = 0; j < P.sh.n; ++j) {
@@ -200,7 +253,7 @@ __global__ void potential_eval_kernel(PotDev<double> P, const double* __restrict
     if (grad || hess) {
         double g[3], H[6];
         const double xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
-        pot_grad<double, double, true>(P, x, xs, g, H);
+        pot_grad<double, double, true>(P, x, xs, g, H, td);
         if (P.sh.n > 0) subhalo_sum_grad<double>(P.sh, x, t, g);
         if (grad)
             for (int k = 0; k < 3; ++k) grad[3 * i + k] = g[k];

@@ -86,7 +86,7 @@ __device__ __forceinline__ void accel_f64(const PotDev<double>& P, const ShDev& 
     if (P.has_track) track_eval(P.track, t, c);
     const double xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
     double g[3];
-    C::template grad<double, double, false>(P, x, xs, g, nullptr);
+    C::template grad<double, double, false>(P, x, xs, g, nullptr, time_dep(P, t));
     if (sh.n > 0) subhalo_sum_grad<double>(sh, x, t, g);
     a[0] = -g[0];
     a[1] = -g[1];

@@ -173,6 +173,7 @@ struct TrackDev {
     double t0;
     double dt;
     int64_t n;
+    int32_t linear;  // 1: piecewise-linear through the knots (slopes unused)
 };
 
 struct ShDev {
@@ -195,6 +196,23 @@ struct PotDev {
     TrackDev track;
     ShDev sh;
     ExpDev ex;
+    // time-dependent parts: the pattern speed shared by the rotating
+    // components, and the frame-velocity track of SS_UNIFORM_ACCEL
+    double omega;
+    int32_t has_rot;
+    int32_t has_facc;
+    TrackDev fvel;
+};
+
+// What the time-dependent components need at one evaluation time: the
+// rotation (c, s) = (cos, sin)(omega t) of the rotating components' frame
+// and the gradient ga = dv_frame/dt of SS_UNIFORM_ACCEL.  FP64 callers form
+// it from t (time_dep), the FP32 stream reads it per stage from a table.
+template <class T>
+struct TimeDep {
+    T c, s;
+    T ga[3];
+    __host__ __device__ TimeDep() : c(T(1)), s(T(0)) { ga[0] = ga[1] = ga[2] = T(0); }
 };
 
 // --------------------------------------------------------------- track
@@ -206,6 +224,14 @@ __device__ inline void track_eval(const TrackDev& tr, double t, double c[3]) {
     if (k < 0) k = 0;
     if (k > tr.n - 2) k = tr.n - 2;
     double s = u - (double)k;
+    if (tr.linear) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            double p0 = __ldg(tr.knots + 3 * k + i), p1 = __ldg(tr.knots + 3 * (k + 1) + i);
+            c[i] = p0 + s * (p1 - p0);
+        }
+        return;
+    }
     double s2 = s * s, s3 = s2 * s;
     double h00 = 2.0 * s3 - 3.0 * s2 + 1.0;
     double h10 = s3 - 2.0 * s2 + s;
@@ -217,6 +243,48 @@ __device__ inline void track_eval(const TrackDev& tr, double t, double c[3]) {
         double m0 = __ldg(tr.slopes + 3 * k + i), m1 = __ldg(tr.slopes + 3 * (k + 1) + i);
         c[i] = h00 * p0 + h10 * tr.dt * m0 + h01 * p1 + h11 * tr.dt * m1;
     }
+}
+
+// d/dt of the piecewise-linear frame-velocity track at t: the slope of the
+// segment holding t (the end segments continue outside the knots), the
+// derivative of a linear RegularGridInterpolator.
+// A cubic track gives the derivative of its Hermite segment.
+__device__ inline void track_slope(const TrackDev& tr, double t, double d[3]) {
+    double u = (t - tr.t0) / tr.dt;
+    int64_t k = (int64_t)floor(u);
+    if (k < 0) k = 0;
+    if (k > tr.n - 2) k = tr.n - 2;
+    const double s = u - (double)k;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const double p0 = __ldg(tr.knots + 3 * k + i), p1 = __ldg(tr.knots + 3 * (k + 1) + i);
+        if (tr.linear) {
+            d[i] = (p1 - p0) / tr.dt;
+        } else {
+            const double m0 = __ldg(tr.slopes + 3 * k + i), m1 = __ldg(tr.slopes + 3 * (k + 1) + i);
+            d[i] = ((6.0 * s * s - 6.0 * s) * (p0 - p1)) / tr.dt + (3.0 * s * s - 4.0 * s + 1.0) * m0 +
+                   (3.0 * s * s - 2.0 * s) * m1;
+        }
+    }
+}
+
+template <class R>
+__device__ inline TimeDep<double> time_dep(const PotDev<R>& P, double t) {
+    TimeDep<double> td;
+    if (P.has_rot) sincos(P.omega * t, &td.s, &td.c);
+    if (P.has_facc) track_slope(P.fvel, t, td.ga);
+    return td;
+}
+
+template <class T, class S>
+__device__ __forceinline__ TimeDep<T> time_dep_as(const TimeDep<S>& a) {
+    TimeDep<T> r;
+    r.c = T(a.c);
+    r.s = T(a.s);
+    r.ga[0] = T(a.ga[0]);
+    r.ga[1] = T(a.ga[1]);
+    r.ga[2] = T(a.ga[2]);
+    return r;
 }
 
 // ------------------------------------------------- spherical profiles
@@ -383,10 +451,131 @@ __device__ __forceinline__ void kind_grad(const R* q, const T x[3], T grad[3], T
     }
 }
 
+// Rotating bars, evaluated in the frame turning with pattern speed omega:
+// x' = (c x + s y, -s x + c y, z) with (c, s) = (cos, sin)(omega t), so
+// grad = R^T grad' and H = R^T H' R (BarPotential, potential.py:178-198:
+// the simulation-frame point rotated by -omega t).
+//
+// SS_BAR, Long & Murali (1992) eq. 8a: Phi' = K [g(X - a) - g(X + a)],
+// K = G m / 2a, g(w) = ln(w + T), T = sqrt(w^2 + Y^2 + B^2),
+// B = b + sqrt(c^2 + z^2); q = {K, a, b, c^2}.  With Q = 1 / (T (w + T)):
+// dg/dw = 1/T, dg/dY = Y Q, dg/dz = B B' Q, and the second derivatives below.
+template <class T, class R, bool HESS>
+__device__ __forceinline__ void bar_lm_grad(const R* q, const T xp[3], T g[3], T H[6]) {
+    const T X = xp[0], Y = xp[1], z = xp[2];
+    const T S = s_sqrt(T(q[3]) + z * z);
+    const T B = T(q[2]) + S;
+    const T Bp = z * s_rcp(S);  // dB/dz
+    const T rho2 = Y * Y + B * B;
+    T acc[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};  // d2 xx yy zz xy xz yz
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+        const T w = side == 0 ? X - T(q[1]) : X + T(q[1]);
+        const R sg = side == 0 ? R(1) : R(-1);
+        const T Tn = s_sqrt(w * w + rho2);
+        const T iT = s_rcp(Tn);
+        const T Q = iT * s_rcp(w + Tn);
+        g[0] += T(q[0]) * sg * iT;
+        g[1] += T(q[0]) * sg * Y * Q;
+        g[2] += T(q[0]) * sg * B * Bp * Q;
+        if constexpr (HESS) {
+            const T iT3 = iT * iT * iT;
+            const T E = Q * (iT * iT + Q);  // -dQ/dY / Y
+            const T Bpp = T(q[3]) * s_rcp(S * S * S);
+            acc[0] += sg * (-w * iT3);
+            acc[3] += sg * (-Y * iT3);
+            acc[4] += sg * (-B * Bp * iT3);
+            acc[1] += sg * (Q - Y * Y * E);
+            acc[5] += sg * (-Y * B * Bp * E);
+            acc[2] += sg * ((Bp * Bp + B * Bpp) * Q - B * B * Bp * Bp * E);
+        }
+    }
+    if constexpr (HESS) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) H[i] = T(q[0]) * acc[i];
+    }
+}
+
+// SS_DEHNEN_BAR (DehnenBarPotential, potential.py:200-222) in its corotating
+// frame: Phi' = A W(r) P2, P2 = (x'^2 - y'^2) cos 2phi_b + 2 x'y' sin 2phi_b,
+// W = U(r)/r^2: -Rb^3 r^-5 for r >= Rb, r/Rb^3 - 2/r^2 inside;
+// q = {A, Rb, cos 2phi_b, sin 2phi_b}, A = alpha v0^2/3 (R0/Rb)^3.
+template <class T, class R, bool HESS>
+__device__ __forceinline__ void bar_dehnen_grad(const R* q, const T xp[3], T g[3], T H[6]) {
+    const T x = xp[0], y = xp[1], z = xp[2];
+    const T r2 = x * x + y * y + z * z;
+    const T r = s_sqrt(r2), ir = s_rcp(r);
+    const R Rb = q[1], Rb3 = q[1] * q[1] * q[1];
+    T W, W1, W2;  // W, dW/dr, d2W/dr2
+    if (sval(r) >= (double)Rb) {
+        const T ir2 = ir * ir, ir5 = ir2 * ir2 * ir;
+        W = T(-Rb3) * ir5;
+        W1 = T(R(5) * Rb3) * ir5 * ir;
+        W2 = T(R(-30) * Rb3) * ir5 * ir2;
+    } else {
+        const T ir2 = ir * ir;
+        W = r * T(R(1) / Rb3) - T(R(2)) * ir2;
+        W1 = T(R(1) / Rb3) + T(R(4)) * ir2 * ir;
+        W2 = T(R(-12)) * ir2 * ir2;
+    }
+    const T C2 = T(q[2]), S2 = T(q[3]);
+    const T P2 = (x * x - y * y) * C2 + T(R(2)) * x * y * S2;
+    const T dP[3] = {T(R(2)) * (x * C2 + y * S2), T(R(2)) * (x * S2 - y * C2), T(0)};
+    const T u[3] = {x * ir, y * ir, z * ir};
+    const T A = T(q[0]);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) g[i] += A * (W1 * u[i] * P2 + W * dP[i]);
+    if constexpr (HESS) {
+        // A [W'' u u^T P2 + W' (I - u u^T)/r P2 + W' (u dP^T + dP u^T) + W d2P]
+        const int ia[6] = {0, 1, 2, 0, 0, 1}, ib[6] = {0, 1, 2, 1, 2, 2};
+        const T d2P[6] = {T(R(2)) * C2, T(R(-2)) * C2, T(0), T(R(2)) * S2, T(0), T(0)};
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const int i = ia[k], j = ib[k];
+            const T uu = u[i] * u[j];
+            const T id = i == j ? T(1) : T(0);
+            H[k] = A * (W2 * uu * P2 + W1 * (id - uu) * ir * P2 + W1 * (u[i] * dP[j] + dP[i] * u[j]) + W * d2P[k]);
+        }
+    }
+}
+
+// A rotating component at x (simulation frame), added to grad / H.
+template <int KIND, class T, class R, bool HESS>
+__device__ __forceinline__ void rot_grad(const R* q, const T x[3], const TimeDep<T>& td, T grad[3], T H[6]) {
+    const T xp[3] = {td.c * x[0] + td.s * x[1], td.c * x[1] - td.s * x[0], x[2]};
+    T gp[3] = {T(0), T(0), T(0)}, Hp[6];
+    if constexpr (KIND == SS_BAR)
+        bar_lm_grad<T, R, HESS>(q, xp, gp, Hp);
+    else
+        bar_dehnen_grad<T, R, HESS>(q, xp, gp, Hp);
+    grad[0] += td.c * gp[0] - td.s * gp[1];
+    grad[1] += td.s * gp[0] + td.c * gp[1];
+    grad[2] += gp[2];
+    if constexpr (HESS) {
+        // H = R^T H' R, R = [[c, s, 0], [-s, c, 0], [0, 0, 1]]
+        const T c = td.c, s = td.s;
+        const T a = Hp[0], b = Hp[1], e = Hp[3], f = Hp[4], h = Hp[5];
+        H[0] += c * c * a - T(R(2)) * c * s * e + s * s * b;
+        H[1] += s * s * a + T(R(2)) * c * s * e + c * c * b;
+        H[2] += Hp[2];
+        H[3] += c * s * (a - b) + (c * c - s * s) * e;
+        H[4] += c * f - s * h;
+        H[5] += s * f + c * h;
+    }
+}
+
 // Runtime-kind dispatch (the generic path for any composition).
 template <class T, class R, bool HESS>
-__device__ __forceinline__ void comp_grad(const CompDev<R>& c, const T x[3], T grad[3], T H[6]) {
+__device__ __forceinline__ void comp_grad(const CompDev<R>& c, const T x[3], T grad[3], T H[6],
+                                          const TimeDep<T>& td = TimeDep<T>()) {
     switch (c.kind) {
+        case SS_BAR: rot_grad<SS_BAR, T, R, HESS>(c.q, x, td, grad, H); break;
+        case SS_DEHNEN_BAR: rot_grad<SS_DEHNEN_BAR, T, R, HESS>(c.q, x, td, grad, H); break;
+        case SS_UNIFORM_ACCEL:
+            grad[0] += td.ga[0];
+            grad[1] += td.ga[1];
+            grad[2] += td.ga[2];
+            break;
         case SS_NFW: kind_grad<SS_NFW, T, R, HESS>(c.q, x, grad, H); break;
         case SS_TRIAXIAL_NFW: kind_grad<SS_TRIAXIAL_NFW, T, R, HESS>(c.q, x, grad, H); break;
         case SS_MIYAMOTO_NAGAI: kind_grad<SS_MIYAMOTO_NAGAI, T, R, HESS>(c.q, x, grad, H); break;
@@ -1136,7 +1325,8 @@ __device__ __forceinline__ void subhalo_grad(int kind, T Gm, T a, const T rel[3]
 // time (used by SS_CENTER_TRACK components; callers that can form it more
 // accurately than x - c pass it directly).
 template <class T, class R, bool HESS>
-__device__ __forceinline__ void pot_grad(const PotDev<R>& P, const T x[3], const T xs[3], T grad[3], T H[6]) {
+__device__ __forceinline__ void pot_grad(const PotDev<R>& P, const T x[3], const T xs[3], T grad[3], T H[6],
+                                         const TimeDep<T>& td = TimeDep<T>()) {
     grad[0] = grad[1] = grad[2] = T(0);
     if (HESS) {
 #pragma unroll
@@ -1148,7 +1338,7 @@ __device__ __forceinline__ void pot_grad(const PotDev<R>& P, const T x[3], const
         if (c.kind == SS_SH_EXPANSION)
             shexp_grad<T, R, HESS>(P.ex, c.q[0], c.center == SS_CENTER_TRACK ? xs : x, grad, H);
         else
-            comp_grad<T, R, HESS>(c, c.center == SS_CENTER_TRACK ? xs : x, grad, H);
+            comp_grad<T, R, HESS>(c, c.center == SS_CENTER_TRACK ? xs : x, grad, H, td);
     }
 }
 
@@ -1165,24 +1355,32 @@ struct Comp {
     static constexpr int n = sizeof...(KCS);
     template <class T, class R, bool HESS, int... I>
     static __device__ __forceinline__ void add(const PotDev<R>& P, const T x[3], const T xs[3], T grad[3], T H[6],
-                                               std::integer_sequence<int, I...>) {
-        (one<(KCS & 15), T, R, HESS>(P, I, (KCS >> 4) ? xs : x, grad, H), ...);
+                                               const TimeDep<T>& td, std::integer_sequence<int, I...>) {
+        (one<(KCS & 15), T, R, HESS>(P, I, (KCS >> 4) ? xs : x, grad, H, td), ...);
     }
     template <int KIND, class T, class R, bool HESS>
-    static __device__ __forceinline__ void one(const PotDev<R>& P, int i, const T x[3], T grad[3], T H[6]) {
+    static __device__ __forceinline__ void one(const PotDev<R>& P, int i, const T x[3], T grad[3], T H[6],
+                                               const TimeDep<T>& td) {
         if constexpr (KIND == SS_SH_EXPANSION)
             shexp_grad<T, R, HESS>(P.ex, P.c[i].q[0], x, grad, H);
-        else
+        else if constexpr (KIND == SS_BAR || KIND == SS_DEHNEN_BAR)
+            rot_grad<KIND, T, R, HESS>(P.c[i].q, x, td, grad, H);
+        else if constexpr (KIND == SS_UNIFORM_ACCEL) {
+            grad[0] += td.ga[0];
+            grad[1] += td.ga[1];
+            grad[2] += td.ga[2];
+        } else
             kind_grad<KIND, T, R, HESS>(P.c[i].q, x, grad, H);
     }
     template <class T, class R, bool HESS>
-    static __device__ __forceinline__ void grad(const PotDev<R>& P, const T x[3], const T xs[3], T g[3], T H[6]) {
+    static __device__ __forceinline__ void grad(const PotDev<R>& P, const T x[3], const T xs[3], T g[3], T H[6],
+                                                const TimeDep<T>& td = TimeDep<T>()) {
         g[0] = g[1] = g[2] = T(0);
         if (HESS) {
 #pragma unroll
             for (int i = 0; i < 6; ++i) H[i] = T(0);
         }
-        add<T, R, HESS>(P, x, xs, g, H, std::make_integer_sequence<int, n>{});
+        add<T, R, HESS>(P, x, xs, g, H, td, std::make_integer_sequence<int, n>{});
     }
     template <class R>
     static bool matches(const PotDev<R>& P) {
@@ -1196,8 +1394,9 @@ struct Comp {
 
 struct GenericComp {
     template <class T, class R, bool HESS>
-    static __device__ __forceinline__ void grad(const PotDev<R>& P, const T x[3], const T xs[3], T g[3], T H[6]) {
-        pot_grad<T, R, HESS>(P, x, xs, g, H);
+    static __device__ __forceinline__ void grad(const PotDev<R>& P, const T x[3], const T xs[3], T g[3], T H[6],
+                                                const TimeDep<T>& td = TimeDep<T>()) {
+        pot_grad<T, R, HESS>(P, x, xs, g, H, td);
     }
 };
 

@@ -369,7 +369,8 @@ __device__ __noinline__ void mlp_grad_wg(const MlpDev& M, const MlpCta& cx, floa
 struct MlpComp {
     static constexpr int n = 1;
     template <class T, class R, bool HESS>
-    static __device__ __forceinline__ void grad(const PotDev<R>& P, const T x[3], const T xs[3], T g[3], T H[6]);
+    static __device__ __forceinline__ void grad(const PotDev<R>& P, const T x[3], const T xs[3], T g[3], T H[6],
+                                                const TimeDep<T>& td = TimeDep<T>());
 };
 
 struct MlpKernelArgs {
@@ -384,7 +385,7 @@ __device__ __forceinline__ const MlpKernelArgs*& mlp_args_ptr() {
 }
 
 template <class T, class R, bool HESS>
-__device__ __forceinline__ void MlpComp::grad(const PotDev<R>&, const T x[3], const T*, T g[3], T*) {
+__device__ __forceinline__ void MlpComp::grad(const PotDev<R>&, const T x[3], const T*, T g[3], T*, const TimeDep<T>&) {
     uint8_t* sm = mlp_smem();
     MlpCta cx;
     cx.wg = threadIdx.x >> 7;

@@ -82,7 +82,8 @@ __device__ __forceinline__ void base_stage(const PotDev<double>& P, const double
     if (P.has_track) track_eval(P.track, t, cc);
     double H[6];
     const double xs[3] = {x[0] - cc[0], x[1] - cc[1], x[2] - cc[2]};
-    pot_grad<double, double, true>(P, x, xs, g, H);
+    const TimeDep<double> td = time_dep(P, t);
+    pot_grad<double, double, true>(P, x, xs, g, H, td);
     r[0] = x[0];
     r[1] = x[1];
     r[2] = x[2];
@@ -97,7 +98,7 @@ __device__ __forceinline__ void base_stage(const PotDev<double>& P, const double
             xsd[c] = Dual<3>(xs[c]);
             xsd[c].d[c] = 1.0;
         }
-        pot_grad<Dual<3>, double, true>(P, xd, xsd, gd, Hd);
+        pot_grad<Dual<3>, double, true>(P, xd, xsd, gd, Hd, time_dep_as<Dual<3>>(td));
         // H order xx yy zz xy xz yz; D_abc = d H_ab / d x_c
         const double D[10] = {Hd[0].d[0], Hd[0].d[1], Hd[0].d[2], Hd[1].d[0], Hd[3].d[2],
                               Hd[2].d[0], Hd[1].d[1], Hd[1].d[2], Hd[2].d[1], Hd[2].d[2]};

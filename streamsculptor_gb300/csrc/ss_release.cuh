@@ -31,7 +31,7 @@ __device__ inline T release_tidal_radius(const PotDev<double>& P, const T x[3], 
     if (P.has_track) track_eval(P.track, t, c);
     T xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
     T g[3], H[6];
-    pot_grad<T, double, true>(P, x, xs, g, H);
+    pot_grad<T, double, true>(P, x, xs, g, H, time_dep_as<T>(time_dep(P, t)));
     // r_hat^T H r_hat
     T d2 = H[0] * rh[0] * rh[0] + H[1] * rh[1] * rh[1] + H[2] * rh[2] * rh[2] +
            2.0 * (H[3] * rh[0] * rh[1] + H[4] * rh[0] * rh[2] + H[5] * rh[1] * rh[2]);

@@ -446,7 +446,7 @@ int ss_orbit_shoot_f64(const ss_potential* pot, const double* w0, double t0, dou
     SS_CHECK_ARG(w0 && out, "NULL buffer");
     SS_CHECK_ARG(tol > 0.0 && tol < 1e-6, "tol must be in (0, 1e-6)");
     cudaStream_t st = (cudaStream_t)stream;
-    const bool is_static = !P.has_track && P.sh.n == 0;
+    const bool is_static = !P.has_track && P.sh.n == 0 && !P.has_rot && !P.has_facc;
     const int64_t S = (n_steps + SHOOT_M - 1) / SHOOT_M;
     bool handled = false;
     if (is_static && S >= 2) {
@@ -501,7 +501,7 @@ int ss_prog_tangents_f64(const ss_potential* pot, const double* raw_params, cons
     PotDev<double> P;
     int rc = prepare_potential<double>(pot, &P, false);
     if (rc) return rc;
-    SS_CHECK_ARG(!P.has_track, "progenitor tangents need a static potential");
+    SS_CHECK_ARG(!P.has_track && !P.has_rot && !P.has_facc, "progenitor tangents need a static potential");
     SS_CHECK_ARG(P.n >= 1 && P.n <= 4, "progenitor tangents support 1 to 4 components (one warp of directions)");
     SS_CHECK_ARG(std::isfinite(dt) && dt > 0.0 && n_steps >= 2 * SHOOT_M && save_every >= 1, "bad steps");
     SS_CHECK_ARG(raw_params && w0 && states && tangents, "NULL buffer");

@@ -52,6 +52,28 @@ __global__ void track_table_kernel(TrackDev tr, double t0, double dt, int32_t n_
     tab[2 * i + 1] = make_float4((float)(c[0] - (double)hx), (float)(c[1] - (double)hy), (float)(c[2] - (double)hz), 0.f);
 }
 
+// The rotation (cos, sin)(omega t) and the frame-acceleration gradient at
+// the same stage times as track_table_kernel, two float4 per slot.
+__global__ void time_table_kernel(PotDev<float> P, double t0, double dt, int32_t n_steps, float4* tab) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t total = 5 * (int64_t)n_steps + 1;
+    if (i >= total) return;
+    int64_t n = i / 5;
+    int s = (int)(i % 5);
+    const double cs[5] = {0.0, SS_C2, SS_C3, SS_C4, SS_C5};
+    const TimeDep<double> td = time_dep(P, t0 + ((double)n + cs[s]) * dt);
+    tab[2 * i] = make_float4((float)td.c, (float)td.s, (float)td.ga[0], (float)td.ga[1]);
+    tab[2 * i + 1] = make_float4((float)td.ga[2], 0.f, 0.f, 0.f);
+}
+
+static bool has_time_dep(const ss_potential* pot) {
+    for (int k = 0; k < pot->n_components && k < SS_MAX_COMPONENTS; ++k) {
+        const int kd = pot->comp[k].kind;
+        if (kd == SS_BAR || kd == SS_DEHNEN_BAR || kd == SS_UNIFORM_ACCEL) return true;
+    }
+    return false;
+}
+
 // Subhalo lines relative to the run start t0: position at t0, velocity,
 // (t0_s - t0, window).
 __global__ void subhalo_table_kernel(ShDev sh, double t0, float4* tab) {
@@ -146,6 +168,8 @@ static int64_t f32k_workspace(const ss_potential* pot, const ss_stream_cfg* cfg)
     for (int k = 0; k < pot->n_components && k < SS_MAX_COMPONENTS; ++k) track |= pot->comp[k].center == SS_CENTER_TRACK;
     if (track) bytes += (5 * cfg->n_steps + 1) * 2 * (int64_t)sizeof(float4);
     bytes = (bytes + 255) / 256 * 256;
+    if (has_time_dep(pot)) bytes += (5 * cfg->n_steps + 1) * 2 * (int64_t)sizeof(float4);
+    bytes = (bytes + 255) / 256 * 256;
     if (pot->subhalos.n > 0) bytes += 3 * pot->subhalos.n * (int64_t)sizeof(float4);
     bytes = (bytes + 255) / 256 * 256;
     if (has_expansion(pot)) bytes += expansion_table_bytes(pot->expansion);
@@ -207,6 +231,15 @@ int ss_stream_f32k(const ss_potential* pot, const ss_stream_cfg* cfg, const doub
                                                                             (int32_t)cfg->n_steps, tab);
         SS_LAUNCH_CHECK();
         a.ctab = tab;
+        ws += (total * 2 * (int64_t)sizeof(float4) + 255) / 256 * 256;
+    }
+    if (has_time_dep(pot)) {
+        float4* tab = (float4*)ws;
+        int64_t total = 5 * cfg->n_steps + 1;
+        time_table_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(P, cfg->t0, cfg->dt, (int32_t)cfg->n_steps,
+                                                                           tab);
+        SS_LAUNCH_CHECK();
+        a.ttab = tab;
         ws += (total * 2 * (int64_t)sizeof(float4) + 255) / 256 * 256;
     }
     if (pot->subhalos.n > 0) {

@@ -27,6 +27,7 @@ struct StreamArgs {
     float h_lo;
     const float4* ctab;   // [(n_steps*5+1) x 2] track positions (hi, lo) at stage times
     const float4* shtab;  // [n_sh*3] subhalo lines
+    const float4* ttab;   // [(n_steps*5+1) x 2] (cos, sin, ga.x, ga.y), (ga.z, -, -, -) at stage times
     int32_t n_sh;
     int32_t sh_kind;
     // optional checkpoints of the compensated state every ckpt_stride local
@@ -133,7 +134,17 @@ __device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamAr
         xs[2] = (xh[2] - ch.z) + (d[2] - cl.z);
     }
     float g[3];
-    C::template grad<float, float, false>(P, X, xs, g, nullptr);
+    TimeDep<float> td;  // read by rotating / frame-accelerated components only
+    if (a.ttab) {
+        const float4 t0 = __ldg(a.ttab + 2 * slot);
+        const float4 t1 = __ldg(a.ttab + 2 * slot + 1);
+        td.c = t0.x;
+        td.s = t0.y;
+        td.ga[0] = t0.z;
+        td.ga[1] = t0.w;
+        td.ga[2] = t1.x;
+    }
+    C::template grad<float, float, false>(P, X, xs, g, nullptr, td);
 #pragma unroll 1
     for (int j = shb; j < she; ++j) {
         float4 s0 = __ldg(a.shtab + 3 * j);

@@ -8,7 +8,9 @@ TriaxialNFWPotential (86-97), Isochrone (114-122), PlummerPotential
 GalaMilkyWayPotential (390-418), TimeDepTranslatingPotential (448-462),
 SubhaloLinePotential (802-850), SubhaloLinePotential_dRadius (852-904),
 SubhaloLinePotential_Custom (908-956) with a Plummer or Hernquist profile,
-Potential_Combine (1279-1296).  CustomPotential (787-797) holds an arbitrary
+Potential_Combine (1279-1296), and the time-dependent BarPotential (178-198),
+DehnenBarPotential (200-222), UniformAcceleration (480-502) and
+MW_LMC_Potential (555-662, its tracks passed in).  CustomPotential (787-797) holds an arbitrary
 Python callable and cannot run in a CUDA kernel: using it raises.
 """
 from __future__ import annotations
@@ -208,6 +210,86 @@ class GalaMilkyWayPotential(Potential):
         return self.pot._flatten()
 
 
+class BarPotential(Potential):
+    """Long & Murali (1992) bar rotating about z at pattern speed Omega
+    (potential.py:178-198): the simulation-frame point is rotated by
+    -Omega t into the bar frame.  The rotating components of one potential
+    share one pattern speed."""
+
+    def __init__(self, m, a, b, c, Omega, units=None):
+        super().__init__(units, {"m": m, "a": a, "b": b, "c": c, "Omega": Omega})
+
+    def _flatten(self):
+        return Flat([(_abi.SS_BAR, _abi.SS_CENTER_ORIGIN,
+                      (_f(self.m), _f(self.a), _f(self.b), _f(self.c), _f(self.Omega)))])
+
+
+class DehnenBarPotential(Potential):
+    """Dehnen (2000) bar: alpha v0^2/3 (R0/Rb)^3 (R/r)^2 U(r) cos 2(phi - phib -
+    Omega t) with U = -(r/Rb)^-3 outside Rb and (r/Rb)^3 - 2 inside
+    (potential.py:200-222)."""
+
+    def __init__(self, alpha, v0, R0, Rb, phib, Omega, units=None):
+        super().__init__(units, {"alpha": alpha, "v0": v0, "R0": R0, "Rb": Rb, "phib": phib, "Omega": Omega})
+
+    def _flatten(self):
+        return Flat([(_abi.SS_DEHNEN_BAR, _abi.SS_CENTER_ORIGIN,
+                      (_f(self.alpha), _f(self.v0), _f(self.R0), _f(self.Rb), _f(self.phib), _f(self.Omega)))])
+
+
+class UniformAcceleration(Potential):
+    """Spatially uniform acceleration -dv/dt of the frame velocity
+    (potential.py:480-502).  velocity_func must be a CenterTrack of the
+    frame's velocity (uniform knots; CenterTrack.linear_from_samples for the
+    reference's linear interpolant).  It has a force but no potential."""
+
+    def __init__(self, velocity_func=None, units=None):
+        super().__init__(units, {"velocity_func": velocity_func})
+
+    def _flatten(self):
+        if not isinstance(self.velocity_func, CenterTrack):
+            raise NotImplementedError("velocity_func must be a CenterTrack (arbitrary callables cannot run on the GPU)")
+        return Flat([(_abi.SS_UNIFORM_ACCEL, _abi.SS_CENTER_ORIGIN, ())], frame_velocity=self.velocity_func)
+
+    def potential(self, xyz, t):
+        raise NotImplementedError("UniformAcceleration has a force but no potential")
+
+
+class MW_LMC_Potential(Potential):
+    """Milky Way + LMC as rigid bodies in the Milky Way's non-inertial frame
+    (potential.py:555-662): Hernquist bulge (5e9, 1.0), Miyamoto-Nagai disk
+    (5e10, 3.0, 0.3), NFW halo (5.4e11, 15.62); the LMC an NFW of
+    0.85e11 Msun and r_s = (m/1e11)^0.6 8.5 kpc moving on its track; the
+    reflex acceleration -dv_MW/dt as a uniform field.  Both tracks are
+    linear interpolants, as the reference's RegularGridInterpolator.
+
+    The reference loads its tracks from data files shipped with its package;
+    here they are arguments: lmc_track = (t [n], xyz [n, 3]) and
+    mw_velocity = (t [n], v [n, 3]), uniformly spaced increasing times."""
+
+    def __init__(self, units=None, lmc_track=None, mw_velocity=None):
+        super().__init__(units, {"params": None})
+        if lmc_track is None or mw_velocity is None:
+            raise ValueError("MW_LMC_Potential needs lmc_track=(t, xyz) and mw_velocity=(t, v)")
+        self.LMC_track = CenterTrack.linear_from_samples(*lmc_track)
+        self.MW_velocity = CenterTrack.linear_from_samples(*mw_velocity)
+        u = self.units
+        self.pot_MW = Potential_Combine([HernquistPotential(m=5e9, r_s=1.0, units=u),
+                                         MiyamotoNagaiDisk(m=5.0e10, a=3.0, b=0.3, units=u),
+                                         NFWPotential(m=5.4e11, r_s=15.62, units=u)], units=u)
+        massLMC = 0.85e11
+        self.pot_LMC = NFWPotential(m=massLMC, r_s=(massLMC / 1e11) ** 0.6 * 8.5, units=u)
+        self.translating_LMC_pot = TimeDepTranslatingPotential(pot=self.pot_LMC, center_spl=self.LMC_track, units=u)
+        self.unif_acc = UniformAcceleration(velocity_func=self.MW_velocity, units=u)
+        self.total_pot = Potential_Combine([self.pot_MW, self.translating_LMC_pot, self.unif_acc], units=u)
+
+    def _flatten(self):
+        return self.total_pot._flatten()
+
+    def potential(self, xyz, t):
+        raise NotImplementedError("Potential not implemented, force is non-conservative")
+
+
 class _SubhaloLines(Potential):
     _kind = _abi.SS_SH_PLUMMER
 
@@ -319,5 +401,6 @@ class CustomPotential(Potential):
 
 __all__ = ["MiyamotoNagaiDisk", "NFWPotential", "TriaxialNFWPotential", "Isochrone", "PlummerPotential",
            "HernquistPotential", "Potential_Combine", "TimeDepTranslatingPotential", "ProgenitorPotential",
-           "GalaMilkyWayPotential", "SubhaloLinePotential", "SubhaloLinePotential_dRadius",
+           "GalaMilkyWayPotential", "SubhaloLinePotential", "SubhaloLinePotential_dRadius", "BarPotential",
+           "DehnenBarPotential", "UniformAcceleration", "MW_LMC_Potential",
            "SubhaloLinePotential_Custom", "CustomPotential", "CenterTrack", "usys"]

@@ -224,3 +224,39 @@ def test_stream_ensemble_mode_equals_separate_streams(oracle):
         row = {k: (v[b:b + 1] if isinstance(v, np.ndarray) else v) for k, v in sh.items()}
         one, _, _ = oracle.stream(oracle.HostModel(oracle.mw3(), subhalos=row), 0.0, 1.0, n_rel, ics[b], ppr, 1)
         assert np.array_equal(full.reshape(B, -1, 6)[b], one)
+
+
+def test_rotating_bars_and_frame_acceleration(oracle):
+    """The oracle's time-dependent components: a bar at time t is the bar at
+    t = 0 seen at the point rotated by -Omega t (potential.py:185-198,
+    205-222); autodiff gradients against central differences; the uniform
+    acceleration's gradient is the frame velocity's derivative (the slope of
+    the linear track, potential.py:497-499)."""
+    rng = np.random.default_rng(3)
+    kinds = [(_abi.SS_BAR, 0, (2e10, 4.0, 1.0, 0.5, 0.045)),
+             (_abi.SS_DEHNEN_BAR, 0, (0.01, 0.22, 8.0, 3.5, 0.4, 0.045))]
+    for comp in kinds:
+        m = oracle.HostModel([comp])
+        x = rng.normal(0, 5, (20, 3))
+        x[:5] *= 0.3  # points inside the Dehnen bar's Rb too
+        t = 37.0
+        om = comp[2][4] if comp[0] == _abi.SS_BAR else comp[2][5]
+        a = -om * t
+        xr = np.stack([np.cos(a) * x[:, 0] - np.sin(a) * x[:, 1], np.sin(a) * x[:, 0] + np.cos(a) * x[:, 1], x[:, 2]], 1)
+        phi_t, g, _ = oracle.potential_eval(m, x, t)
+        phi_0, _, _ = oracle.potential_eval(m, xr, 0.0)
+        assert np.allclose(phi_t, phi_0, rtol=1e-12, atol=1e-16)
+        h = 1e-5
+        for k in range(3):
+            e = np.zeros(3)
+            e[k] = h
+            fd = (oracle.potential_eval(m, x + e, t)[0] - oracle.potential_eval(m, x - e, t)[0]) / (2 * h)
+            assert np.max(np.abs(fd - g[:, k])) <= 1e-6 * np.max(np.abs(g))
+    tv = np.arange(40) * 25.0 - 800.0
+    vel = np.stack([0.01 * np.sin(tv / 300), 0.02 * np.cos(tv / 200), -0.005 * tv / 800], 1)
+    m = oracle.HostModel([(_abi.SS_UNIFORM_ACCEL, 0, ())], frame_velocity=(tv[0], 25.0, vel, "linear"))
+    for t in (-790.0, -312.5, -13.0):
+        k = int((t - tv[0]) // 25.0)
+        _, g, H = oracle.potential_eval(m, rng.normal(0, 5, (4, 3)), t)
+        assert np.allclose(g, (vel[k + 1] - vel[k]) / 25.0, rtol=1e-13, atol=1e-18)
+        assert np.all(H == 0)
