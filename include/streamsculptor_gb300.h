@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define SS_ABI_VERSION 4
+#define SS_ABI_VERSION 5
 #define SS_MAX_COMPONENTS 16
 
 /* ---------------------------------------------------------------- status */
@@ -103,7 +103,7 @@ typedef struct ss_track {
 /* Subhalos moving on straight lines x0 + v (t - t0), active while
  * |t - t0| < t_window: SubhaloLinePotential, potential.py:802-850, and its
  * d/d(r_s) companion SubhaloLinePotential_dRadius, potential.py:852-904. */
-typedef enum ss_subhalo_kind { SS_SH_PLUMMER = 1, SS_SH_HERNQUIST = 2 } ss_subhalo_kind;
+typedef enum ss_subhalo_kind { SS_SH_PLUMMER = 1, SS_SH_HERNQUIST = 2, SS_SH_GRID = 3 } ss_subhalo_kind;
 
 typedef struct ss_subhalos {
     int32_t kind;       /* ss_subhalo_kind */
@@ -115,6 +115,16 @@ typedef struct ss_subhalos {
     const double* v;    /* [n, 3] */
     const double* t0;   /* [n] */
     double t_window;    /* +inf = always active */
+    /* SS_SH_GRID (TNFWSubhaloLinePotential, potential.py:1022-1108): each
+     * subhalo's spherical potential as a cubic Hermite spline in u = ln r
+     * through n_grid knots at grid_u0[s] + k grid_du[s], given by value and
+     * d/du: grid[s][k][2]; outside the knots it continues linearly in u (the
+     * reference's interpolant returns NaN there).  m and a are unused, and
+     * the response to the scale radius (ncol >= 12) is not defined. */
+    const double* grid;
+    const double* grid_u0;
+    const double* grid_du;
+    int64_t n_grid;
 } ss_subhalos;
 
 /* Real spherical-harmonic expansion with spline radial functions:

@@ -128,6 +128,10 @@ class HostModel:
         S.n = arrs["m"].shape[0]
         S.m, S.a, S.x0, S.v, S.t0 = (arrs[k].ctypes.data for k in ("m", "a", "x0", "v", "t0"))
         S.t_window = float(s.get("t_window", np.inf))
+        if "grid" in s:  # SS_SH_GRID: [n, n_grid, 2] tables, u0 [n], du [n]
+            g, u0, du = f8(s["grid"]), f8(s["grid_u0"]), f8(s["grid_du"])
+            self._keep += [g, u0, du]
+            S.grid, S.grid_u0, S.grid_du, S.n_grid = g.ctypes.data, u0.ctypes.data, du.ctypes.data, g.shape[1]
         return S
 
 

@@ -309,13 +309,36 @@ S phi_component_t(const ss_component& c, double G, const S x[3], double t, const
 // SubhaloLinePotential_Custom with a HernquistPotential.  Zero outside the
 // window |t - t0| < t_window.  `S2` lets the caller differentiate in the
 // scale radius a as well (SubhaloLinePotential_dRadius, potential.py:861-866).
+// A tabulated subhalo (SS_SH_GRID): the cubic Hermite spline of row j in
+// u = ln r through its knots (value, d/du), continued linearly outside —
+// interpax.Interpolator1D(method='cubic') over the log-radius grid of
+// TNFWSubhaloLinePotential.single_subhalo_potential (potential.py:1068-1072),
+// whose knot derivatives the caller supplies.
+template <class S>
+S phi_grid_row(const ss_subhalos& sh, int64_t j, const S& r2) {
+    const double* tab = sh.grid + (size_t)j * sh.n_grid * 2;
+    const double u0 = sh.grid_u0[j], du = sh.grid_du[j];
+    const int64_t n = sh.n_grid;
+    S u = 0.5 * log_(r2);
+    double uu = (value(u) - u0) / du;
+    if (uu < 0.0) return tab[0] + tab[1] * (u - u0);
+    if (uu > (double)(n - 1)) return tab[2 * (n - 1)] + tab[2 * (n - 1) + 1] * (u - (u0 + du * (n - 1)));
+    int64_t k = (int64_t)std::floor(uu);
+    if (k > n - 2) k = n - 2;
+    S x = (u - (u0 + du * k)) / du;
+    S x2 = x * x, x3 = x2 * x;
+    return (2.0 * x3 - 3.0 * x2 + 1.0) * tab[2 * k] + (x3 - 2.0 * x2 + x) * (du * tab[2 * k + 1]) +
+           (3.0 * x2 - 2.0 * x3) * tab[2 * k + 2] + (x3 - x2) * (du * tab[2 * k + 3]);
+}
+
 template <class S>
 S phi_subhalo(int kind, double G, double m, const S& a, const double x0[3], const double v[3],
-              double t0, double t_window, const S x[3], double t) {
+              double t0, double t_window, const S x[3], double t, const ss_subhalos* tab = nullptr, int64_t j = 0) {
     if (!(std::fabs(t - t0) < t_window)) return S(0.0);
     S rel[3];
     for (int i = 0; i < 3; ++i) rel[i] = x[i] - (x0[i] + v[i] * (t - t0));
     S r2 = rel[0] * rel[0] + rel[1] * rel[1] + rel[2] * rel[2];
+    if (kind == SS_SH_GRID) return phi_grid_row(*tab, j, r2);
     if (kind == SS_SH_PLUMMER) return -G * m / sqrt_(r2 + a * a);
     return -G * m / (sqrt_(r2) + a);
 }
@@ -409,7 +432,7 @@ S phi_total(const ss_potential& P, const S x[3], double t) {
         S s(0.0);
         for (int64_t j = 0; j < sh.n; ++j)
             s = s + phi_subhalo<S>(sh.kind, P.G, sh.m[j], S(sh.a[j]), sh.x0 + 3 * j, sh.v + 3 * j,
-                                   sh.t0[j], sh.t_window, x, t);
+                                   sh.t0[j], sh.t_window, x, t, &sh, j);
         acc = acc + s;
     }
     return acc;
@@ -661,7 +684,7 @@ struct PertRHS {
             for (int i = 0; i < 3; ++i) xd[i] = Dx::var(Da(x0[i]), i);
             Da a = Da::var(sh->a[s], 0);
             Dx f = phi_subhalo<Dx>(sh->kind, P->G, sh->m[s], Dx::cst(a), sh->x0 + 3 * s,
-                                   sh->v + 3 * s, sh->t0[s], sh->t_window, xd, t);
+                                   sh->v + 3 * s, sh->t0[s], sh->t_window, xd, t, sh, s);
             double a1[3], a1r[3];
             for (int i = 0; i < 3; ++i) {
                 a1[i] = -f.d[i].v;
@@ -690,7 +713,7 @@ struct PertRHS {
                 O3 xs2[3];
                 for (int i = 0; i < 3; ++i) xs2[i] = O3::var(I3::var(x0[i], i), i);
                 O3 fs = phi_subhalo<O3>(sh->kind, P->G, sh->m[s], O3(sh->a[s]), sh->x0 + 3 * s, sh->v + 3 * s,
-                                        sh->t0[s], sh->t_window, xs2, t);
+                                        sh->t0[s], sh->t_window, xs2, t, sh, s);
                 // d2a = T x2 + einsum('ikj,nk->nij') contracted with x1 + dapert_dx x1
                 for (int i = 0; i < 3; ++i) {
                     du[12 + i] = u[15 + i];
@@ -887,7 +910,7 @@ void or_subhalo_eval(const ss_subhalos* sh, double G, const double* xyz, int64_t
         for (int64_t s = 0; s < sh->n; ++s) {
             Da a = Da::var(sh->a[s], 0);
             Dx f = phi_subhalo<Dx>(sh->kind, G, sh->m[s], Dx::cst(a), sh->x0 + 3 * s, sh->v + 3 * s,
-                                   sh->t0[s], sh->t_window, xd, t);
+                                   sh->t0[s], sh->t_window, xd, t, sh, s);
             size_t o = (size_t)i * sh->n + s;
             if (phi) phi[o] = f.v.v;
             if (dphi_da) dphi_da[o] = f.v.d[0];

@@ -10,7 +10,7 @@ import ctypes as C
 import os
 import threading
 
-SS_ABI_VERSION = 4
+SS_ABI_VERSION = 5
 SS_MAX_COMPONENTS = 16
 
 SS_OK = 0
@@ -37,6 +37,7 @@ SS_CENTER_TRACK = 1
 
 SS_SH_PLUMMER = 1
 SS_SH_HERNQUIST = 2
+SS_SH_GRID = 3
 
 SS_RELEASE_FARDAL = 0
 SS_RELEASE_CHEN25 = 1
@@ -56,7 +57,8 @@ class ss_track(C.Structure):
 
 class ss_subhalos(C.Structure):
     _fields_ = [("kind", C.c_int32), ("reserved", C.c_int32), ("n", C.c_int64),
-                ("m", VP), ("a", VP), ("x0", VP), ("v", VP), ("t0", VP), ("t_window", C.c_double)]
+                ("m", VP), ("a", VP), ("x0", VP), ("v", VP), ("t0", VP), ("t_window", C.c_double),
+                ("grid", VP), ("grid_u0", VP), ("grid_du", VP), ("n_grid", C.c_int64)]
 
 
 class ss_expansion(C.Structure):

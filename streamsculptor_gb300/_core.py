@@ -146,6 +146,10 @@ class SubhaloTable:
     v: torch.Tensor
     t0: torch.Tensor
     t_window: float
+    # SS_SH_GRID: [n, n_grid, 2] (value, d/du) spline tables in u = ln r
+    grid: Optional[torch.Tensor] = None
+    grid_u0: Optional[torch.Tensor] = None
+    grid_du: Optional[torch.Tensor] = None
 
     def struct(self) -> _abi.ss_subhalos:
         s = _abi.ss_subhalos()
@@ -154,11 +158,16 @@ class SubhaloTable:
         s.m, s.a, s.x0, s.v, s.t0 = (self.m.data_ptr(), self.a.data_ptr(), self.x0.data_ptr(),
                                      self.v.data_ptr(), self.t0.data_ptr())
         s.t_window = float(self.t_window)
+        if self.grid is not None:
+            s.grid, s.grid_u0, s.grid_du = self.grid.data_ptr(), self.grid_u0.data_ptr(), self.grid_du.data_ptr()
+            s.n_grid = int(self.grid.shape[1])
         return s
 
     def same_lines(self, other: "SubhaloTable") -> bool:
         return (self.kind == other.kind and self.t_window == other.t_window and
-                all(torch.equal(getattr(self, k), getattr(other, k)) for k in ("m", "a", "x0", "v", "t0")))
+                all(torch.equal(getattr(self, k), getattr(other, k)) for k in ("m", "a", "x0", "v", "t0")) and
+                (self.grid is None) == (other.grid is None) and
+                (self.grid is None or torch.equal(self.grid, other.grid)))
 
 
 @dataclass

@@ -151,9 +151,17 @@ int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalo
     SS_CHECK_ARG(sh.n >= 0 && sh.n <= (int64_t)1 << 30, "subhalos: bad n");
     if (sh.n > 0) {
         SS_CHECK_ARG(allow_subhalos, "this entry point takes the subhalos separately; potential.subhalos must be empty");
-        SS_CHECK_ARG(sh.kind == SS_SH_PLUMMER || sh.kind == SS_SH_HERNQUIST, "subhalos: unknown kind %d", sh.kind);
+        SS_CHECK_ARG(sh.kind == SS_SH_PLUMMER || sh.kind == SS_SH_HERNQUIST || sh.kind == SS_SH_GRID,
+                     "subhalos: unknown kind %d", sh.kind);
         SS_CHECK_ARG(sh.m && sh.a && sh.x0 && sh.v && sh.t0, "subhalos: NULL table pointer");
         SS_CHECK_ARG(!(sh.t_window < 0.0), "subhalos: t_window < 0");
+        SS_CHECK_ARG(sh.kind != SS_SH_GRID ||
+                         (sh.grid && sh.grid_u0 && sh.grid_du && sh.n_grid >= 2 && sh.n_grid <= (1 << 20)),
+                     "subhalos: SS_SH_GRID needs grid tables with >= 2 knots");
+        out->sh.grid = sh.grid;
+        out->sh.gu0 = sh.grid_u0;
+        out->sh.gdu = sh.grid_du;
+        out->sh.ng = (int32_t)sh.n_grid;
         out->sh.kind = sh.kind;
         out->sh.n = (int32_t)sh.n;
         out->sh.m = sh.m;
@@ -246,7 +254,13 @@ __global__ void potential_eval_kernel(PotDev<double> P, const double* __restrict
             for (int k = 0; k < 3; ++k) rel[k] = x[k] - (P.sh.x0[3 * j + k] + P.sh.v[3 * j + k] * tau);
             double r2 = rel[0] * rel[0] + rel[1] * rel[1] + rel[2] * rel[2];
             double Gm = P.sh.G * P.sh.m[j], a = P.sh.a[j];
-            f += P.sh.kind == SS_SH_PLUMMER ? -Gm / sqrt(r2 + a * a) : -Gm / (sqrt(r2) + a);
+            if (P.sh.kind == SS_SH_GRID) {
+                double g, gr, ph;
+                grid_subhalo_gh<double, false>(P.sh, j, r2, g, gr, &ph);
+                f += ph;
+            } else {
+                f += P.sh.kind == SS_SH_PLUMMER ? -Gm / sqrt(r2 + a * a) : -Gm / (sqrt(r2) + a);
+            }
         }
         phi[i] = f;
     }

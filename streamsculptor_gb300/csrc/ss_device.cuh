@@ -186,6 +186,11 @@ struct ShDev {
     const double* t0;
     double t_window;
     double G;
+    // SS_SH_GRID: [n][ng][2] (value, d/du) spline tables in u = ln r
+    const double* grid;
+    const double* gu0;
+    const double* gdu;
+    int32_t ng;
 };
 
 template <class R>
@@ -1429,6 +1434,45 @@ inline auto dispatch_comp(const PotDev<R>& P, F&& f) {
     return f(GenericComp{});
 }
 
+// A tabulated spherical subhalo (SS_SH_GRID) at squared distance r2: the
+// cubic Hermite spline Phi(u), u = ln r, of its row s (linear in u outside
+// the knots).  grad Phi = g rel and, with HESS, H = g I + gr rel rel^T:
+// g = Phi_u / r^2, gr = (Phi_uu - 2 Phi_u) / r^4.  phi (optional) = Phi.
+template <class T, bool HESS>
+__device__ __forceinline__ void grid_subhalo_gh(const ShDev& sh, int s, T r2, T& g, T& gr, T* phi = nullptr) {
+    const double* tab = sh.grid + (size_t)s * sh.ng * 2;
+    const double u0 = __ldg(sh.gu0 + s), du = __ldg(sh.gdu + s);
+    const T ir2 = s_rcp(r2);
+    const T u = T(0.5) * s_log(r2);
+    const double uu = (sval(u) - u0) / du;
+    T fu, fuu;
+    if (uu < 0.0 || uu > (double)(sh.ng - 1)) {
+        const int k = uu < 0.0 ? 0 : sh.ng - 1;
+        fu = T(__ldg(tab + 2 * k + 1));
+        fuu = T(0);
+        if (phi) *phi = T(__ldg(tab + 2 * k)) + fu * (u - T(u0 + du * k));
+    } else {
+        int k = (int)floor(uu);
+        if (k > sh.ng - 2) k = sh.ng - 2;
+        const T x = (u - T(u0 + du * k)) * T(1.0 / du);
+        const T f0 = T(__ldg(tab + 2 * k)), d0 = T(du * __ldg(tab + 2 * k + 1));
+        const T f1 = T(__ldg(tab + 2 * k + 2)), d1 = T(du * __ldg(tab + 2 * k + 3));
+        const T x2 = x * x;
+        // d/dx of the Hermite basis h00, h10, h01, h11, then d2/dx2
+        const T a00 = T(6) * x2 - T(6) * x, a10 = T(3) * x2 - T(4) * x + T(1);
+        const T a11 = T(3) * x2 - T(2) * x;
+        fu = (a00 * (f0 - f1) + a10 * d0 + a11 * d1) * T(1.0 / du);
+        fuu = ((T(12) * x - T(6)) * (f0 - f1) + (T(6) * x - T(4)) * d0 + (T(6) * x - T(2)) * d1) * T(1.0 / (du * du));
+        if (phi) {
+            const T x3 = x2 * x;
+            *phi = (T(2) * x3 - T(3) * x2 + T(1)) * f0 + (x3 - T(2) * x2 + x) * d0 + (T(3) * x2 - T(2) * x3) * f1 +
+                   (x3 - x2) * d1;
+        }
+    }
+    g = fu * ir2;
+    if (HESS) gr = (fuu - T(2) * fu) * ir2 * ir2;
+}
+
 // Subhalo sum in the potential (nonlinear perturbed streams), FP64 table.
 template <class T>
 __device__ __forceinline__ void subhalo_sum_grad(const ShDev& sh, const T x[3], double t, T grad[3]) {
@@ -1441,7 +1485,15 @@ __device__ __forceinline__ void subhalo_sum_grad(const ShDev& sh, const T x[3], 
 #pragma unroll
         for (int i = 0; i < 3; ++i) rel[i] = x[i] - T(__ldg(sh.x0 + 3 * j + i) + __ldg(sh.v + 3 * j + i) * tau);
         T gphi[3], dummy[3];
-        subhalo_grad<T, false>(sh.kind, T(sh.G * __ldg(sh.m + j)), T(__ldg(sh.a + j)), rel, gphi, dummy);
+        if (sh.kind == SS_SH_GRID) {
+            T g, gr;
+            grid_subhalo_gh<T, false>(sh, j, rel[0] * rel[0] + rel[1] * rel[1] + rel[2] * rel[2], g, gr);
+            gphi[0] = g * rel[0];
+            gphi[1] = g * rel[1];
+            gphi[2] = g * rel[2];
+        } else {
+            subhalo_grad<T, false>(sh.kind, T(sh.G * __ldg(sh.m + j)), T(__ldg(sh.a + j)), rel, gphi, dummy);
+        }
         grad[0] += gphi[0];
         grad[1] += gphi[1];
         grad[2] += gphi[2];

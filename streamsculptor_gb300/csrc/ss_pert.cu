@@ -204,14 +204,24 @@ __device__ __forceinline__ void subhalo_hess(int kind, R Gm, R a, const R rel[3]
 
 template <class R, int NCOL>
 __device__ __forceinline__ void pert_rhs(const R* recp, const R U[NCOL], int kind, R Gm, R a, const R P0[3],
-                                         const R V[3], R trel, R tau0, R window, R K[NCOL]) {
+                                         const R V[3], R trel, R tau0, R window, R K[NCOL], const ShDev& sh, int sidx) {
     R rec[9];
     load_stage(recp, rec);
     R rel[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) rel[i] = rec[i] - (P0[i] + V[i] * trel);
     R gphi[3], gdphi[3];
-    subhalo_grad<R, NCOL >= 12>(kind, Gm, a, rel, gphi, gdphi);
+    R gg = R(0), ggr = R(0);  // SS_SH_GRID: grad = gg rel, Hessian = gg I + ggr rel rel^T
+    if (kind == SS_SH_GRID) {
+        grid_subhalo_gh<R, NCOL == 18>(sh, sidx, rel[0] * rel[0] + rel[1] * rel[1] + rel[2] * rel[2], gg, ggr);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            gphi[i] = gg * rel[i];
+            gdphi[i] = R(0);
+        }
+    } else {
+        subhalo_grad<R, NCOL >= 12>(kind, Gm, a, rel, gphi, gdphi);
+    }
     // window: |t - t0_s| < t_window
     R on = fabs(trel - tau0) < window ? R(1) : R(0);
     const R* T = rec + 3;
@@ -222,7 +232,16 @@ __device__ __forceinline__ void pert_rhs(const R* recp, const R U[NCOL], int kin
         const R* x1 = U;
         const R* x2 = U + 12;
         R Hs[6];
-        subhalo_hess<R>(kind, Gm, a, rel, Hs);
+        if (kind == SS_SH_GRID) {
+            Hs[0] = gg + ggr * rel[0] * rel[0];
+            Hs[1] = gg + ggr * rel[1] * rel[1];
+            Hs[2] = gg + ggr * rel[2] * rel[2];
+            Hs[3] = ggr * rel[0] * rel[1];
+            Hs[4] = ggr * rel[0] * rel[2];
+            Hs[5] = ggr * rel[1] * rel[2];
+        } else {
+            subhalo_hess<R>(kind, Gm, a, rel, Hs);
+        }
         const R x0s = x1[0] * x1[0], x1s = x1[1] * x1[1], x2s = x1[2] * x1[2];
         const R x01 = x1[0] * x1[1], x02 = x1[0] * x1[2], x12 = x1[1] * x1[2];
         // Q_i = sum_jk d2a_ijk x1_j x1_k with d2a symmetric
@@ -326,7 +345,7 @@ __global__ void __launch_bounds__(128) pert_response_kernel(ShDev sh, PertArgs a
                           R(SS_A65) * k[4][c];
                 U[c] = st == 0 ? u[c] : u[c] + h * acc;
             }
-            pert_rhs<R, NCOL>(&srec[j][st][0], U, sh.kind, Gm, am, P0, V, tn + cs[st] * h, tau0, window, k[st]);
+            pert_rhs<R, NCOL>(&srec[j][st][0], U, sh.kind, Gm, am, P0, V, tn + cs[st] * h, tau0, window, k[st], sh, s);
         }
 #pragma unroll
         for (int c = 0; c < NCOL; ++c)
@@ -353,11 +372,24 @@ __global__ void subhalo_eval_kernel(ShDev sh, const double* __restrict__ xyz, in
     double Gm = sh.G * sh.m[s], a = sh.a[s];
     double r2 = rel[0] * rel[0] + rel[1] * rel[1] + rel[2] * rel[2];
     double gphi[3], gd[3];
-    subhalo_grad<double, true>(sh.kind, Gm, a, rel, gphi, gd);
-    if (phi) phi[idx] = on ? (sh.kind == SS_SH_PLUMMER ? -Gm / sqrt(r2 + a * a) : -Gm / (sqrt(r2) + a)) : 0.0;
+    double phv;
+    if (sh.kind == SS_SH_GRID) {
+        // tabulated profile: no scale radius, so d/da is zero
+        double g, gr;
+        grid_subhalo_gh<double, false>(sh, s, r2, g, gr, &phv);
+        for (int k = 0; k < 3; ++k) {
+            gphi[k] = g * rel[k];
+            gd[k] = 0.0;
+        }
+    } else {
+        subhalo_grad<double, true>(sh.kind, Gm, a, rel, gphi, gd);
+        phv = sh.kind == SS_SH_PLUMMER ? -Gm / sqrt(r2 + a * a) : -Gm / (sqrt(r2) + a);
+    }
+    if (phi) phi[idx] = on ? phv : 0.0;
     if (dphi_da) {
-        double v = sh.kind == SS_SH_PLUMMER ? Gm * a / ((r2 + a * a) * sqrt(r2 + a * a))
-                                            : Gm / ((sqrt(r2) + a) * (sqrt(r2) + a));
+        double v = sh.kind == SS_SH_GRID      ? 0.0
+                   : sh.kind == SS_SH_PLUMMER ? Gm * a / ((r2 + a * a) * sqrt(r2 + a * a))
+                                              : Gm / ((sqrt(r2) + a) * (sqrt(r2) + a));
         dphi_da[idx] = on ? v : 0.0;
     }
     for (int k = 0; k < 3; ++k) {
@@ -396,17 +428,28 @@ __global__ void __launch_bounds__(128) pert_term_kernel(PotDev<double> P, ShDev 
     double U[NCOL], K[NCOL];
 #pragma unroll
     for (int c = 0; c < NCOL; ++c) U[c] = y[6 + s * NCOL + c];
-    pert_rhs<double, NCOL>(r, U, sh.kind, sh.G * sh.m[s], sh.a[s], P0, V, 0.0, sh.t0[s] - t, sh.t_window, K);
+    pert_rhs<double, NCOL>(r, U, sh.kind, sh.G * sh.m[s], sh.a[s], P0, V, 0.0, sh.t0[s] - t, sh.t_window, K, sh,
+                           (int)s);
 #pragma unroll
     for (int c = 0; c < NCOL; ++c) dy[6 + s * NCOL + c] = K[c];
 }
 
-static int prepare_subhalos(const ss_subhalos* in, double G, ShDev* out) {
+static int prepare_subhalos(const ss_subhalos* in, double G, ShDev* out, int ncol = 6) {
     SS_CHECK_ARG(in != nullptr, "subhalos is NULL");
     SS_CHECK_ARG(in->n >= 1 && in->n <= (1 << 30), "subhalos: n must be in [1, 2^30]");
-    SS_CHECK_ARG(in->kind == SS_SH_PLUMMER || in->kind == SS_SH_HERNQUIST, "subhalos: unknown kind %d", in->kind);
+    SS_CHECK_ARG(in->kind == SS_SH_PLUMMER || in->kind == SS_SH_HERNQUIST || in->kind == SS_SH_GRID,
+                 "subhalos: unknown kind %d", in->kind);
     SS_CHECK_ARG(in->m && in->a && in->x0 && in->v && in->t0, "subhalos: NULL table pointer");
     SS_CHECK_ARG(!(in->t_window < 0.0), "subhalos: t_window < 0");
+    if (in->kind == SS_SH_GRID) {
+        SS_CHECK_ARG(in->grid && in->grid_u0 && in->grid_du && in->n_grid >= 2 && in->n_grid <= (1 << 20),
+                     "subhalos: SS_SH_GRID needs grid tables with >= 2 knots");
+        SS_CHECK_ARG(ncol == 6, "tabulated subhalos have no scale-radius response: ncol must be 6");
+    }
+    out->grid = in->grid;
+    out->gu0 = in->grid_u0;
+    out->gdu = in->grid_du;
+    out->ng = (int32_t)in->n_grid;
     out->kind = in->kind;
     out->n = (int32_t)in->n;
     out->m = in->m;
@@ -519,7 +562,7 @@ int ss_pert_response(const ss_potential* base, const ss_subhalos* sh, const ss_p
     int rc = prepare_potential<double>(base, &P, false);
     if (rc) return rc;
     ShDev S;
-    rc = prepare_subhalos(sh, base->G, &S);
+    rc = prepare_subhalos(sh, base->G, &S, cfg ? cfg->ncol : 6);
     if (rc) return rc;
     SS_CHECK_ARG(cfg != nullptr, "cfg is NULL");
     SS_CHECK_ARG(precision == 32 || precision == 64, "precision must be 32 or 64");
@@ -621,7 +664,7 @@ int ss_pert_response_track(const ss_subhalos* sh, double G, const ss_pert_cfg* c
                            const void* track, const void* pert_ics, void* pert_out, void* stream) {
     ShDev S;
     SS_CHECK_ARG(std::isfinite(G) && G > 0.0, "G must be finite and > 0");
-    int rc = prepare_subhalos(sh, G, &S);
+    int rc = prepare_subhalos(sh, G, &S, cfg ? cfg->ncol : 6);
     if (rc) return rc;
     PertArgs a;
     rc = pert_args(cfg, precision, &a);
@@ -641,7 +684,7 @@ int ss_pert_term(const ss_potential* base, const ss_subhalos* sh, int ncol, doub
     int rc = prepare_potential<double>(base, &P, false);
     if (rc) return rc;
     ShDev S;
-    rc = prepare_subhalos(sh, base->G, &S);
+    rc = prepare_subhalos(sh, base->G, &S, ncol);
     if (rc) return rc;
     SS_CHECK_ARG(ncol == 6 || ncol == 12 || ncol == 18, "ncol must be 6, 12 or 18");
     SS_CHECK_ARG(std::isfinite(t), "t must be finite");

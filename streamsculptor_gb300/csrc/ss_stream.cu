@@ -252,6 +252,7 @@ int ss_stream_f32k(const ss_potential* pot, const ss_stream_cfg* cfg, const doub
         a.shtab = tab;
         a.n_sh = Pd.sh.n;
         a.sh_kind = Pd.sh.kind;
+        a.shg = Pd.sh;
         ws += (3 * Pd.sh.n * (int64_t)sizeof(float4) + 255) / 256 * 256;
     }
     if (P.ex.tab64) {

@@ -30,6 +30,7 @@ struct StreamArgs {
     const float4* ttab;   // [(n_steps*5+1) x 2] (cos, sin, ga.x, ga.y), (ga.z, -, -, -) at stage times
     int32_t n_sh;
     int32_t sh_kind;
+    ShDev shg;  // SS_SH_GRID: the FP64 spline tables of the subhalos
     // optional checkpoints of the compensated state every ckpt_stride local
     // steps: [n_seg, N, 3] float4 = (xh, vh.x), (vh.yz, xl.xy), (xl.z, vl)
     float4* ckpt;
@@ -154,7 +155,15 @@ __device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamAr
         if (!(fabsf(tau) < s2.y)) continue;
         float rel[3] = {X[0] - (s0.x + s1.x * trel), X[1] - (s0.y + s1.y * trel), X[2] - (s0.z + s1.z * trel)};
         float gp[3], dummy[3];
-        subhalo_grad<float, false>(a.sh_kind, s0.w, s1.w, rel, gp, dummy);
+        if (a.sh_kind == SS_SH_GRID) {
+            float g, gr;
+            grid_subhalo_gh<float, false>(a.shg, j, rel[0] * rel[0] + rel[1] * rel[1] + rel[2] * rel[2], g, gr);
+            gp[0] = g * rel[0];
+            gp[1] = g * rel[1];
+            gp[2] = g * rel[2];
+        } else {
+            subhalo_grad<float, false>(a.sh_kind, s0.w, s1.w, rel, gp, dummy);
+        }
         g[0] += gp[0];
         g[1] += gp[1];
         g[2] += gp[2];

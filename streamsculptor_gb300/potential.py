@@ -392,6 +392,162 @@ class SubhaloLinePotentialCustom_fromFunc(SubhaloLinePotential_Custom):
         self.func = func
 
 
+# ------------------------------------------------- tidally stripped NFW subhalos
+def tnfw_enclosed_mass(R, rhos, rs, ft, rt):
+    """Mass inside R of the truncated NFW rho_s f_t / (x (1+x)^2 (1 + (r/r_t)^2))
+    (potential.py:958-969)."""
+    R, rhos, rs, ft, rt = (np.asarray(host64(v)) for v in (R, rhos, rs, ft, rt))
+    tau = rt / rs
+    u = R / rs
+    t2 = tau ** 2
+    term1 = (t2 - 1) / (t2 + 1) ** 2 * np.log1p(u)
+    term2 = 1 / (t2 + 1) * (1 / (1 + u) - 1)
+    term3 = -(t2 - 1) / (2 * (t2 + 1) ** 2) * np.log1p(u ** 2 / t2)
+    term4 = 2 * tau / (t2 + 1) ** 2 * np.arctan(u / tau)
+    return 4 * np.pi * rhos * ft * rs ** 3 * t2 * (term1 + term2 + term3 + term4)
+
+
+def nfw_params_from_infall(m_infall, c_infall, z_infall, H0=67.4, Omega_m=0.315, Omega_L=0.685):
+    """(rho_s, r_s, R200) of the NFW halo at infall, m200 with respect to
+    rho_crit(z_infall) (potential.py:971-986; its own G = 4.498e-12 kpc^3
+    Msun^-1 Myr^-2 and H0 conversion, Planck 2018 defaults)."""
+    m, c, z = (np.asarray(host64(v)) for v in (m_infall, c_infall, z_infall))
+    G = 4.498e-12
+    H0_myr = H0 * 1e3 / 3.0856e22 * 3.15576e13
+    Hz = H0_myr * np.sqrt(Omega_m * (1 + z) ** 3 + Omega_L)
+    rho_crit = 3 * Hz ** 2 / (8 * np.pi * G)
+    R200 = (3 * m / (4 * np.pi * 200 * rho_crit)) ** (1 / 3)
+    rs = R200 / c
+    rhos = m / (4 * np.pi * rs ** 3 * (np.log1p(c) - c / (1 + c)))
+    return rhos, rs, R200
+
+
+def tidally_evolved_nfw_params_from_infall(m_infall, c_infall, z_infall, f_bound):
+    """(rho_s, r_s, f_t, r_t) on the Du et al. (2024) tidal track for the
+    bound mass fraction f_bound (potential.py:987-1001)."""
+    rhos, rs, r200 = nfw_params_from_infall(m_infall, c_infall, z_infall)
+    f = np.asarray(host64(f_bound))
+    A, B, C = 0.68492777, 0.66438857, 2.07766512
+    D, E = 0.75826635, 0.23376409
+    ft = np.minimum((1 + D) * f ** E / (1 + D * f ** (2 * E)), 1.0)
+    rt = (1 + A) * f ** B / (1 + A * f ** (2 * B)) / np.exp(C * (1 - f)) * r200
+    return rhos, rs, ft, rt
+
+
+def _tnfw_inner(u, tau):
+    """J(u) = int_0^u v dv / ((1+v)^2 (v^2 + tau^2)), M(<r) = 4 pi rho_s f_t
+    r_s^3 tau^2 J(r/r_s).  The closed form (tnfw_enclosed_mass) cancels its
+    O(u) terms at small u (3e-9 relative at u = 1e-4), so there the Taylor
+    series of the integrand is integrated instead."""
+    u = np.asarray(u, dtype=np.float64)
+    t2 = tau ** 2
+    A = (t2 - 1) / (t2 + 1) ** 2
+    closed = (A * (np.log1p(u) - 0.5 * np.log1p(u ** 2 / t2)) - u / ((1 + u) * (1 + t2)) +
+              2 * tau / (t2 + 1) ** 2 * np.arctan(u / tau))
+    small = u < 0.05 * min(1.0, tau)
+    if np.any(small):
+        us = u[small]
+        # v / ((1+v)^2 (tau^2 + v^2)) = sum_n c_n v^n; J = sum_n c_n u^(n+1) / (n+1)
+        n_terms = 40
+        a = np.array([(-1.0) ** k * (k + 1) for k in range(n_terms)])
+        b = np.zeros(n_terms)
+        b[0::2] = np.array([(-1.0 / t2) ** j for j in range((n_terms + 1) // 2)]) / t2
+        c = np.convolve(a, b)[:n_terms - 1]  # coefficients of v^0.. of a*b; times v shifts by one
+        series = np.zeros_like(us)
+        for n in range(n_terms - 2, -1, -1):  # J = sum_n c_n u^(n+2) / (n+2)
+            series = series * us + c[n] / (n + 2)
+        closed = np.array(closed, dtype=np.float64, copy=True)
+        closed[small] = series * us * us
+    return closed
+
+
+def _tnfw_outer(X, tau):
+    """int_X^inf dx / ((1+x)^2 (x^2 + tau^2)), by partial fractions."""
+    t2 = tau ** 2
+    A = 2.0 / (1 + t2) ** 2
+    B = 1.0 / (1 + t2)
+    D = (1 - t2) / (1 + t2) ** 2
+    return A * (0.5 * np.log(X ** 2 + t2) - np.log1p(X)) + B / (1 + X) + D / tau * (np.pi / 2 - np.arctan(X / tau))
+
+
+class _TNFWGrid:
+    """r_grid and phi_grid of one truncated NFW, as the reference's
+    get_potential_from_density object exposes them (potential.py:504-552)."""
+
+    def __init__(self, r_grid, phi_grid):
+        self.r_grid = r_grid
+        self.phi_grid = phi_grid
+
+
+def make_tnfw_potential_from_density_profile(rhos, rs, ft, rt, n_grid=256, G=None):
+    """Phi on r_grid = logspace(1e-4 r_s, 1e3 r_s, n_grid) (potential.py:1009-1020):
+    Phi(r) = -4 pi G (M(<r) / (4 pi r) + int_r^inf rho r' dr'), here with
+    the enclosed mass and the outer integral in closed form (the reference
+    integrates both numerically with quadgk)."""
+    G = _core.G_for(usys) if G is None else G
+    rhos, rs, ft, rt = (float(host64(v)) for v in (rhos, rs, ft, rt))
+    r = np.logspace(np.log10(1e-4 * rs), np.log10(1e3 * rs), int(n_grid))
+    tau = rt / rs
+    M = 4 * np.pi * rhos * ft * rs ** 3 * tau ** 2 * _tnfw_inner(r / rs, tau)
+    outer = rhos * ft * tau ** 2 * rs ** 2 * _tnfw_outer(r / rs, tau)
+    return _TNFWGrid(r, -G * M / r - 4 * np.pi * G * outer)
+
+
+def make_tnfw_potential_from_infall(m_infall, c_infall, z_infall, f_bound):
+    rhos, rs, ft, rt = tidally_evolved_nfw_params_from_infall(m_infall, c_infall, z_infall, f_bound)
+    return make_tnfw_potential_from_density_profile(rhos, rs, ft, rt)
+
+
+def _cubic_knot_slopes(f, du):
+    """Knot derivatives of interpax's 'cubic' interpolant on a uniform grid:
+    the mean of the adjacent secants, one-sided at the two ends."""
+    d = np.empty_like(f)
+    sec = np.diff(f, axis=-1) / du
+    d[..., 1:-1] = 0.5 * (sec[..., 1:] + sec[..., :-1])
+    d[..., 0] = sec[..., 0]
+    d[..., -1] = sec[..., -1]
+    return d
+
+
+class TNFWSubhaloLinePotential(_SubhaloLines):
+    """Tidally stripped NFW subhalos on lines (potential.py:1022-1108): each
+    subhalo's potential is tabulated on 256 log-spaced radii from its infall
+    mass, concentration, infall redshift and bound fraction, and the kernels
+    evaluate the cubic spline in ln r (SS_SH_GRID).  Outside the tabulated
+    radii (1e-4 to 1e3 r_s) the spline continues linearly in ln r where the
+    reference's interpolant returns NaN."""
+
+    _kind = _abi.SS_SH_GRID
+
+    def __init__(self, m_infall, c_infall, z_infall, f_bound, subhalo_x0, subhalo_v, subhalo_t0, t_window,
+                 units=None, n_grid=256):
+        n = len(np.atleast_1d(host64(m_infall)))
+        bc = [np.broadcast_to(np.asarray(host64(v), dtype=np.float64), (n,)) for v in
+              (m_infall, c_infall, z_infall, f_bound)]
+        rhos, rs, ft, rt = tidally_evolved_nfw_params_from_infall(*bc)
+        super().__init__(units, {"subhalo_x0": subhalo_x0, "subhalo_v": subhalo_v, "subhalo_t0": subhalo_t0,
+                                 "t_window": t_window})
+        grids = [make_tnfw_potential_from_density_profile(rhos[i], rs[i], ft[i], rt[i], n_grid, G=self._G)
+                 for i in range(n)]
+        self.log_r_grids = np.stack([np.log(g.r_grid) for g in grids])
+        self.phi_grids = np.stack([g.phi_grid for g in grids])
+        self.rhos, self.rs, self.ft, self.rt = rhos, rs, ft, rt
+        self.m = np.zeros(n)
+        self.a = np.asarray(rs, dtype=np.float64)
+
+    def _table(self) -> SubhaloTable:
+        dev = _core.device()
+        x0 = f64(self.subhalo_x0, dev).reshape(-1, 3)
+        n = x0.shape[0]
+        du = self.log_r_grids[:, 1] - self.log_r_grids[:, 0]
+        slopes = _cubic_knot_slopes(self.phi_grids, du[:, None])
+        grid = np.stack([self.phi_grids, slopes], axis=2)
+        t0 = f64(np.broadcast_to(host64(self.subhalo_t0), (n,)).copy(), dev)
+        return SubhaloTable(self._kind, f64(self.m, dev), f64(self.a, dev), x0, f64(self.subhalo_v, dev).reshape(n, 3),
+                            t0, _f(self.t_window), grid=f64(grid, dev), grid_u0=f64(self.log_r_grids[:, 0], dev),
+                            grid_du=f64(du, dev))
+
+
 class CustomPotential(Potential):
     """Arbitrary Python potential_func(xyz, t): no GPU implementation."""
 
@@ -402,5 +558,7 @@ class CustomPotential(Potential):
 __all__ = ["MiyamotoNagaiDisk", "NFWPotential", "TriaxialNFWPotential", "Isochrone", "PlummerPotential",
            "HernquistPotential", "Potential_Combine", "TimeDepTranslatingPotential", "ProgenitorPotential",
            "GalaMilkyWayPotential", "SubhaloLinePotential", "SubhaloLinePotential_dRadius", "BarPotential",
-           "DehnenBarPotential", "UniformAcceleration", "MW_LMC_Potential",
+           "DehnenBarPotential", "UniformAcceleration", "MW_LMC_Potential", "TNFWSubhaloLinePotential",
+           "tnfw_enclosed_mass", "nfw_params_from_infall", "tidally_evolved_nfw_params_from_infall",
+           "make_tnfw_potential_from_density_profile", "make_tnfw_potential_from_infall",
            "SubhaloLinePotential_Custom", "CustomPotential", "CenterTrack", "usys"]

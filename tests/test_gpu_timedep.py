@@ -111,3 +111,67 @@ def test_time_dependent_streams(ss, oracle, which):
         lead, trail = gpu.gen_stream_vmapped(ts=ts, prog_w0=back, Msat=2e4, normals=normals, precision=precision)
         assert phase_err(np64(lead), final[:, 0]) <= tol, precision
         assert phase_err(np64(trail), final[:, 1]) <= tol, precision
+
+
+def _tnfw(ss, rng, n=4, t0=None, x0=None):
+    """TNFW subhalos (potential.py:1022-1108) and the oracle's table of them."""
+    from streamsculptor_gb300 import potential as P
+    from streamsculptor_gb300.potential import _cubic_knot_slopes
+    m = 10 ** rng.uniform(7.5, 9.0, n)
+    c = rng.uniform(10, 20, n)
+    z = rng.uniform(1.0, 3.0, n)
+    f = rng.uniform(0.05, 0.8, n)
+    x0 = rng.normal(0, 8, (n, 3)) if x0 is None else x0
+    v = rng.normal(0, 0.15, (n, 3))
+    t0 = rng.uniform(-300, -50, n) if t0 is None else t0
+    pot = P.TNFWSubhaloLinePotential(m, c, z, f, x0, v, t0, 120.0, units=ss.usys)
+    du = pot.log_r_grids[:, 1] - pot.log_r_grids[:, 0]
+    grid = np.stack([pot.phi_grids, _cubic_knot_slopes(pot.phi_grids, du[:, None])], axis=2)
+    sh = dict(kind=_abi.SS_SH_GRID, m=np.zeros(n), a=pot.a, x0=x0, v=v, t0=t0, t_window=120.0, grid=grid,
+              grid_u0=pot.log_r_grids[:, 0], grid_du=du)
+    return pot, sh
+
+
+def test_tnfw_subhalos_eval_and_streams(ss, oracle):
+    """Per-subhalo potential and gradient, then a stream in base + TNFW
+    subhalos (FP64 and FP32 compensated) and the mass response (6 columns),
+    all against the oracle's spline of the same tables."""
+    from streamsculptor_gb300 import _core, perturbative
+    from streamsculptor_gb300.streamhelpers import gen_stream_vmapped_with_pert_fixed_prog
+    rng = np.random.default_rng(44)
+    n_rel = 300
+    orc = oracle.HostModel(oracle.mw3())
+    back = oracle.orbit(orc, PROG_WF, 0.0, -1.0, n_rel, n_rel)[0, -1]
+    ts = -n_rel + np.arange(n_rel + 1) * 1.0
+    ws = oracle.orbit(orc, back, ts[0], 1.0, n_rel, 1)[0]
+    pot, sh = _tnfw(ss, rng, x0=ws[[60, 140, 200, 250], :3] + rng.normal(0, 0.8, (4, 3)),
+                    t0=ts[[60, 140, 200, 250]])
+    x = ws[::7, :3] + rng.normal(0, 1.0, (len(ws[::7]), 3))
+    for t in (ts[60], ts[200]):
+        phi_g = np64(pot.potential_per_SH(x, t))
+        g_g = np64(pot.gradient_per_SH(x, t))
+        phi_o, g_o, _, _ = oracle.subhalo_eval(oracle.HostModel(oracle.mw3(), subhalos=sh), x, t)
+        assert rel_err(phi_g, phi_o) < 1e-12 and rel_err(g_g, g_o) < 1e-12
+    normals = rng.standard_normal((n_rel + 1, 1, 4))
+    ics, _ = oracle.release(orc, ws, ts, 2e4, normals)
+    tot = oracle.HostModel(oracle.mw3(), subhalos=sh)
+    final, _, st = oracle.stream(tot, ts[0], 1.0, n_rel, ics[:-1].reshape(-1, 6), 2, 1)
+    assert (st == 0).all()
+    final = final.reshape(n_rel, 2, 6)
+    for precision, tol in (("f64", 1e-10), ("f32k", 1e-5)):
+        lead, trail = gen_stream_vmapped_with_pert_fixed_prog(mw3_gpu(ss), pot, ts=ts, prog_w0=back, Msat=2e4,
+                                                              normals=normals, precision=precision)
+        assert phase_err(np64(lead), final[:, 0]) <= tol, precision
+        assert phase_err(np64(trail), final[:, 1]) <= tol, precision
+    # first-order mass response of every particle (GenerateMassPerturbation)
+    bsm = perturbative.BaseStreamModel(mw3_gpu(ss), back, ts, 2e4, 0, normals=normals)
+    gen = perturbative.GenerateMassPerturbation(mw3_gpu(ss), pot, bsm)
+    (lb, ld), (tb, td) = gen.compute_perturbation_OTF()
+    base = np.stack([np64(gen.base_realspace_ICs_lead[:n_rel]), np64(gen.base_realspace_ICs_trail[:n_rel])], 1)
+    pert = np.stack([np64(gen.perturbation_ICs_lead[:n_rel]), np64(gen.perturbation_ICs_trail[:n_rel])], 1)
+    bo, po = oracle.pert_response(tot, ts[0], 1.0, n_rel, base.reshape(-1, 6), pert.reshape(2 * n_rel, 4, 6), 2, 1,
+                                  ncol=6)
+    d = np.stack([np64(ld), np64(td)], 1).reshape(2 * n_rel, 4, 6)
+    assert rel_err(d, po[0]) <= 1e-9
+    with pytest.raises(_abi.SSError):
+        perturbative.GenerateMassRadiusPerturbation(mw3_gpu(ss), pot, pot, bsm)  # no scale-radius response
