@@ -284,6 +284,45 @@ def gpu_arm(args, wl):
                   "config": {"workload": wl["name"]}, "clocks": r32["clocks"], "gpu_launches": r32["launches"],
                   "note": "f32k only (profiling run)"})
         return
+    # --- e2e through the public API with host buffers (right after the device timing)
+    n_snap = n_steps // snap if snap else 0
+
+    def e2e_step():
+        # public API with host inputs and host outputs: gen_stream(out="host")
+        # integrates in particle sub-ranges and copies each one to pinned host
+        # memory while the next integrates
+        sol = pot.integrate_orbit(w0=WF, ts=np.array([0.0, -T]), t0=0.0, t1=-T, dt=dt)
+        out = gen_stream(pot, ts, sol.ys[-1], MSAT, normals=normals_h, dt=dt, prog_pot=prog,
+                         n_particles_per_release=ppr, precision="f32k", snapshot_every=snap or None, out="host")
+        assert not out[0].is_cuda
+        torch.cuda.synchronize()
+
+    for _ in range(2):
+        e2e_step()
+    k_e2e = max(1, min(args.steps, 5))
+    tsum = 0.0
+    e2e_samples = []
+    e2e_clk = ClockSampler(gpu_id_for(local))
+    e2e_clk.start()
+    for _ in range(k_e2e):
+        flush.zero_()
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        e2e_step()
+        barrier()
+        dt_s = time.perf_counter() - t0
+        tsum += dt_s
+        e2e_samples.append(dt_s * 1e3)
+    e2e_clocks = e2e_clk.stop()
+    e2e_s = tsum / k_e2e
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = normals_h.nbytes + ts.nbytes + WF.nbytes + 2 * 8
+    d2h = n_rel * ppr * 6 * 8 + (n_snap * n_rel * ppr * 6 * 4 if snap else 0)  # final states + snapshots
+
     # --- FP64 plain beside it
     k64 = max(1, min(args.steps, args.f64_steps))
     r64 = timed("f64", k64, max(1, min(args.warmup, args.f64_warmup)))
@@ -333,39 +372,6 @@ def gpu_arm(args, wl):
         "frac_err_above_1e-5_growth_le_1e3": float(((e > 1e-5) & regular).double().mean())}
     del l32, t32, l64, t64, a, b, bp, b0, ic0, icp
 
-    # --- e2e through the public API with host buffers
-    n_snap = n_steps // snap if snap else 0
-
-    def e2e_step():
-        # public API with host inputs and host outputs: gen_stream(out="host")
-        # integrates in particle sub-ranges and copies each one to pinned host
-        # memory while the next integrates
-        sol = pot.integrate_orbit(w0=WF, ts=np.array([0.0, -T]), t0=0.0, t1=-T, dt=dt)
-        out = gen_stream(pot, ts, sol.ys[-1], MSAT, normals=normals_h, dt=dt, prog_pot=prog,
-                         n_particles_per_release=ppr, precision="f32k", snapshot_every=snap or None, out="host")
-        assert not out[0].is_cuda
-        torch.cuda.synchronize()
-
-    for _ in range(2):
-        e2e_step()
-    k_e2e = max(1, min(args.steps, 5))
-    tsum = 0.0
-    for _ in range(k_e2e):
-        flush.zero_()
-        torch.cuda.synchronize()
-        barrier()
-        t0 = time.perf_counter()
-        e2e_step()
-        barrier()
-        tsum += time.perf_counter() - t0
-    e2e_s = tsum / k_e2e
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    h2d = normals_h.nbytes + ts.nbytes + WF.nbytes + 2 * 8
-    d2h = n_rel * ppr * 6 * 8 + (n_snap * n_rel * ppr * 6 * 4 if snap else 0)  # final states + snapshots
-
     # --- roofline of the dominant kernel (stream_f32k_kernel)
     flat = P.Potential_Combine([pot] + ([P.TimeDepTranslatingPotential(prog, _core.CenterTrack(0.0, 1.0, wf_d.reshape(2, 3)))]
                                         if prog is not None else []), units=u)._flatten()
@@ -407,6 +413,7 @@ def gpu_arm(args, wl):
               "cpu_baseline": cpu,
               "e2e": {"value": world * work / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                       "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
+                      "samples_ms": e2e_samples, "clocks": e2e_clocks,
                       "path": "integrate_orbit + streamhelpers.gen_stream(out='host') with host numpy inputs: "
                               "particle sub-ranges copied to pinned host memory while the next integrates"},
               "clocks": clk, "gpu_launches": r32["launches"],

@@ -265,7 +265,10 @@ int ss_stream_f32k(const ss_potential* pot, const ss_stream_cfg* cfg, const doub
     const int block = 128;
     unsigned grid = (unsigned)((cfg->n_particles + block - 1) / block);
     dispatch_comp(P, [&](auto comp) {
-        stream_f32k_kernel<decltype(comp)><<<grid, block, 0, s>>>(P, a);
+        if (a.n_sh > 0)
+            stream_f32k_kernel<decltype(comp), true><<<grid, block, 0, s>>>(P, a);
+        else
+            stream_f32k_kernel<decltype(comp), false><<<grid, block, 0, s>>>(P, a);
         return 0;
     });
     SS_LAUNCH_CHECK();

@@ -122,7 +122,10 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 // d: the small remainder of the stage offset).  Components on the center
 // track use (xh - c_hi) + (d - c_lo): xh and c_hi are close, so the
 // difference is exact and the separation keeps its relative precision.
-template <class C>
+// SUB: the run has subhalos (the kernels are instantiated without the
+// subhalo loop for the runs that have none, which keeps the six inlined
+// force evaluations of a step compact).
+template <class C, bool SUB = true>
 __device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamArgs& a, const float xh[3],
                                           const float d[3], int slot, float trel, float A[3], int shb, int she) {
     const float X[3] = {xh[0] + d[0], xh[1] + d[1], xh[2] + d[2]};
@@ -146,6 +149,7 @@ __device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamAr
         td.ga[2] = t1.x;
     }
     C::template grad<float, float, false>(P, X, xs, g, nullptr, td);
+    if constexpr (SUB) {
 #pragma unroll 1
     for (int j = shb; j < she; ++j) {
         float4 s0 = __ldg(a.shtab + 3 * j);
@@ -168,6 +172,7 @@ __device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamAr
         g[1] += gp[1];
         g[2] += gp[2];
     }
+    }
     A[0] = -g[0];
     A[1] = -g[1];
     A[2] = -g[2];
@@ -178,7 +183,7 @@ __device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamAr
 // rounded tableau.
 // shb, she: the subhalo rows [shb, she) of the table this particle feels
 // (she < 0: all of them).
-template <class C>
+template <class C, bool SUB = true>
 __device__ __forceinline__ void step_f32k(const PotDev<float>& P, const StreamArgs& a, int n, float xh[3],
                                           float xl[3], float vh[3], float vl[3], int shb = 0, int she = -1) {
     if (she < 0) she = a.n_sh;
@@ -193,32 +198,32 @@ __device__ __forceinline__ void step_f32k(const PotDev<float>& P, const StreamAr
         D[i] = xl[i];
         d1[i] = vl[i];
     }
-    accel_f32<C>(P, a, xh, D, s0, tn, A1, shb, she);
+    accel_f32<C, SUB>(P, a, xh, D, s0, tn, A1, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d2[i] = vl[i] + h * (F_(SS_A21) * A1[i]);
         D[i] = xl[i] + h * (F_C2 * vh[i] + F_(SS_A21) * d1[i]);
     }
-    accel_f32<C>(P, a, xh, D, s0 + 1, tn + F_C2 * h, A2, shb, she);
+    accel_f32<C, SUB>(P, a, xh, D, s0 + 1, tn + F_C2 * h, A2, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d3[i] = vl[i] + h * (F_(SS_A31) * A1[i] + F_(SS_A32) * A2[i]);
         D[i] = xl[i] + h * (F_C3 * vh[i] + F_(SS_A31) * d1[i] + F_(SS_A32) * d2[i]);
     }
-    accel_f32<C>(P, a, xh, D, s0 + 2, tn + F_C3 * h, A3, shb, she);
+    accel_f32<C, SUB>(P, a, xh, D, s0 + 2, tn + F_C3 * h, A3, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d4[i] = vl[i] + h * (F_(SS_A41) * A1[i] + F_(SS_A42) * A2[i] + F_(SS_A43) * A3[i]);
         D[i] = xl[i] + h * (F_C4 * vh[i] + F_(SS_A41) * d1[i] + F_(SS_A42) * d2[i] + F_(SS_A43) * d3[i]);
     }
-    accel_f32<C>(P, a, xh, D, s0 + 3, tn + F_C4 * h, A4, shb, she);
+    accel_f32<C, SUB>(P, a, xh, D, s0 + 3, tn + F_C4 * h, A4, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d5[i] = vl[i] + h * (F_(SS_A51) * A1[i] + F_(SS_A52) * A2[i] + F_(SS_A53) * A3[i] + F_(SS_A54) * A4[i]);
         D[i] = xl[i] + h * (F_C5 * vh[i] + F_(SS_A51) * d1[i] + F_(SS_A52) * d2[i] + F_(SS_A53) * d3[i] +
                             F_(SS_A54) * d4[i]);
     }
-    accel_f32<C>(P, a, xh, D, s0 + 4, tn + F_C5 * h, A5, shb, she);
+    accel_f32<C, SUB>(P, a, xh, D, s0 + 4, tn + F_C5 * h, A5, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d6[i] = vl[i] + h * (F_(SS_A61) * A1[i] + F_(SS_A62) * A2[i] + F_(SS_A63) * A3[i] + F_(SS_A64) * A4[i] +
@@ -226,7 +231,7 @@ __device__ __forceinline__ void step_f32k(const PotDev<float>& P, const StreamAr
         D[i] = xl[i] + h * (vh[i] + F_(SS_A61) * d1[i] + F_(SS_A62) * d2[i] + F_(SS_A63) * d3[i] +
                             F_(SS_A64) * d4[i] + F_(SS_A65) * d5[i]);
     }
-    accel_f32<C>(P, a, xh, D, s0 + 5, tn + h, A6, shb, she);
+    accel_f32<C, SUB>(P, a, xh, D, s0 + 5, tn + h, A6, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         // position: h * (vh + Db), Db = sum b_i d_i
@@ -251,7 +256,7 @@ __device__ __forceinline__ void step_f32k(const PotDev<float>& P, const StreamAr
     }
 }
 
-template <class C>
+template <class C, bool SUB>
 __global__ void __launch_bounds__(128) stream_f32k_kernel(PotDev<float> P, StreamArgs a) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p < a.N;
@@ -284,7 +289,7 @@ __global__ void __launch_bounds__(128) stream_f32k_kernel(PotDev<float> P, Strea
                 c[1] = make_float4(vh[1], vh[2], xl[0], xl[1]);
                 c[2] = make_float4(xl[2], vl[0], vl[1], vl[2]);
             }
-            step_f32k<C>(P, a, n, xh, xl, vh, vl, shb, she);
+            step_f32k<C, SUB>(P, a, n, xh, xl, vh, vl, shb, she);
         }
         if (a.snaps && (n + 1) % a.stride == 0 && valid) {
             float y[6] = {xh[0], xh[1], xh[2], vh[0], vh[1], vh[2]};
