@@ -1358,6 +1358,11 @@ struct KC_ {
 template <int... KCS>
 struct Comp {
     static constexpr int n = sizeof...(KCS);
+    // whether a component sits on the center track, known at compile time
+    template <class R>
+    static __device__ __forceinline__ constexpr bool uses_track(const PotDev<R>&) {
+        return ((KCS >> 4) | ... | 0) != 0;
+    }
     template <class T, class R, bool HESS, int... I>
     static __device__ __forceinline__ void add(const PotDev<R>& P, const T x[3], const T xs[3], T grad[3], T H[6],
                                                const TimeDep<T>& td, std::integer_sequence<int, I...>) {
@@ -1398,6 +1403,10 @@ struct Comp {
 };
 
 struct GenericComp {
+    template <class R>
+    static __device__ __forceinline__ bool uses_track(const PotDev<R>& P) {
+        return P.has_track != 0;
+    }
     template <class T, class R, bool HESS>
     static __device__ __forceinline__ void grad(const PotDev<R>& P, const T x[3], const T xs[3], T g[3], T H[6],
                                                 const TimeDep<T>& td = TimeDep<T>()) {

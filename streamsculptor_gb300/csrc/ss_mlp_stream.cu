@@ -368,6 +368,10 @@ __device__ __noinline__ void mlp_grad_wg(const MlpDev& M, const MlpCta& cx, floa
 // network evaluation (the CTA context lives in shared memory).
 struct MlpComp {
     static constexpr int n = 1;
+    template <class R>
+    static __device__ __forceinline__ constexpr bool uses_track(const PotDev<R>&) {
+        return false;
+    }
     template <class T, class R, bool HESS>
     static __device__ __forceinline__ void grad(const PotDev<R>& P, const T x[3], const T xs[3], T g[3], T H[6],
                                                 const TimeDep<T>& td = TimeDep<T>());

@@ -130,7 +130,7 @@ __device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamAr
                                           const float d[3], int slot, float trel, float A[3], int shb, int she) {
     const float X[3] = {xh[0] + d[0], xh[1] + d[1], xh[2] + d[2]};
     float xs[3] = {X[0], X[1], X[2]};
-    if (P.has_track) {
+    if (C::uses_track(P)) {
         const float4 ch = __ldg(a.ctab + 2 * slot);
         const float4 cl = __ldg(a.ctab + 2 * slot + 1);
         xs[0] = (xh[0] - ch.x) + (d[0] - cl.x);
@@ -281,6 +281,7 @@ __global__ void __launch_bounds__(128) stream_f32k_kernel(PotDev<float> P, Strea
             write_snap<float>(a.snaps, a.snap_pitch, k, p + a.p_off, step >= start, y);
         }
     }
+    int next_snap = (wstart / a.stride + 1) * a.stride;  // first snapshot step after wstart
     for (int n = wstart; n < a.n_steps; ++n) {
         if (valid && n >= start) {
             if (a.ckpt != nullptr && (n - start) % a.ckpt_stride == 0) {
@@ -291,9 +292,12 @@ __global__ void __launch_bounds__(128) stream_f32k_kernel(PotDev<float> P, Strea
             }
             step_f32k<C, SUB>(P, a, n, xh, xl, vh, vl, shb, she);
         }
-        if (a.snaps && (n + 1) % a.stride == 0 && valid) {
-            float y[6] = {xh[0], xh[1], xh[2], vh[0], vh[1], vh[2]};
-            write_snap<float>(a.snaps, a.snap_pitch, (n + 1) / a.stride - 1, p + a.p_off, n + 1 >= start, y);
+        if (n + 1 == next_snap) {  // snapshot rows follow every a.stride global steps
+            next_snap += a.stride;
+            if (a.snaps && valid) {
+                float y[6] = {xh[0], xh[1], xh[2], vh[0], vh[1], vh[2]};
+                write_snap<float>(a.snaps, a.snap_pitch, (n + 1) / a.stride - 1, p + a.p_off, n + 1 >= start, y);
+            }
         }
     }
     if (!valid) return;
