@@ -444,7 +444,7 @@ int ss_stream_f32k_ckpt(const ss_potential* pot, const ss_stream_cfg* cfg, const
     const int block = 128;
     unsigned grid = (unsigned)((cfg->n_particles + block - 1) / block);
     dispatch_comp(P, [&](auto comp) {
-        stream_f32k_kernel<decltype(comp), false><<<grid, block, 0, (cudaStream_t)stream>>>(P, a);  // no subhalos
+        stream_f32k_kernel<decltype(comp), false, true><<<grid, block, 0, (cudaStream_t)stream>>>(P, a);
         return 0;
     });
     SS_LAUNCH_CHECK();

@@ -256,7 +256,8 @@ __device__ __forceinline__ void step_f32k(const PotDev<float>& P, const StreamAr
     }
 }
 
-template <class C, bool SUB>
+// CKPT: the run records checkpoints (the adjoint's forward pass).
+template <class C, bool SUB, bool CKPT = false>
 __global__ void __launch_bounds__(128) stream_f32k_kernel(PotDev<float> P, StreamArgs a) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p < a.N;
@@ -284,7 +285,7 @@ __global__ void __launch_bounds__(128) stream_f32k_kernel(PotDev<float> P, Strea
     int next_snap = (wstart / a.stride + 1) * a.stride;  // first snapshot step after wstart
     for (int n = wstart; n < a.n_steps; ++n) {
         if (valid && n >= start) {
-            if (a.ckpt != nullptr && (n - start) % a.ckpt_stride == 0) {
+            if (CKPT && (n - start) % a.ckpt_stride == 0) {
                 float4* c = a.ckpt + ((int64_t)((n - start) / a.ckpt_stride) * a.N + p) * 3;
                 c[0] = make_float4(xh[0], xh[1], xh[2], vh[0]);
                 c[1] = make_float4(vh[1], vh[2], xl[0], xl[1]);
