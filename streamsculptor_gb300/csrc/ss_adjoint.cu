@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(128) stream_adjoint_kernel(PotDev<float> P, Ad
                 float* tp = tape[n - n0];
                 tp[0] = xh[0]; tp[1] = xh[1]; tp[2] = xh[2];
                 tp[3] = vh[0]; tp[4] = vh[1]; tp[5] = vh[2];
-                step_f32k<C, false>(P, a.s, n, xh, xl, vh, vl);
+                step_f32k<C, SUB_NONE>(P, a.s, n, xh, xl, vh, vl);
             }
             for (int n = n1 - 1; n >= n0; --n) {
                 const float* tp = tape[n - n0];
@@ -444,7 +444,7 @@ int ss_stream_f32k_ckpt(const ss_potential* pot, const ss_stream_cfg* cfg, const
     const int block = 128;
     unsigned grid = (unsigned)((cfg->n_particles + block - 1) / block);
     dispatch_comp(P, [&](auto comp) {
-        stream_f32k_kernel<decltype(comp), false, true><<<grid, block, 0, (cudaStream_t)stream>>>(P, a);
+        stream_f32k_kernel<decltype(comp), SUB_NONE, true><<<grid, block, 0, (cudaStream_t)stream>>>(P, a);
         return 0;
     });
     SS_LAUNCH_CHECK();

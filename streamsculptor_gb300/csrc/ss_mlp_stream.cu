@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) stream_mlp_kernel(const __grid
                 uh[i] = vh[i];
                 ul[i] = vl[i];
             }
-            step_f32k<MlpComp, false>(P, a, n, th, tlo, uh, ul);  // the surrogate alone: no subhalos
+            step_f32k<MlpComp, SUB_NONE>(P, a, n, th, tlo, uh, ul);  // the surrogate alone: no subhalos
             if (valid && n >= start) {
 #pragma unroll
                 for (int i = 0; i < 3; ++i) {

@@ -264,13 +264,18 @@ int ss_stream_f32k(const ss_potential* pot, const ss_stream_cfg* cfg, const doub
     }
     const int block = 128;
     unsigned grid = (unsigned)((cfg->n_particles + block - 1) / block);
-    dispatch_comp(P, [&](auto comp) {
-        if (a.n_sh > 0)
-            stream_f32k_kernel<decltype(comp), true><<<grid, block, 0, s>>>(P, a);
-        else
-            stream_f32k_kernel<decltype(comp), false><<<grid, block, 0, s>>>(P, a);
-        return 0;
-    });
+    if (a.n_sh > 0 && a.sh_kind == SS_SH_GRID) {
+        // tabulated subhalos: one generic instantiation
+        stream_f32k_kernel<GenericComp, SUB_GRID><<<grid, block, 0, s>>>(P, a);
+    } else {
+        dispatch_comp(P, [&](auto comp) {
+            if (a.n_sh > 0)
+                stream_f32k_kernel<decltype(comp), SUB_LINES><<<grid, block, 0, s>>>(P, a);
+            else
+                stream_f32k_kernel<decltype(comp), SUB_NONE><<<grid, block, 0, s>>>(P, a);
+            return 0;
+        });
+    }
     SS_LAUNCH_CHECK();
     return SS_OK;
 }

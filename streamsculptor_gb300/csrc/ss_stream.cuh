@@ -10,6 +10,8 @@
 
 namespace ssg {
 
+enum { SUB_NONE = 0, SUB_LINES = 1, SUB_GRID = 2 };
+
 struct StreamArgs {
     const double* ics;
     double* final_w;
@@ -122,10 +124,11 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 // d: the small remainder of the stage offset).  Components on the center
 // track use (xh - c_hi) + (d - c_lo): xh and c_hi are close, so the
 // difference is exact and the separation keeps its relative precision.
-// SUB: the run has subhalos (the kernels are instantiated without the
-// subhalo loop for the runs that have none, which keeps the six inlined
-// force evaluations of a step compact).
-template <class C, bool SUB = true>
+// SUB: the run's subhalos — SUB_NONE, SUB_LINES (Plummer / Hernquist) or
+// SUB_GRID (tabulated).  The kernels are instantiated per case, so a run
+// carries only the subhalo code it uses: the six force evaluations of a
+// step are inlined, and a compact step issues measurably fewer instructions.
+template <class C, int SUB = SUB_LINES>
 __device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamArgs& a, const float xh[3],
                                           const float d[3], int slot, float trel, float A[3], int shb, int she) {
     const float X[3] = {xh[0] + d[0], xh[1] + d[1], xh[2] + d[2]};
@@ -149,7 +152,7 @@ __device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamAr
         td.ga[2] = t1.x;
     }
     C::template grad<float, float, false>(P, X, xs, g, nullptr, td);
-    if constexpr (SUB) {
+    if constexpr (SUB != SUB_NONE) {
 #pragma unroll 1
     for (int j = shb; j < she; ++j) {
         float4 s0 = __ldg(a.shtab + 3 * j);
@@ -159,7 +162,7 @@ __device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamAr
         if (!(fabsf(tau) < s2.y)) continue;
         float rel[3] = {X[0] - (s0.x + s1.x * trel), X[1] - (s0.y + s1.y * trel), X[2] - (s0.z + s1.z * trel)};
         float gp[3], dummy[3];
-        if (a.sh_kind == SS_SH_GRID) {
+        if constexpr (SUB == SUB_GRID) {
             float g, gr;
             grid_subhalo_gh<float, false>(a.shg, j, rel[0] * rel[0] + rel[1] * rel[1] + rel[2] * rel[2], g, gr);
             gp[0] = g * rel[0];
@@ -183,7 +186,7 @@ __device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamAr
 // rounded tableau.
 // shb, she: the subhalo rows [shb, she) of the table this particle feels
 // (she < 0: all of them).
-template <class C, bool SUB = true>
+template <class C, int SUB = SUB_LINES>
 __device__ __forceinline__ void step_f32k(const PotDev<float>& P, const StreamArgs& a, int n, float xh[3],
                                           float xl[3], float vh[3], float vl[3], int shb = 0, int she = -1) {
     if (she < 0) she = a.n_sh;
@@ -257,7 +260,7 @@ __device__ __forceinline__ void step_f32k(const PotDev<float>& P, const StreamAr
 }
 
 // CKPT: the run records checkpoints (the adjoint's forward pass).
-template <class C, bool SUB, bool CKPT = false>
+template <class C, int SUB, bool CKPT = false>
 __global__ void __launch_bounds__(128) stream_f32k_kernel(PotDev<float> P, StreamArgs a) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p < a.N;
