@@ -443,7 +443,8 @@ def _aux_stream(dev: torch.device, name: str) -> torch.cuda.Stream:
     return _AUX_STREAMS[key]
 
 
-def stream_to_host(P, cfg, ics: torch.Tensor, precision: str, snap_every: int = 0, mlp=None, n_chunks: int = 4):
+def stream_to_host(P, cfg, ics: torch.Tensor, precision: str, snap_every: int = 0, mlp=None, n_chunks: int = 8,
+                   n_streams: int = 2):
     """The stream in particle sub-ranges whose results are copied to pinned
     host memory while later sub-ranges integrate: sub-range kernels alternate
     between two CUDA streams (so one's last wave overlaps the next one's
@@ -462,9 +463,11 @@ def stream_to_host(P, cfg, ics: torch.Tensor, precision: str, snap_every: int = 
     final_h = torch.empty(N, 6, dtype=torch.float64, pin_memory=True)
     snaps_h = torch.empty(n_snap, N, 6, dtype=torch.float32, pin_memory=True) if n_snap else None
     main = torch.cuda.current_stream(dev)
-    comp = [_aux_stream(dev, "compute0"), _aux_stream(dev, "compute1")]
-    side = _aux_stream(dev, "copy")
-    for st in comp + [side]:
+    comp = [_aux_stream(dev, f"compute{i}") for i in range(max(1, int(n_streams)))]
+    # one copy stream per compute stream: a sub-range's copy never queues
+    # behind the copy of a sub-range that is still integrating on the other
+    copies = [_aux_stream(dev, f"copy{i}") for i in range(len(comp))]
+    for st in comp + copies:
         st.wait_stream(main)  # inputs and buffers are ready on the main stream
     lib = _abi.load()
     per = max(128, -(-N // max(1, n_chunks) // 128) * 128)
@@ -475,7 +478,7 @@ def stream_to_host(P, cfg, ics: torch.Tensor, precision: str, snap_every: int = 
         c.snap_pitch = N if n_snap else 0
         c.snap_stride = snap_every if n_snap else 0
         sub_ics, fin, stt = ics[p0:p1], final_d[p0:p1], status_d[p0:p1]
-        cs = comp[c_idx % 2]
+        cs = comp[c_idx % len(comp)]
         h = C.c_void_p(cs.cuda_stream)
         if precision == "f64":
             _abi.call("ss_stream_f64", C.byref(P), C.byref(c), ptr(sub_ics), ptr(fin), ptr(snaps_d), ptr(stt), h)
@@ -483,7 +486,7 @@ def stream_to_host(P, cfg, ics: torch.Tensor, precision: str, snap_every: int = 
             need = lib.ss_stream_workspace_bytes(C.byref(P), C.byref(c))
             if need < 0:
                 raise _abi.SSError("ss_stream_workspace_bytes", need, lib.ss_last_error().decode())
-            ws, nb = aligned_ptr(Workspace.get(need, dev, slot=f"compute{c_idx % 2}"))
+            ws, nb = aligned_ptr(Workspace.get(need, dev, slot=f"compute{c_idx % len(comp)}"))
             _abi.call("ss_stream_f32k", C.byref(P), C.byref(c), ptr(sub_ics), ptr(fin), ptr(snaps_d), ptr(stt), ws,
                       nb, h)
         elif precision == "mlp":
@@ -494,6 +497,7 @@ def stream_to_host(P, cfg, ics: torch.Tensor, precision: str, snap_every: int = 
             raise ValueError("precision must be 'f64', 'f32k' or 'mlp'")
         ev = torch.cuda.Event()
         ev.record(cs)
+        side = copies[c_idx % len(comp)]
         side.wait_event(ev)
         hs = C.c_void_p(side.cuda_stream)
         _abi.call("ss_copy_rows_async", C.c_void_p(final_h.data_ptr()), ptr(final_d), 1, N * 48, p0 * 48,
@@ -501,11 +505,11 @@ def stream_to_host(P, cfg, ics: torch.Tensor, precision: str, snap_every: int = 
         if n_snap:
             _abi.call("ss_copy_rows_async", C.c_void_p(snaps_h.data_ptr()), ptr(snaps_d), n_snap, N * 24, p0 * 24,
                       (p1 - p0) * 24, 0, hs)
-    for st in comp + [side]:
+    for st in comp + copies:
         main.wait_stream(st)
     for t in (final_d, status_d, snaps_d, ics):
         if t is not None:
-            for st in comp + [side]:
+            for st in comp + copies:
                 t.record_stream(st)
     return final_h, snaps_h, status_d
 
