@@ -182,7 +182,8 @@ typedef struct ss_stream_cfg {
      * first_particle + n_particles - 1 of a larger stream (their release
      * steps follow from those global indices); ics/final_w/status are indexed
      * from first_particle, snapshots are rows of snap_pitch particles
-     * (0 = n_particles) written at the global index.  Zero for whole runs. */
+     * (0 = first_particle + n_particles) written at the global index.  Zero
+     * for whole runs. */
     int64_t first_particle;
     int64_t snap_pitch;
     /* Ensembles of independent streams (jax.vmap of gen_stream_vmapped_with_pert

@@ -203,13 +203,14 @@ def release(model: HostModel, prog_w, t_rel, msat, normals, kvals=(2.0, 0.3, 0.0
 
 
 def stream(model: HostModel, t0, dt, n_steps, ics, ppr, spr, snap_stride=0, n_threads=0, stream_particles=0,
-           subhalos_per_stream=0):
+           subhalos_per_stream=0, first_particle=0):
     P = model.struct()
     ics = f8(ics).reshape(-1, 6)
     cfg = _abi.ss_stream_cfg()
     cfg.t0, cfg.dt, cfg.n_steps, cfg.n_particles = float(t0), float(dt), int(n_steps), ics.shape[0]
     cfg.particles_per_release, cfg.steps_per_release, cfg.snap_stride = int(ppr), int(spr), int(snap_stride)
     cfg.stream_particles, cfg.subhalos_per_stream = int(stream_particles), int(subhalos_per_stream)
+    cfg.first_particle = int(first_particle)  # ics are particles first_particle.. of the stream
     final = np.empty_like(ics)
     status = np.empty(ics.shape[0], dtype=np.int32)
     snaps = None

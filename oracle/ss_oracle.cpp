@@ -858,10 +858,11 @@ void or_stream(const ss_potential* P, const ss_stream_cfg* cfg, const double* ic
         // ensembles: particle p is particle p % stream_particles of stream
         // p / stream_particles, which feels its own subhalo rows
         const int64_t grp = cfg->stream_particles;
-        const int64_t pl = grp > 0 ? p % grp : p;
+        const int64_t pg = p + cfg->first_particle;  // global index (sub-range runs)
+        const int64_t pl = grp > 0 ? pg % grp : pg;
         ss_potential Pl = *P;
         if (cfg->subhalos_per_stream > 0) {
-            const int64_t k = cfg->subhalos_per_stream, o = (p / grp) * k;
+            const int64_t k = cfg->subhalos_per_stream, o = (pg / grp) * k;
             Pl.subhalos.n = k;
             Pl.subhalos.m += o;
             Pl.subhalos.a += o;

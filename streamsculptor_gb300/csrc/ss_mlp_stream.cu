@@ -650,7 +650,7 @@ int ss_stream_mlp_bf16(const ss_mlp* mlp, const ss_stream_cfg* cfg, const double
     a.h_hi = (float)cfg->dt;
     a.h_lo = (float)(cfg->dt - (double)a.h_hi);
     a.p_off = cfg->first_particle;
-    a.snap_pitch = cfg->snap_pitch > 0 ? cfg->snap_pitch : cfg->n_particles;
+    a.snap_pitch = cfg->snap_pitch > 0 ? cfg->snap_pitch : cfg->first_particle + cfg->n_particles;
     ka.n_tiles = (cfg->n_particles + 127) / 128;
     int dev = 0, sms = 0;
     SS_CUDA_TRY(cudaGetDevice(&dev));

@@ -133,7 +133,7 @@ static StreamArgs make_args(const ss_stream_cfg* cfg, const double* ics, double*
     a.h_hi = (float)cfg->dt;
     a.h_lo = (float)(cfg->dt - (double)a.h_hi);
     a.p_off = cfg->first_particle;
-    a.snap_pitch = cfg->snap_pitch > 0 ? cfg->snap_pitch : cfg->n_particles;
+    a.snap_pitch = cfg->snap_pitch > 0 ? cfg->snap_pitch : cfg->first_particle + cfg->n_particles;
     a.grp = cfg->stream_particles;
     a.sh_per_grp = cfg->subhalos_per_stream;
     return a;

@@ -40,7 +40,7 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
                kval_arr=1.0, dt=None, dtmax=None, n_particles_per_release=2, normals=None, precision="f64",
                snapshot_every=None, throw=False, release="fardal", prog_pot: Optional[Potential] = None,
                pot_pert: Optional[Potential] = None, prog_in_pert=False, return_ics=False, prog_method="auto",
-               force_surrogate=None, out="device"):
+               force_surrogate=None, out="device", release_range=None):
     """Generate a particle-spray stream on the GPU.
 
     pot_base    smooth potential (release model and integration)
@@ -61,8 +61,12 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
                 in the force of `force_surrogate` (surrogate.MLPSurrogate, BF16
                 tensor cores) while the progenitor orbit and the release use
                 the exact pot_base
-    Returns (lead, trail) [len(ts)-1, 6] (or [len(ts)-1, n_draw, 6]); with
-    snapshot_every also the float32 snapshots [n_snap, len(ts)-1, n_draw, 2, 6].
+    release_range (r0, r1): integrate only the particles of releases r0..r1-1
+                (one rank's share of a stream split across GPUs, sharding.py);
+                the progenitor orbit and the release are computed in full
+    Returns (lead, trail) [len(ts)-1, 6] (or [len(ts)-1, n_draw, 6]; with
+    release_range [r1-r0, ...]); with snapshot_every also the float32
+    snapshots [n_snap, len(ts)-1, n_draw, 2, 6].
     """
     _core.check_solver(solver)
     ts_h = host64(ts).reshape(-1)
@@ -106,6 +110,18 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
     cfg.snap_stride = int(snapshot_every or 0)
     snaps = None
     stream_ics = ics[:n_rel].reshape(N, 6).contiguous()
+    if release_range is not None:
+        r0, r1 = (int(v) for v in release_range)
+        if not 0 <= r0 <= r1 <= n_rel:
+            raise ValueError("release_range must lie within [0, len(ts) - 1]")
+        if snapshot_every or out != "device":
+            raise NotImplementedError("release_range runs return final states on the device only")
+        cfg.first_particle, cfg.n_particles = r0 * ppr, (r1 - r0) * ppr
+        stream_ics = stream_ics[r0 * ppr:r1 * ppr].contiguous()
+        n_rel = r1 - r0
+        if n_rel == 0:
+            empty = torch.empty((0, n_draw, 6) if n_draw > 1 else (0, 6), dtype=torch.float64, device=ws.device)
+            return (empty, empty.clone()) + ((ics, ws) if return_ics else ())
     if precision == "mlp" and (integ is not pot_base or force_surrogate is None):
         raise NotImplementedError("precision='mlp' integrates in the surrogate alone: give force_surrogate and no "
                                   "prog_pot / pot_pert")
@@ -163,6 +179,7 @@ def _tail_phase(integ, cfg, final, status, t_last, t_end, h, precision, force_su
     cfg2.n_particles = cfg.n_particles
     cfg2.particles_per_release, cfg2.steps_per_release = max(int(cfg.n_particles), 1), 0
     cfg2.stream_particles, cfg2.subhalos_per_stream = cfg.stream_particles, cfg.subhalos_per_stream
+    cfg2.first_particle = cfg.first_particle  # the same global particles (subhalo rows of an ensemble)
     final2, status2 = _core.stream(integ._desc(), cfg2, final.contiguous(), precision, mlp=force_surrogate)
     return final2, torch.maximum(status, status2)
 

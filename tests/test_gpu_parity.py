@@ -655,3 +655,20 @@ def test_interp_response_equals_otf_for_several_batches(ss, oracle, precision):
     out_i = f_i.term(ts[-1], d, {"idx": 10, "tail_bool": True})
     out_o = f_o.term(ts[-1], [lo[10], d])[1]
     assert rel_err(np64(out_i), np64(out_o)) < 1e-12
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32k"])
+def test_release_range_equals_whole_stream(ss, oracle, precision):
+    """One rank's share of a stream split across GPUs (gen_stream(release_range=),
+    the ranges of sharding.balanced_ranges) equals the same releases of the
+    whole stream, bit for bit."""
+    from streamsculptor_gb300.sharding import balanced_ranges
+    from streamsculptor_gb300.streamhelpers import gen_stream
+    n = 300
+    _, back, ts, normals = _c1_setup(oracle, n_rel=n)
+    pot = mw3_gpu(ss)
+    lead, trail = gen_stream(pot, ts, back, 2e4, normals=normals, precision=precision)
+    for p0, p1 in balanced_ranges(2 * n, 2, 1, n, 3):
+        r0, r1 = p0 // 2, p1 // 2
+        l, t = gen_stream(pot, ts, back, 2e4, normals=normals, precision=precision, release_range=(r0, r1))
+        assert torch.equal(l, lead[r0:r1]) and torch.equal(t, trail[r0:r1])
