@@ -110,6 +110,45 @@ class SphericalHarmonicExpansionPotential(Potential):
         return Flat([(_abi.SS_SH_EXPANSION, _abi.SS_CENTER_ORIGIN, (_f(self.scale),))], expansion=self._table)
 
 
+class get_potential_from_density(Potential):
+    """Spherical potential tabulated from a density profile
+    (potential.py:504-552): Phi(r_k) = -4 pi G (int_0^r rho r'^2 dr' / r +
+    int_r^inf rho r' dr') on r_grid (default logspace(-3, 3, 128)), by
+    adaptive quadrature on the host (the reference uses quadgk), then a cubic
+    spline in ln r with the knot derivatives of interpax's 'cubic' rule.  The
+    kernels evaluate it as a single-term (l_max = 0) spherical-harmonic
+    expansion.  density_func is a Python callable of r (numpy scalars);
+    r_grid must be log-spaced.  Outside r_grid the spline continues linearly
+    in ln r (the reference's interpolant returns NaN there)."""
+
+    def __init__(self, density_func, r_grid=None, units=None):
+        from scipy import integrate
+        super().__init__(units, {"density_func": density_func, "r_grid": r_grid})
+        r = np.logspace(-3, 3, 128) if r_grid is None else np.asarray(host64(r_grid), dtype=np.float64)
+        u = np.log(r)
+        du = np.diff(u)
+        if len(r) < 2 or not np.allclose(du, du[0], rtol=1e-9, atol=0) or du[0] <= 0:
+            raise NotImplementedError("r_grid must be log-spaced and increasing")
+        self.r_grid = r
+        G = self._G
+        f = lambda x, k: float(density_func(x)) * x ** k  # noqa: E731
+        phi = np.empty_like(r)
+        for i, ri in enumerate(r):
+            inner = integrate.quad(f, 0.0, ri, args=(2,), epsabs=0, epsrel=1e-12, limit=200)[0]
+            outer = integrate.quad(f, ri, np.inf, args=(1,), epsabs=0, epsrel=1e-12, limit=200)[0]
+            phi[i] = -4 * np.pi * G * (inner / ri + outer)
+        self.phi_grid = phi
+        coef = np.stack([phi, _cubic_knot_slopes(phi, du[0])], axis=1)[:, None, :]
+        self._spline = SphericalHarmonicExpansionPotential(coef, u[0], du[0], units=self.units)
+
+    def _flatten(self):
+        return self._spline._flatten()
+
+    def density(self, xyz, t):
+        x = np.asarray(host64(xyz), dtype=np.float64).reshape(-1, 3)
+        return np.array([float(self.density_func(v)) for v in np.linalg.norm(x, axis=1)])
+
+
 def _nfw_phi_and_rderiv(r, GM, rs):
     """NFW potential and r dPhi/dr (= dPhi/d ln r)."""
     L = np.log1p(r / rs)
@@ -561,4 +600,5 @@ __all__ = ["MiyamotoNagaiDisk", "NFWPotential", "TriaxialNFWPotential", "Isochro
            "DehnenBarPotential", "UniformAcceleration", "MW_LMC_Potential", "TNFWSubhaloLinePotential",
            "tnfw_enclosed_mass", "nfw_params_from_infall", "tidally_evolved_nfw_params_from_infall",
            "make_tnfw_potential_from_density_profile", "make_tnfw_potential_from_infall",
+           "get_potential_from_density",
            "SubhaloLinePotential_Custom", "CustomPotential", "CenterTrack", "usys"]

@@ -175,3 +175,31 @@ def test_tnfw_subhalos_eval_and_streams(ss, oracle):
     assert rel_err(d, po[0]) <= 1e-9
     with pytest.raises(_abi.SSError):
         perturbative.GenerateMassRadiusPerturbation(mw3_gpu(ss), pot, pot, bsm)  # no scale-radius response
+
+
+def test_potential_from_density_gpu(ss, oracle):
+    """The tabulated spherical potential on the GPU: its force against the
+    analytic Plummer force (spline accuracy) and a stream through it against
+    the oracle's evaluation of the same spline (FP64 <= 1e-10)."""
+    from streamsculptor_gb300 import _core, potential as P
+    M, a = 8e11, 20.0
+    rho = lambda r: 3 * M / (4 * np.pi * a ** 3) * (1 + r * r / (a * a)) ** -2.5  # noqa: E731
+    pot = P.get_potential_from_density(rho, units=ss.usys)
+    G = _core.G_for(ss.usys)
+    x = np.random.default_rng(2).normal(0, 10, (200, 3))
+    r = np.linalg.norm(x, axis=1, keepdims=True)
+    g_exact = G * M * x / (r * r + a * a) ** 1.5
+    assert rel_err(np64(pot.gradient(x, 0.0)), g_exact) < 1e-4
+    sp = pot._spline
+    orc = oracle.HostModel([(_abi.SS_SH_EXPANSION, 0, (1.0,))],
+                           expansion=(0, sp.log_r0, sp.dlog_r, sp.coef.cpu().numpy()))
+    n = 200
+    back = oracle.orbit(orc, PROG_WF, 0.0, -1.0, n, n)[0, -1]
+    ts = -n + np.arange(n + 1) * 1.0
+    normals = np.random.default_rng(3).standard_normal((n + 1, 1, 4))
+    ws = oracle.orbit(orc, back, ts[0], 1.0, n, 1)[0]
+    ics, _ = oracle.release(orc, ws, ts, 2e4, normals)
+    final, _, _ = oracle.stream(orc, ts[0], 1.0, n, ics[:-1].reshape(-1, 6), 2, 1)
+    lead, trail = pot.gen_stream_vmapped(ts=ts, prog_w0=back, Msat=2e4, normals=normals)
+    final = final.reshape(n, 2, 6)
+    assert phase_err(np64(lead), final[:, 0]) <= 1e-10 and phase_err(np64(trail), final[:, 1]) <= 1e-10

@@ -57,3 +57,16 @@ def test_oracle_grid_spline(oracle):
     _, gm, _, _ = oracle.subhalo_eval(m, np.stack([rm, 0 * rm, 0 * rm], 1), 0.0)
     M = P.tnfw_enclosed_mass(rm, pot.rhos[0], pot.rs[0], pot.ft[0], pot.rt[0])
     assert np.allclose(gm[:, 0, 0], G * M / rm ** 2, rtol=2e-3)
+
+
+def test_potential_from_density_grid():
+    """get_potential_from_density (potential.py:504-552) for a Plummer
+    density reproduces the Plummer potential at its knots."""
+    from streamsculptor_gb300 import _core, potential as P
+    M, a = 1e10, 2.0
+    rho = lambda r: 3 * M / (4 * np.pi * a ** 3) * (1 + r * r / (a * a)) ** -2.5  # noqa: E731
+    pot = P.get_potential_from_density(rho, units=_core.usys)
+    G = _core.G_for(_core.usys)
+    r = pot.r_grid
+    assert np.allclose(pot.phi_grid, -G * M / np.sqrt(r * r + a * a), rtol=1e-12, atol=0)
+    assert pot.density(np.array([[1.0, 0, 0]]), 0.0)[0] == pytest.approx(rho(1.0))
