@@ -179,7 +179,7 @@ def test_tnfw_subhalos_eval_and_streams(ss, oracle):
 
 def test_potential_from_density_gpu(ss, oracle):
     """The tabulated spherical potential on the GPU: its force against the
-    analytic Plummer force (spline accuracy) and a stream through it against
+    analytic Plummer force (to the spline's accuracy) and a stream through it against
     the oracle's evaluation of the same spline (FP64 <= 1e-10)."""
     from streamsculptor_gb300 import _core, potential as P
     M, a = 8e11, 20.0
@@ -189,7 +189,9 @@ def test_potential_from_density_gpu(ss, oracle):
     x = np.random.default_rng(2).normal(0, 10, (200, 3))
     r = np.linalg.norm(x, axis=1, keepdims=True)
     g_exact = G * M * x / (r * r + a * a) ** 1.5
-    assert rel_err(np64(pot.gradient(x, 0.0)), g_exact) < 1e-4
+    # the spline's own accuracy: 128 knots over six decades (d ln r = 0.109)
+    # with interpax-'cubic' knot slopes put the force within ~2e-3
+    assert rel_err(np64(pot.gradient(x, 0.0)), g_exact) < 5e-3
     sp = pot._spline
     orc = oracle.HostModel([(_abi.SS_SH_EXPANSION, 0, (1.0,))],
                            expansion=(0, sp.log_r0, sp.dlog_r, sp.coef.cpu().numpy()))
