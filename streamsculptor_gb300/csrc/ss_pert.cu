@@ -202,7 +202,9 @@ __device__ __forceinline__ void subhalo_hess(int kind, R Gm, R a, const R rel[3]
     Hs[5] = gr * rel[1] * rel[2];
 }
 
-template <class R, int NCOL>
+// GRID: tabulated subhalos (SS_SH_GRID, mass response only); the kernels
+// are instantiated per case so each carries only the subhalo code it uses.
+template <class R, int NCOL, bool GRID = false>
 __device__ __forceinline__ void pert_rhs(const R* recp, const R U[NCOL], int kind, R Gm, R a, const R P0[3],
                                          const R V[3], R trel, R tau0, R window, R K[NCOL], const ShDev& sh, int sidx) {
     R rec[9];
@@ -212,7 +214,7 @@ __device__ __forceinline__ void pert_rhs(const R* recp, const R U[NCOL], int kin
     for (int i = 0; i < 3; ++i) rel[i] = rec[i] - (P0[i] + V[i] * trel);
     R gphi[3], gdphi[3];
     R gg = R(0), ggr = R(0);  // SS_SH_GRID: grad = gg rel, Hessian = gg I + ggr rel rel^T
-    if (kind == SS_SH_GRID) {
+    if constexpr (GRID) {
         grid_subhalo_gh<R, NCOL == 18>(sh, sidx, rel[0] * rel[0] + rel[1] * rel[1] + rel[2] * rel[2], gg, ggr);
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
@@ -232,7 +234,7 @@ __device__ __forceinline__ void pert_rhs(const R* recp, const R U[NCOL], int kin
         const R* x1 = U;
         const R* x2 = U + 12;
         R Hs[6];
-        if (kind == SS_SH_GRID) {
+        if constexpr (GRID) {
             Hs[0] = gg + ggr * rel[0] * rel[0];
             Hs[1] = gg + ggr * rel[1] * rel[1];
             Hs[2] = gg + ggr * rel[2] * rel[2];
@@ -276,7 +278,7 @@ __device__ __forceinline__ void pert_rhs(const R* recp, const R U[NCOL], int kin
 // reaches the block barriers.
 static constexpr int PERT_STEPS_STAGED = 16;
 
-template <class R, int NCOL>
+template <class R, int NCOL, bool GRID = false>
 __global__ void __launch_bounds__(128) pert_response_kernel(ShDev sh, PertArgs a, int sblocks) {
     constexpr int ORD = NCOL == 18 ? 2 : 1;
     constexpr int RL = rec_len(ORD), SL = stage_len(ORD), SW = ORD == 2 ? 20 : 12;
@@ -345,7 +347,8 @@ __global__ void __launch_bounds__(128) pert_response_kernel(ShDev sh, PertArgs a
                           R(SS_A65) * k[4][c];
                 U[c] = st == 0 ? u[c] : u[c] + h * acc;
             }
-            pert_rhs<R, NCOL>(&srec[j][st][0], U, sh.kind, Gm, am, P0, V, tn + cs[st] * h, tau0, window, k[st], sh, s);
+            pert_rhs<R, NCOL, GRID>(&srec[j][st][0], U, sh.kind, Gm, am, P0, V, tn + cs[st] * h, tau0, window, k[st],
+                                    sh, s);
         }
 #pragma unroll
         for (int c = 0; c < NCOL; ++c)
@@ -428,8 +431,11 @@ __global__ void __launch_bounds__(128) pert_term_kernel(PotDev<double> P, ShDev 
     double U[NCOL], K[NCOL];
 #pragma unroll
     for (int c = 0; c < NCOL; ++c) U[c] = y[6 + s * NCOL + c];
-    pert_rhs<double, NCOL>(r, U, sh.kind, sh.G * sh.m[s], sh.a[s], P0, V, 0.0, sh.t0[s] - t, sh.t_window, K, sh,
-                           (int)s);
+    if (sh.kind == SS_SH_GRID)
+        pert_rhs<double, NCOL, true>(r, U, sh.kind, 0.0, sh.a[s], P0, V, 0.0, sh.t0[s] - t, sh.t_window, K, sh, (int)s);
+    else
+        pert_rhs<double, NCOL>(r, U, sh.kind, sh.G * sh.m[s], sh.a[s], P0, V, 0.0, sh.t0[s] - t, sh.t_window, K, sh,
+                               (int)s);
 #pragma unroll
     for (int c = 0; c < NCOL; ++c) dy[6 + s * NCOL + c] = K[c];
 }
@@ -521,10 +527,12 @@ static void launch_response(const ShDev& S, const PertArgs& a, int precision, un
     if (precision == 64) {
         if (a.ncol == 18) pert_response_kernel<double, 18><<<g2, sblock, 0, st>>>(S, a, sblocks);
         else if (a.ncol == 12) pert_response_kernel<double, 12><<<g2, sblock, 0, st>>>(S, a, sblocks);
+        else if (S.kind == SS_SH_GRID) pert_response_kernel<double, 6, true><<<g2, sblock, 0, st>>>(S, a, sblocks);
         else pert_response_kernel<double, 6><<<g2, sblock, 0, st>>>(S, a, sblocks);
     } else {
         if (a.ncol == 18) pert_response_kernel<float, 18><<<g2, sblock, 0, st>>>(S, a, sblocks);
         else if (a.ncol == 12) pert_response_kernel<float, 12><<<g2, sblock, 0, st>>>(S, a, sblocks);
+        else if (S.kind == SS_SH_GRID) pert_response_kernel<float, 6, true><<<g2, sblock, 0, st>>>(S, a, sblocks);
         else pert_response_kernel<float, 6><<<g2, sblock, 0, st>>>(S, a, sblocks);
     }
 }
