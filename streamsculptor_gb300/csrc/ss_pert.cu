@@ -202,10 +202,12 @@ __device__ __forceinline__ void subhalo_hess(int kind, R Gm, R a, const R rel[3]
     Hs[5] = gr * rel[1] * rel[2];
 }
 
-// GRID: tabulated subhalos (SS_SH_GRID, mass response only); the kernels
-// are instantiated per case so each carries only the subhalo code it uses.
-template <class R, int NCOL, bool GRID = false>
-__device__ __forceinline__ void pert_rhs(const R* recp, const R U[NCOL], int kind, R Gm, R a, const R P0[3],
+// SHK: the subhalo kind, known at compile time (SS_SH_PLUMMER,
+// SS_SH_HERNQUIST, or SS_SH_GRID for tabulated subhalos, mass response
+// only); the kernels are instantiated per kind so each carries only the
+// subhalo code it uses.
+template <class R, int NCOL, int SHK>
+__device__ __forceinline__ void pert_rhs(const R* recp, const R U[NCOL], int, R Gm, R a, const R P0[3],
                                          const R V[3], R trel, R tau0, R window, R K[NCOL], const ShDev& sh, int sidx) {
     R rec[9];
     load_stage(recp, rec);
@@ -214,7 +216,7 @@ __device__ __forceinline__ void pert_rhs(const R* recp, const R U[NCOL], int kin
     for (int i = 0; i < 3; ++i) rel[i] = rec[i] - (P0[i] + V[i] * trel);
     R gphi[3], gdphi[3];
     R gg = R(0), ggr = R(0);  // SS_SH_GRID: grad = gg rel, Hessian = gg I + ggr rel rel^T
-    if constexpr (GRID) {
+    if constexpr (SHK == SS_SH_GRID) {
         grid_subhalo_gh<R, NCOL == 18>(sh, sidx, rel[0] * rel[0] + rel[1] * rel[1] + rel[2] * rel[2], gg, ggr);
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
@@ -222,7 +224,7 @@ __device__ __forceinline__ void pert_rhs(const R* recp, const R U[NCOL], int kin
             gdphi[i] = R(0);
         }
     } else {
-        subhalo_grad<R, NCOL >= 12>(kind, Gm, a, rel, gphi, gdphi);
+        subhalo_grad<R, NCOL >= 12>(SHK, Gm, a, rel, gphi, gdphi);
     }
     // window: |t - t0_s| < t_window
     R on = fabs(trel - tau0) < window ? R(1) : R(0);
@@ -234,7 +236,7 @@ __device__ __forceinline__ void pert_rhs(const R* recp, const R U[NCOL], int kin
         const R* x1 = U;
         const R* x2 = U + 12;
         R Hs[6];
-        if constexpr (GRID) {
+        if constexpr (SHK == SS_SH_GRID) {
             Hs[0] = gg + ggr * rel[0] * rel[0];
             Hs[1] = gg + ggr * rel[1] * rel[1];
             Hs[2] = gg + ggr * rel[2] * rel[2];
@@ -242,7 +244,7 @@ __device__ __forceinline__ void pert_rhs(const R* recp, const R U[NCOL], int kin
             Hs[4] = ggr * rel[0] * rel[2];
             Hs[5] = ggr * rel[1] * rel[2];
         } else {
-            subhalo_hess<R>(kind, Gm, a, rel, Hs);
+            subhalo_hess<R>(SHK, Gm, a, rel, Hs);
         }
         const R x0s = x1[0] * x1[0], x1s = x1[1] * x1[1], x2s = x1[2] * x1[2];
         const R x01 = x1[0] * x1[1], x02 = x1[0] * x1[2], x12 = x1[1] * x1[2];
@@ -278,7 +280,7 @@ __device__ __forceinline__ void pert_rhs(const R* recp, const R U[NCOL], int kin
 // reaches the block barriers.
 static constexpr int PERT_STEPS_STAGED = 16;
 
-template <class R, int NCOL, bool GRID = false>
+template <class R, int NCOL, int SHK>
 __global__ void __launch_bounds__(128) pert_response_kernel(ShDev sh, PertArgs a, int sblocks) {
     constexpr int ORD = NCOL == 18 ? 2 : 1;
     constexpr int RL = rec_len(ORD), SL = stage_len(ORD), SW = ORD == 2 ? 20 : 12;
@@ -347,8 +349,8 @@ __global__ void __launch_bounds__(128) pert_response_kernel(ShDev sh, PertArgs a
                           R(SS_A65) * k[4][c];
                 U[c] = st == 0 ? u[c] : u[c] + h * acc;
             }
-            pert_rhs<R, NCOL, GRID>(&srec[j][st][0], U, sh.kind, Gm, am, P0, V, tn + cs[st] * h, tau0, window, k[st],
-                                    sh, s);
+            pert_rhs<R, NCOL, SHK>(&srec[j][st][0], U, sh.kind, Gm, am, P0, V, tn + cs[st] * h, tau0, window, k[st],
+                                   sh, s);
         }
 #pragma unroll
         for (int c = 0; c < NCOL; ++c)
@@ -431,11 +433,16 @@ __global__ void __launch_bounds__(128) pert_term_kernel(PotDev<double> P, ShDev 
     double U[NCOL], K[NCOL];
 #pragma unroll
     for (int c = 0; c < NCOL; ++c) U[c] = y[6 + s * NCOL + c];
+    const double Gm = sh.kind == SS_SH_GRID ? 0.0 : sh.G * sh.m[s];
     if (sh.kind == SS_SH_GRID)
-        pert_rhs<double, NCOL, true>(r, U, sh.kind, 0.0, sh.a[s], P0, V, 0.0, sh.t0[s] - t, sh.t_window, K, sh, (int)s);
+        pert_rhs<double, NCOL, SS_SH_GRID>(r, U, sh.kind, Gm, sh.a[s], P0, V, 0.0, sh.t0[s] - t, sh.t_window, K, sh,
+                                           (int)s);
+    else if (sh.kind == SS_SH_PLUMMER)
+        pert_rhs<double, NCOL, SS_SH_PLUMMER>(r, U, sh.kind, Gm, sh.a[s], P0, V, 0.0, sh.t0[s] - t, sh.t_window, K,
+                                              sh, (int)s);
     else
-        pert_rhs<double, NCOL>(r, U, sh.kind, sh.G * sh.m[s], sh.a[s], P0, V, 0.0, sh.t0[s] - t, sh.t_window, K, sh,
-                               (int)s);
+        pert_rhs<double, NCOL, SS_SH_HERNQUIST>(r, U, sh.kind, Gm, sh.a[s], P0, V, 0.0, sh.t0[s] - t, sh.t_window, K,
+                                                sh, (int)s);
 #pragma unroll
     for (int c = 0; c < NCOL; ++c) dy[6 + s * NCOL + c] = K[c];
 }
@@ -522,19 +529,32 @@ static int pert_args(const ss_pert_cfg* cfg, int precision, PertArgs* a) {
 
 // response kernels over [0, N) in grid-sized chunks; a.table = the records of particle 0
 // response kernel for the run's precision and column count
+extern "C++" {
+template <class R, int SHK>
+static void launch_response_kind(const ShDev& S, const PertArgs& a, unsigned g2, int sblock, int sblocks,
+                                 cudaStream_t st) {
+    if constexpr (SHK == SS_SH_GRID) {
+        pert_response_kernel<R, 6, SHK><<<g2, sblock, 0, st>>>(S, a, sblocks);  // mass response only
+    } else {
+        if (a.ncol == 18) pert_response_kernel<R, 18, SHK><<<g2, sblock, 0, st>>>(S, a, sblocks);
+        else if (a.ncol == 12) pert_response_kernel<R, 12, SHK><<<g2, sblock, 0, st>>>(S, a, sblocks);
+        else pert_response_kernel<R, 6, SHK><<<g2, sblock, 0, st>>>(S, a, sblocks);
+    }
+}
+
+template <class R>
+static void launch_response_r(const ShDev& S, const PertArgs& a, unsigned g2, int sblock, int sblocks,
+                              cudaStream_t st) {
+    if (S.kind == SS_SH_GRID) launch_response_kind<R, SS_SH_GRID>(S, a, g2, sblock, sblocks, st);
+    else if (S.kind == SS_SH_PLUMMER) launch_response_kind<R, SS_SH_PLUMMER>(S, a, g2, sblock, sblocks, st);
+    else launch_response_kind<R, SS_SH_HERNQUIST>(S, a, g2, sblock, sblocks, st);
+}
+}  // extern "C++"
+
 static void launch_response(const ShDev& S, const PertArgs& a, int precision, unsigned g2, int sblock, int sblocks,
                             cudaStream_t st) {
-    if (precision == 64) {
-        if (a.ncol == 18) pert_response_kernel<double, 18><<<g2, sblock, 0, st>>>(S, a, sblocks);
-        else if (a.ncol == 12) pert_response_kernel<double, 12><<<g2, sblock, 0, st>>>(S, a, sblocks);
-        else if (S.kind == SS_SH_GRID) pert_response_kernel<double, 6, true><<<g2, sblock, 0, st>>>(S, a, sblocks);
-        else pert_response_kernel<double, 6><<<g2, sblock, 0, st>>>(S, a, sblocks);
-    } else {
-        if (a.ncol == 18) pert_response_kernel<float, 18><<<g2, sblock, 0, st>>>(S, a, sblocks);
-        else if (a.ncol == 12) pert_response_kernel<float, 12><<<g2, sblock, 0, st>>>(S, a, sblocks);
-        else if (S.kind == SS_SH_GRID) pert_response_kernel<float, 6, true><<<g2, sblock, 0, st>>>(S, a, sblocks);
-        else pert_response_kernel<float, 6><<<g2, sblock, 0, st>>>(S, a, sblocks);
-    }
+    if (precision == 64) launch_response_r<double>(S, a, g2, sblock, sblocks, st);
+    else launch_response_r<float>(S, a, g2, sblock, sblocks, st);
 }
 
 static void launch_base(const PotDev<double>& P, const PertArgs& a, int precision, unsigned g1, cudaStream_t st) {
