@@ -374,7 +374,8 @@ def gpu_arm(args, wl):
         "frac_err_above_1e-5_growth_le_1e3": float(((e > 1e-5) & regular).double().mean())}
     del l32, t32, l64, t64, a, b, bp, b0, ic0, icp
 
-    # --- roofline of the dominant kernel (stream_f32k_kernel)
+    # --- roofline of the dominant kernel (stream_f32k2_kernel: two particles
+    # per thread in packed f32x2 lanes)
     flat = P.Potential_Combine([pot] + ([P.TimeDepTranslatingPotential(prog, _core.CenterTrack(0.0, 1.0, wf_d.reshape(2, 3)))]
                                         if prog is not None else []), units=u)._flatten()
     w32 = roofline.particle_step_work(flat, "f32k")
@@ -411,7 +412,7 @@ def gpu_arm(args, wl):
                       "clocks": r64["clocks"], "roofline": roof(r64, w64, p64, "stream_f64_kernel")},
               "speedup_f32k_vs_f64": value / value64,
               "error_vs_f64": err,
-              "roofline": roof(r32, w32, p32, "stream_f32k_kernel"),
+              "roofline": roof(r32, w32, p32, "stream_f32k2_kernel"),
               "cpu_baseline": cpu,
               "e2e": {"value": world * work / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                       "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,

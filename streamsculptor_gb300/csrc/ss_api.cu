@@ -29,6 +29,18 @@ int set_error(int code, const char* fmt, ...) {
 
 const char* last_error() { return g_err; }
 
+// (v - R(v)) / R(v) in R: the relative rounding error of storing v as R
+// (0 when R is double).
+template <class R>
+static R rel_residual(double v) {
+    if constexpr (std::is_same<R, double>::value) {
+        return R(0);
+    } else {
+        const double r = (double)R(v);
+        return r != 0.0 ? R((v - r) / r) : R(0);
+    }
+}
+
 template <class R>
 int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalos) {
     SS_CHECK_ARG(in != nullptr, "potential is NULL");
@@ -50,10 +62,19 @@ int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalo
         d.center = c.center;
         need_track |= (c.center == SS_CENTER_TRACK);
         for (int i = 0; i < 6; ++i) SS_CHECK_ARG(std::isfinite(p[i]), "component %d: non-finite parameter p[%d]", k, i);
+        // FP32 only: slot 5 of the spherical and disk kinds holds the relative
+        // rounding of q[0] = G m, (G m - q[0]) / q[0], and slot 4 of NFW that
+        // of q[2] = 1 / r_s, so that a kernel can restore them to FP64
+        // accuracy with one FMA each (a fixed relative error in a
+        // component's mass biases every orbit the same way); zero in FP64
+        if (c.kind == SS_NFW || c.kind == SS_MIYAMOTO_NAGAI || c.kind == SS_HERNQUIST || c.kind == SS_PLUMMER ||
+            c.kind == SS_ISOCHRONE)
+            d.q[5] = rel_residual<R>(G * p[0]);
         switch (c.kind) {
             case SS_NFW:
                 SS_CHECK_ARG(p[1] > 0.0 && p[2] >= 0.0, "component %d (NFW): need r_s > 0, soft >= 0", k);
                 d.q[0] = R(G * p[0]); d.q[1] = R(p[1]); d.q[2] = R(1.0 / p[1]); d.q[3] = R(p[2]);
+                d.q[4] = rel_residual<R>(1.0 / p[1]);
                 break;
             case SS_TRIAXIAL_NFW:
                 SS_CHECK_ARG(p[1] > 0.0 && p[2] > 0.0 && p[3] > 0.0 && p[4] > 0.0,

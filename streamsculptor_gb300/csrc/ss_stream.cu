@@ -31,6 +31,7 @@
 #include <cmath>
 
 #include "ss_stream.cuh"
+#include "ss_stream2.cuh"
 
 namespace ssg {
 
@@ -269,10 +270,16 @@ int ss_stream_f32k(const ss_potential* pot, const ss_stream_cfg* cfg, const doub
         stream_f32k_kernel<GenericComp, SUB_GRID><<<grid, block, 0, s>>>(P, a);
     } else {
         dispatch_comp(P, [&](auto comp) {
-            if (a.n_sh > 0)
-                stream_f32k_kernel<decltype(comp), SUB_LINES><<<grid, block, 0, s>>>(P, a);
-            else
-                stream_f32k_kernel<decltype(comp), SUB_NONE><<<grid, block, 0, s>>>(P, a);
+            using CC = decltype(comp);
+            if (a.n_sh > 0) {
+                stream_f32k_kernel<CC, SUB_LINES><<<grid, block, 0, s>>>(P, a);
+            } else if constexpr (PairComp<CC>::ok) {
+                // two particles per thread in packed f32x2 lanes
+                const unsigned grid2 = (unsigned)(((cfg->n_particles + 1) / 2 + block - 1) / block);
+                stream_f32k2_kernel<CC><<<grid2, block, 0, s>>>(P, a);
+            } else {
+                stream_f32k_kernel<CC, SUB_NONE><<<grid, block, 0, s>>>(P, a);
+            }
             return 0;
         });
     }

@@ -672,3 +672,69 @@ def test_release_range_equals_whole_stream(ss, oracle, precision):
         r0, r1 = p0 // 2, p1 // 2
         l, t = gen_stream(pot, ts, back, 2e4, normals=normals, precision=precision, release_range=(r0, r1))
         assert torch.equal(l, lead[r0:r1]) and torch.equal(t, trail[r0:r1])
+
+
+_PAIR_MODELS = {
+    "mw3p": None,  # NFW + MN + Hernquist + the moving Plummer progenitor
+    "tri3": [("TriaxialNFWPotential", dict(m=3e11, r_s=12.0, q1=1.0, q2=0.9, q3=0.8),
+              (_abi.SS_TRIAXIAL_NFW, 0, (3e11, 12.0, 1.0, 0.9, 0.8))),
+             ("MiyamotoNagaiDisk", dict(m=6.8e10, a=3.0, b=0.28), (_abi.SS_MIYAMOTO_NAGAI, 0, (6.8e10, 3.0, 0.28))),
+             ("HernquistPotential", dict(m=5e9, r_s=1.0), (_abi.SS_HERNQUIST, 0, (5e9, 1.0, 0.0)))],
+    "gala": [("MiyamotoNagaiDisk", dict(m=6.8e10, a=3.0, b=0.28), (_abi.SS_MIYAMOTO_NAGAI, 0, (6.8e10, 3.0, 0.28))),
+             ("HernquistPotential", dict(m=5e9, r_s=1.0), (_abi.SS_HERNQUIST, 0, (5e9, 1.0, 0.0))),
+             ("HernquistPotential", dict(m=1.7e9, r_s=0.07), (_abi.SS_HERNQUIST, 0, (1.7e9, 0.07, 0.0))),
+             ("NFWPotential", dict(m=5.4e11, r_s=15.62), (_abi.SS_NFW, 0, (5.4e11, 15.62, 0.0)))],
+}
+
+
+@pytest.mark.parametrize("model,ppr,first", [("mw3p", 3, 5), ("mw3p", 8, 7), ("tri3", 5, 0), ("gala", 3, 2)])
+def test_f32k_paired_lanes_odd_layouts(ss, oracle, model, ppr, first):
+    """The FP32 stream kernel carries two particles per thread.  An odd
+    particle count per release splits a pair across two release times, an
+    odd first particle shifts every pair, and an odd particle count leaves
+    the last thread one particle: each particle still matches the oracle
+    (<= 1e-5), snapshots included (NaN rows before release)."""
+    from streamsculptor_gb300 import _core, potential as P
+    n_rel, dt, spr, stride = 60, 0.5, 3, 7
+    n_steps = n_rel * spr
+    if model == "mw3p":
+        comps, gpu = oracle.mw3(), mw3_gpu(ss)
+    else:
+        comps = [spec for _, _, spec in _PAIR_MODELS[model]]
+        gpu = P.Potential_Combine([getattr(P, name)(**kw, units=ss.usys) for name, kw, _ in _PAIR_MODELS[model]],
+                                  units=ss.usys)
+    base = oracle.HostModel(comps)
+    back = oracle.orbit(base, PROG_WF, 0.0, -dt, n_steps, n_steps)[0, -1]
+    ts = -n_steps * dt + np.arange(n_rel + 1) * spr * dt
+    ws = oracle.orbit(base, back, ts[0], dt, n_steps, spr)[0]  # the progenitor at the release times
+    orc = base
+    if model == "mw3p":
+        orc = oracle.HostModel(comps + [(_abi.SS_PLUMMER, 1, (2e4, 0.01))], track=(ts[0], spr * dt, ws[:, :3]))
+        track = ss.CenterTrack.from_samples(ts, ws[:, :3])
+        gpu = P.Potential_Combine([gpu, P.TimeDepTranslatingPotential(P.PlummerPotential(m=2e4, r_s=0.01,
+                                                                                         units=ss.usys),
+                                                                      track, units=ss.usys)], units=ss.usys)
+    rng = np.random.default_rng(17)
+    n_all = n_rel * ppr
+    scale = np.array([0.05, 0.05, 0.05, 0.005, 0.005, 0.005])
+    ics_all = np.repeat(ws[:n_rel], ppr, axis=0) + rng.normal(0, 1, (n_all, 6)) * scale
+    n = n_all - first
+    n -= 1 - n % 2  # an odd count
+    ics = ics_all[first:first + n]
+    cfg = _abi.ss_stream_cfg()
+    cfg.t0, cfg.dt, cfg.n_steps, cfg.n_particles = float(ts[0]), dt, n_steps, n
+    cfg.particles_per_release, cfg.steps_per_release, cfg.snap_stride = ppr, spr, stride
+    cfg.first_particle = first
+    snaps = torch.full((n_steps // stride, first + n, 6), 7.0, dtype=torch.float32, device="cuda")
+    final, st = _core.stream(gpu._desc(), cfg, torch.as_tensor(ics, device="cuda"), "f32k", snaps=snaps)
+    torch.cuda.synchronize()
+    final_o, snaps_o, st_o = oracle.stream(orc, ts[0], dt, n_steps, ics, ppr, spr, snap_stride=stride,
+                                           first_particle=first)
+    assert (np64(st) == 0).all() and (st_o == 0).all()
+    assert phase_err(np64(final), final_o) <= 1e-5
+    s = snaps.cpu().numpy()
+    assert (s[:, :first] == 7.0).all()  # rows of other particles untouched
+    s = s[:, first:]
+    assert np.array_equal(np.isnan(s), np.isnan(snaps_o))
+    ok = ~np.isnan(snaps_o[..., 0])
+    assert phase_err(s[ok], snaps_o[ok].astype(np.float64)) <= 1e-5 + 3e-7
