@@ -378,7 +378,7 @@ def gpu_arm(args, wl):
     # per thread in packed f32x2 lanes)
     flat = P.Potential_Combine([pot] + ([P.TimeDepTranslatingPotential(prog, _core.CenterTrack(0.0, 1.0, wf_d.reshape(2, 3)))]
                                         if prog is not None else []), units=u)._flatten()
-    w32 = roofline.particle_step_work(flat, "f32k")
+    w32 = roofline.particle_step_work(flat, "f32k2")
     w64 = roofline.particle_step_work(flat, "f64")
     p32, p64 = peak(32), peak(64)
 

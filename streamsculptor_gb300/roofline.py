@@ -24,6 +24,12 @@ Force evaluation (ss_device.cuh, comp_grad without Hessian), per component:
 Dopri5 combinations per step (6 force evaluations, FSAL reuse):
   FP64 plain          6 components x (stages 35 + update 11)            = 276
   FP32 compensated    3 x (stages 84 + position update 27 + velocity 28) = 417
+  FP32 compensated, Nystrom form (stream_f32k2_kernel, two particles per
+  thread): per coordinate, stage positions 6, stage offsets 5 + 8 + 12 + 15
+  + 24, position update 20, velocity update 20 = 110; x 3 = 330.  Its forces
+  also restore the FP32 masses (and NFW's 1 / r_s) from their rounding
+  residuals: one FMA each, 4 flops for NFW and 2 for the other spherical and
+  disk kinds per force evaluation.
 """
 from __future__ import annotations
 
@@ -39,12 +45,20 @@ FORCE_FLOPS = {
 }
 TRANSLATE_FLOPS = 3
 SUBHALO_FLOPS = (25, 1)
-RK_FLOPS = {"f64": 276, "f32k": 417}
+RK_FLOPS = {"f64": 276, "f32k": 417, "f32k2": 330}
+RESIDUAL_FLOPS = {
+    _abi.SS_NFW: 4,
+    _abi.SS_MIYAMOTO_NAGAI: 2,
+    _abi.SS_HERNQUIST: 2,
+    _abi.SS_PLUMMER: 2,
+    _abi.SS_ISOCHRONE: 2,
+}
 STAGES = 6
 
 
-def force_work(flat) -> tuple:
-    """(flops, specials) of one force evaluation of a flattened potential."""
+def force_work(flat, residuals: bool = False) -> tuple:
+    """(flops, specials) of one force evaluation of a flattened potential;
+    residuals adds the mass-residual FMAs of the packed two-particle kernel."""
     fl, sp = 0, 0
     for kind, center, _ in flat.comps:
         if kind == _abi.SS_SH_EXPANSION:
@@ -53,6 +67,8 @@ def force_work(flat) -> tuple:
         else:
             f, s = FORCE_FLOPS[kind]
         fl += f + (TRANSLATE_FLOPS if center == _abi.SS_CENTER_TRACK else 0)
+        if residuals:
+            fl += RESIDUAL_FLOPS.get(kind, 0)
         sp += s
     if flat.subhalos is not None:
         n = int(flat.subhalos.m.shape[0])
@@ -62,7 +78,9 @@ def force_work(flat) -> tuple:
 
 
 def particle_step_work(flat, precision: str) -> dict:
-    """Flops and special ops of one Dopri5 step of one particle."""
-    fl, sp = force_work(flat)
+    """Flops and special ops of one Dopri5 step of one particle: precision
+    "f64", "f32k" (scalar compensated kernel) or "f32k2" (packed two-particle
+    compensated kernel, Nystrom form)."""
+    fl, sp = force_work(flat, residuals=precision == "f32k2")
     return {"flops": STAGES * fl + RK_FLOPS[precision], "specials": STAGES * sp,
             "force_flops": fl, "force_specials": sp, "rk_flops": RK_FLOPS[precision]}
