@@ -272,6 +272,15 @@ int ss_stream_f32k(const ss_potential* pot, const ss_stream_cfg* cfg, const doub
         dispatch_comp(P, [&](auto comp) {
             using CC = decltype(comp);
             if (a.n_sh > 0) {
+                if constexpr (PairComp<CC>::ok) {
+                    // two particles per thread when a pair never straddles
+                    // two streams with different subhalo rows
+                    if (a.sh_per_grp == 0 || (a.grp % 2 == 0 && a.p_off % 2 == 0)) {
+                        const unsigned grid2 = (unsigned)(((cfg->n_particles + 1) / 2 + block - 1) / block);
+                        launch_f32k2_lines<CC>(P, a, grid2, block, s);
+                        return 0;
+                    }
+                }
                 stream_f32k_kernel<CC, SUB_LINES><<<grid, block, 0, s>>>(P, a);
             } else if constexpr (PairComp<CC>::ok) {
                 // two particles per thread in packed f32x2 lanes

@@ -19,8 +19,9 @@
 // form rounds only the combined coefficients, so the corrected masses are
 // what bring its error below the scalar kernel's.
 //
-// Used for runs without subhalos whose composition is compiled (Comp<...>)
-// from the kinds below; the others keep the scalar kernel.
+// Used for runs without subhalos or with analytic subhalo lines (Plummer,
+// Hernquist) whose composition is compiled (Comp<...>) from the kinds below;
+// the others keep the scalar kernel.
 #pragma once
 
 #include "ss_stream.cuh"
@@ -186,11 +187,45 @@ struct PairComp<Comp<KCS...>> {
     }
 };
 
+// grad Phi of the subhalo lines [shb, she) at stage time trel (time since
+// global step 0), added to g: the Plummer and Hernquist forms of
+// subhalo_grad.  Both lanes feel the same rows (the launch guarantees that a
+// pair never straddles two streams of an ensemble), so the table loads and
+// the time-window test are uniform across the pair.
+__device__ __forceinline__ void subhalo_lines2(const StreamArgs& a, const f2 X[3], float trel, int shb, int she,
+                                               f2 g[3]) {
+#pragma unroll 1
+    for (int j = shb; j < she; ++j) {
+        const float4 s0 = __ldg(a.shtab + 3 * j);
+        const float4 s1 = __ldg(a.shtab + 3 * j + 1);
+        const float4 s2 = __ldg(a.shtab + 3 * j + 2);
+        const float tau = trel - s2.x;
+        if (!(fabsf(tau) < s2.y)) continue;
+        const f2 rel[3] = {sub2(X[0], bc(s0.x + s1.x * trel)), sub2(X[1], bc(s0.y + s1.y * trel)),
+                           sub2(X[2], bc(s0.z + s1.z * trel))};
+        const f2 r2 = norm2sq(rel);
+        f2 gg;
+        if (a.sh_kind == SS_SH_PLUMMER) {
+            // G m / (r^2 + a^2)^(3/2)
+            const f2 id = rsqrt2(add2(r2, bc(s1.w * s1.w)));
+            gg = mul2(mul2(bc(s0.w), mul2(id, id)), id);
+        } else {
+            // Hernquist: G m / (r (r + a)^2)
+            const f2 r = make_float2(s_sqrt(r2.x), s_sqrt(r2.y));
+            const f2 ira = rcp2(add2(r, bc(s1.w)));
+            gg = mul2(mul2(mul2(bc(s0.w), rcp2(r)), ira), ira);
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i) g[i] = fma2(gg, rel[i], g[i]);
+    }
+}
+
 // grad Phi (not the acceleration) at the stage position xh + d; see
-// accel_f32 for the center-track difference.
-template <class C>
+// accel_f32 for the center-track difference.  SUB_LINES adds the subhalo
+// lines [shb, she) at stage time trel.
+template <class C, int SUB>
 __device__ __forceinline__ void grad2_at(const PotDev<float>& P, const StreamArgs& a, const f2 xh[3], const f2 d[3],
-                                         int slot, f2 g[3]) {
+                                         int slot, float trel, int shb, int she, f2 g[3]) {
     const f2 X[3] = {add2(xh[0], d[0]), add2(xh[1], d[1]), add2(xh[2], d[2])};
     f2 xs[3] = {X[0], X[1], X[2]};
     if (C::uses_track(P)) {
@@ -201,6 +236,7 @@ __device__ __forceinline__ void grad2_at(const PotDev<float>& P, const StreamArg
         xs[2] = add2(sub2(xh[2], bc(ch.z)), sub2(d[2], bc(cl.z)));
     }
     PairComp<C>::grad(P, X, xs, g);
+    if constexpr (SUB == SUB_LINES) subhalo_lines2(a, X, trel, shb, she, g);
 }
 
 __device__ __forceinline__ void two_sum2(f2 a, f2 b, f2& s, f2& e) {
@@ -236,23 +272,27 @@ constexpr double SS_NB5 = SS_B6 * SS_A65;
 // not yet released gets 0, which leaves its normalised state unchanged.
 // G_i = grad Phi = -A_i, NH = -H.  The stage position offset from xh is
 // D_s = xl + h (c_s vh + T_s), T_s = c_s vl + h sum_k abar_sk A_k (small).
-template <class C>
+// SUB_LINES: the pair feels the subhalo rows [shb, she) at the stage times
+// of step_f32k.
+template <class C, int SUB>
 __device__ __forceinline__ void step2_f32k(const PotDev<float>& P, const StreamArgs& a, int n, f2 H, f2 HLO,
-                                           f2 xh[3], f2 xl[3], f2 vh[3], f2 vl[3]) {
+                                           f2 xh[3], f2 xl[3], f2 vh[3], f2 vl[3], int shb, int she) {
     const f2 NH = neg2(H);
     const int s0 = 5 * n;
+    const float h = a.h_hi;
+    const float tn = (float)n * h;  // time since global step 0 (subhalo lines)
     f2 G1[3], G2[3], G3[3], G4[3], G[3], D[3];
     f2 Sv[3], Sb[3];  // sum_{i>=3} b_i (G_i - G1) and sum_k bbar_k G_k
-    grad2_at<C>(P, a, xh, xl, s0, G1);
+    grad2_at<C, SUB>(P, a, xh, xl, s0, tn, shb, she, G1);
 #pragma unroll
     for (int i = 0; i < 3; ++i) D[i] = fma2(H, fma2(bc(F_C2), vh[i], mul2(bc(F_C2), vl[i])), xl[i]);
-    grad2_at<C>(P, a, xh, D, s0 + 1, G2);
+    grad2_at<C, SUB>(P, a, xh, D, s0 + 1, tn + F_C2 * h, shb, she, G2);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         const f2 T = fma2(NH, mul2(bc(F_(SS_N31)), G1[i]), mul2(bc(F_C3), vl[i]));
         D[i] = fma2(H, fma2(bc(F_C3), vh[i], T), xl[i]);
     }
-    grad2_at<C>(P, a, xh, D, s0 + 2, G3);
+    grad2_at<C, SUB>(P, a, xh, D, s0 + 2, tn + F_C3 * h, shb, she, G3);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         Sv[i] = mul2(bc(F_(SS_B3)), sub2(G3[i], G1[i]));
@@ -260,7 +300,7 @@ __device__ __forceinline__ void step2_f32k(const PotDev<float>& P, const StreamA
         const f2 T = fma2(NH, S, mul2(bc(F_C4), vl[i]));
         D[i] = fma2(H, fma2(bc(F_C4), vh[i], T), xl[i]);
     }
-    grad2_at<C>(P, a, xh, D, s0 + 3, G4);
+    grad2_at<C, SUB>(P, a, xh, D, s0 + 3, tn + F_C4 * h, shb, she, G4);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         Sv[i] = fma2(bc(F_(SS_B4)), sub2(G4[i], G1[i]), Sv[i]);
@@ -268,7 +308,7 @@ __device__ __forceinline__ void step2_f32k(const PotDev<float>& P, const StreamA
         const f2 T = fma2(NH, S, mul2(bc(F_C5), vl[i]));
         D[i] = fma2(H, fma2(bc(F_C5), vh[i], T), xl[i]);
     }
-    grad2_at<C>(P, a, xh, D, s0 + 4, G);  // G5
+    grad2_at<C, SUB>(P, a, xh, D, s0 + 4, tn + F_C5 * h, shb, she, G);  // G5
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         Sv[i] = fma2(bc(F_(SS_B5)), sub2(G[i], G1[i]), Sv[i]);
@@ -280,7 +320,7 @@ __device__ __forceinline__ void step2_f32k(const PotDev<float>& P, const StreamA
         const f2 T = fma2(NH, S, vl[i]);  // c_6 = 1
         D[i] = fma2(H, add2(vh[i], T), xl[i]);
     }
-    grad2_at<C>(P, a, xh, D, s0 + 5, G);  // G6
+    grad2_at<C, SUB>(P, a, xh, D, s0 + 5, tn + h, shb, she, G);  // G6
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         // position: h (vh + Db), Db = vl + h sum_k bbar_k A_k
@@ -304,11 +344,19 @@ __device__ __forceinline__ void step2_f32k(const PotDev<float>& P, const StreamA
     }
 }
 
-template <class C>
+// SUB: SUB_NONE or SUB_LINES (analytic subhalo lines).  With subhalo rows
+// per stream (ensembles), the launch takes this kernel only when a pair
+// never straddles two streams: an even stream length and an even first
+// particle.
+template <class C, int SUB = SUB_NONE>
 __global__ void __launch_bounds__(128, 4) stream_f32k2_kernel(PotDev<float> P, StreamArgs a) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t p0 = 2 * t, p1 = 2 * t + 1;
     const bool v0 = p0 < a.N, v1 = p1 < a.N;
+    // subhalo rows of lane x's stream (lane y's is the same); read only by
+    // threads whose lane x is a particle
+    const int shb = a.sh_per_grp > 0 ? (int)((p0 + a.p_off) / a.grp) * a.sh_per_grp : 0;
+    const int she = a.sh_per_grp > 0 ? shb + a.sh_per_grp : a.n_sh;
     const int st0 = v0 ? stream_start(a, p0 + a.p_off) : a.n_steps;
     const int st1 = v1 ? stream_start(a, p1 + a.p_off) : a.n_steps;
     const int tstart = st0 < st1 ? st0 : st1;
@@ -341,7 +389,7 @@ __global__ void __launch_bounds__(128, 4) stream_f32k2_kernel(PotDev<float> P, S
         if (v0 && n >= tstart) {
             const f2 H = make_float2(n >= st0 ? a.h_hi : 0.0f, n >= st1 ? a.h_hi : 0.0f);
             const f2 HLO = make_float2(n >= st0 ? a.h_lo : 0.0f, n >= st1 ? a.h_lo : 0.0f);
-            step2_f32k<C>(P, a, n, H, HLO, xh, xl, vh, vl);
+            step2_f32k<C, SUB>(P, a, n, H, HLO, xh, xl, vh, vl, shb, she);
         }
         if (n + 1 == next_snap) {
             next_snap += a.stride;
@@ -382,5 +430,11 @@ __global__ void __launch_bounds__(128, 4) stream_f32k2_kernel(PotDev<float> P, S
         }
     }
 }
+
+// Launches stream_f32k2_kernel<C, SUB_LINES> (instantiated in
+// ss_stream2.cu, a translation unit of its own so that it compiles in
+// parallel with the other stream kernels).
+template <class C>
+void launch_f32k2_lines(const PotDev<float>& P, const StreamArgs& a, unsigned grid, int block, cudaStream_t s);
 
 }  // namespace ssg

@@ -738,3 +738,63 @@ def test_f32k_paired_lanes_odd_layouts(ss, oracle, model, ppr, first):
     assert np.array_equal(np.isnan(s), np.isnan(snaps_o))
     ok = ~np.isnan(snaps_o[..., 0])
     assert phase_err(s[ok], snaps_o[ok].astype(np.float64)) <= 1e-5 + 3e-7
+
+
+@pytest.mark.parametrize("kind,grp,first", [("plummer", 0, 0), ("hernquist", 0, 3), ("plummer", 60, 0),
+                                            ("hernquist", 60, 60), ("plummer", 60, 5), ("hernquist", 57, 0)])
+def test_f32k_paired_lanes_with_subhalo_lines(ss, oracle, kind, grp, first):
+    """FP32 streams through Plummer or Hernquist subhalo lines against the
+    oracle (<= 1e-5 per particle).  grp = 0: every particle feels the whole
+    table; grp > 0: an ensemble of streams of grp particles, stream b feeling
+    subhalo rows [2b, 2b + 2).  The two-particle kernel runs when a pair
+    never straddles two streams (whole table, or an even stream length and an
+    even first particle); an odd stream length or an odd first particle takes
+    the one-particle kernel, with the same answer."""
+    from streamsculptor_gb300 import _core, potential as P
+    n_rel, dt, spr, ppr = 20, 0.5, 3, 3
+    n_steps = n_rel * spr + 40
+    base = oracle.HostModel(oracle.mw3())
+    back = oracle.orbit(base, PROG_WF, 0.0, -dt, n_steps, n_steps)[0, -1]
+    t0 = -n_steps * dt
+    ws = oracle.orbit(base, back, t0, dt, n_steps, 1)[0]  # the progenitor at every step
+    rng = np.random.default_rng(23)
+    B = 3
+    n_sh = 2 * B
+    when = rng.integers(10, n_steps - 10, n_sh)
+    sh = dict(m=10 ** rng.uniform(7.0, 8.0, n_sh), a=rng.uniform(0.2, 0.6, n_sh),
+              x0=ws[when, :3] + rng.normal(0, 0.3, (n_sh, 3)), v=rng.normal(0, 0.15, (n_sh, 3)),
+              t0=t0 + when * dt, t_window=15.0)
+    if kind == "plummer":
+        pert = P.SubhaloLinePotential(sh["m"], sh["a"], sh["x0"], sh["v"], sh["t0"], sh["t_window"],
+                                      units=ss.usys)
+        okind = 1
+    else:
+        sh["m"][:] = 4e7
+        sh["a"][:] = 0.4
+        pert = P.SubhaloLinePotential_Custom(P.HernquistPotential(m=4e7, r_s=0.4, units=ss.usys), sh["x0"],
+                                             sh["v"], sh["t0"], sh["t_window"], units=ss.usys)
+        okind = 2
+    gpu = P.Potential_Combine([mw3_gpu(ss), pert], units=ss.usys)
+    orc = oracle.HostModel(oracle.mw3(), subhalos=dict(sh, kind=okind))
+    n_all = B * grp if grp else n_rel * ppr
+    rel = (np.arange(n_all) % (grp or n_all)) // ppr  # release index of each particle in its stream
+    scale = np.array([0.05, 0.05, 0.05, 0.005, 0.005, 0.005])
+    ics_all = ws[rel * spr] + rng.normal(0, 1, (n_all, 6)) * scale
+    n = n_all - first
+    ics = ics_all[first:]
+    cfg = _abi.ss_stream_cfg()
+    cfg.t0, cfg.dt, cfg.n_steps, cfg.n_particles = t0, dt, n_steps, n
+    cfg.particles_per_release, cfg.steps_per_release = ppr, spr
+    cfg.first_particle = first
+    if grp:
+        cfg.stream_particles, cfg.subhalos_per_stream = grp, 2
+    final, st = _core.stream(gpu._desc(), cfg, torch.as_tensor(ics, device="cuda"), "f32k")
+    torch.cuda.synchronize()
+    final_o, _, st_o = oracle.stream(orc, t0, dt, n_steps, ics, ppr, spr, stream_particles=grp if grp else 0,
+                                     subhalos_per_stream=2 if grp else 0, first_particle=first)
+    assert (np64(st) == 0).all() and (st_o == 0).all()
+    # the subhalos move the particles: the comparison is not of unperturbed tracks
+    free, _, _ = oracle.stream(base, t0, dt, n_steps, ics, ppr, spr, stream_particles=grp if grp else 0,
+                               first_particle=first)
+    assert phase_err(free, final_o) > 1e-4
+    assert phase_err(np64(final), final_o) <= 1e-5
