@@ -9,7 +9,8 @@
 // TimeDepTranslatingPotential on a cubic spline of the progenitor orbit);
 // gen_stream_vmapped_with_pert (streamhelpers.py:89-146) adds subhalos.
 //
-// Layout: one thread per particle; particles are ordered by release (release
+// Layout: one thread per particle (two for stream_f32k2_kernel, ss_stream2.cuh,
+// the FP32 form for compiled compositions); particles are ordered by release (release
 // r owns particles [r*ppr, (r+1)*ppr)), so the earliest (longest) particles
 // sit in the lowest blocks and are scheduled first.  A warp runs in global
 // lock-step from its earliest start step: lanes released later idle until
