@@ -59,6 +59,37 @@ def test_nfw_golden_through_gpu(ss):
     assert np.all(np.abs(out - printed) <= 5e-9)
 
 
+def test_notebook_pins_through_gpu(ss):
+    """The reference notebooks' printed values through the public API on the
+    GPU (the same pins as the oracle's, tests/test_oracle.py): the Gala Milky
+    Way orbit of examples/StreamSubhaloExample.ipynb cell 1 (fixed dt = 0.5
+    Myr; the notebook's ts spacing of 3.5 Myr would be a coarse fixed step),
+    its Plummer and Hernquist subhalo lines (cell 9) and the Zhao
+    density-derived potential of examples/potential_from_1D_Density.ipynb
+    (cells 7-8)."""
+    from streamsculptor_gb300 import potential as P
+
+    from .test_oracle import GALA_IC_PRINTED, GALA_W_TODAY, SH_PHI_PRINTED, sh_example_table, zhao_density
+    u = ss.usys
+    sol = P.GalaMilkyWayPotential(units=u).integrate_orbit(w0=GALA_W_TODAY, ts=np.array([0.0, -3500.0]), t0=0.0,
+                                                           t1=-3500.0, dt=0.5)
+    w, ref = np64(sol.ys[-1]), GALA_IC_PRINTED
+    assert np.linalg.norm(w[:3] - ref[:3]) / np.linalg.norm(ref[:3]) <= 2e-5
+    assert np.linalg.norm(w[3:] - ref[3:]) / np.linalg.norm(ref[3:]) <= 2e-5
+    x = np.array([1.0, 2.0, 3.0])
+    t = sh_example_table(1)
+    plummer = P.SubhaloLinePotential(t["m"], t["a"], t["x0"], t["v"], t["t0"], t["t_window"], units=u)
+    hern = P.SubhaloLinePotential_Custom(P.HernquistPotential(m=1e7, r_s=0.2, units=u), t["x0"], t["v"], t["t0"],
+                                         t["t_window"], units=u)
+    for pot, kind in ((plummer, 1), (hern, 2)):
+        phi = float(np64(pot.potential(x, -850.0)).reshape(-1)[0])
+        assert abs(phi / SH_PHI_PRINTED[kind] - 1.0) <= 1e-7
+    zhao = P.get_potential_from_density(zhao_density, units=u)
+    assert abs(float(np64(zhao.potential(x, 0.0)).reshape(-1)[0]) / -0.08283585 - 1.0) <= 1e-6
+    g = np64(zhao.gradient(x, 0.0)).reshape(-1)
+    assert np.all(np.abs(g - np.array([0.0004346, 0.0008692, 0.0013038])) <= 5e-9)
+
+
 def _track_and_subhalos(ss, oracle):
     from streamsculptor_gb300 import potential as P
     rng = np.random.default_rng(11)

@@ -37,6 +37,78 @@ def test_softened_nfw_perturbation_term_golden(oracle):
     assert np.all(d1[:, 0:3] == 1.0) and np.all(d1[:, 6:9] == 1.0)
 
 
+# GalaMilkyWayPotential (potential.py:390-418): disk, bulge, nucleus, halo
+GALA_MW = [(_abi.SS_MIYAMOTO_NAGAI, 0, (6.8e10, 3.0, 0.28)), (_abi.SS_HERNQUIST, 0, (5e9, 1.0, 0.0)),
+           (_abi.SS_HERNQUIST, 0, (1.71e9, 0.07, 0.0)), (_abi.SS_NFW, 0, (5.4e11, 15.62, 0.0))]
+# examples/StreamSubhaloExample.ipynb cell 1: integrate_orbit of w_today back
+# 3500 Myr in GalaMilkyWayPotential (adaptive Dopri8, rtol = atol = 1e-7,
+# main.py:126) printed "Initial condition = [...]" to 8 digits
+GALA_W_TODAY = np.array([20.0, 0.0, 20.0, 0.0, 0.15, 0.0])
+GALA_IC_PRINTED = np.array([-7.23164146, -7.96692572, -10.81840286, 0.19182623, -0.20351324, -0.01770436])
+# cell 7 printed the impact location; cell 9 evaluated a Plummer and a
+# Hernquist subhalo (m = 1e7, r_s = 0.2) on the line through it, with the
+# velocity offset by (0.02, 0, 0.02), at x = (1, 2, 3), t = -850 Myr
+SH_W_IMPACT = np.array([-18.84511332, 4.23873108, -17.32878089, -0.04416233, -0.15074649, -0.07956093])
+SH_PHI_PRINTED = {1: -1.053815931966235e-06, 2: -1.048913077256255e-06}  # Plummer, Hernquist
+
+
+def sh_example_table(kind):
+    """The subhalo line of StreamSubhaloExample.ipynb cells 7-9."""
+    w = SH_W_IMPACT + np.array([0.0, 0.0, 0.0, 0.02, 0.0, 0.02])
+    return dict(kind=kind, m=np.array([1e7]), a=np.array([0.2]), x0=w[None, :3], v=w[None, 3:],
+                t0=np.array([-1000.0]), t_window=250.0)
+
+
+def test_gala_orbit_golden(oracle):
+    """The oracle's converged fixed-step orbit (dt = 0.5 Myr, 7000 steps)
+    against the notebook's printed state.  The residual (8e-6) is the
+    reference's own adaptive tolerance over 3.5 Gyr; a 1e-4 change in the
+    halo mass or scale radius moves the result by ~4e-3 and a 1e-5 change in
+    G by ~5e-4, so the pin fixes the potential's parameters, summation and
+    units."""
+    m = oracle.HostModel(GALA_MW)
+    w = oracle.orbit(m, GALA_W_TODAY, 0.0, -0.5, 7000, 7000)[0, -1]
+    ref = GALA_IC_PRINTED
+    assert np.linalg.norm(w[:3] - ref[:3]) / np.linalg.norm(ref[:3]) <= 2e-5
+    assert np.linalg.norm(w[3:] - ref[3:]) / np.linalg.norm(ref[3:]) <= 2e-5
+
+
+@pytest.mark.parametrize("kind", [1, 2])
+def test_subhalo_line_potential_golden(oracle, kind):
+    """Plummer and Hernquist subhalo lines (potential.py:802-850, 908-956)
+    against the notebook's printed values; the printed 8-digit impact
+    location limits the agreement to ~1e-7.  Outside the window the
+    potential is zero."""
+    m = oracle.HostModel([], subhalos=sh_example_table(kind))
+    phi = oracle.potential_eval(m, np.array([[1.0, 2.0, 3.0]]), -850.0)[0][0]
+    assert abs(phi / SH_PHI_PRINTED[kind] - 1.0) <= 1e-7
+    assert oracle.potential_eval(m, np.array([[1.0, 2.0, 3.0]]), -1300.0)[0][0] == 0.0
+
+
+def zhao_density(r, m=1e11, r_s=10.0, alpha=1.0, beta=2.5, gamma=1.0):
+    """examples/potential_from_1D_Density.ipynb cells 2-4."""
+    uu = r / r_s
+    rho0 = m / (4 * np.pi * r_s ** 3)
+    return rho0 / uu ** gamma / (1.0 + uu ** (1.0 / alpha)) ** ((beta - gamma) * alpha)
+
+
+def test_potential_from_density_golden(oracle):
+    """get_potential_from_density of the Zhao density (potential.py:504-552),
+    evaluated by the oracle from the spline the host builds, against the
+    notebook's printed potential (-0.08283585) and gradient at (1, 2, 3).
+    The spline's own error is ~2e-8 absolute and the reference's knots come
+    from quadgk at its default tolerance, so the potential is pinned to
+    1e-6 and the gradient to its printed precision (~1e-5)."""
+    from streamsculptor_gb300 import _core, potential as P
+    pot = P.get_potential_from_density(zhao_density, units=_core.usys)
+    sp = pot._spline
+    m = oracle.HostModel([(_abi.SS_SH_EXPANSION, 0, (1.0,))],
+                         expansion=(0, sp.log_r0, sp.dlog_r, sp.coef.cpu().numpy()))
+    phi, g, _ = oracle.potential_eval(m, np.array([[1.0, 2.0, 3.0]]), 0.0)
+    assert abs(phi[0] / -0.08283585 - 1.0) <= 1e-6
+    assert np.all(np.abs(g[0] - np.array([0.0004346, 0.0008692, 0.0013038])) <= 5e-9)
+
+
 def _all_kinds():
     return [
         (_abi.SS_NFW, 0, (5.4e11, 15.62, 0.0)),
