@@ -61,16 +61,24 @@ def test_nfw_golden_through_gpu(ss):
 
 def test_notebook_pins_through_gpu(ss):
     """The reference notebooks' printed values through the public API on the
-    GPU (the same pins as the oracle's, tests/test_oracle.py): the Gala Milky
-    Way orbit of examples/StreamSubhaloExample.ipynb cell 1 (fixed dt = 0.5
-    Myr; the notebook's ts spacing of 3.5 Myr would be a coarse fixed step),
-    its Plummer and Hernquist subhalo lines (cell 9) and the Zhao
-    density-derived potential of examples/potential_from_1D_Density.ipynb
-    (cells 7-8)."""
-    from streamsculptor_gb300 import potential as P
+    GPU (the same pins as the oracle's, tests/test_oracle.py): the two NFW
+    orbits of examples/tests.ipynb (cells 17 and 61, integrate_orbit and
+    integrate_field), the Gala Milky Way orbit of
+    examples/StreamSubhaloExample.ipynb cell 1 (fixed dt = 0.5 Myr; the
+    notebook's ts spacing of 3.5 Myr would be a coarse fixed step), its
+    Plummer and Hernquist subhalo lines (cell 9) and the Zhao density-derived
+    potential of examples/potential_from_1D_Density.ipynb (cells 7-8)."""
+    from streamsculptor_gb300 import fields, potential as P
 
-    from .test_oracle import GALA_IC_PRINTED, GALA_W_TODAY, SH_PHI_PRINTED, sh_example_table, zhao_density
+    from .test_oracle import (GALA_IC_PRINTED, GALA_W_TODAY, NFW_T30_PRINTED, NFW_W0_A, NFW_W0_B, SH_PHI_PRINTED,
+                              check_nfw_field_rows, sh_example_table, zhao_density)
     u = ss.usys
+    nfw = P.NFWPotential(m=1e12, r_s=20.0, units=u)
+    w = np64(nfw.integrate_orbit(w0=NFW_W0_A, ts=np.array([0.0, 30.0]), dt=0.5).ys[-1])
+    assert np.all(np.abs(w - NFW_T30_PRINTED) <= 1e-8)
+    sol = fields.integrate_field(w0=NFW_W0_B, ts=np.linspace(0, 3000, 1000), field=fields.hamiltonian_field(nfw),
+                                 dt=3000.0 / 999 / 6)
+    check_nfw_field_rows(np64(sol.ys))
     sol = P.GalaMilkyWayPotential(units=u).integrate_orbit(w0=GALA_W_TODAY, ts=np.array([0.0, -3500.0]), t0=0.0,
                                                            t1=-3500.0, dt=0.5)
     w, ref = np64(sol.ys[-1]), GALA_IC_PRINTED

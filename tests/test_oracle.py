@@ -85,6 +85,42 @@ def test_subhalo_line_potential_golden(oracle, kind):
     assert oracle.potential_eval(m, np.array([[1.0, 2.0, 3.0]]), -1300.0)[0][0] == 0.0
 
 
+# examples/tests.ipynb cell 17: NFW(1e12, 20) orbit from NFW_W0_A, dense
+# output at t = 30 Myr, printed to 8 decimals
+NFW_W0_A = np.array([20.0, 15.0, 20.0, 0.08, 0.1, -0.05])
+NFW_T30_PRINTED = np.array([21.9793661, 17.67654451, 18.10530132, 0.051923, 0.07815599, -0.07552167])
+# cell 61: integrate_field(hamiltonian_field(NFW(1e12, 20))) from NFW_W0_B
+# saved at linspace(0, 3000, 1000); rows 1, 2 and the last three printed
+NFW_W0_B = np.array([20.0, 0.0, 20.0, 0.0, 0.2, 0.0])
+NFW_FIELD_ROWS_PRINTED = {
+    1: [1.99947007e+01, 6.00547553e-01, 1.99947007e+01, -3.52920125e-03, 1.99947006e-01, -3.52920125e-03],
+    2: [1.99788050e+01, 1.20077683e+00, 1.99788050e+01, -7.05704492e-03, 1.99788029e-01, -7.05704492e-03],
+    997: [1.54653741e+01, -1.50646962e+01, 1.54653741e+01, 9.87262702e-02, 1.62473824e-01, 9.87262702e-02],
+    998: [1.57572297e+01, -1.45723635e+01, 1.57572297e+01, 9.56423786e-02, 1.65401168e-01, 9.56423786e-02],
+    999: [1.60397604e+01, -1.40714069e+01, 1.60397604e+01, 9.25163046e-02, 1.68217294e-01, 9.25163046e-02],
+}
+
+
+def check_nfw_field_rows(ys):
+    """ys [1000, 6] at the notebook's save times against its printed rows:
+    the first rows to their 9 printed digits, the rows after 3 Gyr to 5e-6
+    (the reference's adaptive tolerance; measured 1.6e-6)."""
+    for k, row in NFW_FIELD_ROWS_PRINTED.items():
+        r = np.array(row)
+        tol = 1e-8 if k < 10 else 5e-6
+        assert np.max(np.abs(ys[k] - r) / np.abs(r)) <= tol, k
+
+
+def test_nfw_orbit_and_field_golden(oracle):
+    """The two NFW orbits of examples/tests.ipynb (cells 17 and 61) on the
+    oracle's fixed-step Dopri5."""
+    m = oracle.HostModel([(_abi.SS_NFW, 0, (1e12, 20.0, 0.0))])
+    w = oracle.orbit(m, NFW_W0_A, 0.0, 0.5, 60, 60)[0, -1]
+    assert np.all(np.abs(w - NFW_T30_PRINTED) <= 1e-8)
+    h = 3000.0 / 999 / 6
+    check_nfw_field_rows(oracle.orbit(m, NFW_W0_B, 0.0, h, 999 * 6, 6)[0])
+
+
 def zhao_density(r, m=1e11, r_s=10.0, alpha=1.0, beta=2.5, gamma=1.0):
     """examples/potential_from_1D_Density.ipynb cells 2-4."""
     uu = r / r_s
