@@ -400,6 +400,15 @@ class SubhaloLinePotential_dRadius(_SubhaloLines):
         (_, _, _, gd), single = self._per_sh(xyz, t)
         return gd[0] if single else gd
 
+    def potential(self, xyz, t):
+        """Sum over the subhalos of dPhi_s/da_s (potential.py:867-884): [N]
+        for [N, 3] points, a scalar for one point."""
+        return self.potential_per_SH(xyz, t).sum(dim=-1)
+
+    def gradient(self, xyz, t):
+        """Sum over the subhalos of grad dPhi_s/da_s: [N, 3], or [3]."""
+        return self.gradient_per_SH(xyz, t).sum(dim=-2)
+
 
 class SubhaloLinePotential_Custom(_SubhaloLines):
     """One profile `pot` (PlummerPotential or HernquistPotential) for all
@@ -417,6 +426,36 @@ class SubhaloLinePotential_Custom(_SubhaloLines):
         super().__init__(units, {"pot": pot, "m": m, "a": a, "subhalo_x0": subhalo_x0, "subhalo_v": subhalo_v,
                                  "subhalo_t0": subhalo_t0, "t_window": t_window})
         self._kind = kind
+
+
+class SubhaloLinePotential_dRadius_Custom(SubhaloLinePotential_dRadius):
+    """dPhi_s/da_s from a Python callable dpot_dRadius(xyz, t)
+    (potential.py:1110-1160).  A callable cannot run in a kernel: use
+    SubhaloLinePotentialCustom_dRadius_fromFunc with PlummerPotential or
+    HernquistPotential, whose derivative the kernels evaluate in closed form."""
+
+    def __init__(self, dpot_dRadius, subhalo_x0, subhalo_v, subhalo_t0, t_window, units=None):
+        raise NotImplementedError("SubhaloLinePotential_dRadius_Custom evaluates a Python callable; use "
+                                  "SubhaloLinePotentialCustom_dRadius_fromFunc(PlummerPotential or "
+                                  "HernquistPotential, m, r_s, ...)")
+
+
+class SubhaloLinePotentialCustom_dRadius_fromFunc(SubhaloLinePotential_dRadius):
+    """dPhi_s/dr_s of subhalos on lines with the profile class `func`
+    (PlummerPotential or HernquistPotential) built from arrays m, r_s
+    (potential.py:1215-1262, jax.grad of the profile's potential with respect
+    to r_s): G m a / (r^2 + a^2)^(3/2) for Plummer, G m / (r + a)^2 for
+    Hernquist, zero outside the window.  It is the structural companion of
+    SubhaloLinePotentialCustom_fromFunc with the same arguments."""
+
+    def __init__(self, func, m, r_s, subhalo_x0, subhalo_v, subhalo_t0, t_window, units=None):
+        if func not in (PlummerPotential, HernquistPotential):
+            raise NotImplementedError("SubhaloLinePotentialCustom_dRadius_fromFunc supports PlummerPotential and "
+                                      "HernquistPotential")
+        _SubhaloLines.__init__(self, units, {"func": func, "m": m, "r_s": r_s, "a": r_s, "subhalo_x0": subhalo_x0,
+                                             "subhalo_v": subhalo_v, "subhalo_t0": subhalo_t0,
+                                             "t_window": t_window})
+        self._kind = _abi.SS_SH_PLUMMER if func is PlummerPotential else _abi.SS_SH_HERNQUIST
 
 
 class SubhaloLinePotentialCustom_fromFunc(SubhaloLinePotential_Custom):
@@ -601,4 +640,5 @@ __all__ = ["MiyamotoNagaiDisk", "NFWPotential", "TriaxialNFWPotential", "Isochro
            "tnfw_enclosed_mass", "nfw_params_from_infall", "tidally_evolved_nfw_params_from_infall",
            "make_tnfw_potential_from_density_profile", "make_tnfw_potential_from_infall",
            "get_potential_from_density",
-           "SubhaloLinePotential_Custom", "CustomPotential", "CenterTrack", "usys"]
+           "SubhaloLinePotential_Custom", "SubhaloLinePotentialCustom_fromFunc", "SubhaloLinePotential_dRadius_Custom",
+           "SubhaloLinePotentialCustom_dRadius_fromFunc", "CustomPotential", "CenterTrack", "usys"]

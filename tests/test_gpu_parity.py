@@ -837,3 +837,31 @@ def test_f32k_paired_lanes_with_subhalo_lines(ss, oracle, kind, grp, first):
                                first_particle=first)
     assert phase_err(free, final_o) > 1e-4
     assert phase_err(np64(final), final_o) <= 1e-5
+
+
+def test_structural_subhalo_classes(ss, oracle):
+    """The structural (dPhi_s/da_s) subhalo potentials: per subhalo and summed
+    (SubhaloLinePotential_dRadius.potential, potential.py:867-884) for the
+    Plummer lines, and SubhaloLinePotentialCustom_dRadius_fromFunc
+    (potential.py:1215-1262) for Plummer and Hernquist profiles, against the
+    oracle's derivatives with respect to the scale radius (forward-mode
+    autodiff of the profiles); one point gives a scalar sum."""
+    from streamsculptor_gb300 import potential as P
+    sh, _, _, _ = _pert_case(oracle)
+    x = np.random.default_rng(5).normal(0, 10, (50, 3))
+    t = 40.0
+    args = (sh["m"], sh["a"], sh["x0"], sh["v"], sh["t0"], sh["t_window"])
+    for kind, func in ((1, P.PlummerPotential), (2, P.HernquistPotential)):
+        _, _, d_o, gd_o = oracle.subhalo_eval(oracle.HostModel([], subhalos=dict(sh, kind=kind)), x, t)
+        assert (np.abs(d_o) > 0).sum() > 100  # most subhalos are inside their window at t
+        pots = [P.SubhaloLinePotentialCustom_dRadius_fromFunc(func, *args, units=ss.usys)]
+        if kind == 1:
+            pots.append(P.SubhaloLinePotential_dRadius(*args, units=ss.usys))
+        for s in pots:
+            assert rel_err(np64(s.potential_per_SH(x, t)), d_o) < 1e-12
+            assert rel_err(np64(s.gradient_per_SH(x, t)), gd_o) < 1e-12
+            assert rel_err(np64(s.potential(x, t)), d_o.sum(axis=1)) < 1e-12
+            assert rel_err(np64(s.gradient(x, t)), gd_o.sum(axis=1)) < 1e-12
+            assert float(np64(s.potential(x[0], t))) == pytest.approx(float(d_o[0].sum()), rel=1e-12)
+    with pytest.raises(NotImplementedError):
+        P.SubhaloLinePotential_dRadius_Custom(lambda xyz, t: 0.0, *args[2:], units=ss.usys)
