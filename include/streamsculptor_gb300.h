@@ -333,14 +333,21 @@ int ss_stream_f32k(const ss_potential* pot, const ss_stream_cfg* cfg, const doub
  * whose device memory belongs to another allocator.  This entry point takes
  * the same inputs and outputs as ss_stream_f32k (still caller-provided) and
  * keeps its scratch in a fixed 4 MiB device array inside the library
- * (SS_NOALLOC_SCRATCH_BYTES), held by every GPU that loads the library until
- * the process exits.  Runs whose scratch would exceed it (about 26000 steps
- * with a moving progenitor) return SS_ERR_WORKSPACE.  The first call on a
- * device looks the array's device address up (cudaGetSymbolAddress) with
- * that device current; make that first call before any stream capture.
- * Every call overwrites the whole scratch it uses before reading it, and
- * all calls share the one array: calls that overlap on the GPU (different
- * streams, no ordering between them) race and must not be issued. */
+ * (SS_NOALLOC_SCRATCH_BYTES = 4194304), held by every GPU that loads the
+ * library until the process exits.  A run is accepted when
+ * ss_stream_workspace_bytes(pot, cfg) <= 4194304 and otherwise returns
+ * SS_ERR_WORKSPACE.  The scratch is the sum of: a moving progenitor's track,
+ * (5 n_steps + 1) x 32 bytes (about 26000 steps alone); a rotating or
+ * frame-accelerated component, the same again (about 13000 steps together);
+ * subhalo lines, 48 bytes each; an expansion, (n_knots - 1)(l_max + 1)^2 x 16
+ * bytes; each part rounded up to 256 bytes.  The first call on a device
+ * looks the array's device address up (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture.  The
+ * address is kept for the life of the process: do not call this entry point
+ * again after cudaDeviceReset() on that device.  Every call overwrites the
+ * whole scratch it uses before reading it, and all calls share the one
+ * array: calls that overlap on the GPU (on streams with no ordering between
+ * them, or from several host threads) race and must not be issued. */
 int ss_stream_f32k_noalloc(const ss_potential* pot, const ss_stream_cfg* cfg, const double* ics,
                            double* final_w, float* snaps, int32_t* status, void* stream);
 
@@ -448,9 +455,10 @@ int ss_binned_sums(const double* values, const double* key, int64_t n, int32_t n
                    double* sums, double* counts, void* stream);
 
 /* Peak arithmetic throughput probe used for rooflines: eight independent
- * FMA chains per thread on 8 blocks per SM.  precision 64 or 32;
- * *out_flops = flops the launch executes; sink: device buffer of >= 512
- * floats (never written in practice). */
+ * FMA chains per thread on 8 blocks per SM.  precision 64, 32, or 2 for
+ * packed FP32 pairs (fma.rn.f32x2, two FMAs per instruction: the form the
+ * paired FP32 stream kernel issues); *out_flops = flops the launch executes;
+ * sink: device buffer of >= 512 floats (never written in practice). */
 int ss_peak_fma(int precision, int64_t iters, double* out_flops, float* sink, void* stream);
 
 /* Strided copy of `rows` rows of `width_bytes` starting `offset_bytes`

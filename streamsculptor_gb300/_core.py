@@ -443,8 +443,29 @@ def _aux_stream(dev: torch.device, name: str) -> torch.cuda.Stream:
     return _AUX_STREAMS[key]
 
 
+def host_buffers(n_particles: int, n_snap: int = 0):
+    """Pinned host output buffers for stream_to_host / gen_stream(out='host'):
+    (final [N, 6] float64, snapshots [n_snap, N, 6] float32 or None)."""
+    final_h = torch.empty(int(n_particles), 6, dtype=torch.float64, pin_memory=True)
+    snaps_h = torch.empty(int(n_snap), int(n_particles), 6, dtype=torch.float32, pin_memory=True) if n_snap else None
+    return final_h, snaps_h
+
+
+def _check_host_buffers(bufs, N: int, n_snap: int):
+    final_h, snaps_h = bufs
+    if (not isinstance(final_h, torch.Tensor) or final_h.is_cuda or final_h.dtype != torch.float64 or
+            tuple(final_h.shape) != (N, 6) or not final_h.is_contiguous() or not final_h.is_pinned()):
+        raise ValueError(f"out_buffers[0] must be a contiguous pinned host float64 tensor [{N}, 6]")
+    if n_snap:
+        if (not isinstance(snaps_h, torch.Tensor) or snaps_h.is_cuda or snaps_h.dtype != torch.float32 or
+                tuple(snaps_h.shape) != (n_snap, N, 6) or not snaps_h.is_contiguous() or not snaps_h.is_pinned()):
+            raise ValueError(f"out_buffers[1] must be a contiguous pinned host float32 tensor [{n_snap}, {N}, 6]")
+    elif snaps_h is not None:
+        raise ValueError("out_buffers[1] must be None for a run without snapshots")
+
+
 def stream_to_host(P, cfg, ics: torch.Tensor, precision: str, snap_every: int = 0, mlp=None, n_chunks: int = 8,
-                   n_streams: int = 2):
+                   n_streams: int = 2, out_buffers=None):
     """The stream in particle sub-ranges whose results are copied to pinned
     host memory while later sub-ranges integrate: sub-range kernels alternate
     between two CUDA streams (so one's last wave overlaps the next one's
@@ -452,7 +473,9 @@ def stream_to_host(P, cfg, ics: torch.Tensor, precision: str, snap_every: int = 
     strided row blocks with ss_copy_rows_async).  Returns pinned host (final
     [N,6] float64, snapshots [n_snap,N,6] float32 or None) and the device
     status [N]; the host buffers are complete once the current stream is
-    synchronised."""
+    synchronised.  out_buffers: caller-owned pinned buffers (host_buffers())
+    written in place, so that repeated calls allocate no pinned memory (a
+    fresh multi-GB pinned allocation costs more than the copies)."""
     import copy as _cp
     N = int(cfg.n_particles)
     dev = ics.device
@@ -460,8 +483,11 @@ def stream_to_host(P, cfg, ics: torch.Tensor, precision: str, snap_every: int = 
     final_d = torch.empty(N, 6, dtype=torch.float64, device=dev)
     status_d = torch.empty(N, dtype=torch.int32, device=dev)
     snaps_d = torch.empty(n_snap, N, 6, dtype=torch.float32, device=dev) if n_snap else None
-    final_h = torch.empty(N, 6, dtype=torch.float64, pin_memory=True)
-    snaps_h = torch.empty(n_snap, N, 6, dtype=torch.float32, pin_memory=True) if n_snap else None
+    if out_buffers is not None:
+        _check_host_buffers(out_buffers, N, n_snap)
+        final_h, snaps_h = out_buffers
+    else:
+        final_h, snaps_h = host_buffers(N, n_snap)
     main = torch.cuda.current_stream(dev)
     comp = [_aux_stream(dev, f"compute{i}") for i in range(max(1, int(n_streams)))]
     # one copy stream per compute stream: a sub-range's copy never queues

@@ -461,6 +461,27 @@ __global__ void __launch_bounds__(256) peak_fma_kernel(int64_t iters, T* sink) {
     if (s == T(-12345.678)) sink[threadIdx.x] = s;
 }
 
+// The same chains in the packed form of the paired stream kernel: each
+// fma.rn.f32x2 instruction is two FP32 FMAs, one per lane.
+__global__ void __launch_bounds__(256) peak_fma2_kernel(int64_t iters, float* sink) {
+    const float x = (float)threadIdx.x * 1e-3f;
+    float2 a0 = make_float2(x, x + 0.5f), a1 = make_float2(x + 1, x + 1.5f), a2 = make_float2(x + 2, x + 2.5f),
+           a3 = make_float2(x + 3, x + 3.5f), a4 = make_float2(x + 4, x + 4.5f), a5 = make_float2(x + 5, x + 5.5f),
+           a6 = make_float2(x + 6, x + 6.5f), a7 = make_float2(x + 7, x + 7.5f);
+    const float2 b = make_float2(0.999999f, 0.999999f), c = make_float2(1e-6f, 1e-6f);
+    for (int64_t i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            a0 = __ffma2_rn(a0, b, c); a1 = __ffma2_rn(a1, b, c); a2 = __ffma2_rn(a2, b, c);
+            a3 = __ffma2_rn(a3, b, c); a4 = __ffma2_rn(a4, b, c); a5 = __ffma2_rn(a5, b, c);
+            a6 = __ffma2_rn(a6, b, c); a7 = __ffma2_rn(a7, b, c);
+        }
+    }
+    const float s = a0.x + a0.y + a1.x + a1.y + a2.x + a2.y + a3.x + a3.y + a4.x + a4.y + a5.x + a5.y + a6.x +
+                    a6.y + a7.x + a7.y;
+    if (s == -12345.678f) sink[threadIdx.x] = s;
+}
+
 }  // namespace ssg
 
 using namespace ssg;
@@ -629,7 +650,7 @@ int ss_binned_sums(const double* values, const double* key, int64_t n, int32_t n
 }
 
 int ss_peak_fma(int precision, int64_t iters, double* out_flops, float* sink, void* stream) {
-    SS_CHECK_ARG(precision == 32 || precision == 64, "precision must be 32 or 64");
+    SS_CHECK_ARG(precision == 32 || precision == 64 || precision == 2, "precision must be 32, 64 or 2 (f32x2)");
     SS_CHECK_ARG(iters >= 1 && sink != nullptr, "iters >= 1 and a sink buffer of >= 256 floats required");
     int dev = 0, sms = 0;
     SS_CUDA_TRY(cudaGetDevice(&dev));
@@ -638,10 +659,12 @@ int ss_peak_fma(int precision, int64_t iters, double* out_flops, float* sink, vo
     cudaStream_t s = (cudaStream_t)stream;
     if (precision == 32)
         peak_fma_kernel<float><<<blocks, 256, 0, s>>>(iters, sink);
+    else if (precision == 2)
+        peak_fma2_kernel<<<blocks, 256, 0, s>>>(iters, sink);
     else
         peak_fma_kernel<double><<<blocks, 256, 0, s>>>(iters, reinterpret_cast<double*>(sink));  // sink >= 512 floats
     SS_LAUNCH_CHECK();
-    if (out_flops) *out_flops = 2.0 * 32.0 * (double)iters * 256.0 * (double)blocks;
+    if (out_flops) *out_flops = (precision == 2 ? 2.0 : 1.0) * 2.0 * 32.0 * (double)iters * 256.0 * (double)blocks;
     return SS_OK;
 }
 

@@ -323,7 +323,8 @@ void* g_noalloc_ptr[64] = {nullptr};
 
 // Device address of g_noalloc_scratch on the current device, looked up once
 // per device (host code cannot use the symbol's host-side name as a device
-// pointer).
+// pointer) and kept for the life of the process: a cudaDeviceReset() of that
+// device would leave it stale, so the entry point is not for use after one.
 static int noalloc_scratch(void** out) {
     int dev = 0;
     SS_CUDA_TRY(cudaGetDevice(&dev));
@@ -344,8 +345,8 @@ extern "C" int ss_stream_f32k_noalloc(const ss_potential* pot, const ss_stream_c
     const int64_t need = f32k_workspace(pot, cfg);
     if (need > SS_NOALLOC_SCRATCH_BYTES)
         return set_error(SS_ERR_WORKSPACE,
-                         "ss_stream_f32k_noalloc: this run needs %lld bytes of scratch but the fixed scratch holds "
-                         "%lld (about 26000 steps with a moving progenitor); use ss_stream_f32k with a workspace",
+                         "ss_stream_f32k_noalloc: this run needs %lld bytes of scratch (ss_stream_workspace_bytes) "
+                         "but the fixed scratch holds %lld; use ss_stream_f32k with a workspace",
                          (long long)need, (long long)SS_NOALLOC_SCRATCH_BYTES);
     void* scratch = nullptr;
     int rc = noalloc_scratch(&scratch);

@@ -30,6 +30,19 @@ Dopri5 combinations per step (6 force evaluations, FSAL reuse):
   also restore the FP32 masses (and NFW's 1 / r_s) from their rounding
   residuals: one FMA each, 4 flops for NFW and 2 for the other spherical and
   disk kinds per force evaluation.
+
+First-order response (pert_response_kernel, ss_pert.cu), per (particle,
+subhalo)-step, mass columns only (ncol = 6), Plummer subhalos:
+  stage states   per column a-sums of 1..5 terms (1 + 3 + 5 + 7 + 9) and
+                 U = u + h acc (5 x 2)                          = 35; x 6 = 210
+  right-hand side per stage: line position (6) + rel (3) + r^2 (5)
+                 + Plummer g (5; 1 rsqrt) + g rel (3) + T x1 - on g (21) = 43;
+                 x 6 stages = 258, 6 specials
+  stage times    6 FMAs                                          = 12
+  update         per column b-sum (9) + u + h sum (2)            = 11; x 6 = 66
+  total 546 flops, 6 specials.  The radius columns (ncol = 12) repeat the
+  stage, update and T x1 work for six more columns and add the structural
+  gradient (4 per stage): 546 + 210 + 66 + 6 x (21 + 4) = 972.
 """
 from __future__ import annotations
 
@@ -84,3 +97,14 @@ def particle_step_work(flat, precision: str) -> dict:
     fl, sp = force_work(flat, residuals=precision == "f32k2")
     return {"flops": STAGES * fl + RK_FLOPS[precision], "specials": STAGES * sp,
             "force_flops": fl, "force_specials": sp, "rk_flops": RK_FLOPS[precision]}
+
+
+RESPONSE_FLOPS = {6: 546, 12: 972}
+
+
+def response_step_work(ncol: int = 6) -> dict:
+    """Flops and special ops of one Dopri5 step of one (particle, subhalo)
+    linear-response system (first order; Plummer subhalos)."""
+    if ncol not in RESPONSE_FLOPS:
+        raise ValueError("ncol must be 6 or 12")
+    return {"flops": RESPONSE_FLOPS[ncol], "specials": STAGES}

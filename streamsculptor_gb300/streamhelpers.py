@@ -40,7 +40,7 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
                kval_arr=1.0, dt=None, dtmax=None, n_particles_per_release=2, normals=None, precision="f64",
                snapshot_every=None, throw=False, release="fardal", prog_pot: Optional[Potential] = None,
                pot_pert: Optional[Potential] = None, prog_in_pert=False, return_ics=False, prog_method="auto",
-               force_surrogate=None, out="device", release_range=None):
+               force_surrogate=None, out="device", release_range=None, out_buffers=None):
     """Generate a particle-spray stream on the GPU.
 
     pot_base    smooth potential (release model and integration)
@@ -57,6 +57,10 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
     out         'device' (CUDA tensors) or 'host': pinned host tensors, the stream
                 run in particle sub-ranges whose results are copied while the
                 next sub-range integrates (ready when the call returns)
+    out_buffers (out='host' only) caller-owned pinned host buffers to write
+                into, from _core.host_buffers(N, n_snap): (final [N, 6] float64,
+                snapshots [n_snap, N, 6] float32 or None); repeated calls then
+                allocate no pinned memory, and each call overwrites them
     precision   'f64', 'f32k' (FP32 compensated) or 'mlp': the particles move
                 in the force of `force_surrogate` (surrogate.MLPSurrogate, BF16
                 tensor cores) while the progenitor orbit and the release use
@@ -127,9 +131,12 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
                                   "prog_pot / pot_pert")
     if out == "host":
         final, snaps, status = _core.stream_to_host(integ._desc(), cfg, stream_ics, precision,
-                                                    int(snapshot_every or 0), mlp=force_surrogate)
+                                                    int(snapshot_every or 0), mlp=force_surrogate,
+                                                    out_buffers=out_buffers)
         torch.cuda.current_stream().synchronize()
     elif out == "device":
+        if out_buffers is not None:
+            raise ValueError("out_buffers is for out='host'")
         if snapshot_every:
             n_snap = cfg.n_steps // int(snapshot_every)
             snaps = torch.empty(n_snap, N, 6, dtype=torch.float32, device=ws.device)

@@ -36,6 +36,17 @@ def test_headline_work_per_particle_step():
     assert w64["specials"] == w32["specials"] == w2["specials"] == 66
 
 
+def test_response_work_per_system_step():
+    """Mass columns: 210 (stage states) + 6 x 43 (right-hand sides) + 12
+    (stage times) + 66 (update) = 546 flops and one rsqrt per stage."""
+    w = roofline.response_step_work(6)
+    assert w["flops"] == 210 + 6 * 43 + 12 + 66 == 546
+    assert w["specials"] == 6
+    assert roofline.response_step_work(12)["flops"] == 546 + 210 + 66 + 6 * (21 + 4)
+    with pytest.raises(ValueError):
+        roofline.response_step_work(18)
+
+
 @pytest.mark.skipif(torch.cuda.is_available(), reason="checks the behaviour without a CUDA device")
 def test_no_cpu_fallback_for_device_tables():
     """Subhalo tables live on the device; without CUDA the package raises
