@@ -461,6 +461,13 @@ int ss_binned_sums(const double* values, const double* key, int64_t n, int32_t n
  * sink: device buffer of >= 512 floats (never written in practice). */
 int ss_peak_fma(int precision, int64_t iters, double* out_flops, float* sink, void* stream);
 
+/* The FP64 special functions of the force evaluations, for verification
+ * against the CUDA math library (no counterpart in the reference):
+ * fn 0: reciprocal, 1: reciprocal square root, 2: ln(1 + x) (x >= 0);
+ * out[i] = f(x[i]) and, when ref is not NULL, ref[i] = the CUDA math
+ * library's 1.0 / x, rsqrt(x) or log1p(x).  x, out, ref: device [n]. */
+int ss_math_f64(int fn, const double* x, int64_t n, double* out, double* ref, void* stream);
+
 /* Strided copy of `rows` rows of `width_bytes` starting `offset_bytes`
  * into each row of pitch `pitch_bytes` (cudaMemcpy2DAsync, same offset and
  * pitch on both sides): moves a particle sub-range of snapshots

@@ -141,6 +141,7 @@ SIGNATURES = {
                                        VP, VP, VP, C.c_int64, VP]),
     "ss_binned_sums": (C.c_int, [VP, VP, C.c_int64, C.c_int32, VP, C.c_int32, VP, VP, VP]),
     "ss_peak_fma": (C.c_int, [C.c_int, C.c_int64, DP, VP, VP]),
+    "ss_math_f64": (C.c_int, [C.c_int, VP, C.c_int64, VP, VP, VP]),
     "ss_copy_rows_async": (C.c_int, [VP, VP, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int, VP]),
     "ss_pert_track_bytes": (C.c_int64, [C.POINTER(ss_pert_cfg), C.c_int]),
     "ss_pert_base_track": (C.c_int, [C.POINTER(ss_potential), C.POINTER(ss_pert_cfg), C.c_int, VP, VP, VP, C.c_int64,

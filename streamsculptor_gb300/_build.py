@@ -30,7 +30,7 @@ def sources():
 
 
 def _deps():
-    files = sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
+    files = sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".inc"))]
     files.append(os.path.join(INCLUDE, "streamsculptor_gb300.h"))
     files.append(os.path.abspath(__file__))
     return files

@@ -482,6 +482,22 @@ __global__ void __launch_bounds__(256) peak_fma2_kernel(int64_t iters, float* si
     if (s == -12345.678f) sink[threadIdx.x] = s;
 }
 
+__global__ void math_f64_kernel(int fn, const double* __restrict__ x, int64_t n, double* out, double* ref) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = x[i];
+    if (fn == 0) {
+        out[i] = s_rcp(v);
+        if (ref) ref[i] = 1.0 / v;
+    } else if (fn == 1) {
+        out[i] = s_rsqrt(v);
+        if (ref) ref[i] = rsqrt(v);
+    } else {
+        out[i] = s_log1p(v);
+        if (ref) ref[i] = log1p(v);
+    }
+}
+
 }  // namespace ssg
 
 using namespace ssg;
@@ -645,6 +661,16 @@ int ss_binned_sums(const double* values, const double* key, int64_t n, int32_t n
     int64_t blocks = grid_for(n, 256);
     if (blocks > 4 * 152) blocks = 4 * 152;
     binned_sums_kernel<<<(unsigned)blocks, 256, smem, s>>>(values, key, n, ncomp, edges, n_edges, sums, counts);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
+int ss_math_f64(int fn, const double* x, int64_t n, double* out, double* ref, void* stream) {
+    SS_CHECK_ARG(fn >= 0 && fn <= 2, "fn must be 0 (reciprocal), 1 (rsqrt) or 2 (log1p)");
+    SS_CHECK_ARG(n >= 0, "n < 0");
+    if (n == 0) return SS_OK;
+    SS_CHECK_ARG(x != nullptr && out != nullptr, "NULL buffer");
+    math_f64_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(fn, x, n, out, ref);
     SS_LAUNCH_CHECK();
     return SS_OK;
 }

@@ -79,11 +79,19 @@ int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalo
 // at time t: velocity_acceleration, main.py:116-120.
 // C: the composition (Comp<...> or GenericComp); sh: the subhalo rows this
 // particle feels (P.sh, or one stream's slice of it in an ensemble run).
+// cen: the center track's position at t when the caller has it (the stream
+// kernel tabulates it per stage time), else NULL.
 template <class C>
 __device__ __forceinline__ void accel_f64(const PotDev<double>& P, const ShDev& sh, const double x[3], double t,
-                                          double a[3]) {
+                                          double a[3], const double* cen = nullptr) {
     double c[3] = {0.0, 0.0, 0.0};
-    if (P.has_track) track_eval(P.track, t, c);
+    if (cen) {
+        c[0] = cen[0];
+        c[1] = cen[1];
+        c[2] = cen[2];
+    } else if (P.has_track) {
+        track_eval(P.track, t, c);
+    }
     const double xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
     double g[3];
     C::template grad<double, double, false>(P, x, xs, g, nullptr, time_dep(P, t));
@@ -93,36 +101,38 @@ __device__ __forceinline__ void accel_f64(const PotDev<double>& P, const ShDev& 
     a[2] = -g[2];
 }
 
-// One fixed Dopri5 step of the Hamiltonian flow (x, v) in FP64.
+// One fixed Dopri5 step of the Hamiltonian flow (x, v) in FP64.  cen: the
+// center track at the six stage times t + c_s h (c = 0, 1/5, 3/10, 4/5, 8/9,
+// 1), or NULL to evaluate it per stage.
 template <class C>
 __device__ __forceinline__ void dopri5_step_f64(const PotDev<double>& P, const ShDev& sh, double t, double h,
-                                                double y[6]) {
+                                                double y[6], const double (*cen)[3] = nullptr) {
     double k1[6], k2[6], k3[6], k4[6], k5[6], k6[6], ys[6];
     // stage 1
     k1[0] = y[3]; k1[1] = y[4]; k1[2] = y[5];
-    accel_f64<C>(P, sh, y, t, k1 + 3);
+    accel_f64<C>(P, sh, y, t, k1 + 3, cen ? cen[0] : nullptr);
 #pragma unroll
     for (int i = 0; i < 6; ++i) ys[i] = y[i] + h * (SS_A21 * k1[i]);
     k2[0] = ys[3]; k2[1] = ys[4]; k2[2] = ys[5];
-    accel_f64<C>(P, sh, ys, t + SS_C2 * h, k2 + 3);
+    accel_f64<C>(P, sh, ys, t + SS_C2 * h, k2 + 3, cen ? cen[1] : nullptr);
 #pragma unroll
     for (int i = 0; i < 6; ++i) ys[i] = y[i] + h * (SS_A31 * k1[i] + SS_A32 * k2[i]);
     k3[0] = ys[3]; k3[1] = ys[4]; k3[2] = ys[5];
-    accel_f64<C>(P, sh, ys, t + SS_C3 * h, k3 + 3);
+    accel_f64<C>(P, sh, ys, t + SS_C3 * h, k3 + 3, cen ? cen[2] : nullptr);
 #pragma unroll
     for (int i = 0; i < 6; ++i) ys[i] = y[i] + h * (SS_A41 * k1[i] + SS_A42 * k2[i] + SS_A43 * k3[i]);
     k4[0] = ys[3]; k4[1] = ys[4]; k4[2] = ys[5];
-    accel_f64<C>(P, sh, ys, t + SS_C4 * h, k4 + 3);
+    accel_f64<C>(P, sh, ys, t + SS_C4 * h, k4 + 3, cen ? cen[3] : nullptr);
 #pragma unroll
     for (int i = 0; i < 6; ++i)
         ys[i] = y[i] + h * (SS_A51 * k1[i] + SS_A52 * k2[i] + SS_A53 * k3[i] + SS_A54 * k4[i]);
     k5[0] = ys[3]; k5[1] = ys[4]; k5[2] = ys[5];
-    accel_f64<C>(P, sh, ys, t + SS_C5 * h, k5 + 3);
+    accel_f64<C>(P, sh, ys, t + SS_C5 * h, k5 + 3, cen ? cen[4] : nullptr);
 #pragma unroll
     for (int i = 0; i < 6; ++i)
         ys[i] = y[i] + h * (SS_A61 * k1[i] + SS_A62 * k2[i] + SS_A63 * k3[i] + SS_A64 * k4[i] + SS_A65 * k5[i]);
     k6[0] = ys[3]; k6[1] = ys[4]; k6[2] = ys[5];
-    accel_f64<C>(P, sh, ys, t + h, k6 + 3);
+    accel_f64<C>(P, sh, ys, t + h, k6 + 3, cen ? cen[5] : nullptr);
 #pragma unroll
     for (int i = 0; i < 6; ++i)
         y[i] = y[i] + h * (SS_B1 * k1[i] + SS_B3 * k3[i] + SS_B4 * k4[i] + SS_B5 * k5[i] + SS_B6 * k6[i]);

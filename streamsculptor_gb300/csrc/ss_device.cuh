@@ -115,7 +115,16 @@ __device__ inline Dual<N> chain(const Dual<N>& x, double fv, double dfv) {
 // Scalar helpers overloaded for float / double / Dual.
 // FP32: hardware reciprocal (square root) estimates refined by one Newton
 // step (no IEEE special-case paths; arguments are positive and finite).
-// FP64: rsqrt (<= 1 ulp) saves the separate square root and division.
+// FP64: the hardware estimates of rcp.approx.ftz.f64 / rsqrt.approx.ftz.f64
+// refined by one third-order step: with e = 1 - x y (reciprocal) or
+// e = 1 - x y^2 (reciprocal square root), 1/x = y / (1 - e) and x^(-1/2) =
+// y (1 - e)^(-1/2) are expanded to e^2, which leaves an error of order e^3
+// below the final rounding; no IEEE special-case paths (arguments are
+// positive and finite).  GB300 issues FP64 at 1/64 of the FP32 rate, so the
+// force evaluations are written in as few FP64 instructions as their
+// accuracy allows.
+#include "ss_log_table.inc"
+
 __device__ __forceinline__ float  s_sqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double s_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float s_rsqrt(float x) {
@@ -124,15 +133,60 @@ __device__ __forceinline__ float s_rsqrt(float x) {
     float e = fmaf(-x * y, y, 1.0f);
     return fmaf(0.5f * y, e, y);
 }
-__device__ __forceinline__ double s_rsqrt(double x) { return rsqrt(x); }
+__device__ __forceinline__ double rsqrt_estimate(double x) {
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    return y;
+}
+__device__ __forceinline__ double rcp_estimate(double x) {
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    return y;
+}
+__device__ __forceinline__ double s_rsqrt(double x) {
+    const double y = rsqrt_estimate(x);
+    const double e = fma(-x * y, y, 1.0);
+    return fma(y * e, fma(e, 0.375, 0.5), y);  // y (1 + e/2 + 3 e^2 / 8)
+}
 __device__ __forceinline__ float  s_log1p(float x) { return log1pf(x); }
-__device__ __forceinline__ double s_log1p(double x) { return log1p(x); }
+// ln(1 + u), u >= 0 (NFW's ln(1 + r / r_s)), table-driven after Tang (ACM
+// TOMS 16, 1990): w = 1 + u is rounded and its rounding error c kept
+// (ln(1 + u) = ln w + c / w to first order in c); w = 2^k m with m in
+// [1, 2) and j the nearest breakpoint F_j = 1 + j / 128; with G_j = 1 / F_j
+// rounded and L_j = -ln G_j from the table, ln m = L_j + ln(1 + r) exactly,
+// r = m G_j - 1 from one FMA, |r| < 2^-8; ln(1 + r) by its Taylor series
+// through r^7 (the next term is below 2^-59 r).
+__device__ __forceinline__ double s_log1p(double u) {
+    const double w = 1.0 + u;
+    const double bb = w - 1.0;
+    const double c = (1.0 - (w - bb)) + (u - bb);  // the rounding error of 1 + u, exactly (TwoSum)
+    const double rw0 = rcp_estimate(w);
+    const double rw = fma(rw0, fma(-w, rw0, 1.0), rw0);  // 1 / w to ~2^-44: c / w is the whole result for tiny u
+    const int hi = __double2hiint(w), lo = __double2loint(w);
+    const int k = (hi >> 20) - 1023;
+    const int j = ((hi & 0x000fffff) + 0x1000) >> 13;  // nearest of 128 breakpoints: 0 .. 128
+    const double m = __hiloint2double((hi & 0x000fffff) | 0x3ff00000, lo);
+    const double2 t = __ldg(&g_ln_tab[j]);
+    const double r = fma(m, t.x, -1.0);
+    double q = fma(r, -1.0 / 7.0, 1.0 / 6.0);
+    q = fma(r, q, -0.2);
+    q = fma(r, q, 0.25);
+    q = fma(r, q, -1.0 / 3.0);
+    q = fma(r, q, 0.5);
+    const double p = fma(-r * r, q, r);  // ln(1 + r)
+    const double kd = (double)k;
+    return fma(kd, SS_LN2_HI, t.y) + (p + fma(kd, SS_LN2_LO, c * rw));
+}
 __device__ __forceinline__ float s_rcp(float x) {
     // hardware estimate + one Newton step: r (2 - x r)
     float r = __fdividef(1.0f, x);
     return fmaf(r, fmaf(-x, r, 1.0f), r);
 }
-__device__ __forceinline__ double s_rcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ double s_rcp(double x) {
+    const double y = rcp_estimate(x);
+    const double e = fma(-x, y, 1.0);
+    return fma(y, fma(e, e, e), y);  // y (1 + e + e^2)
+}
 __device__ __forceinline__ double s_cbrt(double x) { return cbrt(x); }
 template <int N> __device__ inline Dual<N> s_sqrt(const Dual<N>& x) { double s = sqrt(x.v); return chain(x, s, 0.5 / s); }
 template <int N> __device__ inline Dual<N> s_rsqrt(const Dual<N>& x) { double s = 1.0 / sqrt(x.v); return chain(x, s, -0.5 * s / x.v); }

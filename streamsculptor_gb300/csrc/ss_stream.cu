@@ -36,6 +36,23 @@
 
 namespace ssg {
 
+// The FP64 stream kernel (its body, stream_f64_body, is in ss_stream.cuh).
+// The analytic compositions fit the compiler's default register budget for
+// 64-thread blocks without spills; the expansion and the generic
+// composition need their larger register sets (one block per SM at least).
+template <class C>
+__global__ void __launch_bounds__(F64_BLOCK) stream_f64_kernel(PotDev<double> P, StreamArgs a) {
+    stream_f64_body<C>(P, a);
+}
+template <>
+__global__ void __launch_bounds__(F64_BLOCK, 1) stream_f64_kernel<GenericComp>(PotDev<double> P, StreamArgs a) {
+    stream_f64_body<GenericComp>(P, a);
+}
+template <>
+__global__ void __launch_bounds__(F64_BLOCK, 1) stream_f64_kernel<CompSHExp>(PotDev<double> P, StreamArgs a) {
+    stream_f64_body<CompSHExp>(P, a);
+}
+
 // Track positions at every stage time of the run, FP64 Hermite -> a hi/lo
 // float pair (two float4).  Slot 5n + s holds c(t0 + (n + c_s) dt) for
 // c = {0, 1/5, 3/10, 4/5, 8/9}; slot 5 n_steps holds c(t0 + n_steps dt).
@@ -194,7 +211,7 @@ int ss_stream_f64(const ss_potential* pot, const ss_stream_cfg* cfg, const doubl
     if (cfg->n_particles == 0) return SS_OK;
     SS_CHECK_ARG(ics != nullptr, "ics is NULL");
     StreamArgs a = make_args(cfg, ics, final_w, snaps, status);
-    const int block = 64;
+    const int block = F64_BLOCK;
     unsigned grid = (unsigned)((cfg->n_particles + block - 1) / block);
     dispatch_comp(P, [&](auto comp) {
         stream_f64_kernel<decltype(comp)><<<grid, block, 0, (cudaStream_t)stream>>>(P, a);

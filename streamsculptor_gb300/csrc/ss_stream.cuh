@@ -70,12 +70,30 @@ __device__ __forceinline__ void write_snap(float* snaps, int64_t N, int64_t k, i
 }
 
 // ------------------------------------------------------------------ FP64
+// Steps per chunk of the FP64 kernel's shared stage-time track table.
+constexpr int F64_CHUNK = 32;
+constexpr int F64_BLOCK = 64;
+
+// The block steps in chunks of F64_CHUNK steps from its earliest start.
+// With a center track (the moving progenitor) the block first tabulates
+// the track at the chunk's 6 F64_CHUNK stage times in shared memory (each
+// thread evaluates a few), so a stage reads its center instead of
+// evaluating the FP64 Hermite segment: the evaluations are the same
+// (same times, same arithmetic), one per block instead of one per thread.
 template <class C>
-__global__ void __launch_bounds__(64) stream_f64_kernel(PotDev<double> P, StreamArgs a) {
+__device__ __forceinline__ void stream_f64_body(const PotDev<double>& P, const StreamArgs& a) {
+    __shared__ double ctab[6 * F64_CHUNK][3];
+    __shared__ int s_start;
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p < a.N;
     const int start = valid ? stream_start(a, p + a.p_off) : a.n_steps;
     const int wstart = (int)__reduce_min_sync(0xffffffffu, (unsigned)start);
+    if (threadIdx.x == 0) s_start = a.n_steps;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) atomicMin(&s_start, wstart);
+    __syncthreads();
+    const int bstart = s_start;
+    const bool tab = P.has_track;
     const ShDev sh = a.sh_per_grp > 0 ? subhalo_slice(P.sh, (p + a.p_off) / a.grp, a.sh_per_grp) : P.sh;
     double y[6];
     if (valid) {
@@ -86,15 +104,31 @@ __global__ void __launch_bounds__(64) stream_f64_kernel(PotDev<double> P, Stream
         for (int i = 0; i < 6; ++i) y[i] = 0.0;
     }
     if (a.snaps && valid) {
-        for (int64_t k = 0; (k + 1) * (int64_t)a.stride <= wstart; ++k) {
+        for (int64_t k = 0; (k + 1) * (int64_t)a.stride <= bstart; ++k) {
             int64_t step = (k + 1) * (int64_t)a.stride;
             write_snap<double>(a.snaps, a.snap_pitch, k, p + a.p_off, step >= start, y);
         }
     }
-    for (int n = wstart; n < a.n_steps; ++n) {
-        if (valid && n >= start) dopri5_step_f64<C>(P, sh, a.t0 + (double)n * a.dt, a.dt, y);
-        if (a.snaps && (n + 1) % a.stride == 0 && valid)
-            write_snap<double>(a.snaps, a.snap_pitch, (n + 1) / a.stride - 1, p + a.p_off, n + 1 >= start, y);
+    for (int n0 = bstart; n0 < a.n_steps; n0 += F64_CHUNK) {
+        const int cnt = min(F64_CHUNK, a.n_steps - n0);
+        if (tab) {
+            __syncthreads();  // the previous chunk's table has been read
+            for (int i = threadIdx.x; i < 6 * cnt; i += blockDim.x) {
+                const int j = i / 6, s = i - 6 * j;
+                // the stage times of dopri5_step_f64: t_n + c_s h
+                const double t = a.t0 + (double)(n0 + j) * a.dt;
+                const double c = s == 1 ? SS_C2 : s == 2 ? SS_C3 : s == 3 ? SS_C4 : SS_C5;
+                track_eval(P.track, s == 0 ? t : s == 5 ? t + a.dt : t + c * a.dt, ctab[i]);
+            }
+            __syncthreads();
+        }
+        for (int j = 0; j < cnt; ++j) {
+            const int n = n0 + j;
+            if (valid && n >= start)
+                dopri5_step_f64<C>(P, sh, a.t0 + (double)n * a.dt, a.dt, y, tab ? &ctab[6 * j] : nullptr);
+            if (a.snaps && (n + 1) % a.stride == 0 && valid)
+                write_snap<double>(a.snaps, a.snap_pitch, (n + 1) / a.stride - 1, p + a.p_off, n + 1 >= start, y);
+        }
     }
     if (!valid) return;
     bool ok = true;
