@@ -269,3 +269,22 @@ def binned_sums(values, key, edges):
     counts = np.empty_like(sums)
     lib().or_binned_sums(_p(v), _p(k), n, nc, _p(e), e.shape[0], _p(sums), _p(counts))
     return sums, counts
+
+
+def mn3_components(m, h_R, h_z, positive_density=True, sech2_z=True):
+    """The three Miyamoto-Nagai components of MN3ExponentialDiskPotential
+    (reference potential.py:224-280): masses and scale lengths K x (b^4 ..
+    1) from the published coefficient table (Smith et al. 2015, Table 1, as
+    the reference holds it at potential.py:226-241), b = b_MN / h_R from the
+    cubic fit in h_z / h_R; all three share b_MN."""
+    Kp = [[0.0036, -0.0330, 0.1117, -0.1335, 0.1749], [-0.0131, 0.1090, -0.3035, 0.2921, -5.7976],
+          [-0.0048, 0.0454, -0.1425, 0.1012, 6.7120], [-0.0158, 0.0993, -0.2070, -0.7089, 0.6445],
+          [-0.0319, 0.1514, -0.1279, -0.9325, 2.6836], [-0.0326, 0.1816, -0.2943, -0.6329, 2.3193]]
+    Kn = [[-0.0090, 0.0640, -0.1653, 0.1164, 1.9487], [0.0173, -0.0903, 0.0877, 0.2029, -1.3077],
+          [-0.0051, 0.0287, -0.0361, -0.0544, 0.2242], [-0.0358, 0.2610, -0.6987, -0.1193, 2.0074],
+          [-0.0830, 0.4992, -0.7967, -1.2966, 4.4441], [-0.0247, 0.1718, -0.4124, -0.5944, 0.7333]]
+    K = np.array(Kp if positive_density else Kn)
+    q = h_z / h_R
+    b = (-0.033 * q ** 3 + 0.262 * q ** 2 + 0.659 * q) if sech2_z else (-0.269 * q ** 3 + 1.08 * q ** 2 + 1.092 * q)
+    pv = K.dot(np.array([b ** 4, b ** 3, b ** 2, b, 1.0]))
+    return [(_abi.SS_MIYAMOTO_NAGAI, 0, (pv[i] * m, pv[3 + i] * h_R, b * h_R)) for i in range(3)]

@@ -35,6 +35,51 @@ class MiyamotoNagaiDisk(Potential):
         return Flat([(_abi.SS_MIYAMOTO_NAGAI, _abi.SS_CENTER_ORIGIN, (_f(self.m), _f(self.a), _f(self.b)))])
 
 
+class MN3ExponentialDiskPotential(Potential):
+    """An exponential disk (scale length h_R, scale height h_z) as the sum of
+    three Miyamoto-Nagai disks (MN3ExponentialDiskPotential, potential.py:224-280;
+    Smith et al. 2015, MNRAS 448, 2934).  The three masses and scale
+    lengths are K x (b^4, b^3, b^2, b, 1) with b = b_MN / h_R a cubic fit in
+    h_z / h_R; K is the published 6 x 5 coefficient table for a positive
+    (or, positive_density=False, the unconstrained) density, the cubic for
+    a sech^2 (or exponential, sech2_z=False) vertical profile.  The three
+    disks share b_MN and are summed in order, as Potential_Combine sums."""
+
+    # Smith et al. (2015), Table 1: rows m1, m2, m3 (in m), a1, a2, a3 (in
+    # h_R); columns the coefficients of (b/h_R)^4 .. (b/h_R)^0.
+    K_POSITIVE = np.array([[0.0036, -0.0330, 0.1117, -0.1335, 0.1749],
+                           [-0.0131, 0.1090, -0.3035, 0.2921, -5.7976],
+                           [-0.0048, 0.0454, -0.1425, 0.1012, 6.7120],
+                           [-0.0158, 0.0993, -0.2070, -0.7089, 0.6445],
+                           [-0.0319, 0.1514, -0.1279, -0.9325, 2.6836],
+                           [-0.0326, 0.1816, -0.2943, -0.6329, 2.3193]])
+    K_NEGATIVE = np.array([[-0.0090, 0.0640, -0.1653, 0.1164, 1.9487],
+                           [0.0173, -0.0903, 0.0877, 0.2029, -1.3077],
+                           [-0.0051, 0.0287, -0.0361, -0.0544, 0.2242],
+                           [-0.0358, 0.2610, -0.6987, -0.1193, 2.0074],
+                           [-0.0830, 0.4992, -0.7967, -1.2966, 4.4441],
+                           [-0.0247, 0.1718, -0.4124, -0.5944, 0.7333]])
+
+    def __init__(self, m, h_R, h_z, units=None, positive_density=True, sech2_z=True):
+        super().__init__(units, {"m": m, "h_R": h_R, "h_z": h_z})
+        self.positive_density = bool(positive_density)
+        self.sech2_z = bool(sech2_z)
+        K = self.K_POSITIVE if self.positive_density else self.K_NEGATIVE
+        q = _f(h_z) / _f(h_R)
+        if self.sech2_z:
+            b = -0.033 * q ** 3 + 0.262 * q ** 2 + 0.659 * q
+        else:
+            b = -0.269 * q ** 3 + 1.08 * q ** 2 + 1.092 * q
+        pv = K @ np.array([b ** 4, b ** 3, b ** 2, b, 1.0])
+        self._ms = pv[:3] * _f(m)
+        self._as = pv[3:] * _f(h_R)
+        self._b = b * _f(h_R)
+
+    def _flatten(self):
+        return Flat([(_abi.SS_MIYAMOTO_NAGAI, _abi.SS_CENTER_ORIGIN, (float(mi), float(ai), float(self._b)))
+                     for mi, ai in zip(self._ms, self._as)])
+
+
 class NFWPotential(Potential):
     """Phi = -G m log(1 + r/r_s) / r (unsoftened, potential.py:80-84)."""
 
