@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define SS_ABI_VERSION 5
+#define SS_ABI_VERSION 6
 #define SS_MAX_COMPONENTS 16
 
 /* ---------------------------------------------------------------- status */
@@ -495,7 +495,22 @@ typedef struct ss_mlp {
     float in_shift[4];
     float out_scale;
     float out_shift;
+    /* Optional exact spherical part Phi_0(r) added to the network (NULL =
+     * none): a cubic Hermite spline in u = ln r through base_n knots at
+     * base_u0 + k base_du, [base_n][2] (value, d/du) FP64 on the device,
+     * continued linearly in u outside the knots (the form of an expansion's
+     * l = 0 radial function).  The network then represents Phi - Phi_0 (it
+     * is trained on that residual) and every evaluation adds Phi_0 and its
+     * gradient exactly: FP64 in ss_mlp_eval, FP32 from a shared-memory copy
+     * in the tensor-core kernels (2 <= base_n <= SS_MLP_BASE_MAX). */
+    const double* base;
+    int32_t base_n;
+    int32_t reserved;
+    double base_u0;
+    double base_du;
 } ss_mlp;
+
+#define SS_MLP_BASE_MAX 256
 
 /* FP32 evaluation (CUDA cores) of Phi and grad Phi at n points xyz [n,3]
  * (either output may be NULL).  Workspace: ss_mlp_eval_workspace_bytes(n). */

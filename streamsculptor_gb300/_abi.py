@@ -10,7 +10,7 @@ import ctypes as C
 import os
 import threading
 
-SS_ABI_VERSION = 5
+SS_ABI_VERSION = 6
 SS_MAX_COMPONENTS = 16
 
 SS_OK = 0
@@ -95,9 +95,14 @@ SS_MLP_WIDTH = 128
 SS_MLP_NPARAM = 128 * 4 + 128 + 3 * (128 * 128 + 128) + 128 + 1
 
 
+SS_MLP_BASE_MAX = 256
+
+
 class ss_mlp(C.Structure):
     _fields_ = [("params", VP), ("in_scale", C.c_float * 4), ("in_shift", C.c_float * 4),
-                ("out_scale", C.c_float), ("out_shift", C.c_float)]
+                ("out_scale", C.c_float), ("out_shift", C.c_float),
+                ("base", VP), ("base_n", C.c_int32), ("reserved", C.c_int32), ("base_u0", C.c_double),
+                ("base_du", C.c_double)]
 
 
 STRUCTS = [ss_potential, ss_stream_cfg, ss_release_cfg, ss_pert_cfg, ss_component, ss_track, ss_subhalos,

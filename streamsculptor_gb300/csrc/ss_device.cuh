@@ -784,6 +784,26 @@ __device__ __forceinline__ void radial_basis(const ExpDev& E, const T& u, Radial
     B.hss[3] = inside ? six * sc - two : T(0);
 }
 
+// Phi_0(u) and dPhi_0/du of a cubic Hermite spline in u through n knots at
+// u0 + k du, knot k holding (value, d/du) at tab[2k], tab[2k + 1], continued
+// linearly in u outside the knots: the form of an expansion's radial
+// functions (radial_basis, radial_term), used for the exact spherical part
+// of the learned surrogate (ss_mlp.base).
+template <class T, class V>
+__device__ __forceinline__ void base_spline(const V* tab, int n, T u0, T du, T inv_du, T u, T& f, T& fu) {
+    int k = (int)floor((u - u0) * inv_du);
+    k = k < 0 ? 0 : (k > n - 2 ? n - 2 : k);
+    const T s = (u - (u0 + T(k) * du)) * inv_du;
+    const T sc = s < T(0) ? T(0) : (s > T(1) ? T(1) : s);
+    const T e = s - sc, om = T(1) - sc;
+    const T c0 = T(tab[2 * k]), c1 = T(tab[2 * k + 1]) * du, c2 = T(tab[2 * k + 2]), c3 = T(tab[2 * k + 3]) * du;
+    const T fs = T(6) * sc * (sc - T(1)) * c0 + om * (T(1) - T(3) * sc) * c1 + T(6) * sc * om * c2 +
+                 sc * (T(3) * sc - T(2)) * c3;
+    f = (T(1) + T(2) * sc) * om * om * c0 + sc * om * om * c1 + sc * sc * (T(3) - T(2) * sc) * c2 +
+        sc * sc * (sc - T(1)) * c3 + e * fs;
+    fu = fs * inv_du;
+}
+
 // f, df/ds, d2f/ds2 of term j (s in knot spacings).
 template <class T>
 __device__ __forceinline__ void radial_term(const ExpDev& E, const RadialBasis<T>& B, int nt, int j, T& f, T& fs,

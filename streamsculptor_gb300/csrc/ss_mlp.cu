@@ -45,6 +45,9 @@ static_assert(OFF_B5 + 1 == SS_MLP_NPARAM, "parameter packing");
 struct MlpNorm {
     float c[4], s[4];  // u_i = (feature_i - s_i) c_i
     float out_scale, out_shift;
+    const double* base;  // exact spherical part (ss_mlp.base), or NULL
+    int base_n;
+    double base_u0, base_du;
 };
 
 static MlpNorm norm_of(const ss_mlp* m) {
@@ -55,6 +58,10 @@ static MlpNorm norm_of(const ss_mlp* m) {
     }
     n.out_scale = m->out_scale;
     n.out_shift = m->out_shift;
+    n.base = m->base;
+    n.base_n = m->base_n;
+    n.base_u0 = m->base_u0;
+    n.base_du = m->base_du;
     return n;
 }
 
@@ -217,15 +224,23 @@ __global__ void eval_out_kernel(const float* A4, const float* w5, const float* b
                                 const double* x, int64_t B, MlpNorm nm, double* phi, double* grad) {
     const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
+    // the exact spherical part, FP64
+    double f0 = 0.0, fu = 0.0, r2 = 1.0;
+    if (nm.base) {
+        r2 = x[3 * b] * x[3 * b] + x[3 * b + 1] * x[3 * b + 1] + x[3 * b + 2] * x[3 * b + 2];
+        base_spline<double, double>(nm.base, nm.base_n, nm.base_u0, nm.base_du, 1.0 / nm.base_du, 0.5 * log(r2), f0,
+                                    fu);
+    }
     if (phi) {
         float y = b5[0];
         for (int j = 0; j < MW; ++j) y = fmaf(A4[b * MW + j], w5[j], y);
-        phi[b] = (double)nm.out_scale * y + nm.out_shift;
+        phi[b] = (double)nm.out_scale * y + nm.out_shift + f0;
     }
     if (grad) {
         const float* gb = g + 4 * b;
         for (int j = 0; j < 3; ++j)
-            grad[3 * b + j] = (double)nm.out_scale * (gb[j] * nm.c[j] + gb[3] * nm.c[3] * (float)x[3 * b + j] * ir2[b]);
+            grad[3 * b + j] = (double)nm.out_scale * (gb[j] * nm.c[j] + gb[3] * nm.c[3] * (float)x[3 * b + j] * ir2[b]) +
+                              fu / r2 * x[3 * b + j];
     }
 }
 
@@ -405,6 +420,8 @@ int ss_mlp_eval(const ss_mlp* mlp, const double* xyz, int64_t n, double* phi, do
     SS_CHECK_ARG(n >= 0, "n < 0");
     if (n == 0) return SS_OK;
     SS_CHECK_ARG(xyz != nullptr, "xyz is NULL");
+    SS_CHECK_ARG(mlp->base == nullptr || (mlp->base_n >= 2 && mlp->base_n <= SS_MLP_BASE_MAX && mlp->base_du > 0.0),
+                 "mlp base table needs 2 <= base_n <= %d knots and base_du > 0", SS_MLP_BASE_MAX);
     const int64_t need = ss_mlp_eval_workspace_bytes(n);
     if (workspace == nullptr || workspace_bytes < need)
         return set_error(SS_ERR_WORKSPACE, "workspace of %lld bytes needed", (long long)need);

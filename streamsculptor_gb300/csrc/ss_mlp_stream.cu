@@ -52,7 +52,8 @@ static constexpr uint32_t SM_BAR = SM_W5 + 512;       // 2 mbarriers (8 B each)
 static constexpr uint32_t SM_TMEM = SM_BAR + 16;      // TMEM base address
 static constexpr uint32_t SM_ABORT = SM_TMEM + 4;     // 2 abort flags
 static constexpr uint32_t SM_START = SM_ABORT + 8;    // 2 tile start steps
-static constexpr uint32_t SM_BYTES = SM_START + 8;
+static constexpr uint32_t SM_BASE = SM_START + 8;     // float2 [SS_MLP_BASE_MAX]: the exact spherical part
+static constexpr uint32_t SM_BYTES = SM_BASE + 8 * SS_MLP_BASE_MAX;
 static constexpr uint32_t SM_ALLOC = SM_BYTES + 1024;  // slack for the 1024-byte alignment
 
 // TMEM columns within a warpgroup's 256
@@ -70,6 +71,9 @@ struct MlpDev {
     const float* params;
     float c[4], s[4];
     float out_scale, out_shift;
+    const double* base;  // exact spherical part (ss_mlp.base), or NULL; copied to shared memory as float
+    int base_n;
+    float base_u0, base_du;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -358,10 +362,17 @@ __device__ __noinline__ void mlp_grad_wg(const MlpDev& M, const MlpCta& cx, floa
             }
         }
     }
-    const float k3 = gi[3] * M.c[3] / r2;
-    g0 = M.out_scale * (gi[0] * M.c[0] + k3 * X0);
-    g1 = M.out_scale * (gi[1] * M.c[1] + k3 * X1);
-    g2 = M.out_scale * (gi[2] * M.c[2] + k3 * X2);
+    float k3 = M.out_scale * gi[3] * M.c[3] / r2;
+    if (M.base_n > 0) {
+        // + grad Phi_0 = (dPhi_0 / du) x / r^2, u = ln r
+        float f0, fu;
+        base_spline<float, float>(reinterpret_cast<const float*>(sm + SM_BASE), M.base_n, M.base_u0, M.base_du,
+                                  1.0f / M.base_du, 0.5f * logf(r2), f0, fu);
+        k3 += fu / r2;
+    }
+    g0 = M.out_scale * gi[0] * M.c[0] + k3 * X0;
+    g1 = M.out_scale * gi[1] * M.c[1] + k3 * X1;
+    g2 = M.out_scale * gi[2] * M.c[2] + k3 * X2;
 }
 
 // The "composition" handed to step_f32k: its gradient is the CTA-collective
@@ -419,6 +430,8 @@ __device__ __forceinline__ void mlp_cta_setup(const MlpKernelArgs& ka) {
     float* Bb = reinterpret_cast<float*>(sm + SM_B);
     float* w5 = reinterpret_cast<float*>(sm + SM_W5);
     for (int e = t; e < 512; e += blockDim.x) W1[e] = prm[P_W1 + e];
+    float* base = reinterpret_cast<float*>(sm + SM_BASE);
+    for (int e = t; e < 2 * ka.M.base_n; e += blockDim.x) base[e] = (float)ka.M.base[e];
     for (int e = t; e < 128; e += blockDim.x) {
         Bb[e] = prm[P_B1 + e];
         Bb[128 + e] = prm[P_B2 + e];
@@ -571,7 +584,9 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) stream_mlp_kernel(const __grid
     mlp_cta_teardown();
 }
 
-static void mlp_dev_of(const ss_mlp* mlp, MlpDev* M) {
+static int mlp_dev_of(const ss_mlp* mlp, MlpDev* M) {
+    SS_CHECK_ARG(mlp->base == nullptr || (mlp->base_n >= 2 && mlp->base_n <= SS_MLP_BASE_MAX && mlp->base_du > 0.0),
+                 "mlp base table needs 2 <= base_n <= %d knots and base_du > 0", SS_MLP_BASE_MAX);
     M->params = mlp->params;
     for (int i = 0; i < 4; ++i) {
         M->c[i] = mlp->in_scale[i];
@@ -579,6 +594,11 @@ static void mlp_dev_of(const ss_mlp* mlp, MlpDev* M) {
     }
     M->out_scale = mlp->out_scale;
     M->out_shift = mlp->out_shift;
+    M->base = mlp->base;
+    M->base_n = mlp->base ? mlp->base_n : 0;
+    M->base_u0 = (float)mlp->base_u0;
+    M->base_du = (float)mlp->base_du;
+    return SS_OK;
 }
 
 }  // namespace ssg
@@ -594,7 +614,8 @@ int ss_mlp_grad_bf16(const ss_mlp* mlp, const double* xyz, int64_t n, double* gr
     SS_CHECK_ARG(xyz != nullptr && grad != nullptr, "NULL buffer");
     MlpKernelArgs ka;
     memset(&ka, 0, sizeof(ka));
-    mlp_dev_of(mlp, &ka.M);
+    const int rc_m = mlp_dev_of(mlp, &ka.M);
+    if (rc_m) return rc_m;
     int dev = 0, sms = 0;
     SS_CUDA_TRY(cudaGetDevice(&dev));
     SS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -634,7 +655,8 @@ int ss_stream_mlp_bf16(const ss_mlp* mlp, const ss_stream_cfg* cfg, const double
     SS_CHECK_ARG(ics != nullptr, "ics is NULL");
     MlpKernelArgs ka;
     memset(&ka, 0, sizeof(ka));
-    mlp_dev_of(mlp, &ka.M);
+    const int rc_m = mlp_dev_of(mlp, &ka.M);
+    if (rc_m) return rc_m;
     StreamArgs& a = ka.a;
     a.ics = ics;
     a.final_w = final_w;

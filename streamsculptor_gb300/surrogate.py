@@ -46,6 +46,12 @@ class MLPSurrogate:
     out_scale: float = 1.0
     out_shift: float = 0.0
     history: list = field(default_factory=list)
+    # exact spherical part Phi_0(r) added to the network (ss_mlp.base): a
+    # [n, 2] float64 device table of (value, d/du) at u = base_u0 + k base_du,
+    # u = ln r; None = the network alone
+    base: Optional[torch.Tensor] = None
+    base_u0: float = 0.0
+    base_du: float = 1.0
 
     @staticmethod
     def init(seed=0, in_scale=(1.0, 1.0, 1.0, 1.0), in_shift=(0.0, 0.0, 0.0, 0.0), out_scale=1.0, out_shift=0.0,
@@ -69,7 +75,25 @@ class MLPSurrogate:
             m.in_shift[i] = float(self.in_shift[i])
         m.out_scale = float(self.out_scale)
         m.out_shift = float(self.out_shift)
+        if self.base is not None:
+            m.base = self.base.data_ptr()
+            m.base_n = int(self.base.shape[0])
+            m.base_u0 = float(self.base_u0)
+            m.base_du = float(self.base_du)
         return m
+
+    @staticmethod
+    def monopole_of(pot):
+        """(table [n, 2], u0, du) of the l = 0 term of a spherical-harmonic
+        expansion potential: its exact spherical part."""
+        coef = pot.coef.to(_core.device(), torch.float64)
+        return (float(pot.scale) * coef[:, 0, :]).contiguous(), float(pot.log_r0), float(pot.dlog_r)
+
+    def with_base(self, base, u0, du) -> "MLPSurrogate":
+        """Add the exact spherical part (ss_mlp.base); returns self."""
+        self.base = base.to(_core.device(), torch.float64).contiguous()
+        self.base_u0, self.base_du = float(u0), float(du)
+        return self
 
     # ---------------------------------------------------------- evaluation
     def potential_and_gradient(self, xyz):
@@ -110,16 +134,22 @@ class MLPSurrogate:
 
     # ------------------------------------------------------------ training
     def fit(self, x, phi, grad, steps=4000, batch=8192, lr=2e-3, lr_min=2e-5, force_weight=1.0, seed=0,
-            log_every=0):
+            log_every=0, force_scale=None):
         """Adam on the value + force loss with cosine learning-rate decay.
-        x [N,3], phi [N], grad [N,3] (exact targets, any float dtype)."""
+        x [N,3], phi [N], grad [N,3] (exact targets, any float dtype).  The
+        force loss is relative: each sample's force error is divided by
+        force_scale [N] (default |grad|; a residual fit passes the total
+        force's magnitude, so that it minimises the error of the sum)."""
         dev = self.params.device
         x = x.to(dev, torch.float32).contiguous()
         phi = phi.to(dev, torch.float32).contiguous()
-        grad = grad.to(dev, torch.float32).contiguous()
         N = x.shape[0]
         batch = min(batch, N)
-        gnorm2 = (grad.double() ** 2).sum(1).clamp_min(1e-300)
+        if force_scale is None:
+            gnorm2 = (grad.double() ** 2).sum(1).clamp_min(1e-300)
+        else:
+            gnorm2 = (force_scale.to(dev, torch.float64) ** 2).clamp_min(1e-300)
+        grad = grad.to(dev, torch.float32).contiguous()
         w_val_all = torch.full((N,), 1.0 / (batch * self.out_scale ** 2), dtype=torch.float32, device=dev)
         w_force_all = (force_weight / (batch * gnorm2)).float()
         m = torch.zeros_like(self.params)
@@ -186,15 +216,43 @@ def orbit_samples(pot, prog_w0, n_orbits=4096, n_per_orbit=1024, dt=1.0, every=2
     return ys[:, 1:, :3].reshape(-1, 3).contiguous()
 
 
-def train_surrogate(pot, prog_w0, n_points=1 << 22, steps=6000, batch=8192, seed=0, **kw) -> MLPSurrogate:
+def residual_targets(pot, x):
+    """Phi and grad Phi of an expansion potential at x minus its exact
+    spherical part (the l = 0 term, evaluated by the same FP64 kernels as a
+    one-term expansion), and that part's table: what a surrogate with an
+    exact base is trained on."""
+    from .potential import SphericalHarmonicExpansionPotential
+    table, u0, du = MLPSurrogate.monopole_of(pot)
+    mono = SphericalHarmonicExpansionPotential(pot.coef[:, :1, :], pot.log_r0, pot.dlog_r, scale=pot.scale,
+                                               units=pot.units)
+    phi = pot.potential(x, 0.0) - mono.potential(x, 0.0)
+    grad = pot.gradient(x, 0.0) - mono.gradient(x, 0.0)
+    return phi, grad, (table, u0, du)
+
+
+def train_surrogate(pot, prog_w0, n_points=1 << 22, steps=6000, batch=8192, seed=0, residual=None,
+                    **kw) -> MLPSurrogate:
     """Sample `n_points` along orbits of the exact potential, evaluate Phi and
-    grad Phi there with the exact FP64 kernels, and fit the network."""
+    grad Phi there with the exact FP64 kernels, and fit the network.  For an
+    expansion potential (residual=None or True) the network learns the
+    residual Phi - Phi_0 and the l = 0 term Phi_0 is added exactly, so the
+    network's error multiplies only the anisotropic part; the force loss is
+    relative to the total force."""
+    from .potential import SphericalHarmonicExpansionPotential
     n_per = 1024
     n_orb = max(1, n_points // n_per)
     x = orbit_samples(pot, prog_w0, n_orbits=n_orb, n_per_orbit=n_per, seed=seed)
-    phi = pot.potential(x, 0.0)
-    grad = pot.gradient(x, 0.0)
+    if residual is None:
+        residual = isinstance(pot, SphericalHarmonicExpansionPotential)
+    base, scale = None, None
+    if residual:
+        phi, grad, base = residual_targets(pot, x)
+        scale = torch.linalg.norm(pot.gradient(x, 0.0), dim=1)
+    else:
+        phi, grad = pot.potential(x, 0.0), pot.gradient(x, 0.0)
     nm = MLPSurrogate.normalisation(x.cpu(), phi.cpu())
     s = MLPSurrogate.init(seed=seed, **nm)
-    s.fit(x, phi, grad, steps=steps, batch=batch, seed=seed, **kw)
+    if base is not None:
+        s.with_base(*base)
+    s.fit(x, phi, grad, steps=steps, batch=batch, seed=seed, force_scale=scale, **kw)
     return s

@@ -102,15 +102,41 @@ def test_mlp_tensor_core_force_matches_fp32(ss):
     assert np.median(per) < 3e-2
 
 
+def test_exact_base_is_added_in_fp64_and_on_the_tensor_cores(ss):
+    """A surrogate with an exact spherical base (ss_mlp.base: the l = 0 term
+    of an expansion) returns the network plus that term: the FP64 evaluation
+    adds it to 1e-12 of the expansion kernels' own l = 0 evaluation, and the
+    tensor-core force with the base stays within the BF16 bound of the FP32
+    one."""
+    from streamsculptor_gb300 import potential as P
+    from streamsculptor_gb300.surrogate import MLPSurrogate
+    pot = P.seeded_triaxial_expansion(units=ss.usys)
+    mono = P.SphericalHarmonicExpansionPotential(pot.coef[:, :1, :], pot.log_r0, pot.dlog_r, units=ss.usys)
+    s0 = _surrogate(ss, seed=4)
+    s1 = _surrogate(ss, seed=4).with_base(*MLPSurrogate.monopole_of(pot))
+    x = np.concatenate([_points(4000, seed=5), _points(100, seed=6) * 5.0])  # some beyond the last knot
+    p0, g0 = s0.potential_and_gradient(x)
+    p1, g1 = s1.potential_and_gradient(x)
+    pm, gm = mono.potential(x, 0.0), mono.gradient(x, 0.0)
+    assert float((p1 - p0 - pm).abs().max()) <= 1e-12 * float(pm.abs().max())
+    assert float((g1 - g0 - gm).abs().max()) <= 1e-12 * float(gm.abs().max())
+    g16 = s1.gradient_bf16(x).cpu().numpy()
+    g32 = g1.cpu().numpy()
+    assert np.linalg.norm(g16 - g32) / np.linalg.norm(g32) < 3e-2
+
+
 @pytest.fixture(scope="module")
 def trained(ss):
+    """The network trained on the residual Phi - Phi_0 of the expansion
+    (its l = 0 term Phi_0 is added exactly), relative to the total force."""
     from streamsculptor_gb300 import potential as P
-    from streamsculptor_gb300.surrogate import MLPSurrogate, orbit_samples
+    from streamsculptor_gb300.surrogate import MLPSurrogate, orbit_samples, residual_targets
     pot = P.seeded_triaxial_expansion(units=ss.usys)
     x = orbit_samples(pot, PROG, n_orbits=192, n_per_orbit=512, seed=1)
-    phi, g = pot.potential(x, 0.0), pot.gradient(x, 0.0)
-    s = MLPSurrogate.init(seed=1, **MLPSurrogate.normalisation(x.cpu(), phi.cpu()))
-    s.fit(x, phi, g, steps=2500, batch=4096, lr=3e-3, seed=1, log_every=500)
+    phi, g, base = residual_targets(pot, x)
+    scale = torch.linalg.norm(pot.gradient(x, 0.0), dim=1)
+    s = MLPSurrogate.init(seed=1, **MLPSurrogate.normalisation(x.cpu(), phi.cpu())).with_base(*base)
+    s.fit(x, phi, g, steps=2500, batch=4096, lr=3e-3, seed=1, log_every=500, force_scale=scale)
     return pot, s
 
 
