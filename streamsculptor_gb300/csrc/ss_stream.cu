@@ -53,44 +53,22 @@ __global__ void __launch_bounds__(F64_BLOCK, 1) stream_f64_kernel<CompSHExp>(Pot
     stream_f64_body<CompSHExp>(P, a);
 }
 
-// The center track for the FP32 kernels, per step n (TRACK_ROW float4):
-//   [0] c_hi = c(t_n) rounded to float,
-//   [1] v_n = dc/dt at t_n (the Hermite segment's derivative) in float,
-//   [2 + k] for the stage times t_n + c_s dt, c_s = 0, 1/5, 3/10, 4/5, 8/9,
-//       1 (k = 0..5): E = c(t_n + c_s dt) - c_hi - h c_s' v_n, with h the
-//       float step and c_s' the float stage coefficients of the kernels
-//       (E_0 is the FP64 remainder of c_hi).
-// A particle's separation from the center at stage s is then
-//   (x_hi - c_hi) + ((x_lo + h (c_s' (v_hi - v_n) + T_s)) - E_s)
-// (T_s the stage's small velocity terms): near the center every term is
-// small, so the separation keeps its relative precision through a close
-// passage, where x_hi + h c_s' v_hi and c(t_s), each rounded near 0.1 kpc,
-// would cancel to ~1e-8 kpc.  E is of order h^2 times the center's
-// acceleration (~1e-3 kpc).
-__global__ void track_table_kernel(TrackDev tr, double t0, double dt, float h, int32_t n_steps, float4* tab) {
-    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= n_steps) return;
-    const double t = t0 + (double)n * dt;
-    double c0[3], v0[3];
-    track_eval(tr, t, c0);
-    track_slope(tr, t, v0);
-    float4* o = tab + TRACK_ROW * n;
-    const float hx = (float)c0[0], hy = (float)c0[1], hz = (float)c0[2];
-    const float vx = (float)v0[0], vy = (float)v0[1], vz = (float)v0[2];
-    o[0] = make_float4(hx, hy, hz, 0.f);
-    o[1] = make_float4(vx, vy, vz, 0.f);
-    o[2] = make_float4((float)(c0[0] - (double)hx), (float)(c0[1] - (double)hy), (float)(c0[2] - (double)hz), 0.f);
-    const double cd[5] = {SS_C2, SS_C3, SS_C4, SS_C5, 1.0};
-    const float cf[5] = {F_C2, F_C3, F_C4, F_C5, 1.0f};
-#pragma unroll 1
-    for (int k = 0; k < 5; ++k) {
-        double c[3];
-        track_eval(tr, k == 4 ? t0 + (double)(n + 1) * dt : t0 + ((double)n + cd[k]) * dt, c);
-        const double hc = (double)h * (double)cf[k];
-        o[3 + k] = make_float4((float)((c[0] - (double)hx) - hc * (double)vx),
-                               (float)((c[1] - (double)hy) - hc * (double)vy),
-                               (float)((c[2] - (double)hz) - hc * (double)vz), 0.f);
-    }
+// Track positions at every stage time of the run, FP64 Hermite -> a hi/lo
+// float pair (two float4).  Slot 5n + s holds c(t0 + (n + c_s) dt) for
+// c = {0, 1/5, 3/10, 4/5, 8/9}; slot 5 n_steps holds c(t0 + n_steps dt).
+__global__ void track_table_kernel(TrackDev tr, double t0, double dt, int32_t n_steps, float4* tab) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t total = 5 * (int64_t)n_steps + 1;
+    if (i >= total) return;
+    int64_t n = i / 5;
+    int s = (int)(i % 5);
+    const double cs[5] = {0.0, SS_C2, SS_C3, SS_C4, SS_C5};
+    double t = t0 + ((double)n + cs[s]) * dt;
+    double c[3];
+    track_eval(tr, t, c);
+    float hx = (float)c[0], hy = (float)c[1], hz = (float)c[2];
+    tab[2 * i] = make_float4(hx, hy, hz, 0.f);
+    tab[2 * i + 1] = make_float4((float)(c[0] - (double)hx), (float)(c[1] - (double)hy), (float)(c[2] - (double)hz), 0.f);
 }
 
 // The rotation (cos, sin)(omega t) and the frame-acceleration gradient at
@@ -207,7 +185,7 @@ static int64_t f32k_workspace(const ss_potential* pot, const ss_stream_cfg* cfg)
     int64_t bytes = 0;
     bool track = false;
     for (int k = 0; k < pot->n_components && k < SS_MAX_COMPONENTS; ++k) track |= pot->comp[k].center == SS_CENTER_TRACK;
-    if (track) bytes += cfg->n_steps * TRACK_ROW * (int64_t)sizeof(float4);
+    if (track) bytes += (5 * cfg->n_steps + 1) * 2 * (int64_t)sizeof(float4);
     bytes = (bytes + 255) / 256 * 256;
     if (has_time_dep(pot)) bytes += (5 * cfg->n_steps + 1) * 2 * (int64_t)sizeof(float4);
     bytes = (bytes + 255) / 256 * 256;
@@ -267,14 +245,12 @@ int ss_stream_f32k(const ss_potential* pot, const ss_stream_cfg* cfg, const doub
     char* ws = (char*)workspace;
     if (P.has_track) {
         float4* tab = (float4*)ws;
-        const int64_t total = cfg->n_steps;
-        if (total > 0) {
-            track_table_kernel<<<(unsigned)((total + 127) / 128), 128, 0, s>>>(P.track, cfg->t0, cfg->dt, a.h_hi,
-                                                                               (int32_t)cfg->n_steps, tab);
-            SS_LAUNCH_CHECK();
-        }
+        int64_t total = 5 * cfg->n_steps + 1;
+        track_table_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(P.track, cfg->t0, cfg->dt,
+                                                                            (int32_t)cfg->n_steps, tab);
+        SS_LAUNCH_CHECK();
         a.ctab = tab;
-        ws += (total * TRACK_ROW * (int64_t)sizeof(float4) + 255) / 256 * 256;
+        ws += (total * 2 * (int64_t)sizeof(float4) + 255) / 256 * 256;
     }
     if (has_time_dep(pot)) {
         float4* tab = (float4*)ws;

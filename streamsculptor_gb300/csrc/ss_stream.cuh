@@ -27,7 +27,7 @@ struct StreamArgs {
     // f32k only
     float h_hi;
     float h_lo;
-    const float4* ctab;   // [n_steps x TRACK_ROW] center track per step (track_table_kernel)
+    const float4* ctab;   // [(n_steps*5+1) x 2] track positions (hi, lo) at stage times
     const float4* shtab;  // [n_sh*3] subhalo lines
     const float4* ttab;   // [(n_steps*5+1) x 2] (cos, sin, ga.x, ga.y), (ga.z, -, -, -) at stage times
     int32_t n_sh;
@@ -154,42 +154,26 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     e = (a - (s - bb)) + (b - bb);
 }
 
-// float4 per step of the FP32 kernels' center-track table (ss_stream.cu,
-// track_table_kernel): c_hi(t_n); v_n; E for the six stages.
-constexpr int TRACK_ROW = 8;
-
-// The particle's separation from the center track at step n in parts that
-// stay small near the center: SA = x_hi - c_hi (exact when close, by
-// Sterbenz) and DV = v_hi - v_n.  At a stage with position offset
-// x_lo + h (c v_hi + T) from x_hi the separation is
-// SA + ((x_lo + h (c DV + T)) - E) with E the table's stage row.
-struct TrackRel {
-    float SA[3], DV[3];
-    const float4* row;
-};
-
-__device__ __forceinline__ void track_rel(const StreamArgs& a, int n, const float xh[3], const float vh[3],
-                                          TrackRel& r) {
-    r.row = a.ctab + TRACK_ROW * (int64_t)n;
-    const float4 ch = __ldg(r.row), vp = __ldg(r.row + 1);
-    r.SA[0] = xh[0] - ch.x, r.SA[1] = xh[1] - ch.y, r.SA[2] = xh[2] - ch.z;
-    r.DV[0] = vh[0] - vp.x, r.DV[1] = vh[1] - vp.y, r.DV[2] = vh[2] - vp.z;
-}
-
-// Acceleration at the stage position X = xh + D (D: the small remainder of
-// the stage offset); components on the center track take xs_in, the
-// separation the caller formed from TrackRel.  SUB: the run's subhalos —
-// SUB_NONE, SUB_LINES (Plummer / Hernquist) or SUB_GRID (tabulated).  The
-// kernels are instantiated per case, so a run carries only the subhalo code
-// it uses: the six force evaluations of a step are inlined, and a compact
-// step issues measurably fewer instructions.
+// Acceleration at the stage position xh + d (xh: the particle's hi part,
+// d: the small remainder of the stage offset).  Components on the center
+// track use (xh - c_hi) + (d - c_lo): xh and c_hi are close, so the
+// difference is exact and the separation keeps its relative precision.
+// SUB: the run's subhalos — SUB_NONE, SUB_LINES (Plummer / Hernquist) or
+// SUB_GRID (tabulated).  The kernels are instantiated per case, so a run
+// carries only the subhalo code it uses: the six force evaluations of a
+// step are inlined, and a compact step issues measurably fewer instructions.
 template <class C, int SUB = SUB_LINES>
 __device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamArgs& a, const float xh[3],
-                                          const float D[3], const float xs_in[3], int slot, float trel, float A[3],
-                                          int shb, int she) {
-    const float X[3] = {xh[0] + D[0], xh[1] + D[1], xh[2] + D[2]};
-    const bool trk = C::uses_track(P);
-    const float xs[3] = {trk ? xs_in[0] : X[0], trk ? xs_in[1] : X[1], trk ? xs_in[2] : X[2]};
+                                          const float d[3], int slot, float trel, float A[3], int shb, int she) {
+    const float X[3] = {xh[0] + d[0], xh[1] + d[1], xh[2] + d[2]};
+    float xs[3] = {X[0], X[1], X[2]};
+    if (C::uses_track(P)) {
+        const float4 ch = __ldg(a.ctab + 2 * slot);
+        const float4 cl = __ldg(a.ctab + 2 * slot + 1);
+        xs[0] = (xh[0] - ch.x) + (d[0] - cl.x);
+        xs[1] = (xh[1] - ch.y) + (d[1] - cl.y);
+        xs[2] = (xh[2] - ch.z) + (d[2] - cl.z);
+    }
     float g[3];
     TimeDep<float> td;  // read by rotating / frame-accelerated components only
     if (a.ttab) {
@@ -231,23 +215,6 @@ __device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamAr
     A[2] = -g[2];
 }
 
-// Stage position offset D = xl + h (c vh + T) and, on a center track, the
-// separation SA + ((xl + h (c DV + T)) - E_k); k: the table's stage row
-// (1..5; row 0 is the first stage's, c = 0).
-template <class C>
-__device__ __forceinline__ void stage_point(const PotDev<float>& P, const TrackRel& tr, float h, float c, int k,
-                                            const float xl[3], const float vh[3], const float T[3], float D[3],
-                                            float xs[3]) {
-#pragma unroll
-    for (int i = 0; i < 3; ++i) D[i] = xl[i] + h * fmaf(c, vh[i], T[i]);
-    if (C::uses_track(P)) {
-        const float4 E = __ldg(tr.row + 2 + k);
-        const float e[3] = {E.x, E.y, E.z};
-#pragma unroll
-        for (int i = 0; i < 3; ++i) xs[i] = tr.SA[i] + (fmaf(h, fmaf(c, tr.DV[i], T[i]), xl[i]) - e[i]);
-    }
-}
-
 // One compensated step.  V_i = vh + d_i and sum_j a_ij = c_i, sum_i b_i = 1
 // are used exactly, so only the small parts d_i and A_i - A_1 see the
 // rounded tableau.
@@ -262,56 +229,46 @@ __device__ __forceinline__ void step_f32k(const PotDev<float>& P, const StreamAr
     const int s0 = 5 * n;
     float A1[3], A2[3], A3[3], A4[3], A5[3], A6[3];
     float d1[3], d2[3], d3[3], d4[3], d5[3], d6[3];
-    float D[3], xs[3], T[3];  // stage offset from xh (small); separation from the center track
-    TrackRel tr;
-    if (C::uses_track(P)) {
-        track_rel(a, n, xh, vh, tr);
-        const float4 E = __ldg(tr.row + 2);
-        xs[0] = tr.SA[0] + (xl[0] - E.x), xs[1] = tr.SA[1] + (xl[1] - E.y), xs[2] = tr.SA[2] + (xl[2] - E.z);
-    }
+    float D[3];  // stage position offset from xh (small)
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         D[i] = xl[i];
         d1[i] = vl[i];
     }
-    accel_f32<C, SUB>(P, a, xh, D, xs, s0, tn, A1, shb, she);
+    accel_f32<C, SUB>(P, a, xh, D, s0, tn, A1, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d2[i] = vl[i] + h * (F_(SS_A21) * A1[i]);
-        T[i] = F_(SS_A21) * d1[i];
+        D[i] = xl[i] + h * (F_C2 * vh[i] + F_(SS_A21) * d1[i]);
     }
-    stage_point<C>(P, tr, h, F_C2, 1, xl, vh, T, D, xs);
-    accel_f32<C, SUB>(P, a, xh, D, xs, s0 + 1, tn + F_C2 * h, A2, shb, she);
+    accel_f32<C, SUB>(P, a, xh, D, s0 + 1, tn + F_C2 * h, A2, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d3[i] = vl[i] + h * (F_(SS_A31) * A1[i] + F_(SS_A32) * A2[i]);
-        T[i] = F_(SS_A31) * d1[i] + F_(SS_A32) * d2[i];
+        D[i] = xl[i] + h * (F_C3 * vh[i] + F_(SS_A31) * d1[i] + F_(SS_A32) * d2[i]);
     }
-    stage_point<C>(P, tr, h, F_C3, 2, xl, vh, T, D, xs);
-    accel_f32<C, SUB>(P, a, xh, D, xs, s0 + 2, tn + F_C3 * h, A3, shb, she);
+    accel_f32<C, SUB>(P, a, xh, D, s0 + 2, tn + F_C3 * h, A3, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d4[i] = vl[i] + h * (F_(SS_A41) * A1[i] + F_(SS_A42) * A2[i] + F_(SS_A43) * A3[i]);
-        T[i] = F_(SS_A41) * d1[i] + F_(SS_A42) * d2[i] + F_(SS_A43) * d3[i];
+        D[i] = xl[i] + h * (F_C4 * vh[i] + F_(SS_A41) * d1[i] + F_(SS_A42) * d2[i] + F_(SS_A43) * d3[i]);
     }
-    stage_point<C>(P, tr, h, F_C4, 3, xl, vh, T, D, xs);
-    accel_f32<C, SUB>(P, a, xh, D, xs, s0 + 3, tn + F_C4 * h, A4, shb, she);
+    accel_f32<C, SUB>(P, a, xh, D, s0 + 3, tn + F_C4 * h, A4, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d5[i] = vl[i] + h * (F_(SS_A51) * A1[i] + F_(SS_A52) * A2[i] + F_(SS_A53) * A3[i] + F_(SS_A54) * A4[i]);
-        T[i] = F_(SS_A51) * d1[i] + F_(SS_A52) * d2[i] + F_(SS_A53) * d3[i] + F_(SS_A54) * d4[i];
+        D[i] = xl[i] + h * (F_C5 * vh[i] + F_(SS_A51) * d1[i] + F_(SS_A52) * d2[i] + F_(SS_A53) * d3[i] +
+                            F_(SS_A54) * d4[i]);
     }
-    stage_point<C>(P, tr, h, F_C5, 4, xl, vh, T, D, xs);
-    accel_f32<C, SUB>(P, a, xh, D, xs, s0 + 4, tn + F_C5 * h, A5, shb, she);
+    accel_f32<C, SUB>(P, a, xh, D, s0 + 4, tn + F_C5 * h, A5, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         d6[i] = vl[i] + h * (F_(SS_A61) * A1[i] + F_(SS_A62) * A2[i] + F_(SS_A63) * A3[i] + F_(SS_A64) * A4[i] +
                              F_(SS_A65) * A5[i]);
-        T[i] = F_(SS_A61) * d1[i] + F_(SS_A62) * d2[i] + F_(SS_A63) * d3[i] + F_(SS_A64) * d4[i] +
-               F_(SS_A65) * d5[i];
+        D[i] = xl[i] + h * (vh[i] + F_(SS_A61) * d1[i] + F_(SS_A62) * d2[i] + F_(SS_A63) * d3[i] +
+                            F_(SS_A64) * d4[i] + F_(SS_A65) * d5[i]);
     }
-    stage_point<C>(P, tr, h, 1.0f, 5, xl, vh, T, D, xs);
-    accel_f32<C, SUB>(P, a, xh, D, xs, s0 + 5, tn + h, A6, shb, she);
+    accel_f32<C, SUB>(P, a, xh, D, s0 + 5, tn + h, A6, shb, she);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         // position: h * (vh + Db), Db = sum b_i d_i

@@ -173,35 +173,17 @@ struct PairComp {
     static constexpr bool ok = false;
 };
 
-// The separation from the center track, (xh - c_hi) + Q, is formed only
-// where a component on the track is evaluated, so that Q (small) rather
-// than the separation is what stays live across the other components.
-// row: the step's table row (c_hi first; ss_stream.cu, track_table_kernel).
-template <int KC>
-__device__ __forceinline__ void kind_grad2_at(const PotDev<float>& P, int i, const f2 x[3], const f2 xh[3],
-                                              const f2 Q[3], const float4* row, f2 g[3]) {
-    if constexpr ((KC >> 4) != 0) {
-        const float4 ch = __ldg(row);
-        const f2 xs[3] = {add2(sub2(xh[0], bc(ch.x)), Q[0]), add2(sub2(xh[1], bc(ch.y)), Q[1]),
-                          add2(sub2(xh[2], bc(ch.z)), Q[2])};
-        kind_grad2<(KC & 15)>(P.c[i].q, xs, g);
-    } else {
-        kind_grad2<(KC & 15)>(P.c[i].q, x, g);
-    }
-}
-
 template <int... KCS>
 struct PairComp<Comp<KCS...>> {
     static constexpr bool ok = (PairKind<(KCS & 15)>::ok && ...);
     template <int... I>
-    static __device__ __forceinline__ void add(const PotDev<float>& P, const f2 x[3], const f2 xh[3], const f2 Q[3],
-                                               const float4* row, f2 g[3], std::integer_sequence<int, I...>) {
-        (kind_grad2_at<KCS>(P, I, x, xh, Q, row, g), ...);
+    static __device__ __forceinline__ void add(const PotDev<float>& P, const f2 x[3], const f2 xs[3], f2 g[3],
+                                               std::integer_sequence<int, I...>) {
+        (kind_grad2<(KCS & 15)>(P.c[I].q, (KCS >> 4) ? xs : x, g), ...);
     }
-    static __device__ __forceinline__ void grad(const PotDev<float>& P, const f2 x[3], const f2 xh[3], const f2 Q[3],
-                                                const float4* row, f2 g[3]) {
+    static __device__ __forceinline__ void grad(const PotDev<float>& P, const f2 x[3], const f2 xs[3], f2 g[3]) {
         g[0] = g[1] = g[2] = make_float2(0.0f, 0.0f);
-        add(P, x, xh, Q, row, g, std::make_integer_sequence<int, sizeof...(KCS)>{});
+        add(P, x, xs, g, std::make_integer_sequence<int, sizeof...(KCS)>{});
     }
 };
 
@@ -238,32 +220,23 @@ __device__ __forceinline__ void subhalo_lines2(const StreamArgs& a, const f2 X[3
     }
 }
 
-// grad Phi (not the acceleration) at the stage position X; on a center
-// track the separation is (xh - c_hi) + Q (see stage_point2).  SUB_LINES
-// adds the subhalo lines [shb, she) at stage time trel.
+// grad Phi (not the acceleration) at the stage position xh + d; see
+// accel_f32 for the center-track difference.  SUB_LINES adds the subhalo
+// lines [shb, she) at stage time trel.
 template <class C, int SUB>
-__device__ __forceinline__ void grad2_at(const PotDev<float>& P, const StreamArgs& a, const f2 X[3], const f2 xh[3],
-                                         const f2 Q[3], const float4* row, float trel, int shb, int she, f2 g[3]) {
-    PairComp<C>::grad(P, X, xh, Q, row, g);
-    if constexpr (SUB == SUB_LINES) subhalo_lines2(a, X, trel, shb, she, g);
-}
-
-// Stage point of both lanes at step n: X = xh + (xl + H (c vh + T)) and, on
-// a center track (table row `row`), the small part of the separation
-// Q = (xl + H (c (vh - v_n) + T)) - E_k (k = 1..5, the stage row; the
-// separation is (xh - c_hi) + Q, see TrackRel in ss_stream.cuh).
-template <class C>
-__device__ __forceinline__ void stage_point2(const PotDev<float>& P, const float4* row, f2 H, float c, int k,
-                                             const f2 xh[3], const f2 xl[3], const f2 vh[3], const f2 T[3], f2 X[3],
-                                             f2 Q[3]) {
-#pragma unroll
-    for (int i = 0; i < 3; ++i) X[i] = add2(xh[i], fma2(H, fma2(bc(c), vh[i], T[i]), xl[i]));
+__device__ __forceinline__ void grad2_at(const PotDev<float>& P, const StreamArgs& a, const f2 xh[3], const f2 d[3],
+                                         int slot, float trel, int shb, int she, f2 g[3]) {
+    const f2 X[3] = {add2(xh[0], d[0]), add2(xh[1], d[1]), add2(xh[2], d[2])};
+    f2 xs[3] = {X[0], X[1], X[2]};
     if (C::uses_track(P)) {
-        const float4 vp = __ldg(row + 1), E = __ldg(row + 2 + k);
-        const float v[3] = {vp.x, vp.y, vp.z}, e[3] = {E.x, E.y, E.z};
-#pragma unroll
-        for (int i = 0; i < 3; ++i) Q[i] = sub2(fma2(H, fma2(bc(c), sub2(vh[i], bc(v[i])), T[i]), xl[i]), bc(e[i]));
+        const float4 ch = __ldg(a.ctab + 2 * slot);
+        const float4 cl = __ldg(a.ctab + 2 * slot + 1);
+        xs[0] = add2(sub2(xh[0], bc(ch.x)), sub2(d[0], bc(cl.x)));
+        xs[1] = add2(sub2(xh[1], bc(ch.y)), sub2(d[1], bc(cl.y)));
+        xs[2] = add2(sub2(xh[2], bc(ch.z)), sub2(d[2], bc(cl.z)));
     }
+    PairComp<C>::grad(P, X, xs, g);
+    if constexpr (SUB == SUB_LINES) subhalo_lines2(a, X, trel, shb, she, g);
 }
 
 __device__ __forceinline__ void two_sum2(f2 a, f2 b, f2& s, f2& e) {
@@ -305,46 +278,37 @@ template <class C, int SUB>
 __device__ __forceinline__ void step2_f32k(const PotDev<float>& P, const StreamArgs& a, int n, f2 H, f2 HLO,
                                            f2 xh[3], f2 xl[3], f2 vh[3], f2 vl[3], int shb, int she) {
     const f2 NH = neg2(H);
+    const int s0 = 5 * n;
     const float h = a.h_hi;
     const float tn = (float)n * h;  // time since global step 0 (subhalo lines)
-    f2 G1[3], G2[3], G3[3], G4[3], G[3], X[3], Q[3], T[3];
+    f2 G1[3], G2[3], G3[3], G4[3], G[3], D[3];
     f2 Sv[3], Sb[3];  // sum_{i>=3} b_i (G_i - G1) and sum_k bbar_k G_k
-    // the step's track row, formed where it is read (no register kept for it)
-#define SS_ROW (a.ctab + TRACK_ROW * n)
-    // stage 1: X = xh + xl, Q = xl - E_0
+    grad2_at<C, SUB>(P, a, xh, xl, s0, tn, shb, she, G1);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) X[i] = add2(xh[i], xl[i]);
-    if (C::uses_track(P)) {
-        const float4 E = __ldg(SS_ROW + 2);
-        const float e[3] = {E.x, E.y, E.z};
+    for (int i = 0; i < 3; ++i) D[i] = fma2(H, fma2(bc(F_C2), vh[i], mul2(bc(F_C2), vl[i])), xl[i]);
+    grad2_at<C, SUB>(P, a, xh, D, s0 + 1, tn + F_C2 * h, shb, she, G2);
 #pragma unroll
-        for (int i = 0; i < 3; ++i) Q[i] = sub2(xl[i], bc(e[i]));
+    for (int i = 0; i < 3; ++i) {
+        const f2 T = fma2(NH, mul2(bc(F_(SS_N31)), G1[i]), mul2(bc(F_C3), vl[i]));
+        D[i] = fma2(H, fma2(bc(F_C3), vh[i], T), xl[i]);
     }
-    grad2_at<C, SUB>(P, a, X, xh, Q, SS_ROW, tn, shb, she, G1);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) T[i] = mul2(bc(F_C2), vl[i]);
-    stage_point2<C>(P, SS_ROW, H, F_C2, 1, xh, xl, vh, T, X, Q);
-    grad2_at<C, SUB>(P, a, X, xh, Q, SS_ROW, tn + F_C2 * h, shb, she, G2);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) T[i] = fma2(NH, mul2(bc(F_(SS_N31)), G1[i]), mul2(bc(F_C3), vl[i]));
-    stage_point2<C>(P, SS_ROW, H, F_C3, 2, xh, xl, vh, T, X, Q);
-    grad2_at<C, SUB>(P, a, X, xh, Q, SS_ROW, tn + F_C3 * h, shb, she, G3);
+    grad2_at<C, SUB>(P, a, xh, D, s0 + 2, tn + F_C3 * h, shb, she, G3);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         Sv[i] = mul2(bc(F_(SS_B3)), sub2(G3[i], G1[i]));
         const f2 S = fma2(bc(F_(SS_N42)), G2[i], mul2(bc(F_(SS_N41)), G1[i]));
-        T[i] = fma2(NH, S, mul2(bc(F_C4), vl[i]));
+        const f2 T = fma2(NH, S, mul2(bc(F_C4), vl[i]));
+        D[i] = fma2(H, fma2(bc(F_C4), vh[i], T), xl[i]);
     }
-    stage_point2<C>(P, SS_ROW, H, F_C4, 3, xh, xl, vh, T, X, Q);
-    grad2_at<C, SUB>(P, a, X, xh, Q, SS_ROW, tn + F_C4 * h, shb, she, G4);
+    grad2_at<C, SUB>(P, a, xh, D, s0 + 3, tn + F_C4 * h, shb, she, G4);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         Sv[i] = fma2(bc(F_(SS_B4)), sub2(G4[i], G1[i]), Sv[i]);
         const f2 S = fma2(bc(F_(SS_N53)), G3[i], fma2(bc(F_(SS_N52)), G2[i], mul2(bc(F_(SS_N51)), G1[i])));
-        T[i] = fma2(NH, S, mul2(bc(F_C5), vl[i]));
+        const f2 T = fma2(NH, S, mul2(bc(F_C5), vl[i]));
+        D[i] = fma2(H, fma2(bc(F_C5), vh[i], T), xl[i]);
     }
-    stage_point2<C>(P, SS_ROW, H, F_C5, 4, xh, xl, vh, T, X, Q);
-    grad2_at<C, SUB>(P, a, X, xh, Q, SS_ROW, tn + F_C5 * h, shb, she, G);  // G5
+    grad2_at<C, SUB>(P, a, xh, D, s0 + 4, tn + F_C5 * h, shb, she, G);  // G5
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         Sv[i] = fma2(bc(F_(SS_B5)), sub2(G[i], G1[i]), Sv[i]);
@@ -353,11 +317,10 @@ __device__ __forceinline__ void step2_f32k(const PotDev<float>& P, const StreamA
                           fma2(bc(F_(SS_NB3)), G3[i], fma2(bc(F_(SS_NB2)), G2[i], mul2(bc(F_(SS_NB1)), G1[i])))));
         const f2 S = fma2(bc(F_(SS_N64)), G4[i],
                           fma2(bc(F_(SS_N63)), G3[i], fma2(bc(F_(SS_N62)), G2[i], mul2(bc(F_(SS_N61)), G1[i]))));
-        T[i] = fma2(NH, S, vl[i]);  // c_6 = 1
+        const f2 T = fma2(NH, S, vl[i]);  // c_6 = 1
+        D[i] = fma2(H, add2(vh[i], T), xl[i]);
     }
-    stage_point2<C>(P, SS_ROW, H, 1.0f, 5, xh, xl, vh, T, X, Q);
-    grad2_at<C, SUB>(P, a, X, xh, Q, SS_ROW, tn + h, shb, she, G);  // G6
-#undef SS_ROW
+    grad2_at<C, SUB>(P, a, xh, D, s0 + 5, tn + h, shb, she, G);  // G6
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         // position: h (vh + Db), Db = vl + h sum_k bbar_k A_k
