@@ -549,6 +549,24 @@ int64_t ss_stream_mlp_workspace_bytes(const ss_stream_cfg* cfg);
 int ss_stream_mlp_bf16(const ss_mlp* mlp, const ss_stream_cfg* cfg, const double* ics, double* final_w,
                        float* snaps, int32_t* status, void* workspace, int64_t workspace_bytes, void* stream);
 
+/* The same with the exact potential kept as error judge and fallback (the
+ * force it replaces is Potential.gradient, main.py:37-40): every
+ * judge_every steps of each 128-particle tile, the first stage's surrogate
+ * force is compared with `exact`'s force (FP32, CUDA cores) for every
+ * particle of the tile; if any |g_mlp - g_exact| > tol |g_exact|, that
+ * evaluation takes the exact force and the tile integrates with the exact
+ * force for the rest of the run.  fallbacks (device int64, optional; not
+ * zeroed by the call) is incremented once per tile that fell back.  exact:
+ * a static potential of the analytic kinds and/or an l_max = 8 expansion
+ * (no center track, subhalos or rotation).  Workspace:
+ * ss_stream_mlp_judged_workspace_bytes(exact, cfg) (the expansion's FP32
+ * interval table), 256-byte aligned. */
+int64_t ss_stream_mlp_judged_workspace_bytes(const ss_potential* exact, const ss_stream_cfg* cfg);
+int ss_stream_mlp_judged_bf16(const ss_mlp* mlp, const ss_potential* exact, const ss_stream_cfg* cfg, float tol,
+                              int32_t judge_every, const double* ics, double* final_w, float* snaps,
+                              int32_t* status, int64_t* fallbacks, void* workspace, int64_t workspace_bytes,
+                              void* stream);
+
 #ifdef __cplusplus
 }
 #endif

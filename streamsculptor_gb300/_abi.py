@@ -163,6 +163,9 @@ SIGNATURES = {
     "ss_stream_mlp_workspace_bytes": (C.c_int64, [C.POINTER(ss_stream_cfg)]),
     "ss_stream_mlp_bf16": (C.c_int, [C.POINTER(ss_mlp), C.POINTER(ss_stream_cfg), VP, VP, VP, VP, VP, C.c_int64,
                                      VP]),
+    "ss_stream_mlp_judged_workspace_bytes": (C.c_int64, [C.POINTER(ss_potential), C.POINTER(ss_stream_cfg)]),
+    "ss_stream_mlp_judged_bf16": (C.c_int, [C.POINTER(ss_mlp), C.POINTER(ss_potential), C.POINTER(ss_stream_cfg),
+                                            C.c_float, C.c_int32, VP, VP, VP, VP, VP, VP, C.c_int64, VP]),
 }
 
 HERE = os.path.dirname(os.path.abspath(__file__))

@@ -400,7 +400,12 @@ def aligned_ptr(buf: Optional[torch.Tensor], align: int = 256):
 STREAM_EVENTS = None
 
 
-def stream(P, cfg, ics: torch.Tensor, precision: str, want_final=True, snaps=None, status=True, mlp=None):
+def stream(P, cfg, ics: torch.Tensor, precision: str, want_final=True, snaps=None, status=True, mlp=None,
+           judge=None):
+    """One stream launch.  precision 'mlp' integrates in the surrogate's force
+    (mlp); with judge = dict(tol=, every=) the potential P is kept as its error
+    judge and fallback (ss_stream_mlp_judged_bf16) and judge['fallbacks'] /
+    judge['tiles'] are filled in (reading the count synchronises)."""
     N = cfg.n_particles
     dev = ics.device
     final = torch.empty(N, 6, dtype=torch.float64, device=dev) if want_final else None
@@ -423,8 +428,20 @@ def stream(P, cfg, ics: torch.Tensor, precision: str, want_final=True, snaps=Non
         if mlp is None:
             raise ValueError("precision='mlp' needs a force surrogate")
         m = mlp.struct()
-        _abi.call("ss_stream_mlp_bf16", C.byref(m), C.byref(cfg), ptr(ics), ptr(final), ptr(snaps), ptr(st), None, 0,
-                  stream_handle())
+        if judge is None:
+            _abi.call("ss_stream_mlp_bf16", C.byref(m), C.byref(cfg), ptr(ics), ptr(final), ptr(snaps), ptr(st), None,
+                      0, stream_handle())
+        else:
+            need = _abi.load().ss_stream_mlp_judged_workspace_bytes(C.byref(P), C.byref(cfg))
+            if need < 0:
+                raise _abi.SSError("ss_stream_mlp_judged_workspace_bytes", need, _abi.load().ss_last_error().decode())
+            ws, nb = aligned_ptr(Workspace.get(need, dev, slot="judge"))
+            count = torch.zeros(1, dtype=torch.int64, device=dev)
+            _abi.call("ss_stream_mlp_judged_bf16", C.byref(m), C.byref(P), C.byref(cfg), C.c_float(judge["tol"]),
+                      int(judge.get("every", 64)), ptr(ics), ptr(final), ptr(snaps), ptr(st), ptr(count), ws, nb,
+                      stream_handle())
+            judge["fallbacks_device"] = count
+            judge["tiles"] = (int(N) + 127) // 128
     else:
         raise ValueError("precision must be 'f64', 'f32k' or 'mlp'")
     if evs is not None:
@@ -436,11 +453,25 @@ def stream(P, cfg, ics: torch.Tensor, precision: str, want_final=True, snaps=Non
 _AUX_STREAMS = {}
 
 
-def _aux_stream(dev: torch.device, name: str) -> torch.cuda.Stream:
-    key = (dev.type, dev.index, name)
+def _aux_stream(dev: torch.device, name: str, priority: int = 0) -> torch.cuda.Stream:
+    key = (dev.type, dev.index, name, priority)
     if key not in _AUX_STREAMS:
-        _AUX_STREAMS[key] = torch.cuda.Stream(device=dev)
+        _AUX_STREAMS[key] = torch.cuda.Stream(device=dev, priority=priority)
     return _AUX_STREAMS[key]
+
+
+def _chunk_priorities(n: int):
+    """Stream priorities for n sub-range kernels, the first (its particles
+    released first: the longest tracks) highest: spread over the device's
+    range (lower numbers are higher priorities)."""
+    try:
+        lo, hi = torch.cuda.Stream.priority_range()  # (least, greatest)
+    except (RuntimeError, AttributeError):
+        return [0] * max(1, n)
+    span = lo - hi
+    if n <= 1 or span <= 0:
+        return [hi] * max(1, n)
+    return [hi + (span * i) // (n - 1) for i in range(n)]
 
 
 def host_buffers(n_particles: int, n_snap: int = 0):
@@ -465,12 +496,17 @@ def _check_host_buffers(bufs, N: int, n_snap: int):
 
 
 def stream_to_host(P, cfg, ics: torch.Tensor, precision: str, snap_every: int = 0, mlp=None, n_chunks: int = 8,
-                   n_streams: int = 2, out_buffers=None):
+                   n_streams: int = 0, out_buffers=None):
     """The stream in particle sub-ranges whose results are copied to pinned
-    host memory while later sub-ranges integrate: sub-range kernels alternate
-    between two CUDA streams (so one's last wave overlaps the next one's
-    first), each followed by its copies on a third stream (snapshots move as
-    strided row blocks with ss_copy_rows_async).  Returns pinned host (final
+    host memory while later sub-ranges integrate.  Each sub-range kernel has
+    a CUDA stream of its own (n_streams = 0: one per sub-range), so that none
+    waits in stream order behind another; the streams carry decreasing
+    priorities, so that the block scheduler places the first sub-range (the
+    earliest releases: the longest tracks, which set the run's length) ahead
+    of the others whatever the launch race between streams (without that,
+    a later sub-range taking the SMs first made some runs take twice as
+    long).  Each sub-range's copies follow on a copy stream of its own
+    (snapshots move as strided row blocks with ss_copy_rows_async).  Returns pinned host (final
     [N,6] float64, snapshots [n_snap,N,6] float32 or None) and the device
     status [N]; the host buffers are complete once the current stream is
     synchronised.  out_buffers: caller-owned pinned buffers (host_buffers())
@@ -489,7 +525,10 @@ def stream_to_host(P, cfg, ics: torch.Tensor, precision: str, snap_every: int = 
     else:
         final_h, snaps_h = host_buffers(N, n_snap)
     main = torch.cuda.current_stream(dev)
-    comp = [_aux_stream(dev, f"compute{i}") for i in range(max(1, int(n_streams)))]
+    n_sub = -(-N // max(128, -(-N // max(1, n_chunks) // 128) * 128)) if N > 0 else 1
+    n_cs = int(n_streams) if n_streams else n_sub
+    prios = _chunk_priorities(n_cs)
+    comp = [_aux_stream(dev, f"compute{i}", prios[i]) for i in range(max(1, n_cs))]
     # one copy stream per compute stream: a sub-range's copy never queues
     # behind the copy of a sub-range that is still integrating on the other
     copies = [_aux_stream(dev, f"copy{i}") for i in range(len(comp))]

@@ -26,6 +26,13 @@
 // 0,1,0,1,0,1 in every evaluation.  Every wait is bounded: on a timeout the
 // warpgroup records SS_STATUS_ABORTED for its particles, stops issuing MMAs
 // and the CTA releases its TMEM.
+//
+// The judged form (ss_stream_mlp_judged_bf16) keeps the exact potential as
+// error judge and fallback: every judge_every steps of a tile, the first
+// stage's surrogate force is compared with the exact force (FP32, CUDA
+// cores) for every particle of the tile; if any differs by more than tol
+// relative, that evaluation takes the exact force and the tile integrates
+// with the exact force from then on (no more tensor-core work for it).
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -53,7 +60,9 @@ static constexpr uint32_t SM_TMEM = SM_BAR + 16;      // TMEM base address
 static constexpr uint32_t SM_ABORT = SM_TMEM + 4;     // 2 abort flags
 static constexpr uint32_t SM_START = SM_ABORT + 8;    // 2 tile start steps
 static constexpr uint32_t SM_BASE = SM_START + 8;     // float2 [SS_MLP_BASE_MAX]: the exact spherical part
-static constexpr uint32_t SM_BYTES = SM_BASE + 8 * SS_MLP_BASE_MAX;
+static constexpr uint32_t SM_MODE = SM_BASE + 8 * SS_MLP_BASE_MAX;  // 2 flags: tile on the exact force
+static constexpr uint32_t SM_JUDGE = SM_MODE + 8;     // 2 flags: judge the next force evaluation
+static constexpr uint32_t SM_BYTES = SM_JUDGE + 8;
 static constexpr uint32_t SM_ALLOC = SM_BYTES + 1024;  // slack for the 1024-byte alignment
 
 // TMEM columns within a warpgroup's 256
@@ -392,7 +401,40 @@ struct MlpKernelArgs {
     MlpDev M;
     StreamArgs a;
     int64_t n_tiles;
+    // judged form: the exact potential (analytic kinds and an l_max = 8
+    // expansion with its FP32 table), the tolerance, the judging interval
+    // in steps, the fallback counter (device); judged = 0: surrogate only
+    PotDev<float> X;
+    float tol;
+    int judge_every;
+    int judged;
+    unsigned long long* fallbacks;
 };
+
+// The exact force of the judge, components in list order: the FP32 forms of
+// the stream kernels (kind_grad, shexp_grad_fixed).  Kept out of line so
+// that it does not add to the tensor-core path's registers.
+__device__ __noinline__ void judge_exact_grad(const PotDev<float>& P, float x0, float x1, float x2, float g[3]) {
+    const float x[3] = {x0, x1, x2};
+    g[0] = g[1] = g[2] = 0.0f;
+    for (int i = 0; i < P.n; ++i) {
+        switch (P.c[i].kind) {
+            case SS_SH_EXPANSION: {
+                const Vec3<float> v = shexp_grad_fixed<SS_SHEXP_LMAX>(P.ex, P.c[i].q[0], x0, x1, x2);
+                g[0] += v.x;
+                g[1] += v.y;
+                g[2] += v.z;
+                break;
+            }
+            case SS_NFW: kind_grad<SS_NFW, float, float, false>(P.c[i].q, x, g, nullptr); break;
+            case SS_TRIAXIAL_NFW: kind_grad<SS_TRIAXIAL_NFW, float, float, false>(P.c[i].q, x, g, nullptr); break;
+            case SS_MIYAMOTO_NAGAI: kind_grad<SS_MIYAMOTO_NAGAI, float, float, false>(P.c[i].q, x, g, nullptr); break;
+            case SS_HERNQUIST: kind_grad<SS_HERNQUIST, float, float, false>(P.c[i].q, x, g, nullptr); break;
+            case SS_PLUMMER: kind_grad<SS_PLUMMER, float, float, false>(P.c[i].q, x, g, nullptr); break;
+            default: kind_grad<SS_ISOCHRONE, float, float, false>(P.c[i].q, x, g, nullptr); break;
+        }
+    }
+}
 
 __device__ __forceinline__ const MlpKernelArgs*& mlp_args_ptr() {
     __shared__ const MlpKernelArgs* p;
@@ -410,7 +452,31 @@ __device__ __forceinline__ void MlpComp::grad(const PotDev<R>&, const T x[3], co
     cx.base = smem_u32(sm);
     cx.a_off = SM_A + 32768u * cx.wg;
     const MlpKernelArgs* ka = mlp_args_ptr();
+    volatile uint32_t* mode = reinterpret_cast<volatile uint32_t*>(sm + SM_MODE) + cx.wg;
+    volatile uint32_t* judge = reinterpret_cast<volatile uint32_t*>(sm + SM_JUDGE) + cx.wg;
+    if (*mode) {  // the tile fell back to the exact force
+        judge_exact_grad(ka->X, x[0], x[1], x[2], g);
+        return;
+    }
     mlp_grad_wg(ka->M, cx, x[0], x[1], x[2], g[0], g[1], g[2]);
+    if (*judge) {
+        float ge[3];
+        judge_exact_grad(ka->X, x[0], x[1], x[2], ge);
+        const float d0 = g[0] - ge[0], d1 = g[1] - ge[1], d2 = g[2] - ge[2];
+        const float d2s = d0 * d0 + d1 * d1 + d2 * d2, n2 = ge[0] * ge[0] + ge[1] * ge[1] + ge[2] * ge[2];
+        const bool bad = !(d2s <= ka->tol * ka->tol * n2);  // NaN counts as bad
+        if (wg_sync_or(cx.wg, bad)) {
+            g[0] = ge[0];
+            g[1] = ge[1];
+            g[2] = ge[2];
+            if ((threadIdx.x & 127) == 0) {
+                *mode = 1u;
+                if (ka->fallbacks) atomicAdd(ka->fallbacks, 1ull);
+            }
+        }
+        wg_sync(cx.wg);
+        if ((threadIdx.x & 127) == 0) *judge = 0u;
+    }
 }
 
 // CTA prologue: weights -> shared memory (BF16 core-matrix tiles, FP32
@@ -443,6 +509,10 @@ __device__ __forceinline__ void mlp_cta_setup(const MlpKernelArgs& ka) {
         mlp_args_ptr() = &ka;
         reinterpret_cast<uint32_t*>(sm + SM_ABORT)[0] = 0u;
         reinterpret_cast<uint32_t*>(sm + SM_ABORT)[1] = 0u;
+        for (int w = 0; w < 2; ++w) {
+            reinterpret_cast<uint32_t*>(sm + SM_MODE)[w] = 0u;
+            reinterpret_cast<uint32_t*>(sm + SM_JUDGE)[w] = 0u;
+        }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(sm + SM_BAR)), "r"(1));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(sm + SM_BAR + 8)), "r"(1));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -520,7 +590,13 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) stream_mlp_kernel(const __grid
         const int start = valid ? (int)(((p + a.p_off) / a.ppr) * (int64_t)a.spr) : a.n_steps;
         // the tile steps from its earliest start; particles not yet released
         // step a copy (their rows of the GEMMs are independent)
-        if (t == 0) *s_start = a.n_steps;
+        volatile uint32_t* mode = reinterpret_cast<volatile uint32_t*>(sm + SM_MODE) + wg;
+        volatile uint32_t* judge = reinterpret_cast<volatile uint32_t*>(sm + SM_JUDGE) + wg;
+        if (t == 0) {
+            *s_start = a.n_steps;
+            *mode = 0u;
+            *judge = 0u;
+        }
         wg_sync(wg);
         atomicMin(s_start, start);
         wg_sync(wg);
@@ -543,6 +619,9 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) stream_mlp_kernel(const __grid
         }
         for (int n = tstart; n < a.n_steps; ++n) {
             if (*abort) break;
+            // judged form: the first stage of every judge_every-th step is judged
+            // (read by the warpgroup after the next force's barriers)
+            if (ka.judged && t == 0 && !*mode && (n - tstart) % ka.judge_every == 0) *judge = 1u;
             float th[3], tlo[3], uh[3], ul[3];
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
@@ -632,10 +711,14 @@ int64_t ss_stream_mlp_workspace_bytes(const ss_stream_cfg* cfg) {
     return 0;
 }
 
-int ss_stream_mlp_bf16(const ss_mlp* mlp, const ss_stream_cfg* cfg, const double* ics, double* final_w, float* snaps,
-                       int32_t* status, void* workspace, int64_t workspace_bytes, void* stream) {
-    (void)workspace;
-    (void)workspace_bytes;
+int64_t ss_stream_mlp_judged_workspace_bytes(const ss_potential* exact, const ss_stream_cfg* cfg) {
+    if (exact == nullptr || cfg == nullptr) return set_error(SS_ERR_INVALID_ARGUMENT, "NULL argument");
+    return expansion_table32_bytes(exact);
+}
+
+static int mlp_stream(const ss_mlp* mlp, const ss_potential* exact, const ss_stream_cfg* cfg, float tol,
+                      int32_t judge_every, const double* ics, double* final_w, float* snaps, int32_t* status,
+                      int64_t* fallbacks, void* workspace, int64_t workspace_bytes, void* stream) {
     SS_CHECK_ARG(mlp != nullptr && mlp->params != nullptr, "mlp or its params is NULL");
     SS_CHECK_ARG(cfg != nullptr, "cfg is NULL");
     SS_CHECK_ARG(cfg->n_particles >= 0, "n_particles < 0");
@@ -651,12 +734,43 @@ int ss_stream_mlp_bf16(const ss_mlp* mlp, const ss_stream_cfg* cfg, const double
         (cfg->first_particle + cfg->n_particles + cfg->particles_per_release - 1) / cfg->particles_per_release;
     SS_CHECK_ARG(n_rel == 0 || (n_rel - 1) * (int64_t)cfg->steps_per_release <= cfg->n_steps,
                  "last release starts after n_steps");
-    if (cfg->n_particles == 0) return SS_OK;
-    SS_CHECK_ARG(ics != nullptr, "ics is NULL");
     MlpKernelArgs ka;
     memset(&ka, 0, sizeof(ka));
+    if (exact) {
+        SS_CHECK_ARG(std::isfinite(tol) && tol >= 0.0f, "tol must be finite and >= 0");
+        SS_CHECK_ARG(judge_every >= 1, "judge_every must be >= 1");
+        int rc = prepare_potential<float>(exact, &ka.X, false);
+        if (rc) return rc;
+        SS_CHECK_ARG(!ka.X.has_track && !ka.X.has_rot && !ka.X.has_facc,
+                     "the judge's exact potential must be static, without a center track");
+        for (int k = 0; k < ka.X.n; ++k) {
+            const int kd = ka.X.c[k].kind;
+            if (kd == SS_SH_EXPANSION)
+                SS_CHECK_ARG(ka.X.ex.lmax == SS_SHEXP_LMAX, "the judge evaluates expansions of l_max = %d only",
+                             SS_SHEXP_LMAX);
+            else
+                SS_CHECK_ARG(kd == SS_NFW || kd == SS_TRIAXIAL_NFW || kd == SS_MIYAMOTO_NAGAI || kd == SS_HERNQUIST ||
+                                 kd == SS_PLUMMER || kd == SS_ISOCHRONE,
+                             "component %d: kind %d is not available to the judge", k, kd);
+        }
+        const int64_t need = expansion_table32_bytes(exact);
+        if (need > 0 && (workspace == nullptr || workspace_bytes < need))
+            return set_error(SS_ERR_WORKSPACE, "workspace of %lld bytes needed, %lld given", (long long)need,
+                             (long long)workspace_bytes);
+        SS_CHECK_ARG(need == 0 || ((uintptr_t)workspace % 256) == 0, "workspace must be 256-byte aligned");
+        ka.tol = tol;
+        ka.judge_every = judge_every;
+        ka.judged = 1;
+        ka.fallbacks = reinterpret_cast<unsigned long long*>(fallbacks);
+    }
+    if (cfg->n_particles == 0) return SS_OK;
+    SS_CHECK_ARG(ics != nullptr, "ics is NULL");
     const int rc_m = mlp_dev_of(mlp, &ka.M);
     if (rc_m) return rc_m;
+    if (exact) {
+        const int rc = expansion_table32(ka.X, workspace, (cudaStream_t)stream);
+        if (rc) return rc;
+    }
     StreamArgs& a = ka.a;
     a.ics = ics;
     a.final_w = final_w;
@@ -683,6 +797,20 @@ int ss_stream_mlp_bf16(const ss_mlp* mlp, const ss_stream_cfg* cfg, const double
     stream_mlp_kernel<<<(unsigned)grid, MLP_THREADS, SM_ALLOC, (cudaStream_t)stream>>>(ka);
     SS_LAUNCH_CHECK();
     return SS_OK;
+}
+
+int ss_stream_mlp_bf16(const ss_mlp* mlp, const ss_stream_cfg* cfg, const double* ics, double* final_w, float* snaps,
+                       int32_t* status, void* workspace, int64_t workspace_bytes, void* stream) {
+    return mlp_stream(mlp, nullptr, cfg, 0.0f, 1, ics, final_w, snaps, status, nullptr, workspace, workspace_bytes,
+                      stream);
+}
+
+int ss_stream_mlp_judged_bf16(const ss_mlp* mlp, const ss_potential* exact, const ss_stream_cfg* cfg, float tol,
+                              int32_t judge_every, const double* ics, double* final_w, float* snaps, int32_t* status,
+                              int64_t* fallbacks, void* workspace, int64_t workspace_bytes, void* stream) {
+    SS_CHECK_ARG(exact != nullptr, "exact potential is NULL");
+    return mlp_stream(mlp, exact, cfg, tol, judge_every, ics, final_w, snaps, status, fallbacks, workspace,
+                      workspace_bytes, stream);
 }
 
 }  // extern "C"

@@ -181,6 +181,20 @@ __global__ void expansion_table_kernel(ExpDev E, float4* out) {
     out[i] = make_float4((float)a[0], (float)(a[1] * E.du), (float)b[0], (float)(b[1] * E.du));
 }
 
+int64_t expansion_table32_bytes(const ss_potential* pot) {
+    return has_expansion(pot) ? expansion_table_bytes(pot->expansion) : 0;
+}
+
+int expansion_table32(PotDev<float>& P, void* ws, cudaStream_t s) {
+    if (!P.ex.tab64) return SS_OK;
+    float4* tab = (float4*)ws;
+    const int64_t total = (int64_t)(P.ex.nk - 1) * (P.ex.lmax + 1) * (P.ex.lmax + 1);
+    expansion_table_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(P.ex, tab);
+    SS_LAUNCH_CHECK();
+    P.ex.tab32 = tab;
+    return SS_OK;
+}
+
 static int64_t f32k_workspace(const ss_potential* pot, const ss_stream_cfg* cfg) {
     int64_t bytes = 0;
     bool track = false;

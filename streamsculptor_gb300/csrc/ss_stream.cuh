@@ -46,6 +46,12 @@ struct StreamArgs {
     int32_t sh_per_grp;
 };
 
+// The FP32 per-interval copy of a potential's expansion table (ss_stream.cu):
+// its size in bytes (0 without an expansion), and its construction into
+// `ws` (16-byte aligned) on stream s, which sets P.ex.tab32.
+int64_t expansion_table32_bytes(const ss_potential* pot);
+int expansion_table32(PotDev<float>& P, void* ws, cudaStream_t s);
+
 // Release step of global particle q (its index within its stream picks the
 // release when the run is an ensemble of streams).
 __device__ __forceinline__ int stream_start(const StreamArgs& a, int64_t q) {

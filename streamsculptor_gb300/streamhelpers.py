@@ -40,7 +40,7 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
                kval_arr=1.0, dt=None, dtmax=None, n_particles_per_release=2, normals=None, precision="f64",
                snapshot_every=None, throw=False, release="fardal", prog_pot: Optional[Potential] = None,
                pot_pert: Optional[Potential] = None, prog_in_pert=False, return_ics=False, prog_method="auto",
-               force_surrogate=None, out="device", release_range=None, out_buffers=None):
+               force_surrogate=None, out="device", release_range=None, out_buffers=None, surrogate_judge=None):
     """Generate a particle-spray stream on the GPU.
 
     pot_base    smooth potential (release model and integration)
@@ -57,6 +57,12 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
     out         'device' (CUDA tensors) or 'host': pinned host tensors, the stream
                 run in particle sub-ranges whose results are copied while the
                 next sub-range integrates (ready when the call returns)
+    surrogate_judge (precision='mlp') dict(tol=, every=): keep pot_base as the
+                surrogate's error judge and fallback (ss_stream_mlp_judged_bf16):
+                every `every` steps each 128-particle tile compares its surrogate
+                force with the exact one and falls back to the exact force for
+                good where any particle differs by more than tol (relative);
+                fills in surrogate_judge['fallbacks'] and ['tiles']
     out_buffers (out='host' only) caller-owned pinned host buffers to write
                 into, from _core.host_buffers(N, n_snap): (final [N, 6] float64,
                 snapshots [n_snap, N, 6] float32 or None); repeated calls then
@@ -140,7 +146,12 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
         if snapshot_every:
             n_snap = cfg.n_steps // int(snapshot_every)
             snaps = torch.empty(n_snap, N, 6, dtype=torch.float32, device=ws.device)
-        final, status = _core.stream(integ._desc(), cfg, stream_ics, precision, snaps=snaps, mlp=force_surrogate)
+        if surrogate_judge is not None and precision != "mlp":
+            raise ValueError("surrogate_judge is for precision='mlp'")
+        final, status = _core.stream(integ._desc(), cfg, stream_ics, precision, snaps=snaps, mlp=force_surrogate,
+                                     judge=surrogate_judge)
+        if surrogate_judge is not None:
+            surrogate_judge["fallbacks"] = int(surrogate_judge.pop("fallbacks_device").item())
         if t_end is not None:
             final, status = _tail_phase(integ, cfg, final, status, float(ts_grid[-1]), float(t_end), h, precision,
                                         force_surrogate)

@@ -184,3 +184,30 @@ def test_stream_in_surrogate_force(ss, trained):
     dx = np.linalg.norm(a[:, :3] - b[:, :3], axis=1) / np.linalg.norm(a[:, :3], axis=1)
     print(f"surrogate stream vs exact: median position error {np.median(dx):.2e}, max {dx.max():.2e}")
     assert np.median(dx) < 5e-2
+
+
+def test_judged_surrogate_stream_falls_back_to_the_exact_force(ss, trained):
+    """The exact potential as the surrogate's error judge and fallback
+    (ss_stream_mlp_judged_bf16): with tol = 0 every tile fails its first
+    judgement and integrates with the exact force, which reproduces the
+    exact FP32 stream bit for bit; with a tolerance nothing reaches, no tile
+    falls back and the stream is the plain surrogate stream bit for bit."""
+    from streamsculptor_gb300.streamhelpers import gen_stream
+    pot, s = trained
+    n_rel, ppr = 150, 8
+    back = pot.integrate_orbit(w0=PROG, ts=np.array([0.0, -2.0 * n_rel]), t0=0.0, t1=-2.0 * n_rel, dt=1.0).ys[-1]
+    ts = -2.0 * n_rel + np.arange(n_rel + 1) * 2.0
+    normals = np.random.default_rng(3).standard_normal((n_rel + 1, ppr // 2, 4))
+    kw = dict(normals=normals, dt=1.0, n_particles_per_release=ppr)
+    exact = gen_stream(pot, ts, back, 2e4, precision="f32k", **kw)
+    plain = gen_stream(pot, ts, back, 2e4, precision="mlp", force_surrogate=s, **kw)
+    j0 = dict(tol=0.0, every=64)
+    all_exact = gen_stream(pot, ts, back, 2e4, precision="mlp", force_surrogate=s, surrogate_judge=j0, **kw)
+    jn = dict(tol=1e30, every=16)
+    none = gen_stream(pot, ts, back, 2e4, precision="mlp", force_surrogate=s, surrogate_judge=jn, **kw)
+    assert j0["fallbacks"] == j0["tiles"] == (n_rel * ppr + 127) // 128
+    assert jn["fallbacks"] == 0
+    for a, b in zip(all_exact, exact):
+        assert torch.equal(a, b)
+    for a, b in zip(none, plain):
+        assert torch.equal(a, b)
