@@ -28,11 +28,14 @@
 // and the CTA releases its TMEM.
 //
 // The judged form (ss_stream_mlp_judged_bf16) keeps the exact potential as
-// error judge and fallback: every judge_every steps of a tile, the first
-// stage's surrogate force is compared with the exact force (FP32, CUDA
-// cores) for every particle of the tile; if any differs by more than tol
-// relative, that evaluation takes the exact force and the tile integrates
-// with the exact force from then on (no more tensor-core work for it).
+// error judge and fallback: before every judge_every-th step of a tile, the
+// surrogate's force at the step's first stage point is compared with the
+// exact force (FP32, CUDA cores) for every particle of the tile; if any
+// differs by more than tol relative, the tile integrates with the exact
+// force from that step on (no more tensor-core work for it).  The judgement
+// sits between steps, where the warpgroup is converged, and the decision is
+// warpgroup-uniform (a barrier reduction), so the tensor-core path runs
+// unchanged for tiles that pass.
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -60,9 +63,7 @@ static constexpr uint32_t SM_TMEM = SM_BAR + 16;      // TMEM base address
 static constexpr uint32_t SM_ABORT = SM_TMEM + 4;     // 2 abort flags
 static constexpr uint32_t SM_START = SM_ABORT + 8;    // 2 tile start steps
 static constexpr uint32_t SM_BASE = SM_START + 8;     // float2 [SS_MLP_BASE_MAX]: the exact spherical part
-static constexpr uint32_t SM_MODE = SM_BASE + 8 * SS_MLP_BASE_MAX;  // 2 flags: tile on the exact force
-static constexpr uint32_t SM_JUDGE = SM_MODE + 8;     // 2 flags: judge the next force evaluation
-static constexpr uint32_t SM_BYTES = SM_JUDGE + 8;
+static constexpr uint32_t SM_BYTES = SM_BASE + 8 * SS_MLP_BASE_MAX;
 static constexpr uint32_t SM_ALLOC = SM_BYTES + 1024;  // slack for the 1024-byte alignment
 
 // TMEM columns within a warpgroup's 256
@@ -452,32 +453,23 @@ __device__ __forceinline__ void MlpComp::grad(const PotDev<R>&, const T x[3], co
     cx.base = smem_u32(sm);
     cx.a_off = SM_A + 32768u * cx.wg;
     const MlpKernelArgs* ka = mlp_args_ptr();
-    volatile uint32_t* mode = reinterpret_cast<volatile uint32_t*>(sm + SM_MODE) + cx.wg;
-    volatile uint32_t* judge = reinterpret_cast<volatile uint32_t*>(sm + SM_JUDGE) + cx.wg;
-    if (*mode) {  // the tile fell back to the exact force
-        judge_exact_grad(ka->X, x[0], x[1], x[2], g);
-        return;
-    }
     mlp_grad_wg(ka->M, cx, x[0], x[1], x[2], g[0], g[1], g[2]);
-    if (*judge) {
-        float ge[3];
-        judge_exact_grad(ka->X, x[0], x[1], x[2], ge);
-        const float d0 = g[0] - ge[0], d1 = g[1] - ge[1], d2 = g[2] - ge[2];
-        const float d2s = d0 * d0 + d1 * d1 + d2 * d2, n2 = ge[0] * ge[0] + ge[1] * ge[1] + ge[2] * ge[2];
-        const bool bad = !(d2s <= ka->tol * ka->tol * n2);  // NaN counts as bad
-        if (wg_sync_or(cx.wg, bad)) {
-            g[0] = ge[0];
-            g[1] = ge[1];
-            g[2] = ge[2];
-            if ((threadIdx.x & 127) == 0) {
-                *mode = 1u;
-                if (ka->fallbacks) atomicAdd(ka->fallbacks, 1ull);
-            }
-        }
-        wg_sync(cx.wg);
-        if ((threadIdx.x & 127) == 0) *judge = 0u;
-    }
 }
+
+// The judge's fallback composition for step_f32k: the exact force
+// (judge_exact_grad) of the potential passed as P, no tensor-core work.
+struct ExactComp {
+    static constexpr int n = 1;
+    template <class R>
+    static __device__ __forceinline__ constexpr bool uses_track(const PotDev<R>&) {
+        return false;
+    }
+    template <class T, class R, bool HESS>
+    static __device__ __forceinline__ void grad(const PotDev<R>& P, const T x[3], const T*, T g[3], T*,
+                                                const TimeDep<T>& = TimeDep<T>()) {
+        judge_exact_grad(P, x[0], x[1], x[2], g);
+    }
+};
 
 // CTA prologue: weights -> shared memory (BF16 core-matrix tiles, FP32
 // small parts), mbarrier, 512 TMEM columns.
@@ -509,10 +501,6 @@ __device__ __forceinline__ void mlp_cta_setup(const MlpKernelArgs& ka) {
         mlp_args_ptr() = &ka;
         reinterpret_cast<uint32_t*>(sm + SM_ABORT)[0] = 0u;
         reinterpret_cast<uint32_t*>(sm + SM_ABORT)[1] = 0u;
-        for (int w = 0; w < 2; ++w) {
-            reinterpret_cast<uint32_t*>(sm + SM_MODE)[w] = 0u;
-            reinterpret_cast<uint32_t*>(sm + SM_JUDGE)[w] = 0u;
-        }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(sm + SM_BAR)), "r"(1));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(sm + SM_BAR + 8)), "r"(1));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -590,13 +578,7 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) stream_mlp_kernel(const __grid
         const int start = valid ? (int)(((p + a.p_off) / a.ppr) * (int64_t)a.spr) : a.n_steps;
         // the tile steps from its earliest start; particles not yet released
         // step a copy (their rows of the GEMMs are independent)
-        volatile uint32_t* mode = reinterpret_cast<volatile uint32_t*>(sm + SM_MODE) + wg;
-        volatile uint32_t* judge = reinterpret_cast<volatile uint32_t*>(sm + SM_JUDGE) + wg;
-        if (t == 0) {
-            *s_start = a.n_steps;
-            *mode = 0u;
-            *judge = 0u;
-        }
+        if (t == 0) *s_start = a.n_steps;
         wg_sync(wg);
         atomicMin(s_start, start);
         wg_sync(wg);
@@ -617,11 +599,23 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) stream_mlp_kernel(const __grid
             for (int64_t k = 0; (k + 1) * (int64_t)a.stride <= tstart; ++k)
                 write_snap<float>(a.snaps, a.snap_pitch, k, p + a.p_off, (k + 1) * (int64_t)a.stride >= start, y);
         }
+        bool exact = false;  // the tile fell back to the exact force (uniform over the warpgroup)
         for (int n = tstart; n < a.n_steps; ++n) {
             if (*abort) break;
-            // judged form: the first stage of every judge_every-th step is judged
-            // (read by the warpgroup after the next force's barriers)
-            if (ka.judged && t == 0 && !*mode && (n - tstart) % ka.judge_every == 0) *judge = 1u;
+            if (ka.judged && !exact && (n - tstart) % ka.judge_every == 0) {
+                // judge at the step's first stage point, x_hi + x_lo: the
+                // surrogate's force there against the exact one
+                const float X[3] = {xh[0] + xl[0], xh[1] + xl[1], xh[2] + xl[2]};
+                float gm[3], ge[3];
+                MlpComp::grad<float, float, false>(P, X, X, gm, nullptr);
+                judge_exact_grad(ka.X, X[0], X[1], X[2], ge);
+                const float d0 = gm[0] - ge[0], d1 = gm[1] - ge[1], d2 = gm[2] - ge[2];
+                const float e2 = d0 * d0 + d1 * d1 + d2 * d2, n2 = ge[0] * ge[0] + ge[1] * ge[1] + ge[2] * ge[2];
+                const bool bad = !(e2 <= ka.tol * ka.tol * n2);  // NaN counts as bad
+                exact = wg_sync_or(wg, bad);
+                if (exact && t == 0 && ka.fallbacks) atomicAdd(ka.fallbacks, 1ull);
+                __syncwarp();
+            }
             float th[3], tlo[3], uh[3], ul[3];
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
@@ -630,7 +624,10 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) stream_mlp_kernel(const __grid
                 uh[i] = vh[i];
                 ul[i] = vl[i];
             }
-            step_f32k<MlpComp, SUB_NONE>(P, a, n, th, tlo, uh, ul);  // the surrogate alone: no subhalos
+            if (exact)
+                step_f32k<ExactComp, SUB_NONE>(ka.X, a, n, th, tlo, uh, ul);
+            else
+                step_f32k<MlpComp, SUB_NONE>(P, a, n, th, tlo, uh, ul);  // the surrogate alone: no subhalos
             if (valid && n >= start) {
 #pragma unroll
                 for (int i = 0; i < 3; ++i) {
