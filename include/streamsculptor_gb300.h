@@ -472,7 +472,10 @@ int ss_math_f64(int fn, const double* x, int64_t n, double* out, double* ref, vo
  * into each row of pitch `pitch_bytes` (cudaMemcpy2DAsync, same offset and
  * pitch on both sides): moves a particle sub-range of snapshots
  * [n_snap, N, 6] between device and pinned host memory on `stream`.
- * kind: 0 device -> host, 1 host -> device, 2 device -> device. */
+ * kind: 0 device -> host, 1 host -> device, 2 device -> device (copy
+ * engine); 3 device -> pinned host by a kernel (SM loads and stores: pinned
+ * host memory is addressable from the device under unified addressing; dst
+ * must be pinned host memory, src device memory, else SS_ERR_INVALID_ARGUMENT). */
 int ss_copy_rows_async(void* dst, const void* src, int64_t rows, int64_t pitch_bytes, int64_t offset_bytes,
                        int64_t width_bytes, int kind, void* stream);
 
@@ -551,11 +554,12 @@ int ss_stream_mlp_bf16(const ss_mlp* mlp, const ss_stream_cfg* cfg, const double
 
 /* The same with the exact potential kept as error judge and fallback (the
  * force it replaces is Potential.gradient, main.py:37-40): every
- * judge_every steps of each 128-particle tile, the first stage's surrogate
- * force is compared with `exact`'s force (FP32, CUDA cores) for every
- * particle of the tile; if any |g_mlp - g_exact| > tol |g_exact|, that
- * evaluation takes the exact force and the tile integrates with the exact
- * force for the rest of the run.  fallbacks (device int64, optional; not
+ * judge_every steps of each 128-particle tile (counted from the tile's
+ * first step), the surrogate's force at the step's starting point is
+ * compared with `exact`'s force (FP32, CUDA cores) for every particle of
+ * the tile; if any |g_mlp - g_exact| > tol |g_exact| (or either is not
+ * finite), the tile integrates with the exact force from that step to the
+ * end of the run.  fallbacks (device int64, optional; not
  * zeroed by the call) is incremented once per tile that fell back.  exact:
  * a static potential of the analytic kinds and/or an l_max = 8 expansion
  * (no center track, subhalos or rotation).  Workspace:

@@ -404,8 +404,9 @@ def stream(P, cfg, ics: torch.Tensor, precision: str, want_final=True, snaps=Non
            judge=None):
     """One stream launch.  precision 'mlp' integrates in the surrogate's force
     (mlp); with judge = dict(tol=, every=) the potential P is kept as its error
-    judge and fallback (ss_stream_mlp_judged_bf16) and judge['fallbacks'] /
-    judge['tiles'] are filled in (reading the count synchronises)."""
+    judge and fallback (ss_stream_mlp_judged_bf16): judge['fallbacks_device']
+    receives the device count of tiles that fell back (int64 [1], complete
+    when the current stream is) and judge['tiles'] the number of tiles."""
     N = cfg.n_particles
     dev = ics.device
     final = torch.empty(N, 6, dtype=torch.float64, device=dev) if want_final else None

@@ -8,6 +8,7 @@
 #include <string.h>
 
 #include <atomic>
+#include <algorithm>
 #include <cmath>
 
 #include "ss_release.cuh"
@@ -504,6 +505,56 @@ using namespace ssg;
 
 static inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
+// Device -> pinned host copy by SM stores.  Pinned host memory is
+// addressable from kernels under unified addressing (on Grace-Blackwell
+// over the coherent chip-to-chip link), so a kernel can move a strided row
+// block with plain loads and stores, without the copy engine.  Units of 16,
+// 4 or 1 bytes, the widest that every address, the width and the pitch
+// allow; a grid-stride loop over the rows x units of the block.
+template <class U>
+__global__ void __launch_bounds__(256) copy_rows_kernel(char* __restrict__ dst, const char* __restrict__ src,
+                                                        int64_t rows, int64_t pitch, int64_t off, int64_t units) {
+    const int64_t total = rows * units;
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total;
+         u += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = u / units, c = u - r * units;
+        const int64_t b = r * pitch + off + c * (int64_t)sizeof(U);
+        *reinterpret_cast<U*>(dst + b) = __ldcs(reinterpret_cast<const U*>(src + b));
+    }
+}
+
+static int copy_rows_sm(void* dst, const void* src, int64_t rows, int64_t pitch, int64_t off, int64_t width,
+                        cudaStream_t s) {
+    cudaPointerAttributes ad{}, as{};
+    if (cudaPointerGetAttributes(&ad, dst) != cudaSuccess || cudaPointerGetAttributes(&as, src) != cudaSuccess) {
+        cudaGetLastError();  // not sticky: clear it so that later launch checks do not see it
+        return set_error(SS_ERR_INVALID_ARGUMENT, "kind 3: cannot query the buffers' memory types");
+    }
+    SS_CHECK_ARG(ad.type == cudaMemoryTypeHost && ad.devicePointer != nullptr,
+                 "kind 3: dst must be pinned host memory addressable from the device");
+    SS_CHECK_ARG(as.type == cudaMemoryTypeDevice || as.type == cudaMemoryTypeManaged,
+                 "kind 3: src must be device memory");
+    char* d = static_cast<char*>(ad.devicePointer);
+    const char* sp = static_cast<const char*>(src);
+    auto al = [&](int64_t a) {
+        return ((uintptr_t)d % a) == 0 && ((uintptr_t)sp % a) == 0 && off % a == 0 && width % a == 0 && pitch % a == 0;
+    };
+    int dev = 0, n_sm = 0;
+    SS_CUDA_TRY(cudaGetDevice(&dev));
+    SS_CUDA_TRY(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t ub = al(16) ? 16 : al(4) ? 4 : 1;
+    const int64_t units = width / ub, total = rows * units;
+    const unsigned grid = (unsigned)std::min<int64_t>((total + 255) / 256, 4 * (int64_t)n_sm);
+    if (ub == 16)
+        copy_rows_kernel<uint4><<<grid, 256, 0, s>>>(d, sp, rows, pitch, off, units);
+    else if (ub == 4)
+        copy_rows_kernel<uint32_t><<<grid, 256, 0, s>>>(d, sp, rows, pitch, off, units);
+    else
+        copy_rows_kernel<unsigned char><<<grid, 256, 0, s>>>(d, sp, rows, pitch, off, units);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
 extern "C" {
 
 int ss_abi_version(void) { return SS_ABI_VERSION; }
@@ -517,8 +568,9 @@ int ss_copy_rows_async(void* dst, const void* src, int64_t rows, int64_t pitch_b
     SS_CHECK_ARG(dst != nullptr && src != nullptr, "NULL buffer");
     SS_CHECK_ARG(rows >= 0 && width_bytes >= 0 && offset_bytes >= 0 && offset_bytes + width_bytes <= pitch_bytes,
                  "bad rows/pitch/offset/width");
-    SS_CHECK_ARG(kind >= 0 && kind <= 2, "kind must be 0 (D2H), 1 (H2D) or 2 (D2D)");
+    SS_CHECK_ARG(kind >= 0 && kind <= 3, "kind must be 0 (D2H), 1 (H2D), 2 (D2D) or 3 (D2H by SM stores)");
     if (rows == 0 || width_bytes == 0) return SS_OK;
+    if (kind == 3) return copy_rows_sm(dst, src, rows, pitch_bytes, offset_bytes, width_bytes, (cudaStream_t)stream);
     const cudaMemcpyKind k = kind == 0 ? cudaMemcpyDeviceToHost : kind == 1 ? cudaMemcpyHostToDevice
                                                                              : cudaMemcpyDeviceToDevice;
     SS_CUDA_TRY(cudaMemcpy2DAsync((char*)dst + offset_bytes, (size_t)pitch_bytes, (const char*)src + offset_bytes,

@@ -713,6 +713,29 @@ def test_release_range_equals_whole_stream(ss, oracle, precision):
         assert torch.equal(l, lead[r0:r1]) and torch.equal(t, trail[r0:r1])
 
 
+@pytest.mark.parametrize("precision", ["f64", "f32k"])
+def test_gen_stream_sharded_ranks_tile_the_whole_stream(ss, oracle, precision):
+    """sharding.gen_stream_sharded called as each of 3 ranks would call it
+    (in one process, without the gather): the ranks' release ranges tile the
+    stream in order and each rank's result equals the same releases of the
+    whole stream, bit for bit.  The gather itself is tested on CPU with two
+    gloo ranks (tests/test_sharding.py)."""
+    from streamsculptor_gb300.sharding import gen_stream_sharded
+    from streamsculptor_gb300.streamhelpers import gen_stream
+    n = 300
+    _, back, ts, normals = _c1_setup(oracle, n_rel=n)
+    pot = mw3_gpu(ss)
+    lead, trail = gen_stream(pot, ts, back, 2e4, normals=normals, precision=precision)
+    edge = 0
+    for rank in range(3):
+        l, t, (r0, r1) = gen_stream_sharded(pot, ts, back, 2e4, rank, 3, gather=False, normals=normals,
+                                            precision=precision)
+        assert r0 == edge and r1 > r0
+        assert torch.equal(l, lead[r0:r1]) and torch.equal(t, trail[r0:r1])
+        edge = r1
+    assert edge == n
+
+
 _PAIR_MODELS = {
     "mw3p": None,  # NFW + MN + Hernquist + the moving Plummer progenitor
     "tri3": [("TriaxialNFWPotential", dict(m=3e11, r_s=12.0, q1=1.0, q2=0.9, q3=0.8),
