@@ -486,31 +486,35 @@ def gpu_arm(args, wl):
     normals_pin = torch.as_tensor(s.normals_h).pin_memory()
     host_out = _core.host_buffers(s.N, n_snap)  # caller-owned pinned outputs, reused by every call
 
-    def e2e_step():
-        # public API with host inputs and host outputs: gen_stream(out="host")
-        # integrates in particle sub-ranges and copies each one to pinned host
-        # memory while the next integrates
+    def e2e_step(mode):
+        # public API with host inputs and host outputs: gen_stream(out="host");
+        # "direct": the stream kernel writes its snapshots into the pinned
+        # host buffer; "chunked": particle sub-ranges copied by the copy
+        # engine while the next sub-range integrates
         sol = s.pot.integrate_orbit(w0=WF, ts=np.array([0.0, -s.T]), t0=0.0, t1=-s.T, dt=s.dt)
         out = gen_stream(s.pot, s.ts, sol.ys[-1], MSAT, normals=normals_pin, dt=s.dt, prog_pot=s.prog,
                          n_particles_per_release=s.ppr, precision="f32k", snapshot_every=s.snap or None,
-                         out="host", out_buffers=host_out)
+                         out="host", out_buffers=host_out, host_mode=mode)
         assert not out[0].is_cuda
         torch.cuda.synchronize()
 
-    for _ in range(2):
-        e2e_step()
+    for mode in ("direct", "chunked"):
+        for _ in range(2):
+            e2e_step(mode)
     k_e2e = max(1, min(2 * args.steps, 10))
-    e2e_samples = []
+    e2e_samples, chunked_samples = [], []
     e2e_clk = ClockSampler(gpu_id_for(local))
     e2e_clk.start()
     for _ in range(k_e2e):
-        flush.zero_()
-        torch.cuda.synchronize()
-        barrier()
-        t0 = time.perf_counter()
-        e2e_step()
-        barrier()
-        e2e_samples.append((time.perf_counter() - t0) * 1e3)
+        # the two host paths alternate, so both see the same conditions
+        for mode, dst in (("direct", e2e_samples), ("chunked", chunked_samples)):
+            flush.zero_()
+            torch.cuda.synchronize()
+            barrier()
+            t0 = time.perf_counter()
+            e2e_step(mode)
+            barrier()
+            dst.append((time.perf_counter() - t0) * 1e3)
     e2e_clocks = e2e_clk.stop()
     e2e_s = statistics.mean(e2e_samples) * 1e-3
     if world > 1:
@@ -542,8 +546,13 @@ def gpu_arm(args, wl):
                         "ms_median": statistics.median(e2e_samples), "samples_ms": e2e_samples,
                         "clocks": e2e_clocks,
                         "path": "integrate_orbit + streamhelpers.gen_stream(out='host', out_buffers=...) with "
-                                "pinned host inputs: particle sub-ranges copied into caller-owned pinned host "
-                                "buffers while the next sub-range integrates"},
+                                "pinned host inputs: the stream kernel writes its snapshot rows straight into the "
+                                "caller-owned pinned host buffer, the final states are copied after it",
+                        "chunked": {"ms_mean": statistics.mean(chunked_samples),
+                                    "ms_median": statistics.median(chunked_samples),
+                                    "samples_ms": chunked_samples,
+                                    "path": "gen_stream(out='host', host_mode='chunked'): 8 particle sub-ranges, "
+                                            "each copied by the copy engine while the next integrates"}},
                 "clocks": r32["clocks"], "gpu_launches": r32["launches"],
                 "gpu_launches_per_step": r32["launches"] / args.steps}
     if not args.no_analysis:

@@ -533,6 +533,14 @@ int ss_mlp_loss_grad(const ss_mlp* mlp, const float* x, const float* phi_t, cons
                      const float* w_val, const float* w_force, int64_t batch, float* loss, float* grad,
                      void* workspace, int64_t workspace_bytes, void* stream);
 
+/* Which units run the training's 128-wide products (every ss_mlp_loss_grad
+ * and ss_mlp_eval GEMM with N = 128 and K a multiple of 32): 1 (default) the
+ * tensor cores (tcgen05 kind::tf32, each FP32 operand split into a TF32 head
+ * and remainder, three MMAs per product: FP32 accuracy), 0 the CUDA-core
+ * GEMM.  Other values leave the setting.  Returns the previous setting.
+ * Process-wide: set it between calls, not while a call is in flight. */
+int ss_mlp_train_backend(int tensor_cores);
+
 /* One Adam step (bias-corrected; step counts from 1) on n parameters. */
 int ss_mlp_adam(float* params, const float* grad, float* m, float* v, int64_t n, int64_t step, float lr,
                 float beta1, float beta2, float eps, void* stream);

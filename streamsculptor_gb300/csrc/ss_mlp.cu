@@ -25,6 +25,7 @@
 #include <cstdint>
 
 #include "ss_common.cuh"
+#include "ss_tcgen05.cuh"
 
 namespace ssg {
 
@@ -134,9 +135,23 @@ __global__ void __launch_bounds__(256) gemm_kernel(int M, int N, int K, const fl
     }
 }
 
+// 1: the 128-wide training products on the tensor cores (tc_gemm below);
+// 0: every product on the CUDA-core GEMM (ss_mlp_train_backend)
+static int g_tc_train = 1;
+
+template <bool TA, bool TB, bool ATOMIC>
+static void tc_gemm(int M, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
+                    const float* bias, int splits, cudaStream_t st);
+static bool tc_ok(int N, int K, const float* A, int lda, const float* B, int ldb, const float* C, int ldc,
+                  const float* bias);
+
 template <bool TA, bool TB>
 static void gemm(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
                  const float* bias, cudaStream_t st) {
+    if (g_tc_train && tc_ok(N, K, A, lda, B, ldb, C, ldc, bias)) {
+        tc_gemm<TA, TB, false>(M, K, A, lda, B, ldb, C, ldc, bias, 1, st);
+        return;
+    }
     dim3 grid((N + GB_N - 1) / GB_N, (M + GB_M - 1) / GB_M, 1);
     gemm_kernel<TA, TB, false><<<grid, 256, 0, st>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, K);
     count_launch();
@@ -146,6 +161,11 @@ static void gemm(int M, int N, int K, const float* A, int lda, const float* B, i
 template <bool TA, bool TB>
 static void gemm_acc(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
                      cudaStream_t st) {
+    if (g_tc_train && tc_ok(N, K, A, lda, B, ldb, C, ldc, nullptr)) {
+        // split-K over the batch: K ranges of 128 (four chunks) per CTA
+        tc_gemm<TA, TB, true>(M, K, A, lda, B, ldb, C, ldc, nullptr, (K + 127) / 128, st);
+        return;
+    }
     const int tiles = ((N + GB_N - 1) / GB_N) * ((M + GB_M - 1) / GB_M);
     int splits = (4 * 152 + tiles - 1) / tiles;
     int kchunk = (K + splits - 1) / splits;
@@ -153,6 +173,234 @@ static void gemm_acc(int M, int N, int K, const float* A, int lda, const float* 
     splits = (K + kchunk - 1) / kchunk;
     dim3 grid((N + GB_N - 1) / GB_N, (M + GB_M - 1) / GB_M, splits);
     gemm_kernel<TA, TB, true><<<grid, 256, 0, st>>>(M, N, K, A, lda, B, ldb, C, ldc, nullptr, kchunk);
+    count_launch();
+}
+
+// ------------------------------------------ tensor-core GEMM (N = 128)
+// C[M,128] (= acc + bias, or += acc by atomics for split-K) =
+// op(A)[M,K] op(B)[K,128] with tcgen05.mma kind::tf32 (FP32 accumulation
+// in TMEM).  Every FP32 operand is split into a TF32 head and remainder,
+// a = a_h + a_l (a_h: a with its 13 low mantissa bits cleared, a_l = a - a_h
+// exactly), and the product is a_h b_h + a_h b_l + a_l b_h: the dropped
+// a_l b_l is 2^-22 relative, so the GEMM keeps FP32 accuracy while the
+// tensor cores do the work (three MMAs where a single TF32 one would drop
+// 11 bits of every operand).
+// Operands as in the CUDA-core GEMM: A is [M,K] (lda) or, with TA, [K,M];
+// B is [K,N] (ldb) or, with TB, [N,K] (C = A W^T with W[out][in]).  Both
+// are staged K-major: an operand whose K is not the contiguous index is
+// transposed on the way into shared memory.
+// One CTA of 128 threads per 128-row tile of C (grid.x) and K range
+// (grid.y); K in chunks of 32 staged in shared memory as K-major core
+// matrices (8 rows x 4 elements, 128 bytes), element (r, k) of a 128 x 32
+// chunk at byte (r/8) 1024 + (k/4) 128 + (r%8) 16 + (k%4) 4 (LBO 128,
+// SBO 1024), double-buffered: the threads stage chunk c + 1 while the MMAs
+// of chunk c run.  Warp w reads TMEM lanes 32w..32w+31 (rows of C).  A wait
+// that runs out writes NaN into the CTA's part of C, so the failure reaches
+// the loss.
+constexpr int TC_THREADS = 128, TC_KC = 32;
+constexpr uint32_t TC_OPER = 16384;            // one 128 x 32 FP32 chunk
+constexpr uint32_t TC_BUF = 4 * TC_OPER;       // A_h, A_l, B_h, B_l
+constexpr uint32_t TC_BAR = 2 * TC_BUF;        // 2 mbarriers
+constexpr uint32_t TC_TMEM = TC_BAR + 16;      // TMEM base address
+constexpr uint32_t TC_SMEM = TC_TMEM + 16 + 1024;  // + slack for the 1024-byte alignment
+
+__device__ __forceinline__ uint32_t tc_off(int r, int k) {
+    return (uint32_t)((r >> 3) * 1024 + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4);
+}
+
+__device__ __forceinline__ float tf32_head(float a) { return __uint_as_float(__float_as_uint(a) & 0xffffe000u); }
+
+// stage rows [r0, r0 + 128) x K [k0, k0 + 32) of one operand as head and
+// remainder; rows at or past `rows` are zero
+template <bool T>
+__device__ __forceinline__ void tc_stage(uint8_t* hi, uint8_t* lo, const float* X, int ld, int r0, int rows, int k0) {
+    const int t = threadIdx.x;
+    if (!T) {
+        // float4 along K: 8 consecutive threads take rows r..r+7 at one K
+        // quad (conflict-free 16-byte stores), a warp 8 rows x 64 bytes
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int idx = t + TC_THREADS * i;
+            const int r = ((idx >> 6) << 3) | (idx & 7), kq = (idx >> 3) & 7;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (r0 + r < rows) v = *reinterpret_cast<const float4*>(X + (int64_t)(r0 + r) * ld + k0 + 4 * kq);
+            const float4 h = make_float4(tf32_head(v.x), tf32_head(v.y), tf32_head(v.z), tf32_head(v.w));
+            const uint32_t o = tc_off(r, 4 * kq);
+            *reinterpret_cast<float4*>(hi + o) = h;
+            *reinterpret_cast<float4*>(lo + o) = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+        }
+    } else {
+        // X[k][r]: a 4 x 4 block per thread (four float4 along r at
+        // consecutive k), transposed in registers into four 16-byte stores
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const int idx = t + TC_THREADS * i;
+            const int rq = idx & 31, kq = idx >> 5;
+            const int r = 4 * rq;
+            float4 v[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                v[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+                const float* src = X + (int64_t)(k0 + 4 * kq + j) * ld + r0 + r;
+                if (r0 + r + 3 < rows) {
+                    v[j] = *reinterpret_cast<const float4*>(src);
+                } else {
+                    if (r0 + r < rows) v[j].x = src[0];
+                    if (r0 + r + 1 < rows) v[j].y = src[1];
+                    if (r0 + r + 2 < rows) v[j].z = src[2];
+                }
+            }
+            const float c[4][4] = {{v[0].x, v[1].x, v[2].x, v[3].x},
+                                   {v[0].y, v[1].y, v[2].y, v[3].y},
+                                   {v[0].z, v[1].z, v[2].z, v[3].z},
+                                   {v[0].w, v[1].w, v[2].w, v[3].w}};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float4 w = make_float4(c[q][0], c[q][1], c[q][2], c[q][3]);
+                const float4 h = make_float4(tf32_head(w.x), tf32_head(w.y), tf32_head(w.z), tf32_head(w.w));
+                const uint32_t o = tc_off(r + q, 4 * kq);
+                *reinterpret_cast<float4*>(hi + o) = h;
+                *reinterpret_cast<float4*>(lo + o) = make_float4(w.x - h.x, w.y - h.y, w.z - h.z, w.w - h.w);
+            }
+        }
+    }
+}
+
+template <bool TA, bool TB, bool ATOMIC>
+__global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(int M, int K, const float* __restrict__ A, int lda,
+                                                                const float* __restrict__ B, int ldb, float* C,
+                                                                int ldc, const float* __restrict__ bias, int kchunk) {
+    extern __shared__ uint8_t tc_dyn[];
+    uint8_t* sm = (uint8_t*)(((uintptr_t)tc_dyn + 1023) & ~(uintptr_t)1023);
+    const int t = threadIdx.x, w = t >> 5;
+    const int m0 = blockIdx.x * 128;
+    const int kb = blockIdx.y * kchunk, ke = min(K, kb + kchunk);
+    const int nc = ke > kb ? (ke - kb) / TC_KC : 0;
+    const uint32_t bar0 = smem_u32(sm + TC_BAR), base = smem_u32(sm);
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar0), "r"(1));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar0 + 8), "r"(1));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (w == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(sm + TC_TMEM)),
+                     "r"(128));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (nc > 0) {
+        tc_stage<TA>(sm, sm + TC_OPER, A, lda, m0, M, kb);
+        tc_stage<!TB>(sm + 2 * TC_OPER, sm + 3 * TC_OPER, B, ldb, 0, 128, kb);
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + TC_TMEM);
+    const uint32_t id = idesc_tf32();
+    bool ok = true;
+    for (int c = 0; c < nc; ++c) {
+        const uint32_t b = c & 1, buf = base + b * TC_BUF;
+        fence_async_smem();  // this thread's staged chunk -> the tensor cores' proxy
+        fence_before();
+        __syncthreads();
+        fence_after();
+        if (t == 0) {
+#pragma unroll
+            for (int kk = 0; kk < TC_KC / 8; ++kk) {
+                const uint64_t ah = smem_desc(buf + kk * 256, 128, 1024);
+                const uint64_t al = smem_desc(buf + TC_OPER + kk * 256, 128, 1024);
+                const uint64_t bh = smem_desc(buf + 2 * TC_OPER + kk * 256, 128, 1024);
+                const uint64_t bl = smem_desc(buf + 3 * TC_OPER + kk * 256, 128, 1024);
+                mma_tf32(tmem, ah, bh, id, (c > 0 || kk > 0) ? 1u : 0u);
+                mma_tf32(tmem, ah, bl, id, 1u);
+                mma_tf32(tmem, al, bh, id, 1u);
+            }
+            mma_commit(bar0 + 8 * b);
+        }
+        if (c + 1 < nc) {
+            const uint32_t b1 = (c + 1) & 1;
+            // buffer b1 last fed chunk c - 1: wait for its MMAs
+            if (c >= 1) ok = ok && mbar_wait(bar0 + 8 * b1, (uint32_t)(((c - 1) >> 1) & 1));
+            if (__syncthreads_or(!ok)) {
+                ok = false;
+                break;
+            }
+            uint8_t* nb = sm + b1 * TC_BUF;
+            tc_stage<TA>(nb, nb + TC_OPER, A, lda, m0, M, kb + (c + 1) * TC_KC);
+            tc_stage<!TB>(nb + 2 * TC_OPER, nb + 3 * TC_OPER, B, ldb, 0, 128, kb + (c + 1) * TC_KC);
+        }
+    }
+    if (nc > 0 && ok) ok = mbar_wait(bar0 + 8 * ((nc - 1) & 1), (uint32_t)(((nc - 1) >> 1) & 1));
+    ok = !__syncthreads_or(!ok);
+    fence_after();
+    const int row = m0 + 32 * w + (t & 31);
+    const float qnan = __int_as_float(0x7fc00000);
+    if (nc > 0) {
+#pragma unroll 1
+        for (int q = 0; q < 4; ++q) {
+            uint32_t r[32];
+            SS_TMEM_LD32(r, tmem + ((uint32_t)(32 * w) << 16) + 32 * q);
+            tmem_wait_ld();
+            if (row < M) {
+                float* out = C + (int64_t)row * ldc + 32 * q;
+#pragma unroll
+                for (int j = 0; j < 32; j += 4) {
+                    float4 v = ok ? make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]),
+                                                __uint_as_float(r[j + 2]), __uint_as_float(r[j + 3]))
+                                  : make_float4(qnan, qnan, qnan, qnan);
+                    if (ATOMIC) {
+                        atomicAdd(out + j, v.x);
+                        atomicAdd(out + j + 1, v.y);
+                        atomicAdd(out + j + 2, v.z);
+                        atomicAdd(out + j + 3, v.w);
+                    } else {
+                        if (bias) {
+                            const float4 bb = *reinterpret_cast<const float4*>(bias + 32 * q + j);
+                            v.x += bb.x;
+                            v.y += bb.y;
+                            v.z += bb.z;
+                            v.w += bb.w;
+                        }
+                        *reinterpret_cast<float4*>(out + j) = v;
+                    }
+                }
+            }
+        }
+    }
+    if (!ok && t == 0) {
+        // give the outstanding commits a bounded wait before TMEM is released
+        mbar_wait(bar0, 0u);
+        mbar_wait(bar0 + 8, 0u);
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (w == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128));
+}
+
+// Whether a product can take the tensor-core GEMM: N = 128, K a multiple of
+// 32, 16-byte aligned operands and leading dimensions.
+static bool tc_ok(int N, int K, const float* A, int lda, const float* B, int ldb, const float* C, int ldc,
+                  const float* bias) {
+    auto al = [](const void* p) { return ((uintptr_t)p & 15) == 0; };
+    return N == 128 && K > 0 && K % TC_KC == 0 && lda % 4 == 0 && ldb % 4 == 0 && ldc % 4 == 0 && al(A) && al(B) &&
+           al(C) && (bias == nullptr || al(bias));
+}
+
+template <bool TA, bool TB, bool ATOMIC>
+static void tc_gemm(int M, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
+                    const float* bias, int splits, cudaStream_t st) {
+    static bool attr[64] = {};  // the shared-memory opt-in, once per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && !attr[dev]) {
+        cudaFuncSetAttribute(tc_gemm_kernel<TA, TB, ATOMIC>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+        attr[dev] = true;
+    }
+    int kchunk = (K + splits - 1) / splits;
+    kchunk = (kchunk + TC_KC - 1) / TC_KC * TC_KC;
+    splits = (K + kchunk - 1) / kchunk;
+    dim3 grid((M + 127) / 128, splits);
+    tc_gemm_kernel<TA, TB, ATOMIC><<<grid, TC_THREADS, TC_SMEM, st>>>(M, K, A, lda, B, ldb, C, ldc, bias, kchunk);
     count_launch();
 }
 
@@ -516,6 +764,12 @@ int ss_mlp_loss_grad(const ss_mlp* mlp, const float* x, const float* phi_t, cons
         Dbar = t;
     }
     return SS_OK;
+}
+
+int ss_mlp_train_backend(int tensor_cores) {
+    const int prev = g_tc_train;
+    if (tensor_cores == 0 || tensor_cores == 1) g_tc_train = tensor_cores;
+    return prev;
 }
 
 int ss_mlp_adam(float* params, const float* grad, float* m, float* v, int64_t n, int64_t step, float lr, float beta1,

@@ -98,6 +98,30 @@ __device__ __forceinline__ f2 nfw_F2(f2 u) {
     return F;
 }
 
+// Snapshot rows of the paired kernel: one warp holds 64 consecutive
+// particles (particles 2l and 2l + 1 in lane l), 12 floats per lane and
+// 1536 contiguous bytes per row.  Written per lane as 8-byte pieces, each
+// store instruction covers a third of every 128-byte line it touches; the
+// warp instead stages its row in shared memory (each lane's 48 bytes as
+// three float4, conflict-free at that stride) and writes it back as three
+// stores of 512 contiguous bytes, whole lines, which matters most when the
+// snapshots go straight into pinned host memory.
+#ifndef SS_SNAP_COALESCED
+#define SS_SNAP_COALESCED 1
+#endif
+constexpr int F2_WARPS = 4;  // warps per block of the paired kernel (128 threads)
+
+__device__ __forceinline__ void write_snap_warp(float4* out, float4* stage, float4 f0, float4 f1, float4 f2) {
+    const int l = threadIdx.x & 31;
+    stage[3 * l] = f0;
+    stage[3 * l + 1] = f1;
+    stage[3 * l + 2] = f2;
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 3; ++j) out[32 * j + l] = stage[32 * j + l];
+    __syncwarp();
+}
+
 // grad Phi of one component of kind KIND at x (shifted to its center), added
 // to g: the FP32 forms of kind_grad without the Hessian, with the masses
 // (and NFW's 1 / r_s) restored to FP64 accuracy from their stored FP32
@@ -384,6 +408,9 @@ __global__ void __launch_bounds__(128, 4) stream_f32k2_kernel(PotDev<float> P, S
             if (v1) write_snap<float>(a.snaps, a.snap_pitch, k, p1 + a.p_off, step >= st1, y1);
         }
     }
+#if SS_SNAP_COALESCED
+    __shared__ float4 snap_stage[F2_WARPS][96];  // one 1536-byte snapshot row per warp
+#endif
     int next_snap = (wstart / a.stride + 1) * a.stride;
     for (int n = wstart; n < a.n_steps; ++n) {
         if (v0 && n >= tstart) {
@@ -391,15 +418,34 @@ __global__ void __launch_bounds__(128, 4) stream_f32k2_kernel(PotDev<float> P, S
             const f2 HLO = make_float2(n >= st0 ? a.h_lo : 0.0f, n >= st1 ? a.h_lo : 0.0f);
             step2_f32k<C, SUB>(P, a, n, H, HLO, xh, xl, vh, vl, shb, she);
         }
-        if (n + 1 == next_snap) {
+        if (n + 1 == next_snap) {  // warp-uniform: every lane steps from wstart
             next_snap += a.stride;
-            if (a.snaps && v0) {
+            if (a.snaps) {
                 const int64_t k = (n + 1) / a.stride - 1;
-                const float y0[6] = {xh[0].x, xh[1].x, xh[2].x, vh[0].x, vh[1].x, vh[2].x};
-                write_snap<float>(a.snaps, a.snap_pitch, k, p0 + a.p_off, n + 1 >= st0, y0);
-                if (v1) {
-                    const float y1[6] = {xh[0].y, xh[1].y, xh[2].y, vh[0].y, vh[1].y, vh[2].y};
-                    write_snap<float>(a.snaps, a.snap_pitch, k, p1 + a.p_off, n + 1 >= st1, y1);
+                const bool ex0 = n + 1 >= st0, ex1 = n + 1 >= st1;
+#if SS_SNAP_COALESCED
+                // the row of the warp's 64 consecutive particles; a warp of
+                // 32 full pairs at a 16-byte aligned address writes it in
+                // three coalesced stores
+                float* row = a.snaps + (k * a.snap_pitch + (p0 - 2 * (int64_t)(threadIdx.x & 31)) + a.p_off) * 6;
+                const bool full = blockDim.x <= 32 * F2_WARPS && __all_sync(0xffffffffu, v1) &&
+                                  (reinterpret_cast<uintptr_t>(row) & 15) == 0;
+                if (full) {
+                    const float q = __int_as_float(0x7fc00000);  // NaN: not yet released
+                    write_snap_warp(reinterpret_cast<float4*>(row), snap_stage[threadIdx.x >> 5],
+                                    ex0 ? make_float4(xh[0].x, xh[1].x, xh[2].x, vh[0].x) : make_float4(q, q, q, q),
+                                    make_float4(ex0 ? vh[1].x : q, ex0 ? vh[2].x : q, ex1 ? xh[0].y : q,
+                                                ex1 ? xh[1].y : q),
+                                    ex1 ? make_float4(xh[2].y, vh[0].y, vh[1].y, vh[2].y) : make_float4(q, q, q, q));
+                } else
+#endif
+                if (v0) {
+                    const float y0[6] = {xh[0].x, xh[1].x, xh[2].x, vh[0].x, vh[1].x, vh[2].x};
+                    write_snap<float>(a.snaps, a.snap_pitch, k, p0 + a.p_off, ex0, y0);
+                    if (v1) {
+                        const float y1[6] = {xh[0].y, xh[1].y, xh[2].y, vh[0].y, vh[1].y, vh[2].y};
+                        write_snap<float>(a.snaps, a.snap_pitch, k, p1 + a.p_off, ex1, y1);
+                    }
                 }
             }
         }

@@ -40,7 +40,8 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
                kval_arr=1.0, dt=None, dtmax=None, n_particles_per_release=2, normals=None, precision="f64",
                snapshot_every=None, throw=False, release="fardal", prog_pot: Optional[Potential] = None,
                pot_pert: Optional[Potential] = None, prog_in_pert=False, return_ics=False, prog_method="auto",
-               force_surrogate=None, out="device", release_range=None, out_buffers=None, surrogate_judge=None):
+               force_surrogate=None, out="device", release_range=None, out_buffers=None, surrogate_judge=None,
+               host_mode="direct"):
     """Generate a particle-spray stream on the GPU.
 
     pot_base    smooth potential (release model and integration)
@@ -54,9 +55,12 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
     prog_method progenitor orbit solver (FP64 either way): 'serial', 'shoot'
                 (parallel in time, multiple shooting) or 'auto' (shoot when the
                 progenitor's potential is static)
-    out         'device' (CUDA tensors) or 'host': pinned host tensors, the stream
-                run in particle sub-ranges whose results are copied while the
-                next sub-range integrates (ready when the call returns)
+    out         'device' (CUDA tensors) or 'host': pinned host tensors, ready
+                when the call returns
+    host_mode   (out='host') 'direct': the stream kernel writes its snapshots
+                straight into the pinned host buffer; 'chunked': the stream runs
+                in particle sub-ranges whose results the copy engine moves to
+                the host while the next sub-range integrates (_core.stream_to_host)
     surrogate_judge (precision='mlp') dict(tol=, every=): keep pot_base as the
                 surrogate's error judge and fallback (ss_stream_mlp_judged_bf16):
                 every `every` steps each 128-particle tile compares its surrogate
@@ -138,7 +142,7 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
     if out == "host":
         final, snaps, status = _core.stream_to_host(integ._desc(), cfg, stream_ics, precision,
                                                     int(snapshot_every or 0), mlp=force_surrogate,
-                                                    out_buffers=out_buffers)
+                                                    out_buffers=out_buffers, mode=host_mode)
         torch.cuda.current_stream().synchronize()
     elif out == "device":
         if out_buffers is not None:

@@ -647,17 +647,21 @@ def test_orbit_parallel_in_time_vs_oracle(ss, oracle):
     assert phase_err(np64(w3), ref3) < 1e-11
 
 
-@pytest.mark.parametrize("precision", ["f64", "f32k"])
-def test_host_output_matches_device(ss, oracle, precision):
-    """gen_stream(out='host') runs the stream in particle sub-ranges
-    (first_particle / snap_pitch) with overlapped copies; every particle's
-    arithmetic is unchanged, so the results equal the one-launch run."""
+@pytest.mark.parametrize("precision,host_mode", [("f64", "direct"), ("f32k", "direct"), ("f64", "chunked"),
+                                                  ("f32k", "chunked")])
+def test_host_output_matches_device(ss, oracle, precision, host_mode):
+    """gen_stream(out='host'): 'direct' writes the snapshots from the stream
+    kernel straight into pinned host memory, 'chunked' runs the stream in
+    particle sub-ranges (first_particle / snap_pitch) with overlapped copies;
+    every particle's arithmetic is unchanged, so both equal the device run.
+    12 particles per release: the paired kernel's warps cover 64 particles,
+    so rows are written both as whole-warp lines and per particle."""
     from streamsculptor_gb300.streamhelpers import gen_stream
     orc_mov, back, ts, normals, ics, prog, c = _moving_prog_case(ss, oracle, n_rel=150, ppr=12)
     kw = dict(normals=normals, dt=c["dt"], prog_pot=prog, n_particles_per_release=c["ppr"], precision=precision,
               snapshot_every=20)
     d = gen_stream(mw3_gpu(ss), ts, back, 2e4, **kw)
-    h = gen_stream(mw3_gpu(ss), ts, back, 2e4, out="host", **kw)
+    h = gen_stream(mw3_gpu(ss), ts, back, 2e4, out="host", host_mode=host_mode, **kw)
     assert not h[0].is_cuda and h[0].is_pinned()
     for a, b in zip(d, h):
         a, b = a.cpu().numpy(), b.numpy()

@@ -86,6 +86,80 @@ def test_mlp_loss_gradient_matches_double_backward(ss):
     assert err <= 2e-3
 
 
+def _backend(tc):
+    from streamsculptor_gb300 import _abi
+    return _abi.load().ss_mlp_train_backend(int(tc))
+
+
+def test_tensor_core_training_gemms_keep_fp32_accuracy(ss):
+    """The training's 128-wide products on the tensor cores (tcgen05
+    kind::tf32 with each FP32 operand split into a TF32 head and remainder,
+    ss_mlp_train_backend(1), the default) against the same products on the
+    CUDA-core FP32 GEMM (ss_mlp_train_backend(0)) and against the float64
+    double backward.  B = 1024: the weight-gradient products (K = batch) take
+    the tensor cores too, split over K with atomics."""
+    s = _surrogate(ss, seed=11)
+    B = 1024
+    x = _points(B, seed=12)
+    rng = np.random.default_rng(13)
+    phi_t = rng.normal(-0.5, 0.2, B)
+    g_t = rng.normal(0, 0.01, (B, 3))
+    w_val = rng.uniform(0.5, 1.5, B) / B
+    w_force = rng.uniform(0.5, 1.5, B) / B * 1e4
+    dev = s.params.device
+    f32 = lambda a: torch.tensor(a, dtype=torch.float32, device=dev)  # noqa: E731
+    args = (f32(x), f32(phi_t), f32(g_t), f32(w_val), f32(w_force))
+    prev = _backend(1)
+    try:
+        loss_tc, grad_tc = s.loss_grad(*args)
+        _backend(0)
+        loss_cc, grad_cc = s.loss_grad(*args)
+    finally:
+        _backend(prev)
+    gtc, gcc = grad_tc.cpu().numpy(), grad_cc.cpu().numpy()
+    rel = np.max(np.abs(gtc - gcc)) / np.max(np.abs(gcc))
+    p = s.params.detach().cpu().double().requires_grad_(True)
+    xt = torch.tensor(x, requires_grad=True)
+    phi = _net64(p, s, xt)
+    (gx,) = torch.autograd.grad(phi.sum(), xt, create_graph=True)
+    lv = (torch.tensor(w_val) * (phi - torch.tensor(phi_t)) ** 2).sum()
+    lf = (torch.tensor(w_force) * ((gx - torch.tensor(g_t)) ** 2).sum(1)).sum()
+    (gp,) = torch.autograd.grad(lv + lf, p)
+    gp = gp.numpy()
+    e_tc = np.max(np.abs(gtc - gp)) / np.max(np.abs(gp))
+    e_cc = np.max(np.abs(gcc - gp)) / np.max(np.abs(gp))
+    print(f"tensor cores vs CUDA cores {rel:.2e}; vs float64: tensor cores {e_tc:.2e}, CUDA cores {e_cc:.2e}")
+    np.testing.assert_allclose(loss_tc.cpu().numpy(), loss_cc.cpu().numpy(), rtol=1e-5)
+    assert rel <= 1e-4
+    assert e_tc <= 2e-3 and e_tc <= 3.0 * e_cc + 1e-6
+
+
+def test_tensor_core_training_follows_the_cuda_core_loss_curve(ss):
+    """The same fit (seed, data, 300 Adam steps of 2048 points) with the
+    training products on the tensor cores and on the CUDA cores: the loss
+    curves agree (FP32-level products; the two runs round differently, so
+    they drift apart only slowly)."""
+    from streamsculptor_gb300 import potential as P
+    from streamsculptor_gb300.surrogate import MLPSurrogate
+    pot = P.NFWPotential(m=5.4e11, r_s=15.62, units=ss.usys)
+    x = torch.tensor(_points(1 << 14, seed=21), dtype=torch.float64, device="cuda")
+    phi, grad = pot.potential(x, 0.0), pot.gradient(x, 0.0)
+    curves = {}
+    prev = _backend(1)
+    try:
+        for tc in (1, 0):
+            _backend(tc)
+            nm = MLPSurrogate.normalisation(x.cpu(), phi.cpu())
+            s = MLPSurrogate.init(seed=4, **nm)
+            s.fit(x, phi, grad, steps=300, batch=2048, seed=4, log_every=100)
+            curves[tc] = np.array([h[1] + h[2] for h in s.history])
+    finally:
+        _backend(prev)
+    print("loss (tensor cores):", curves[1], "(CUDA cores):", curves[0])
+    assert curves[1][-1] < 0.2 * curves[1][0]
+    np.testing.assert_allclose(curves[1], curves[0], rtol=0.05)
+
+
 def test_mlp_tensor_core_force_matches_fp32(ss):
     """The tcgen05 path (BF16 weights and activations, FP32 accumulation in
     TMEM, transposed weight tiles for the backward chain) against the FP32
