@@ -536,8 +536,8 @@ int ss_mlp_loss_grad(const ss_mlp* mlp, const float* x, const float* phi_t, cons
 /* Which units run the training's 128-wide products (every ss_mlp_loss_grad
  * and ss_mlp_eval GEMM with N = 128 and K a multiple of 32): 1 (default) the
  * tensor cores (tcgen05 kind::tf32, each FP32 operand split into a TF32 head
- * and remainder, three MMAs per product: FP32 accuracy), 0 the CUDA-core
- * GEMM.  Other values leave the setting.  Returns the previous setting.
+ * and remainder, three MMAs per product: about 1e-5 relative, where one
+ * TF32 product would give about 1e-3), 0 the CUDA-core FP32 GEMM.  Other values leave the setting.  Returns the previous setting.
  * Process-wide: set it between calls, not while a call is in flight. */
 int ss_mlp_train_backend(int tensor_cores);
 

@@ -182,9 +182,10 @@ static void gemm_acc(int M, int N, int K, const float* A, int lda, const float* 
 // in TMEM).  Every FP32 operand is split into a TF32 head and remainder,
 // a = a_h + a_l (a_h: a with its 13 low mantissa bits cleared, a_l = a - a_h
 // exactly), and the product is a_h b_h + a_h b_l + a_l b_h: the dropped
-// a_l b_l is 2^-22 relative, so the GEMM keeps FP32 accuracy while the
-// tensor cores do the work (three MMAs where a single TF32 one would drop
-// 11 bits of every operand).
+// a_l b_l is 2^-22 relative, so the products stay near FP32 accuracy
+// (about 1e-5 relative on the training gradient, where single TF32 MMAs,
+// dropping 13 bits of every operand, give about 1e-3) while the tensor
+// cores do the work.
 // Operands as in the CUDA-core GEMM: A is [M,K] (lda) or, with TA, [K,M];
 // B is [K,N] (ldb) or, with TB, [N,K] (C = A W^T with W[out][in]).  Both
 // are staged K-major: an operand whose K is not the contiguous index is
