@@ -54,6 +54,9 @@ typedef enum ss_status {
  *                     (the rotating components of one potential share one Omega)
  *   SS_UNIFORM_ACCEL  p = {}                       UniformAcceleration: gradient dv/dt of the
  *                     potential's frame_velocity track, no potential value (0)  potential.py:480-502
+ *   SS_POWERLAW_CUTOFF p = {m, alpha, r_c}         PowerLawCutoffPotential (alpha < 3; the
+ *                     potential value needs alpha < 2, else NaN as in the reference)
+ *                                                  potential.py:357-388
  * A component with center = SS_CENTER_TRACK is evaluated at x - c(t), where
  * c(t) is the potential's center track: TimeDepTranslatingPotential,
  * potential.py:448-462.  Components are summed in list order
@@ -68,7 +71,8 @@ typedef enum ss_kind {
     SS_SH_EXPANSION = 7,
     SS_BAR = 8,
     SS_DEHNEN_BAR = 9,
-    SS_UNIFORM_ACCEL = 10
+    SS_UNIFORM_ACCEL = 10,
+    SS_POWERLAW_CUTOFF = 11
 } ss_kind;
 
 /* Largest degree of a spherical-harmonic expansion. */

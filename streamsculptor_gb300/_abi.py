@@ -30,6 +30,7 @@ SS_SH_EXPANSION = 7
 SS_BAR = 8
 SS_DEHNEN_BAR = 9
 SS_UNIFORM_ACCEL = 10
+SS_POWERLAW_CUTOFF = 11
 SS_SHEXP_LMAX = 8
 
 SS_CENTER_ORIGIN = 0

@@ -99,6 +99,15 @@ int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalo
                 SS_CHECK_ARG(p[1] > 0.0, "component %d (Isochrone): need a > 0", k);
                 d.q[0] = R(G * p[0]); d.q[1] = R(p[1]); d.q[2] = R(p[1] * p[1]);
                 break;
+            case SS_POWERLAW_CUTOFF: {
+                // q = {G m, a = (3 - alpha) / 2, 1 / r_c^2, ln Gamma(a), ln Gamma(a - 1/2) (NaN for
+                // a <= 1/2: no potential value), 1 / r_c}
+                SS_CHECK_ARG(p[1] < 3.0 && p[2] > 0.0, "component %d (PowerLawCutoff): need alpha < 3, r_c > 0", k);
+                const double a = 0.5 * (3.0 - p[1]);
+                d.q[0] = R(G * p[0]); d.q[1] = R(a); d.q[2] = R(1.0 / (p[2] * p[2])); d.q[3] = R(std::lgamma(a));
+                d.q[4] = R(a > 0.5 ? std::lgamma(a - 0.5) : std::nan("")); d.q[5] = R(1.0 / p[2]);
+                break;
+            }
             case SS_SH_EXPANSION: {
                 const ss_expansion& e = in->expansion;
                 SS_CHECK_ARG(!need_expansion, "component %d: only one SS_SH_EXPANSION component per potential", k);
@@ -244,6 +253,14 @@ __device__ double comp_phi(const PotDev<double>& P, const CompDev<double>& c, co
             return -q[0] / sqrt(r2 + q[1]);
         case SS_ISOCHRONE:
             return -q[0] / (q[1] + sqrt(r2 + q[2]));
+        case SS_POWERLAW_CUTOFF: {
+            // Phi = -G m P(a, x) / r + G m Gamma(a - 1/2) P(a - 1/2, x) / (Gamma(a) r_c), x = r^2 / r_c^2
+            // (PowerLawCutoffPotential.potential, potential.py:365-378, with Gamma(a + 1) = a Gamma(a))
+            if (!(q[1] > 0.5)) return nan("");
+            const double xx = r2 * q[2];
+            return -q[0] * gammainc_p(q[1], q[3], xx) / sqrt(r2) +
+                   q[0] * exp(q[4] - q[3]) * q[5] * gammainc_p(q[1] - 0.5, q[4], xx);
+        }
         default:
             return nan("");
     }

@@ -437,12 +437,90 @@ __device__ __forceinline__ void isochrone_gh(const R* q, const T& r2, T& g, T& h
     if (HESS) h = -q[0] * (3.0f * s + q[1]) * inv_s * inv_s * inv_s * inv_as * inv_as * inv_as;
 }
 
+// Regularised lower incomplete gamma function P(a, x) = gamma(a, x) /
+// Gamma(a), a > 0, x >= 0, given lg = ln Gamma(a) (PowerLawCutoffPotential,
+// potential.py:357-388, evaluates it with jax.scipy.special.gammainc).  With
+// e = x^a e^-x / Gamma(a): for x < a + 1 the power series
+//   P = e sum_{n>=0} x^n / (a (a+1) ... (a+n)),
+// else P = 1 - e F with the continued fraction
+//   F = 1 / (x + 1 - a - 1 (1 - a) / (x + 3 - a - 2 (2 - a) / (x + 5 - a - ...)))
+// (Abramowitz & Stegun 6.5.29 and 6.5.31), evaluated by the modified Lentz
+// method; both stop once a term moves the result by less than the
+// precision of S (bounded at 500 terms).
+template <class S>
+__device__ __forceinline__ S gammainc_p_s(S a, S lg, S x) {
+    constexpr bool dbl = sizeof(S) == 8;
+    const S eps = dbl ? S(1e-16) : S(6e-8);
+    const S tiny = dbl ? S(1e-300) : S(1e-30);
+    if (!(x > S(0))) return S(0);
+    const S e = exp(a * log(x) - x - lg);
+    if (x < a + S(1)) {
+        S term = S(1) / a, sum = term;
+        for (int n = 1; n < 500; ++n) {
+            term *= x / (a + S(n));
+            sum += term;
+            if (fabs(term) < fabs(sum) * eps) break;
+        }
+        return sum * e;
+    }
+    S b = x + S(1) - a, c = S(1) / tiny, d = S(1) / b, h = d;
+    for (int i = 1; i < 500; ++i) {
+        const S an = -S(i) * (S(i) - a);
+        b += S(2);
+        d = an * d + b;
+        if (fabs(d) < tiny) d = tiny;
+        c = b + an / c;
+        if (fabs(c) < tiny) c = tiny;
+        d = S(1) / d;
+        const S del = d * c;
+        h *= del;
+        if (fabs(del - S(1)) < eps) break;
+    }
+    return S(1) - e * h;
+}
+// dP/dx = x^(a-1) e^-x / Gamma(a)
+template <class S>
+__device__ __forceinline__ S gammainc_dp_s(S a, S lg, S x) {
+    return x > S(0) ? exp((a - S(1)) * log(x) - x - lg) : S(0);
+}
+__device__ __forceinline__ float gammainc_p(float a, float lg, float x) { return gammainc_p_s<float>(a, lg, x); }
+__device__ __forceinline__ double gammainc_p(double a, double lg, double x) { return gammainc_p_s<double>(a, lg, x); }
+__device__ __forceinline__ float gammainc_dp(float a, float lg, float x) { return gammainc_dp_s<float>(a, lg, x); }
+__device__ __forceinline__ double gammainc_dp(double a, double lg, double x) { return gammainc_dp_s<double>(a, lg, x); }
+template <int N>
+__device__ inline Dual<N> gammainc_p(double a, double lg, const Dual<N>& x) {
+    return chain(x, gammainc_p(a, lg, x.v), gammainc_dp(a, lg, x.v));
+}
+template <int N>
+__device__ inline Dual<N> gammainc_dp(double a, double lg, const Dual<N>& x) {
+    const double dp = gammainc_dp(a, lg, x.v);
+    return chain(x, dp, dp * ((a - 1.0) / x.v - 1.0));
+}
+
+template <class T, class R, bool HESS>
+__device__ __forceinline__ void powerlaw_cutoff_gh(const R* q, const T& r2, T& g, T& h) {
+    // dPhi/dr = G m P(a, r^2 / r_c^2) / r^2, a = (3 - alpha) / 2
+    // (PowerLawCutoffPotential.gradient_func, potential.py:380-388);
+    // q = {G m, a, 1 / r_c^2, ln Gamma(a), ...}
+    const T x = r2 * q[2];
+    const T P = gammainc_p(q[1], q[3], x);
+    const T inv_r = s_rsqrt(r2);
+    const T inv_r3 = inv_r * inv_r * inv_r;
+    g = q[0] * P * inv_r3;
+    if (HESS) {
+        // g'(r) / r = G m (2 P'(x) / r_c^2 - 3 P / r^2) / r^3
+        const T dP = gammainc_dp(q[1], q[3], x);
+        h = q[0] * (2.0f * q[2] * dP - 3.0f * P * inv_r * inv_r) * inv_r3;
+    }
+}
+
 // Adds grad Phi of one component of compile-time kind KIND at x (already
 // shifted to its center) to grad[3]; when HESS, adds its Hessian
 // (xx, yy, zz, xy, xz, yz) to H[6].
 template <int KIND, class T, class R, bool HESS>
 __device__ __forceinline__ void kind_grad(const R* q, const T x[3], T grad[3], T H[6]) {
-    if constexpr (KIND == SS_NFW || KIND == SS_HERNQUIST || KIND == SS_PLUMMER || KIND == SS_ISOCHRONE) {
+    if constexpr (KIND == SS_NFW || KIND == SS_HERNQUIST || KIND == SS_PLUMMER || KIND == SS_ISOCHRONE ||
+                  KIND == SS_POWERLAW_CUTOFF) {
         T r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
         T g, h;
         if constexpr (KIND == SS_NFW) {
@@ -451,6 +529,8 @@ __device__ __forceinline__ void kind_grad(const R* q, const T x[3], T grad[3], T
             hernquist_gh<T, R, HESS>(q, r2 + q[2], g, h);
         } else if constexpr (KIND == SS_PLUMMER) {
             plummer_gh<T, R, HESS>(q, r2, g, h);
+        } else if constexpr (KIND == SS_POWERLAW_CUTOFF) {
+            powerlaw_cutoff_gh<T, R, HESS>(q, r2, g, h);
         } else {
             isochrone_gh<T, R, HESS>(q, r2, g, h);
         }
@@ -641,6 +721,7 @@ __device__ __forceinline__ void comp_grad(const CompDev<R>& c, const T x[3], T g
         case SS_HERNQUIST: kind_grad<SS_HERNQUIST, T, R, HESS>(c.q, x, grad, H); break;
         case SS_PLUMMER: kind_grad<SS_PLUMMER, T, R, HESS>(c.q, x, grad, H); break;
         case SS_ISOCHRONE: kind_grad<SS_ISOCHRONE, T, R, HESS>(c.q, x, grad, H); break;
+        case SS_POWERLAW_CUTOFF: kind_grad<SS_POWERLAW_CUTOFF, T, R, HESS>(c.q, x, grad, H); break;
         default: break;
     }
 }

@@ -57,6 +57,14 @@ template <class S> __device__ __forceinline__ D1<S> s_sqrt(const D1<S>& x) {
     return D1<S>(r, (0.5f * s_rcp(r)) * x.d);
 }
 
+template <class S> __device__ __forceinline__ D1<S> gammainc_p(S a, S lg, const D1<S>& x) {
+    return D1<S>(gammainc_p(a, lg, x.v), gammainc_dp(a, lg, x.v) * x.d);
+}
+template <class S> __device__ __forceinline__ D1<S> gammainc_dp(S a, S lg, const D1<S>& x) {
+    const S dp = gammainc_dp(a, lg, x.v);
+    return D1<S>(dp, (dp * ((a - S(1)) * s_rcp(x.v) - S(1))) * x.d);
+}
+
 template <class S> __device__ __forceinline__ S from_double(double c);
 template <> __device__ __forceinline__ double from_double<double>(double c) { return c; }
 template <> __device__ __forceinline__ float from_double<float>(double c) { return (float)c; }

@@ -274,6 +274,41 @@ class ProgenitorPotential(Potential):
         return TimeDepTranslatingPotential(self.prog_pot, self.interp_func, units=self.units)._flatten()
 
 
+class PowerLawCutoffPotential(Potential):
+    """Spherical power law rho ~ r^-alpha with an exp(-(r / r_c)^2) cutoff
+    (PowerLawCutoffPotential, potential.py:357-388): dPhi/dr = G m
+    P((3 - alpha) / 2, r^2 / r_c^2) / r^2 with P the regularised lower
+    incomplete gamma function, evaluated in the kernels (series or continued
+    fraction); the potential value needs alpha < 2 (NaN otherwise, as the
+    reference's formula gives)."""
+
+    def __init__(self, m, alpha, r_c, units=None):
+        super().__init__(units, {"m": m, "alpha": alpha, "r_c": r_c})
+
+    def _flatten(self):
+        return Flat([(_abi.SS_POWERLAW_CUTOFF, _abi.SS_CENTER_ORIGIN, (_f(self.m), _f(self.alpha), _f(self.r_c)))])
+
+
+class BovyMWPotential2014(Potential):
+    """Disk + bulge + halo of Bovy (2015) MWPotential2014 (potential.py:420-446):
+    Miyamoto-Nagai disk, power-law bulge with cutoff, NFW halo, summed in
+    that order."""
+
+    def __init__(self, units=None):
+        super().__init__(units, {"params": None})
+        self.m_disk, self.a_disk, self.b_disk = 6.82e10, 3.0, 0.28
+        self.m_bulge, self.alpha_bulge, self.r_c_bulge = 4.50e9, 1.80, 1.90
+        self.m_halo, self.r_s_halo = 4.37e11, 16.0
+        self.pot = Potential_Combine([
+            MiyamotoNagaiDisk(m=self.m_disk, a=self.a_disk, b=self.b_disk, units=self.units),
+            PowerLawCutoffPotential(m=self.m_bulge, alpha=self.alpha_bulge, r_c=self.r_c_bulge, units=self.units),
+            NFWPotential(m=self.m_halo, r_s=self.r_s_halo, units=self.units),
+        ], units=self.units)
+
+    def _flatten(self):
+        return self.pot._flatten()
+
+
 class GalaMilkyWayPotential(Potential):
     """Disk + bulge + nucleus + halo (potential.py:390-418), summed in that order."""
 
@@ -678,7 +713,8 @@ class CustomPotential(Potential):
         super().__init__(units, {"potential_func": potential_func})
 
 
-__all__ = ["MiyamotoNagaiDisk", "NFWPotential", "TriaxialNFWPotential", "Isochrone", "PlummerPotential",
+__all__ = ["PowerLawCutoffPotential", "BovyMWPotential2014", "MiyamotoNagaiDisk", "NFWPotential",
+           "TriaxialNFWPotential", "Isochrone", "PlummerPotential",
            "HernquistPotential", "Potential_Combine", "TimeDepTranslatingPotential", "ProgenitorPotential",
            "GalaMilkyWayPotential", "SubhaloLinePotential", "SubhaloLinePotential_dRadius", "BarPotential",
            "DehnenBarPotential", "UniformAcceleration", "MW_LMC_Potential", "TNFWSubhaloLinePotential",
