@@ -153,10 +153,11 @@ def _all_kinds():
         (_abi.SS_HERNQUIST, 0, (5e9, 1.0, 0.01)),
         (_abi.SS_PLUMMER, 0, (2e9, 0.5)),
         (_abi.SS_ISOCHRONE, 0, (4e9, 1.5)),
+        (_abi.SS_POWERLAW_CUTOFF, 0, (4.5e9, 1.8, 1.9)),
     ]
 
 
-@pytest.mark.parametrize("k", range(6))
+@pytest.mark.parametrize("k", range(7))
 def test_autodiff_matches_finite_differences(oracle, k):
     m = oracle.HostModel([_all_kinds()[k]])
     rng = np.random.default_rng(k)
@@ -184,6 +185,28 @@ def test_spherical_potential_closed_forms(oracle):
     ]:
         _, g, _ = oracle.potential_eval(oracle.HostModel([(kind, 0, p)]), x)
         assert abs(g[0, 0] - dphidr()) <= 1e-13 * abs(dphidr())
+
+
+@pytest.mark.parametrize("m,alpha,r_c", [(4.5e9, 1.8, 1.9), (1e10, 1.0, 0.5), (3e9, 0.5, 3.0)])
+def test_powerlaw_cutoff_matches_scipy(oracle, m, alpha, r_c):
+    """The oracle's PowerLawCutoffPotential (its own regularised incomplete
+    gamma function, forces by autodiff of the potential) against the
+    reference's potential formula and gradient_func (potential.py:365-388)
+    evaluated with scipy.special.gammainc and gamma, from 1e-3 to 200 kpc."""
+    from scipy import special
+    rng = np.random.default_rng(0)
+    d = rng.normal(size=(300, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r = np.exp(rng.uniform(np.log(1e-3), np.log(200.0), 300))
+    x = d * r[:, None]
+    phi, g, _ = oracle.potential_eval(oracle.HostModel([(_abi.SS_POWERLAW_CUTOFF, 0, (m, alpha, r_c))]), x)
+    t0 = alpha / 2
+    t1, t2, xx = -t0, 1.5 - t0, r ** 2 / r_c ** 2
+    t6 = G * m * special.gammainc(t2, xx) * special.gamma(t2) / (r * special.gamma(t1 + 2.5))
+    phi_ref = t0 * t6 - 1.5 * t6 + G * m * special.gammainc(t1 + 1, xx) * special.gamma(t1 + 1) / (r_c * special.gamma(t2))
+    g_ref = (G * m / r ** 2 * special.gammainc(t2, xx))[:, None] * x / r[:, None]
+    assert np.max(np.abs(phi - phi_ref) / np.abs(phi_ref)) < 1e-13
+    assert np.max(np.linalg.norm(g - g_ref, axis=1) / np.linalg.norm(g_ref, axis=1)) < 1e-13
 
 
 def test_dopri5_fifth_order(oracle):
