@@ -202,6 +202,30 @@ def release(model: HostModel, prog_w, t_rel, msat, normals, kvals=(2.0, 0.3, 0.0
     return ics, J
 
 
+def streakline_ics(model: HostModel, prog_w, t_rel, msat):
+    """Streakline release (get_Streakline_ICs, streamhelpers.py:657-705) on
+    the oracle: Lagrange points x -/+ r_t x / |x| with the tidal radius
+    r_t = (G M / (omega^2 - r^T H r / r^2))^(1/3) (main.py:88-112, H the
+    oracle's autodiff Hessian), velocities along v / |v| with magnitude
+    omega |x_L| / sin(theta).  Returns [n, 2, 6]: (close, far) per release."""
+    w = f8(prog_w).reshape(-1, 6)
+    x, v = w[:, :3], w[:, 3:]
+    _, _, H = potential_eval(model, x, f8(t_rel).reshape(-1))
+    r = np.linalg.norm(x, axis=1)
+    rh = x / r[:, None]
+    d2 = np.einsum("ni,nij,nj->n", rh, H, rh)
+    om = np.linalg.norm(np.cross(x, v), axis=1) / r ** 2
+    rt = (model.G * float(msat) / (om ** 2 - d2)) ** (1.0 / 3.0)
+    ph = v / np.linalg.norm(v, axis=1)[:, None]
+    sin_t = np.linalg.norm(np.cross(rh, ph), axis=1)
+    out = np.empty((w.shape[0], 2, 6))
+    for k, sgn in enumerate((-1.0, 1.0)):
+        xl = x + sgn * rh * rt[:, None]
+        out[:, k, :3] = xl
+        out[:, k, 3:] = (om * np.linalg.norm(xl, axis=1) / sin_t)[:, None] * ph
+    return out
+
+
 def stream(model: HostModel, t0, dt, n_steps, ics, ppr, spr, snap_stride=0, n_threads=0, stream_particles=0,
            subhalos_per_stream=0, first_particle=0):
     P = model.struct()

@@ -435,6 +435,63 @@ def custom_release_model(pos_prog=None, vel_prog=None, pos_rel=None, vel_rel=Non
     return f64(pos_prog) + f64(pos_rel), f64(vel_prog) + f64(vel_rel)
 
 
+# ---------------------------------------------------------------- streakline
+def _streakline_grid(t0, t1, Nstrip, dt):
+    """Release times linspace(t0, t1, Nstrip) and the fixed step: the release
+    spacing, or that spacing split into the fewest steps no longer than dt."""
+    ts = np.linspace(float(t0), float(t1), int(Nstrip))
+    if int(Nstrip) < 2:
+        raise ValueError("Nstrip must be >= 2")
+    gap = (ts[-1] - ts[0]) / (len(ts) - 1)
+    spr = 1 if dt is None else max(1, int(np.ceil(abs(gap) / float(dt) - 1e-12)))
+    return ts, gap / spr, spr
+
+
+def get_Streakline_ICs(pot, prog_w0, Msat, t0, t1, Nstrip, solver=None, rtol=1e-6, atol=1e-6, dt=None):
+    """Streakline release (streamhelpers.py:657-705): at Nstrip times
+    linspace(t0, t1) one particle leaves each of the progenitor's Lagrange
+    points (Potential.lagrange_pts, main.py:106-112) moving along the
+    progenitor's velocity direction at the progenitor's angular velocity,
+    |v| = omega |x_L| / sin(theta), theta between the progenitor's position
+    and velocity.  The progenitor runs forward from prog_w0 at t0 (fixed-step
+    FP64, the release spacing or steps of at most dt; the reference's
+    adaptive solver arguments are accepted and not used).  Returns
+    (L_close, v_lead, L_far, v_trail, ts), CUDA tensors and ts on the host."""
+    _core.check_solver(solver)
+    ts, h, _ = _streakline_grid(t0, t1, Nstrip, dt)
+    w = pot.integrate_orbit(w0=prog_w0, ts=ts, dt=h).ys
+    x, v = w[:, :3], w[:, 3:]
+    L_close, L_far = pot.lagrange_pts(x, v, Msat, torch.as_tensor(ts, device=x.device))
+    om = pot.omega(x, v)
+    rh = x / torch.linalg.norm(x, dim=1, keepdim=True)
+    ph = v / torch.linalg.norm(v, dim=1, keepdim=True)
+    sin_t = torch.linalg.norm(torch.linalg.cross(rh, ph, dim=1), dim=1)
+    v_lead = (om * torch.linalg.norm(L_close, dim=1) / sin_t)[:, None] * ph
+    v_trail = (om * torch.linalg.norm(L_far, dim=1) / sin_t)[:, None] * ph
+    return L_close, v_lead, L_far, v_trail, ts
+
+
+def gen_streakline(pot, prog_w0, Msat, t0, t1, Nstrip, solver=None, rtol=1e-6, atol=1e-6, dt=None,
+                   precision="f64"):
+    """Streakline stream (streamhelpers.py:708-732): the particles of
+    get_Streakline_ICs, each integrated from its release time to t1 (the last
+    pair, released at t1, is its initial state).  One stream launch: release
+    r is particles 2r (from L_close, 'lead') and 2r + 1 (L_far, 'trail'),
+    starting at step r * steps_per_release.  precision 'f64' or 'f32k'.
+    Returns (lead [Nstrip, 6], trail [Nstrip, 6], ts)."""
+    ts, h, spr = _streakline_grid(t0, t1, Nstrip, dt)
+    L_close, v_lead, L_far, v_trail, _ = get_Streakline_ICs(pot, prog_w0, Msat, t0, t1, Nstrip, solver=solver,
+                                                            dt=dt)
+    n = len(ts)
+    ics = torch.stack([torch.cat([L_close, v_lead], 1), torch.cat([L_far, v_trail], 1)], 1).reshape(2 * n, 6)
+    cfg = _abi.ss_stream_cfg()
+    cfg.t0, cfg.dt, cfg.n_steps, cfg.n_particles = float(ts[0]), float(h), (n - 1) * spr, 2 * n
+    cfg.particles_per_release, cfg.steps_per_release, cfg.snap_stride = 2, spr, 0
+    final, _ = _core.stream(pot._desc(), cfg, ics.contiguous(), precision)
+    final = final.reshape(n, 2, 6)
+    return final[:, 0], final[:, 1], ts
+
+
 def computed_binned_track(stream, phi1, bins=20):
     """Mean 6-D state in phi1 bins (streamhelpers.py:201-228).
 
@@ -584,4 +641,5 @@ __all__ = ["gen_stream", "eval_dense_stream", "eval_dense_stream_id", "gen_strea
            "compute_stream_length",
            "compute_length_oscillations", "sample_from_1D_pdf", "release_model_Chen25", "gen_stream_ics_Chen25",
            "gen_stream_vmapped_Chen25", "gen_stream_ics_pert_Chen25", "gen_stream_vmapped_with_pert_Chen25",
-           "gen_stream_vmapped_with_pert_Chen25_fixed_prog", "chen25_factor", "CHEN25_MEAN", "CHEN25_COV"]
+           "gen_stream_vmapped_with_pert_Chen25_fixed_prog", "chen25_factor", "CHEN25_MEAN", "CHEN25_COV",
+           "get_Streakline_ICs", "gen_streakline"]

@@ -892,3 +892,30 @@ def test_structural_subhalo_classes(ss, oracle):
             assert float(np64(s.potential(x[0], t))) == pytest.approx(float(d_o[0].sum()), rel=1e-12)
     with pytest.raises(NotImplementedError):
         P.SubhaloLinePotential_dRadius_Custom(lambda xyz, t: 0.0, *args[2:], units=ss.usys)
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-10), ("f32k", 1e-5)])
+def test_streakline_matches_oracle(ss, oracle, precision, tol):
+    """gen_streakline (streamhelpers.py:708-732): the progenitor forward from
+    t0, one particle per Lagrange point at each of Nstrip release times
+    (get_Streakline_ICs, streamhelpers.py:657-705), every pair integrated to
+    t1 (the last pair, released at t1, is its initial state), against the
+    oracle's restatement; 2 Myr between releases in 1 Myr steps."""
+    from streamsculptor_gb300.streamhelpers import gen_streakline, get_Streakline_ICs
+    pot = mw3_gpu(ss)
+    orc = oracle.HostModel(oracle.mw3())
+    t0, t1, n = -1000.0, 0.0, 501
+    w0 = oracle.orbit(orc, PROG_WF, 0.0, -1.0, 1000, 1000)[0, -1]
+    lead, trail, ts = gen_streakline(pot, w0, 2e4, t0, t1, n, dt=1.0, precision=precision)
+    ws = oracle.orbit(orc, w0, t0, 1.0, 1000, 2)[0]
+    ics = oracle.streakline_ics(orc, ws, ts, 2e4)
+    Lc, vl, Lf, vt, _ = get_Streakline_ICs(pot, w0, 2e4, t0, t1, n, dt=1.0)
+    got_ics = np.stack([np.concatenate([np64(Lc), np64(vl)], 1), np.concatenate([np64(Lf), np64(vt)], 1)], 1)
+    assert phase_err(got_ics.reshape(-1, 6), ics.reshape(-1, 6)) < 1e-11
+    ref, _, _ = oracle.stream(orc, t0, 1.0, 1000, ics.reshape(-1, 6), 2, 2)
+    got = np.stack([np64(lead), np64(trail)], 1).reshape(-1, 6)
+    err = phase_err(got, ref)
+    print(f"streakline ({precision}) vs oracle: {err:.2e}")
+    assert err <= tol
+    # released at t1: the pair's initial states (hi + lo in the FP32 form)
+    np.testing.assert_allclose(got[-2:], got_ics[-1], rtol=1e-15 if precision == "f64" else 1e-13)
