@@ -537,6 +537,23 @@ int ss_mlp_loss_grad(const ss_mlp* mlp, const float* x, const float* phi_t, cons
                      const float* w_val, const float* w_force, int64_t batch, float* loss, float* grad,
                      void* workspace, int64_t workspace_bytes, void* stream);
 
+/* The whole Adam fit, run by the library: for step s = 0 .. steps-1 the
+ * batch is samples order[s*batch .. s*batch + batch - 1] of the training
+ * set (x [n,3], phi_t [n], g_t [n,3], w_val, w_force [n] FP32 device
+ * arrays; order int32 device [steps*batch], indices < n), its loss gradient
+ * as ss_mlp_loss_grad, then one Adam step with the learning rate
+ * lr_min + (lr - lr_min) (1 + cos(pi s / (steps - 1))) / 2 and the bias
+ * corrections of step s + 1.  params [SS_MLP_NPARAM] (device) are updated in
+ * place and take the place of mlp->params (the rest of mlp: normalisation,
+ * exact base); m, v [SS_MLP_NPARAM]: the Adam moments, zero for a fresh fit.
+ * loss_log (device [steps][2], nullable): each step's (value, force) loss.
+ * No host synchronisation inside.  Workspace: ss_mlp_fit_workspace_bytes(batch). */
+int64_t ss_mlp_fit_workspace_bytes(int64_t batch);
+int ss_mlp_fit(const ss_mlp* mlp, float* params, const float* x, const float* phi_t, const float* g_t,
+               const float* w_val, const float* w_force, int64_t n, const int32_t* order, int64_t batch,
+               int64_t steps, float lr, float lr_min, float beta1, float beta2, float eps, float* m, float* v,
+               float* loss_log, void* workspace, int64_t workspace_bytes, void* stream);
+
 /* Which units run the training's 128-wide products (every ss_mlp_loss_grad
  * and ss_mlp_eval GEMM with N = 128 and K a multiple of 32): 1 (default) the
  * tensor cores (tcgen05 kind::tf32, each FP32 operand split into a TF32 head

@@ -159,6 +159,10 @@ SIGNATURES = {
     "ss_mlp_train_workspace_bytes": (C.c_int64, [C.c_int64]),
     "ss_mlp_loss_grad": (C.c_int, [C.POINTER(ss_mlp), VP, VP, VP, VP, VP, C.c_int64, VP, VP, VP, C.c_int64, VP]),
     "ss_mlp_train_backend": (C.c_int, [C.c_int]),
+    "ss_mlp_fit_workspace_bytes": (C.c_int64, [C.c_int64]),
+    "ss_mlp_fit": (C.c_int, [C.POINTER(ss_mlp), VP, VP, VP, VP, VP, VP, C.c_int64, VP, C.c_int64, C.c_int64,
+                             C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, VP, VP, VP, VP, C.c_int64,
+                             VP]),
     "ss_mlp_adam": (C.c_int, [VP, VP, VP, VP, C.c_int64, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float,
                               VP]),
     "ss_mlp_grad_bf16": (C.c_int, [C.POINTER(ss_mlp), VP, C.c_int64, VP, VP, VP]),

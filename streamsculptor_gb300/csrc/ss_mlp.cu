@@ -695,18 +695,14 @@ int64_t ss_mlp_train_workspace_bytes(int64_t batch) {
     return bufs_bytes(batch, true);
 }
 
-int ss_mlp_loss_grad(const ss_mlp* mlp, const float* x, const float* phi_t, const float* g_t, const float* w_val,
-                     const float* w_force, int64_t batch, float* loss, float* grad, void* workspace,
-                     int64_t workspace_bytes, void* stream) {
-    SS_CHECK_ARG(mlp != nullptr && mlp->params != nullptr, "mlp or its params is NULL");
-    SS_CHECK_ARG(batch > 0 && batch <= (1 << 24), "batch outside [1, 2^24]");
-    SS_CHECK_ARG(x && phi_t && g_t && w_val && w_force && loss && grad, "NULL buffer");
-    const int64_t need = ss_mlp_train_workspace_bytes(batch);
-    if (workspace == nullptr || workspace_bytes < need)
-        return set_error(SS_ERR_WORKSPACE, "workspace of %lld bytes needed", (long long)need);
-    cudaStream_t st = (cudaStream_t)stream;
-    const MlpNorm nm = norm_of(mlp);
-    const float* prm = mlp->params;
+}  // extern "C"
+
+namespace ssg {
+
+// The body of ss_mlp_loss_grad (arguments checked by the callers).
+static int loss_grad_impl(const MlpNorm& nm, const float* prm, const float* x, const float* phi_t, const float* g_t,
+                          const float* w_val, const float* w_force, int64_t batch, float* loss, float* grad,
+                          void* workspace, cudaStream_t st) {
     const int B = (int)batch;
     const int64_t n = (int64_t)B * MW;
     float* rest = nullptr;
@@ -763,6 +759,99 @@ int ss_mlp_loss_grad(const ss_mlp* mlp, const float* x, const float* phi_t, cons
         float* t = Zbar;
         Zbar = Dbar;
         Dbar = t;
+    }
+    return SS_OK;
+}
+
+// One training batch gathered from the training set by sample index.
+__global__ void gather_batch_kernel(const float* __restrict__ x, const float* __restrict__ phi,
+                                    const float* __restrict__ g, const float* __restrict__ wv,
+                                    const float* __restrict__ wf, const int32_t* __restrict__ idx, int64_t B,
+                                    float* xb, float* pb, float* gb, float* wvb, float* wfb) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B) return;
+    const int64_t j = idx[i];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        xb[3 * i + c] = x[3 * j + c];
+        gb[3 * i + c] = g[3 * j + c];
+    }
+    pb[i] = phi[j];
+    wvb[i] = wv[j];
+    wfb[i] = wf[j];
+}
+
+// the gathered batch (x, phi, g, w_val, w_force), the gradient and the loss
+// ahead of the training buffers in the fit workspace, 256-byte aligned each
+static int64_t fit_head_floats(int64_t B) {
+    auto up = [](int64_t f) { return (f + 63) / 64 * 64; };
+    return up(3 * B) + up(B) + up(3 * B) + up(B) + up(B) + up(SS_MLP_NPARAM) + 64;
+}
+
+}  // namespace ssg
+
+extern "C" {
+
+int ss_mlp_loss_grad(const ss_mlp* mlp, const float* x, const float* phi_t, const float* g_t, const float* w_val,
+                     const float* w_force, int64_t batch, float* loss, float* grad, void* workspace,
+                     int64_t workspace_bytes, void* stream) {
+    SS_CHECK_ARG(mlp != nullptr && mlp->params != nullptr, "mlp or its params is NULL");
+    SS_CHECK_ARG(batch > 0 && batch <= (1 << 24), "batch outside [1, 2^24]");
+    SS_CHECK_ARG(x && phi_t && g_t && w_val && w_force && loss && grad, "NULL buffer");
+    const int64_t need = ss_mlp_train_workspace_bytes(batch);
+    if (workspace == nullptr || workspace_bytes < need)
+        return set_error(SS_ERR_WORKSPACE, "workspace of %lld bytes needed", (long long)need);
+    return loss_grad_impl(norm_of(mlp), mlp->params, x, phi_t, g_t, w_val, w_force, batch, loss, grad, workspace,
+                          (cudaStream_t)stream);
+}
+
+int64_t ss_mlp_fit_workspace_bytes(int64_t batch) {
+    if (batch <= 0 || batch > (1 << 24)) return set_error(SS_ERR_INVALID_ARGUMENT, "batch outside [1, 2^24]");
+    return fit_head_floats(batch) * (int64_t)sizeof(float) + bufs_bytes(batch, true);
+}
+
+int ss_mlp_fit(const ss_mlp* mlp, float* params, const float* x, const float* phi_t, const float* g_t,
+               const float* w_val, const float* w_force, int64_t n, const int32_t* order, int64_t batch,
+               int64_t steps, float lr, float lr_min, float beta1, float beta2, float eps, float* m, float* v,
+               float* loss_log, void* workspace, int64_t workspace_bytes, void* stream) {
+    SS_CHECK_ARG(mlp != nullptr && params != nullptr, "mlp or params is NULL");
+    SS_CHECK_ARG(n > 0 && n <= INT32_MAX, "n outside [1, 2^31)");
+    SS_CHECK_ARG(batch > 0 && batch <= (1 << 24), "batch outside [1, 2^24]");
+    SS_CHECK_ARG(steps >= 0, "steps < 0");
+    SS_CHECK_ARG(x && phi_t && g_t && w_val && w_force && order && m && v, "NULL buffer");
+    SS_CHECK_ARG(mlp->base == nullptr || (mlp->base_n >= 2 && mlp->base_n <= SS_MLP_BASE_MAX && mlp->base_du > 0.0),
+                 "mlp base table needs 2 <= base_n <= %d knots and base_du > 0", SS_MLP_BASE_MAX);
+    const int64_t need = ss_mlp_fit_workspace_bytes(batch);
+    if (workspace == nullptr || workspace_bytes < need)
+        return set_error(SS_ERR_WORKSPACE, "workspace of %lld bytes needed", (long long)need);
+    if (steps == 0) return SS_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const MlpNorm nm = norm_of(mlp);
+    auto up = [](int64_t f) { return (f + 63) / 64 * 64; };
+    float* p = static_cast<float*>(workspace);
+    float* xb = p;
+    float* pb = xb + up(3 * batch);
+    float* gb = pb + up(batch);
+    float* wvb = gb + up(3 * batch);
+    float* wfb = wvb + up(batch);
+    float* grad = wfb + up(batch);
+    float* loss_tmp = grad + up(SS_MLP_NPARAM);
+    void* train_ws = static_cast<void*>(p + fit_head_floats(batch));
+    for (int64_t s = 0; s < steps; ++s) {
+        gather_batch_kernel<<<blocks(batch, 256), 256, 0, st>>>(x, phi_t, g_t, w_val, w_force, order + s * batch, batch,
+                                                                xb, pb, gb, wvb, wfb);
+        SS_LAUNCH_CHECK();
+        const int rc = loss_grad_impl(nm, params, xb, pb, gb, wvb, wfb, batch, loss_log ? loss_log + 2 * s : loss_tmp,
+                                      grad, train_ws, st);
+        if (rc) return rc;
+        // cosine decay from lr to lr_min over the run; bias corrections of step s + 1
+        const double lr_s = (double)lr_min + 0.5 * ((double)lr - (double)lr_min) *
+                                                 (1.0 + std::cos(M_PI * (double)s / (double)std::max<int64_t>(steps - 1, 1)));
+        const float c1 = (float)(1.0 / (1.0 - std::pow((double)beta1, (double)(s + 1))));
+        const float c2 = (float)(1.0 / (1.0 - std::pow((double)beta2, (double)(s + 1))));
+        adam_kernel<<<blocks(SS_MLP_NPARAM, 256), 256, 0, st>>>(params, grad, m, v, SS_MLP_NPARAM, (float)lr_s, beta1,
+                                                                 beta2, eps, c1, c2);
+        SS_LAUNCH_CHECK();
     }
     return SS_OK;
 }

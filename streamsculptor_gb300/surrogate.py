@@ -151,24 +151,30 @@ class MLPSurrogate:
             gnorm2 = (force_scale.to(dev, torch.float64) ** 2).clamp_min(1e-300)
         grad = grad.to(dev, torch.float32).contiguous()
         w_val_all = torch.full((N,), 1.0 / (batch * self.out_scale ** 2), dtype=torch.float32, device=dev)
-        w_force_all = (force_weight / (batch * gnorm2)).float()
+        w_force_all = (force_weight / (batch * gnorm2)).float().contiguous()
         m = torch.zeros_like(self.params)
         v = torch.zeros_like(self.params)
+        # the batches: consecutive slices of a fresh permutation per pass over
+        # the set (the last partial slice of a pass is dropped)
         gen = torch.Generator(device=dev).manual_seed(seed)
-        perm = torch.randperm(N, generator=gen, device=dev)
-        pos = 0
-        for it in range(1, steps + 1):
-            if pos + batch > N:
-                perm = torch.randperm(N, generator=gen, device=dev)
-                pos = 0
-            idx = perm[pos:pos + batch]
-            pos += batch
-            loss, g = self.loss_grad(x[idx], phi[idx], grad[idx], w_val_all[idx], w_force_all[idx])
-            lr_t = lr_min + 0.5 * (lr - lr_min) * (1.0 + math.cos(math.pi * (it - 1) / max(steps - 1, 1)))
-            _abi.call("ss_mlp_adam", ptr(self.params), ptr(g), ptr(m), ptr(v), NPARAM, it, C.c_float(lr_t),
-                      C.c_float(0.9), C.c_float(0.999), C.c_float(1e-8), stream_handle())
-            if log_every and (it % log_every == 0 or it == steps):
-                self.history.append((it, float(loss[0]), float(loss[1])))
+        per_pass = N // batch
+        parts, have = [], 0
+        while have < steps:
+            parts.append(torch.randperm(N, generator=gen, device=dev)[:per_pass * batch])
+            have += per_pass
+        order = torch.cat(parts)[:steps * batch].to(torch.int32).contiguous()
+        log = torch.empty(max(steps, 1), 2, dtype=torch.float32, device=dev)
+        lib = _abi.load()
+        need = lib.ss_mlp_fit_workspace_bytes(batch)
+        ws, nb = _core.aligned_ptr(_core.Workspace.get(need, dev, "mlp_fit"))
+        st = self.struct()
+        _abi.call("ss_mlp_fit", C.byref(st), ptr(self.params), ptr(x), ptr(phi), ptr(grad), ptr(w_val_all),
+                  ptr(w_force_all), N, ptr(order), batch, steps, C.c_float(lr), C.c_float(lr_min), C.c_float(0.9),
+                  C.c_float(0.999), C.c_float(1e-8), ptr(m), ptr(v), ptr(log), ws, nb, stream_handle())
+        if log_every and steps:
+            logged = [it for it in range(1, steps + 1) if it % log_every == 0 or it == steps]
+            lh = log[torch.as_tensor([it - 1 for it in logged], device=dev)].cpu().numpy()
+            self.history.extend((it, float(a), float(b)) for it, (a, b) in zip(logged, lh))
         return self
 
     @staticmethod

@@ -288,3 +288,47 @@ def test_judged_surrogate_stream_falls_back_to_the_exact_force(ss, trained):
         assert torch.equal(a, b)
     for a, b in zip(none, plain):
         assert torch.equal(a, b)
+
+
+def test_library_fit_equals_step_by_step_adam(ss):
+    """ss_mlp_fit (the whole Adam loop in the library: batch gather, loss
+    gradient, Adam step with the cosine learning rate) equals the same steps
+    taken one call at a time (ss_mlp_loss_grad + ss_mlp_adam on the same
+    batches), bit for bit."""
+    import ctypes as C
+
+    from streamsculptor_gb300 import _abi
+    from streamsculptor_gb300._core import ptr, stream_handle
+    from streamsculptor_gb300.surrogate import NPARAM
+    a, b = _surrogate(ss, seed=17), _surrogate(ss, seed=17)
+    N, B, steps = 4096, 512, 20
+    x = torch.tensor(_points(N, seed=18), dtype=torch.float32, device="cuda")
+    rng = np.random.default_rng(19)
+    phi = torch.tensor(rng.normal(-0.5, 0.2, N), dtype=torch.float32, device="cuda")
+    g = torch.tensor(rng.normal(0, 0.01, (N, 3)), dtype=torch.float32, device="cuda")
+    wv = torch.full((N,), 1.0 / B, dtype=torch.float32, device="cuda")
+    wf = torch.tensor(rng.uniform(0.5, 1.5, N) / B * 1e4, dtype=torch.float32, device="cuda")
+    order = torch.tensor(rng.integers(0, N, steps * B), dtype=torch.int32, device="cuda")
+    lr, lr_min = float(np.float32(2e-3)), float(np.float32(2e-5))  # as the library receives them
+    # step by step
+    m, v = torch.zeros_like(a.params), torch.zeros_like(a.params)
+    for s in range(steps):
+        idx = order[s * B:(s + 1) * B].long()
+        _, gr = a.loss_grad(x[idx], phi[idx], g[idx], wv[idx], wf[idx])
+        lr_s = lr_min + 0.5 * (lr - lr_min) * (1.0 + math.cos(math.pi * s / (steps - 1)))
+        _abi.call("ss_mlp_adam", ptr(a.params), ptr(gr), ptr(m), ptr(v), NPARAM, s + 1, C.c_float(lr_s),
+                  C.c_float(0.9), C.c_float(0.999), C.c_float(1e-8), stream_handle())
+    # the library loop
+    m2, v2 = torch.zeros_like(b.params), torch.zeros_like(b.params)
+    log = torch.empty(steps, 2, dtype=torch.float32, device="cuda")
+    lib = _abi.load()
+    ws = torch.empty(lib.ss_mlp_fit_workspace_bytes(B) + 256, dtype=torch.uint8, device="cuda")
+    base = (ws.data_ptr() + 255) // 256 * 256
+    st = b.struct()
+    _abi.call("ss_mlp_fit", C.byref(st), ptr(b.params), ptr(x), ptr(phi), ptr(g), ptr(wv), ptr(wf), N, ptr(order), B,
+              steps, C.c_float(lr), C.c_float(lr_min), C.c_float(0.9), C.c_float(0.999), C.c_float(1e-8), ptr(m2),
+              ptr(v2), ptr(log), C.c_void_p(base), ws.numel() - (base - ws.data_ptr()), stream_handle())
+    torch.cuda.synchronize()
+    assert torch.equal(a.params, b.params)
+    assert torch.equal(m, m2) and torch.equal(v, v2)
+    assert bool(torch.isfinite(log).all())
