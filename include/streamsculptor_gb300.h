@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define SS_ABI_VERSION 6
+#define SS_ABI_VERSION 7
 #define SS_MAX_COMPONENTS 16
 
 /* ---------------------------------------------------------------- status */
@@ -78,7 +78,10 @@ typedef enum ss_kind {
 /* Largest degree of a spherical-harmonic expansion. */
 #define SS_SHEXP_LMAX 8
 
-enum { SS_CENTER_ORIGIN = 0, SS_CENTER_TRACK = 1 };
+/* ss_component.center: SS_CENTER_ORIGIN or SS_CENTER_TRACK, optionally OR
+ * SS_GROWS: the component is multiplied by the potential's growth track g(t)
+ * (column 0 of ss_potential.growth): GrowingPotential, potential.py:464-477. */
+enum { SS_CENTER_ORIGIN = 0, SS_CENTER_TRACK = 1, SS_GROWS = 4 };
 
 typedef struct ss_component {
     int32_t kind;   /* ss_kind */
@@ -165,6 +168,9 @@ typedef struct ss_potential {
      * is d/dt of this track, a linear track's segment slopes; unused
      * otherwise): the MW's reflex motion of MW_LMC_Potential, potential.py:555-662. */
     ss_track frame_velocity;
+    /* Growth factor g(t) of the SS_GROWS components: column 0 of this track
+     * (cubic Hermite or linear like the center track; unused otherwise). */
+    ss_track growth;
 } ss_potential;
 
 /* ------------------------------------------------------------- configs */

@@ -80,6 +80,7 @@ class HostModel:
     subhalos: Optional[dict] = None  # kind, m, a, x0, v, t0, t_window
     expansion: Optional[tuple] = None  # (l_max, log_r0, dlog_r, coef [n_knots, (l_max+1)^2, 2])
     frame_velocity: Optional[tuple] = None  # (t0, dt, velocities [n,3]) or (..., "linear")
+    growth: Optional[tuple] = None  # (t0, dt, g [n]) or (..., "linear"): the SS_GROWS components' factor
     _keep: list = field(default_factory=list)
 
     def _track(self, spec) -> _abi.ss_track:
@@ -106,6 +107,10 @@ class HostModel:
             P.track = self._track(self.track)
         if self.frame_velocity is not None:
             P.frame_velocity = self._track(self.frame_velocity)
+        if self.growth is not None:
+            g = f8(self.growth[2]).reshape(-1)
+            P.growth = self._track((self.growth[0], self.growth[1], np.stack([g, 0 * g, 0 * g], 1)) +
+                                   tuple(self.growth[3:]))
         if self.subhalos is not None:
             P.subhalos = self.sh_struct()
         if self.expansion is not None:

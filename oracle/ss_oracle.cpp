@@ -474,17 +474,25 @@ S phi_total(const ss_potential& P, const S x[3], double t) {
     bool have_c = false;
     for (int k = 0; k < P.n_components; ++k) {
         const ss_component& comp = P.comp[k];
-        if (comp.center == SS_CENTER_TRACK) {
+        // GrowingPotential.potential, potential.py:474-477: the wrapped
+        // potential times growth_func(t) (column 0 of the growth track)
+        double gk = 1.0;
+        if (comp.center & SS_GROWS) {
+            double gv[3];
+            track_eval(P.growth, t, gv);
+            gk = gv[0];
+        }
+        if (comp.center & SS_CENTER_TRACK) {
             if (!have_c) {
                 track_eval(P.track, t, c);
                 have_c = true;
             }
             S xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
-            acc = acc + (comp.kind == SS_SH_EXPANSION ? phi_expansion(P.expansion, comp.p[0], xs)
-                                                      : phi_component_t(comp, P.G, xs, t, P.frame_velocity));
+            acc = acc + gk * (comp.kind == SS_SH_EXPANSION ? phi_expansion(P.expansion, comp.p[0], xs)
+                                                           : phi_component_t(comp, P.G, xs, t, P.frame_velocity));
         } else {
-            acc = acc + (comp.kind == SS_SH_EXPANSION ? phi_expansion(P.expansion, comp.p[0], x)
-                                                      : phi_component_t(comp, P.G, x, t, P.frame_velocity));
+            acc = acc + gk * (comp.kind == SS_SH_EXPANSION ? phi_expansion(P.expansion, comp.p[0], x)
+                                                           : phi_component_t(comp, P.G, x, t, P.frame_velocity));
         }
     }
     const ss_subhalos& sh = P.subhalos;

@@ -10,7 +10,7 @@ import ctypes as C
 import os
 import threading
 
-SS_ABI_VERSION = 6
+SS_ABI_VERSION = 7
 SS_MAX_COMPONENTS = 16
 
 SS_OK = 0
@@ -35,6 +35,7 @@ SS_SHEXP_LMAX = 8
 
 SS_CENTER_ORIGIN = 0
 SS_CENTER_TRACK = 1
+SS_GROWS = 4
 
 SS_SH_PLUMMER = 1
 SS_SH_HERNQUIST = 2
@@ -70,7 +71,8 @@ class ss_expansion(C.Structure):
 class ss_potential(C.Structure):
     _fields_ = [("G", C.c_double), ("n_components", C.c_int32), ("reserved", C.c_int32),
                 ("comp", ss_component * SS_MAX_COMPONENTS), ("track", ss_track),
-                ("subhalos", ss_subhalos), ("expansion", ss_expansion), ("frame_velocity", ss_track)]
+                ("subhalos", ss_subhalos), ("expansion", ss_expansion), ("frame_velocity", ss_track),
+                ("growth", ss_track)]
 
 
 class ss_stream_cfg(C.Structure):

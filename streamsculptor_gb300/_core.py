@@ -136,6 +136,15 @@ class CenterTrack:
                       stream_handle())
         return self.slopes
 
+    @staticmethod
+    def growth_from_samples(ts, values, linear=False) -> "CenterTrack":
+        """A scalar track (GrowingPotential's growth factor) through values at
+        uniform times ts: column 0 of a three-column track."""
+        v = f64(values).reshape(-1)
+        t = CenterTrack.from_samples(ts, torch.stack([v, torch.zeros_like(v), torch.zeros_like(v)], 1))
+        t.linear = bool(linear)
+        return t
+
 
 @dataclass
 class SubhaloTable:
@@ -197,6 +206,7 @@ class Flat:
     subhalos: Optional[SubhaloTable] = None
     expansion: Optional[ExpansionTable] = None
     frame_velocity: Optional[CenterTrack] = None
+    growth: Optional[CenterTrack] = None
 
     def extend(self, other: "Flat"):
         self.comps.extend(other.comps)
@@ -216,6 +226,10 @@ class Flat:
             if self.frame_velocity is not None and self.frame_velocity is not other.frame_velocity:
                 raise NotImplementedError("at most one uniform frame acceleration per potential")
             self.frame_velocity = other.frame_velocity
+        if other.growth is not None:
+            if self.growth is not None and self.growth is not other.growth:
+                raise NotImplementedError("at most one growth track per potential")
+            self.growth = other.growth
 
 
 def make_struct(flat: Flat, G: float) -> _abi.ss_potential:
@@ -233,6 +247,8 @@ def make_struct(flat: Flat, G: float) -> _abi.ss_potential:
         P.track = flat.track.struct()
     if flat.frame_velocity is not None:
         P.frame_velocity = flat.frame_velocity.struct()
+    if flat.growth is not None:
+        P.growth = flat.growth.struct()
     if flat.subhalos is not None:
         P.subhalos = flat.subhalos.struct()
     if flat.expansion is not None:

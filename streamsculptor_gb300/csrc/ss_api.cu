@@ -58,10 +58,10 @@ int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalo
         const double* p = c.p;
         CompDev<R>& d = out->c[k];
         d.kind = c.kind;
-        SS_CHECK_ARG(c.center == SS_CENTER_ORIGIN || c.center == SS_CENTER_TRACK,
-                     "component %d: center=%d invalid", k, c.center);
-        d.center = c.center;
-        need_track |= (c.center == SS_CENTER_TRACK);
+        SS_CHECK_ARG((c.center & ~(SS_CENTER_TRACK | SS_GROWS)) == 0, "component %d: center=%d invalid", k, c.center);
+        d.center = c.center & SS_CENTER_TRACK;
+        need_track |= (d.center == SS_CENTER_TRACK);
+        if (c.center & SS_GROWS) out->grow_mask |= 1 << k;
         for (int i = 0; i < 6; ++i) SS_CHECK_ARG(std::isfinite(p[i]), "component %d: non-finite parameter p[%d]", k, i);
         // FP32 only: slot 5 of the spherical and disk kinds holds the relative
         // rounding of q[0] = G m, (G m - q[0]) / q[0], and slot 4 of NFW that
@@ -164,6 +164,18 @@ int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalo
             default:
                 return set_error(SS_ERR_INVALID_ARGUMENT, "component %d: unknown kind %d", k, c.kind);
         }
+    }
+    if (out->grow_mask) {
+        const ss_track& gr = in->growth;
+        SS_CHECK_ARG(gr.knots != nullptr && gr.n_knots >= 2 && std::isfinite(gr.dt) && gr.dt > 0.0 &&
+                         std::isfinite(gr.t0) && (gr.linear || gr.slopes != nullptr),
+                     "SS_GROWS components need a growth track with >= 2 knots, dt > 0");
+        out->growth.knots = gr.knots;
+        out->growth.slopes = gr.slopes;
+        out->growth.t0 = gr.t0;
+        out->growth.dt = gr.dt;
+        out->growth.n = gr.n_knots;
+        out->growth.linear = gr.linear ? 1 : 0;
     }
     out->has_track = need_track ? 1 : 0;
     if (need_track) {
@@ -279,11 +291,12 @@ __global__ void potential_eval_kernel(PotDev<double> P, const double* __restrict
     if (phi) {
         double f = 0.0;
         for (int k = 0; k < P.n; ++k) {
+            const double gk = ((P.grow_mask >> k) & 1) ? td.amp : 1.0;  // GrowingPotential
             if (P.c[k].center == SS_CENTER_TRACK) {
                 double xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
-                f += comp_phi(P, P.c[k], xs, td);
+                f += gk * comp_phi(P, P.c[k], xs, td);
             } else {
-                f += comp_phi(P, P.c[k], x, td);
+                f += gk * comp_phi(P, P.c[k], x, td);
             }
         }
         for (int j = 0; j < P.sh.n; ++j) {

@@ -261,6 +261,10 @@ struct PotDev {
     int32_t has_rot;
     int32_t has_facc;
     TrackDev fvel;
+    // SS_GROWS: bit k set when component k is multiplied by g(t), column 0
+    // of the growth track
+    int32_t grow_mask;
+    TrackDev growth;
 };
 
 // What the time-dependent components need at one evaluation time: the
@@ -271,7 +275,8 @@ template <class T>
 struct TimeDep {
     T c, s;
     T ga[3];
-    __host__ __device__ TimeDep() : c(T(1)), s(T(0)) { ga[0] = ga[1] = ga[2] = T(0); }
+    T amp;  // growth factor g(t) of the SS_GROWS components
+    __host__ __device__ TimeDep() : c(T(1)), s(T(0)), amp(T(1)) { ga[0] = ga[1] = ga[2] = T(0); }
 };
 
 // --------------------------------------------------------------- track
@@ -332,6 +337,11 @@ __device__ inline TimeDep<double> time_dep(const PotDev<R>& P, double t) {
     TimeDep<double> td;
     if (P.has_rot) sincos(P.omega * t, &td.s, &td.c);
     if (P.has_facc) track_slope(P.fvel, t, td.ga);
+    if (P.grow_mask) {
+        double gv[3];
+        track_eval(P.growth, t, gv);
+        td.amp = gv[0];
+    }
     return td;
 }
 
@@ -343,6 +353,7 @@ __device__ __forceinline__ TimeDep<T> time_dep_as(const TimeDep<S>& a) {
     r.ga[0] = T(a.ga[0]);
     r.ga[1] = T(a.ga[1]);
     r.ga[2] = T(a.ga[2]);
+    r.amp = T(a.amp);
     return r;
 }
 
@@ -1495,10 +1506,25 @@ __device__ __forceinline__ void pot_grad(const PotDev<R>& P, const T x[3], const
 #pragma unroll 1
     for (int k = 0; k < P.n; ++k) {
         const CompDev<R>& c = P.c[k];
-        if (c.kind == SS_SH_EXPANSION)
-            shexp_grad<T, R, HESS>(P.ex, c.q[0], c.center == SS_CENTER_TRACK ? xs : x, grad, H);
-        else
-            comp_grad<T, R, HESS>(c, c.center == SS_CENTER_TRACK ? xs : x, grad, H, td);
+        const T* xc = c.center == SS_CENTER_TRACK ? xs : x;
+        if ((P.grow_mask >> k) & 1) {
+            // GrowingPotential: this component times g(t)
+            T g2[3] = {T(0), T(0), T(0)}, H2[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+            if (c.kind == SS_SH_EXPANSION)
+                shexp_grad<T, R, HESS>(P.ex, c.q[0], xc, g2, H2);
+            else
+                comp_grad<T, R, HESS>(c, xc, g2, H2, td);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) grad[i] += td.amp * g2[i];
+            if (HESS) {
+#pragma unroll
+                for (int i = 0; i < 6; ++i) H[i] += td.amp * H2[i];
+            }
+        } else if (c.kind == SS_SH_EXPANSION) {
+            shexp_grad<T, R, HESS>(P.ex, c.q[0], xc, grad, H);
+        } else {
+            comp_grad<T, R, HESS>(c, xc, grad, H, td);
+        }
     }
 }
 
@@ -1586,6 +1612,7 @@ using CompSHExp = Comp<SS_SH_EXPANSION>;
 // Calls f(Comp{}) for the matching compiled composition, else f(GenericComp{}).
 template <class R, class F>
 inline auto dispatch_comp(const PotDev<R>& P, F&& f) {
+    if (P.grow_mask) return f(GenericComp{});  // growing components: the generic loop scales them
     if (CompMW3::matches(P)) return f(CompMW3{});
     if (CompMW3P::matches(P)) return f(CompMW3P{});
     if (CompGala::matches(P)) return f(CompGala{});

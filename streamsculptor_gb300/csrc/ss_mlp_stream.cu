@@ -659,7 +659,7 @@ static int mlp_stream(const ss_mlp* mlp, const ss_potential* exact, const ss_str
         SS_CHECK_ARG(judge_every >= 1, "judge_every must be >= 1");
         int rc = prepare_potential<float>(exact, &ka.X, false);
         if (rc) return rc;
-        SS_CHECK_ARG(!ka.X.has_track && !ka.X.has_rot && !ka.X.has_facc,
+        SS_CHECK_ARG(!ka.X.has_track && !ka.X.has_rot && !ka.X.has_facc && !ka.X.grow_mask,
                      "the judge's exact potential must be static, without a center track");
         for (int k = 0; k < ka.X.n; ++k) {
             const int kd = ka.X.c[k].kind;

@@ -141,6 +141,7 @@ __global__ void __launch_bounds__(96) shoot_jac_kernel(PotDev<float> P32, ShootA
     PotDev<T> Q;
     Q.n = P32.n;
     Q.has_track = 0;
+    Q.grow_mask = 0;
     Q.ex = P32.ex;
 #pragma unroll
     for (int c = 0; c < C::n; ++c) {
@@ -339,6 +340,7 @@ template <class S_>
 __device__ __forceinline__ void seed_params(const PotDev<double>& P, const TanArgs& a, int slot, PotDev<D1<S_>>& Q) {
     Q.n = P.n;
     Q.has_track = 0;
+    Q.grow_mask = 0;
     Q.ex = P.ex;
     for (int c = 0; c < P.n; ++c) {
         double dq[6] = {0, 0, 0, 0, 0, 0};
@@ -446,7 +448,7 @@ int ss_orbit_shoot_f64(const ss_potential* pot, const double* w0, double t0, dou
     SS_CHECK_ARG(w0 && out, "NULL buffer");
     SS_CHECK_ARG(tol > 0.0 && tol < 1e-6, "tol must be in (0, 1e-6)");
     cudaStream_t st = (cudaStream_t)stream;
-    const bool is_static = !P.has_track && P.sh.n == 0 && !P.has_rot && !P.has_facc;
+    const bool is_static = !P.has_track && P.sh.n == 0 && !P.has_rot && !P.has_facc && !P.grow_mask;
     const int64_t S = (n_steps + SHOOT_M - 1) / SHOOT_M;
     bool handled = false;
     if (is_static && S >= 2) {
@@ -501,7 +503,7 @@ int ss_prog_tangents_f64(const ss_potential* pot, const double* raw_params, cons
     PotDev<double> P;
     int rc = prepare_potential<double>(pot, &P, false);
     if (rc) return rc;
-    SS_CHECK_ARG(!P.has_track && !P.has_rot && !P.has_facc, "progenitor tangents need a static potential");
+    SS_CHECK_ARG(!P.has_track && !P.has_rot && !P.has_facc && !P.grow_mask, "progenitor tangents need a static potential");
     SS_CHECK_ARG(P.n >= 1 && P.n <= 4, "progenitor tangents support 1 to 4 components (one warp of directions)");
     SS_CHECK_ARG(std::isfinite(dt) && dt > 0.0 && n_steps >= 2 * SHOOT_M && save_every >= 1, "bad steps");
     SS_CHECK_ARG(raw_params && w0 && states && tangents, "NULL buffer");

@@ -82,13 +82,14 @@ __global__ void time_table_kernel(PotDev<float> P, double t0, double dt, int32_t
     const double cs[5] = {0.0, SS_C2, SS_C3, SS_C4, SS_C5};
     const TimeDep<double> td = time_dep(P, t0 + ((double)n + cs[s]) * dt);
     tab[2 * i] = make_float4((float)td.c, (float)td.s, (float)td.ga[0], (float)td.ga[1]);
-    tab[2 * i + 1] = make_float4((float)td.ga[2], 0.f, 0.f, 0.f);
+    tab[2 * i + 1] = make_float4((float)td.ga[2], (float)td.amp, 0.f, 0.f);
 }
 
 static bool has_time_dep(const ss_potential* pot) {
     for (int k = 0; k < pot->n_components && k < SS_MAX_COMPONENTS; ++k) {
         const int kd = pot->comp[k].kind;
-        if (kd == SS_BAR || kd == SS_DEHNEN_BAR || kd == SS_UNIFORM_ACCEL) return true;
+        if (kd == SS_BAR || kd == SS_DEHNEN_BAR || kd == SS_UNIFORM_ACCEL || (pot->comp[k].center & SS_GROWS))
+            return true;
     }
     return false;
 }
@@ -198,7 +199,7 @@ int expansion_table32(PotDev<float>& P, void* ws, cudaStream_t s) {
 static int64_t f32k_workspace(const ss_potential* pot, const ss_stream_cfg* cfg) {
     int64_t bytes = 0;
     bool track = false;
-    for (int k = 0; k < pot->n_components && k < SS_MAX_COMPONENTS; ++k) track |= pot->comp[k].center == SS_CENTER_TRACK;
+    for (int k = 0; k < pot->n_components && k < SS_MAX_COMPONENTS; ++k) track |= (pot->comp[k].center & SS_CENTER_TRACK) != 0;
     if (track) bytes += (5 * cfg->n_steps + 1) * 2 * (int64_t)sizeof(float4);
     bytes = (bytes + 255) / 256 * 256;
     if (has_time_dep(pot)) bytes += (5 * cfg->n_steps + 1) * 2 * (int64_t)sizeof(float4);

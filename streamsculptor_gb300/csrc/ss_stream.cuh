@@ -29,7 +29,7 @@ struct StreamArgs {
     float h_lo;
     const float4* ctab;   // [(n_steps*5+1) x 2] track positions (hi, lo) at stage times
     const float4* shtab;  // [n_sh*3] subhalo lines
-    const float4* ttab;   // [(n_steps*5+1) x 2] (cos, sin, ga.x, ga.y), (ga.z, -, -, -) at stage times
+    const float4* ttab;   // [(n_steps*5+1) x 2] (cos, sin, ga.x, ga.y), (ga.z, g, -, -) at stage times
     int32_t n_sh;
     int32_t sh_kind;
     ShDev shg;  // SS_SH_GRID: the FP64 spline tables of the subhalos
@@ -190,6 +190,7 @@ __device__ __forceinline__ void accel_f32(const PotDev<float>& P, const StreamAr
         td.ga[0] = t0.z;
         td.ga[1] = t0.w;
         td.ga[2] = t1.x;
+        td.amp = t1.y;
     }
     C::template grad<float, float, false>(P, X, xs, g, nullptr, td);
     if constexpr (SUB != SUB_NONE) {

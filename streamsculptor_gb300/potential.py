@@ -263,6 +263,30 @@ class TimeDepTranslatingPotential(Potential):
         return Flat(comps, track=self.center_spl)
 
 
+class GrowingPotential(Potential):
+    """pot times a growth factor g(t) (GrowingPotential, potential.py:464-477).
+
+    growth_func must be a scalar track on uniform knots, e.g.
+    CenterTrack.growth_from_samples(ts, g) (cubic Hermite with the
+    interpax-'cubic' slopes of the center tracks, or linear=True); a Python
+    callable cannot run in a kernel.  Every component of pot is multiplied
+    by g(t) in the potential, its gradient and Hessian."""
+
+    def __init__(self, pot, growth_func, units=None):
+        super().__init__(units, {"pot": pot, "growth_func": growth_func})
+
+    def _flatten(self):
+        if not isinstance(self.growth_func, CenterTrack):
+            raise NotImplementedError("growth_func must be a track (CenterTrack.growth_from_samples): arbitrary "
+                                      "callables cannot run on the GPU")
+        inner = self.pot._flatten()
+        if inner.growth is not None or inner.subhalos is not None:
+            raise NotImplementedError("nested growing potentials / subhalos inside a growing potential")
+        comps = [(k, c | _abi.SS_GROWS, p) for (k, c, p) in inner.comps]
+        return Flat(comps, track=inner.track, expansion=inner.expansion, frame_velocity=inner.frame_velocity,
+                    growth=self.growth_func)
+
+
 class ProgenitorPotential(Potential):
     """prog_pot(m, r_s) centred on the progenitor track (potential.py:140-153)."""
 
@@ -713,7 +737,7 @@ class CustomPotential(Potential):
         super().__init__(units, {"potential_func": potential_func})
 
 
-__all__ = ["PowerLawCutoffPotential", "BovyMWPotential2014", "MiyamotoNagaiDisk", "NFWPotential",
+__all__ = ["GrowingPotential", "PowerLawCutoffPotential", "BovyMWPotential2014", "MiyamotoNagaiDisk", "NFWPotential",
            "TriaxialNFWPotential", "Isochrone", "PlummerPotential",
            "HernquistPotential", "Potential_Combine", "TimeDepTranslatingPotential", "ProgenitorPotential",
            "GalaMilkyWayPotential", "SubhaloLinePotential", "SubhaloLinePotential_dRadius", "BarPotential",

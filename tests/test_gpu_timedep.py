@@ -1,6 +1,7 @@
 """GPU parity of the time-dependent potentials: the rotating bars
-(BarPotential, DehnenBarPotential), the uniform frame acceleration and
-MW_LMC_Potential (linear LMC and Milky Way velocity tracks) — the potential,
+(BarPotential, DehnenBarPotential), the uniform frame acceleration,
+MW_LMC_Potential (linear LMC and Milky Way velocity tracks) and
+GrowingPotential (cubic and linear growth tracks) — the potential,
 gradient and Hessian at points and times, the release at each release
 time, and whole streams in FP64 (<= 1e-10) and FP32 compensated (<= 1e-5),
 all against the oracle."""
@@ -205,3 +206,56 @@ def test_potential_from_density_gpu(ss, oracle):
     lead, trail = pot.gen_stream_vmapped(ts=ts, prog_w0=back, Msat=2e4, normals=normals)
     final = final.reshape(n, 2, 6)
     assert phase_err(np64(lead), final[:, 0]) <= 1e-10 and phase_err(np64(trail), final[:, 1]) <= 1e-10
+
+
+def _growing(ss, oracle, linear):
+    """GrowingPotential (potential.py:464-477) of the stream workloads'
+    potential with a growth factor from 0.6 to 1 over 3 Gyr (knots every
+    50 Myr), and the oracle's model of it."""
+    import torch
+
+    from streamsculptor_gb300 import potential as P
+    from streamsculptor_gb300._core import CenterTrack
+    tk = np.arange(61) * 50.0 - 3000.0
+    g = 0.6 + 0.4 * (1.0 + tk / 3000.0) ** 1.5 + 0.02 * np.sin(tk / 170.0)
+    tr = CenterTrack.growth_from_samples(tk, torch.as_tensor(g, device="cuda"), linear=linear)
+    gpu = P.GrowingPotential(mw3_gpu(ss), tr, units=ss.usys)
+    orc = oracle.HostModel([(k, c | _abi.SS_GROWS, p) for (k, c, p) in oracle.mw3()],
+                           growth=(tk[0], 50.0, g) + (("linear",) if linear else ()))
+    return gpu, orc
+
+
+@pytest.mark.parametrize("linear", [False, True])
+def test_growing_potential_eval(ss, oracle, linear):
+    """Potential, gradient and Hessian of a growing potential at points and
+    times spread over the growth track, against the oracle."""
+    gpu, orc = _growing(ss, oracle, linear)
+    rng = np.random.default_rng(23)
+    x = rng.normal(0, 10, (400, 3))
+    t = rng.uniform(-3100.0, 50.0, 400)  # past both ends too (the end segments continue)
+    phi_o, g_o, H_o = oracle.potential_eval(orc, x, t)
+    import torch
+    tt = torch.as_tensor(t, device="cuda")
+    assert rel_err(np64(gpu.potential(x, tt)), phi_o) < 1e-12
+    assert rel_err(np64(gpu.gradient(x, tt)), g_o) < 1e-12
+    assert rel_err(np64(gpu.jacobian_force(x, tt)), H_o) < 1e-11
+
+
+def test_growing_potential_stream(ss, oracle):
+    """A Fardal stream (400 releases, 1 Myr steps) in a growing potential:
+    progenitor orbit, release and particles, FP64 and FP32 compensated,
+    against the oracle."""
+    gpu, orc = _growing(ss, oracle, False)
+    n = 400
+    back = oracle.orbit(orc, PROG_WF, 0.0, -1.0, n, n)[0, -1]
+    ts = -n + np.arange(n + 1) * 1.0
+    normals = np.random.default_rng(29).standard_normal((n + 1, 1, 4))
+    ws = oracle.orbit(orc, back, ts[0], 1.0, n, 1)[0]
+    ics, _ = oracle.release(orc, ws, ts, 2e4, normals)
+    final, _, st = oracle.stream(orc, ts[0], 1.0, n, ics[:-1].reshape(-1, 6), 2, 1)
+    assert (st == 0).all()
+    final = final.reshape(n, 2, 6)
+    for precision, tol in (("f64", 1e-10), ("f32k", 1e-5)):
+        lead, trail = gpu.gen_stream_vmapped(ts=ts, prog_w0=back, Msat=2e4, normals=normals, precision=precision)
+        assert phase_err(np64(lead), final[:, 0]) <= tol, precision
+        assert phase_err(np64(trail), final[:, 1]) <= tol, precision

@@ -391,3 +391,23 @@ def test_rotating_bars_and_frame_acceleration(oracle):
         _, g, H = oracle.potential_eval(m, rng.normal(0, 5, (4, 3)), t)
         assert np.allclose(g, (vel[k + 1] - vel[k]) / 25.0, rtol=1e-13, atol=1e-18)
         assert np.all(H == 0)
+
+
+def test_growing_potential_oracle(oracle):
+    """GrowingPotential on the oracle (potential.py:474-477): the wrapped
+    potential times the growth track's value at t (linear here, so the
+    factor is known in closed form), in the potential and its derivatives."""
+    comps = [(_abi.SS_NFW, 0, (5.4e11, 15.62, 0.0)), (_abi.SS_MIYAMOTO_NAGAI, 0, (6.8e10, 3.0, 0.28))]
+    tk = np.arange(11) * 100.0 - 1000.0
+    g = 0.5 + 0.05 * np.arange(11) ** 1.3
+    grow = oracle.HostModel([(k, c | _abi.SS_GROWS, p) for (k, c, p) in comps], growth=(tk[0], 100.0, g, "linear"))
+    plain = oracle.HostModel(comps)
+    rng = np.random.default_rng(3)
+    x = rng.normal(0, 8, (50, 3))
+    t = rng.uniform(-1000.0, 0.0, 50)
+    gt = np.interp(t, tk, g)
+    p1, g1, H1 = oracle.potential_eval(grow, x, t)
+    p0, g0, H0 = oracle.potential_eval(plain, x, t)
+    assert np.allclose(p1, gt * p0, rtol=1e-14, atol=0)
+    assert np.allclose(g1, gt[:, None] * g0, rtol=1e-14, atol=0)
+    assert np.allclose(H1, gt[:, None, None] * H0, rtol=1e-13, atol=1e-30)
