@@ -294,7 +294,7 @@ def test_library_fit_equals_step_by_step_adam(ss):
     """ss_mlp_fit (the whole Adam loop in the library: batch gather, loss
     gradient, Adam step with the cosine learning rate) equals the same steps
     taken one call at a time (ss_mlp_loss_grad + ss_mlp_adam on the same
-    batches), bit for bit."""
+    batches), up to the rounding of the atomic weight-gradient sums."""
     import ctypes as C
 
     from streamsculptor_gb300 import _abi
@@ -329,6 +329,10 @@ def test_library_fit_equals_step_by_step_adam(ss):
               steps, C.c_float(lr), C.c_float(lr_min), C.c_float(0.9), C.c_float(0.999), C.c_float(1e-8), ptr(m2),
               ptr(v2), ptr(log), C.c_void_p(base), ws.numel() - (base - ws.data_ptr()), stream_handle())
     torch.cuda.synchronize()
-    assert torch.equal(a.params, b.params)
-    assert torch.equal(m, m2) and torch.equal(v, v2)
+    # the weight-gradient products sum over the batch with atomics across
+    # CTAs, so two runs differ in the last bits: compare to a tolerance far
+    # below one step's update (lr ~ 2e-3)
+    assert float((a.params - b.params).abs().max()) <= 1e-7 * float(a.params.abs().max())
+    assert float((m - m2).abs().max()) <= 1e-5 * float(m.abs().max())
+    assert float((v - v2).abs().max()) <= 1e-5 * float(v.abs().max())
     assert bool(torch.isfinite(log).all())
