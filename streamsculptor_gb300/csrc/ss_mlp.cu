@@ -349,10 +349,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(int M, int K, co
                                                 __uint_as_float(r[j + 2]), __uint_as_float(r[j + 3]))
                                   : make_float4(qnan, qnan, qnan, qnan);
                     if (ATOMIC) {
-                        atomicAdd(out + j, v.x);
-                        atomicAdd(out + j + 1, v.y);
-                        atomicAdd(out + j + 2, v.z);
-                        atomicAdd(out + j + 3, v.w);
+                        atomicAdd(reinterpret_cast<float4*>(out + j), v);  // one vector atomic (sm_90 and later)
                     } else {
                         if (bias) {
                             const float4 bb = *reinterpret_cast<const float4*>(bias + 32 * q + j);
@@ -494,38 +491,43 @@ __global__ void eval_out_kernel(const float* A4, const float* w5, const float* b
 }
 
 // Loss of each sample; seeds ybar [B] and gbar [B,4]; accumulates loss[0..1].
+// One warp per sample: the lanes read the sample's 128 activations
+// coalesced for y = w5 . a4 and reduce it with shuffles; lane 0 does the rest.
+constexpr int LOSS_ROWS = 8;  // samples (warps) per block
 __global__ void loss_kernel(const float* A4, const float* prm, const float* g, const float* ir2, const float* x,
                             const float* phi_t, const float* g_t, const float* w_val, const float* w_force,
                             int64_t B, MlpNorm nm, float* ybar, float* gbar, float* loss) {
-    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    const int64_t b = (int64_t)blockIdx.x * LOSS_ROWS + w;
     float lv = 0.0f, lf = 0.0f;
     if (b < B) {
         const float* w5 = prm + OFF_W5;
-        float y = prm[OFF_B5];
-        for (int j = 0; j < MW; ++j) y = fmaf(A4[b * MW + j], w5[j], y);
-        const float ev = nm.out_scale * y + nm.out_shift - phi_t[b];
-        lv = w_val[b] * ev * ev;
-        ybar[b] = 2.0f * w_val[b] * ev * nm.out_scale;
-        const float* gb = g + 4 * b;
-        float e[3], ex = 0.0f;
-        for (int j = 0; j < 3; ++j) {
-            const float pred = nm.out_scale * (gb[j] * nm.c[j] + gb[3] * nm.c[3] * x[3 * b + j] * ir2[b]);
-            e[j] = pred - g_t[3 * b + j];
-            lf += e[j] * e[j];
-            ex += e[j] * x[3 * b + j];
+        float y = 0.0f;
+#pragma unroll
+        for (int j = l; j < MW; j += 32) y = fmaf(A4[b * MW + j], w5[j], y);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) y += __shfl_xor_sync(0xffffffffu, y, o);
+        if (l == 0) {
+            y += prm[OFF_B5];
+            const float ev = nm.out_scale * y + nm.out_shift - phi_t[b];
+            lv = w_val[b] * ev * ev;
+            ybar[b] = 2.0f * w_val[b] * ev * nm.out_scale;
+            const float* gb = g + 4 * b;
+            float e[3], ex = 0.0f;
+            for (int j = 0; j < 3; ++j) {
+                const float pred = nm.out_scale * (gb[j] * nm.c[j] + gb[3] * nm.c[3] * x[3 * b + j] * ir2[b]);
+                e[j] = pred - g_t[3 * b + j];
+                lf += e[j] * e[j];
+                ex += e[j] * x[3 * b + j];
+            }
+            lf *= w_force[b];
+            const float k = 2.0f * w_force[b] * nm.out_scale;
+            for (int j = 0; j < 3; ++j) gbar[4 * b + j] = k * nm.c[j] * e[j];
+            gbar[4 * b + 3] = k * nm.c[3] * ex * ir2[b];
         }
-        lf *= w_force[b];
-        const float k = 2.0f * w_force[b] * nm.out_scale;
-        for (int j = 0; j < 3; ++j) gbar[4 * b + j] = k * nm.c[j] * e[j];
-        gbar[4 * b + 3] = k * nm.c[3] * ex * ir2[b];
     }
-    // block reduction of the two loss parts
-    __shared__ float red[2][32];
-    for (int o = 16; o > 0; o >>= 1) {
-        lv += __shfl_down_sync(0xffffffffu, lv, o);
-        lf += __shfl_down_sync(0xffffffffu, lf, o);
-    }
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    // block reduction of the two loss parts (lane 0 of each warp holds its sample's)
+    __shared__ float red[2][LOSS_ROWS];
     if (l == 0) {
         red[0][w] = lv;
         red[1][w] = lf;
@@ -533,7 +535,7 @@ __global__ void loss_kernel(const float* A4, const float* prm, const float* g, c
     __syncthreads();
     if (threadIdx.x == 0) {
         float a = 0.0f, c = 0.0f;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+        for (int i = 0; i < LOSS_ROWS; ++i) {
             a += red[0][i];
             c += red[1][i];
         }
@@ -542,14 +544,18 @@ __global__ void loss_kernel(const float* A4, const float* prm, const float* g, c
     }
 }
 
+// rows per block of the column sums below (one thread per feature): short
+// loops and many blocks, the partial sums added with atomics
+constexpr int SUM_ROWS = 8;
+
 // Zbar4 = ybar w5 * S4 + Sbar4 * P4, Sbar4 = Dbar4 * w5 (computed here);
 // accumulates w5bar += Dbar4 * S4 + ybar A4 (column sums) and b5bar.
 __global__ void top_kernel(const float* Dbar4, const float* S4, const float* P4, const float* A4, const float* ybar,
                            const float* w5, int64_t B, float* Zbar4, float* w5bar, float* b5bar) {
     const int j = threadIdx.x;  // feature (blockDim.x == 128)
-    const int64_t r0 = (int64_t)blockIdx.x * 64;
+    const int64_t r0 = (int64_t)blockIdx.x * SUM_ROWS;
     float acc = 0.0f, accb = 0.0f;
-    for (int64_t b = r0; b < r0 + 64 && b < B; ++b) {
+    for (int64_t b = r0; b < r0 + SUM_ROWS && b < B; ++b) {
         const int64_t i = b * MW + j;
         const float sb = Dbar4[i] * w5[j];
         Zbar4[i] = ybar[b] * w5[j] * S4[i] + sb * P4[i];
@@ -563,9 +569,9 @@ __global__ void top_kernel(const float* Dbar4, const float* S4, const float* P4,
 // bbar[j] += sum_b Zbar[b][j]
 __global__ void colsum_kernel(const float* Z, int64_t B, float* out) {
     const int j = threadIdx.x;
-    const int64_t r0 = (int64_t)blockIdx.x * 64;
+    const int64_t r0 = (int64_t)blockIdx.x * SUM_ROWS;
     float acc = 0.0f;
-    for (int64_t b = r0; b < r0 + 64 && b < B; ++b) acc += Z[b * MW + j];
+    for (int64_t b = r0; b < r0 + SUM_ROWS && b < B; ++b) acc += Z[b * MW + j];
     atomicAdd(out + j, acc);
 }
 
@@ -723,7 +729,7 @@ static int loss_grad_impl(const MlpNorm& nm, const float* prm, const float* x, c
     features_kernel<float><<<blocks(B, 256), 256, 0, st>>>(x, B, nm, w.u, w.ir2);
     SS_LAUNCH_CHECK();
     forward_and_input_grad(prm, B, w, true, st);
-    loss_kernel<<<blocks(B, 256), 256, 0, st>>>(w.A[4], prm, w.g, w.ir2, x, phi_t, g_t, w_val, w_force, B, nm, ybar,
+    loss_kernel<<<blocks(B, LOSS_ROWS), 32 * LOSS_ROWS, 0, st>>>(w.A[4], prm, w.g, w.ir2, x, phi_t, g_t, w_val, w_force, B, nm, ybar,
                                                 gbar, loss);
     SS_LAUNCH_CHECK();
     const float* Wk[5] = {nullptr, prm + OFF_W1, prm + OFF_W2, prm + OFF_W3, prm + OFF_W4};
@@ -741,7 +747,7 @@ static int loss_grad_impl(const MlpNorm& nm, const float* prm, const float* x, c
         gemm<false, true>(B, MW, MW, Ubar, MW, Wk[k + 1], MW, Dbar, MW, nullptr, st);
     }
     // top: Sbar4 = Dbar4 * w5, w5bar, b5bar, Zbar4
-    top_kernel<<<blocks(B, 64), MW, 0, st>>>(Dbar, w.S[4], w.P[4], w.A[4], ybar, prm + OFF_W5, B, Zbar,
+    top_kernel<<<blocks(B, SUM_ROWS), MW, 0, st>>>(Dbar, w.S[4], w.P[4], w.A[4], ybar, prm + OFF_W5, B, Zbar,
                                              grad + OFF_W5, grad + OFF_B5);
     SS_LAUNCH_CHECK();
     for (int k = 4; k >= 1; --k) {
@@ -749,7 +755,7 @@ static int loss_grad_impl(const MlpNorm& nm, const float* prm, const float* x, c
         const float* Aprev = k == 1 ? w.u : w.A[k - 1];
         const int kin = k == 1 ? 4 : MW;
         gemm_acc<true, false>(MW, kin, B, Zbar, MW, Aprev, kin, gW[k], kin, st);
-        colsum_kernel<<<blocks(B, 64), MW, 0, st>>>(Zbar, B, gb[k]);
+        colsum_kernel<<<blocks(B, SUM_ROWS), MW, 0, st>>>(Zbar, B, gb[k]);
         SS_LAUNCH_CHECK();
         if (k == 1) break;
         // Abar_{k-1} = Zbar_k W_k ; Zbar_{k-1} = Abar * S_{k-1} + Sbar_{k-1} * P_{k-1}
