@@ -211,10 +211,17 @@ __device__ __forceinline__ uint32_t tc_off(int r, int k) {
 
 __device__ __forceinline__ float tf32_head(float a) { return __uint_as_float(__float_as_uint(a) & 0xffffe000u); }
 
-// stage rows [r0, r0 + 128) x K [k0, k0 + 32) of one operand as head and
-// remainder; rows at or past `rows` are zero
+// One operand's 128 x 32 chunk in flight: rows [r0, r0 + 128) x K [k0,
+// k0 + 32), 8 float4 per thread, loaded to registers first (tc_load) so the
+// loads of chunk c + 1 overlap the MMAs of chunk c, then split into head and
+// remainder and stored as core matrices (tc_put).  Rows at or past `rows`
+// are zero.
+struct TcRegs {
+    float4 v[8];
+};
+
 template <bool T>
-__device__ __forceinline__ void tc_stage(uint8_t* hi, uint8_t* lo, const float* X, int ld, int r0, int rows, int k0) {
+__device__ __forceinline__ void tc_load(TcRegs& g, const float* X, int ld, int r0, int rows, int k0) {
     const int t = threadIdx.x;
     if (!T) {
         // float4 along K: 8 consecutive threads take rows r..r+7 at one K
@@ -223,46 +230,60 @@ __device__ __forceinline__ void tc_stage(uint8_t* hi, uint8_t* lo, const float* 
         for (int i = 0; i < 8; ++i) {
             const int idx = t + TC_THREADS * i;
             const int r = ((idx >> 6) << 3) | (idx & 7), kq = (idx >> 3) & 7;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (r0 + r < rows) v = *reinterpret_cast<const float4*>(X + (int64_t)(r0 + r) * ld + k0 + 4 * kq);
-            const float4 h = make_float4(tf32_head(v.x), tf32_head(v.y), tf32_head(v.z), tf32_head(v.w));
-            const uint32_t o = tc_off(r, 4 * kq);
-            *reinterpret_cast<float4*>(hi + o) = h;
-            *reinterpret_cast<float4*>(lo + o) = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+            g.v[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (r0 + r < rows) g.v[i] = *reinterpret_cast<const float4*>(X + (int64_t)(r0 + r) * ld + k0 + 4 * kq);
         }
     } else {
-        // X[k][r]: a 4 x 4 block per thread (four float4 along r at
-        // consecutive k), transposed in registers into four 16-byte stores
+        // X[k][r]: a 4 x 4 block per thread and pass (four float4 along r at
+        // consecutive k), transposed in registers when stored
 #pragma unroll
         for (int i = 0; i < 2; ++i) {
             const int idx = t + TC_THREADS * i;
             const int rq = idx & 31, kq = idx >> 5;
             const int r = 4 * rq;
-            float4 v[4];
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                v[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+                float4& v = g.v[4 * i + j];
+                v = make_float4(0.f, 0.f, 0.f, 0.f);
                 const float* src = X + (int64_t)(k0 + 4 * kq + j) * ld + r0 + r;
                 if (r0 + r + 3 < rows) {
-                    v[j] = *reinterpret_cast<const float4*>(src);
+                    v = *reinterpret_cast<const float4*>(src);
                 } else {
-                    if (r0 + r < rows) v[j].x = src[0];
-                    if (r0 + r + 1 < rows) v[j].y = src[1];
-                    if (r0 + r + 2 < rows) v[j].z = src[2];
+                    if (r0 + r < rows) v.x = src[0];
+                    if (r0 + r + 1 < rows) v.y = src[1];
+                    if (r0 + r + 2 < rows) v.z = src[2];
                 }
             }
-            const float c[4][4] = {{v[0].x, v[1].x, v[2].x, v[3].x},
-                                   {v[0].y, v[1].y, v[2].y, v[3].y},
-                                   {v[0].z, v[1].z, v[2].z, v[3].z},
-                                   {v[0].w, v[1].w, v[2].w, v[3].w}};
+        }
+    }
+}
+
+__device__ __forceinline__ void tc_put4(uint8_t* hi, uint8_t* lo, uint32_t o, float4 w) {
+    const float4 h = make_float4(tf32_head(w.x), tf32_head(w.y), tf32_head(w.z), tf32_head(w.w));
+    *reinterpret_cast<float4*>(hi + o) = h;
+    *reinterpret_cast<float4*>(lo + o) = make_float4(w.x - h.x, w.y - h.y, w.z - h.z, w.w - h.w);
+}
+
+template <bool T>
+__device__ __forceinline__ void tc_put(const TcRegs& g, uint8_t* hi, uint8_t* lo) {
+    const int t = threadIdx.x;
+    if (!T) {
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const float4 w = make_float4(c[q][0], c[q][1], c[q][2], c[q][3]);
-                const float4 h = make_float4(tf32_head(w.x), tf32_head(w.y), tf32_head(w.z), tf32_head(w.w));
-                const uint32_t o = tc_off(r + q, 4 * kq);
-                *reinterpret_cast<float4*>(hi + o) = h;
-                *reinterpret_cast<float4*>(lo + o) = make_float4(w.x - h.x, w.y - h.y, w.z - h.z, w.w - h.w);
-            }
+        for (int i = 0; i < 8; ++i) {
+            const int idx = t + TC_THREADS * i;
+            const int r = ((idx >> 6) << 3) | (idx & 7), kq = (idx >> 3) & 7;
+            tc_put4(hi, lo, tc_off(r, 4 * kq), g.v[i]);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const int idx = t + TC_THREADS * i;
+            const int rq = idx & 31, kq = idx >> 5;
+            const float4* v = g.v + 4 * i;
+            tc_put4(hi, lo, tc_off(4 * rq, 4 * kq), make_float4(v[0].x, v[1].x, v[2].x, v[3].x));
+            tc_put4(hi, lo, tc_off(4 * rq + 1, 4 * kq), make_float4(v[0].y, v[1].y, v[2].y, v[3].y));
+            tc_put4(hi, lo, tc_off(4 * rq + 2, 4 * kq), make_float4(v[0].z, v[1].z, v[2].z, v[3].z));
+            tc_put4(hi, lo, tc_off(4 * rq + 3, 4 * kq), make_float4(v[0].w, v[1].w, v[2].w, v[3].w));
         }
     }
 }
@@ -288,9 +309,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(int M, int K, co
                      "r"(128));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
+    TcRegs ra, rb;
     if (nc > 0) {
-        tc_stage<TA>(sm, sm + TC_OPER, A, lda, m0, M, kb);
-        tc_stage<!TB>(sm + 2 * TC_OPER, sm + 3 * TC_OPER, B, ldb, 0, 128, kb);
+        tc_load<TA>(ra, A, lda, m0, M, kb);
+        tc_load<!TB>(rb, B, ldb, 0, 128, kb);
+        tc_put<TA>(ra, sm, sm + TC_OPER);
+        tc_put<!TB>(rb, sm + 2 * TC_OPER, sm + 3 * TC_OPER);
     }
     fence_before();
     __syncthreads();
@@ -319,15 +343,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(int M, int K, co
         }
         if (c + 1 < nc) {
             const uint32_t b1 = (c + 1) & 1;
-            // buffer b1 last fed chunk c - 1: wait for its MMAs
+            // chunk c + 1 into registers while the MMAs run; buffer b1 last
+            // fed chunk c - 1: wait for its MMAs before storing
+            tc_load<TA>(ra, A, lda, m0, M, kb + (c + 1) * TC_KC);
+            tc_load<!TB>(rb, B, ldb, 0, 128, kb + (c + 1) * TC_KC);
             if (c >= 1) ok = ok && mbar_wait(bar0 + 8 * b1, (uint32_t)(((c - 1) >> 1) & 1));
             if (__syncthreads_or(!ok)) {
                 ok = false;
                 break;
             }
             uint8_t* nb = sm + b1 * TC_BUF;
-            tc_stage<TA>(nb, nb + TC_OPER, A, lda, m0, M, kb + (c + 1) * TC_KC);
-            tc_stage<!TB>(nb + 2 * TC_OPER, nb + 3 * TC_OPER, B, ldb, 0, 128, kb + (c + 1) * TC_KC);
+            tc_put<TA>(ra, nb, nb + TC_OPER);
+            tc_put<!TB>(rb, nb + 2 * TC_OPER, nb + 3 * TC_OPER);
         }
     }
     if (nc > 0 && ok) ok = mbar_wait(bar0 + 8 * ((nc - 1) & 1), (uint32_t)(((nc - 1) >> 1) & 1));

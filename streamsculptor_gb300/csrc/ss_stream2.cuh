@@ -122,6 +122,43 @@ __device__ __forceinline__ void write_snap_warp(float4* out, float4* stage, floa
     __syncwarp();
 }
 
+// Snapshot row k of one warp's particles (every lane calls it; the callers
+// are warp-uniform): lane l holds particles p0 = 2t and p1 = 2t + 1 (v0, v1:
+// they exist; ex0, ex1: released by the row's step).  A warp of 32 full
+// pairs at a 16-byte aligned address writes the row in three coalesced
+// stores (write_snap_warp), any other warp per particle.
+__device__ __forceinline__ void snap_row2(const StreamArgs& a, float4* stage, int64_t k, int64_t p0, int64_t p1,
+                                          bool v0, bool v1, bool ex0, bool ex1, const f2 xh[3], const f2 vh[3]) {
+#if SS_SNAP_COALESCED
+    float* row = a.snaps + (k * a.snap_pitch + (p0 - 2 * (int64_t)(threadIdx.x & 31)) + a.p_off) * 6;
+    const bool full = blockDim.x <= 32 * F2_WARPS && __all_sync(0xffffffffu, v1) &&
+                      (reinterpret_cast<uintptr_t>(row) & 15) == 0;
+    if (full) {
+        const float q = __int_as_float(0x7fc00000);  // NaN: not yet released
+        write_snap_warp(reinterpret_cast<float4*>(row), stage,
+                        ex0 ? make_float4(xh[0].x, xh[1].x, xh[2].x, vh[0].x) : make_float4(q, q, q, q),
+                        make_float4(ex0 ? vh[1].x : q, ex0 ? vh[2].x : q, ex1 ? xh[0].y : q, ex1 ? xh[1].y : q),
+                        ex1 ? make_float4(xh[2].y, vh[0].y, vh[1].y, vh[2].y) : make_float4(q, q, q, q));
+        return;
+    }
+#endif
+    if (v0) {
+        const float y0[6] = {xh[0].x, xh[1].x, xh[2].x, vh[0].x, vh[1].x, vh[2].x};
+        write_snap<float>(a.snaps, a.snap_pitch, k, p0 + a.p_off, ex0, y0);
+        if (v1) {
+            const float y1[6] = {xh[0].y, xh[1].y, xh[2].y, vh[0].y, vh[1].y, vh[2].y};
+            write_snap<float>(a.snaps, a.snap_pitch, k, p1 + a.p_off, ex1, y1);
+        }
+    }
+}
+
+// The same out of line, for the rows before a warp's first release (run
+// once per row before the step loop, so the loop keeps its registers).
+__device__ __noinline__ void snap_row2_cold(const StreamArgs& a, float4* stage, int64_t k, int64_t p0, int64_t p1,
+                                            bool v0, bool v1, bool ex0, bool ex1, const f2 xh[3], const f2 vh[3]) {
+    snap_row2(a, stage, k, p0, p1, v0, v1, ex0, ex1, xh, vh);
+}
+
 // grad Phi of one component of kind KIND at x (shifted to its center), added
 // to g: the FP32 forms of kind_grad without the Hessian, with the masses
 // (and NFW's 1 / r_s) restored to FP64 accuracy from their stored FP32
@@ -399,18 +436,17 @@ __global__ void __launch_bounds__(128, 4) stream_f32k2_kernel(PotDev<float> P, S
             vl[i] = make_float2((float)(u0 - (double)vh[i].x), (float)(u1 - (double)vh[i].y));
         }
     }
-    if (a.snaps && v0) {
-        const float y0[6] = {xh[0].x, xh[1].x, xh[2].x, vh[0].x, vh[1].x, vh[2].x};
-        const float y1[6] = {xh[0].y, xh[1].y, xh[2].y, vh[0].y, vh[1].y, vh[2].y};
-        for (int64_t k = 0; (k + 1) * (int64_t)a.stride <= wstart; ++k) {
-            const int64_t step = (k + 1) * (int64_t)a.stride;
-            write_snap<float>(a.snaps, a.snap_pitch, k, p0 + a.p_off, step >= st0, y0);
-            if (v1) write_snap<float>(a.snaps, a.snap_pitch, k, p1 + a.p_off, step >= st1, y1);
-        }
-    }
 #if SS_SNAP_COALESCED
     __shared__ float4 snap_stage[F2_WARPS][96];  // one 1536-byte snapshot row per warp
 #endif
+    // the rows before the warp's first release (NaN, or the initial state at
+    // a particle's own release step)
+    if (a.snaps) {
+        for (int64_t k = 0; (k + 1) * (int64_t)a.stride <= wstart; ++k) {
+            const int64_t step = (k + 1) * (int64_t)a.stride;
+            snap_row2_cold(a, snap_stage[threadIdx.x >> 5], k, p0, p1, v0, v1, step >= st0, step >= st1, xh, vh);
+        }
+    }
     int next_snap = (wstart / a.stride + 1) * a.stride;
     for (int n = wstart; n < a.n_steps; ++n) {
         if (v0 && n >= tstart) {
@@ -420,34 +456,9 @@ __global__ void __launch_bounds__(128, 4) stream_f32k2_kernel(PotDev<float> P, S
         }
         if (n + 1 == next_snap) {  // warp-uniform: every lane steps from wstart
             next_snap += a.stride;
-            if (a.snaps) {
-                const int64_t k = (n + 1) / a.stride - 1;
-                const bool ex0 = n + 1 >= st0, ex1 = n + 1 >= st1;
-#if SS_SNAP_COALESCED
-                // the row of the warp's 64 consecutive particles; a warp of
-                // 32 full pairs at a 16-byte aligned address writes it in
-                // three coalesced stores
-                float* row = a.snaps + (k * a.snap_pitch + (p0 - 2 * (int64_t)(threadIdx.x & 31)) + a.p_off) * 6;
-                const bool full = blockDim.x <= 32 * F2_WARPS && __all_sync(0xffffffffu, v1) &&
-                                  (reinterpret_cast<uintptr_t>(row) & 15) == 0;
-                if (full) {
-                    const float q = __int_as_float(0x7fc00000);  // NaN: not yet released
-                    write_snap_warp(reinterpret_cast<float4*>(row), snap_stage[threadIdx.x >> 5],
-                                    ex0 ? make_float4(xh[0].x, xh[1].x, xh[2].x, vh[0].x) : make_float4(q, q, q, q),
-                                    make_float4(ex0 ? vh[1].x : q, ex0 ? vh[2].x : q, ex1 ? xh[0].y : q,
-                                                ex1 ? xh[1].y : q),
-                                    ex1 ? make_float4(xh[2].y, vh[0].y, vh[1].y, vh[2].y) : make_float4(q, q, q, q));
-                } else
-#endif
-                if (v0) {
-                    const float y0[6] = {xh[0].x, xh[1].x, xh[2].x, vh[0].x, vh[1].x, vh[2].x};
-                    write_snap<float>(a.snaps, a.snap_pitch, k, p0 + a.p_off, ex0, y0);
-                    if (v1) {
-                        const float y1[6] = {xh[0].y, xh[1].y, xh[2].y, vh[0].y, vh[1].y, vh[2].y};
-                        write_snap<float>(a.snaps, a.snap_pitch, k, p1 + a.p_off, ex1, y1);
-                    }
-                }
-            }
+            if (a.snaps)
+                snap_row2(a, snap_stage[threadIdx.x >> 5], (n + 1) / a.stride - 1, p0, p1, v0, v1, n + 1 >= st0,
+                          n + 1 >= st1, xh, vh);
         }
     }
     if (!v0) return;
