@@ -31,7 +31,7 @@
 
 namespace ssg {
 
-static constexpr int SHOOT_M = 16;  // FP64 steps per slice
+static constexpr int SHOOT_M = 8;   // FP64 steps per slice
 static constexpr int SHOOT_C = 8;   // FP64 steps per coarse FP32 guess step
 static constexpr int SHOOT_ITERS = 8;
 

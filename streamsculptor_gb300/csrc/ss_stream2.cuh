@@ -154,7 +154,7 @@ __device__ __forceinline__ void snap_row2(const StreamArgs& a, float4* stage, in
 
 // The same out of line, for the rows before a warp's first release (run
 // once per row before the step loop, so the loop keeps its registers).
-__device__ __noinline__ void snap_row2_cold(const StreamArgs& a, float4* stage, int64_t k, int64_t p0, int64_t p1,
+static __device__ __noinline__ void snap_row2_cold(const StreamArgs& a, float4* stage, int64_t k, int64_t p0, int64_t p1,
                                             bool v0, bool v1, bool ex0, bool ex1, const f2 xh[3], const f2 vh[3]) {
     snap_row2(a, stage, k, p0, p1, v0, v1, ex0, ex1, xh, vh);
 }
