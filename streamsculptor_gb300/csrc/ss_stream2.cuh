@@ -436,9 +436,7 @@ __global__ void __launch_bounds__(128, 4) stream_f32k2_kernel(PotDev<float> P, S
             vl[i] = make_float2((float)(u0 - (double)vh[i].x), (float)(u1 - (double)vh[i].y));
         }
     }
-#if SS_SNAP_COALESCED
     __shared__ float4 snap_stage[F2_WARPS][96];  // one 1536-byte snapshot row per warp
-#endif
     // the rows before the warp's first release (NaN, or the initial state at
     // a particle's own release step)
     if (a.snaps) {
