@@ -296,6 +296,9 @@ int ss_orbit_ensemble_f64(const ss_potential* pot, const double* w0, int64_t n_o
  * ss_orbit_shoot_workspace_bytes(n_steps) bytes (8-byte aligned).  Static
  * potentials only; others run the serial ss_orbit_f64 kernel. */
 int64_t ss_orbit_shoot_workspace_bytes(int64_t n_steps);
+/* The number of slices S of an n_steps orbit (the converged slice starts,
+ * [S + 1, 6] doubles, are the first 6 (S + 1) doubles of the workspace). */
+int64_t ss_orbit_shoot_slices(int64_t n_steps);
 int ss_orbit_shoot_f64(const ss_potential* pot, const double* w0, double t0, double dt,
                        int64_t n_steps, int64_t save_every, double* out,
                        void* workspace, int64_t workspace_bytes, double tol, void* stream);
@@ -444,7 +447,7 @@ int ss_release_vjp(const ss_potential* pot, const ss_release_cfg* cfg, const dou
  * (n_dir = 6 n_comp + 6): states [n_steps/save_every + 1, 6] and tangents
  * [n_steps/save_every + 1, n_dir, 6] on the forward leg.  workspace >=
  * ss_prog_tangents_workspace_bytes(n_steps, n_comp).  starts_back and
- * starts_fwd (optional, [S + 1, 6], S = ceil(n_steps / 16)) are the
+ * starts_fwd (optional, [S + 1, 6], S = ss_orbit_shoot_slices(n_steps)) are the
  * converged slice starts of the two legs from earlier ss_orbit_shoot_f64
  * calls on the same potential (the first 6 (S + 1) doubles of their
  * workspaces); given, the legs are not solved again. */

@@ -123,6 +123,7 @@ SIGNATURES = {
     "ss_orbit_ensemble_f64": (C.c_int, [C.POINTER(ss_potential), VP, C.c_int64, C.c_double, VP, C.c_double,
                                         C.c_int64, C.c_int64, C.c_int32, VP, VP]),
     "ss_orbit_shoot_workspace_bytes": (C.c_int64, [C.c_int64]),
+    "ss_orbit_shoot_slices": (C.c_int64, [C.c_int64]),
     "ss_orbit_shoot_f64": (C.c_int, [C.POINTER(ss_potential), VP, C.c_double, C.c_double, C.c_int64, C.c_int64, VP,
                                      VP, C.c_int64, C.c_double, VP]),
     "ss_track_slopes": (C.c_int, [VP, C.c_int64, C.c_double, VP, VP]),

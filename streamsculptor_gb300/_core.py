@@ -335,7 +335,7 @@ def orbit(P, w0: torch.Tensor, t0: float, dt: float, n_steps: int, save_every: i
                   ptr(out), ws, nb, SHOOT_TOL, stream_handle())
         if keep_starts:
             # converged slice starts: the first 6 (S + 1) doubles of the workspace
-            S = (int(n_steps) + 15) // 16
+            S = int(_abi.load().ss_orbit_shoot_slices(int(n_steps)))
             off = ws.value - buf.data_ptr()
             starts = buf[off:off + 48 * (S + 1)].view(torch.float64).reshape(S + 1, 6).clone()
             return out, starts

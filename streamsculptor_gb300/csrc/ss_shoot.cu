@@ -430,6 +430,11 @@ using namespace ssg;
 
 extern "C" {
 
+int64_t ss_orbit_shoot_slices(int64_t n_steps) {
+    if (n_steps < 0) return set_error(SS_ERR_INVALID_ARGUMENT, "n_steps < 0");
+    return (n_steps + SHOOT_M - 1) / SHOOT_M;
+}
+
 int64_t ss_orbit_shoot_workspace_bytes(int64_t n_steps) {
     if (n_steps < 0) return set_error(SS_ERR_INVALID_ARGUMENT, "n_steps < 0");
     const int64_t S = (n_steps + SHOOT_M - 1) / SHOOT_M;
