@@ -31,6 +31,7 @@
 #include <cmath>
 
 #include "ss_common.cuh"
+#include "ss_f2.cuh"
 
 namespace ssg {
 
@@ -362,6 +363,156 @@ __global__ void __launch_bounds__(128) pert_response_kernel(ShDev sh, PertArgs a
     if (a.save_stride == 0) save(0);
 }
 
+// The FP32 response with two subhalos per thread (s0 = 2q, s1 = 2q + 1 of
+// the block's 256) in packed f32x2 lanes, for Plummer and Hernquist subhalo
+// lines (ncol 6 and 12): the arithmetic of pert_rhs / pert_response_kernel,
+// each add, multiply and FMA one packed instruction for both systems, and
+// each base-track record read from shared memory once for the pair.  The
+// scalar kernel issues an instruction nearly every cycle (issue-bound); the
+// pair halves the issue slots of the per-system work.
+template <int NCOL, int SHK>
+__device__ __forceinline__ void pert_rhs2(const float* recp, const f2 U[NCOL], f2 Gm, f2 am, const f2 P0[3],
+                                          const f2 V[3], float trel, f2 tau0, float window, f2 K[NCOL]) {
+    float rec[9];
+    load_stage(recp, rec);
+    const f2 tr = bc(trel);
+    f2 rel[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) rel[i] = sub2(bc(rec[i]), fma2(V[i], tr, P0[i]));
+    const f2 r2 = norm2sq(rel);
+    f2 g, gs = bc(0.0f);
+    if constexpr (SHK == SS_SH_PLUMMER) {
+        const f2 id = rsqrt2(fma2(am, am, r2));
+        const f2 id2 = mul2(id, id);
+        const f2 id3 = mul2(id2, id);
+        g = mul2(Gm, id3);
+        if constexpr (NCOL >= 12) gs = mul2(mul2(bc(-3.0f), mul2(g, am)), id2);  // grad(Gm a D^-3) = -3 Gm a D^-5 rel
+    } else {
+        const f2 r = make_float2(s_sqrt(r2.x), s_sqrt(r2.y));
+        const f2 inv_r = rcp2(r);
+        const f2 inv_ra = rcp2(add2(r, am));
+        g = mul2(mul2(mul2(Gm, inv_r), inv_ra), inv_ra);
+        if constexpr (NCOL >= 12) gs = mul2(mul2(bc(-2.0f), g), inv_ra);  // grad(Gm (r+a)^-2)
+    }
+    // window: |t - t0_s| < t_window, per lane
+    const f2 on = make_float2(fabsf(trel - tau0.x) < window ? 1.0f : 0.0f, fabsf(trel - tau0.y) < window ? 1.0f : 0.0f);
+    const f2 T0 = bc(rec[3]), T1 = bc(rec[4]), T2 = bc(rec[5]), T3 = bc(rec[6]), T4 = bc(rec[7]), T5 = bc(rec[8]);
+#pragma unroll
+    for (int b = 0; b < NCOL / 6; ++b) {
+        const f2* x1 = U + 6 * b;
+        K[6 * b + 0] = U[6 * b + 3];
+        K[6 * b + 1] = U[6 * b + 4];
+        K[6 * b + 2] = U[6 * b + 5];
+        const f2 ng = neg2(mul2(on, b == 0 ? g : gs));  // -on * (force factor)
+        K[6 * b + 3] = fma2(ng, rel[0], fma2(T4, x1[2], fma2(T3, x1[1], mul2(T0, x1[0]))));
+        K[6 * b + 4] = fma2(ng, rel[1], fma2(T5, x1[2], fma2(T1, x1[1], mul2(T3, x1[0]))));
+        K[6 * b + 5] = fma2(ng, rel[2], fma2(T2, x1[2], fma2(T5, x1[1], mul2(T4, x1[0]))));
+    }
+}
+
+template <int NCOL, int SHK>
+__global__ void __launch_bounds__(128) pert_response2_kernel(ShDev sh, PertArgs a, int sblocks) {
+    constexpr int RL = rec_len(1), SL = stage_len(1), SW = 12;
+    __shared__ __align__(16) float srec[PERT_STEPS_STAGED][6][SW];
+    const int64_t i = blockIdx.x / sblocks;          // particle within the chunk
+    const int sb = blockIdx.x - (int)(i * sblocks);
+    const int64_t q = (int64_t)sb * blockDim.x + threadIdx.x;  // subhalo pair
+    if (i >= a.np) return;                           // whole block
+    const bool act0 = 2 * q < sh.n, act1 = 2 * q + 1 < sh.n;
+    const int s0 = act0 ? (int)(2 * q) : 0, s1 = act1 ? (int)(2 * q + 1) : s0;
+    const int64_t p = a.p0 + i;
+    const int start = (int)pert_start(p, a.ppr, a.spr);
+    const float* rec = reinterpret_cast<const float*>(a.table) +
+                       (pert_offset(p, a.ppr, a.spr, a.n_steps) - pert_offset(a.p0, a.ppr, a.spr, a.n_steps)) * RL;
+    // subhalo lines relative to the run start t0: P0 + V (t - t0)
+    const double tau_0 = a.t0 - sh.t0[s0], tau_1 = a.t0 - sh.t0[s1];
+    f2 P0[3], V[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        P0[d] = make_float2((float)(sh.x0[3 * s0 + d] + sh.v[3 * s0 + d] * tau_0),
+                            (float)(sh.x0[3 * s1 + d] + sh.v[3 * s1 + d] * tau_1));
+        V[d] = make_float2((float)sh.v[3 * s0 + d], (float)sh.v[3 * s1 + d]);
+    }
+    const f2 Gm = make_float2((float)(sh.G * sh.m[s0]), (float)(sh.G * sh.m[s1]));
+    const f2 am = make_float2((float)sh.a[s0], (float)sh.a[s1]);
+    const f2 tau0 = make_float2((float)(sh.t0[s0] - a.t0), (float)(sh.t0[s1] - a.t0));
+    const float window = (float)sh.t_window;
+    const int64_t nsh = sh.n;
+
+    f2 u[NCOL];
+    const float* ic = reinterpret_cast<const float*>(a.pert_ics);
+#pragma unroll
+    for (int c = 0; c < NCOL; ++c)
+        u[c] = ic ? make_float2(ic[(p * nsh + s0) * NCOL + c], ic[(p * nsh + s1) * NCOL + c]) : bc(0.0f);
+    float* out = reinterpret_cast<float*>(a.pert_out);
+    auto save = [&](int slot) {
+        float* o = out + (((int64_t)slot * a.N + p) * nsh + s0) * NCOL;  // s1 = s0 + 1 follows
+        if (act0) {
+#pragma unroll
+            for (int c = 0; c < NCOL; ++c) o[c] = u[c].x;
+        }
+        if (act1) {
+#pragma unroll
+            for (int c = 0; c < NCOL; ++c) o[NCOL + c] = u[c].y;
+        }
+    };
+    if (a.save_stride > 0) {
+        for (int k = 0; k < a.n_saves && (int64_t)k * a.save_stride <= start; ++k) save(k);
+    }
+    const float h = (float)a.dt;
+    const f2 H = bc(h);
+    const float cs[6] = {0.0f, (float)SS_C2, (float)SS_C3, (float)SS_C4, (float)SS_C5, 1.0f};
+    for (int n0 = start; n0 < a.n_steps; n0 += PERT_STEPS_STAGED, rec += PERT_STEPS_STAGED * RL) {
+        const int cnt = min(PERT_STEPS_STAGED, a.n_steps - n0);
+        __syncthreads();  // the previous chunk has been consumed
+        for (int e = threadIdx.x; e < cnt * 6 * SL; e += blockDim.x) {
+            const int j = e / (6 * SL), r = e - 6 * SL * j, st = r / SL, qq = r - SL * st;
+            srec[j][st][qq] = rec[(int64_t)j * RL + r];
+        }
+        __syncthreads();
+        for (int j = 0; j < cnt; ++j) {
+            const int n = n0 + j;
+            const float tn = (float)n * h;
+            f2 k[6][NCOL];
+            f2 U[NCOL];
+#pragma unroll
+            for (int st = 0; st < 6; ++st) {
+#pragma unroll
+                for (int c = 0; c < NCOL; ++c) {
+                    f2 acc = bc(0.0f);
+                    if (st == 1) acc = mul2(bc((float)SS_A21), k[0][c]);
+                    if (st == 2) acc = fma2(bc((float)SS_A32), k[1][c], mul2(bc((float)SS_A31), k[0][c]));
+                    if (st == 3)
+                        acc = fma2(bc((float)SS_A43), k[2][c],
+                                   fma2(bc((float)SS_A42), k[1][c], mul2(bc((float)SS_A41), k[0][c])));
+                    if (st == 4)
+                        acc = fma2(bc((float)SS_A54), k[3][c],
+                                   fma2(bc((float)SS_A53), k[2][c],
+                                        fma2(bc((float)SS_A52), k[1][c], mul2(bc((float)SS_A51), k[0][c]))));
+                    if (st == 5)
+                        acc = fma2(bc((float)SS_A65), k[4][c],
+                                   fma2(bc((float)SS_A64), k[3][c],
+                                        fma2(bc((float)SS_A63), k[2][c],
+                                             fma2(bc((float)SS_A62), k[1][c], mul2(bc((float)SS_A61), k[0][c])))));
+                    U[c] = st == 0 ? u[c] : fma2(H, acc, u[c]);
+                }
+                pert_rhs2<NCOL, SHK>(&srec[j][st][0], U, Gm, am, P0, V, tn + cs[st] * h, tau0, window, k[st]);
+            }
+#pragma unroll
+            for (int c = 0; c < NCOL; ++c) {
+                f2 b = mul2(bc((float)SS_B1), k[0][c]);
+                b = fma2(bc((float)SS_B3), k[2][c], b);
+                b = fma2(bc((float)SS_B4), k[3][c], b);
+                b = fma2(bc((float)SS_B5), k[4][c], b);
+                b = fma2(bc((float)SS_B6), k[5][c], b);
+                u[c] = fma2(H, b, u[c]);
+            }
+            if (a.save_stride > 0 && (n + 1) % a.save_stride == 0) save((n + 1) / a.save_stride);
+        }
+    }
+    if (a.save_stride == 0) save(0);
+}
+
 // Per-subhalo potentials and derivatives at points (the perturbation
 // generator's jacfwd(potential_per_SH), perturbative.py:40-41).
 __global__ void subhalo_eval_kernel(ShDev sh, const double* __restrict__ xyz, int64_t n, double t, double* phi,
@@ -535,6 +686,12 @@ static void launch_response_kind(const ShDev& S, const PertArgs& a, unsigned g2,
                                  cudaStream_t st) {
     if constexpr (SHK == SS_SH_GRID) {
         pert_response_kernel<R, 6, SHK><<<g2, sblock, 0, st>>>(S, a, sblocks);  // mass response only
+    } else if (std::is_same<R, float>::value && (a.ncol == 6 || a.ncol == 12)) {
+        // two subhalos per thread (packed f32x2): blocks of 128 pairs
+        const int sblocks2 = (int)((S.n + 2 * sblock - 1) / (2 * sblock));
+        const unsigned g = (unsigned)(a.np * sblocks2);
+        if (a.ncol == 12) pert_response2_kernel<12, SHK><<<g, sblock, 0, st>>>(S, a, sblocks2);
+        else pert_response2_kernel<6, SHK><<<g, sblock, 0, st>>>(S, a, sblocks2);
     } else {
         if (a.ncol == 18) pert_response_kernel<R, 18, SHK><<<g2, sblock, 0, st>>>(S, a, sblocks);
         else if (a.ncol == 12) pert_response_kernel<R, 12, SHK><<<g2, sblock, 0, st>>>(S, a, sblocks);
