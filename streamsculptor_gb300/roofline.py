@@ -31,7 +31,8 @@ Dopri5 combinations per step (6 force evaluations, FSAL reuse):
   residuals: one FMA each, 4 flops for NFW and 2 for the other spherical and
   disk kinds per force evaluation.
 
-First-order response (pert_response_kernel, ss_pert.cu), per (particle,
+First-order response (pert_response2_kernel, two subhalos per thread in
+packed f32x2 lanes, and pert_response_kernel, ss_pert.cu), per (particle,
 subhalo)-step, mass columns only (ncol = 6), Plummer subhalos:
   stage states   per column a-sums of 1..5 terms (1 + 3 + 5 + 7 + 9) and
                  U = u + h acc (5 x 2)                          = 35; x 6 = 210
