@@ -74,6 +74,24 @@ int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalo
 #define SS_B4 (125.0 / 192.0)
 #define SS_B5 (-2187.0 / 6784.0)
 #define SS_B6 (11.0 / 84.0)
+// Nystrom coefficients of the tableau for second-order systems x'' = A(x, t):
+// stage positions x + c_s h v + h^2 sum_k abar_sk A_k with abar = a a, and
+// the 5th-order position update x + h v + h^2 sum_k bbar_k A_k, bbar = b a.
+constexpr double SS_N31 = SS_A32 * SS_A21;
+constexpr double SS_N41 = SS_A42 * SS_A21 + SS_A43 * SS_A31;
+constexpr double SS_N42 = SS_A43 * SS_A32;
+constexpr double SS_N51 = SS_A52 * SS_A21 + SS_A53 * SS_A31 + SS_A54 * SS_A41;
+constexpr double SS_N52 = SS_A53 * SS_A32 + SS_A54 * SS_A42;
+constexpr double SS_N53 = SS_A54 * SS_A43;
+constexpr double SS_N61 = SS_A62 * SS_A21 + SS_A63 * SS_A31 + SS_A64 * SS_A41 + SS_A65 * SS_A51;
+constexpr double SS_N62 = SS_A63 * SS_A32 + SS_A64 * SS_A42 + SS_A65 * SS_A52;
+constexpr double SS_N63 = SS_A64 * SS_A43 + SS_A65 * SS_A53;
+constexpr double SS_N64 = SS_A65 * SS_A54;
+constexpr double SS_NB1 = SS_B3 * SS_A31 + SS_B4 * SS_A41 + SS_B5 * SS_A51 + SS_B6 * SS_A61;
+constexpr double SS_NB2 = SS_B3 * SS_A32 + SS_B4 * SS_A42 + SS_B5 * SS_A52 + SS_B6 * SS_A62;
+constexpr double SS_NB3 = SS_B4 * SS_A43 + SS_B5 * SS_A53 + SS_B6 * SS_A63;
+constexpr double SS_NB4 = SS_B5 * SS_A54 + SS_B6 * SS_A64;
+constexpr double SS_NB5 = SS_B6 * SS_A65;
 
 // FP64 acceleration of the full potential (components + track + subhalos)
 // at time t: velocity_acceleration, main.py:116-120.

@@ -365,14 +365,19 @@ __global__ void __launch_bounds__(128) pert_response_kernel(ShDev sh, PertArgs a
 
 // The FP32 response with two subhalos per thread (s0 = 2q, s1 = 2q + 1 of
 // the block's 256) in packed f32x2 lanes, for Plummer and Hernquist subhalo
-// lines (ncol 6 and 12): the arithmetic of pert_rhs / pert_response_kernel,
-// each add, multiply and FMA one packed instruction for both systems, and
-// each base-track record read from shared memory once for the pair.  The
-// scalar kernel issues an instruction nearly every cycle (issue-bound); the
-// pair halves the issue slots of the per-system work.
-template <int NCOL, int SHK>
-__device__ __forceinline__ void pert_rhs2(const float* recp, const f2 U[NCOL], f2 Gm, f2 am, const f2 P0[3],
-                                          const f2 V[3], float trel, f2 tau0, float window, f2 K[NCOL]) {
+// lines (ncol 6 and 12), in Nystrom form.  Each response column block is a
+// second-order system x1'' = T(t) x1 - grad(Phi_s or dPhi_s/da_s)(x0(t))
+// (the acceleration does not depend on v1), so the Dormand-Prince stages
+// need only each stage's acceleration: stage positions
+// x1 + c_s h v1 + h^2 sum_k abar_sk A_k, and the update x1 + h v1 +
+// h^2 sum_k bbar_k A_k, v1 + h sum_k b_k A_k — the same step as
+// pert_response_kernel's first-order form with half the stage storage and a
+// third less stage arithmetic.  Each add, multiply and FMA is one packed
+// instruction for both systems, and each base-track record is read from
+// shared memory once for the pair.
+template <int NB, int SHK>
+__device__ __forceinline__ void pert_acc2(const float* recp, const f2 X[NB][3], f2 Gm, f2 am, const f2 P0[3],
+                                          const f2 V[3], float trel, f2 tau0, float window, f2 A[NB][3]) {
     float rec[9];
     load_stage(recp, rec);
     const f2 tr = bc(trel);
@@ -384,35 +389,31 @@ __device__ __forceinline__ void pert_rhs2(const float* recp, const f2 U[NCOL], f
     if constexpr (SHK == SS_SH_PLUMMER) {
         const f2 id = rsqrt2(fma2(am, am, r2));
         const f2 id2 = mul2(id, id);
-        const f2 id3 = mul2(id2, id);
-        g = mul2(Gm, id3);
-        if constexpr (NCOL >= 12) gs = mul2(mul2(bc(-3.0f), mul2(g, am)), id2);  // grad(Gm a D^-3) = -3 Gm a D^-5 rel
+        g = mul2(Gm, mul2(id2, id));
+        if constexpr (NB == 2) gs = mul2(mul2(bc(-3.0f), mul2(g, am)), id2);  // grad(Gm a D^-3) = -3 Gm a D^-5 rel
     } else {
         const f2 r = make_float2(s_sqrt(r2.x), s_sqrt(r2.y));
         const f2 inv_r = rcp2(r);
         const f2 inv_ra = rcp2(add2(r, am));
         g = mul2(mul2(mul2(Gm, inv_r), inv_ra), inv_ra);
-        if constexpr (NCOL >= 12) gs = mul2(mul2(bc(-2.0f), g), inv_ra);  // grad(Gm (r+a)^-2)
+        if constexpr (NB == 2) gs = mul2(mul2(bc(-2.0f), g), inv_ra);  // grad(Gm (r+a)^-2)
     }
     // window: |t - t0_s| < t_window, per lane
     const f2 on = make_float2(fabsf(trel - tau0.x) < window ? 1.0f : 0.0f, fabsf(trel - tau0.y) < window ? 1.0f : 0.0f);
+    // T: xx yy zz xy xz yz
     const f2 T0 = bc(rec[3]), T1 = bc(rec[4]), T2 = bc(rec[5]), T3 = bc(rec[6]), T4 = bc(rec[7]), T5 = bc(rec[8]);
 #pragma unroll
-    for (int b = 0; b < NCOL / 6; ++b) {
-        const f2* x1 = U + 6 * b;
-        K[6 * b + 0] = U[6 * b + 3];
-        K[6 * b + 1] = U[6 * b + 4];
-        K[6 * b + 2] = U[6 * b + 5];
-        const f2 ng = neg2(mul2(on, b == 0 ? g : gs));  // -on * (force factor)
-        K[6 * b + 3] = fma2(ng, rel[0], fma2(T4, x1[2], fma2(T3, x1[1], mul2(T0, x1[0]))));
-        K[6 * b + 4] = fma2(ng, rel[1], fma2(T5, x1[2], fma2(T1, x1[1], mul2(T3, x1[0]))));
-        K[6 * b + 5] = fma2(ng, rel[2], fma2(T2, x1[2], fma2(T5, x1[1], mul2(T4, x1[0]))));
+    for (int b = 0; b < NB; ++b) {
+        const f2 ng = neg2(mul2(on, b == 0 ? g : gs));
+        A[b][0] = fma2(ng, rel[0], fma2(T4, X[b][2], fma2(T3, X[b][1], mul2(T0, X[b][0]))));
+        A[b][1] = fma2(ng, rel[1], fma2(T5, X[b][2], fma2(T1, X[b][1], mul2(T3, X[b][0]))));
+        A[b][2] = fma2(ng, rel[2], fma2(T2, X[b][2], fma2(T5, X[b][1], mul2(T4, X[b][0]))));
     }
 }
 
 template <int NCOL, int SHK>
 __global__ void __launch_bounds__(128) pert_response2_kernel(ShDev sh, PertArgs a, int sblocks) {
-    constexpr int RL = rec_len(1), SL = stage_len(1), SW = 12;
+    constexpr int RL = rec_len(1), SL = stage_len(1), SW = 12, NB = NCOL / 6;
     __shared__ __align__(16) float srec[PERT_STEPS_STAGED][6][SW];
     const int64_t i = blockIdx.x / sblocks;          // particle within the chunk
     const int sb = blockIdx.x - (int)(i * sblocks);
@@ -473,39 +474,51 @@ __global__ void __launch_bounds__(128) pert_response2_kernel(ShDev sh, PertArgs 
         for (int j = 0; j < cnt; ++j) {
             const int n = n0 + j;
             const float tn = (float)n * h;
-            f2 k[6][NCOL];
-            f2 U[NCOL];
+            f2 A[6][NB][3];  // stage accelerations of each column block
 #pragma unroll
             for (int st = 0; st < 6; ++st) {
+                f2 X[NB][3];
 #pragma unroll
-                for (int c = 0; c < NCOL; ++c) {
-                    f2 acc = bc(0.0f);
-                    if (st == 1) acc = mul2(bc((float)SS_A21), k[0][c]);
-                    if (st == 2) acc = fma2(bc((float)SS_A32), k[1][c], mul2(bc((float)SS_A31), k[0][c]));
-                    if (st == 3)
-                        acc = fma2(bc((float)SS_A43), k[2][c],
-                                   fma2(bc((float)SS_A42), k[1][c], mul2(bc((float)SS_A41), k[0][c])));
-                    if (st == 4)
-                        acc = fma2(bc((float)SS_A54), k[3][c],
-                                   fma2(bc((float)SS_A53), k[2][c],
-                                        fma2(bc((float)SS_A52), k[1][c], mul2(bc((float)SS_A51), k[0][c]))));
-                    if (st == 5)
-                        acc = fma2(bc((float)SS_A65), k[4][c],
-                                   fma2(bc((float)SS_A64), k[3][c],
-                                        fma2(bc((float)SS_A63), k[2][c],
-                                             fma2(bc((float)SS_A62), k[1][c], mul2(bc((float)SS_A61), k[0][c])))));
-                    U[c] = st == 0 ? u[c] : fma2(H, acc, u[c]);
+                for (int bl = 0; bl < NB; ++bl) {
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        // h sum_k abar_sk A_k (stage 2 has none)
+                        f2 acc = bc(0.0f);
+                        if (st == 2) acc = mul2(bc((float)SS_N31), A[0][bl][d]);
+                        if (st == 3) acc = fma2(bc((float)SS_N42), A[1][bl][d], mul2(bc((float)SS_N41), A[0][bl][d]));
+                        if (st == 4)
+                            acc = fma2(bc((float)SS_N53), A[2][bl][d],
+                                       fma2(bc((float)SS_N52), A[1][bl][d], mul2(bc((float)SS_N51), A[0][bl][d])));
+                        if (st == 5)
+                            acc = fma2(bc((float)SS_N64), A[3][bl][d],
+                                       fma2(bc((float)SS_N63), A[2][bl][d],
+                                            fma2(bc((float)SS_N62), A[1][bl][d],
+                                                 mul2(bc((float)SS_N61), A[0][bl][d]))));
+                        const f2 x = u[6 * bl + d], v = u[6 * bl + 3 + d];
+                        X[bl][d] = st == 0 ? x : fma2(H, fma2(bc(cs[st]), v, mul2(H, acc)), x);
+                    }
                 }
-                pert_rhs2<NCOL, SHK>(&srec[j][st][0], U, Gm, am, P0, V, tn + cs[st] * h, tau0, window, k[st]);
+                pert_acc2<NB, SHK>(&srec[j][st][0], X, Gm, am, P0, V, tn + cs[st] * h, tau0, window, A[st]);
             }
 #pragma unroll
-            for (int c = 0; c < NCOL; ++c) {
-                f2 b = mul2(bc((float)SS_B1), k[0][c]);
-                b = fma2(bc((float)SS_B3), k[2][c], b);
-                b = fma2(bc((float)SS_B4), k[3][c], b);
-                b = fma2(bc((float)SS_B5), k[4][c], b);
-                b = fma2(bc((float)SS_B6), k[5][c], b);
-                u[c] = fma2(H, b, u[c]);
+            for (int bl = 0; bl < NB; ++bl) {
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    f2 sx = mul2(bc((float)SS_NB1), A[0][bl][d]);
+                    sx = fma2(bc((float)SS_NB2), A[1][bl][d], sx);
+                    sx = fma2(bc((float)SS_NB3), A[2][bl][d], sx);
+                    sx = fma2(bc((float)SS_NB4), A[3][bl][d], sx);
+                    sx = fma2(bc((float)SS_NB5), A[4][bl][d], sx);
+                    f2 sv = mul2(bc((float)SS_B1), A[0][bl][d]);
+                    sv = fma2(bc((float)SS_B3), A[2][bl][d], sv);
+                    sv = fma2(bc((float)SS_B4), A[3][bl][d], sv);
+                    sv = fma2(bc((float)SS_B5), A[4][bl][d], sv);
+                    sv = fma2(bc((float)SS_B6), A[5][bl][d], sv);
+                    f2& x = u[6 * bl + d];
+                    f2& v = u[6 * bl + 3 + d];
+                    x = fma2(H, fma2(H, sx, v), x);  // x + h (v + h sum bbar_k A_k)
+                    v = fma2(H, sv, v);
+                }
             }
             if (a.save_stride > 0 && (n + 1) % a.save_stride == 0) save((n + 1) / a.save_stride);
         }

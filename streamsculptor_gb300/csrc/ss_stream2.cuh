@@ -273,24 +273,9 @@ __device__ __forceinline__ void two_sum2(f2 a, f2 b, f2& s, f2& e) {
 // Nystrom form of the Dormand-Prince stages.  With V_j = v + h sum_k a_jk A_k
 // the stage positions x + h sum_j a_sj V_j are x + c_s h v + h^2 sum_k
 // abar_sk A_k, abar = a a, and the 5th-order position update is
-// x + h v + h^2 sum_k bbar_k A_k, bbar = b a: the same numbers without the
-// stage velocities, so a step keeps five fewer vectors and does a third less
-// stage arithmetic.
-constexpr double SS_N31 = SS_A32 * SS_A21;
-constexpr double SS_N41 = SS_A42 * SS_A21 + SS_A43 * SS_A31;
-constexpr double SS_N42 = SS_A43 * SS_A32;
-constexpr double SS_N51 = SS_A52 * SS_A21 + SS_A53 * SS_A31 + SS_A54 * SS_A41;
-constexpr double SS_N52 = SS_A53 * SS_A32 + SS_A54 * SS_A42;
-constexpr double SS_N53 = SS_A54 * SS_A43;
-constexpr double SS_N61 = SS_A62 * SS_A21 + SS_A63 * SS_A31 + SS_A64 * SS_A41 + SS_A65 * SS_A51;
-constexpr double SS_N62 = SS_A63 * SS_A32 + SS_A64 * SS_A42 + SS_A65 * SS_A52;
-constexpr double SS_N63 = SS_A64 * SS_A43 + SS_A65 * SS_A53;
-constexpr double SS_N64 = SS_A65 * SS_A54;
-constexpr double SS_NB1 = SS_B3 * SS_A31 + SS_B4 * SS_A41 + SS_B5 * SS_A51 + SS_B6 * SS_A61;
-constexpr double SS_NB2 = SS_B3 * SS_A32 + SS_B4 * SS_A42 + SS_B5 * SS_A52 + SS_B6 * SS_A62;
-constexpr double SS_NB3 = SS_B4 * SS_A43 + SS_B5 * SS_A53 + SS_B6 * SS_A63;
-constexpr double SS_NB4 = SS_B5 * SS_A54 + SS_B6 * SS_A64;
-constexpr double SS_NB5 = SS_B6 * SS_A65;
+// x + h v + h^2 sum_k bbar_k A_k, bbar = b a (SS_N.., ss_common.cuh): the
+// same numbers without the stage velocities, so a step keeps five fewer
+// vectors and does a third less stage arithmetic.
 
 // One compensated step of both lanes: the arithmetic of step_f32k in
 // Nystrom form.  H, HLO: each lane's step (hi, lo); a lane whose particle is
