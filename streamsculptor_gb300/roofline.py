@@ -44,6 +44,20 @@ subhalo)-step, mass columns only (ncol = 6), Plummer subhalos:
   total 546 flops, 6 specials.  The radius columns (ncol = 12) repeat the
   stage, update and T x1 work for six more columns and add the structural
   gradient (4 per stage): 546 + 210 + 66 + 6 x (21 + 4) = 972.
+
+The same step in Nystrom form (pert_response2_kernel: only the stage
+accelerations are kept), per response dimension (3 per column block):
+  stage positions  abar-sums of 0..4 terms (0 + 1 + 3 + 5 + 7 = 16) and
+                   x + h (c v + h acc) for stages 2..6 (5 x 5 = 25)  = 41; x 3 = 123
+  right-hand side  as above, 43 per stage (the position rows of the
+                   first-order form are the velocity itself)         = 258
+  stage times                                                        = 12
+  update           bbar- and b-sums (9 + 9), x + h (v + h .) (4),
+                   v + h . (2)                                       = 24; x 3 = 72
+  total 465 flops, 6 specials.  With the radius columns (ncol = 12) the
+  positions and update double and each stage adds T X, the structural
+  gradient's force factor and its rel terms (25): 465 + 123 + 72 + 6 x 25
+  = 810.
 """
 from __future__ import annotations
 
@@ -101,11 +115,16 @@ def particle_step_work(flat, precision: str) -> dict:
 
 
 RESPONSE_FLOPS = {6: 546, 12: 972}
+RESPONSE_FLOPS_NYSTROM = {6: 465, 12: 810}
 
 
-def response_step_work(ncol: int = 6) -> dict:
+def response_step_work(ncol: int = 6, form: str = "nystrom") -> dict:
     """Flops and special ops of one Dopri5 step of one (particle, subhalo)
-    linear-response system (first order; Plummer subhalos)."""
-    if ncol not in RESPONSE_FLOPS:
+    linear-response system (Plummer subhalos): form 'nystrom' (the packed
+    FP32 kernel) or 'first_order' (the scalar kernel)."""
+    table = {"nystrom": RESPONSE_FLOPS_NYSTROM, "first_order": RESPONSE_FLOPS}.get(form)
+    if table is None:
+        raise ValueError("form must be 'nystrom' or 'first_order'")
+    if ncol not in table:
         raise ValueError("ncol must be 6 or 12")
-    return {"flops": RESPONSE_FLOPS[ncol], "specials": STAGES}
+    return {"flops": table[ncol], "specials": STAGES}

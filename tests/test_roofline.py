@@ -37,12 +37,17 @@ def test_headline_work_per_particle_step():
 
 
 def test_response_work_per_system_step():
-    """Mass columns: 210 (stage states) + 6 x 43 (right-hand sides) + 12
-    (stage times) + 66 (update) = 546 flops and one rsqrt per stage."""
-    w = roofline.response_step_work(6)
+    """First-order form, mass columns: 210 (stage states) + 6 x 43
+    (right-hand sides) + 12 (stage times) + 66 (update) = 546 flops and one
+    rsqrt per stage; Nystrom form: 3 x 41 (stage positions) + 6 x 43 + 12 +
+    3 x 24 (update) = 465."""
+    w = roofline.response_step_work(6, "first_order")
     assert w["flops"] == 210 + 6 * 43 + 12 + 66 == 546
     assert w["specials"] == 6
-    assert roofline.response_step_work(12)["flops"] == 546 + 210 + 66 + 6 * (21 + 4)
+    assert roofline.response_step_work(12, "first_order")["flops"] == 546 + 210 + 66 + 6 * (21 + 4)
+    n = roofline.response_step_work(6)
+    assert n["flops"] == 3 * 41 + 6 * 43 + 12 + 3 * 24 == 465
+    assert roofline.response_step_work(12)["flops"] == 465 + 3 * 41 + 3 * 24 + 6 * 25
     with pytest.raises(ValueError):
         roofline.response_step_work(18)
 
