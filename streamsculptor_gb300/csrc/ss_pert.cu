@@ -411,8 +411,11 @@ __device__ __forceinline__ void pert_acc2(const float* recp, const f2 X[NB][3], 
     }
 }
 
+// Mass columns only (ncol 6): 5 blocks of 128 per SM (96 registers: no
+// spills for Plummer subhalos, 16 bytes for Hernquist; 1 % faster than the
+// unbounded 116 registers on the Plummer workload).
 template <int NCOL, int SHK>
-__global__ void __launch_bounds__(128) pert_response2_kernel(ShDev sh, PertArgs a, int sblocks) {
+__global__ void __launch_bounds__(128, NCOL == 6 ? 5 : 1) pert_response2_kernel(ShDev sh, PertArgs a, int sblocks) {
     constexpr int RL = rec_len(1), SL = stage_len(1), SW = 12, NB = NCOL / 6;
     __shared__ __align__(16) float srec[PERT_STEPS_STAGED][6][SW];
     const int64_t i = blockIdx.x / sblocks;          // particle within the chunk
