@@ -31,27 +31,31 @@ namespace ssg {
 
 
 // F(u) = ln(1+u) - u/(1+u) for both lanes (nfw_F_over_u3 without the
-// 1/u^3): the series for lanes with u < 2, the direct difference for the
-// others (each branch runs only when a lane needs it).
+// 1/u^3).  For lanes with u < 2, with s = u / (2+u) and w = s^2 (<= 1/4):
+// ln(1+u) = 2 atanh(s) = 2 s sum_k w^k / (2k+1), so
+//   F = s (u / (1+u) + w P(w)),  P(w) = 2 sum_k w^k / (2k+3),
+// with one reciprocal R = 1 / ((2+u)(1+u)) for both s = u (1+u) R and
+// u / (1+u) = u (2+u) R, and P fitted over [0, 1/4] by a polynomial of
+// degree 6 (least squares in relative error; 3e-8 with its coefficients
+// rounded to FP32, where the Taylor series needs degree 12; gen_nfw_poly.py
+// makes and checks them).  No term cancels, so F keeps
+// its relative accuracy as u -> 0 (F ~ u^2 / 2).  Lanes with u >= 2 take
+// the direct difference (each branch runs only when a lane needs it).
 __device__ __forceinline__ f2 nfw_F2(f2 u) {
     const bool sx = u.x < 2.0f, sy = u.y < 2.0f;
     f2 F = make_float2(0.0f, 0.0f);
     if (sx || sy) {
-        const f2 s = mul2(u, rcp2(add2(bc(2.0f), u)));
+        const f2 A = add2(bc(2.0f), u), B = add2(bc(1.0f), u);
+        const f2 uR = mul2(u, rcp2(mul2(A, B)));
+        const f2 s = mul2(uR, B);
         const f2 w = mul2(s, s);
-        f2 P = fma2(bc(1.0f / 27.0f), w, bc(1.0f / 25.0f));
-        P = fma2(P, w, bc(1.0f / 23.0f));
-        P = fma2(P, w, bc(1.0f / 21.0f));
-        P = fma2(P, w, bc(1.0f / 19.0f));
-        P = fma2(P, w, bc(1.0f / 17.0f));
-        P = fma2(P, w, bc(1.0f / 15.0f));
-        P = fma2(P, w, bc(1.0f / 13.0f));
-        P = fma2(P, w, bc(1.0f / 11.0f));
-        P = fma2(P, w, bc(1.0f / 9.0f));
-        P = fma2(P, w, bc(1.0f / 7.0f));
-        P = fma2(P, w, bc(1.0f / 5.0f));
-        P = fma2(P, w, bc(1.0f / 3.0f));
-        F = mul2(mul2(bc(2.0f), w), fma2(s, P, rcp2(add2(bc(1.0f), s))));
+        f2 P = fma2(bc(0.312188774f), w, bc(0.0821260512f));
+        P = fma2(P, w, bc(0.194957018f));
+        P = fma2(P, w, bc(0.221027091f));
+        P = fma2(P, w, bc(0.285765111f));
+        P = fma2(P, w, bc(0.399999201f));
+        P = fma2(P, w, bc(0.666666687f));
+        F = mul2(s, fma2(w, P, mul2(uR, A)));
     }
     if (!(sx && sy)) {
         const f2 L = make_float2(log1pf(u.x), log1pf(u.y));
