@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define SS_ABI_VERSION 7
+#define SS_ABI_VERSION 8
 #define SS_MAX_COMPONENTS 16
 
 /* ---------------------------------------------------------------- status */
@@ -57,6 +57,11 @@ typedef enum ss_status {
  *   SS_POWERLAW_CUTOFF p = {m, alpha, r_c}         PowerLawCutoffPotential (alpha < 3; the
  *                     potential value needs alpha < 2, else NaN as in the reference)
  *                                                  potential.py:357-388
+ *   SS_ZHAO           p = {m, r_s, alpha, beta, gamma}  ZhaoPotential (alpha > 0, beta > 3,
+ *                     0 <= gamma < 2): the gradient is dPhi/dr = G m I_z(alpha (3 - gamma),
+ *                     alpha (beta - 3)) / r^2 at r + dr / 2, dr = 1e-5 r + 1e-8, which is the
+ *                     reference's forward difference of Phi over [r, r + dr] to O(dr^2)
+ *                                                  potential.py:282-355
  * A component with center = SS_CENTER_TRACK is evaluated at x - c(t), where
  * c(t) is the potential's center track: TimeDepTranslatingPotential,
  * potential.py:448-462.  Components are summed in list order
@@ -72,7 +77,8 @@ typedef enum ss_kind {
     SS_BAR = 8,
     SS_DEHNEN_BAR = 9,
     SS_UNIFORM_ACCEL = 10,
-    SS_POWERLAW_CUTOFF = 11
+    SS_POWERLAW_CUTOFF = 11,
+    SS_ZHAO = 12
 } ss_kind;
 
 /* Largest degree of a spherical-harmonic expansion. */

@@ -190,6 +190,46 @@ Dual<T, N> gammainc_(double a, const Dual<T, N>& x) {
     return chain(x, gammainc_(a, x.v), dgammainc_t<T, N>(a, x.v));
 }
 
+inline double log1p_(double x) { return std::log1p(x); }
+template <class T, int N>
+Dual<T, N> log1p_(const Dual<T, N>& x) {
+    return chain(x, log1p_(x.v), T(1.0) / (1.0 + x.v));
+}
+
+// Regularised incomplete beta function I_z(a, b) (what
+// jax.scipy.special.betainc computes; ZhaoPotential, potential.py:282-355):
+// the hypergeometric series
+//   I_z(a, b) = z^a (1 - z)^b / (a B(a, b)) sum_n (a + b)_n / (a + 1)_n z^n
+// (Abramowitz & Stegun 26.5.23 with 15.1.1) for z < (a + 1) / (a + b + 2),
+// where its term ratio stays below one, else 1 - I_{1-z}(b, a); to double
+// precision.  (The product kernels evaluate the continued fraction instead.)
+// Pinned against scipy.special.betainc by the oracle tests.
+inline double lbeta_(double a, double b) { return std::lgamma(a) + std::lgamma(b) - std::lgamma(a + b); }
+inline double betainc_(double a, double b, double z) {
+    if (!(z > 0.0)) return 0.0;
+    if (!(z < 1.0)) return 1.0;
+    if (z >= (a + 1.0) / (a + b + 2.0)) return 1.0 - betainc_(b, a, 1.0 - z);
+    double term = 1.0, sum = 1.0;
+    for (int n = 0; n < 100000; ++n) {
+        term *= (a + b + n) * z / (a + 1.0 + n);
+        sum += term;
+        if (std::fabs(term) < 1e-17 * sum) break;
+    }
+    return std::exp(a * std::log(z) + b * std::log1p(-z) - lbeta_(a, b)) * sum / a;
+}
+// dI_z/dz = z^(a-1) (1 - z)^(b-1) / B(a, b)
+template <class T, int N>
+T dbetainc_t(double a, double b, const T& z) {
+    return exp_((a - 1.0) * log_(z) + (b - 1.0) * log_(1.0 - z) - lbeta_(a, b));
+}
+inline double dbetainc_t(double a, double b, double z) {
+    return std::exp((a - 1.0) * std::log(z) + (b - 1.0) * std::log1p(-z) - lbeta_(a, b));
+}
+template <class T, int N>
+Dual<T, N> betainc_(double a, double b, const Dual<T, N>& z) {
+    return chain(z, betainc_(a, b, z.v), dbetainc_t<T, N>(a, b, z.v));
+}
+
 inline double cos_(double x) { return std::cos(x); }
 inline double sin_(double x) { return std::sin(x); }
 inline double atan2_(double y, double x) { return std::atan2(y, x); }
@@ -285,6 +325,35 @@ static void track_deriv(const ss_track& tr, double t, double d[3]) {
 }
 
 // ------------------------------------------------------------ potentials
+// ZhaoPotential._potential (potential.py:314-331) as written, at radius r:
+// p = {m, r_s, alpha, beta, gamma}, rho0 from _rho0 (:308-312), and the
+// reference's replacement of p0 = alpha (2 - gamma) <= 0 by sqrt(eps).
+template <class S>
+S zhao_phi_r(const double* p, double G, const S& r) {
+    const double m = p[0], r_s = p[1], al = p[2], be = p[3], ga = p[4];
+    const double rho0 = m / (4.0 * M_PI * al * std::exp(lbeta_(al * (3.0 - ga), al * (be - 3.0))));
+    const S xa = pow_(r / r_s, 1.0 / al);
+    const S z = xa / (1.0 + xa);
+    const double p0 = al * (2.0 - ga), q0 = al * (be - 3.0), c0 = al * (be - ga);
+    const S term_l = std::exp(lbeta_(c0 - q0, q0)) * betainc_(c0 - q0, q0, z);
+    const double p0s = p0 <= 0.0 ? std::sqrt(std::numeric_limits<double>::epsilon()) : p0;
+    const double logB = lbeta_(p0s, c0 - p0);
+    const S log1mI = log1p_(-betainc_(p0s, c0 - p0, z));
+    const S term_r = exp_(logB + log1mI);
+    return -4.0 * M_PI * G * rho0 * al * (term_l / r + term_r / r_s);
+}
+
+// ZhaoPotential.gradient_func (potential.py:347-354) as written: the forward
+// difference of the potential over [r, r + dr], dr = 1e-5 r + 1e-8, along
+// x / r; adds scale times it to g.
+template <class S>
+void zhao_grad_add(const double* p, double G, const S x[3], double scale, S g[3]) {
+    const S r = sqrt_(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+    const S dr = 1e-5 * r + 1e-8;
+    const S dphi_dr = (zhao_phi_r(p, G, r + dr) - zhao_phi_r(p, G, r)) / dr;
+    for (int i = 0; i < 3; ++i) g[i] = g[i] + scale * (dphi_dr * x[i] / r);
+}
+
 // Each follows the scalar formula of the reference class named beside it.
 template <class S>
 S phi_component(const ss_component& c, double G, const S x[3]) {
@@ -326,6 +395,8 @@ S phi_component(const ss_component& c, double G, const S x[3]) {
             S t6 = t5 * gammainc_(t2, t4) * std::tgamma(t2) / (sqrt_(t3) * std::tgamma(t1 + 2.5));
             return t0 * t6 - 1.5 * t6 + t5 * gammainc_(t1 + 1.0, t4) * std::tgamma(t1 + 1.0) / (p[2] * std::tgamma(t2));
         }
+        case SS_ZHAO:  // ZhaoPotential.potential, potential.py:333-336
+            return zhao_phi_r(p, G, sqrt_(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]));
         default:
             return S(std::numeric_limits<double>::quiet_NaN());
     }
@@ -467,13 +538,20 @@ S phi_expansion(const ss_expansion& E, double scale, const S x[3]) {
     return scale * phi;
 }
 
+// Components whose reference gradient is not the derivative of their
+// potential: ZhaoPotential (a forward difference of it).
+inline bool fd_kind(int kind) { return kind == SS_ZHAO; }
+
+// skip_fd: leave out the fd_kind components (their gradients are added by
+// fd_grad_add instead of differentiating this sum).
 template <class S>
-S phi_total(const ss_potential& P, const S x[3], double t) {
+S phi_total(const ss_potential& P, const S x[3], double t, bool skip_fd = false) {
     S acc(0.0);
     double c[3] = {0, 0, 0};
     bool have_c = false;
     for (int k = 0; k < P.n_components; ++k) {
         const ss_component& comp = P.comp[k];
+        if (skip_fd && fd_kind(comp.kind)) continue;
         // GrowingPotential.potential, potential.py:474-477: the wrapped
         // potential times growth_func(t) (column 0 of the growth track)
         double gk = 1.0;
@@ -509,13 +587,48 @@ S phi_total(const ss_potential& P, const S x[3], double t) {
 typedef Dual<double, 3> D3;
 typedef Dual<D3, 3> DD3;
 
-// gradient by forward-mode AD of the scalar potential (main.py:37-40)
+// The gradients of the fd_kind components at x, added to g, with the
+// center and growth handling of phi_total.
+template <class S>
+void fd_grad_add(const ss_potential& P, const S x[3], double t, S g[3]) {
+    double c[3] = {0, 0, 0};
+    bool have_c = false;
+    for (int k = 0; k < P.n_components; ++k) {
+        const ss_component& comp = P.comp[k];
+        if (!fd_kind(comp.kind)) continue;
+        double gk = 1.0;
+        if (comp.center & SS_GROWS) {
+            double gv[3];
+            track_eval(P.growth, t, gv);
+            gk = gv[0];
+        }
+        if (comp.center & SS_CENTER_TRACK) {
+            if (!have_c) {
+                track_eval(P.track, t, c);
+                have_c = true;
+            }
+            S xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
+            zhao_grad_add(comp.p, P.G, xs, gk, g);
+        } else {
+            zhao_grad_add(comp.p, P.G, x, gk, g);
+        }
+    }
+}
+inline bool has_fd(const ss_potential& P) {
+    for (int k = 0; k < P.n_components; ++k)
+        if (fd_kind(P.comp[k].kind)) return true;
+    return false;
+}
+
+// gradient by forward-mode AD of the scalar potential (main.py:37-40), plus
+// the fd_kind components' own gradients
 template <class S>
 void grad_total(const ss_potential& P, const S x[3], double t, S g[3]) {
     Dual<S, 3> xd[3];
     for (int i = 0; i < 3; ++i) xd[i] = Dual<S, 3>::var(x[i], i);
-    Dual<S, 3> f = phi_total(P, xd, t);
+    Dual<S, 3> f = phi_total(P, xd, t, true);
     for (int i = 0; i < 3; ++i) g[i] = f.d[i];
+    if (has_fd(P)) fd_grad_add(P, x, t, g);
 }
 
 // Hessian by nested forward-mode AD (jacfwd of the gradient, main.py:59-65)
@@ -528,11 +641,22 @@ void hess_total(const ss_potential& P, const S x[3], double t, S* phi, S g[3], S
         I inner = I::var(x[i], i);
         xd[i] = O::var(inner, i);
     }
-    O f = phi_total(P, xd, t);
-    if (phi) *phi = f.v.v;
+    const bool fd = has_fd(P);
+    O f = phi_total(P, xd, t, true);
+    if (phi) *phi = fd ? phi_total(P, x, t) : f.v.v;
     for (int i = 0; i < 3; ++i) {
         g[i] = f.d[i].v;
         for (int j = 0; j < 3; ++j) H[i][j] = f.d[i].d[j];
+    }
+    if (fd) {
+        // the fd_kind gradients and their Jacobian (jacfwd of the gradient)
+        I xi[3], gi[3] = {I(0.0), I(0.0), I(0.0)};
+        for (int i = 0; i < 3; ++i) xi[i] = I::var(x[i], i);
+        fd_grad_add(P, xi, t, gi);
+        for (int i = 0; i < 3; ++i) {
+            g[i] = g[i] + gi[i].v;
+            for (int j = 0; j < 3; ++j) H[i][j] = H[i][j] + gi[i].d[j];
+        }
     }
 }
 

@@ -10,7 +10,7 @@ import ctypes as C
 import os
 import threading
 
-SS_ABI_VERSION = 7
+SS_ABI_VERSION = 8
 SS_MAX_COMPONENTS = 16
 
 SS_OK = 0
@@ -31,6 +31,7 @@ SS_BAR = 8
 SS_DEHNEN_BAR = 9
 SS_UNIFORM_ACCEL = 10
 SS_POWERLAW_CUTOFF = 11
+SS_ZHAO = 12
 SS_SHEXP_LMAX = 8
 
 SS_CENTER_ORIGIN = 0

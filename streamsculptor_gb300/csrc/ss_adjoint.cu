@@ -459,7 +459,7 @@ int ss_stream_adjoint_f32(const ss_potential* pot, const ss_stream_cfg* cfg, con
     SS_CHECK_ARG(cfg != nullptr && cfg->first_particle == 0 && cfg->snap_pitch == 0 && cfg->stream_particles == 0,
                  "the adjoint path runs whole single streams (first_particle = snap_pitch = stream_particles = 0)");
     for (int k = 0; k < P.n; ++k)
-        SS_CHECK_ARG(P.c[k].kind != SS_SH_EXPANSION && P.c[k].kind != SS_POWERLAW_CUTOFF,
+        SS_CHECK_ARG(P.c[k].kind != SS_SH_EXPANSION && P.c[k].kind != SS_POWERLAW_CUTOFF && P.c[k].kind != SS_ZHAO,
                      "component %d: kind %d has no adjoint", k, P.c[k].kind);
     SS_CHECK_ARG(!P.has_track && !P.has_rot && !P.has_facc && !P.grow_mask,
                  "the adjoint supports static potentials (no center track, rotation or frame acceleration) only");
@@ -509,7 +509,8 @@ int ss_release_vjp(const ss_potential* pot, const ss_release_cfg* cfg, const dou
     int rc = prepare_potential<double>(pot, &P, false);
     if (rc) return rc;
     for (int k = 0; k < P.n; ++k)
-        SS_CHECK_ARG(P.c[k].kind != SS_SH_EXPANSION, "component %d: SS_SH_EXPANSION has no adjoint", k);
+        SS_CHECK_ARG(P.c[k].kind != SS_SH_EXPANSION && P.c[k].kind != SS_POWERLAW_CUTOFF && P.c[k].kind != SS_ZHAO,
+                     "component %d: kind %d has no adjoint", k, P.c[k].kind);
     SS_CHECK_ARG(!P.has_rot && !P.has_facc && !P.grow_mask, "the release adjoint supports static potentials only");
     SS_CHECK_ARG(cfg && cfg->n_release >= 0 && cfg->n_draw >= 1, "bad cfg");
     int64_t total = cfg->n_release * cfg->n_draw;

@@ -108,6 +108,17 @@ int prepare_potential(const ss_potential* in, PotDev<R>* out, bool allow_subhalo
                 d.q[4] = R(a > 0.5 ? std::lgamma(a - 0.5) : std::nan("")); d.q[5] = R(1.0 / p[2]);
                 break;
             }
+            case SS_ZHAO: {
+                // q = {G m, 1 / r_s, 1 / alpha, a1 = alpha (3 - gamma), b1 = alpha (beta - 3), ln B(a1, b1)};
+                // gamma < 2 keeps the potential's second incomplete beta function proper (the reference
+                // replaces alpha (2 - gamma) <= 0 by sqrt(eps), a different potential)
+                SS_CHECK_ARG(p[1] > 0.0 && p[2] > 0.0 && p[3] > 3.0 && p[4] >= 0.0 && p[4] < 2.0,
+                             "component %d (Zhao): need r_s > 0, alpha > 0, beta > 3, 0 <= gamma < 2", k);
+                const double a1 = p[2] * (3.0 - p[4]), b1 = p[2] * (p[3] - 3.0);
+                d.q[0] = R(G * p[0]); d.q[1] = R(1.0 / p[1]); d.q[2] = R(1.0 / p[2]); d.q[3] = R(a1);
+                d.q[4] = R(b1); d.q[5] = R(std::lgamma(a1) + std::lgamma(b1) - std::lgamma(a1 + b1));
+                break;
+            }
             case SS_SH_EXPANSION: {
                 const ss_expansion& e = in->expansion;
                 SS_CHECK_ARG(!need_expansion, "component %d: only one SS_SH_EXPANSION component per potential", k);
@@ -272,6 +283,17 @@ __device__ double comp_phi(const PotDev<double>& P, const CompDev<double>& c, co
             const double xx = r2 * q[2];
             return -q[0] * gammainc_p(q[1], q[3], xx) / sqrt(r2) +
                    q[0] * exp(q[4] - q[3]) * q[5] * gammainc_p(q[1] - 0.5, q[4], xx);
+        }
+        case SS_ZHAO: {
+            // Phi = -G m (I_z(a1, b1) / r + B(p0, c0 - p0) / B(a1, b1) I_zc(c0 - p0, p0) / r_s),
+            // p0 = alpha (2 - gamma) = a1 - alpha, c0 - p0 = alpha (beta - 2) = b1 + alpha, zc = 1 - z
+            // (ZhaoPotential._potential, potential.py:314-331, with 4 pi G rho0 alpha = G m / B(a1, b1)
+            // and 1 - I_z(p, q) = I_zc(q, p))
+            const double r = sqrt(r2), al = 1.0 / q[2];
+            const double y = s_pow(r * q[1], q[2]), zc = 1.0 / (1.0 + y), z = y * zc;
+            const double p0 = q[3] - al, p1 = q[4] + al;
+            const double lb2 = lgamma(p0) + lgamma(p1) - lgamma(p0 + p1);
+            return -q[0] * (betainc(q[3], q[4], q[5], z, zc) / r + exp(lb2 - q[5]) * betainc(p1, p0, lb2, zc, z) * q[1]);
         }
         default:
             return nan("");

@@ -525,13 +525,129 @@ __device__ __forceinline__ void powerlaw_cutoff_gh(const R* q, const T& r2, T& g
     }
 }
 
+// Regularised incomplete beta function I_z(a, b) = B(z; a, b) / B(a, b),
+// a, b > 0, for ZhaoPotential (potential.py:282-355, which evaluates it with
+// jax.scipy.special.betainc).  lb = ln B(a, b); zc = 1 - z is passed
+// separately so that callers can form it without cancellation.  With
+// f = z^a zc^b / B(a, b), for z < (a + 1) / (a + b + 2)
+//   I = f / a * 1 / (1 + d1 / (1 + d2 / (1 + ...))),
+//   d_{2m+1} = -(a + m)(a + b + m) z / ((a + 2m)(a + 2m + 1)),
+//   d_{2m}   = m (b - m) z / ((a + 2m - 1)(a + 2m))
+// (Abramowitz & Stegun 26.5.8), else I = 1 - I_zc(b, a); the fraction is
+// evaluated by the modified Lentz method and stops once a pair of terms
+// moves it by less than the precision of S (bounded at 300 pairs).
+template <class S>
+__device__ __forceinline__ S betainc_cf(S a, S b, S z) {
+    constexpr bool dbl = sizeof(S) == 8;
+    const S eps = dbl ? S(1e-16) : S(6e-8);
+    const S tiny = dbl ? S(1e-300) : S(1e-30);
+    S c = S(1), d = S(1) - (a + b) * z / (a + S(1));
+    if (fabs(d) < tiny) d = tiny;
+    d = S(1) / d;
+    S h = d;
+    for (int m = 1; m < 300; ++m) {
+        const S m2 = S(2 * m);
+        S an = S(m) * (b - S(m)) * z / ((a + m2 - S(1)) * (a + m2));
+        d = S(1) + an * d;
+        if (fabs(d) < tiny) d = tiny;
+        c = S(1) + an / c;
+        if (fabs(c) < tiny) c = tiny;
+        d = S(1) / d;
+        h *= d * c;
+        an = -(a + S(m)) * (a + b + S(m)) * z / ((a + m2) * (a + m2 + S(1)));
+        d = S(1) + an * d;
+        if (fabs(d) < tiny) d = tiny;
+        c = S(1) + an / c;
+        if (fabs(c) < tiny) c = tiny;
+        d = S(1) / d;
+        const S del = d * c;
+        h *= del;
+        if (fabs(del - S(1)) < eps) break;
+    }
+    return h;
+}
+template <class S>
+__device__ __forceinline__ S betainc_s(S a, S b, S lb, S z, S zc) {
+    if (!(z > S(0))) return S(0);
+    if (!(zc > S(0))) return S(1);
+    const S f = exp(a * log(z) + b * log(zc) - lb);
+    if (z < (a + S(1)) / (a + b + S(2))) return f * betainc_cf(a, b, z) / a;
+    return S(1) - f * betainc_cf(b, a, zc) / b;
+}
+// dI_z/dz = z^(a-1) zc^(b-1) / B(a, b)
+template <class S>
+__device__ __forceinline__ S betainc_dz_s(S a, S b, S lb, S z, S zc) {
+    return (z > S(0) && zc > S(0)) ? exp((a - S(1)) * log(z) + (b - S(1)) * log(zc) - lb) : S(0);
+}
+__device__ __forceinline__ float betainc(float a, float b, float lb, float z, float zc) {
+    return betainc_s<float>(a, b, lb, z, zc);
+}
+__device__ __forceinline__ double betainc(double a, double b, double lb, double z, double zc) {
+    return betainc_s<double>(a, b, lb, z, zc);
+}
+__device__ __forceinline__ float betainc_dz(float a, float b, float lb, float z, float zc) {
+    return betainc_dz_s<float>(a, b, lb, z, zc);
+}
+__device__ __forceinline__ double betainc_dz(double a, double b, double lb, double z, double zc) {
+    return betainc_dz_s<double>(a, b, lb, z, zc);
+}
+// z and zc = 1 - z carry the same derivative with opposite signs; the
+// duals follow z
+template <int N>
+__device__ inline Dual<N> betainc(double a, double b, double lb, const Dual<N>& z, const Dual<N>& zc) {
+    return chain(z, betainc(a, b, lb, z.v, zc.v), betainc_dz(a, b, lb, z.v, zc.v));
+}
+template <int N>
+__device__ inline Dual<N> betainc_dz(double a, double b, double lb, const Dual<N>& z, const Dual<N>& zc) {
+    const double dz = betainc_dz(a, b, lb, z.v, zc.v);
+    return chain(z, dz, dz * ((a - 1.0) / z.v - (b - 1.0) / zc.v));
+}
+// x^p for x > 0
+__device__ __forceinline__ float s_pow(float x, float p) { return exp2f(p * log2f(x)); }
+__device__ __forceinline__ double s_pow(double x, double p) { return exp(p * log(x)); }
+template <int N>
+__device__ inline Dual<N> s_pow(const Dual<N>& x, double p) {
+    const double v = s_pow(x.v, p);
+    return chain(x, v, p * v / x.v);
+}
+
+// ZhaoPotential (potential.py:282-355).  Its gradient in the reference is
+// the forward difference (Phi(r + dr) - Phi(r)) / dr, dr = 1e-5 r + 1e-8, of
+// its potential (potential.py:347-354); here it is the exact derivative
+// dPhi/dr = G m I_z(a1, b1) / r^2 (the enclosed mass, a1 = alpha (3 - gamma),
+// b1 = alpha (beta - 3), z = y / (1 + y), y = (r / r_s)^(1/alpha)) taken at
+// the difference's midpoint r_m = r + dr / 2, which equals the forward
+// difference to O(dr^2) (relative ~1e-11) without its cancellation, and
+// whose r-derivative is the reference's autodiff Hessian of the difference
+// to the same order.  q = {G m, 1 / r_s, 1 / alpha, a1, b1, ln B(a1, b1)}.
+template <class T, class R, bool HESS>
+__device__ __forceinline__ void zhao_gh(const R* q, const T& r2, T& g, T& h) {
+    const T r = s_sqrt(r2);
+    const T rm = r + (r * 5e-6f + 5e-9f);  // the FP32 constants only round the small term
+    const T y = s_pow(rm * q[1], q[2]);
+    const T zc = s_rcp(1.0f + y);
+    const T z = y * zc;
+    const T I = betainc(q[3], q[4], q[5], z, zc);
+    const T irm = s_rcp(rm);
+    const T gr = q[0] * I * irm * irm;  // dPhi/dr at r_m
+    const T ir = s_rcp(r);
+    g = gr * ir;
+    if (HESS) {
+        // dz/dr_m = z zc / (alpha r_m); dr_m/dr = 1 + 5e-6
+        const T dI = betainc_dz(q[3], q[4], q[5], z, zc) * z * zc * q[2] * irm;
+        T dgr = q[0] * (dI - 2.0f * I * irm) * irm * irm;
+        dgr = dgr + dgr * 5e-6f;
+        h = (dgr - g) * ir * ir;
+    }
+}
+
 // Adds grad Phi of one component of compile-time kind KIND at x (already
 // shifted to its center) to grad[3]; when HESS, adds its Hessian
 // (xx, yy, zz, xy, xz, yz) to H[6].
 template <int KIND, class T, class R, bool HESS>
 __device__ __forceinline__ void kind_grad(const R* q, const T x[3], T grad[3], T H[6]) {
     if constexpr (KIND == SS_NFW || KIND == SS_HERNQUIST || KIND == SS_PLUMMER || KIND == SS_ISOCHRONE ||
-                  KIND == SS_POWERLAW_CUTOFF) {
+                  KIND == SS_POWERLAW_CUTOFF || KIND == SS_ZHAO) {
         T r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
         T g, h;
         if constexpr (KIND == SS_NFW) {
@@ -542,6 +658,8 @@ __device__ __forceinline__ void kind_grad(const R* q, const T x[3], T grad[3], T
             plummer_gh<T, R, HESS>(q, r2, g, h);
         } else if constexpr (KIND == SS_POWERLAW_CUTOFF) {
             powerlaw_cutoff_gh<T, R, HESS>(q, r2, g, h);
+        } else if constexpr (KIND == SS_ZHAO) {
+            zhao_gh<T, R, HESS>(q, r2, g, h);
         } else {
             isochrone_gh<T, R, HESS>(q, r2, g, h);
         }
@@ -733,6 +851,7 @@ __device__ __forceinline__ void comp_grad(const CompDev<R>& c, const T x[3], T g
         case SS_PLUMMER: kind_grad<SS_PLUMMER, T, R, HESS>(c.q, x, grad, H); break;
         case SS_ISOCHRONE: kind_grad<SS_ISOCHRONE, T, R, HESS>(c.q, x, grad, H); break;
         case SS_POWERLAW_CUTOFF: kind_grad<SS_POWERLAW_CUTOFF, T, R, HESS>(c.q, x, grad, H); break;
+        case SS_ZHAO: kind_grad<SS_ZHAO, T, R, HESS>(c.q, x, grad, H); break;
         default: break;
     }
 }

@@ -15,6 +15,8 @@ Python callable and cannot run in a CUDA kernel: using it raises.
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
 import torch
 
@@ -311,6 +313,35 @@ class PowerLawCutoffPotential(Potential):
 
     def _flatten(self):
         return Flat([(_abi.SS_POWERLAW_CUTOFF, _abi.SS_CENTER_ORIGIN, (_f(self.m), _f(self.alpha), _f(self.r_c)))])
+
+
+class ZhaoPotential(Potential):
+    """Zhao (1996) double power-law sphere (ZhaoPotential, potential.py:282-355):
+    rho = rho0 / (x^gamma (1 + x^(1/alpha))^((beta - gamma) alpha)), x = r / r_s,
+    with rho0 normalising the total mass to m.  The kernels evaluate the
+    potential with the regularised incomplete beta function (continued
+    fraction) and the gradient as dPhi/dr = G m I_z(alpha (3 - gamma),
+    alpha (beta - 3)) / r^2 at r + dr / 2, dr = 1e-5 r + 1e-8: the reference's
+    forward difference of its potential over [r, r + dr] (gradient_func) to
+    O(dr^2), without the difference's cancellation.  Needs alpha > 0,
+    beta > 3 and 0 <= gamma < 2 (the reference replaces alpha (2 - gamma) <= 0
+    by sqrt(eps), which changes the potential)."""
+
+    def __init__(self, m, r_s, alpha, beta, gamma, units=None):
+        super().__init__(units, {"m": m, "r_s": r_s, "alpha": alpha, "beta": beta, "gamma": gamma})
+
+    def _flatten(self):
+        return Flat([(_abi.SS_ZHAO, _abi.SS_CENTER_ORIGIN,
+                      (_f(self.m), _f(self.r_s), _f(self.alpha), _f(self.beta), _f(self.gamma)))])
+
+    def density(self, xyz, t):
+        """ZhaoPotential._density (potential.py:308-319), on the host."""
+        al, be, ga = _f(self.alpha), _f(self.beta), _f(self.gamma)
+        a1, b1 = al * (3.0 - ga), al * (be - 3.0)
+        rho0 = _f(self.m) / (4.0 * np.pi * al * np.exp(math.lgamma(a1) + math.lgamma(b1) - math.lgamma(a1 + b1)))
+        r = np.linalg.norm(np.asarray(host64(xyz), dtype=np.float64).reshape(-1, 3), axis=1)
+        x = r / _f(self.r_s)
+        return rho0 / _f(self.r_s) ** 3 / x ** ga / (1.0 + x ** (1.0 / al)) ** ((be - ga) * al)
 
 
 class BovyMWPotential2014(Potential):
@@ -737,7 +768,7 @@ class CustomPotential(Potential):
         super().__init__(units, {"potential_func": potential_func})
 
 
-__all__ = ["GrowingPotential", "PowerLawCutoffPotential", "BovyMWPotential2014", "MiyamotoNagaiDisk", "NFWPotential",
+__all__ = ["GrowingPotential", "PowerLawCutoffPotential", "ZhaoPotential", "BovyMWPotential2014", "MiyamotoNagaiDisk", "NFWPotential",
            "TriaxialNFWPotential", "Isochrone", "PlummerPotential",
            "HernquistPotential", "Potential_Combine", "TimeDepTranslatingPotential", "ProgenitorPotential",
            "GalaMilkyWayPotential", "SubhaloLinePotential", "SubhaloLinePotential_dRadius", "BarPotential",

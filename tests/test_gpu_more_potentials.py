@@ -102,3 +102,103 @@ def test_bovy_mw_stream_matches_oracle(ss, oracle, precision, tol):
                             np.linalg.norm(got[:, 3:] - ref[:, 3:], axis=1) / np.linalg.norm(ref[:, 3:], axis=1)))
     print(f"Bovy MW stream ({precision}) vs oracle: {err:.2e}")
     assert err <= tol
+
+
+ZHAO_CASES = [(1e11, 10.0, 1.0, 4.0, 1.0), (5e11, 15.0, 0.5, 3.5, 0.5), (2e10, 3.0, 2.0, 5.0, 1.5),
+              (1e11, 20.0, 1.0, 3.2, 0.0)]
+
+
+def _zhao_midpoint(p, x, Gv):
+    """The exact form the kernels evaluate, with scipy.special.betainc:
+    dPhi/dr = G m I_z(a1, b1) / r^2 at r_m = r + dr / 2 along x / r, and its
+    Jacobian."""
+    from scipy import special
+    m, rs, al, be, ga = p
+    a1, b1 = al * (3 - ga), al * (be - 3)
+    r = np.linalg.norm(x, axis=1)
+    dr = 1e-5 * r + 1e-8
+    rm = r + dr / 2
+    xa = (rm / rs) ** (1 / al)
+    z, zc = xa / (1 + xa), 1 / (1 + xa)
+    I = special.betainc(a1, b1, z)
+    gr = Gv * m * I / rm ** 2
+    dI = z ** (a1 - 1) * zc ** (b1 - 1) / special.beta(a1, b1) * z * zc / (al * rm)
+    dgr = Gv * m * (dI - 2 * I / rm) / rm ** 2 * (1 + 5e-6)
+    g = gr / r
+    h = (dgr - g) / r ** 2
+    H = g[:, None, None] * np.eye(3)[None] + h[:, None, None] * x[:, :, None] * x[:, None, :]
+    depth = Gv * m * special.beta(al * (2 - ga), al * (be - 2)) / (special.beta(a1, b1) * rs)
+    return g[:, None] * x, H, depth, dr, r
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("p", ZHAO_CASES)
+def test_zhao_eval_matches_oracle(ss, oracle, p):
+    """ZhaoPotential (potential.py:282-355) from 1e-2 to 300 kpc.  The
+    potential against the oracle to 1e-12.  The kernels' gradient and
+    Hessian (the exact derivative at the forward difference's midpoint)
+    against the same form written with scipy.special.betainc to 1e-12 / 1e-11,
+    and against the oracle's forward difference (gradient_func as written) and
+    its autodiff Jacobian to 1e-9 / 1e-8 plus the difference's rounding
+    bound, 16 eps |Phi(0)| / dr (times 1 / r + 1e-5 / dr for the Jacobian):
+    where dPhi/dr is small against Phi / dr the reference's own gradient
+    carries that noise."""
+    from streamsculptor_gb300 import _abi, potential as P
+    rng = np.random.default_rng(2)
+    d = rng.normal(size=(600, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    x = d * np.exp(rng.uniform(np.log(1e-2), np.log(300.0), 600))[:, None]
+    pot = P.ZhaoPotential(*p, units=ss.usys)
+    phi_o, g_o, H_o = oracle.potential_eval(oracle.HostModel([(_abi.SS_ZHAO, 0, p)]), x)
+    phi = pot.potential(x, 0.0).cpu().numpy()
+    g = pot.gradient(x, 0.0).cpu().numpy()
+    H = pot.jacobian_force(x, 0.0).cpu().numpy()
+    g_m, H_m, depth, dr, r = _zhao_midpoint(p, x, pot._G)
+    assert rel_err(phi, phi_o) < 1e-12
+    assert np.max(np.linalg.norm(g - g_m, axis=1) / np.linalg.norm(g_m, axis=1)) < 1e-12
+    assert np.max(np.linalg.norm((H - H_m).reshape(-1, 9), axis=1) / np.linalg.norm(H_m.reshape(-1, 9), axis=1)) < 1e-11
+    noise = 16 * np.finfo(float).eps * depth / dr
+    assert np.all(np.linalg.norm(g - g_o, axis=1) <= 1e-9 * np.linalg.norm(g_o, axis=1) + noise)
+    assert np.all(np.linalg.norm((H - H_o).reshape(-1, 9), axis=1)
+                  <= 1e-8 * np.linalg.norm(H_o.reshape(-1, 9), axis=1) + noise * (1 / r + 1e-5 / dr))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [("f64", 2e-9), ("f32k", 1e-5)])
+def test_zhao_stream_matches_oracle(ss, oracle, precision, tol):
+    """A stream in a Miyamoto-Nagai disk plus a Zhao halo against the oracle.
+    FP64 to 2e-9: the oracle, like the reference, takes the halo's force as a
+    forward difference of its potential, whose rounding noise (~1e-10 of the
+    force at these radii) moves 300-step orbits by 1e-11 to 1.2e-10 from the
+    exact-derivative form the kernels evaluate.  The FP32-compensated form to
+    1e-5."""
+    from streamsculptor_gb300 import _abi, potential as P
+    zp = (5e11, 15.0, 1.0, 3.5, 1.0)
+    pot = P.Potential_Combine([P.MiyamotoNagaiDisk(m=6.8e10, a=3.0, b=0.28, units=ss.usys),
+                               P.ZhaoPotential(*zp, units=ss.usys)], units=ss.usys)
+    orc = oracle.HostModel([(_abi.SS_MIYAMOTO_NAGAI, 0, (6.8e10, 3.0, 0.28)), (_abi.SS_ZHAO, 0, zp)])
+    wf = np.array([10.0, 0.0, 1.0, 0.0, 0.2, 0.02])
+    n_rel = 150
+    back = oracle.orbit(orc, wf, 0.0, -1.0, n_rel, n_rel)[0, -1]
+    ts = -float(n_rel) + np.arange(n_rel + 1)
+    normals = np.random.default_rng(6).standard_normal((n_rel + 1, 1, 4))
+    ws = oracle.orbit(orc, back, ts[0], 1.0, n_rel, 1)[0]
+    ics, _ = oracle.release(orc, ws, ts, 2e4, normals)
+    ref, _, _ = oracle.stream(orc, ts[0], 1.0, n_rel, ics[:-1].reshape(-1, 6), 2, 1)
+    lead, trail = pot.gen_stream_vmapped(ts=ts, prog_w0=back, Msat=2e4, normals=normals, precision=precision)
+    got = np.stack([lead.cpu().numpy(), trail.cpu().numpy()], axis=1).reshape(-1, 6)
+    err = np.max(np.maximum(np.linalg.norm(got[:, :3] - ref[:, :3], axis=1) / np.linalg.norm(ref[:, :3], axis=1),
+                            np.linalg.norm(got[:, 3:] - ref[:, 3:], axis=1) / np.linalg.norm(ref[:, 3:], axis=1)))
+    print(f"Zhao stream ({precision}) vs oracle: {err:.2e}")
+    assert err <= tol
+
+
+@pytest.mark.gpu
+def test_zhao_rejects_gamma_at_least_two(ss):
+    """gamma >= 2 (where the reference replaces alpha (2 - gamma) by
+    sqrt(eps), a different potential) and beta <= 3 are refused with an
+    argument error, before any kernel runs."""
+    from streamsculptor_gb300 import potential as P
+    for bad in [(1e11, 10.0, 1.0, 4.0, 2.0), (1e11, 10.0, 1.0, 3.0, 1.0), (1e11, 10.0, 0.0, 4.0, 1.0)]:
+        with pytest.raises(Exception, match="Zhao"):
+            P.ZhaoPotential(*bad, units=ss.usys).gradient(np.array([[1.0, 2.0, 3.0]]), 0.0)

@@ -209,6 +209,67 @@ def test_powerlaw_cutoff_matches_scipy(oracle, m, alpha, r_c):
     assert np.max(np.linalg.norm(g - g_ref, axis=1) / np.linalg.norm(g_ref, axis=1)) < 1e-13
 
 
+ZHAO_CASES = [(1e11, 10.0, 1.0, 4.0, 1.0), (5e11, 15.0, 0.5, 3.5, 0.5), (2e10, 3.0, 2.0, 5.0, 1.5),
+              (1e11, 20.0, 1.0, 3.2, 0.0)]
+
+
+def zhao_reference(p, r, Gv):
+    """ZhaoPotential (potential.py:282-355) as the reference writes it, with
+    scipy.special's beta, betaln and betainc: the potential at r and
+    gradient_func's forward difference dPhi/dr; also the potential's depth
+    |Phi(0)| = G m B(p0, c0 - p0) / (B(a1, b1) r_s), which bounds the
+    rounding noise of that difference."""
+    from scipy import special
+    m, rs, al, be, ga = p
+
+    def phi(r):
+        rho0 = m / (4 * np.pi * al * special.beta(al * (3 - ga), al * (be - 3)))
+        xa = (r / rs) ** (1 / al)
+        z = xa / (1 + xa)
+        p0, q0, c0 = al * (2 - ga), al * (be - 3), al * (be - ga)
+        term_l = special.beta(c0 - q0, q0) * special.betainc(c0 - q0, q0, z)
+        p0s = p0 if p0 > 0 else np.sqrt(np.finfo(float).eps)
+        term_r = np.exp(special.betaln(p0s, c0 - p0) + np.log1p(-special.betainc(p0s, c0 - p0, z)))
+        return -4 * np.pi * Gv * rho0 * al * (term_l / r + term_r / rs)
+
+    dr = 1e-5 * r + 1e-8
+    depth = Gv * m * special.beta(al * (2 - ga), al * (be - 2)) / (special.beta(al * (3 - ga), al * (be - 3)) * rs)
+    return phi(r), (phi(r + dr) - phi(r)) / dr, depth, dr
+
+
+@pytest.mark.parametrize("p", ZHAO_CASES)
+def test_zhao_matches_scipy(oracle, p):
+    """The oracle's ZhaoPotential (its own incomplete beta function from the
+    hypergeometric series; the gradient as gradient_func's forward difference,
+    potential.py:347-354) against the reference's formulas evaluated with
+    scipy.special, from 1e-2 to 300 kpc.  The difference cancels most of the
+    potential's digits where dPhi/dr is small against Phi / dr, so the
+    gradients are compared to 1e-9 plus that rounding bound,
+    16 eps |Phi(0)| / dr."""
+    rng = np.random.default_rng(0)
+    d = rng.normal(size=(300, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r = np.exp(rng.uniform(np.log(1e-2), np.log(300.0), 300))
+    x = d * r[:, None]
+    phi, g, _ = oracle.potential_eval(oracle.HostModel([(_abi.SS_ZHAO, 0, p)]), x)
+    phi_ref, dphi, depth, dr = zhao_reference(p, r, G)
+    assert np.max(np.abs(phi - phi_ref) / np.abs(phi_ref)) < 1e-13
+    g_ref = dphi[:, None] * x / r[:, None]
+    bound = 1e-9 * np.linalg.norm(g_ref, axis=1) + 16 * np.finfo(float).eps * depth / dr
+    assert np.all(np.linalg.norm(g - g_ref, axis=1) <= bound)
+
+
+def test_zhao_closed_form_hernquist(oracle):
+    """alpha = 1, beta = 4, gamma = 1 is the Hernquist sphere: the oracle's
+    Zhao potential equals -G m / (r + r_s) to round-off, and its forward
+    difference the Hernquist force to the difference's truncation (5e-6)."""
+    r = np.array([0.5, 3.0, 10.0, 40.0])
+    x = np.stack([r, 0 * r, 0 * r], axis=1)
+    phi, g, _ = oracle.potential_eval(oracle.HostModel([(_abi.SS_ZHAO, 0, (1e11, 10.0, 1.0, 4.0, 1.0))]), x)
+    assert np.max(np.abs(phi / (-G * 1e11 / (r + 10.0)) - 1)) < 1e-13
+    assert np.max(np.abs(g[:, 0] / (G * 1e11 / (r + 10.0) ** 2) - 1)) < 1e-5
+
+
 def test_dopri5_fifth_order(oracle):
     # smooth (Plummer) potential so the asymptotic regime is reached
     m = oracle.HostModel([(_abi.SS_PLUMMER, 0, (1e11, 5.0))])
