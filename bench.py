@@ -375,7 +375,8 @@ class Spray:
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             ms = float(t.item())
         return {"ms_total": ms, "ms_per_step": ms / K, "kernel_ms": statistics.mean(kms) if kms else None,
-                "launches": launches, "clocks": ck, "steps": K, "warmup": W}
+                "samples_ms": [a.elapsed_time(b) for a, b in evs], "launches": launches, "clocks": ck,
+                "steps": K, "warmup": W}
 
     def roofline(self, r, precision, kernel, peak):
         from streamsculptor_gb300 import _core, potential as P, roofline
@@ -553,7 +554,7 @@ def gpu_arm(args, wl):
                                     "samples_ms": chunked_samples,
                                     "path": "gen_stream(out='host', host_mode='chunked'): 8 particle sub-ranges, "
                                             "each copied by the copy engine while the next integrates"}},
-                "clocks": r32["clocks"], "gpu_launches": r32["launches"],
+                "samples_ms": r32["samples_ms"], "clocks": r32["clocks"], "gpu_launches": r32["launches"],
                 "gpu_launches_per_step": r32["launches"] / args.steps}
     if not args.no_analysis:
         # --- the stated error: FP32 vs FP64 on the same inputs, the FP64

@@ -41,13 +41,20 @@ namespace ssg {
 // makes and checks them).  No term cancels, so F keeps
 // its relative accuracy as u -> 0 (F ~ u^2 / 2).  Lanes with u >= 2 take
 // the direct difference (each branch runs only when a lane needs it).
+// lanes with u >= 2: out of line, so that log1pf's registers do not count
+// against the step loop's (the branch is rare on bound orbits)
+static __device__ __noinline__ f2 nfw_F2_far(f2 u) {
+    const f2 L = make_float2(log1pf(u.x), log1pf(u.y));
+    return fma2(neg2(u), rcp2(add2(bc(1.0f), u)), L);
+}
+
 __device__ __forceinline__ f2 nfw_F2(f2 u) {
     const bool sx = u.x < 2.0f, sy = u.y < 2.0f;
     f2 F = make_float2(0.0f, 0.0f);
     if (sx || sy) {
         const f2 A = add2(bc(2.0f), u), B = add2(bc(1.0f), u);
         const f2 uR = mul2(u, rcp2(mul2(A, B)));
-        const f2 s = mul2(uR, B);
+        const f2 s = mul2(uR, B), t = mul2(uR, A);  // u / (2+u), u / (1+u)
         const f2 w = mul2(s, s);
         f2 P = fma2(bc(0.312188774f), w, bc(0.0821260512f));
         P = fma2(P, w, bc(0.194957018f));
@@ -55,11 +62,10 @@ __device__ __forceinline__ f2 nfw_F2(f2 u) {
         P = fma2(P, w, bc(0.285765111f));
         P = fma2(P, w, bc(0.399999201f));
         P = fma2(P, w, bc(0.666666687f));
-        F = mul2(s, fma2(w, P, mul2(uR, A)));
+        F = mul2(s, fma2(w, P, t));
     }
     if (!(sx && sy)) {
-        const f2 L = make_float2(log1pf(u.x), log1pf(u.y));
-        const f2 Fl = fma2(neg2(u), rcp2(add2(bc(1.0f), u)), L);
+        const f2 Fl = nfw_F2_far(u);
         if (!sx) F.x = Fl.x;
         if (!sy) F.y = Fl.y;
     }
