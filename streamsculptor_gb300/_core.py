@@ -654,9 +654,14 @@ def pert_response(P, table: SubhaloTable, cfg, precision: int, base_ics, pert_ic
     out = torch.empty(n_saves, N, ns, ncol, dtype=dtype, device=dev)
     base_out = torch.empty(N, 6, dtype=torch.float64, device=dev)
     if chunk_particles is None:
-        # about 2 GB of base-track records per chunk
+        # base-track records of up to a quarter of the free device memory
+        # (at least 2 GB, at most 32 GB) per chunk: each chunk's FP64 base
+        # pass lasts as long as its longest track whatever the chunk's size,
+        # so few large chunks keep it from dominating
         per = max(1, cfg.n_steps) * (120 if ncol == 18 else 56) * (8 if precision == 64 else 4)
-        chunk_particles = max(1, min(N, (2 << 30) // per))
+        free, _ = torch.cuda.mem_get_info(dev)
+        budget = min(32 << 30, max(2 << 30, free // 4))
+        chunk_particles = max(1, min(N, budget // per))
     need = _abi.load().ss_pert_workspace_bytes(C.byref(cfg), precision, int(chunk_particles))
     if need < 0:
         raise _abi.SSError("ss_pert_workspace_bytes", need, _abi.load().ss_last_error().decode())

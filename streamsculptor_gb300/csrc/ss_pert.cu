@@ -32,132 +32,9 @@
 
 #include "ss_common.cuh"
 #include "ss_f2.cuh"
+#include "ss_pert.cuh"
 
 namespace ssg {
-
-// Base-track records per step: first order 6 stages x (x0[3], T[6]) + 2 pad;
-// second order (ncol = 18) adds the 10 independent third derivatives of the
-// base acceleration per stage: 6 x 19 + 6 pad.
-static constexpr int REC = 56;
-static constexpr int REC2 = 120;
-__host__ __device__ constexpr int rec_len(int ord) { return ord == 2 ? REC2 : REC; }
-__host__ __device__ constexpr int stage_len(int ord) { return ord == 2 ? 19 : 9; }
-
-struct PertArgs {
-    int64_t N;       // particles in the whole run
-    int64_t p0;      // first particle of the chunk
-    int64_t np;      // particles in the chunk
-    int32_t ppr;
-    int32_t spr;
-    int32_t n_steps;
-    int32_t ncol;
-    int32_t save_stride;
-    int32_t n_saves;
-    double t0;
-    double dt;
-    const double* base_ics;
-    double* base_out;
-    const void* pert_ics;
-    void* pert_out;
-    void* table;
-};
-
-__host__ __device__ inline int64_t pert_start(int64_t p, int32_t ppr, int32_t spr) { return (p / ppr) * (int64_t)spr; }
-
-// Number of records (steps) of particles [0, p): sum of (n_steps - start_q).
-__host__ __device__ inline int64_t pert_offset(int64_t p, int32_t ppr, int32_t spr, int32_t n_steps) {
-    int64_t R = p / ppr;
-    int64_t floors = (int64_t)ppr * (R * (R - 1) / 2) + (p - R * ppr) * R;
-    return p * (int64_t)n_steps - (int64_t)spr * floors;
-}
-
-// ------------------------------------------------------------- phase 1
-// One stage record of the base track at (x, t): x0, T = -Hessian(Phi)
-// (xx yy zz xy xz yz) and, for the second order, d2a/dx dx = -(third
-// derivatives of Phi) by forward-mode differentiation of the analytic
-// Hessian, ordered xxx xxy xxz xyy xyz xzz yyy yyz yzz zzz.  g = grad Phi.
-template <int ORD>
-__device__ __forceinline__ void base_stage(const PotDev<double>& P, const double x[3], double t, double g[3],
-                                           double r[19]) {
-    double cc[3] = {0.0, 0.0, 0.0};
-    if (P.has_track) track_eval(P.track, t, cc);
-    double H[6];
-    const double xs[3] = {x[0] - cc[0], x[1] - cc[1], x[2] - cc[2]};
-    const TimeDep<double> td = time_dep(P, t);
-    pot_grad<double, double, true>(P, x, xs, g, H, td);
-    r[0] = x[0];
-    r[1] = x[1];
-    r[2] = x[2];
-#pragma unroll
-    for (int c = 0; c < 6; ++c) r[3 + c] = -H[c];
-    if constexpr (ORD == 2) {
-        Dual<3> xd[3], xsd[3], gd[3], Hd[6];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            xd[c] = Dual<3>(x[c]);
-            xd[c].d[c] = 1.0;
-            xsd[c] = Dual<3>(xs[c]);
-            xsd[c].d[c] = 1.0;
-        }
-        pot_grad<Dual<3>, double, true>(P, xd, xsd, gd, Hd, time_dep_as<Dual<3>>(td));
-        // H order xx yy zz xy xz yz; D_abc = d H_ab / d x_c
-        const double D[10] = {Hd[0].d[0], Hd[0].d[1], Hd[0].d[2], Hd[1].d[0], Hd[3].d[2],
-                              Hd[2].d[0], Hd[1].d[1], Hd[1].d[2], Hd[2].d[1], Hd[2].d[2]};
-#pragma unroll
-        for (int c = 0; c < 10; ++c) r[9 + c] = -D[c];
-    }
-}
-
-template <class R, int ORD>
-__global__ void __launch_bounds__(64) pert_base_kernel(PotDev<double> P, PertArgs a) {
-    constexpr int RL = rec_len(ORD), SL = stage_len(ORD);
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.np) return;
-    const int64_t p = a.p0 + i;
-    const int start = (int)pert_start(p, a.ppr, a.spr);
-    R* rec = reinterpret_cast<R*>(a.table) +
-             (pert_offset(p, a.ppr, a.spr, a.n_steps) - pert_offset(a.p0, a.ppr, a.spr, a.n_steps)) * RL;
-    double y[6];
-    for (int k = 0; k < 6; ++k) y[k] = a.base_ics[6 * p + k];
-    const double h = a.dt;
-    const double cs[6] = {0.0, SS_C2, SS_C3, SS_C4, SS_C5, 1.0};
-    for (int n = start; n < a.n_steps; ++n, rec += RL) {
-        const double t = a.t0 + (double)n * h;
-        double k[6][6];
-        double ys[6];
-#pragma unroll
-        for (int s = 0; s < 6; ++s) {
-            // stage state
-#pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                double acc = 0.0;
-                if (s == 1) acc = SS_A21 * k[0][c];
-                if (s == 2) acc = SS_A31 * k[0][c] + SS_A32 * k[1][c];
-                if (s == 3) acc = SS_A41 * k[0][c] + SS_A42 * k[1][c] + SS_A43 * k[2][c];
-                if (s == 4) acc = SS_A51 * k[0][c] + SS_A52 * k[1][c] + SS_A53 * k[2][c] + SS_A54 * k[3][c];
-                if (s == 5)
-                    acc = SS_A61 * k[0][c] + SS_A62 * k[1][c] + SS_A63 * k[2][c] + SS_A64 * k[3][c] + SS_A65 * k[4][c];
-                ys[c] = s == 0 ? y[c] : y[c] + h * acc;
-            }
-            double g[3], r[19];
-            base_stage<ORD>(P, ys, t + cs[s] * h, g, r);
-            k[s][0] = ys[3];
-            k[s][1] = ys[4];
-            k[s][2] = ys[5];
-            k[s][3] = -g[0];
-            k[s][4] = -g[1];
-            k[s][5] = -g[2];
-            R* o = rec + SL * s;
-#pragma unroll
-            for (int c = 0; c < SL; ++c) o[c] = (R)r[c];
-        }
-#pragma unroll
-        for (int c = 0; c < 6; ++c)
-            y[c] = y[c] + h * (SS_B1 * k[0][c] + SS_B3 * k[2][c] + SS_B4 * k[3][c] + SS_B5 * k[4][c] + SS_B6 * k[5][c]);
-    }
-    if (a.base_out)
-        for (int c = 0; c < 6; ++c) a.base_out[6 * p + c] = y[c];
-}
 
 // ------------------------------------------------------------- phase 2
 // derivative of one ncol-state at a stage: K = (v1, a1 + T x1 [, v1r, a1r + T x1r])
@@ -583,7 +460,7 @@ __global__ void __launch_bounds__(128) pert_term_kernel(PotDev<double> P, ShDev 
     if (s >= sh.n) return;
     __align__(16) double r[20];
     double g[3];
-    base_stage<ORD>(P, y, t, g, r);
+    base_stage<GenericComp, ORD>(P, y, t, g, r);
     if (s == 0) {
         dy[0] = y[3];
         dy[1] = y[4];
@@ -728,16 +605,6 @@ static void launch_response(const ShDev& S, const PertArgs& a, int precision, un
                             cudaStream_t st) {
     if (precision == 64) launch_response_r<double>(S, a, g2, sblock, sblocks, st);
     else launch_response_r<float>(S, a, g2, sblock, sblocks, st);
-}
-
-static void launch_base(const PotDev<double>& P, const PertArgs& a, int precision, unsigned g1, cudaStream_t st) {
-    if (precision == 64) {
-        if (a.ncol == 18) pert_base_kernel<double, 2><<<g1, 64, 0, st>>>(P, a);
-        else pert_base_kernel<double, 1><<<g1, 64, 0, st>>>(P, a);
-    } else {
-        if (a.ncol == 18) pert_base_kernel<float, 2><<<g1, 64, 0, st>>>(P, a);
-        else pert_base_kernel<float, 1><<<g1, 64, 0, st>>>(P, a);
-    }
 }
 
 static int pert_response_launch(const ShDev& S, PertArgs a, int precision, cudaStream_t st) {
