@@ -202,3 +202,41 @@ def test_zhao_rejects_gamma_at_least_two(ss):
     for bad in [(1e11, 10.0, 1.0, 4.0, 2.0), (1e11, 10.0, 1.0, 3.0, 1.0), (1e11, 10.0, 0.0, 4.0, 1.0)]:
         with pytest.raises(Exception, match="Zhao"):
             P.ZhaoPotential(*bad, units=ss.usys).gradient(np.array([[1.0, 2.0, 3.0]]), 0.0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ncol", [6, 12])
+def test_zhao_pert_response_matches_oracle(ss, oracle, ncol):
+    """The first-order subhalo response (perturbative.py:24-135) on base
+    tracks in a Miyamoto-Nagai disk plus a Zhao halo: the base track needs
+    the Zhao Hessian along the track (the generic component loop of
+    pert_base_kernel).  Against the oracle, whose Hessian is the autodiff of
+    the reference's forward-difference gradient: FP64 base track to 1e-9 and
+    response to 1e-7 (the difference's rounding noise, ~1e-10 of the force,
+    is what separates them), FP32 response to 2e-4."""
+    from streamsculptor_gb300 import _abi, _core, potential as P
+    from .conftest import PROG_WF
+    zp = (5e11, 15.0, 1.0, 3.5, 1.0)
+    rng = np.random.default_rng(8)
+    N, nsh, ppr, spr, n_steps, dt = 16, 5, 4, 10, 100, 1.0
+    sh = dict(kind=1, m=10 ** rng.uniform(5, 8, nsh), a=rng.uniform(0.1, 1.0, nsh), x0=rng.normal(0, 10, (nsh, 3)),
+              v=rng.normal(0, 0.12, (nsh, 3)), t0=rng.uniform(0, 100, nsh), t_window=60.0)
+    orc = oracle.HostModel([(_abi.SS_MIYAMOTO_NAGAI, 0, (6.8e10, 3.0, 0.28)), (_abi.SS_ZHAO, 0, zp)], subhalos=sh)
+    base = PROG_WF + rng.normal(0, 0.3, (N, 6)) * np.array([1, 1, 1, 0.01, 0.01, 0.01])
+    pert = np.ascontiguousarray(rng.normal(0, 1e-3, (N, nsh, ncol)))
+    bo, po = oracle.pert_response(orc, 0.0, dt, n_steps, base, pert, ppr, spr, ncol=ncol, save_stride=25)
+    pot = P.Potential_Combine([P.MiyamotoNagaiDisk(m=6.8e10, a=3.0, b=0.28, units=ss.usys),
+                               P.ZhaoPotential(*zp, units=ss.usys)], units=ss.usys)
+    table = _core.SubhaloTable(1, *(_core.f64(sh[k]) for k in ("m", "a")), _core.f64(sh["x0"]), _core.f64(sh["v"]),
+                               _core.f64(sh["t0"]), sh["t_window"])
+    cfg = _abi.ss_pert_cfg()
+    cfg.t0, cfg.dt, cfg.n_steps, cfg.n_particles = 0.0, dt, n_steps, N
+    cfg.particles_per_release, cfg.steps_per_release, cfg.ncol, cfg.save_stride = ppr, spr, ncol, 25
+    for prec, tol in ((64, 1e-7), (32, 2e-4)):
+        b, p = _core.pert_response(pot._desc(), table, cfg, prec, _core.f64(base), _core.f64(pert))
+        b = b.double().cpu().numpy()
+        eb = np.max(np.linalg.norm(b - bo, axis=1) / np.linalg.norm(bo, axis=1))
+        ep = rel_err(p.double().cpu().numpy(), po)
+        print(f"Zhao response ({prec}, ncol {ncol}): base {eb:.2e}, response {ep:.2e}")
+        assert eb < 1e-9
+        assert ep < tol, prec
