@@ -1692,6 +1692,18 @@ struct Comp {
         }
         add<T, R, HESS>(P, x, xs, g, H, td, std::make_integer_sequence<int, n>{});
     }
+    // component k alone (k uniform across the warp), added to g
+    template <class T, class R, bool HESS, int... I>
+    static __device__ __forceinline__ void add_only(const PotDev<R>& P, int k, const T x[3], const T xs[3], T g[3],
+                                                    T H[6], const TimeDep<T>& td, std::integer_sequence<int, I...>) {
+        ((k == I ? one<(KCS & 15), T, R, HESS>(P, I, (KCS >> 4) ? xs : x, g, H, td) : void()), ...);
+    }
+    template <class T, class R, bool HESS>
+    static __device__ __forceinline__ void grad_only(const PotDev<R>& P, int k, const T x[3], const T xs[3], T g[3],
+                                                     T H[6], const TimeDep<T>& td = TimeDep<T>()) {
+        g[0] = g[1] = g[2] = T(0);
+        add_only<T, R, HESS>(P, k, x, xs, g, H, td, std::make_integer_sequence<int, n>{});
+    }
     template <class R>
     static bool matches(const PotDev<R>& P) {
         const int kc[] = {KCS...};

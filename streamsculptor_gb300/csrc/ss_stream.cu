@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <type_traits>
 
 #include "ss_stream.cuh"
 #include "ss_stream2.cuh"
@@ -51,6 +52,12 @@ __global__ void __launch_bounds__(F64_BLOCK, 1) stream_f64_kernel<GenericComp>(P
 template <>
 __global__ void __launch_bounds__(F64_BLOCK, 1) stream_f64_kernel<CompSHExp>(PotDev<double> P, StreamArgs a) {
     stream_f64_body<CompSHExp>(P, a);
+}
+
+// The component-split FP64 kernel for small runs (stream_f64_split_body).
+template <class C>
+__global__ void __launch_bounds__(32 * C::n) stream_f64_split_kernel(PotDev<double> P, StreamArgs a) {
+    stream_f64_split_body<C>(P, a);
 }
 
 // Track positions at every stage time of the run, FP64 Hermite -> a hi/lo
@@ -228,8 +235,23 @@ int ss_stream_f64(const ss_potential* pot, const ss_stream_cfg* cfg, const doubl
     StreamArgs a = make_args(cfg, ics, final_w, snaps, status);
     const int block = F64_BLOCK;
     unsigned grid = (unsigned)((cfg->n_particles + block - 1) / block);
+    // fewer warps than schedulers (4 per SM): the component-split form
+    int dev = 0, sms = 0;
+    SS_CUDA_TRY(cudaGetDevice(&dev));
+    SS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const bool small = P.sh.n == 0 && (cfg->n_particles + 31) / 32 < 4 * (int64_t)sms;
     dispatch_comp(P, [&](auto comp) {
-        stream_f64_kernel<decltype(comp)><<<grid, block, 0, (cudaStream_t)stream>>>(P, a);
+        using C = decltype(comp);
+        if constexpr (!std::is_same<C, GenericComp>::value) {
+            if constexpr (C::n >= 2) {
+                if (small) {
+                    const unsigned g = (unsigned)((cfg->n_particles + 31) / 32);
+                    stream_f64_split_kernel<C><<<g, 32 * C::n, 0, (cudaStream_t)stream>>>(P, a);
+                    return 0;
+                }
+            }
+        }
+        stream_f64_kernel<C><<<grid, block, 0, (cudaStream_t)stream>>>(P, a);
         return 0;
     });
     SS_LAUNCH_CHECK();

@@ -147,6 +147,148 @@ __device__ __forceinline__ void stream_f64_body(const PotDev<double>& P, const S
     }
 }
 
+// ------------------------------------------------- FP64, component-split
+// Small runs (fewer warps than the GPU has schedulers) leave most of the FP64
+// units idle, and each warp's FP64 instructions are issued one after another
+// by its scheduler's FP64 unit: the run lasts as long as the longest tracks'
+// warps take to issue their instructions, whatever the number of active
+// lanes.  This form spreads each particle over C::n warps of one block, warp
+// w evaluating component w of the force: all warps hold the same 32
+// particles and do the same Dopri5 arithmetic on identical copies of the
+// state; at each stage they exchange their component gradients through
+// shared memory (double-buffered, one barrier per stage) and every warp sums
+// them in component order, so the copies stay identical.  A lane whose
+// particle is not yet released steps with h = 0 (its state is unchanged), so
+// that every thread reaches every barrier.  Compiled compositions without
+// subhalos only.
+template <class C>
+__device__ __forceinline__ void split_accel_f64(const PotDev<double>& P, const double x[3], double t, double acc[3],
+                                                const double* cen, double (*gs)[32][3], int w, int lane) {
+    double c[3] = {0.0, 0.0, 0.0};
+    if (cen) {
+        c[0] = cen[0];
+        c[1] = cen[1];
+        c[2] = cen[2];
+    } else if (P.has_track) {
+        track_eval(P.track, t, c);
+    }
+    const double xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
+    double g[3];
+    C::template grad_only<double, double, false>(P, w, x, xs, g, nullptr, time_dep(P, t));
+    gs[w][lane][0] = g[0];
+    gs[w][lane][1] = g[1];
+    gs[w][lane][2] = g[2];
+    __syncthreads();
+    double s0 = gs[0][lane][0], s1 = gs[0][lane][1], s2 = gs[0][lane][2];
+#pragma unroll
+    for (int k = 1; k < C::n; ++k) {
+        s0 += gs[k][lane][0];
+        s1 += gs[k][lane][1];
+        s2 += gs[k][lane][2];
+    }
+    acc[0] = -s0;
+    acc[1] = -s1;
+    acc[2] = -s2;
+}
+
+// One Dopri5 step of dopri5_step_f64 with split_accel_f64 (stage times from
+// the global step dt, increments from h); buf[2][C::n][32][3] alternates per
+// stage.
+template <class C>
+__device__ __forceinline__ void split_step_f64(const PotDev<double>& P, double t, double dt, double h, double y[6],
+                                               const double (*cen)[3], double (*buf)[C::n][32][3], int& par, int w,
+                                               int lane) {
+    double k1[6], k2[6], k3[6], k4[6], k5[6], k6[6], ys[6];
+    k1[0] = y[3]; k1[1] = y[4]; k1[2] = y[5];
+    split_accel_f64<C>(P, y, t, k1 + 3, cen ? cen[0] : nullptr, buf[par], w, lane);
+    par ^= 1;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) ys[i] = y[i] + h * (SS_A21 * k1[i]);
+    k2[0] = ys[3]; k2[1] = ys[4]; k2[2] = ys[5];
+    split_accel_f64<C>(P, ys, t + SS_C2 * dt, k2 + 3, cen ? cen[1] : nullptr, buf[par], w, lane);
+    par ^= 1;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) ys[i] = y[i] + h * (SS_A31 * k1[i] + SS_A32 * k2[i]);
+    k3[0] = ys[3]; k3[1] = ys[4]; k3[2] = ys[5];
+    split_accel_f64<C>(P, ys, t + SS_C3 * dt, k3 + 3, cen ? cen[2] : nullptr, buf[par], w, lane);
+    par ^= 1;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) ys[i] = y[i] + h * (SS_A41 * k1[i] + SS_A42 * k2[i] + SS_A43 * k3[i]);
+    k4[0] = ys[3]; k4[1] = ys[4]; k4[2] = ys[5];
+    split_accel_f64<C>(P, ys, t + SS_C4 * dt, k4 + 3, cen ? cen[3] : nullptr, buf[par], w, lane);
+    par ^= 1;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        ys[i] = y[i] + h * (SS_A51 * k1[i] + SS_A52 * k2[i] + SS_A53 * k3[i] + SS_A54 * k4[i]);
+    k5[0] = ys[3]; k5[1] = ys[4]; k5[2] = ys[5];
+    split_accel_f64<C>(P, ys, t + SS_C5 * dt, k5 + 3, cen ? cen[4] : nullptr, buf[par], w, lane);
+    par ^= 1;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        ys[i] = y[i] + h * (SS_A61 * k1[i] + SS_A62 * k2[i] + SS_A63 * k3[i] + SS_A64 * k4[i] + SS_A65 * k5[i]);
+    k6[0] = ys[3]; k6[1] = ys[4]; k6[2] = ys[5];
+    split_accel_f64<C>(P, ys, t + dt, k6 + 3, cen ? cen[5] : nullptr, buf[par], w, lane);
+    par ^= 1;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        y[i] = y[i] + h * (SS_B1 * k1[i] + SS_B3 * k3[i] + SS_B4 * k4[i] + SS_B5 * k5[i] + SS_B6 * k6[i]);
+}
+
+// Block of 32 C::n threads: warp w = threadIdx.x / 32 evaluates component w
+// for the block's 32 particles; warp 0 writes the outputs.
+template <class C>
+__device__ __forceinline__ void stream_f64_split_body(const PotDev<double>& P, const StreamArgs& a) {
+    __shared__ double buf[2][C::n][32][3];
+    __shared__ double ctab[6 * F64_CHUNK][3];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t p = (int64_t)blockIdx.x * 32 + lane;
+    const bool valid = p < a.N;
+    const int64_t q = valid ? p : a.N - 1;  // lanes past the end follow the last particle (never written)
+    const int start = stream_start(a, q + a.p_off);
+    const int bstart = (int)__reduce_min_sync(0xffffffffu, (unsigned)start);  // the same in every warp
+    const bool tab = P.has_track;
+    double y[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) y[i] = a.ics[6 * q + i];
+    const bool out = w == 0 && valid;
+    if (a.snaps && out) {
+        for (int64_t k = 0; (k + 1) * (int64_t)a.stride <= bstart; ++k) {
+            const int64_t step = (k + 1) * (int64_t)a.stride;
+            write_snap<double>(a.snaps, a.snap_pitch, k, p + a.p_off, step >= start, y);
+        }
+    }
+    int par = 0;
+    for (int n0 = bstart; n0 < a.n_steps; n0 += F64_CHUNK) {
+        const int cnt = min(F64_CHUNK, a.n_steps - n0);
+        if (tab) {
+            __syncthreads();  // the previous chunk's table has been read
+            for (int i = threadIdx.x; i < 6 * cnt; i += blockDim.x) {
+                const int j = i / 6, s = i - 6 * j;
+                const double t = a.t0 + (double)(n0 + j) * a.dt;
+                const double c = s == 1 ? SS_C2 : s == 2 ? SS_C3 : s == 3 ? SS_C4 : SS_C5;
+                track_eval(P.track, s == 0 ? t : s == 5 ? t + a.dt : t + c * a.dt, ctab[i]);
+            }
+            __syncthreads();
+        }
+        for (int j = 0; j < cnt; ++j) {
+            const int n = n0 + j;
+            split_step_f64<C>(P, a.t0 + (double)n * a.dt, a.dt, n >= start ? a.dt : 0.0, y,
+                              tab ? &ctab[6 * j] : nullptr, buf, par, w, lane);
+            if (a.snaps && (n + 1) % a.stride == 0 && out)
+                write_snap<double>(a.snaps, a.snap_pitch, (n + 1) / a.stride - 1, p + a.p_off, n + 1 >= start, y);
+        }
+    }
+    if (!out) return;
+    bool ok = true;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) ok = ok && isfinite(y[i]);
+    if (a.status) a.status[p] = ok ? 0 : 1;
+    if (a.final_w) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) a.final_w[6 * p + i] = y[i];
+    }
+}
+
 // ------------------------------------------------------------------ FP32-K
 #define F_C2 0.2f
 #define F_C3 0.3f

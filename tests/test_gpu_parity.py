@@ -919,3 +919,38 @@ def test_streakline_matches_oracle(ss, oracle, precision, tol):
     assert err <= tol
     # released at t1: the pair's initial states (hi + lo in the FP32 form)
     np.testing.assert_allclose(got[-2:], got_ics[-1], rtol=1e-15 if precision == "f64" else 1e-13)
+
+
+@pytest.mark.parametrize("snap", [0, 25])
+def test_f64_split_kernel_matches_plain_kernel(ss, snap):
+    """Runs with fewer warps than the GPU has schedulers take the
+    component-split FP64 kernel (one warp per potential component, the
+    gradients exchanged through shared memory); larger runs the
+    one-thread-per-particle kernel.  The same particles through both (the
+    first 6400 of a run just above the threshold, then alone): the same
+    arithmetic but the order of the component sum, so the final states agree
+    to 1e-13 and the status and snapshot NaN pattern exactly."""
+    from streamsculptor_gb300 import _core
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    n_big, n_small, ppr, n_steps = 4 * sms * 32 + 96, 6400, 100, 300
+    rng = np.random.default_rng(11)
+    ics = PROG_WF + rng.normal(0, 0.4, (n_big, 6)) * np.array([1, 1, 1, 0.01, 0.01, 0.01])
+    ics_d = torch.as_tensor(ics, device="cuda")
+    P = mw3_gpu(ss)._desc()
+    outs = []
+    for n in (n_big, n_small):
+        cfg = _abi.ss_stream_cfg()
+        cfg.t0, cfg.dt, cfg.n_steps, cfg.n_particles = 0.0, 1.0, n_steps, n
+        cfg.particles_per_release, cfg.steps_per_release, cfg.snap_stride = ppr, 1, snap
+        snaps = torch.empty(n_steps // snap, n, 6, dtype=torch.float32, device="cuda") if snap else None
+        final, st = _core.stream(P, cfg, ics_d[:n].contiguous(), "f64", snaps=snaps)
+        outs.append((final, st, snaps))
+    (fb, sb, snb), (fs, ss_, sns) = outs
+    assert torch.equal(sb[:n_small], ss_)
+    assert bool((ss_ == 0).all())
+    assert phase_err(np64(fs), np64(fb[:n_small])) <= 1e-13
+    if snap:
+        a, b = np64(snb[:, :n_small]), np64(sns)
+        assert np.array_equal(np.isnan(a), np.isnan(b))
+        ok = ~np.isnan(a)
+        assert np.max(np.abs(a[ok] - b[ok]) / np.maximum(np.abs(a[ok]), 1e-3)) <= 1e-6
