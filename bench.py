@@ -627,7 +627,7 @@ def c1_leg(dev, flush):
     out = {"workload": wl["name"], "particle_steps_per_step": s.work,
            "f64": {"value": s.work / (r64["ms_per_step"] * 1e-3), "unit": UNIT, "ms_per_step": r64["ms_per_step"],
                    "steps": r64["steps"], "warmup": r64["warmup"], "clocks": r64["clocks"],
-                   "roofline": s.roofline(r64, "f64", "stream_f64_kernel", p64)},
+                   "roofline": s.roofline(r64, "f64", "stream_f64_split_kernel", p64)},
            "f32k": {"value": s.work / (r32["ms_per_step"] * 1e-3), "unit": UNIT, "ms_per_step": r32["ms_per_step"],
                     "steps": r32["steps"], "warmup": r32["warmup"], "clocks": r32["clocks"],
                     "roofline": s.roofline(r32, "f32k2", "stream_f32k2_kernel", p2)},
@@ -635,7 +635,8 @@ def c1_leg(dev, flush):
            "parity_vs_oracle": dict(oracle_parity(s, orc, F64, F32), ics_max=ics_vs_oracle(X0, orc, dev),
                                     sample="every particle; the oracle integrates this run's initial conditions"),
            "note": "6000 particles on 152 SMs: the FP64 time is set by the longest tracks' serial step chain "
-                   "(3000 steps), not by the FP64 pipe"}
+                   "(3000 steps), not by the FP64 pipe; the FP64 run takes the component-split kernel (one warp "
+                   "per potential component, 188 blocks of 3 warps)"}
     del F64, F32, X0
     torch.cuda.synchronize()
     return out
