@@ -10,7 +10,9 @@
 // gen_stream_vmapped_with_pert (streamhelpers.py:89-146) adds subhalos.
 //
 // Layout: one thread per particle (two for stream_f32k2_kernel, ss_stream2.cuh,
-// the FP32 form for compiled compositions); particles are ordered by release (release
+// the FP32 form for compiled compositions; one warp per potential component
+// for stream_f64_split_kernel, the FP64 form of runs too small to occupy the
+// GPU's schedulers); particles are ordered by release (release
 // r owns particles [r*ppr, (r+1)*ppr)), so the earliest (longest) particles
 // sit in the lowest blocks and are scheduled first.  A warp runs in global
 // lock-step from its earliest start step: lanes released later idle until
