@@ -245,7 +245,7 @@ int ss_stream_f64(const ss_potential* pot, const ss_stream_cfg* cfg, const doubl
     dispatch_comp(P, [&](auto comp) {
         using C = decltype(comp);
         if constexpr (!std::is_same<C, GenericComp>::value) {
-            if constexpr (C::n >= 2) {
+            if constexpr (C::n >= 3) {
                 if (small) {
                     const unsigned g = (unsigned)((cfg->n_particles + 31) / 32);
                     stream_f64_split_kernel<C><<<g, 32 * C::n, 0, (cudaStream_t)stream>>>(P, a);

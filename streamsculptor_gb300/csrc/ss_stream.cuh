@@ -152,18 +152,23 @@ __device__ __forceinline__ void stream_f64_body(const PotDev<double>& P, const S
 // units idle, and each warp's FP64 instructions are issued one after another
 // by its scheduler's FP64 unit: the run lasts as long as the longest tracks'
 // warps take to issue their instructions, whatever the number of active
-// lanes.  This form spreads each particle over C::n warps of one block, warp
-// w evaluating component w of the force: all warps hold the same 32
-// particles and do the same Dopri5 arithmetic on identical copies of the
-// state; at each stage they exchange their component gradients through
-// shared memory (double-buffered, one barrier per stage) and every warp sums
-// them in component order, so the copies stay identical.  A lane whose
-// particle is not yet released steps with h = 0 (its state is unchanged), so
-// that every thread reaches every barrier.  Compiled compositions without
-// subhalos only.
+// lanes.  This form spreads each particle over the C::n (>= 3) warps of one
+// block: warp w evaluates component w of the force, and warps 0-2 each own
+// one coordinate pair (x_w, v_w) of the state and do its share of the Dopri5
+// arithmetic.  Per stage the owners publish their stage position through
+// shared memory, every warp evaluates its component there, and each owner
+// sums its coordinate of the component gradients in component order: the
+// same operations per coordinate as dopri5_step_f64, with two barriers per
+// stage.  A lane whose particle is not yet released steps with h = 0 (its
+// state is unchanged), so that every thread reaches every barrier.
+// Compiled compositions without subhalos only.
+
+// Component w's gradient at the stage position in xsh (time t, center cen
+// or the track), into gsh[w][lane].
 template <class C>
-__device__ __forceinline__ void split_accel_f64(const PotDev<double>& P, const double x[3], double t, double acc[3],
-                                                const double* cen, double (*gs)[32][3], int w, int lane) {
+__device__ __forceinline__ void split_component(const PotDev<double>& P, double t, const double* cen,
+                                                const double (*xsh)[32], double (*gsh)[32][3], int w, int lane) {
+    const double x[3] = {xsh[0][lane], xsh[1][lane], xsh[2][lane]};
     double c[3] = {0.0, 0.0, 0.0};
     if (cen) {
         c[0] = cen[0];
@@ -175,89 +180,90 @@ __device__ __forceinline__ void split_accel_f64(const PotDev<double>& P, const d
     const double xs[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
     double g[3];
     C::template grad_only<double, double, false>(P, w, x, xs, g, nullptr, time_dep(P, t));
-    gs[w][lane][0] = g[0];
-    gs[w][lane][1] = g[1];
-    gs[w][lane][2] = g[2];
-    __syncthreads();
-    double s0 = gs[0][lane][0], s1 = gs[0][lane][1], s2 = gs[0][lane][2];
-#pragma unroll
-    for (int k = 1; k < C::n; ++k) {
-        s0 += gs[k][lane][0];
-        s1 += gs[k][lane][1];
-        s2 += gs[k][lane][2];
-    }
-    acc[0] = -s0;
-    acc[1] = -s1;
-    acc[2] = -s2;
+    gsh[w][lane][0] = g[0];
+    gsh[w][lane][1] = g[1];
+    gsh[w][lane][2] = g[2];
 }
 
-// One Dopri5 step of dopri5_step_f64 with split_accel_f64 (stage times from
-// the global step dt, increments from h); buf[2][C::n][32][3] alternates per
-// stage.
+// One Dopri5 step (stage times from the global step dt, increments from h)
+// of the coordinate pair (yp, yv) = (x_w, v_w) owned by warps w < 3.
 template <class C>
-__device__ __forceinline__ void split_step_f64(const PotDev<double>& P, double t, double dt, double h, double y[6],
-                                               const double (*cen)[3], double (*buf)[C::n][32][3], int& par, int w,
-                                               int lane) {
-    double k1[6], k2[6], k3[6], k4[6], k5[6], k6[6], ys[6];
-    k1[0] = y[3]; k1[1] = y[4]; k1[2] = y[5];
-    split_accel_f64<C>(P, y, t, k1 + 3, cen ? cen[0] : nullptr, buf[par], w, lane);
-    par ^= 1;
+__device__ __forceinline__ void split_step_f64(const PotDev<double>& P, double t, double dt, double h, double& yp,
+                                               double& yv, const double (*cen)[3], double (*xsh)[32],
+                                               double (*gsh)[32][3], int w, int lane) {
+    const bool own = w < 3;
+    double kp[6], kv[6];  // per stage: the coordinate's velocity and acceleration
+    const double cs[6] = {0.0, SS_C2, SS_C3, SS_C4, SS_C5, 1.0};
 #pragma unroll
-    for (int i = 0; i < 6; ++i) ys[i] = y[i] + h * (SS_A21 * k1[i]);
-    k2[0] = ys[3]; k2[1] = ys[4]; k2[2] = ys[5];
-    split_accel_f64<C>(P, ys, t + SS_C2 * dt, k2 + 3, cen ? cen[1] : nullptr, buf[par], w, lane);
-    par ^= 1;
+    for (int s = 0; s < 6; ++s) {
+        double xp = yp, xv = yv;  // warps w >= 3 own no coordinate
+        if (own && s == 1) { xp = yp + h * (SS_A21 * kp[0]); xv = yv + h * (SS_A21 * kv[0]); }
+        if (own && s == 2) {
+            xp = yp + h * (SS_A31 * kp[0] + SS_A32 * kp[1]);
+            xv = yv + h * (SS_A31 * kv[0] + SS_A32 * kv[1]);
+        }
+        if (own && s == 3) {
+            xp = yp + h * (SS_A41 * kp[0] + SS_A42 * kp[1] + SS_A43 * kp[2]);
+            xv = yv + h * (SS_A41 * kv[0] + SS_A42 * kv[1] + SS_A43 * kv[2]);
+        }
+        if (own && s == 4) {
+            xp = yp + h * (SS_A51 * kp[0] + SS_A52 * kp[1] + SS_A53 * kp[2] + SS_A54 * kp[3]);
+            xv = yv + h * (SS_A51 * kv[0] + SS_A52 * kv[1] + SS_A53 * kv[2] + SS_A54 * kv[3]);
+        }
+        if (own && s == 5) {
+            xp = yp + h * (SS_A61 * kp[0] + SS_A62 * kp[1] + SS_A63 * kp[2] + SS_A64 * kp[3] + SS_A65 * kp[4]);
+            xv = yv + h * (SS_A61 * kv[0] + SS_A62 * kv[1] + SS_A63 * kv[2] + SS_A64 * kv[3] + SS_A65 * kv[4]);
+        }
+        if (own) xsh[w][lane] = xp;
+        __syncthreads();  // the stage position is complete
+        split_component<C>(P, t + cs[s] * dt, cen ? cen[s] : nullptr, xsh, gsh, w, lane);
+        __syncthreads();  // every component's gradient is in
+        if (own) {
+            double g = gsh[0][lane][w];
 #pragma unroll
-    for (int i = 0; i < 6; ++i) ys[i] = y[i] + h * (SS_A31 * k1[i] + SS_A32 * k2[i]);
-    k3[0] = ys[3]; k3[1] = ys[4]; k3[2] = ys[5];
-    split_accel_f64<C>(P, ys, t + SS_C3 * dt, k3 + 3, cen ? cen[2] : nullptr, buf[par], w, lane);
-    par ^= 1;
-#pragma unroll
-    for (int i = 0; i < 6; ++i) ys[i] = y[i] + h * (SS_A41 * k1[i] + SS_A42 * k2[i] + SS_A43 * k3[i]);
-    k4[0] = ys[3]; k4[1] = ys[4]; k4[2] = ys[5];
-    split_accel_f64<C>(P, ys, t + SS_C4 * dt, k4 + 3, cen ? cen[3] : nullptr, buf[par], w, lane);
-    par ^= 1;
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-        ys[i] = y[i] + h * (SS_A51 * k1[i] + SS_A52 * k2[i] + SS_A53 * k3[i] + SS_A54 * k4[i]);
-    k5[0] = ys[3]; k5[1] = ys[4]; k5[2] = ys[5];
-    split_accel_f64<C>(P, ys, t + SS_C5 * dt, k5 + 3, cen ? cen[4] : nullptr, buf[par], w, lane);
-    par ^= 1;
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-        ys[i] = y[i] + h * (SS_A61 * k1[i] + SS_A62 * k2[i] + SS_A63 * k3[i] + SS_A64 * k4[i] + SS_A65 * k5[i]);
-    k6[0] = ys[3]; k6[1] = ys[4]; k6[2] = ys[5];
-    split_accel_f64<C>(P, ys, t + dt, k6 + 3, cen ? cen[5] : nullptr, buf[par], w, lane);
-    par ^= 1;
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-        y[i] = y[i] + h * (SS_B1 * k1[i] + SS_B3 * k3[i] + SS_B4 * k4[i] + SS_B5 * k5[i] + SS_B6 * k6[i]);
+            for (int k = 1; k < C::n; ++k) g += gsh[k][lane][w];
+            kp[s] = xv;
+            kv[s] = -g;
+        }
+    }
+    if (own) {
+        yp = yp + h * (SS_B1 * kp[0] + SS_B3 * kp[2] + SS_B4 * kp[3] + SS_B5 * kp[4] + SS_B6 * kp[5]);
+        yv = yv + h * (SS_B1 * kv[0] + SS_B3 * kv[2] + SS_B4 * kv[3] + SS_B5 * kv[4] + SS_B6 * kv[5]);
+    }
 }
 
-// Block of 32 C::n threads: warp w = threadIdx.x / 32 evaluates component w
-// for the block's 32 particles; warp 0 writes the outputs.
+// Block of 32 C::n threads for 32 particles; the outputs go through a
+// shared copy of the state (warp 0 writes them).
 template <class C>
 __device__ __forceinline__ void stream_f64_split_body(const PotDev<double>& P, const StreamArgs& a) {
-    __shared__ double buf[2][C::n][32][3];
+    static_assert(C::n >= 3, "the split form needs a warp per coordinate");
+    __shared__ double xsh[3][32];
+    __shared__ double gsh[C::n][32][3];
+    __shared__ double ysh[6][32];
     __shared__ double ctab[6 * F64_CHUNK][3];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool own = w < 3;
     const int64_t p = (int64_t)blockIdx.x * 32 + lane;
     const bool valid = p < a.N;
     const int64_t q = valid ? p : a.N - 1;  // lanes past the end follow the last particle (never written)
     const int start = stream_start(a, q + a.p_off);
     const int bstart = (int)__reduce_min_sync(0xffffffffu, (unsigned)start);  // the same in every warp
     const bool tab = P.has_track;
-    double y[6];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) y[i] = a.ics[6 * q + i];
+    double yp = 0.0, yv = 0.0;
+    if (own) {
+        yp = a.ics[6 * q + w];
+        yv = a.ics[6 * q + 3 + w];
+    }
     const bool out = w == 0 && valid;
     if (a.snaps && out) {
+        double y0[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) y0[i] = a.ics[6 * q + i];
         for (int64_t k = 0; (k + 1) * (int64_t)a.stride <= bstart; ++k) {
             const int64_t step = (k + 1) * (int64_t)a.stride;
-            write_snap<double>(a.snaps, a.snap_pitch, k, p + a.p_off, step >= start, y);
+            write_snap<double>(a.snaps, a.snap_pitch, k, p + a.p_off, step >= start, y0);
         }
     }
-    int par = 0;
     for (int n0 = bstart; n0 < a.n_steps; n0 += F64_CHUNK) {
         const int cnt = min(F64_CHUNK, a.n_steps - n0);
         if (tab) {
@@ -272,16 +278,37 @@ __device__ __forceinline__ void stream_f64_split_body(const PotDev<double>& P, c
         }
         for (int j = 0; j < cnt; ++j) {
             const int n = n0 + j;
-            split_step_f64<C>(P, a.t0 + (double)n * a.dt, a.dt, n >= start ? a.dt : 0.0, y,
-                              tab ? &ctab[6 * j] : nullptr, buf, par, w, lane);
-            if (a.snaps && (n + 1) % a.stride == 0 && out)
-                write_snap<double>(a.snaps, a.snap_pitch, (n + 1) / a.stride - 1, p + a.p_off, n + 1 >= start, y);
+            split_step_f64<C>(P, a.t0 + (double)n * a.dt, a.dt, n >= start ? a.dt : 0.0, yp, yv,
+                              tab ? &ctab[6 * j] : nullptr, xsh, gsh, w, lane);
+            if (a.snaps && (n + 1) % a.stride == 0) {  // block-uniform
+                if (own) {
+                    ysh[w][lane] = yp;
+                    ysh[3 + w][lane] = yv;
+                }
+                __syncthreads();
+                if (out) {
+                    double y[6];
+#pragma unroll
+                    for (int i = 0; i < 6; ++i) y[i] = ysh[i][lane];
+                    write_snap<double>(a.snaps, a.snap_pitch, (n + 1) / a.stride - 1, p + a.p_off, n + 1 >= start, y);
+                }
+                __syncthreads();  // read before the next gather
+            }
         }
     }
+    if (own) {
+        ysh[w][lane] = yp;
+        ysh[3 + w][lane] = yv;
+    }
+    __syncthreads();
     if (!out) return;
+    double y[6];
     bool ok = true;
 #pragma unroll
-    for (int i = 0; i < 6; ++i) ok = ok && isfinite(y[i]);
+    for (int i = 0; i < 6; ++i) {
+        y[i] = ysh[i][lane];
+        ok = ok && isfinite(y[i]);
+    }
     if (a.status) a.status[p] = ok ? 0 : 1;
     if (a.final_w) {
 #pragma unroll
