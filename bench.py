@@ -378,6 +378,58 @@ class Spray:
                 "samples_ms": [a.elapsed_time(b) for a, b in evs], "launches": launches, "clocks": ck,
                 "steps": K, "warmup": W}
 
+    def timed_pipelined(self, K, W, flush, barrier=lambda: None, world=1):
+        """The same K FP32-compensated steps as timed('f32k') (the
+        progenitor's orbit back from the present, its forward orbit, the
+        release, the track tables and the stream with snapshots) through the
+        public gen_stream_batches: each step's orbits, release and tables run
+        on a side stream while the previous step's stream kernel fills the
+        GPU.  The L2 flush stays between consecutive stream kernels."""
+        import torch
+        import torch.distributed as dist
+
+        from streamsculptor_gb300 import _abi, _core
+        from streamsculptor_gb300.streamhelpers import gen_stream_batches
+        lib = _abi.load()
+
+        def run(n, evs=None):
+            for out in gen_stream_batches(self.pot, self.ts, self.wf_d, MSAT, self.normals_d, n_batches=n,
+                                          dt=self.dt, prog_pot=self.prog, n_particles_per_release=self.ppr,
+                                          precision="f32k", snapshot_every=self.snap or None, prog_w0_at="end"):
+                del out
+                flush.zero_()
+                if evs is not None:
+                    ev = torch.cuda.Event(enable_timing=True)
+                    ev.record()
+                    evs.append(ev)
+
+        run(W)
+        torch.cuda.synchronize()
+        barrier()
+        kev = []
+        _core.STREAM_EVENTS = kev
+        l0 = lib.ss_kernel_launches()
+        clocks = ClockSampler(gpu_id_for(self.dev.index or 0))
+        clocks.start()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        evs = []
+        run(K, evs)
+        torch.cuda.synchronize()
+        barrier()
+        ck = clocks.stop()
+        launches = lib.ss_kernel_launches() - l0
+        _core.STREAM_EVENTS = None
+        ms = e0.elapsed_time(evs[-1])
+        marks = [e0] + evs
+        samples = [a.elapsed_time(b) for a, b in zip(marks[:-1], marks[1:])]
+        if world > 1:
+            t = torch.tensor([ms], device=self.dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return {"ms_total": ms, "ms_per_step": ms / K, "kernel_ms": statistics.mean(a.elapsed_time(b) for a, b in kev),
+                "samples_ms": samples, "launches": launches, "clocks": ck, "steps": K, "warmup": W}
+
     def roofline(self, r, precision, kernel, peak):
         from streamsculptor_gb300 import _core, potential as P, roofline
         parts = [self.pot]
@@ -478,8 +530,11 @@ def gpu_arm(args, wl):
                   "kernel_ms": r1["kernel_ms"], "config": config_for(wl), "clocks": r1["clocks"],
                   "gpu_launches": r1["launches"], "note": f"{precisions[0]} only (profiling run)"})
         return
-    # --- headline: FP32-compensated, inputs resident
-    r32 = s.timed("f32k", args.steps, args.warmup, flush, barrier, world)
+    # --- headline: FP32-compensated, inputs resident; K steps one after the
+    # other, then the same K steps pipelined (gen_stream_batches: a step's
+    # orbits and release overlap the previous step's stream kernel)
+    r32s = s.timed("f32k", args.steps, args.warmup, flush, barrier, world)
+    r32 = s.timed_pipelined(args.steps, args.warmup, flush, barrier, world)
     value = world * s.work / (r32["ms_per_step"] * 1e-3)
     # --- e2e through the public API with host buffers (right after the device timing)
     from streamsculptor_gb300.streamhelpers import gen_stream
@@ -555,6 +610,12 @@ def gpu_arm(args, wl):
                                     "path": "gen_stream(out='host', host_mode='chunked'): 8 particle sub-ranges, "
                                             "each copied by the copy engine while the next integrates"}},
                 "samples_ms": r32["samples_ms"], "clocks": r32["clocks"], "gpu_launches": r32["launches"],
+                "timing": "the K steps through gen_stream_batches (each step's progenitor orbits, release and track "
+                          "tables on a side stream while the previous step's stream kernel runs; every step does "
+                          "all of its work); 'sequential': the same K steps one after the other",
+                "sequential": {"value": world * s.work / (r32s["ms_per_step"] * 1e-3), "ms_per_step": r32s["ms_per_step"],
+                               "kernel_ms": r32s["kernel_ms"], "samples_ms": r32s["samples_ms"],
+                               "clocks": r32s["clocks"]},
                 "gpu_launches_per_step": r32["launches"] / args.steps}
     if not args.no_analysis:
         # --- the stated error: FP32 vs FP64 on the same inputs, the FP64

@@ -176,6 +176,102 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
     return out
 
 
+def gen_stream_batches(pot_base: Potential, ts=None, prog_w0s=None, Msat=None, normals=None, *, n_batches=None,
+                       dt=None, prog_pot: Optional[Potential] = None, n_particles_per_release=2, precision="f32k",
+                       snapshot_every=None, release="fardal", kval_arr=1.0, prog_w0_at="start", prog_method="auto",
+                       lookahead=1):
+    """gen_stream for a sequence of streams (other progenitors, or the same
+    one with other draws), pipelined on two CUDA streams: the progenitor
+    orbits (with prog_w0_at='end', first back from the present, as
+    integrate_orbit over [ts[-1], ts[0]]), the release and the track tables
+    of the next `lookahead` streams run on a high-priority side stream while
+    the current stream's kernel fills the GPU (those steps are a few blocks,
+    bound by the issue latency of their warps).  Every stream does all of
+    its own work; only its order against the others changes.
+
+    prog_w0s and normals: one value for every stream or a list with one per
+    stream (n_batches gives the count when neither is a list).  ts must be a
+    uniform release grid; no perturbation, device outputs; precision 'f64'
+    or 'f32k'.  Yields each stream's gen_stream result ((lead, trail[,
+    snapshots])), enqueued on the current stream."""
+    if precision not in ("f64", "f32k"):
+        raise ValueError("precision must be 'f64' or 'f32k'")
+    if prog_w0_at not in ("start", "end"):
+        raise ValueError("prog_w0_at must be 'start' or 'end'")
+    ts_h = host64(ts).reshape(-1)
+    if len(ts_h) < 2 or _split_tail(ts_h)[1] is not None:
+        raise NotImplementedError("gen_stream_batches needs a uniform release grid ts")
+    lists = [len(v) for v in (prog_w0s, normals) if isinstance(v, (list, tuple))]
+    B = lists[0] if lists else n_batches
+    if B is None or any(n != B for n in lists):
+        raise ValueError("give lists of equal length for prog_w0s / normals, or n_batches")
+    w0s = prog_w0s if isinstance(prog_w0s, (list, tuple)) else [prog_w0s] * B
+    nrm = normals if isinstance(normals, (list, tuple)) else [normals] * B
+    n_draw = _n_draw(n_particles_per_release)
+    model = _abi.SS_RELEASE_CHEN25 if release == "chen25" else _abi.SS_RELEASE_FARDAL
+    if release not in ("fardal", "chen25"):
+        raise ValueError("release must be 'fardal' or 'chen25'")
+    chen = (CHEN25_MEAN, chen25_factor()) if model == _abi.SS_RELEASE_CHEN25 else None
+    nz = 6 if model == _abi.SS_RELEASE_CHEN25 else 4
+    main = torch.cuda.current_stream()
+    pot_base._desc()
+    side = torch.cuda.Stream(priority=-1)
+    side.wait_stream(main)
+    n_rel = len(ts_h) - 1
+    ppr = 2 * n_draw
+
+    def prepare(i):
+        with torch.cuda.stream(side):
+            w0 = w0s[i]
+            if prog_w0_at == "end":
+                w0 = pot_base.integrate_orbit(w0=w0, ts=np.array([ts_h[-1], ts_h[0]]), t0=float(ts_h[-1]),
+                                              t1=float(ts_h[0]), dt=dt).ys[-1]
+            ws, h, spr = pot_base._prog_orbit(ts_h, w0, dt, None, None, method=prog_method)
+            nm = nrm[i] if nrm[i] is not None else release_normals(None, len(ts_h), n_draw, nz)
+            ics, _ = pot_base._release(ws, ts_h, Msat, nm, kval_arr, model=model, chen=chen)
+            integ = pot_base
+            keep = [ws, ics]
+            if prog_pot is not None:
+                track = CenterTrack.from_samples(ts_h, ws[:, :3])
+                integ = _pot.Potential_Combine([pot_base, _pot.TimeDepTranslatingPotential(prog_pot, track,
+                                                                                          units=pot_base.units)],
+                                               units=pot_base.units)
+                integ._desc()  # the track's slopes, on the side stream
+                keep += [track.knots, track.slopes]
+            stream_ics = ics[:n_rel].reshape(n_rel * ppr, 6).contiguous()
+            keep.append(stream_ics)
+            ev = torch.cuda.Event()
+            ev.record(side)
+        # the main stream reads these after the side stream made them
+        for t in keep:
+            t.record_stream(main)
+        return dict(integ=integ, h=h, spr=spr, stream_ics=stream_ics, ev=ev)
+
+    ready = {}
+    for i in range(B):
+        for j in range(i, min(i + max(1, int(lookahead)) + 1, B)):
+            if j not in ready:
+                ready[j] = prepare(j)
+        prep = ready.pop(i)
+        main.wait_event(prep["ev"])
+        N = n_rel * ppr
+        cfg = _abi.ss_stream_cfg()
+        cfg.t0, cfg.dt = float(ts_h[0]), float(prep["h"])
+        cfg.n_steps, cfg.n_particles = prep["spr"] * n_rel, N
+        cfg.particles_per_release, cfg.steps_per_release = ppr, prep["spr"]
+        cfg.snap_stride = int(snapshot_every or 0)
+        snaps = None
+        if snapshot_every:
+            snaps = torch.empty(cfg.n_steps // int(snapshot_every), N, 6, dtype=torch.float32,
+                                device=prep["stream_ics"].device)
+        final, _ = _core.stream(prep["integ"]._desc(), cfg, prep["stream_ics"], precision, snaps=snaps)
+        final = final.reshape(n_rel, n_draw, 2, 6)
+        out = (final[:, 0, 0], final[:, 0, 1]) if n_draw == 1 else (final[:, :, 0], final[:, :, 1])
+        if snapshot_every:
+            out = out + (snaps.reshape(-1, n_rel, n_draw, 2, 6),)
+        yield out
+
+
 def _split_tail(ts_h: np.ndarray):
     """(release grid, end time): the reference integrates every release
     ts[i], i < len(ts) - 1, to ts[-1], and its notebooks end on a time off
@@ -635,7 +731,7 @@ def gen_stream_vmapped_with_pert_Chen25_fixed_prog(pot_base=None, pot_pert=None,
                       n_particles_per_release=n_particles_per_release, snapshot_every=snapshot_every)
 
 
-__all__ = ["gen_stream", "eval_dense_stream", "eval_dense_stream_id", "gen_stream_ics_pert",
+__all__ = ["gen_stream", "gen_stream_batches", "eval_dense_stream", "eval_dense_stream_id", "gen_stream_ics_pert",
            "gen_stream_vmapped_with_pert", "gen_stream_vmapped_with_pert_fixed_prog", "gen_stream_scan_with_pert",
            "custom_release_model", "computed_binned_track", "gen_stream_ensemble", "gen_stream_ensemble_batches",
            "compute_stream_length",
