@@ -199,7 +199,7 @@ def gen_stream_batches(pot_base: Potential, ts=None, prog_w0s=None, Msat=None, n
     if prog_w0_at not in ("start", "end"):
         raise ValueError("prog_w0_at must be 'start' or 'end'")
     ts_h = host64(ts).reshape(-1)
-    if len(ts_h) < 2 or _split_tail(ts_h)[1] is not None:
+    if len(ts_h) < 2 or _grid_spacing(ts_h) is None:
         raise NotImplementedError("gen_stream_batches needs a uniform release grid ts")
     lists = [len(v) for v in (prog_w0s, normals) if isinstance(v, (list, tuple))]
     B = lists[0] if lists else n_batches
