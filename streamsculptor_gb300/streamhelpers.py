@@ -177,7 +177,8 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
 
 
 def gen_stream_batches(pot_base: Potential, ts=None, prog_w0s=None, Msat=None, normals=None, *, n_batches=None,
-                       dt=None, prog_pot: Optional[Potential] = None, n_particles_per_release=2, precision="f32k",
+                       seed_num=None, dt=None, prog_pot: Optional[Potential] = None, n_particles_per_release=2,
+                       precision="f32k",
                        snapshot_every=None, release="fardal", kval_arr=1.0, prog_w0_at="start", prog_method="auto",
                        lookahead=1):
     """gen_stream for a sequence of streams (other progenitors, or the same
@@ -190,7 +191,8 @@ def gen_stream_batches(pot_base: Potential, ts=None, prog_w0s=None, Msat=None, n
     its own work; only its order against the others changes.
 
     prog_w0s and normals: one value for every stream or a list with one per
-    stream (n_batches gives the count when neither is a list).  ts must be a
+    stream (n_batches gives the count when neither is a list); a stream
+    whose normals are None draws them from seed_num + its index.  ts must be a
     uniform release grid; no perturbation, device outputs; precision 'f64'
     or 'f32k'.  Yields each stream's gen_stream result ((lead, trail[,
     snapshots])), enqueued on the current stream."""
@@ -207,6 +209,8 @@ def gen_stream_batches(pot_base: Potential, ts=None, prog_w0s=None, Msat=None, n
         raise ValueError("give lists of equal length for prog_w0s / normals, or n_batches")
     w0s = prog_w0s if isinstance(prog_w0s, (list, tuple)) else [prog_w0s] * B
     nrm = normals if isinstance(normals, (list, tuple)) else [normals] * B
+    if seed_num is None and any(n is None for n in nrm):
+        raise ValueError("give normals, or seed_num, for every stream")
     n_draw = _n_draw(n_particles_per_release)
     model = _abi.SS_RELEASE_CHEN25 if release == "chen25" else _abi.SS_RELEASE_FARDAL
     if release not in ("fardal", "chen25"):
@@ -227,7 +231,7 @@ def gen_stream_batches(pot_base: Potential, ts=None, prog_w0s=None, Msat=None, n
                 w0 = pot_base.integrate_orbit(w0=w0, ts=np.array([ts_h[-1], ts_h[0]]), t0=float(ts_h[-1]),
                                               t1=float(ts_h[0]), dt=dt).ys[-1]
             ws, h, spr = pot_base._prog_orbit(ts_h, w0, dt, None, None, method=prog_method)
-            nm = nrm[i] if nrm[i] is not None else release_normals(None, len(ts_h), n_draw, nz)
+            nm = nrm[i] if nrm[i] is not None else release_normals(int(seed_num) + i, len(ts_h), n_draw, nz)
             ics, _ = pot_base._release(ws, ts_h, Msat, nm, kval_arr, model=model, chen=chen)
             integ = pot_base
             keep = [ws, ics]

@@ -983,3 +983,19 @@ def test_gen_stream_batches_equal_gen_stream(ss, precision):
         for a, b in zip(got[i], want):
             assert a.shape == b.shape
             assert torch.equal(torch.nan_to_num(a, nan=7.0), torch.nan_to_num(b, nan=7.0)), i
+
+
+def test_gen_stream_batches_seeded_draws(ss):
+    """Streams without given normals draw them from seed_num + their index,
+    as gen_stream does from its seed_num."""
+    from streamsculptor_gb300.streamhelpers import gen_stream, gen_stream_batches
+    pot = mw3_gpu(ss)
+    n_rel, dt = 40, 1.0
+    ts = -float(n_rel) * dt + np.arange(n_rel + 1) * dt
+    w_start = [PROG_WF, PROG_WF + np.array([0.2, 0.1, -0.1, 0.001, 0.0, -0.001])]
+    got = list(gen_stream_batches(pot, ts, w_start, 2e4, seed_num=5, dt=dt, n_particles_per_release=4))
+    for i in range(2):
+        want = gen_stream(pot, ts, w_start[i], 2e4, seed_num=5 + i, dt=dt, n_particles_per_release=4,
+                          precision="f32k")
+        for a, b in zip(got[i], want):
+            assert torch.equal(a, b), i

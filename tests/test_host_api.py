@@ -11,7 +11,8 @@ G = 4.498502151469554e-12
 
 def _batches(**kw):
     args = dict(pot_base=P.NFWPotential(m=1e12, r_s=20.0), ts=np.arange(11.0) - 10.0,
-                prog_w0s=np.array([10.0, 0, 0, 0, 0.2, 0]), Msat=1e4, normals=None, n_batches=2, dt=1.0)
+                prog_w0s=np.array([10.0, 0, 0, 0, 0.2, 0]), Msat=1e4, normals=None, n_batches=2, seed_num=3,
+                dt=1.0)
     args.update(kw)
     return list(gen_stream_batches(**args))
 
@@ -23,6 +24,7 @@ def _batches(**kw):
     (dict(n_batches=None), "n_batches"),
     (dict(prog_w0s=[np.zeros(6)] * 3, normals=[None] * 2), "equal length"),
     (dict(release="spray"), "release"),
+    (dict(seed_num=None), "seed_num"),
 ])
 def test_gen_stream_batches_rejects_bad_arguments(kw, msg):
     """Every check runs before the first device call (a generator: the
