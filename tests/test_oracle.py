@@ -259,6 +259,26 @@ def test_zhao_matches_scipy(oracle, p):
     assert np.all(np.linalg.norm(g - g_ref, axis=1) <= bound)
 
 
+@pytest.mark.parametrize("p", ZHAO_CASES[:3])
+def test_zhao_oracle_hessian_is_the_jacobian_of_its_gradient(oracle, p):
+    """The oracle's Zhao Hessian (forward-mode autodiff through the forward
+    difference of gradient_func) against central differences of its own
+    gradient, at 1-100 kpc where the difference's rounding noise is small:
+    within 1e-5 of the differences, and symmetric to 1e-9 (differentiating
+    the forward difference cancels about five digits, so the two orders of
+    a mixed derivative round apart by ~1e-11)."""
+    m = oracle.HostModel([(_abi.SS_ZHAO, 0, p)])
+    rng = np.random.default_rng(3)
+    for x in rng.normal(0, 1, size=(6, 3)):
+        x = x / np.linalg.norm(x) * np.exp(rng.uniform(0.0, np.log(100.0)))
+        _, g, H = oracle.potential_eval(m, x)
+        eps = 1e-4 * np.linalg.norm(x)
+        Hfd = np.stack([(oracle.potential_eval(m, x + eps * e)[1][0] - oracle.potential_eval(m, x - eps * e)[1][0])
+                        / (2 * eps) for e in np.eye(3)], axis=1)
+        assert rel_err(H[0], Hfd) < 1e-5
+        assert np.abs(H[0] - H[0].T).max() <= 1e-9 * np.abs(H[0]).max()
+
+
 def test_zhao_closed_form_hernquist(oracle):
     """alpha = 1, beta = 4, gamma = 1 is the Hernquist sphere: the oracle's
     Zhao potential equals -G m / (r + r_s) to round-off, and its forward
