@@ -178,9 +178,8 @@ def gen_stream(pot_base: Potential, ts=None, prog_w0=None, Msat=None, seed_num=N
 
 def gen_stream_batches(pot_base: Potential, ts=None, prog_w0s=None, Msat=None, normals=None, *, n_batches=None,
                        seed_num=None, dt=None, prog_pot: Optional[Potential] = None, n_particles_per_release=2,
-                       precision="f32k",
-                       snapshot_every=None, release="fardal", kval_arr=1.0, prog_w0_at="start", prog_method="auto",
-                       lookahead=1):
+                       precision="f32k", snapshot_every=None, release="fardal", kval_arr=1.0, prog_w0_at="start",
+                       prog_method="auto", lookahead=1):
     """gen_stream for a sequence of streams (other progenitors, or the same
     one with other draws), pipelined on two CUDA streams: the progenitor
     orbits (with prog_w0_at='end', first back from the present, as
